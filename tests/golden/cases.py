@@ -1,0 +1,37 @@
+"""Load the golden cases written by ``make_golden.py`` into plain Python objects.
+
+No reference import here: the golden ``.npz`` files carry every input.
+"""
+
+from __future__ import annotations
+
+import glob
+import json
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def render_case_names():
+    return sorted(os.path.basename(p)[len("render_") : -len(".npz")] for p in glob.glob(os.path.join(HERE, "render_*.npz")))
+
+
+def lm_case_names():
+    return sorted(os.path.basename(p)[: -len(".npz")] for p in glob.glob(os.path.join(HERE, "lm_*.npz")))
+
+
+def load_render(name):
+    z = np.load(os.path.join(HERE, f"render_{name}.npz"))
+    d = {k: z[k] for k in z.files}
+    d["spec"] = json.loads(str(d["spec"]))
+    return d
+
+
+def load_lm(name):
+    z = np.load(os.path.join(HERE, f"{name}.npz"))
+    d = {k: z[k] for k in z.files}
+    d["spec"] = json.loads(str(d["spec"]))
+    d["message"] = str(d["message"])
+    return d

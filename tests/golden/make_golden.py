@@ -1,0 +1,336 @@
+"""Generate the golden vectors in this folder by running the reference itself.
+
+Run in a container that has the reference checkout (default path below, or
+``ASTROPHOT_REFERENCE=<path>``):
+
+    python tests/golden/make_golden.py
+
+The reference (AstroPhot 0.x) is imported through a ``sys.modules`` shim for
+the optional packages it imports at module level but never calls on this
+path (astropy, yaml, h5py, matplotlib, pyro, requests, tqdm).  Everything
+runs in float64 on the CPU (``AP_config.ap_dtype``).  Each case stores the
+inputs (data, PSF, parameters, knobs) together with the reference's outputs,
+so the oracle and the CUDA path are checked on exactly the same arrays.
+"""
+
+from __future__ import annotations
+
+import importlib.abc
+import importlib.machinery
+import json
+import math
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+from astrophot_gb300 import synthetic  # noqa: E402
+
+REFERENCE = os.environ.get("ASTROPHOT_REFERENCE", "/root/reference")
+
+
+class _StubObj:
+    def __init__(self, *a, **k):
+        pass
+
+    def __call__(self, *a, **k):
+        return _StubObj()
+
+    def __getattr__(self, name):
+        if name.startswith("__"):
+            raise AttributeError(name)
+        return _StubObj()
+
+    def __mro_entries__(self, bases):
+        return (object,)
+
+
+class _StubModule(types.ModuleType):
+    def __getattr__(self, name):
+        if name.startswith("__"):
+            raise AttributeError(name)
+        return _StubObj()
+
+
+class _StubFinder(importlib.abc.MetaPathFinder, importlib.abc.Loader):
+    ROOTS = ("astropy", "yaml", "h5py", "matplotlib", "pyro", "requests", "tqdm")
+
+    def find_spec(self, fullname, path, target=None):
+        if fullname.split(".")[0] in self.ROOTS:
+            return importlib.machinery.ModuleSpec(fullname, self, is_package=True)
+        return None
+
+    def create_module(self, spec):
+        m = _StubModule(spec.name)
+        m.__path__ = []
+        return m
+
+    def exec_module(self, module):
+        pass
+
+
+def import_reference():
+    sys.meta_path.insert(0, _StubFinder())
+    sys.path.insert(0, REFERENCE)
+    import astrophot as ap  # noqa: E402
+
+    return ap
+
+
+# --------------------------------------------------------------------------
+# case definitions (inputs only)
+# --------------------------------------------------------------------------
+
+MOFFAT_25 = ("moffat", 3.5, 3.0, 25)
+
+
+def psf_array(spec, scale=1.0):
+    if spec is None:
+        return None
+    kind = spec[0]
+    if kind == "moffat":
+        _, beta, fwhm, width = spec
+        return synthetic.moffat_stamp(beta, synthetic.moffat_rd(fwhm, beta) * scale, width, scale)
+    if kind == "gaussian":
+        _, sigma, width = spec
+        return synthetic.gaussian_stamp(sigma * scale, width, scale)
+    raise ValueError(kind)
+
+
+RENDER_CASES = {
+    "sersic_psf_64": dict(
+        kind="sersic",
+        nx=64,
+        ny=64,
+        scale=1.0,
+        psf=MOFFAT_25,
+        params={"center": [31.7, 32.4], "q": 0.55, "PA": 0.9, "n": 2.5, "Re": 8.0, "Ie": 1.2},
+        knobs={"psf_mode": "full"},
+    ),
+    "sersic_psf_n4": dict(
+        kind="sersic",
+        nx=48,
+        ny=40,
+        scale=1.0,
+        psf=("moffat", 3.5, 2.5, 11),
+        params={"center": [20.2, 23.9], "q": 0.35, "PA": 2.8, "n": 4.2, "Re": 4.0, "Ie": 0.8},
+        knobs={"psf_mode": "full"},
+    ),
+    "sersic_psf_direct": dict(
+        kind="sersic",
+        nx=64,
+        ny=64,
+        scale=1.0,
+        psf=MOFFAT_25,
+        params={"center": [31.7, 32.4], "q": 0.55, "PA": 0.9, "n": 2.5, "Re": 8.0, "Ie": 1.2},
+        knobs={"psf_mode": "full", "psf_convolve_mode": "direct"},
+    ),
+    "sersic_nopsf": dict(
+        kind="sersic",
+        nx=40,
+        ny=48,
+        scale=1.0,
+        psf=None,
+        params={"center": [17.3, 26.6], "q": 0.7, "PA": 0.3, "n": 1.3, "Re": 6.0, "Ie": 1.0},
+        knobs={},
+    ),
+    "sersic_nopsf_quad3": dict(
+        kind="sersic",
+        nx=40,
+        ny=48,
+        scale=1.0,
+        psf=None,
+        params={"center": [17.3, 26.6], "q": 0.7, "PA": 0.3, "n": 1.3, "Re": 6.0, "Ie": 1.0},
+        knobs={"sampling_mode": "quad:3"},
+    ),
+    "sersic_nopsf_simpsons": dict(
+        kind="sersic",
+        nx=40,
+        ny=48,
+        scale=1.0,
+        psf=None,
+        params={"center": [17.3, 26.6], "q": 0.7, "PA": 0.3, "n": 1.3, "Re": 6.0, "Ie": 1.0},
+        knobs={"sampling_mode": "simpsons"},
+    ),
+    "sersic_nopsf_trapezoid": dict(
+        kind="sersic",
+        nx=40,
+        ny=48,
+        scale=1.0,
+        psf=None,
+        params={"center": [17.3, 26.6], "q": 0.7, "PA": 0.3, "n": 1.3, "Re": 6.0, "Ie": 1.0},
+        knobs={"sampling_mode": "trapezoid"},
+    ),
+    "sersic_nopsf_noint": dict(
+        kind="sersic",
+        nx=40,
+        ny=48,
+        scale=1.0,
+        psf=None,
+        params={"center": [17.3, 26.6], "q": 0.7, "PA": 0.3, "n": 1.3, "Re": 6.0, "Ie": 1.0},
+        knobs={"integrate_mode": "none"},
+    ),
+    "exp_psf": dict(
+        kind="exponential",
+        nx=48,
+        ny=48,
+        scale=1.0,
+        psf=("gaussian", 1.5, 13),
+        params={"center": [23.6, 24.2], "q": 0.6, "PA": 1.7, "Re": 7.0, "Ie": 1.5},
+        knobs={"psf_mode": "full"},
+    ),
+    "sersic_scale08": dict(
+        kind="sersic",
+        nx=50,
+        ny=60,
+        scale=0.8,
+        psf=("gaussian", 2.0, 11),
+        params={"center": [19.66, 24.05], "q": 0.7, "PA": math.pi / 4, "n": 1.0, "Re": 12.0, "Ie": 0.0},
+        knobs={"psf_mode": "full"},
+    ),
+}
+
+LM_CASES = {
+    # 64 x 64 single Sersic + locked sky 1.0, Moffat 25^2 (a smaller cousin of the 128^2 case)
+    "lm_64": dict(size=64, seed=11, psf=MOFFAT_25),
+    # the 128 x 128 single-Sersic stamp workload, two seeds
+    "lm_c0_seed0": dict(size=128, seed=0, psf=MOFFAT_25),
+    "lm_c0_seed1": dict(size=128, seed=1, psf=MOFFAT_25),
+}
+
+
+# --------------------------------------------------------------------------
+# reference drivers
+# --------------------------------------------------------------------------
+
+
+def ref_component(ap, case, target, name):
+    model_type = {"sersic": "sersic galaxy model", "exponential": "exponential galaxy model"}[case["kind"]]
+    kw = dict(case["knobs"])
+    params = {k: (list(v) if isinstance(v, (list, tuple)) else v) for k, v in case["params"].items()}
+    return ap.models.AstroPhot_Model(name=name, model_type=model_type, target=target, parameters=params, **kw)
+
+
+def run_render_case(ap, key, case):
+
+    psf = psf_array(case["psf"], case["scale"])
+    target = ap.image.Target_Image(
+        data=np.zeros((case["ny"], case["nx"])), pixelscale=case["scale"], psf=psf
+    )
+    model = ref_component(ap, case, target, f"golden {key}")
+    img = model().data.detach().cpu().numpy()
+    J_rep = model.jacobian(as_representation=True).data.detach().cpu().numpy()
+    J_val = model.jacobian(as_representation=False).data.detach().cpu().numpy()
+    rep = model.parameters.vector_representation().detach().cpu().numpy()
+    val = model.parameters.vector_values().detach().cpu().numpy()
+    out = dict(
+        model=img,
+        jac_rep=J_rep,
+        jac_val=J_val,
+        rep=rep,
+        val=val,
+        psf=np.zeros((0, 0)) if psf is None else psf,
+        spec=json.dumps(case),
+    )
+    # sky groups: the same component plus a flat sky.  ``Group_Model`` pushes its own
+    # ``psf_mode`` onto every sub-model when they are added (group_model_object.py:88,
+    # :292-297), so the group is built with psf_mode="full"; the "quirk" entry keeps the
+    # default group psf_mode ("none"), which silently turns the galaxy's PSF off.
+    if key == "sersic_psf_64":
+        for tag, lock, F, gmode in (
+            ("locked", True, 0.0, "full"),
+            ("free", False, 0.3, "full"),
+            ("quirk", True, 0.0, None),
+        ):
+            sky = ap.models.AstroPhot_Model(
+                name=f"golden sky {key} {tag}",
+                model_type="flat sky model",
+                target=target,
+                parameters={"F": {"value": F, "locked": lock}},
+            )
+            sky.initialize()  # sets the (locked) sky centre to the window centre
+            comp = ref_component(ap, case, target, f"golden {key} g {tag}")
+            gkw = {} if gmode is None else {"psf_mode": gmode}
+            group = ap.models.AstroPhot_Model(
+                name=f"golden group {key} {tag}", model_type="group model", target=target, models=[comp, sky], **gkw
+            )
+            out[f"group_{tag}_model"] = group().data.detach().cpu().numpy()
+            out[f"group_{tag}_jac_rep"] = group.jacobian(as_representation=True).data.detach().cpu().numpy()
+    return out
+
+
+def make_lm_data(ap, case):
+    """Truth image from the reference (Sersic + sky 1.0), noise sigma = sqrt(model + 10)."""
+    spec = synthetic.c0_stamp(case["seed"], size=case["size"])
+    psf = psf_array(case["psf"])
+    target = ap.image.Target_Image(data=np.zeros((spec.ny, spec.nx)), pixelscale=1.0, psf=psf)
+    group = build_lm_group(ap, target, spec.truth, f"truth {case['seed']} {case['size']}")
+    truth_img = group().data.detach().cpu().numpy()
+    data, weight = synthetic.add_noise(truth_img, spec.seed)
+    return spec, psf, truth_img, data, weight
+
+
+def build_lm_group(ap, target, vals, name):
+    cx, cy, q, PA, n, Re, Ie = [float(v) for v in vals]
+    gal = ap.models.AstroPhot_Model(
+        name=f"{name} gal",
+        model_type="sersic galaxy model",
+        target=target,
+        psf_mode="full",
+        parameters={"center": [cx, cy], "q": q, "PA": PA, "n": n, "Re": Re, "Ie": Ie},
+    )
+    sky = ap.models.AstroPhot_Model(
+        name=f"{name} sky",
+        model_type="flat sky model",
+        target=target,
+        parameters={"F": {"value": 0.0, "locked": True}},
+    )
+    sky.initialize()  # sets the (locked) sky centre to the window centre
+    return ap.models.AstroPhot_Model(
+        name=f"{name} group", model_type="group model", target=target, models=[gal, sky], psf_mode="full"
+    )
+
+
+def run_lm_case(ap, key, case):
+    spec, psf, truth_img, data, weight = make_lm_data(ap, case)
+    target = ap.image.Target_Image(data=data, pixelscale=1.0, psf=psf, variance=1.0 / weight)
+    group = build_lm_group(ap, target, spec.init, f"fit {key}")
+    rep0 = group.parameters.vector_representation().detach().cpu().numpy().copy()
+    res = ap.fit.LM(group, initial_state=rep0).fit()
+    return dict(
+        truth=spec.truth,
+        init=spec.init,
+        psf=psf,
+        truth_model=truth_img,
+        data=data,
+        weight=weight,
+        rep0=rep0,
+        loss_history=np.array(res.loss_history),
+        L_history=np.array(res.L_history),
+        lambda_history=np.array(res.lambda_history),
+        res=np.array(res.res()),
+        final_values=group.parameters.vector_values().detach().cpu().numpy(),
+        message=np.array(res.message),
+        spec=json.dumps(case),
+    )
+
+
+def main():
+    ap = import_reference()
+    for key, case in RENDER_CASES.items():
+        out = run_render_case(ap, key, case)
+        np.savez_compressed(os.path.join(HERE, f"render_{key}.npz"), **out)
+        print("render", key, out["model"].shape, float(out["model"].sum()))
+    for key, case in LM_CASES.items():
+        out = run_lm_case(ap, key, case)
+        np.savez_compressed(os.path.join(HERE, f"{key}.npz"), **out)
+        print("lm", key, len(out["loss_history"]), out["loss_history"][-1], str(out["message"]))
+
+
+if __name__ == "__main__":
+    main()

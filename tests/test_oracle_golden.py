@@ -1,0 +1,155 @@
+"""The CPU oracle against golden vectors recorded from the reference itself
+(``tests/golden/make_golden.py``) and against the reference's own known-answer
+tests (``tests/test_utils.py:16-38`` FFT convolution vs scipy, ``:344-435`` Sersic
+closed forms, ``tests/test_model.py:49-74`` representation round trip)."""
+
+import math
+
+import numpy as np
+import pytest
+import scipy.signal
+
+import cases
+from oracle.lm import GroupProblem, LMOracle
+from oracle.render import (
+    PSF,
+    Component,
+    Window,
+    convolve_direct_semantics,
+    convolve_fft_semantics,
+    drep_dvalue,
+    rep_to_value,
+    sample_component,
+    sample_group,
+    sersic_total_flux,
+    value_to_rep,
+)
+
+
+def component_from_spec(spec, **extra):
+    p = dict(spec["params"])
+    p["center"] = np.array(p["center"], dtype=float)
+    knobs = dict(spec["knobs"])
+    knobs.update(extra)
+    return Component(spec["kind"], p, **knobs)
+
+
+def window_from_spec(spec):
+    return Window.from_scale(spec["nx"], spec["ny"], spec["scale"])
+
+
+def psf_from_case(d):
+    return PSF(d["psf"], d["spec"]["scale"]) if d["psf"].size else None
+
+
+@pytest.mark.parametrize("name", cases.render_case_names())
+def test_render_and_jacobian_match_reference(name):
+    d = cases.load_render(name)
+    spec = d["spec"]
+    comp = component_from_spec(spec)
+    r = sample_component(comp, window_from_spec(spec), psf_from_case(d), grad=True)
+    scale = np.max(np.abs(d["model"]))
+    assert np.max(np.abs(r.model - d["model"])) <= 1e-12 * scale
+    J = np.stack([r.jac[s] for s in comp.free_slots()], -1)
+    assert J.shape == d["jac_val"].shape
+    for k in range(J.shape[-1]):
+        colscale = np.max(np.abs(d["jac_val"][..., k]))
+        assert np.max(np.abs(J[..., k] - d["jac_val"][..., k])) <= 1e-11 * colscale
+    # representation-space Jacobian = value-space columns x d value / d rep
+    names = [s[0] for s in comp.free_slots()]
+    drep = np.array([drep_dvalue(nm, r_) for nm, r_ in zip(names, d["rep"])])
+    Jr = J * drep
+    for k in range(Jr.shape[-1]):
+        colscale = np.max(np.abs(d["jac_rep"][..., k]))
+        assert np.max(np.abs(Jr[..., k] - d["jac_rep"][..., k])) <= 1e-11 * colscale
+
+
+@pytest.mark.parametrize("tag", ["locked", "free", "quirk"])
+def test_group_with_sky_matches_reference(tag):
+    d = cases.load_render("sersic_psf_64")
+    spec = d["spec"]
+    gal = component_from_spec(spec, psf_mode="none" if tag == "quirk" else "full")
+    F = 0.3 if tag == "free" else 0.0
+    sky = Component("flat_sky", {"F": F}, locked=() if tag == "free" else ("F",))
+    model, J = sample_group([gal, sky], window_from_spec(spec), psf_from_case(d), grad=True)
+    ref = d[f"group_{tag}_model"]
+    assert np.max(np.abs(model - ref)) <= 1e-12 * np.max(np.abs(ref))
+    slots = [s for c in (gal, sky) for s in c.free_slots()]
+    names = [s[0] for s in slots]
+    rep = np.concatenate([d["rep"], [F]] if tag == "free" else [d["rep"]])
+    Jr = J * np.array([drep_dvalue(nm, r_) for nm, r_ in zip(names, rep)])
+    refJ = d[f"group_{tag}_jac_rep"]
+    assert Jr.shape == refJ.shape
+    for k in range(Jr.shape[-1]):
+        assert np.max(np.abs(Jr[..., k] - refJ[..., k])) <= 1e-11 * np.max(np.abs(refJ[..., k]))
+
+
+def lm_problem(d):
+    size = d["spec"]["size"]
+    cx, cy, q, PA, n, Re, Ie = d["init"]
+    gal = Component("sersic", {"center": [cx, cy], "q": q, "PA": PA, "n": n, "Re": Re, "Ie": Ie}, psf_mode="full")
+    sky = Component("flat_sky", {"F": 0.0}, locked=("F",))
+    return GroupProblem([gal, sky], Window.from_scale(size, size), PSF(d["psf"]), d["data"], d["weight"])
+
+
+@pytest.mark.parametrize("name", [n for n in cases.lm_case_names() if n == "lm_64"])
+def test_lm_trajectory_matches_reference(name):
+    d = cases.load_lm(name)
+    prob = lm_problem(d)
+    rep0 = prob.representation()
+    assert np.allclose(rep0, d["rep0"], rtol=0, atol=1e-13)
+    lm = LMOracle(prob, rep0).fit()
+    assert lm.message == d["message"]
+    assert len(lm.loss_history) == len(d["loss_history"])
+    assert np.allclose(lm.loss_history, d["loss_history"], rtol=1e-12, atol=0)
+    assert np.allclose(lm.L_history, d["L_history"], rtol=1e-12, atol=0)
+    assert np.allclose(lm.res(), d["res"], rtol=1e-10, atol=1e-12)
+
+
+def test_truth_model_matches_reference():
+    d = cases.load_lm("lm_c0_seed0")
+    size = d["spec"]["size"]
+    cx, cy, q, PA, n, Re, Ie = d["truth"]
+    gal = Component("sersic", {"center": [cx, cy], "q": q, "PA": PA, "n": n, "Re": Re, "Ie": Ie}, psf_mode="full")
+    sky = Component("flat_sky", {"F": 0.0}, locked=("F",))
+    model, _ = sample_group([gal, sky], Window.from_scale(size, size), PSF(d["psf"]))
+    assert np.max(np.abs(model - d["truth_model"])) <= 1e-12 * np.max(d["truth_model"])
+
+
+# ---- the reference's own known-answer tests, restated ------------------------------
+
+
+def test_fft_convolution_equals_scipy_same():
+    """tests/test_utils.py:16-38: fft_convolve_torch == scipy.signal.fftconvolve(mode="same")
+    on a zero-bordered image; both of the oracle's convolution forms must agree with it."""
+    rng = np.random.default_rng(3)
+    img = np.zeros((60, 70))
+    img[15:-15, 15:-15] = rng.uniform(size=(30, 40))
+    kern = rng.uniform(size=(11, 13))
+    want = scipy.signal.fftconvolve(img, kern, mode="same")
+    assert np.allclose(convolve_fft_semantics(img, kern), want, atol=1e-12)
+    assert np.allclose(convolve_direct_semantics(img, kern), want, atol=1e-12)
+
+
+def test_sersic_flux_closed_form():
+    """tests/test_utils.py:344-435 pins sersic_Ie_to_flux against numerical integration."""
+    from scipy.integrate import quad
+    from oracle.render import sersic_b
+
+    for n, Re, q in ((1.0, 5.0, 0.6), (4.0, 3.0, 0.9), (0.7, 12.0, 0.3)):
+        b = sersic_b(n)
+        num = quad(lambda r: 2 * math.pi * q * r * math.exp(-b * ((r / Re) ** (1 / n) - 1)), 0, np.inf, limit=500)[0]
+        assert sersic_total_flux(1.0, n, Re, q) == pytest.approx(num, rel=1e-6)
+
+
+@pytest.mark.parametrize("name,vals", [("q", [0.01, 0.5, 0.99]), ("n", [0.4, 2.0, 7.9]), ("Re", [0.1, 5.0, 400.0]),
+                                       ("PA", [0.2, 1.0, 3.1]), ("center", [-3.0, 64.5]), ("Ie", [-1.0, 2.0])])
+def test_representation_round_trip(name, vals):
+    """tests/test_model.py:49-74: value -> representation -> value is the identity."""
+    v = np.array(vals)
+    assert np.allclose(rep_to_value(name, value_to_rep(name, v)), v, rtol=1e-12, atol=1e-12)
+    # derivative of rep -> value against a central difference
+    r = value_to_rep(name, v)
+    h = 1e-6 * np.maximum(1.0, np.abs(r))
+    fd = (rep_to_value(name, r + h) - rep_to_value(name, r - h)) / (2 * h)
+    assert np.allclose(drep_dvalue(name, r), fd, rtol=1e-6, atol=1e-9)
