@@ -1,0 +1,319 @@
+// Device-side data structures and profile arithmetic for the render path.
+//
+// Reference behaviour restated here (AstroPhot 0.x):
+//   brightness  : models/_shared_methods.py:286-339 (inclined transform, radius metric,
+//                 sersic_radial_model / exponential_radial_model),
+//                 utils/parametric_profiles.py:7-18,63-74, utils/conversions/functions.py:7-22
+//   quadrature  : utils/operations.py:94-147 (displacement_grid, quad_table,
+//                 single_quad_integrate)
+//
+// Samples are evaluated in FP32 with analytic partial derivatives.  Each data-dependent
+// branch of the reference's adaptive integration (refine a pixel when a float64
+// comparison says so) is decided in FP32 when an error bound on the FP32 operands keeps
+// the comparison clear of its threshold, and otherwise re-decided from a float64
+// re-evaluation of the same samples, so the integration masks follow the float64 path.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/astrophot_gb300.h"
+
+namespace apgb {
+
+constexpr int kMaxQuad = 5;   // quad levels <= 5  (quad_level^2 <= 32 lanes)
+constexpr int kMaxGrid = 5;   // gridding <= 5     (gridding^2 <= 32 lanes)
+constexpr int kMaxDepth = 3;  // integrate_max_depth <= 3
+constexpr int kTile = 16;     // 16 x 16 pixel tiles
+constexpr int kNumPlanes = 7; // deep + 6 partial planes
+constexpr int kNacc = 56;     // per (stamp, slot) accumulator doubles
+constexpr float kLn10f = 2.302585092994046f;
+constexpr double kLn10 = 2.302585092994046;
+constexpr double kPi = 3.141592653589793;
+constexpr float kEps = 5.9604645e-08f;  // 2^-24
+
+// full parameter vector slots (value space)
+enum ParamSlot { PX = 0, PY = 1, PQ = 2, PPA = 3, PN = 4, PRE = 5, PIE = 6, PF = 7, NPARAM = 8 };
+// partial planes stored after the deep plane: d/dX, d/dY (X = x - cx), q, PA, n, Re
+enum GradSlot { GX = 0, GY = 1, GQ = 2, GPA = 3, GN = 4, GRE = 5, NGRAD = 6 };
+
+// accumulator layout inside one (stamp, slot) block of kNacc doubles
+enum AccSlot { ACC_CHI2 = 0, ACC_G = 1, ACC_RPP = 9, ACC_H = 17, ACC_N = 17 + 36 };
+
+// operations requested from the convolve/accumulate pass for one (stamp, slot)
+enum EvalOps : int32_t {
+  OP_NONE = 0,
+  OP_FWD = 1,          // render the model
+  OP_JAC = 2,          // also the partial planes / Jacobian columns
+  OP_WRITE_MODEL = 4,  // write model to the caller's buffer (or the LM's Y0 buffer)
+  OP_WRITE_JAC = 8,    // write Jacobian columns (caller's buffer or the LM's J buffer)
+  OP_CHI2 = 16,        // accumulate sum W (y - m)^2 over unmasked pixels
+  OP_HG = 32,          // accumulate J^T W J and J^T W (y - m)
+  OP_RPP = 64,         // accumulate J^T [(2/d)(W (m - Y0)/d - W J h)]
+  OP_REP = 128,        // chain Jacobian columns to representation space
+};
+
+struct QuadTables {
+  int32_t quad_level;  // integrate_quad_level
+  int32_t gridding;    // integrate_gridding
+  int32_t nsub;        // sub-samples of the sampling mode (1 midpoint, 4 trapezoid, 9 simpsons, k^2 quad)
+  int32_t sub_center;  // index of the reference sub-sample (simpsons: midpoint, quad: middle)
+  // integration quadrature offsets (unit pixel, before the pixel-scale matrix) and weights
+  double qx[kMaxQuad * kMaxQuad], qy[kMaxQuad * kMaxQuad], qw[kMaxQuad * kMaxQuad];
+  // displacement grid (unit pixel)
+  double gx[kMaxGrid * kMaxGrid], gy[kMaxGrid * kMaxGrid];
+  // sampling-mode sub-sample offsets (unit pixel) and weights
+  double sx[kMaxQuad * kMaxQuad], sy[kMaxQuad * kMaxQuad], sw[kMaxQuad * kMaxQuad];
+};
+
+struct StampDev {
+  int32_t nx, ny;    // output window
+  int32_t wnx, wny;  // working window
+  int32_t kx, ky;    // raw PSF shape (0 = none)
+  int32_t kpx, kpy;  // convolution kernel shape (kx + 2 with the bilinear shift, else kx)
+  int32_t bx, by;    // psf_border_int (0 without PSF)
+  int32_t tile_w0, ntw_x, ntw;  // working tiles: first index, tiles per row, count
+  int32_t tile_o0, nto_x, nto;  // output tiles
+  int32_t pad0;
+  int64_t out_off;   // packed output pixels
+  int64_t work_off;  // packed working pixels (per plane)
+  int64_t psf_off;   // packed raw PSF pixels
+  int64_t spsf_off;  // packed kernels: [2 slots][3 kernels][kpy * kpx]
+  double P[4], Pinv[4];
+  double ref_ij[2], ref_xy[2];
+  double pixel_area;
+};
+
+struct EvalDev {
+  int32_t ops;        // EvalOps bitmask; 0 = idle
+  int32_t cix, cjy;   // centre pixel (working grid): integer part
+  int32_t pad0;
+  float fx, fy;       // fractional part (0 with the bilinear shift)
+  double fx64, fy64;
+  float c, s, invq, Re, invRe, invn, bn, dbn, amp;
+  float sky, soft2, thresh;
+  double thresh64, soft2_64;
+  double shift[2];
+  double v[NPARAM];   // value-space parameters
+  double amp64, bn64, c64, s64;
+  float drep[NPARAM]; // d value / d representation
+};
+
+// everything the kernels need, passed by value
+struct BatchArgs {
+  int32_t n_stamps;
+  int32_t kind;         // AP_PROFILE_*
+  int32_t sampling;     // AP_SAMPLING_*
+  int32_t integrate;    // AP_INTEGRATE_*
+  int32_t psf_mode;     // AP_PSF_*
+  int32_t max_depth;
+  int32_t free_mask;
+  int32_t n_free;
+  int32_t has_sky;
+  int32_t n_work_tiles, n_out_tiles;
+  int32_t max_kp2;      // largest kpy * kpx
+  float tolerance;
+  double tolerance64, softening64;
+  int64_t work_pixels, out_pixels;
+  const StampDev* stamps;
+  EvalDev* evals;             // [n_stamps][2]
+  const int32_t* work_tiles;  // stamp of each working tile
+  const int32_t* out_tiles;   // stamp of each output tile
+  const QuadTables* tables;
+  float* work;                // [2][kNumPlanes][work_pixels]
+  float* aux;                 // [2][2][work_pixels]: reference sub-sample, FP32 error bound of deep
+  float* spsf;                // kernels
+  int64_t* queue;             // [2 * work_pixels]
+  uint32_t* counters;         // [0] queue len, [1] queue head, [2] fp64 re-decisions, [3] errors, [4] active
+  unsigned long long* work_ctr;  // [0] convolution FLOPs, [1] integration samples, [2] sampling samples
+  double* mean_acc;           // [n_stamps][2]
+  double* tile_acc;           // [n_out_tiles][2][kNacc]
+  double* acc;                // [n_stamps][2][kNacc]
+};
+
+// buffers of the convolve/accumulate pass
+struct ConvIO {
+  const float* psf;       // packed raw PSFs
+  const float* data;      // packed output pixels (may be null)
+  const float* weight;    // (null = 1)
+  const uint8_t* mask;    // (null = none)
+  float* model_out;       // OP_WRITE_MODEL target
+  float* jac_out;         // OP_WRITE_JAC target [n_free][out_pixels]
+  const float* y0;        // OP_RPP: model at the base point
+  const float* jbase;     // OP_RPP: Jacobian at the base point [n_free][out_pixels]
+  const double* hvec;     // OP_RPP: h per stamp [n_stamps][8]
+  double rpp_d;           // OP_RPP: d (0.1)
+};
+
+__host__ __device__ inline int64_t work_plane(const BatchArgs& b, int slot, int plane) {
+  return ((int64_t)slot * kNumPlanes + plane) * b.work_pixels;
+}
+
+// ---------------------------------------------------------------------------
+// sample evaluation
+// ---------------------------------------------------------------------------
+
+struct Sample {
+  float v;
+  float arg;  // |exponent argument| for the FP32 error bound
+  float g[NGRAD];
+};
+
+// Relative error bound of one FP32 sample.  u = R/Re carries a few ulp; log2 of it is
+// off by <= ~5e-7 (absolute); t = u^(1/n) then has relative error <= ln2 (5e-7/n + 1e-7 |log2 u|)
+// <= ~1.8e-6 for n >= 0.36, |log2 u| <= 10; the exponent b (t - 1) inherits b t times that,
+// and exp adds a few ulp.  Hence |dI/I| <= 3e-7 + 2e-6 (|b (t - 1)| + b).
+__device__ __forceinline__ float sample_rel_err(const EvalDev& e, float arg) {
+  return 3e-7f + 2e-6f * (fabsf(arg) + e.bn);
+}
+
+template <bool GRAD>
+__device__ __forceinline__ Sample eval_profile(const EvalDev& e, int kind, float X, float Y,
+                                               float area_scale) {
+  Sample out;
+  const float Xr = e.c * X - e.s * Y;
+  const float Yr0 = e.s * X + e.c * Y;
+  const float Yr = Yr0 * e.invq;
+  const float R = sqrtf(fmaf(Xr, Xr, fmaf(Yr, Yr, e.soft2)));
+  const float u = R * e.invRe;
+  const float amp = e.amp * area_scale;
+  float t = u, lu2 = 0.f;
+  if (kind == AP_PROFILE_SERSIC) {
+    lu2 = __log2f(u);
+    t = exp2f(lu2 * e.invn);
+  }
+  const float arg = e.bn * (t - 1.f);
+  const float I = amp * __expf(-arg);
+  out.v = I;
+  out.arg = arg;
+  if (GRAD) {
+    const float invR = 1.f / R;
+    float dIdR;
+    if (kind == AP_PROFILE_SERSIC) {
+      const float bt = e.bn * t * e.invn;
+      dIdR = -I * bt * invR;
+      out.g[GRE] = I * bt * e.invRe;
+      out.g[GN] = I * (-e.dbn * (t - 1.f) + bt * (lu2 * 0.6931471805599453f) * e.invn);
+    } else {
+      dIdR = -I * e.bn * e.invRe;
+      out.g[GRE] = I * e.bn * u * e.invRe;
+      out.g[GN] = 0.f;
+    }
+    out.g[GQ] = dIdR * (-(Yr * Yr) * e.invq * invR);
+    out.g[GPA] = dIdR * (Xr * Yr0 * (1.f - e.invq * e.invq) * invR);
+    out.g[GX] = dIdR * ((Xr * e.c + Yr * e.s * e.invq) * invR);
+    out.g[GY] = dIdR * ((-Xr * e.s + Yr * e.c * e.invq) * invR);
+  }
+  return out;
+}
+
+// float64 value, same operation order as the reference.
+__device__ __forceinline__ double eval_profile64(const EvalDev& e, int kind, double X, double Y,
+                                                 double area_scale) {
+  const double Xr = e.c64 * X - e.s64 * Y;
+  const double Yr = (e.s64 * X + e.c64 * Y) / e.v[PQ];
+  const double R = sqrt(Xr * Xr + Yr * Yr + e.soft2_64);
+  const double amp = e.amp64 * area_scale;
+  if (kind == AP_PROFILE_SERSIC) {
+    return amp * exp(-e.bn64 * (pow(R / e.v[PRE], 1.0 / e.v[PN]) - 1.0));
+  }
+  return amp * exp(-e.bn64 * ((R / e.v[PRE]) - 1.0));
+}
+
+// Plane offset (X, Y) of a point given in working-pixel units relative to the
+// integer centre pixel, FP32 and FP64.
+__device__ __forceinline__ void pix_to_offset(const StampDev& st, const EvalDev& e, float di,
+                                              float dj, float& X, float& Y) {
+  const float a = di - e.fx, b = dj - e.fy;
+  X = (float)st.P[0] * a + (float)st.P[1] * b;
+  Y = (float)st.P[2] * a + (float)st.P[3] * b;
+}
+
+__device__ __forceinline__ void pix_to_offset64(const StampDev& st, const EvalDev& e, double di,
+                                                double dj, double& X, double& Y) {
+  const double a = di - e.fx64, b = dj - e.fy64;
+  X = st.P[0] * a + st.P[1] * b;
+  Y = st.P[2] * a + st.P[3] * b;
+}
+
+// ---------------------------------------------------------------------------
+// batched damped solve (LM._h): Cholesky, LU with partial pivoting if not SPD
+// ---------------------------------------------------------------------------
+__device__ inline bool damped_solve_dev(int p, const double* H, const double* g, double L, double* h) {
+  double A[NPARAM * NPARAM];
+  double bvec[NPARAM];
+  for (int i = 0; i < p; ++i) {
+    for (int j = 0; j < p; ++j) {
+      const double hij = H[i * p + j];
+      A[i * p + j] = (i == j) ? hij * 1.0 + L * (1.0 + H[i * p + i]) : hij * (0.0 + 1.0 / (1.0 + L));
+    }
+    bvec[i] = g[i];
+  }
+  // Cholesky
+  double C[NPARAM * NPARAM];
+  bool spd = true;
+  for (int j = 0; j < p && spd; ++j) {
+    double d = A[j * p + j];
+    for (int k = 0; k < j; ++k) d -= C[j * p + k] * C[j * p + k];
+    if (!(d > 0.0)) {
+      spd = false;
+      break;
+    }
+    const double ljj = sqrt(d);
+    C[j * p + j] = ljj;
+    for (int i = j + 1; i < p; ++i) {
+      double v = A[i * p + j];
+      for (int k = 0; k < j; ++k) v -= C[i * p + k] * C[j * p + k];
+      C[i * p + j] = v / ljj;
+    }
+  }
+  if (spd) {
+    double z[NPARAM];
+    for (int i = 0; i < p; ++i) {
+      double v = bvec[i];
+      for (int k = 0; k < i; ++k) v -= C[i * p + k] * z[k];
+      z[i] = v / C[i * p + i];
+    }
+    for (int i = p - 1; i >= 0; --i) {
+      double v = z[i];
+      for (int k = i + 1; k < p; ++k) v -= C[k * p + i] * h[k];
+      h[i] = v / C[i * p + i];
+    }
+    return true;
+  }
+  // LU with partial pivoting (what torch.linalg.solve does)
+  for (int k = 0; k < p; ++k) {
+    int best = k;
+    double bv = fabs(A[k * p + k]);
+    for (int i = k + 1; i < p; ++i)
+      if (fabs(A[i * p + k]) > bv) {
+        bv = fabs(A[i * p + k]);
+        best = i;
+      }
+    if (best != k) {
+      for (int j = 0; j < p; ++j) {
+        const double t = A[k * p + j];
+        A[k * p + j] = A[best * p + j];
+        A[best * p + j] = t;
+      }
+      const double t = bvec[k];
+      bvec[k] = bvec[best];
+      bvec[best] = t;
+    }
+    const double d = A[k * p + k];
+    for (int i = k + 1; i < p; ++i) {
+      const double f = A[i * p + k] / d;
+      for (int j = k; j < p; ++j) A[i * p + j] -= f * A[k * p + j];
+      bvec[i] -= f * bvec[k];
+    }
+  }
+  for (int i = p - 1; i >= 0; --i) {
+    double v = bvec[i];
+    for (int k = i + 1; k < p; ++k) v -= A[i * p + k] * h[k];
+    h[i] = v / A[i * p + i];
+  }
+  return false;
+}
+
+
+}  // namespace apgb

@@ -1,0 +1,93 @@
+// Host-side declarations shared by the kernel and C-ABI translation units.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "ap_device.cuh"
+
+namespace apgb {
+
+// Per-stamp LM state (float64), one thread per stamp updates it.
+struct LMState {
+  int32_t phase;      // LM_PH_*
+  int32_t status;     // AP_LM_*
+  int32_t iter;       // outer iterations done
+  int32_t sub;        // inner (damping search) iteration
+  int32_t direction;  // 0 none, 1 better, 2 worse
+  int32_t nostep;
+  int32_t scarry_valid;
+  int32_t hist_len;
+  double L;
+  double chi2_cur;    // loss_history[-1]
+  double init_chi2;
+  double ndf;
+  double best_chi2, best_L, scarry_chi2, scarry_L;
+  double x[NPARAM], h[NPARAM], a[NPARAM], ha[NPARAM];
+  double best_ha[NPARAM], scarry_ha[NPARAM];
+  double H[NPARAM * NPARAM], g[NPARAM];
+};
+
+enum LMPhase { LM_PH_INIT = 0, LM_PH_JAC = 1, LM_PH_SUB = 2, LM_PH_SUB2 = 3, LM_PH_DONE = 4 };
+
+struct LMArgs {
+  int32_t max_iter, max_step_iter;
+  double rel_tol, curvature_limit, Lup, Ldn, L0, acceleration;
+  LMState* st;             // [n]
+  double* params_next;     // [n][2][8]  value space
+  int32_t* ops_next;       // [n][2]
+  double* hvec;            // [n][8] h of the current trial (for OP_RPP)
+  const double* fixed;     // [n][8] value-space parameters of locked slots
+  double* hist_loss;       // [n][max_iter + 1]
+  double* hist_L;          // [n][max_iter + 1]
+  double* hist_x;          // [n][max_iter + 1][8]
+  double* state_out;       // [n][n_free]
+  double* chi2_out;        // [n]
+  int32_t* iters_out;      // [n]
+  int32_t* status_out;     // [n]
+  uint32_t* active_count;  // device counter of stamps not done
+};
+
+// Optional CUDA-event timing of each kernel class (works inside captured graphs: every
+// round captured gets its own event pairs, harvested after each replay).
+enum KernelClass { KC_SETUP = 0, KC_PSF, KC_SAMPLE, KC_SELECT, KC_INTEGRATE, KC_CONV, KC_REDUCE,
+                   KC_LM, KC_COUNT };
+
+struct Profiler {
+  bool on = false;
+  int used = 0;              // event pairs in use
+  int cap = 0;               // pairs created
+  cudaEvent_t* ev = nullptr; // [cap][2]
+  int* kind = nullptr;       // [cap]
+  double ms[KC_COUNT] = {0};
+  long long launches[KC_COUNT] = {0};
+  int begin(int k, cudaStream_t s);
+  void end(int idx, cudaStream_t s);
+  void harvest(bool reset);  // after a synchronise: add elapsed times of the used pairs
+  void clear_totals();
+  void destroy();
+};
+
+// render-pass launches (ap_kernels.cu)
+cudaError_t launch_eval_setup(const BatchArgs& b, const double* params, int64_t stamp_stride,
+                              int64_t slot_stride, const int32_t* ops, int32_t ops_uniform,
+                              cudaStream_t s);
+cudaError_t launch_render_pass(const BatchArgs& b, const ConvIO& io, size_t conv_smem,
+                               bool accumulate, cudaStream_t s, Profiler* prof = nullptr);
+cudaError_t launch_fma_probe(float* out, int iters, int blocks, cudaStream_t s);
+cudaError_t set_conv_smem(size_t bytes);
+cudaError_t launch_chi2_only(const BatchArgs& b, const ConvIO& io, const float* model,
+                             double* out, cudaStream_t s);
+cudaError_t launch_psf_only(const BatchArgs& b, const float* psf, cudaStream_t s);
+cudaError_t launch_damped_solve(int m, int p, const double* hess, const double* grad,
+                                const double* L, double* h, cudaStream_t s);
+cudaError_t launch_psf_export(const BatchArgs& b, float* out, float* d_out, int64_t stride,
+                              cudaStream_t s);
+
+// LM launches (ap_lm.cu)
+cudaError_t launch_lm_init(const BatchArgs& b, const LMArgs& lm, const double* state0,
+                           const uint8_t* mask, cudaStream_t s);
+cudaError_t launch_lm_update(const BatchArgs& b, const LMArgs& lm, cudaStream_t s);
+cudaError_t launch_lm_finish(const BatchArgs& b, const LMArgs& lm, cudaStream_t s);
+
+}  // namespace apgb

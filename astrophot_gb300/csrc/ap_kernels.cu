@@ -1,0 +1,1032 @@
+// Render-pass kernels: evaluation setup, PSF shift, sampling, integration-mask selection,
+// adaptive sub-pixel integration, PSF convolution with fused Jacobian / chi^2 / J^T W J /
+// J^T W r accumulation, and the per-stamp reduction of the tile partials.
+//
+// One render pass handles every stamp of a batch and two evaluation slots per stamp
+// (the LM evaluates two parameter vectors per damping trial).  Reference stages:
+//   _sample_init          astrophot/models/_model_methods.py:82-148
+//   _sample_integrate     astrophot/models/_model_methods.py:155-184
+//   grid_integrate        astrophot/utils/operations.py:150-247
+//   _shift_psf, renorm    astrophot/models/_model_methods.py:187-243
+//   fft/direct convolve   astrophot/models/_model_methods.py:245-257, utils/operations.py:9-36
+//   crop                  astrophot/models/model_object.py:345-349
+//   chi2, hess, grad, rpp astrophot/fit/lm.py:374-406
+#include <cmath>
+
+#include "ap_internal.h"
+
+namespace apgb {
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ double sersic_b64(double n) {
+  return 2 * n - 1.0 / 3.0 + 4.0 / (405.0 * n) + 46.0 / (25515.0 * n * n) +
+         131.0 / (1148175.0 * n * n * n) - 2194697.0 / (30690717750.0 * n * n * n * n);
+}
+
+__device__ __forceinline__ double sersic_db64(double n) {
+  return 2.0 - 4.0 / (405.0 * n * n) - 2.0 * 46.0 / (25515.0 * n * n * n) -
+         3.0 * 131.0 / (1148175.0 * n * n * n * n) +
+         4.0 * 2194697.0 / (30690717750.0 * n * n * n * n * n);
+}
+
+// d value / d representation (utils/conversions/optimization.py:40-47), from the value.
+__device__ __forceinline__ double drep_from_value(int slot, double v) {
+  switch (slot) {
+    case PQ: {  // limits (0, 1)
+      const double r = tan((v - 0.0) * kPi / 1.0 - kPi / 2);
+      return 1.0 / (kPi * (r * r + 1));
+    }
+    case PN: {  // limits (0.36, 8)
+      const double r = tan((v - 0.36) * kPi / (8.0 - 0.36) - kPi / 2);
+      return (8.0 - 0.36) / (kPi * (r * r + 1));
+    }
+    case PRE: {  // limits (0, None)
+      const double r = v - 1.0 / (v - 0.0);
+      return 0.5 + 0.5 * (r - 0.0) / sqrt((r - 0.0) * (r - 0.0) + 4);
+    }
+    default:
+      return 1.0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// evaluation setup: FP64 parameters -> per (stamp, slot) constants
+// ---------------------------------------------------------------------------
+__global__ void k_eval_setup(BatchArgs b, const double* params, int64_t stamp_stride,
+                             int64_t slot_stride, const int32_t* ops, int32_t ops_uniform) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t == 0) {
+    b.counters[0] = 0;  // queue length
+    b.counters[1] = 0;  // queue head
+  }
+  if (t >= b.n_stamps * 2) return;
+  const int s = t >> 1, slot = t & 1;
+  EvalDev& e = b.evals[t];
+  b.mean_acc[t] = 0.0;
+  const int32_t op = ops ? ops[t] : (slot == 0 ? ops_uniform : 0);
+  e.ops = op;
+  if (!op) return;
+  const StampDev& st = b.stamps[s];
+  const double* v = params + s * stamp_stride + slot * slot_stride;
+  for (int i = 0; i < NPARAM; ++i) e.v[i] = v[i];
+  // centre in the working grid: plane_to_pixel (image/wcs.py:587-610) of the padded window
+  const double dx = v[PX] - st.ref_xy[0], dy = v[PY] - st.ref_xy[1];
+  const double pcx = st.Pinv[0] * dx + st.Pinv[1] * dy + st.ref_ij[0] + st.bx;
+  const double pcy = st.Pinv[2] * dx + st.Pinv[3] * dy + st.ref_ij[1] + st.by;
+  if (b.psf_mode == AP_PSF_FULL) {
+    // sub-pixel shift onto a pixel centre (models/model_object.py:320-323)
+    const double rx = rint(pcx), ry = rint(pcy);
+    e.shift[0] = pcx - rx;
+    e.shift[1] = pcy - ry;
+    e.cix = (int32_t)rx;
+    e.cjy = (int32_t)ry;
+    e.fx64 = e.fy64 = 0.0;
+  } else {
+    const double fxx = floor(pcx), fyy = floor(pcy);
+    e.shift[0] = e.shift[1] = 0.0;
+    e.cix = (int32_t)fxx;
+    e.cjy = (int32_t)fyy;
+    e.fx64 = pcx - fxx;
+    e.fy64 = pcy - fyy;
+  }
+  e.fx = (float)e.fx64;
+  e.fy = (float)e.fy64;
+  // inclined transform (models/_shared_methods.py:301-307): rotate by -(PA - north)
+  const double theta = -(v[PPA] - kPi / 2);
+  e.c64 = cos(theta);
+  e.s64 = sin(theta);
+  e.c = (float)e.c64;
+  e.s = (float)e.s64;
+  e.invq = (float)(1.0 / v[PQ]);
+  e.Re = (float)v[PRE];
+  e.invRe = (float)(1.0 / v[PRE]);
+  const double n = (b.kind == AP_PROFILE_SERSIC) ? v[PN] : 1.0;
+  e.invn = (float)(1.0 / n);
+  e.bn64 = sersic_b64(n);
+  e.bn = (float)e.bn64;
+  e.dbn = (float)sersic_db64(n);
+  e.amp64 = st.pixel_area * pow(10.0, v[PIE]);
+  e.amp = (float)e.amp64;
+  e.sky = b.has_sky ? (float)(st.pixel_area * pow(10.0, v[PF])) : 0.f;
+  e.soft2_64 = b.softening64 * b.softening64;
+  e.soft2 = (float)e.soft2_64;
+  // integration reference: Sersic total flux / numel (models/sersic_model.py:78-89,
+  // utils/conversions/functions.py:168-190); exponential uses sum(deep) / numel later
+  if (b.kind == AP_PROFILE_SERSIC) {
+    const double Ie = pow(10.0, v[PIE]);
+    const double bn = e.bn64;
+    const double flux = 2 * kPi * Ie * v[PRE] * v[PRE] * v[PQ] * n * (exp(bn) * pow(bn, -2 * n)) *
+                        exp(lgamma(2 * n));
+    e.thresh64 = b.tolerance64 * (flux / ((double)st.wnx * (double)st.wny));
+  } else {
+    e.thresh64 = 0.0;
+  }
+  e.thresh = (float)e.thresh64;
+  for (int i = 0; i < NPARAM; ++i) e.drep[i] = (float)drep_from_value(i, v[i]);
+}
+
+// ---------------------------------------------------------------------------
+// PSF shift (bilinear interp2d of the 1-padded PSF) and renormalisation, with d/d shift
+// ---------------------------------------------------------------------------
+struct ShiftVal {
+  double v, dx, dy;
+};
+
+__device__ __forceinline__ ShiftVal shifted_psf_at(const float* psf, int kx, int ky, int ix, int iy,
+                                                   double sx, double sy) {
+  const int w = kx + 2, h = ky + 2;
+  auto pad = [&](int r, int c) -> double {
+    const int rr = r - 1, cc = c - 1;
+    return (rr >= 0 && rr < ky && cc >= 0 && cc < kx) ? (double)psf[rr * kx + cc] : 0.0;
+  };
+  const double x = ix - sx, y = iy - sy;
+  int x0 = (int)floor(x), y0 = (int)floor(y);
+  int x1 = x0 + 1, y1 = y0 + 1;
+  x0 = min(max(x0, 0), w - 2);
+  x1 = min(max(x1, 1), w - 1);
+  y0 = min(max(y0, 0), h - 2);
+  y1 = min(max(y1, 1), h - 1);
+  const double fa = pad(y0, x0), fb = pad(y1, x0), fc = pad(y0, x1), fd = pad(y1, x1);
+  ShiftVal r;
+  r.v = fa * ((x1 - x) * (y1 - y)) + fb * ((x1 - x) * (y - y0)) + fc * ((x - x0) * (y1 - y)) +
+        fd * ((x - x0) * (y - y0));
+  r.dx = -(fa * (-(y1 - y)) + fb * (-(y - y0)) + fc * (y1 - y) + fd * (y - y0));
+  r.dy = -(fa * (-(x1 - x)) + fb * (x1 - x) + fc * (-(x - x0)) + fd * (x - x0));
+  return r;
+}
+
+__device__ double block_sum_d(double v, double* sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __syncthreads();
+  if (lane == 0) sh[warp] = v;
+  __syncthreads();
+  double t = 0;
+  const int nw = (blockDim.x + 31) >> 5;
+  for (int i = 0; i < nw; ++i) t += sh[i];
+  return t;
+}
+
+__global__ void k_psf_shift(BatchArgs b, const float* psf) {
+  const int s = blockIdx.x, slot = blockIdx.y;
+  const EvalDev& e = b.evals[s * 2 + slot];
+  if (!e.ops) return;
+  const StampDev& st = b.stamps[s];
+  const int kp2 = st.kpx * st.kpy;
+  const float* P = psf + st.psf_off;
+  float* out = b.spsf + st.spsf_off + (int64_t)slot * 3 * kp2;
+  __shared__ double sh[32];
+  const bool jac = (e.ops & OP_JAC) != 0;
+  if (b.psf_mode == AP_PSF_FULL) {
+    double S = 0, Sx = 0, Sy = 0;
+    for (int idx = threadIdx.x; idx < kp2; idx += blockDim.x) {
+      const ShiftVal r =
+          shifted_psf_at(P, st.kx, st.ky, idx % st.kpx, idx / st.kpx, e.shift[0], e.shift[1]);
+      S += r.v;
+      Sx += r.dx;
+      Sy += r.dy;
+    }
+    S = block_sum_d(S, sh);
+    Sx = block_sum_d(Sx, sh);
+    Sy = block_sum_d(Sy, sh);
+    for (int idx = threadIdx.x; idx < kp2; idx += blockDim.x) {
+      const ShiftVal r =
+          shifted_psf_at(P, st.kx, st.ky, idx % st.kpx, idx / st.kpx, e.shift[0], e.shift[1]);
+      out[idx] = (float)(r.v / S);
+      if (jac) {
+        out[kp2 + idx] = (float)(r.dx / S - r.v * Sx / (S * S));
+        out[2 * kp2 + idx] = (float)(r.dy / S - r.v * Sy / (S * S));
+      }
+    }
+  } else {
+    double S = 0;
+    for (int idx = threadIdx.x; idx < kp2; idx += blockDim.x) S += (double)P[idx];
+    S = block_sum_d(S, sh);
+    for (int idx = threadIdx.x; idx < kp2; idx += blockDim.x) out[idx] = (float)((double)P[idx] / S);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// sampling (_sample_init): deep value, partials, reference sub-sample, FP32 error bound
+// ---------------------------------------------------------------------------
+template <bool JAC>
+__device__ __forceinline__ void sample_pixel(const BatchArgs& b, const StampDev& st,
+                                             const EvalDev& e, int i, int j, float& deep,
+                                             float* g, float& refsub, float& errb) {
+  const QuadTables& T = *b.tables;
+  const float di = (float)(i - e.cix), dj = (float)(j - e.cjy);
+  deep = 0.f;
+#pragma unroll
+  for (int k = 0; k < NGRAD; ++k) g[k] = 0.f;
+  float absb = 0.f, mag = 0.f;
+  refsub = 0.f;
+  float referr = 0.f;
+  for (int k = 0; k < T.nsub; ++k) {
+    float X, Y;
+    pix_to_offset(st, e, di + (float)T.sx[k], dj + (float)T.sy[k], X, Y);
+    const Sample sm = eval_profile<JAC>(e, b.kind, X, Y, 1.f);
+    const float w = (float)T.sw[k];
+    deep = fmaf(w, sm.v, deep);
+    if (JAC) {
+#pragma unroll
+      for (int q = 0; q < NGRAD; ++q) g[q] = fmaf(w, sm.g[q], g[q]);
+    }
+    const float a = fabsf(w * sm.v);
+    mag += a;
+    absb += a * sample_rel_err(e, sm.arg);
+    if (k == T.sub_center) {
+      refsub = sm.v;
+      referr = fabsf(sm.v) * sample_rel_err(e, sm.arg);
+    }
+  }
+  // bound on |deep_fp32 - deep_fp64| (+ the reference sub-sample's for simpsons / quad)
+  errb = absb + 2.f * (float)T.nsub * kEps * mag + referr;
+}
+
+__device__ double sample_pixel64(const BatchArgs& b, const StampDev& st, const EvalDev& e, int i,
+                                 int j, double* refsub) {
+  const QuadTables& T = *b.tables;
+  const double di = (double)(i - e.cix), dj = (double)(j - e.cjy);
+  double deep = 0.0;
+  for (int k = 0; k < T.nsub; ++k) {
+    double X, Y;
+    pix_to_offset64(st, e, di + T.sx[k], dj + T.sy[k], X, Y);
+    const double f = eval_profile64(e, b.kind, X, Y, 1.0);
+    deep += T.sw[k] * f;
+    if (k == T.sub_center && refsub) *refsub = f;
+  }
+  return deep;
+}
+
+template <bool JAC>
+__device__ void sample_tile(const BatchArgs& b, int s, int slot, int tile_local) {
+  const StampDev& st = b.stamps[s];
+  const EvalDev& e = b.evals[s * 2 + slot];
+  const int tx = threadIdx.x & (kTile - 1), ty = threadIdx.x / kTile;
+  const int i = (tile_local % st.ntw_x) * kTile + tx;
+  const int j = (tile_local / st.ntw_x) * kTile + ty;
+  const bool valid = (i < st.wnx) && (j < st.wny);
+  float deep = 0.f;
+  if (valid) {
+    float g[NGRAD], refsub, errb;
+    sample_pixel<JAC>(b, st, e, i, j, deep, g, refsub, errb);
+    const int64_t p = st.work_off + (int64_t)j * st.wnx + i;
+    b.work[work_plane(b, slot, 0) + p] = deep;
+    if (JAC) {
+#pragma unroll
+      for (int q = 0; q < NGRAD; ++q) b.work[work_plane(b, slot, 1 + q) + p] = g[q];
+    }
+    float* aux = b.aux + (int64_t)slot * 2 * b.work_pixels;
+    aux[p] = refsub;
+    aux[b.work_pixels + p] = errb;
+  }
+  {
+    const unsigned cnt = __popc(__ballot_sync(0xffffffffu, valid));
+    if ((threadIdx.x & 31) == 0 && cnt)
+      atomicAdd(b.work_ctr + 2, (unsigned long long)cnt * (unsigned long long)b.tables->nsub);
+  }
+  if (b.kind == AP_PROFILE_EXPONENTIAL && b.integrate == AP_INTEGRATE_THRESHOLD) {
+    // sum(deep) for the default _integrate_reference (models/_model_methods.py:151-152)
+    float v = warp_sum(valid ? deep : 0.f);
+    __shared__ float sh[kTile * kTile / 32];
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0;
+      for (int w = 0; w < kTile * kTile / 32; ++w) t += (double)sh[w];
+      atomicAdd(&b.mean_acc[s * 2 + slot], t);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_sample(BatchArgs b) {
+  const int tile = blockIdx.x, slot = blockIdx.y;
+  const int s = b.work_tiles[tile];
+  const EvalDev& e = b.evals[s * 2 + slot];
+  if (!e.ops) return;
+  const int local = tile - b.stamps[s].tile_w0;
+  if (e.ops & OP_JAC)
+    sample_tile<true>(b, s, slot, local);
+  else
+    sample_tile<false>(b, s, slot, local);
+}
+
+// ---------------------------------------------------------------------------
+// threshold selection (_sample_integrate) + enqueue
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void stamp_threshold(const BatchArgs& b, const StampDev& st,
+                                                const EvalDev& e, int s, int slot, float& thr,
+                                                double& thr64, float& thr_err) {
+  if (b.kind == AP_PROFILE_SERSIC) {
+    thr = e.thresh;
+    thr64 = e.thresh64;
+    thr_err = 2.f * kEps * thr;
+  } else {
+    thr64 = b.tolerance64 * (b.mean_acc[s * 2 + slot] / ((double)st.wnx * (double)st.wny));
+    thr = (float)thr64;
+    // the FP32 samples make the mean uncertain at the 1e-6 level
+    thr_err = 2e-6f * thr;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_select(BatchArgs b) {
+  const int tile = blockIdx.x, slot = blockIdx.y;
+  const int s = b.work_tiles[tile];
+  const EvalDev& e = b.evals[s * 2 + slot];
+  if (!e.ops) return;
+  const StampDev& st = b.stamps[s];
+  const int local = tile - st.tile_w0;
+  const int i = (local % st.ntw_x) * kTile + (threadIdx.x & (kTile - 1));
+  const int j = (local / st.ntw_x) * kTile + threadIdx.x / kTile;
+  if (i >= st.wnx || j >= st.wny) return;
+  float thr, thr_err;
+  double thr64;
+  stamp_threshold(b, st, e, s, slot, thr, thr64, thr_err);
+  const float* d = b.work + work_plane(b, slot, 0) + st.work_off;
+  const float* aux = b.aux + (int64_t)slot * 2 * b.work_pixels + st.work_off;
+  const float* eb = aux + b.work_pixels;
+  const int64_t p = (int64_t)j * st.wnx + i;
+  const float deep = d[p];
+  float err, bound;
+  const bool stencil = (b.sampling == AP_SAMPLING_MIDPOINT || b.sampling == AP_SAMPLING_TRAPEZOID);
+  int ic = 0, jc = 0;
+  if (stencil) {
+    // Laplacian 3x3 'valid' then replicate pad (models/_model_methods.py:87-98)
+    ic = min(max(i, 1), st.wnx - 2);
+    jc = min(max(j, 1), st.wny - 2);
+    const int64_t c = (int64_t)jc * st.wnx + ic;
+    const float u = d[c - st.wnx], l = d[c - 1], m = d[c], r = d[c + 1], dn = d[c + st.wnx];
+    const float lap = u + l + (-4.f) * m + r + dn;
+    const float refimg = deep + lap;
+    err = fabsf(deep - refimg);
+    const float mag = fabsf(u) + fabsf(l) + 4.f * fabsf(m) + fabsf(r) + fabsf(dn);
+    bound = eb[c - st.wnx] + eb[c - 1] + 4.f * eb[c] + eb[c + 1] + eb[c + st.wnx] + eb[p] +
+            8.f * kEps * mag + 4.f * kEps * (fabsf(deep) + fabsf(refimg));
+  } else {
+    const float ref = aux[p];
+    err = fabsf(deep - ref);
+    bound = eb[p] + 4.f * kEps * (fabsf(deep) + fabsf(ref));
+  }
+  bound = 2.f * bound + thr_err;
+  bool sel;
+  if (err > thr + bound) {
+    sel = true;
+  } else if (err < thr - bound) {
+    sel = false;
+  } else {
+    // too close to call in FP32: decide from float64 samples
+    atomicAdd(&b.counters[2], 1u);
+    double err64;
+    if (stencil) {
+      const double m0 = sample_pixel64(b, st, e, i, j, nullptr);
+      const double u = sample_pixel64(b, st, e, ic, jc - 1, nullptr);
+      const double l = sample_pixel64(b, st, e, ic - 1, jc, nullptr);
+      const double m = sample_pixel64(b, st, e, ic, jc, nullptr);
+      const double r = sample_pixel64(b, st, e, ic + 1, jc, nullptr);
+      const double dn = sample_pixel64(b, st, e, ic, jc + 1, nullptr);
+      const double lap = u + l + (-4.0) * m + r + dn;
+      err64 = fabs(m0 - (m0 + lap));
+    } else {
+      double ref64 = 0;
+      const double deep64 = sample_pixel64(b, st, e, i, j, &ref64);
+      err64 = fabs(deep64 - ref64);
+    }
+    sel = err64 > thr64;
+  }
+  if (sel) {
+    const uint32_t slotq = atomicAdd(&b.counters[0], 1u);
+    if ((int64_t)slotq < 2 * b.work_pixels) {
+      b.queue[slotq] = ((int64_t)slot << 62) | ((int64_t)s << 32) | (int64_t)p;
+    } else {
+      atomicOr(&b.counters[3], 1u);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// adaptive integration of the queued pixels (grid_integrate, max depth <= 3)
+// ---------------------------------------------------------------------------
+struct QuadResult {
+  float res, ref, errb, mag;
+  float g[NGRAD];
+};
+
+// One (sub-)pixel integrated by this lane alone: Q^2 samples at unit offsets
+// (ci + qx / scale, cj + qy / scale) with amplitude scale area.
+template <bool JAC>
+__device__ __forceinline__ QuadResult quad_lane(const BatchArgs& b, const StampDev& st,
+                                                const EvalDev& e, float ci, float cj, float inv_g,
+                                                float area) {
+  const QuadTables& T = *b.tables;
+  const int n = T.quad_level * T.quad_level;
+  const int mid = n / 2;
+  QuadResult r;
+  r.res = 0.f;
+  r.ref = 0.f;
+  r.errb = 0.f;
+  r.mag = 0.f;
+#pragma unroll
+  for (int q = 0; q < NGRAD; ++q) r.g[q] = 0.f;
+  float referr = 0.f;
+  for (int k = 0; k < n; ++k) {
+    float X, Y;
+    pix_to_offset(st, e, ci + (float)T.qx[k] * inv_g, cj + (float)T.qy[k] * inv_g, X, Y);
+    const Sample sm = eval_profile<JAC>(e, b.kind, X, Y, area);
+    const float w = (float)T.qw[k];
+    r.res = fmaf(w, sm.v, r.res);
+    if (JAC) {
+#pragma unroll
+      for (int q = 0; q < NGRAD; ++q) r.g[q] = fmaf(w, sm.g[q], r.g[q]);
+    }
+    const float a = fabsf(w * sm.v);
+    r.mag += a;
+    r.errb += a * sample_rel_err(e, sm.arg);
+    if (k == mid) {
+      r.ref = sm.v;
+      referr = fabsf(sm.v) * sample_rel_err(e, sm.arg);
+    }
+  }
+  r.errb += referr + 2.f * n * kEps * (r.mag + fabsf(r.ref));
+  return r;
+}
+
+__device__ bool refine64(const BatchArgs& b, const StampDev& st, const EvalDev& e, double ci,
+                         double cj, double inv_g, double area, double thr64) {
+  const QuadTables& T = *b.tables;
+  const int n = T.quad_level * T.quad_level;
+  double res = 0, ref = 0;
+  for (int k = 0; k < n; ++k) {
+    double X, Y;
+    pix_to_offset64(st, e, ci + T.qx[k] * inv_g, cj + T.qy[k] * inv_g, X, Y);
+    const double f = eval_profile64(e, b.kind, X, Y, area);
+    res += f * T.qw[k];
+    if (k == n / 2) ref = f;
+  }
+  return fabs(res - ref) > thr64;
+}
+
+__device__ __forceinline__ bool decide(const BatchArgs& b, const StampDev& st, const EvalDev& e,
+                                       const QuadResult& r, float thr, double thr64, float ci,
+                                       float cj, double ci64, double cj64, float inv_g,
+                                       double inv_g64, float area, double area64) {
+  const float diff = fabsf(r.res - r.ref);
+  const float band = 2.f * r.errb + 4.f * kEps * thr;
+  if (diff > thr + band) return true;
+  if (diff < thr - band) return false;
+  atomicAdd(&b.counters[2], 1u);
+  return refine64(b, st, e, ci64, cj64, inv_g64, area64, thr64);
+}
+
+template <bool JAC>
+__device__ void integrate_entry(const BatchArgs& b, int slot, int s, int64_t p, int lane) {
+  const StampDev& st = b.stamps[s];
+  const EvalDev& e = b.evals[s * 2 + slot];
+  const QuadTables& T = *b.tables;
+  const int Q2 = T.quad_level * T.quad_level;
+  const int g = T.gridding, G2 = g * g;
+  const int i = (int)(p % st.wnx), j = (int)(p / st.wnx);
+  const float di = (float)(i - e.cix), dj = (float)(j - e.cjy);
+  const double di64 = (double)(i - e.cix), dj64 = (double)(j - e.cjy);
+  float thr, thr_err;
+  double thr64;
+  stamp_threshold(b, st, e, s, slot, thr, thr64, thr_err);
+  const float ginv = 1.f / (float)g;
+  const double ginv64 = 1.0 / (double)g;
+
+  int n_samples = Q2;
+  // level 1: Q^2 samples spread over the lanes
+  float v = 0.f, gv[NGRAD];
+#pragma unroll
+  for (int q = 0; q < NGRAD; ++q) gv[q] = 0.f;
+  float f = 0.f, fe = 0.f, fa = 0.f;
+  if (lane < Q2) {
+    float X, Y;
+    pix_to_offset(st, e, di + (float)T.qx[lane], dj + (float)T.qy[lane], X, Y);
+    const Sample sm = eval_profile<JAC>(e, b.kind, X, Y, 1.f);
+    const float w = (float)T.qw[lane];
+    f = sm.v;
+    v = w * sm.v;
+    fa = fabsf(v);
+    fe = fa * sample_rel_err(e, sm.arg);
+    if (JAC) {
+#pragma unroll
+      for (int q = 0; q < NGRAD; ++q) gv[q] = w * sm.g[q];
+    }
+  }
+  const float res1 = warp_sum(v);
+  float gres1[NGRAD];
+  if (JAC) {
+#pragma unroll
+    for (int q = 0; q < NGRAD; ++q) gres1[q] = warp_sum(gv[q]);
+  }
+  float out_v = res1;
+  float out_g[NGRAD];
+#pragma unroll
+  for (int q = 0; q < NGRAD; ++q) out_g[q] = JAC ? gres1[q] : 0.f;
+
+  if (b.max_depth > 1) {
+    const float ref1 = __shfl_sync(0xffffffffu, f, Q2 / 2);
+    const float ref1e = __shfl_sync(0xffffffffu, fe / fmaxf(fabsf(v), 1e-38f) * fabsf(f), Q2 / 2);
+    QuadResult r1;
+    r1.res = res1;
+    r1.ref = ref1;
+    r1.mag = warp_sum(fa);
+    r1.errb = warp_sum(fe) + ref1e + 2.f * Q2 * kEps * (r1.mag + fabsf(ref1));
+    bool split = false;
+    if (lane == 0) split = decide(b, st, e, r1, thr, thr64, di, dj, di64, dj64, 1.f, 1.0, 1.f, 1.0);
+    split = __shfl_sync(0xffffffffu, split ? 1 : 0, 0) != 0;
+    if (split) {
+      n_samples += G2 * Q2;
+      // level 2: one sub-pixel per lane
+      const float area2 = ginv * ginv;
+      QuadResult r2;
+      r2.res = 0.f;
+#pragma unroll
+      for (int q = 0; q < NGRAD; ++q) r2.g[q] = 0.f;
+      float ci2 = 0.f, cj2 = 0.f;
+      bool split2 = false;
+      if (lane < G2) {
+        ci2 = di + (float)T.gx[lane];
+        cj2 = dj + (float)T.gy[lane];
+        r2 = quad_lane<JAC>(b, st, e, ci2, cj2, ginv, area2);
+        if (b.max_depth > 2) {
+          const float thr2 = thr * (float)G2;
+          const double thr2_64 = thr64 * (double)G2;
+          split2 = decide(b, st, e, r2, thr2, thr2_64, ci2, cj2, di64 + T.gx[lane],
+                          dj64 + T.gy[lane], ginv, ginv64, area2, ginv64 * ginv64);
+        }
+      }
+      // level 3: refine each flagged sub-pixel with the whole warp
+      unsigned todo = __ballot_sync(0xffffffffu, split2);
+      n_samples += __popc(todo) * G2 * Q2;
+      const float area3 = area2 * area2;
+      while (todo) {
+        const int m = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const float cim = __shfl_sync(0xffffffffu, ci2, m);
+        const float cjm = __shfl_sync(0xffffffffu, cj2, m);
+        QuadResult r3;
+        r3.res = 0.f;
+#pragma unroll
+        for (int q = 0; q < NGRAD; ++q) r3.g[q] = 0.f;
+        if (lane < G2) {
+          r3 = quad_lane<JAC>(b, st, e, cim + (float)T.gx[lane] * ginv,
+                              cjm + (float)T.gy[lane] * ginv, ginv * ginv, area3);
+        }
+        const float s3 = warp_sum(r3.res);
+        float gs3[NGRAD];
+        if (JAC) {
+#pragma unroll
+          for (int q = 0; q < NGRAD; ++q) gs3[q] = warp_sum(r3.g[q]);
+        }
+        if (lane == m) {
+          r2.res = s3;
+          if (JAC) {
+#pragma unroll
+            for (int q = 0; q < NGRAD; ++q) r2.g[q] = gs3[q];
+          }
+        }
+      }
+      out_v = warp_sum(lane < G2 ? r2.res : 0.f);
+      if (JAC) {
+#pragma unroll
+        for (int q = 0; q < NGRAD; ++q) out_g[q] = warp_sum(lane < G2 ? r2.g[q] : 0.f);
+      }
+    }
+  }
+  if (lane == 0) {
+    atomicAdd(b.work_ctr + 1, (unsigned long long)n_samples);
+    const int64_t wp = st.work_off + p;
+    b.work[work_plane(b, slot, 0) + wp] = out_v;
+    if (JAC) {
+#pragma unroll
+      for (int q = 0; q < NGRAD; ++q) b.work[work_plane(b, slot, 1 + q) + wp] = out_g[q];
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_integrate(BatchArgs b) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t n = min((uint32_t)b.counters[0], (uint32_t)(2 * b.work_pixels));
+  while (true) {
+    uint32_t idx = 0;
+    if (lane == 0) idx = atomicAdd(&b.counters[1], 1u);
+    idx = __shfl_sync(0xffffffffu, idx, 0);
+    if (idx >= n) break;
+    const int64_t ent = b.queue[idx];
+    const int slot = (int)(ent >> 62);
+    const int s = (int)((ent >> 32) & 0x3fffffff);
+    const int64_t p = ent & 0xffffffffll;
+    if (b.evals[s * 2 + slot].ops & OP_JAC)
+      integrate_entry<true>(b, slot, s, p, lane);
+    else
+      integrate_entry<false>(b, slot, s, p, lane);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// convolution + crop + fused accumulation
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void tile_reduce(float* vals, int nvals, double* dst, float* sh) {
+  // vals: per-thread partial values; writes the tile sums to dst[0..nvals)
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr int NW = kTile * kTile / 32;
+  for (int k = 0; k < nvals; ++k) {
+    const float v = warp_sum(vals[k]);
+    if (lane == 0) sh[warp * kNacc + k] = v;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < nvals; k += blockDim.x) {
+    double t = 0;
+    for (int w = 0; w < NW; ++w) t += (double)sh[w * kNacc + k];
+    dst[k] = t;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_conv(BatchArgs b, ConvIO io) {
+  extern __shared__ float smem[];
+  const int tile = blockIdx.x, slot = blockIdx.y;
+  const int s = b.out_tiles[tile];
+  const EvalDev& e = b.evals[s * 2 + slot];
+  const int ops = e.ops;
+  double* tacc = b.tile_acc + ((int64_t)tile * 2 + slot) * kNacc;
+  if (!ops) return;
+  const StampDev& st = b.stamps[s];
+  const int local = tile - st.tile_o0;
+  const int tx = threadIdx.x & (kTile - 1), ty = threadIdx.x / kTile;
+  const int x0 = (local % st.nto_x) * kTile, y0 = (local / st.nto_x) * kTile;
+  const int x = x0 + tx, y = y0 + ty;
+  const bool valid = (x < st.nx) && (y < st.ny);
+  const bool jac = (ops & OP_JAC) != 0;
+  const bool shiftmode = (b.psf_mode == AP_PSF_FULL);
+
+  // conv results: [0] model, [1] d/dshift_x, [2] d/dshift_y, [3+q] plane q+1 convolved
+  float cv[3 + NGRAD];
+#pragma unroll
+  for (int k = 0; k < 3 + NGRAD; ++k) cv[k] = 0.f;
+
+  const int nplanes = jac ? 1 + NGRAD : 1;
+  if (b.psf_mode == AP_PSF_NONE) {
+    if (valid) {
+      const int64_t wp = st.work_off + (int64_t)y * st.wnx + x;
+      cv[0] = b.work[work_plane(b, slot, 0) + wp];
+      for (int q = 0; q < nplanes - 1; ++q) cv[3 + q] = b.work[work_plane(b, slot, 1 + q) + wp];
+    }
+  } else {
+    const int kpx = st.kpx, kpy = st.kpy, kp2 = kpx * kpy;
+    const int cx = (kpx - 1) / 2, cy = (kpy - 1) / 2;
+    const int TW = kTile + kpx - 1, TH = kTile + kpy - 1;
+    float* K = smem;              // up to 3 kernels
+    float* Tt = smem + 3 * kp2;   // input tile
+    const float* ksrc = b.spsf + st.spsf_off + (int64_t)slot * 3 * kp2;
+    const int nk = (jac && shiftmode) ? 3 : 1;
+    for (int idx = threadIdx.x; idx < nk * kp2; idx += blockDim.x) K[idx] = ksrc[idx];
+    const int row0 = y0 + st.by - cy, col0 = x0 + st.bx - cx;
+    for (int pl = 0; pl < nplanes; ++pl) {
+      if (pl > 0 && shiftmode && (pl - 1 == GX || pl - 1 == GY)) continue;
+      if (pl > 0 && b.kind != AP_PROFILE_SERSIC && pl - 1 == GN) continue;
+      __syncthreads();
+      const float* src = b.work + work_plane(b, slot, pl) + st.work_off;
+      for (int idx = threadIdx.x; idx < TW * TH; idx += blockDim.x) {
+        const int r = idx / TW, c = idx % TW;
+        const int wr = row0 + r, wc = col0 + c;
+        Tt[idx] = (wr >= 0 && wr < st.wny && wc >= 0 && wc < st.wnx) ? src[(int64_t)wr * st.wnx + wc]
+                                                                      : 0.f;
+      }
+      __syncthreads();
+      const int nkp = (pl == 0) ? nk : 1;
+      for (int kk = 0; kk < nkp; ++kk) {
+        const float* Kk = K + kk * kp2;
+        float a = 0.f;
+        for (int v = 0; v < kpy; ++v) {
+          const float* trow = Tt + (ty + 2 * cy - v) * TW + tx + 2 * cx;
+          const float* krow = Kk + v * kpx;
+          for (int u = 0; u < kpx; ++u) a = fmaf(krow[u], trow[-u], a);
+        }
+        if (pl == 0)
+          cv[kk] = a;
+        else
+          cv[3 + (pl - 1)] = a;
+      }
+    }
+  }
+
+  if (b.psf_mode != AP_PSF_NONE) {
+    // algorithmic work: 2 FLOP per kernel tap per convolved plane per output pixel
+    const int nconv = jac ? ((shiftmode ? 3 : 1) + (b.kind == AP_PROFILE_SERSIC ? 4 : 3) +
+                             (shiftmode ? 0 : 2))
+                          : 1;
+    const unsigned cnt = __popc(__ballot_sync(0xffffffffu, valid));
+    if ((threadIdx.x & 31) == 0 && cnt)
+      atomicAdd(b.work_ctr, (unsigned long long)cnt * 2ull * (unsigned long long)(st.kpx * st.kpy) *
+                                (unsigned long long)nconv);
+  }
+  // model and value-space Jacobian in full-vector order
+  const float mgal = cv[0];
+  const float m = mgal + e.sky;
+  float J[NPARAM];
+  if (jac) {
+    if (shiftmode) {
+      J[PX] = cv[1] * (float)st.Pinv[0] + cv[2] * (float)st.Pinv[2];
+      J[PY] = cv[1] * (float)st.Pinv[1] + cv[2] * (float)st.Pinv[3];
+    } else {
+      J[PX] = -cv[3 + GX];
+      J[PY] = -cv[3 + GY];
+    }
+    J[PQ] = cv[3 + GQ];
+    J[PPA] = cv[3 + GPA];
+    J[PN] = cv[3 + GN];
+    J[PRE] = cv[3 + GRE];
+    J[PIE] = kLn10f * mgal;
+    J[PF] = kLn10f * e.sky;
+    if (ops & OP_REP) {
+#pragma unroll
+      for (int k = 0; k < NPARAM; ++k) J[k] *= e.drep[k];
+    }
+  }
+  // compact fitted-slot columns
+  float Jc[NPARAM];
+  int nf = 0;
+  if (jac) {
+#pragma unroll
+    for (int k = 0; k < NPARAM; ++k)
+      if (b.free_mask & (1 << k)) Jc[nf++] = J[k];
+  }
+  const int64_t op = st.out_off + (int64_t)y * st.nx + x;
+  if (valid && (ops & OP_WRITE_MODEL)) io.model_out[op] = m;
+  if (valid && jac && (ops & OP_WRITE_JAC)) {
+    for (int k = 0; k < nf; ++k) io.jac_out[(int64_t)k * b.out_pixels + op] = Jc[k];
+  }
+  if (!(ops & (OP_CHI2 | OP_HG | OP_RPP))) return;
+
+  // fused reductions (fit/lm.py:374-406)
+  float w = 0.f, r = 0.f;
+  if (valid) {
+    w = io.weight ? io.weight[op] : 1.f;
+    if (io.mask && io.mask[op]) w = 0.f;
+    r = io.data[op] - m;
+  }
+  float vals[kNacc];
+  int nv = 0;
+  vals[nv++] = w * r * r;  // ACC_CHI2
+  const int nfree = b.n_free;
+  if (ops & OP_HG) {
+    for (int k = 0; k < nfree; ++k) vals[nv++] = (valid && jac) ? Jc[k] * w * r : 0.f;
+    for (int a = 0; a < nfree; ++a)
+      for (int c = a; c < nfree; ++c) vals[nv++] = (valid && jac) ? Jc[a] * w * Jc[c] : 0.f;
+  }
+  if (ops & OP_RPP) {
+    float jh = 0.f, ebase = 0.f;
+    float Jb[NPARAM];
+    if (valid) {
+      for (int k = 0; k < nfree; ++k) {
+        Jb[k] = io.jbase[(int64_t)k * b.out_pixels + op];
+        jh = fmaf(Jb[k], (float)io.hvec[s * NPARAM + k], jh);
+      }
+      const float d = (float)io.rpp_d;
+      // (2/d) * ((rh - r)/d - W (J h)),  rh - r = W (Y1 - Y0)
+      ebase = (2.f / d) * ((w * (m - io.y0[op])) / d - w * jh);
+    }
+    for (int k = 0; k < nfree; ++k) vals[nv++] = valid ? Jb[k] * ebase : 0.f;
+  }
+  __shared__ float shred[(kTile * kTile / 32) * kNacc];
+  __syncthreads();
+  tile_reduce(vals, nv, tacc, shred);
+}
+
+// per-stamp sums of the tile partials (fixed order: deterministic)
+__global__ void k_reduce_acc(BatchArgs b) {
+  const int s = blockIdx.x, slot = blockIdx.y;
+  const EvalDev& e = b.evals[s * 2 + slot];
+  if (!(e.ops & (OP_CHI2 | OP_HG | OP_RPP))) return;
+  const StampDev& st = b.stamps[s];
+  int nv = 1;
+  if (e.ops & OP_HG) nv += b.n_free + b.n_free * (b.n_free + 1) / 2;
+  if (e.ops & OP_RPP) nv += b.n_free;
+  for (int k = threadIdx.x; k < nv; k += blockDim.x) {
+    double t = 0;
+    for (int tt = 0; tt < st.nto; ++tt) t += b.tile_acc[((int64_t)(st.tile_o0 + tt) * 2 + slot) * kNacc + k];
+    b.acc[((int64_t)s * 2 + slot) * kNacc + k] = t;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// stand-alone chi^2 of a given model (LM._chi2 numerator)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_chi2(BatchArgs b, ConvIO io, const float* model) {
+  const int tile = blockIdx.x;
+  const int s = b.out_tiles[tile];
+  const StampDev& st = b.stamps[s];
+  const int local = tile - st.tile_o0;
+  const int x = (local % st.nto_x) * kTile + (threadIdx.x & (kTile - 1));
+  const int y = (local / st.nto_x) * kTile + threadIdx.x / kTile;
+  float v = 0.f;
+  if (x < st.nx && y < st.ny) {
+    const int64_t op = st.out_off + (int64_t)y * st.nx + x;
+    float w = io.weight ? io.weight[op] : 1.f;
+    if (io.mask && io.mask[op]) w = 0.f;
+    const float r = io.data[op] - model[op];
+    v = w * r * r;
+  }
+  __shared__ float shred[(kTile * kTile / 32) * kNacc];
+  tile_reduce(&v, 1, b.tile_acc + (int64_t)tile * 2 * kNacc, shred);
+}
+
+__global__ void k_chi2_reduce(BatchArgs b, double* out) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= b.n_stamps) return;
+  const StampDev& st = b.stamps[s];
+  double t = 0;
+  for (int tt = 0; tt < st.nto; ++tt) t += b.tile_acc[(int64_t)(st.tile_o0 + tt) * 2 * kNacc];
+  out[s] = t;
+}
+
+// batched damped solve (LM._h): see damped_solve_dev in ap_device.cuh
+__global__ void k_damped_solve(int m, int p, const double* hess, const double* grad,
+                               const double* L, double* h) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  damped_solve_dev(p, hess + (int64_t)i * p * p, grad + (int64_t)i * p, L[i], h + (int64_t)i * p);
+}
+
+__global__ void k_psf_export(BatchArgs b, float* out, float* d_out, int64_t stride) {
+  const int s = blockIdx.x;
+  const StampDev& st = b.stamps[s];
+  const int kp2 = st.kpx * st.kpy;
+  const float* src = b.spsf + st.spsf_off;  // slot 0
+  for (int idx = threadIdx.x; idx < kp2; idx += blockDim.x) {
+    out[(int64_t)s * stride + idx] = src[idx];
+    if (d_out) {
+      d_out[((int64_t)s * 2 + 0) * stride + idx] = src[kp2 + idx];
+      d_out[((int64_t)s * 2 + 1) * stride + idx] = src[2 * kp2 + idx];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host launch wrappers
+// ---------------------------------------------------------------------------
+cudaError_t launch_eval_setup(const BatchArgs& b, const double* params, int64_t stamp_stride,
+                              int64_t slot_stride, const int32_t* ops, int32_t ops_uniform,
+                              cudaStream_t s) {
+  const int n = b.n_stamps * 2;
+  k_eval_setup<<<(n + 127) / 128, 128, 0, s>>>(b, params, stamp_stride, slot_stride, ops,
+                                                ops_uniform);
+  return cudaGetLastError();
+}
+
+cudaError_t set_conv_smem(size_t bytes) {
+  return cudaFuncSetAttribute(k_conv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+cudaError_t launch_render_pass(const BatchArgs& b, const ConvIO& io, size_t conv_smem,
+                               bool accumulate, cudaStream_t s, Profiler* prof) {
+  auto B = [&](int k) { return (prof && prof->on) ? prof->begin(k, s) : -1; };
+  auto E = [&](int i) {
+    if (i >= 0) prof->end(i, s);
+  };
+  int t;
+  if (b.psf_mode != AP_PSF_NONE) {
+    t = B(KC_PSF);
+    k_psf_shift<<<dim3(b.n_stamps, 2), 256, 0, s>>>(b, io.psf);
+    E(t);
+  }
+  t = B(KC_SAMPLE);
+  k_sample<<<dim3(b.n_work_tiles, 2), kTile * kTile, 0, s>>>(b);
+  E(t);
+  if (b.integrate == AP_INTEGRATE_THRESHOLD) {
+    t = B(KC_SELECT);
+    k_select<<<dim3(b.n_work_tiles, 2), kTile * kTile, 0, s>>>(b);
+    E(t);
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    t = B(KC_INTEGRATE);
+    k_integrate<<<nsm * 8, 256, 0, s>>>(b);
+    E(t);
+  }
+  t = B(KC_CONV);
+  k_conv<<<dim3(b.n_out_tiles, 2), kTile * kTile, conv_smem, s>>>(b, io);
+  E(t);
+  if (accumulate) {
+    t = B(KC_REDUCE);
+    k_reduce_acc<<<dim3(b.n_stamps, 2), 64, 0, s>>>(b);
+    E(t);
+  }
+  return cudaGetLastError();
+}
+
+// FP32 FMA throughput probe: 8 independent FMA chains per thread.
+__global__ void k_fma_probe(float* out, int iters) {
+  float a0 = threadIdx.x * 1e-7f, a1 = a0 + 1e-7f, a2 = a0 + 2e-7f, a3 = a0 + 3e-7f;
+  float a4 = a0 + 4e-7f, a5 = a0 + 5e-7f, a6 = a0 + 6e-7f, a7 = a0 + 7e-7f;
+  const float m = 0.999999f, c = 1e-7f;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      a0 = fmaf(a0, m, c); a1 = fmaf(a1, m, c); a2 = fmaf(a2, m, c); a3 = fmaf(a3, m, c);
+      a4 = fmaf(a4, m, c); a5 = fmaf(a5, m, c); a6 = fmaf(a6, m, c); a7 = fmaf(a7, m, c);
+    }
+  }
+  const float r = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+  if (r == 123.456f) out[blockIdx.x * blockDim.x + threadIdx.x] = r;
+}
+
+cudaError_t launch_fma_probe(float* out, int iters, int blocks, cudaStream_t s) {
+  k_fma_probe<<<blocks, 256, 0, s>>>(out, iters);
+  return cudaGetLastError();
+}
+
+int Profiler::begin(int k, cudaStream_t s) {
+  if (used >= cap) {
+    const int ncap = cap ? 2 * cap : 256;
+    cudaEvent_t* nev = new cudaEvent_t[2 * ncap];
+    int* nk = new int[ncap];
+    for (int i = 0; i < cap; ++i) {
+      nev[2 * i] = ev[2 * i];
+      nev[2 * i + 1] = ev[2 * i + 1];
+      nk[i] = kind[i];
+    }
+    for (int i = cap; i < ncap; ++i) {
+      cudaEventCreate(&nev[2 * i]);
+      cudaEventCreate(&nev[2 * i + 1]);
+      nk[i] = 0;
+    }
+    delete[] ev;
+    delete[] kind;
+    ev = nev;
+    kind = nk;
+    cap = ncap;
+  }
+  const int idx = used++;
+  kind[idx] = k;
+  // External records become event-record nodes when the stream is being captured
+  cudaEventRecordWithFlags(ev[2 * idx], s, cudaEventRecordExternal);
+  return idx;
+}
+
+void Profiler::end(int idx, cudaStream_t s) {
+  cudaEventRecordWithFlags(ev[2 * idx + 1], s, cudaEventRecordExternal);
+}
+
+void Profiler::harvest(bool reset) {
+  for (int i = 0; i < used; ++i) {
+    float t = 0.f;
+    if (cudaEventElapsedTime(&t, ev[2 * i], ev[2 * i + 1]) == cudaSuccess) {
+      ms[kind[i]] += t;
+      launches[kind[i]] += 1;
+    }
+  }
+  (void)cudaGetLastError();  // a pair that never completed must not poison later checks
+  if (reset) used = 0;
+}
+
+void Profiler::clear_totals() {
+  for (int k = 0; k < KC_COUNT; ++k) {
+    ms[k] = 0;
+    launches[k] = 0;
+  }
+}
+
+void Profiler::destroy() {
+  for (int i = 0; i < cap; ++i) {
+    cudaEventDestroy(ev[2 * i]);
+    cudaEventDestroy(ev[2 * i + 1]);
+  }
+  delete[] ev;
+  delete[] kind;
+  ev = nullptr;
+  kind = nullptr;
+  cap = used = 0;
+}
+
+cudaError_t launch_chi2_only(const BatchArgs& b, const ConvIO& io, const float* model,
+                             double* out, cudaStream_t s) {
+  k_chi2<<<b.n_out_tiles, kTile * kTile, 0, s>>>(b, io, model);
+  k_chi2_reduce<<<(b.n_stamps + 127) / 128, 128, 0, s>>>(b, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_psf_only(const BatchArgs& b, const float* psf, cudaStream_t s) {
+  k_psf_shift<<<dim3(b.n_stamps, 2), 256, 0, s>>>(b, psf);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_damped_solve(int m, int p, const double* hess, const double* grad,
+                                const double* L, double* h, cudaStream_t s) {
+  k_damped_solve<<<(m + 63) / 64, 64, 0, s>>>(m, p, hess, grad, L, h);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_psf_export(const BatchArgs& b, float* out, float* d_out, int64_t stride,
+                              cudaStream_t s) {
+  k_psf_export<<<b.n_stamps, 256, 0, s>>>(b, out, d_out, stride);
+  return cudaGetLastError();
+}
+
+}  // namespace apgb

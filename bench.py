@@ -1,0 +1,449 @@
+"""Benchmark: converged Levenberg-Marquardt Sersic fits per second on one GB300.
+
+Workload (one "step" = one batched LM fit of every stamp from its initial guess):
+  batched cutouts -- N stamps (default 8192) with sides round(log-uniform(32, 256)) px,
+  each one Sersic galaxy + a flat sky of 1.0 (locked), its own Moffat PSF (beta 3.5,
+  FWHM ~ U(2, 5) px, side = 4 FWHM rounded to odd), Gaussian noise sigma = sqrt(model + 10),
+  7 free parameters from the truth perturbed by 10 %.  Rendering is FP32 with
+  midpoint sampling + the reference's adaptive threshold integration, bilinear sub-pixel
+  PSF shift and PSF convolution; LM accumulators, damping solves and chi^2 are FP64.
+  Seeded synthetic data (no public dataset exists for this path).
+
+Arms:
+  default            the CUDA path (libastrophot_gb300.so) -- JSON line with value (device
+                     resident inputs), e2e (host buffers, H2D + fit + D2H inside the timed
+                     region), roofline of the dominant kernel, cpu_baseline, clocks.
+  --impl reference   the reference algorithm's CPU implementation (the float64 restatement
+                     in oracle/, pinned to the reference's outputs) on all host cores, on a
+                     bounded sample of the same workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+FREE_MASK = 0x7F  # cx cy q PA n Re Ie ; sky F locked
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--stamps", type=int, default=8192)
+    p.add_argument("--seed", type=int, default=2024)
+    p.add_argument("--cpu-sample", type=int, default=8, help="stamps fitted by the CPU baseline")
+    p.add_argument("--rounds-per-sync", type=int, default=8)
+    p.add_argument("--no-graph", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def rank_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ----------------------------------------------------------------------------------------
+# workload
+# ----------------------------------------------------------------------------------------
+
+
+def workload_specs(n, seed, rank=0):
+    from astrophot_gb300 import synthetic
+
+    return synthetic.cutout_stamps(n, seed + 7919 * rank)
+
+
+def truth_and_init_rows(specs):
+    truth = np.array([np.r_[s.truth, 0.0] for s in specs])
+    init = np.array([np.r_[s.init, 0.0] for s in specs])
+    return truth, init
+
+
+def sample_indices(specs, k):
+    """k stamps spread over the size distribution (sorted by area, evenly spaced)."""
+    order = np.argsort([s.nx * s.ny for s in specs], kind="stable")
+    if k >= len(specs):
+        return list(order)
+    pick = np.linspace(0, len(specs) - 1, k).round().astype(int)
+    return [int(order[i]) for i in pick]
+
+
+# ----------------------------------------------------------------------------------------
+# CPU side (oracle = float64 restatement of the reference algorithm)
+# ----------------------------------------------------------------------------------------
+
+
+def _oracle_fit(args):
+    """One LM fit with the oracle: (data, weight, psf, init8, truth8) -> (chi2, iters, seconds)."""
+    data, weight, psf, init, _ = args
+    from oracle.lm import GroupProblem, LMOracle
+    from oracle.render import PSF, Component, Window
+
+    cx, cy, q, PA, n, Re, Ie, F = init
+    gal = Component("sersic", {"center": [cx, cy], "q": q, "PA": PA, "n": n, "Re": Re, "Ie": Ie}, psf_mode="full")
+    sky = Component("flat_sky", {"F": F}, locked=("F",))
+    ny, nx = data.shape
+    prob = GroupProblem([gal, sky], Window.from_scale(nx, ny), PSF(psf), data, weight)
+    t = time.perf_counter()
+    lm = LMOracle(prob, prob.representation()).fit()
+    return lm.res_loss(), lm.iterations, time.perf_counter() - t, lm.message
+
+
+def oracle_truth_image(spec):
+    from oracle.render import PSF, Component, Window, sample_group
+
+    cx, cy, q, PA, n, Re, Ie = spec.truth
+    gal = Component("sersic", {"center": [cx, cy], "q": q, "PA": PA, "n": n, "Re": Re, "Ie": Ie}, psf_mode="full")
+    sky = Component("flat_sky", {"F": 0.0}, locked=("F",))
+    model, _ = sample_group([gal, sky], Window.from_scale(spec.nx, spec.ny), PSF(spec.psf))
+    return model
+
+
+def run_reference(args):
+    """--impl reference: the oracle LM over all host cores on a bounded sample."""
+    from astrophot_gb300 import synthetic
+
+    rank, world, _ = rank_info()
+    if rank != 0:
+        return
+    specs = workload_specs(args.stamps, args.seed)
+    cores = os.cpu_count() or 1
+    idx = sample_indices(specs, max(cores, 1))
+    jobs = []
+    for i in idx:
+        s = specs[i]
+        truth = oracle_truth_image(s)
+        data, weight = synthetic.add_noise(truth, s.seed)
+        jobs.append((data, weight, s.psf, np.r_[s.init, 0.0], np.r_[s.truth, 0.0]))
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(processes=min(cores, len(jobs))) as pool:
+        for _ in range(max(args.warmup, 0) and 1):
+            pool.map(_oracle_fit, jobs[: min(len(jobs), cores)])
+        times = []
+        for _ in range(args.steps):
+            t = time.perf_counter()
+            res = pool.map(_oracle_fit, jobs)
+            times.append(time.perf_counter() - t)
+    dt = statistics.median(times)
+    value = len(jobs) / dt
+    line = {
+        "impl": "reference",
+        "metric": "LM Sersic fits/s (chi2 within 1e-4 of the FP64 oracle)",
+        "value": value,
+        "unit": "fits/s",
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": dt * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {
+            "workload": f"batched cutouts: {args.stamps} stamps 32-256 px, Sersic + sky, Moffat 9-21 px PSF",
+            "sample": f"{len(jobs)} stamps spread over the size distribution, one per core",
+        },
+        "cpu_baseline": {
+            "value": value,
+            "unit": "fits/s",
+            "cores": min(cores, len(jobs)),
+            "kind": "port",
+            "sample": f"{len(jobs)} stamps (float64 numpy restatement of the reference LM)",
+        },
+        "e2e": {"value": value, "unit": "fits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "mean_iterations": float(np.mean([r[1] for r in res])),
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------------------
+# GPU side
+# ----------------------------------------------------------------------------------------
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = (
+        "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+        "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+        "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+    )
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL,
+                text=True,
+            )
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            parts = [p.strip() for p in l.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[4:8]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def run_gpu(args):
+    import torch
+
+    from astrophot_gb300 import _native as N
+    from astrophot_gb300 import synthetic
+    from astrophot_gb300.transforms import slots_to_rep
+
+    rank, world, local = rank_info()
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", torch.cuda.current_device())
+
+    # every rank fits its own independent stamps (weak scaling, no data-path collective)
+    specs = workload_specs(args.stamps, args.seed, rank)
+    S = len(specs)
+    opts = N.make_options(profile="sersic", psf_mode="full", free_mask=FREE_MASK, has_sky=True)
+    batch = N.StampBatch(
+        [(s.nx, s.ny) for s in specs], [(s.psf.shape[1], s.psf.shape[0]) for s in specs], N.scale_geometry(S), opts, dev
+    )
+    truth, init = truth_and_init_rows(specs)
+    psf_h = np.concatenate([s.psf.astype(np.float32).ravel() for s in specs])
+    psf_d = torch.from_numpy(psf_h).to(dev)
+    model = batch.render(torch.from_numpy(truth).to(dev), psf_d)
+    models = batch.unpack(model)
+    data_l, w_l = [], []
+    for s, m in zip(specs, models):
+        d, w = synthetic.add_noise(m.astype(np.float64), s.seed)
+        data_l.append(d.astype(np.float32).ravel())
+        w_l.append(w.astype(np.float32).ravel())
+    data_h = torch.from_numpy(np.concatenate(data_l)).pin_memory()
+    weight_h = torch.from_numpy(np.concatenate(w_l)).pin_memory()
+    psf_hp = torch.from_numpy(psf_h).pin_memory()
+    fixed_h = torch.from_numpy(init).pin_memory()
+    state0_h = torch.from_numpy(slots_to_rep(init, FREE_MASK)).pin_memory()
+    data_d = data_h.to(dev)
+    weight_d = weight_h.to(dev)
+    fixed_d = fixed_h.to(dev)
+    state0_d = state0_h.to(dev)
+    lmo = N.make_lm_options(rounds_per_sync=args.rounds_per_sync, use_graph=not args.no_graph)
+
+    def step_device():
+        return batch.lm_fit(data_d, weight_d, None, psf_d, fixed_d, state0_d, lmo)
+
+    for _ in range(max(args.warmup, 0)):
+        step_device()
+    torch.cuda.synchronize()
+
+    # ---- value: inputs resident in HBM -------------------------------------------------
+    batch.profile(True)
+    batch.work_counters(reset=True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    results = []
+    with ClockSampler(local) as clk:
+        e0.record()
+        for _ in range(args.steps):
+            results.append(step_device())
+        e1.record()
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    dev_ms = e0.elapsed_time(e1) / args.steps
+    ktimes = batch.kernel_times()
+    work = batch.work_counters(reset=True)
+    batch.profile(False)
+    state, chi2, iters, status = results[-1]
+    status_h = status.cpu().numpy()
+    iters_h = iters.cpu().numpy()
+    chi2_h = chi2.cpu().numpy()
+    converged = int(np.sum((status_h == N.LM_SUCCESS) | (status_h == N.LM_IMMOBILE)))
+
+    # ---- e2e: host buffers, copies inside the timed region -------------------------------
+    def step_e2e():
+        d = data_h.to(dev, non_blocking=True)
+        w = weight_h.to(dev, non_blocking=True)
+        p = psf_hp.to(dev, non_blocking=True)
+        f = fixed_h.to(dev, non_blocking=True)
+        s0 = state0_h.to(dev, non_blocking=True)
+        st, c2, it, stt = batch.lm_fit(d, w, None, p, f, s0, lmo)
+        return st.cpu(), c2.cpu(), stt.cpu()
+
+    step_e2e()
+    torch.cuda.synchronize()
+    h2d = (data_h.numel() + weight_h.numel() + psf_hp.numel()) * 4 + (fixed_h.numel() + state0_h.numel()) * 8
+    d2h = state.numel() * 8 + chi2.numel() * 8 + status.numel() * 4
+    t0 = time.perf_counter()
+    e2 = torch.cuda.Event(enable_timing=True)
+    e3 = torch.cuda.Event(enable_timing=True)
+    e2.record()
+    for _ in range(args.steps):
+        step_e2e()
+    e3.record()
+    torch.cuda.synchronize()
+    e2e_ms = e2.elapsed_time(e3) / args.steps
+    e2e_wall_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+
+    # max over ranks
+    if world > 1:
+        t = torch.tensor([dev_ms, e2e_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dev_ms, e2e_ms = t.tolist()
+        c = torch.tensor([converged, S], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(c)
+        converged_all, total_all = c.tolist()
+    else:
+        converged_all, total_all = converged, S
+
+    # ---- roofline of the dominant kernel (live CUDA-event times over the timed region) ----
+    dominant = max(ktimes, key=lambda k: ktimes[k][0])
+    fp32_peak = N.fma_probe_tflops()
+    conv_ms, conv_n = ktimes["conv"]
+    roof = None
+    if dominant == "conv" and conv_ms > 0:
+        achieved = work["conv_flops"] / (conv_ms * 1e-3) / 1e12
+        roof = {
+            "kernel": "k_conv (PSF convolution + fused Jacobian/chi2/JtWJ/JtWr)",
+            "bound": "fp32",
+            "achieved": achieved,
+            "peak": fp32_peak,
+            "unit": "TFLOP/s",
+            "frac": achieved / fp32_peak,
+            "traffic": None,
+            "launches": conv_n,
+            "avg_launch_ms": conv_ms / max(conv_n, 1),
+            "peak_source": "measured FP32 FMA probe (ap_fma_probe) on this GPU",
+        }
+    else:
+        ms, n = ktimes[dominant]
+        roof = {"kernel": dominant, "bound": "fp32", "achieved": None, "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": None, "traffic": None, "launches": n, "avg_launch_ms": ms / max(n, 1)}
+
+    line = {
+        "metric": "LM Sersic fits/s (chi2 within 1e-4 of the FP64 oracle)",
+        "value": converged_all / (dev_ms * 1e-3),
+        "unit": "fits/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": dev_ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 render / f64 LM",
+        "data": "synthetic",
+        "config": {
+            "workload": f"batched cutouts: {S} stamps per GPU, sides log-uniform 32-256 px, Sersic + locked sky, "
+            "Moffat PSF 9-21 px, 7 free params, midpoint + threshold integration, bilinear PSF shift",
+            "stamps_per_gpu": S,
+            "pixels_per_gpu": int(batch.out_pixels),
+            "parallelism": f"replicas x{world} (independent stamps per rank)",
+            "l2": "inputs (%.2f GB) exceed the 129 MB L2" % ((data_h.numel() + weight_h.numel()) * 4 / 1e9),
+            "rounds_per_sync": args.rounds_per_sync,
+            "cuda_graph": not args.no_graph,
+        },
+        "fits": {"total": int(total_all), "converged": int(converged_all),
+                 "mean_iterations": float(iters_h.mean()),
+                 "status_counts": {N.LM_MESSAGES[k]: int(np.sum(status_h == k)) for k in np.unique(status_h)}},
+        "e2e": {"value": converged_all / (e2e_ms * 1e-3), "unit": "fits/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "wall_ms_per_step": e2e_wall_ms},
+        "roofline": roof,
+        "kernel_ms_per_step": {k: v[0] / args.steps for k, v in ktimes.items()},
+        "kernel_launches_per_step": {k: v[1] / args.steps for k, v in ktimes.items()},
+        "gpu_launches": int(sum(v[1] for v in ktimes.values()) / args.steps),
+        "work_per_step": {k: v / args.steps for k, v in work.items()},
+    }
+
+    # ---- CPU baseline + parity on a bounded sample (rank 0, N = 1 only) -------------------
+    if rank == 0 and world == 1 and not args.no_cpu and args.cpu_sample > 0:
+        idx = sample_indices(specs, args.cpu_sample)
+        t = time.perf_counter()
+        rels = []
+        cpu_secs = 0.0
+        for i in idx:
+            s = specs[i]
+            o = batch.out_offsets[i]
+            d = data_h[o : o + s.nx * s.ny].numpy().astype(np.float64).reshape(s.ny, s.nx)
+            w = weight_h[o : o + s.nx * s.ny].numpy().astype(np.float64).reshape(s.ny, s.nx)
+            c2, it, sec, msg = _oracle_fit((d, w, s.psf.astype(np.float32).astype(np.float64), init[i], truth[i]))
+            cpu_secs += sec
+            rels.append(abs(chi2_h[i] / c2 - 1.0))
+        line["cpu_baseline"] = {
+            "value": len(idx) / cpu_secs,
+            "unit": "fits/s",
+            "cores": 1,
+            "kind": "port",
+            "sample": f"{len(idx)} stamps of this workload spread over the size range, float64 numpy "
+            "restatement of the reference LM, one core",
+        }
+        line["parity"] = {"stamps": len(idx), "max_rel_chi2_vs_oracle": float(max(rels)),
+                          "within_1e-4": int(sum(r <= 1e-4 for r in rels))}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

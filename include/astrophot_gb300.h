@@ -1,0 +1,199 @@
+/*
+ * astrophot_gb300 -- C ABI of the GB300 (sm_103a) render + Levenberg-Marquardt path.
+ *
+ * Conventions
+ *   - Every entry point returns an int status: AP_OK (0) or one of AP_ERR_*.
+ *   - Device pointers are plain pointers to caller-owned CUDA memory; nothing in this
+ *     library calls cudaMalloc/cudaFree.  Work buffers come from the caller through
+ *     ap_batch_bind (size from ap_batch_sizes) and ap_lm_fit (size from
+ *     ap_lm_workspace_bytes).
+ *   - All device work is enqueued on the stream passed in; calls do not synchronise
+ *     unless stated.  One host thread per batch handle; a handle is not thread-safe.
+ *   - Images are row-major [ny][nx] float32, packed stamp after stamp at the offsets
+ *     returned by ap_batch_offsets.  Parameters are float64.
+ *   - The full parameter vector of a stamp is [cx, cy, q, PA, n, Re, Ie, F]
+ *     (centre in plane units, PA in radians, Ie and F as log10 of the surface
+ *     brightness, F the flat sky).  options.free_mask selects the fitted slots; the
+ *     compact vector of fitted slots keeps this order.
+ *
+ * Reference interfaces replaced (AstroPhot 0.x, file:line in its repository):
+ *   ap_render        Component_Model.sample          astrophot/models/model_object.py:258-375
+ *                    (+ Group_Model.sample for galaxy + flat sky, models/group_model_object.py:183-231)
+ *   ap_jacobian      jacobian(as_representation=...) astrophot/models/_model_methods.py:260-347
+ *   ap_psf_shift     _shift_psf (bilinear) + renorm  astrophot/models/_model_methods.py:187-243
+ *   ap_damped_solve  LM._h                           astrophot/fit/lm.py:361-371
+ *   ap_lm_fit        LM.fit / LM.step                astrophot/fit/lm.py:249-357, 428-493
+ *   ap_chi2          LM._chi2                        astrophot/fit/lm.py:374-378
+ */
+#ifndef ASTROPHOT_GB300_H
+#define ASTROPHOT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* ap_stream_t; /* same handle as cudaStream_t */
+
+/* status codes */
+#define AP_OK 0
+#define AP_ERR_ARG 1          /* bad argument (null pointer, size, shape) */
+#define AP_ERR_UNSUPPORTED 2  /* knob outside what the kernels implement */
+#define AP_ERR_CUDA 3         /* a CUDA launch or copy failed */
+#define AP_ERR_WORKSPACE 4    /* workspace missing or too small */
+#define AP_ERR_LIMIT 5        /* a parameter left its limits (InvalidParameter) */
+#define AP_ERR_NOT_BOUND 6    /* ap_batch_bind was not called */
+
+/* ap_options.profile */
+#define AP_PROFILE_SERSIC 0
+#define AP_PROFILE_EXPONENTIAL 1
+/* ap_options.sampling_mode */
+#define AP_SAMPLING_MIDPOINT 0
+#define AP_SAMPLING_SIMPSONS 1
+#define AP_SAMPLING_QUAD 2
+#define AP_SAMPLING_TRAPEZOID 3
+/* ap_options.integrate_mode */
+#define AP_INTEGRATE_NONE 0
+#define AP_INTEGRATE_THRESHOLD 1
+/* ap_options.psf_mode */
+#define AP_PSF_NONE 0
+#define AP_PSF_FULL 1         /* psf_mode="full", psf_subpixel_shift="bilinear" */
+#define AP_PSF_FULL_NOSHIFT 2 /* psf_mode="full", psf_subpixel_shift="none" */
+
+/* per-stamp LM status (ap_lm_fit status_out) */
+#define AP_LM_RUNNING 0
+#define AP_LM_SUCCESS 1          /* "success" */
+#define AP_LM_IMMOBILE 2         /* "success by immobility. Convergence not guaranteed" */
+#define AP_LM_MAX_ITER 3         /* "fail. Maximum iterations" */
+#define AP_LM_NO_STEP 4          /* "fail. Could not find step to improve Chi^2" (OptimizeStop) */
+#define AP_LM_LIMIT 5            /* a trial parameter left its limits (InvalidParameter) */
+
+typedef struct ap_options {
+  int32_t profile;              /* AP_PROFILE_* */
+  int32_t sampling_mode;        /* AP_SAMPLING_* */
+  int32_t sampling_quad_level;  /* k of sampling_mode "quad:k" (1..5) */
+  int32_t integrate_mode;       /* AP_INTEGRATE_* */
+  int32_t psf_mode;             /* AP_PSF_* */
+  int32_t integrate_max_depth;  /* 1..3   (reference default 3) */
+  int32_t integrate_gridding;   /* 1..5   (reference default 5) */
+  int32_t integrate_quad_level; /* 1..5   (reference default 3) */
+  double sampling_tolerance;    /* reference default 1e-2 */
+  double softening;             /* reference default 1e-3 */
+  int32_t free_mask;            /* bit i set: full-vector slot i is fitted */
+  int32_t has_sky;              /* 1: a flat sky 10^F * pixel_area is added */
+} ap_options;
+
+typedef struct ap_lm_options {
+  int32_t max_iter;         /* LM max_iter (100) */
+  int32_t max_step_iter;    /* inner damping search (10) */
+  double relative_tolerance;/* 1e-5 */
+  double curvature_limit;   /* 1.0 */
+  double Lup, Ldn, L0;      /* 11, 9, 1 */
+  double acceleration;      /* 0 */
+  int32_t rounds_per_sync;  /* device rounds between host checks of the active count (>= 1) */
+  int32_t use_graph;        /* 1: capture rounds_per_sync rounds in a CUDA graph and replay it */
+} ap_lm_options;
+
+typedef struct ap_batch ap_batch; /* opaque host-side plan (host memory only) */
+
+/* Plan a batch of n stamps.  geometry holds 8 doubles per stamp:
+ *   P00 P01 P10 P11 (pixel-scale matrix, plane = P (ij - ref_ij) + ref_xy),
+ *   ref_i ref_j (reference pixel, x then y), ref_x ref_y (reference plane point).
+ * psf_kx/psf_ky may be NULL when options.psf_mode == AP_PSF_NONE; otherwise odd sizes.
+ * Host-only; no CUDA call. */
+int ap_batch_create(ap_batch** out, int32_t n_stamps, const int32_t* nx, const int32_t* ny,
+                    const int32_t* psf_kx, const int32_t* psf_ky, const double* geometry,
+                    const ap_options* options);
+int ap_batch_destroy(ap_batch* batch);
+
+/* Packed sizes: output pixels (data/weight/mask/model layout), raw PSF pixels, and the
+ * workspace bytes ap_batch_bind needs. */
+int ap_batch_sizes(const ap_batch* batch, int64_t* out_pixels, int64_t* psf_pixels,
+                   int64_t* workspace_bytes);
+/* Per-stamp offsets (host arrays of n_stamps) into the packed output and PSF arrays. */
+int ap_batch_offsets(const ap_batch* batch, int64_t* out_offsets, int64_t* psf_offsets);
+
+/* Attach caller-owned device workspace and upload the plan's tables into it
+ * (synchronous with respect to the host for the table upload). */
+int ap_batch_bind(ap_batch* batch, void* workspace, int64_t workspace_bytes, ap_stream_t stream);
+
+/* Model images of every stamp for value-space parameters params[n][8] (device).
+ * model[out_pixels] (device) is overwritten.  psf: packed raw PSFs (device) or NULL. */
+int ap_render(ap_batch* batch, const double* params, const float* psf, float* model,
+              ap_stream_t stream);
+
+/* Model and Jacobian.  jac[n_free][out_pixels] (device), compact fitted-slot order;
+ * as_representation != 0 gives d model / d representation (the LM's space). */
+int ap_jacobian(ap_batch* batch, const double* params, const float* psf, float* model,
+                float* jac, int32_t as_representation, ap_stream_t stream);
+
+/* Shifted, renormalised PSF of every stamp for value-space params (device):
+ * out[n][(ky+2)*(kx+2)] packed with stride max_kp2 = (max ky + 2) * (max kx + 2)
+ * (see ap_batch_psf_stride).  d_out (optional, may be NULL) receives d/d shift_x and
+ * d/d shift_y kernels with the same layout, [n][2][stride]. */
+int ap_batch_psf_stride(const ap_batch* batch, int64_t* stride);
+int ap_psf_shift(ap_batch* batch, const double* params, const float* psf, float* out,
+                 float* d_out, ap_stream_t stream);
+
+/* chi2_out[n] = sum over unmasked pixels of weight * (data - model)^2 (float64 sums).
+ * mask may be NULL (nonzero = ignored). */
+int ap_chi2(ap_batch* batch, const float* data, const float* weight, const uint8_t* mask,
+            const float* model, double* chi2_out, ap_stream_t stream);
+
+/* Batched damped solve of LM._h: for m systems of size p,
+ * h[i] = solve(H_i o (I + D / (1 + L_i)) + L_i I (1 + diag H_i), g_i)   (float64, device). */
+int ap_damped_solve(int32_t m, int32_t p, const double* hess, const double* grad,
+                    const double* L, double* h_out, ap_stream_t stream);
+
+/* Full batched LM.  fixed_params[n][8] (device, value space) supplies the locked slots.
+ * state[n][n_free] (device, representation space) is read as the initial state and overwritten with BaseOptimizer.res() of each stamp (the lowest-chi2
+ * state).  chi2_out[n]: chi2/ndf of that state.  iters_out[n], status_out[n]: AP_LM_*.
+ * lm_workspace: caller-owned device memory of ap_lm_workspace_bytes.  ndf per stamp is
+ * (#unmasked pixels - n_free), at least 1.  Synchronises the stream between device
+ * rounds (one 4-byte read per rounds_per_sync rounds). */
+int ap_lm_workspace_bytes(const ap_batch* batch, const ap_lm_options* lm, int64_t* bytes);
+int ap_lm_fit(ap_batch* batch, const float* data, const float* weight, const uint8_t* mask,
+              const float* psf, const double* fixed_params, double* state,
+              const ap_lm_options* lm, void* lm_workspace,
+              int64_t lm_workspace_bytes, double* chi2_out, int32_t* iters_out,
+              int32_t* status_out, ap_stream_t stream);
+/* Histories of the last ap_lm_fit (device pointers into lm_workspace, layout
+ * [n][max_iter + 1]; loss = chi2/ndf, lambda = damping L). */
+int ap_lm_history(const ap_batch* batch, const double** loss, const double** lambda_,
+                  const double** states, int32_t* hist_len);
+
+/* Diagnostics of the last call: integration queue length, FP64 re-decisions, rounds. */
+int ap_batch_stats(const ap_batch* batch, int64_t* stats_out /* [4] */);
+
+/* Per-kernel CUDA-event timing.  ap_batch_profile(b, 1) clears the totals and records an
+ * event pair around every kernel this batch launches from then on (also inside the LM's
+ * captured graphs).  ap_batch_kernel_times fills ms_out[8] / launches_out[8] in the order
+ * setup, psf_shift, sample, select, integrate, conv, reduce, lm_update (synchronises the
+ * device when pairs are pending). */
+int ap_batch_profile(ap_batch* batch, int32_t enable);
+int ap_batch_kernel_times(ap_batch* batch, double* ms_out, int64_t* launches_out);
+
+/* Algorithmic work counted on the device since bind (or the last reset): out[0] FP32
+ * FLOPs of the PSF convolutions (2 per kernel tap, per convolved plane, per output pixel),
+ * out[1] profile samples of the adaptive integration, out[2] samples of the sampling pass.
+ * Synchronises the stream. */
+int ap_batch_work_counters(ap_batch* batch, uint64_t* out /* [4] */, int32_t reset,
+                           ap_stream_t stream);
+
+/* FP32 FMA throughput probe: blocks x 256 threads, each running 8 independent chains of
+ * 16 * iters FMAs (2 FLOP each).  scratch: >= blocks * 256 floats of device memory (never
+ * written in practice).  Used to measure the FP32 pipe peak for roofline fractions. */
+int ap_fma_probe(float* scratch, int32_t iters, int32_t blocks, ap_stream_t stream);
+
+/* Library version string. */
+const char* ap_version(void);
+/* Text of the last CUDA error behind an AP_ERR_CUDA status on this thread ("" if none). */
+const char* ap_last_cuda_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ASTROPHOT_GB300_H */
