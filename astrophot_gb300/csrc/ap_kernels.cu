@@ -765,10 +765,11 @@ __global__ void __launch_bounds__(256) k_conv(BatchArgs b, ConvIO io) {
   if (!(ops & (OP_CHI2 | OP_HG | OP_RPP))) return;
 
   // fused reductions (fit/lm.py:374-406)
+  // masked pixels (mask != 0) are left out entirely: their data may be anything, NaN included
   float w = 0.f, r = 0.f;
-  if (valid) {
+  const bool use = valid && !(io.mask && io.mask[op]);
+  if (use) {
     w = io.weight ? io.weight[op] : 1.f;
-    if (io.mask && io.mask[op]) w = 0.f;
     r = io.data[op] - m;
   }
   float vals[kNacc];
@@ -776,14 +777,14 @@ __global__ void __launch_bounds__(256) k_conv(BatchArgs b, ConvIO io) {
   vals[nv++] = w * r * r;  // ACC_CHI2
   const int nfree = b.n_free;
   if (ops & OP_HG) {
-    for (int k = 0; k < nfree; ++k) vals[nv++] = (valid && jac) ? Jc[k] * w * r : 0.f;
+    for (int k = 0; k < nfree; ++k) vals[nv++] = (use && jac) ? Jc[k] * w * r : 0.f;
     for (int a = 0; a < nfree; ++a)
-      for (int c = a; c < nfree; ++c) vals[nv++] = (valid && jac) ? Jc[a] * w * Jc[c] : 0.f;
+      for (int c = a; c < nfree; ++c) vals[nv++] = (use && jac) ? Jc[a] * w * Jc[c] : 0.f;
   }
   if (ops & OP_RPP) {
     float jh = 0.f, ebase = 0.f;
     float Jb[NPARAM];
-    if (valid) {
+    if (use) {
       for (int k = 0; k < nfree; ++k) {
         Jb[k] = io.jbase[(int64_t)k * b.out_pixels + op];
         jh = fmaf(Jb[k], (float)io.hvec[s * NPARAM + k], jh);
@@ -792,7 +793,7 @@ __global__ void __launch_bounds__(256) k_conv(BatchArgs b, ConvIO io) {
       // (2/d) * ((rh - r)/d - W (J h)),  rh - r = W (Y1 - Y0)
       ebase = (2.f / d) * ((w * (m - io.y0[op])) / d - w * jh);
     }
-    for (int k = 0; k < nfree; ++k) vals[nv++] = valid ? Jb[k] * ebase : 0.f;
+    for (int k = 0; k < nfree; ++k) vals[nv++] = use ? Jb[k] * ebase : 0.f;
   }
   __shared__ float shred[(kTile * kTile / 32) * kNacc];
   __syncthreads();
@@ -828,10 +829,11 @@ __global__ void __launch_bounds__(256) k_chi2(BatchArgs b, ConvIO io, const floa
   float v = 0.f;
   if (x < st.nx && y < st.ny) {
     const int64_t op = st.out_off + (int64_t)y * st.nx + x;
-    float w = io.weight ? io.weight[op] : 1.f;
-    if (io.mask && io.mask[op]) w = 0.f;
-    const float r = io.data[op] - model[op];
-    v = w * r * r;
+    if (!(io.mask && io.mask[op])) {
+      const float w = io.weight ? io.weight[op] : 1.f;
+      const float r = io.data[op] - model[op];
+      v = w * r * r;
+    }
   }
   __shared__ float shred[(kTile * kTile / 32) * kNacc];
   tile_reduce(&v, 1, b.tile_acc + (int64_t)tile * 2 * kNacc, shred);
