@@ -115,6 +115,7 @@ EXPORTS = [
     ("ap_batch_work_counters", [_P, ctypes.POINTER(ctypes.c_uint64), _I32, _P]),
     ("ap_fma_probe", [_P, _I32, _I32, _P]),
     ("ap_batch_stats", [_P, _PI64]),
+    ("ap_render_noalloc", [_I32, _I32, _I32, _I32, _PD, ctypes.POINTER(ApOptions), _P, _P, _P, _P]),
     ("ap_version", []),
     ("ap_last_cuda_error", []),
 ]

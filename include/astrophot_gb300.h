@@ -187,6 +187,22 @@ int ap_batch_work_counters(ap_batch* batch, uint64_t* out /* [4] */, int32_t res
  * written in practice).  Used to measure the FP32 pipe peak for roofline fractions. */
 int ap_fma_probe(float* scratch, int32_t iters, int32_t blocks, ap_stream_t stream);
 
+/* Render of one stamp for callers that cannot allocate device memory (a host that owns
+ * the whole device memory pool, a plugin without access to its allocator, a pipeline that
+ * must not stall on an allocation).  No counterpart in the reference: it is the
+ * ap_render of a single stamp with its scratch in a fixed 8 MiB array inside this library
+ * instead of a caller workspace.  geometry / options are host pointers (8 doubles as in
+ * ap_batch_create); params[8] (value space), psf[psf_ky * psf_kx] (NULL without a PSF) and
+ * model[ny * nx] are device pointers.  Working windows that need more than
+ * AP_NOALLOC_SCRATCH_BYTES of scratch (about 90,000 pixels, e.g. 256 x 256 with a 21 x 21
+ * PSF) are rejected with AP_ERR_WORKSPACE.  The first call on each device resolves the
+ * array's address; make it before any stream capture.  All calls on a device share the
+ * array, so calls that overlap on the GPU race.  Calls no cudaMalloc / cudaFree. */
+#define AP_NOALLOC_SCRATCH_BYTES ((size_t)8 << 20)
+int ap_render_noalloc(int32_t nx, int32_t ny, int32_t psf_kx, int32_t psf_ky,
+                      const double* geometry, const ap_options* options, const double* params,
+                      const float* psf, float* model, ap_stream_t stream);
+
 /* Library version string. */
 const char* ap_version(void);
 /* Text of the last CUDA error behind an AP_ERR_CUDA status on this thread ("" if none). */
