@@ -444,9 +444,10 @@ class StampBatch:
         return {"conv_flops": out[0], "integrate_samples": out[1], "sample_samples": out[2]}
 
     def stats(self):
-        out = (ctypes.c_int64 * 4)()
+        out = (ctypes.c_int64 * 5)()
         check(self.lib.ap_batch_stats(self.handle, out), "stats")
-        return {"queue": out[0], "fp64_redecisions": out[1], "overflow": out[2], "rounds": out[3]}
+        return {"queue": out[0], "fp64_redecisions": out[1], "overflow": out[2], "rounds": out[3],
+                "fp64_integrate": out[4]}
 
 
 def fma_probe_tflops(iters=4096, blocks=None) -> float:

@@ -17,7 +17,7 @@ constexpr int64_t kAlign = 256;
 int64_t align_up(int64_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
 
 struct Layout {
-  int64_t stamps, evals, work_tiles, out_tiles, tables, work, aux, spsf, queue, counters,
+  int64_t stamps, evals, work_tiles, out_tiles, tables, work, aux, spsf, queue, recheck, counters,
       work_ctr, mean_acc, tile_acc, acc, total;
 };
 
@@ -235,8 +235,8 @@ int ap_batch_create(ap_batch** out, int32_t n, const int32_t* nx, const int32_t*
     b->max_kp2 = std::max(b->max_kp2, kp2);
     st.ntw_x = (st.wnx + kTile - 1) / kTile;
     st.ntw = st.ntw_x * ((st.wny + kTile - 1) / kTile);
-    st.nto_x = (st.nx + kTile - 1) / kTile;
-    st.nto = st.nto_x * ((st.ny + kTile - 1) / kTile);
+    st.nto_x = (st.nx + kOutTileX - 1) / kOutTileX;
+    st.nto = st.nto_x * ((st.ny + kOutTileY - 1) / kOutTileY);
     st.tile_w0 = tw;
     st.tile_o0 = to;
     if ((int64_t)tw + st.ntw > (int64_t)INT32_MAX / 2 || (int64_t)to + st.nto > (int64_t)INT32_MAX / 2) {
@@ -248,8 +248,7 @@ int ap_batch_create(ap_batch** out, int32_t n, const int32_t* nx, const int32_t*
     tw += st.ntw;
     to += st.nto;
     if (psf) {
-      const size_t need = sizeof(float) * (3 * (size_t)kp2 +
-                                           (size_t)(kTile + st.kpx - 1) * (kTile + st.kpy - 1));
+      const size_t need = conv_smem_bytes(st.kpx, st.kpy);
       smem = std::max(smem, need);
     }
     if ((int64_t)st.wnx * st.wny >= (int64_t)1 << 31) {
@@ -341,6 +340,7 @@ int ap_batch_create(ap_batch** out, int32_t n, const int32_t* nx, const int32_t*
   L.aux = take(sizeof(float) * 2 * 2 * b->work_pixels);
   L.spsf = take(sizeof(float) * std::max<int64_t>(b->spsf_total, 1));
   L.queue = take(sizeof(int64_t) * 2 * b->work_pixels);
+  L.recheck = take(sizeof(int64_t) * 2 * b->work_pixels);
   L.counters = take(sizeof(uint32_t) * 16);
   L.work_ctr = take(sizeof(unsigned long long) * 4);
   L.mean_acc = take(sizeof(double) * 2 * (int64_t)n);
@@ -418,6 +418,7 @@ int ap_batch_bind(ap_batch* b, void* workspace, int64_t bytes, ap_stream_t strea
   A.aux = (float*)(ws + L.aux);
   A.spsf = (float*)(ws + L.spsf);
   A.queue = (int64_t*)(ws + L.queue);
+  A.recheck = (int64_t*)(ws + L.recheck);
   A.counters = (uint32_t*)(ws + L.counters);
   A.work_ctr = (unsigned long long*)(ws + L.work_ctr);
   A.mean_acc = (double*)(ws + L.mean_acc);
@@ -723,7 +724,7 @@ int ap_fma_probe(float* scratch, int32_t iters, int32_t blocks, ap_stream_t stre
 
 int ap_batch_stats(const ap_batch* b, int64_t* stats_out) {
   if (!b || !stats_out) return AP_ERR_ARG;
-  uint32_t c[4] = {0, 0, 0, 0};
+  uint32_t c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   if (b->bound) {
     if (cudaMemcpy(c, b->args.counters, sizeof(c), cudaMemcpyDeviceToHost) != cudaSuccess)
       return AP_ERR_CUDA;
@@ -732,6 +733,7 @@ int ap_batch_stats(const ap_batch* b, int64_t* stats_out) {
   stats_out[1] = c[2];
   stats_out[2] = c[3];
   stats_out[3] = b->stats[3];
+  stats_out[4] = c[6];
   return AP_OK;
 }
 

@@ -24,7 +24,12 @@ namespace apgb {
 constexpr int kMaxQuad = 5;   // quad levels <= 5  (quad_level^2 <= 32 lanes)
 constexpr int kMaxGrid = 5;   // gridding <= 5     (gridding^2 <= 32 lanes)
 constexpr int kMaxDepth = 3;  // integrate_max_depth <= 3
-constexpr int kTile = 16;     // 16 x 16 pixel tiles
+constexpr int kTile = 16;     // 16 x 16 working-pixel tiles (sampling / selection)
+constexpr int kOutTileX = 32; // output tiles of the convolve/accumulate pass: 32 x 16 pixels,
+constexpr int kOutTileY = 16; // 128 threads, each thread 4 consecutive rows of one column
+constexpr int kConvRows = 4;
+constexpr int kConvThreads = kOutTileX * kOutTileY / kConvRows;
+constexpr int kConvMaxKP = 29; // square kernels up to this size use the register-blocked path
 constexpr int kNumPlanes = 7; // deep + 6 partial planes
 constexpr int kNacc = 56;     // per (stamp, slot) accumulator doubles
 constexpr float kLn10f = 2.302585092994046f;
@@ -123,8 +128,10 @@ struct BatchArgs {
   float* work;                // [2][kNumPlanes][work_pixels]
   float* aux;                 // [2][2][work_pixels]: reference sub-sample, FP32 error bound of deep
   float* spsf;                // kernels
-  int64_t* queue;             // [2 * work_pixels]
-  uint32_t* counters;         // [0] queue len, [1] queue head, [2] fp64 re-decisions, [3] errors, [4] active
+  int64_t* queue;             // [2 * work_pixels] pixels to integrate
+  int64_t* recheck;           // [2 * work_pixels] pixels whose selection needs float64
+  uint32_t* counters;         // [0] queue len, [1] queue head, [2] fp64 re-decisions (select),
+                              // [3] errors, [4] active, [5] recheck len, [6] fp64 (integrate)
   unsigned long long* work_ctr;  // [0] convolution FLOPs, [1] integration samples, [2] sampling samples
   double* mean_acc;           // [n_stamps][2]
   double* tile_acc;           // [n_out_tiles][2][kNacc]
@@ -145,6 +152,12 @@ struct ConvIO {
   double rpp_d;           // OP_RPP: d (0.1)
 };
 
+// dynamic shared memory of the convolve pass for a kpx x kpy kernel: 3 kernels + input tile
+__host__ __device__ inline size_t conv_smem_bytes(int kpx, int kpy) {
+  return sizeof(float) * (3 * (size_t)kpx * kpy +
+                          (size_t)(kOutTileX + kpx - 1) * (kOutTileY + kpy - 1));
+}
+
 __host__ __device__ inline int64_t work_plane(const BatchArgs& b, int slot, int plane) {
   return ((int64_t)slot * kNumPlanes + plane) * b.work_pixels;
 }
@@ -159,12 +172,12 @@ struct Sample {
   float g[NGRAD];
 };
 
-// Relative error bound of one FP32 sample.  u = R/Re carries a few ulp; log2 of it is
-// off by <= ~5e-7 (absolute); t = u^(1/n) then has relative error <= ln2 (5e-7/n + 1e-7 |log2 u|)
-// <= ~1.8e-6 for n >= 0.36, |log2 u| <= 10; the exponent b (t - 1) inherits b t times that,
-// and exp adds a few ulp.  Hence |dI/I| <= 3e-7 + 2e-6 (|b (t - 1)| + b).
+// Relative error bound of one FP32 sample.  u = R/Re carries a few ulp (<= 2e-7); the MUFU
+// log2 adds <= 2.4e-7 absolute, so t = 2^(log2(u)/n) has relative error <= 4e-7 + 5e-7/n;
+// the exponent b (t - 1) inherits b t times that, and the MUFU exp adds <= 3e-7 plus
+// 1.2e-7 per unit of exponent.  Hence |dI/I| <= 4e-7 + (|b (t - 1)| + b) (5e-7 + 5e-7/n).
 __device__ __forceinline__ float sample_rel_err(const EvalDev& e, float arg) {
-  return 3e-7f + 2e-6f * (fabsf(arg) + e.bn);
+  return 4e-7f + (fabsf(arg) + e.bn) * (5e-7f + 5e-7f * e.invn);
 }
 
 template <bool GRAD>
@@ -215,7 +228,7 @@ __device__ __forceinline__ double eval_profile64(const EvalDev& e, int kind, dou
   const double R = sqrt(Xr * Xr + Yr * Yr + e.soft2_64);
   const double amp = e.amp64 * area_scale;
   if (kind == AP_PROFILE_SERSIC) {
-    return amp * exp(-e.bn64 * (pow(R / e.v[PRE], 1.0 / e.v[PN]) - 1.0));
+    return amp * exp(-e.bn64 * (exp(log(R / e.v[PRE]) * (1.0 / e.v[PN])) - 1.0));
   }
   return amp * exp(-e.bn64 * ((R / e.v[PRE]) - 1.0));
 }

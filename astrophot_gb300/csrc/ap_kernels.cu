@@ -63,6 +63,7 @@ __global__ void k_eval_setup(BatchArgs b, const double* params, int64_t stamp_st
   if (t == 0) {
     b.counters[0] = 0;  // queue length
     b.counters[1] = 0;  // queue head
+    b.counters[5] = 0;  // recheck length
   }
   if (t >= b.n_stamps * 2) return;
   const int s = t >> 1, slot = t & 1;
@@ -338,74 +339,138 @@ __global__ void __launch_bounds__(256) k_select(BatchArgs b) {
   const int tile = blockIdx.x, slot = blockIdx.y;
   const int s = b.work_tiles[tile];
   const EvalDev& e = b.evals[s * 2 + slot];
-  if (!e.ops) return;
+  if (!e.ops) return;  // uniform per block
   const StampDev& st = b.stamps[s];
   const int local = tile - st.tile_w0;
   const int i = (local % st.ntw_x) * kTile + (threadIdx.x & (kTile - 1));
   const int j = (local / st.ntw_x) * kTile + threadIdx.x / kTile;
-  if (i >= st.wnx || j >= st.wny) return;
-  float thr, thr_err;
-  double thr64;
-  stamp_threshold(b, st, e, s, slot, thr, thr64, thr_err);
-  const float* d = b.work + work_plane(b, slot, 0) + st.work_off;
-  const float* aux = b.aux + (int64_t)slot * 2 * b.work_pixels + st.work_off;
-  const float* eb = aux + b.work_pixels;
-  const int64_t p = (int64_t)j * st.wnx + i;
-  const float deep = d[p];
-  float err, bound;
-  const bool stencil = (b.sampling == AP_SAMPLING_MIDPOINT || b.sampling == AP_SAMPLING_TRAPEZOID);
-  int ic = 0, jc = 0;
-  if (stencil) {
-    // Laplacian 3x3 'valid' then replicate pad (models/_model_methods.py:87-98)
-    ic = min(max(i, 1), st.wnx - 2);
-    jc = min(max(j, 1), st.wny - 2);
-    const int64_t c = (int64_t)jc * st.wnx + ic;
-    const float u = d[c - st.wnx], l = d[c - 1], m = d[c], r = d[c + 1], dn = d[c + st.wnx];
-    const float lap = u + l + (-4.f) * m + r + dn;
-    const float refimg = deep + lap;
-    err = fabsf(deep - refimg);
-    const float mag = fabsf(u) + fabsf(l) + 4.f * fabsf(m) + fabsf(r) + fabsf(dn);
-    bound = eb[c - st.wnx] + eb[c - 1] + 4.f * eb[c] + eb[c + 1] + eb[c + st.wnx] + eb[p] +
-            8.f * kEps * mag + 4.f * kEps * (fabsf(deep) + fabsf(refimg));
-  } else {
-    const float ref = aux[p];
-    err = fabsf(deep - ref);
-    bound = eb[p] + 4.f * kEps * (fabsf(deep) + fabsf(ref));
-  }
-  bound = 2.f * bound + thr_err;
-  bool sel;
-  if (err > thr + bound) {
-    sel = true;
-  } else if (err < thr - bound) {
-    sel = false;
-  } else {
-    // too close to call in FP32: decide from float64 samples
-    atomicAdd(&b.counters[2], 1u);
-    double err64;
+  const bool valid = (i < st.wnx) && (j < st.wny);
+  bool sel = false, redecided = false;
+  int64_t p = 0;
+  if (valid) {
+    float thr, thr_err;
+    double thr64;
+    stamp_threshold(b, st, e, s, slot, thr, thr64, thr_err);
+    const float* d = b.work + work_plane(b, slot, 0) + st.work_off;
+    const float* aux = b.aux + (int64_t)slot * 2 * b.work_pixels + st.work_off;
+    const float* eb = aux + b.work_pixels;
+    p = (int64_t)j * st.wnx + i;
+    const float deep = d[p];
+    float err, bound;
+    const bool stencil =
+        (b.sampling == AP_SAMPLING_MIDPOINT || b.sampling == AP_SAMPLING_TRAPEZOID);
+    int ic = 0, jc = 0;
     if (stencil) {
-      const double m0 = sample_pixel64(b, st, e, i, j, nullptr);
-      const double u = sample_pixel64(b, st, e, ic, jc - 1, nullptr);
-      const double l = sample_pixel64(b, st, e, ic - 1, jc, nullptr);
-      const double m = sample_pixel64(b, st, e, ic, jc, nullptr);
-      const double r = sample_pixel64(b, st, e, ic + 1, jc, nullptr);
-      const double dn = sample_pixel64(b, st, e, ic, jc + 1, nullptr);
-      const double lap = u + l + (-4.0) * m + r + dn;
-      err64 = fabs(m0 - (m0 + lap));
+      // Laplacian 3x3 'valid' then replicate pad (models/_model_methods.py:87-98)
+      ic = min(max(i, 1), st.wnx - 2);
+      jc = min(max(j, 1), st.wny - 2);
+      const int64_t c = (int64_t)jc * st.wnx + ic;
+      const float u = d[c - st.wnx], l = d[c - 1], m = d[c], r = d[c + 1], dn = d[c + st.wnx];
+      const float lap = u + l + (-4.f) * m + r + dn;
+      const float refimg = deep + lap;
+      err = fabsf(deep - refimg);
+      const float mag = fabsf(u) + fabsf(l) + 4.f * fabsf(m) + fabsf(r) + fabsf(dn);
+      bound = eb[c - st.wnx] + eb[c - 1] + 4.f * eb[c] + eb[c + 1] + eb[c + st.wnx] + eb[p] +
+              8.f * kEps * mag + 4.f * kEps * (fabsf(deep) + fabsf(refimg));
     } else {
-      double ref64 = 0;
-      const double deep64 = sample_pixel64(b, st, e, i, j, &ref64);
-      err64 = fabs(deep64 - ref64);
+      const float ref = aux[p];
+      err = fabsf(deep - ref);
+      bound = eb[p] + 4.f * kEps * (fabsf(deep) + fabsf(ref));
     }
-    sel = err64 > thr64;
-  }
-  if (sel) {
-    const uint32_t slotq = atomicAdd(&b.counters[0], 1u);
-    if ((int64_t)slotq < 2 * b.work_pixels) {
-      b.queue[slotq] = ((int64_t)slot << 62) | ((int64_t)s << 32) | (int64_t)p;
-    } else {
-      atomicOr(&b.counters[3], 1u);
+    bound = 1.5f * bound + thr_err;
+    if (err > thr + bound) {
+      sel = true;
+    } else if (err >= thr - bound) {
+      redecided = true;  // too close to call in FP32: k_recheck decides from float64 samples
     }
   }
+  // warp-aggregated enqueue: one atomic per warp instead of one per pixel
+  const int lane = threadIdx.x & 31;
+  const int64_t entry = ((int64_t)slot << 62) | ((int64_t)s << 32) | (int64_t)p;
+  const unsigned mask = __ballot_sync(0xffffffffu, sel);
+  if (mask) {
+    const int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(&b.counters[0], (unsigned)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (sel) {
+      const uint32_t q = base + __popc(mask & ((1u << lane) - 1u));
+      if ((int64_t)q < 2 * b.work_pixels)
+        b.queue[q] = entry;
+      else
+        atomicOr(&b.counters[3], 1u);
+    }
+  }
+  const unsigned rmask = __ballot_sync(0xffffffffu, redecided);
+  if (rmask) {
+    const int leader = __ffs(rmask) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(&b.counters[5], (unsigned)__popc(rmask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (redecided) {
+      const uint32_t q = base + __popc(rmask & ((1u << lane) - 1u));
+      if ((int64_t)q < 2 * b.work_pixels)
+        b.recheck[q] = entry;
+      else
+        atomicOr(&b.counters[3], 2u);
+    }
+  }
+}
+
+// Selection of the pixels the FP32 bound could not settle, one pixel per thread in float64
+// (the FP64 pipe retires whole-warp instructions, so the work is packed densely here).
+__global__ void __launch_bounds__(256) k_recheck(BatchArgs b) {
+  const uint32_t n = min((uint32_t)b.counters[5], (uint32_t)(2 * b.work_pixels));
+  const int lane = threadIdx.x & 31;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    const uint32_t idx = base + threadIdx.x;
+    bool sel = false;
+    int64_t ent = 0;
+    if (idx < n) {
+      ent = b.recheck[idx];
+      const int slot = (int)(ent >> 62);
+      const int s = (int)((ent >> 32) & 0x3fffffff);
+      const int64_t p = ent & 0xffffffffll;
+      const StampDev& st = b.stamps[s];
+      const EvalDev& e = b.evals[s * 2 + slot];
+      float thr, thr_err;
+      double thr64;
+      stamp_threshold(b, st, e, s, slot, thr, thr64, thr_err);
+      const int i = (int)(p % st.wnx), j = (int)(p / st.wnx);
+      double err64;
+      if (b.sampling == AP_SAMPLING_MIDPOINT || b.sampling == AP_SAMPLING_TRAPEZOID) {
+        const int ic = min(max(i, 1), st.wnx - 2), jc = min(max(j, 1), st.wny - 2);
+        const double m0 = sample_pixel64(b, st, e, i, j, nullptr);
+        const double u = sample_pixel64(b, st, e, ic, jc - 1, nullptr);
+        const double l = sample_pixel64(b, st, e, ic - 1, jc, nullptr);
+        const double m = (ic == i && jc == j) ? m0 : sample_pixel64(b, st, e, ic, jc, nullptr);
+        const double r = sample_pixel64(b, st, e, ic + 1, jc, nullptr);
+        const double dn = sample_pixel64(b, st, e, ic, jc + 1, nullptr);
+        const double lap = u + l + (-4.0) * m + r + dn;
+        err64 = fabs(m0 - (m0 + lap));
+      } else {
+        double ref64 = 0;
+        const double deep64 = sample_pixel64(b, st, e, i, j, &ref64);
+        err64 = fabs(deep64 - ref64);
+      }
+      sel = err64 > thr64;
+    }
+    const unsigned mask = __ballot_sync(0xffffffffu, sel);
+    if (mask) {
+      const int leader = __ffs(mask) - 1;
+      uint32_t qb = 0;
+      if (lane == leader) qb = atomicAdd(&b.counters[0], (unsigned)__popc(mask));
+      qb = __shfl_sync(0xffffffffu, qb, leader);
+      if (sel) {
+        const uint32_t q = qb + __popc(mask & ((1u << lane) - 1u));
+        if ((int64_t)q < 2 * b.work_pixels)
+          b.queue[q] = ent;
+        else
+          atomicOr(&b.counters[3], 1u);
+      }
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&b.counters[2], n);
 }
 
 // ---------------------------------------------------------------------------
@@ -473,17 +538,18 @@ __device__ bool refine64(const BatchArgs& b, const StampDev& st, const EvalDev& 
 __device__ __forceinline__ bool decide(const BatchArgs& b, const StampDev& st, const EvalDev& e,
                                        const QuadResult& r, float thr, double thr64, float ci,
                                        float cj, double ci64, double cj64, float inv_g,
-                                       double inv_g64, float area, double area64) {
+                                       double inv_g64, float area, double area64, int& n64) {
   const float diff = fabsf(r.res - r.ref);
-  const float band = 2.f * r.errb + 4.f * kEps * thr;
+  const float band = 1.5f * r.errb + 4.f * kEps * thr;
   if (diff > thr + band) return true;
   if (diff < thr - band) return false;
-  atomicAdd(&b.counters[2], 1u);
+  ++n64;
   return refine64(b, st, e, ci64, cj64, inv_g64, area64, thr64);
 }
 
 template <bool JAC>
-__device__ void integrate_entry(const BatchArgs& b, int slot, int s, int64_t p, int lane) {
+__device__ void integrate_entry(const BatchArgs& b, int slot, int s, int64_t p, int lane,
+                                unsigned long long& samples, int& n64) {
   const StampDev& st = b.stamps[s];
   const EvalDev& e = b.evals[s * 2 + slot];
   const QuadTables& T = *b.tables;
@@ -537,9 +603,26 @@ __device__ void integrate_entry(const BatchArgs& b, int slot, int s, int64_t p, 
     r1.ref = ref1;
     r1.mag = warp_sum(fa);
     r1.errb = warp_sum(fe) + ref1e + 2.f * Q2 * kEps * (r1.mag + fabsf(ref1));
-    bool split = false;
-    if (lane == 0) split = decide(b, st, e, r1, thr, thr64, di, dj, di64, dj64, 1.f, 1.0, 1.f, 1.0);
-    split = __shfl_sync(0xffffffffu, split ? 1 : 0, 0) != 0;
+    // level-1 decision (warp-uniform): FP32 when clear of the band, else float64 samples,
+    // one per lane
+    const float diff1 = fabsf(r1.res - r1.ref);
+    const float band1 = 1.5f * r1.errb + 4.f * kEps * thr;
+    bool split = diff1 > thr + band1;
+    if (!split && diff1 >= thr - band1) {
+      double f64 = 0.0, wf64 = 0.0;
+      if (lane < Q2) {
+        double X, Y;
+        pix_to_offset64(st, e, di64 + T.qx[lane], dj64 + T.qy[lane], X, Y);
+        f64 = eval_profile64(e, b.kind, X, Y, 1.0);
+        wf64 = f64 * T.qw[lane];
+      }
+      double res64 = wf64;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) res64 += __shfl_xor_sync(0xffffffffu, res64, o);
+      const double ref64 = __shfl_sync(0xffffffffu, f64, Q2 / 2);
+      split = fabs(res64 - ref64) > thr64;
+      if (lane == 0) ++n64;
+    }
     if (split) {
       n_samples += G2 * Q2;
       // level 2: one sub-pixel per lane
@@ -558,7 +641,7 @@ __device__ void integrate_entry(const BatchArgs& b, int slot, int s, int64_t p, 
           const float thr2 = thr * (float)G2;
           const double thr2_64 = thr64 * (double)G2;
           split2 = decide(b, st, e, r2, thr2, thr2_64, ci2, cj2, di64 + T.gx[lane],
-                          dj64 + T.gy[lane], ginv, ginv64, area2, ginv64 * ginv64);
+                          dj64 + T.gy[lane], ginv, ginv64, area2, ginv64 * ginv64, n64);
         }
       }
       // level 3: refine each flagged sub-pixel with the whole warp
@@ -599,8 +682,8 @@ __device__ void integrate_entry(const BatchArgs& b, int slot, int s, int64_t p, 
       }
     }
   }
+  samples += (unsigned long long)n_samples;
   if (lane == 0) {
-    atomicAdd(b.work_ctr + 1, (unsigned long long)n_samples);
     const int64_t wp = st.work_off + p;
     b.work[work_plane(b, slot, 0) + wp] = out_v;
     if (JAC) {
@@ -612,30 +695,44 @@ __device__ void integrate_entry(const BatchArgs& b, int slot, int s, int64_t p, 
 
 __global__ void __launch_bounds__(256) k_integrate(BatchArgs b) {
   const int lane = threadIdx.x & 31;
+  constexpr uint32_t kChunk = 4;  // queue entries grabbed per atomic
   const uint32_t n = min((uint32_t)b.counters[0], (uint32_t)(2 * b.work_pixels));
+  unsigned long long samples = 0;
+  int n64 = 0;
   while (true) {
-    uint32_t idx = 0;
-    if (lane == 0) idx = atomicAdd(&b.counters[1], 1u);
-    idx = __shfl_sync(0xffffffffu, idx, 0);
-    if (idx >= n) break;
-    const int64_t ent = b.queue[idx];
-    const int slot = (int)(ent >> 62);
-    const int s = (int)((ent >> 32) & 0x3fffffff);
-    const int64_t p = ent & 0xffffffffll;
-    if (b.evals[s * 2 + slot].ops & OP_JAC)
-      integrate_entry<true>(b, slot, s, p, lane);
-    else
-      integrate_entry<false>(b, slot, s, p, lane);
+    uint32_t idx0 = 0;
+    if (lane == 0) idx0 = atomicAdd(&b.counters[1], kChunk);
+    idx0 = __shfl_sync(0xffffffffu, idx0, 0);
+    if (idx0 >= n) break;
+    const uint32_t idx1 = min(idx0 + kChunk, n);
+    for (uint32_t idx = idx0; idx < idx1; ++idx) {
+      const int64_t ent = b.queue[idx];
+      const int slot = (int)(ent >> 62);
+      const int s = (int)((ent >> 32) & 0x3fffffff);
+      const int64_t p = ent & 0xffffffffll;
+      if (b.evals[s * 2 + slot].ops & OP_JAC)
+        integrate_entry<true>(b, slot, s, p, lane, samples, n64);
+      else
+        integrate_entry<false>(b, slot, s, p, lane, samples, n64);
+    }
+  }
+  // per-warp totals: the sample count is warp-uniform, the FP64 re-decisions are per lane
+  n64 = __reduce_add_sync(0xffffffffu, n64);
+  if (lane == 0) {
+    if (samples) atomicAdd(b.work_ctr + 1, samples);
+    if (n64) atomicAdd(&b.counters[6], (unsigned)n64);
   }
 }
 
 // ---------------------------------------------------------------------------
 // convolution + crop + fused accumulation
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void tile_reduce(float* vals, int nvals, double* dst, float* sh) {
-  // vals: per-thread partial values; writes the tile sums to dst[0..nvals)
+constexpr int kConvWarps = kConvThreads / 32;
+
+// Block sums of nvals per-thread values (FP32 within a warp, FP64 across warps) -> dst.
+__device__ __forceinline__ void conv_tile_reduce(const float* vals, int nvals, double* dst,
+                                                 float* sh) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  constexpr int NW = kTile * kTile / 32;
   for (int k = 0; k < nvals; ++k) {
     const float v = warp_sum(vals[k]);
     if (lane == 0) sh[warp * kNacc + k] = v;
@@ -643,46 +740,124 @@ __device__ __forceinline__ void tile_reduce(float* vals, int nvals, double* dst,
   __syncthreads();
   for (int k = threadIdx.x; k < nvals; k += blockDim.x) {
     double t = 0;
-    for (int w = 0; w < NW; ++w) t += (double)sh[w * kNacc + k];
+#pragma unroll
+    for (int w = 0; w < kConvWarps; ++w) t += (double)sh[w * kNacc + k];
     dst[k] = t;
   }
 }
 
-__global__ void __launch_bounds__(256) k_conv(BatchArgs b, ConvIO io) {
+// One column x kConvRows rows of a KP x KP convolution, register blocked: for each kernel
+// column u the kernel column and the input column window live in registers, so one shared
+// load feeds about three FMAs.  out[o] = sum_{v,u} K[v][u] T[ty0 + o + KP-1 - v][tx + KP-1 - u].
+template <int KP>
+__device__ __forceinline__ void conv_col_fixed(const float* __restrict__ Tt, int TW,
+                                               const float* __restrict__ Kk, int tx, int ty0,
+                                               float* out) {
+  constexpr int C2 = KP - 1;
+  constexpr int NT = kConvRows + KP - 1;
+  float acc[kConvRows];
+#pragma unroll
+  for (int o = 0; o < kConvRows; ++o) acc[o] = 0.f;
+  const float* base = Tt + ty0 * TW + tx + C2;
+#pragma unroll 1
+  for (int u = 0; u < KP; ++u) {
+    float kc[KP];
+#pragma unroll
+    for (int v = 0; v < KP; ++v) kc[v] = Kk[v * KP + u];
+    float t[NT];
+    const float* col = base - u;
+#pragma unroll
+    for (int r = 0; r < NT; ++r) t[r] = col[r * TW];
+#pragma unroll
+    for (int v = 0; v < KP; ++v)
+#pragma unroll
+      for (int o = 0; o < kConvRows; ++o) acc[o] = fmaf(kc[v], t[o + C2 - v], acc[o]);
+  }
+#pragma unroll
+  for (int o = 0; o < kConvRows; ++o) out[o] = acc[o];
+}
+
+__device__ __forceinline__ void conv_col_generic(const float* __restrict__ Tt, int TW,
+                                                 const float* __restrict__ Kk, int kpx, int kpy,
+                                                 int tx, int ty0, float* out) {
+  float acc[kConvRows];
+#pragma unroll
+  for (int o = 0; o < kConvRows; ++o) acc[o] = 0.f;
+  for (int v = 0; v < kpy; ++v) {
+    const float* krow = Kk + v * kpx;
+    const float* trow = Tt + (ty0 + kpy - 1 - v) * TW + tx + kpx - 1;
+    for (int u = 0; u < kpx; ++u) {
+      const float k = krow[u];
+#pragma unroll
+      for (int o = 0; o < kConvRows; ++o) acc[o] = fmaf(k, trow[o * TW - u], acc[o]);
+    }
+  }
+#pragma unroll
+  for (int o = 0; o < kConvRows; ++o) out[o] = acc[o];
+}
+
+__device__ __forceinline__ void conv_col(const float* Tt, int TW, const float* Kk, int kpx,
+                                         int kpy, int tx, int ty0, float* out) {
+  if (kpx == kpy) {
+    switch (kpx) {
+#define AP_CONV_CASE(K) \
+  case K:               \
+    conv_col_fixed<K>(Tt, TW, Kk, tx, ty0, out); \
+    return;
+      AP_CONV_CASE(3) AP_CONV_CASE(5) AP_CONV_CASE(7) AP_CONV_CASE(9) AP_CONV_CASE(11)
+      AP_CONV_CASE(13) AP_CONV_CASE(15) AP_CONV_CASE(17) AP_CONV_CASE(19) AP_CONV_CASE(21)
+      AP_CONV_CASE(23) AP_CONV_CASE(25) AP_CONV_CASE(27) AP_CONV_CASE(29)
+#undef AP_CONV_CASE
+      default:
+        break;
+    }
+  }
+  conv_col_generic(Tt, TW, Kk, kpx, kpy, tx, ty0, out);
+}
+
+__global__ void __launch_bounds__(kConvThreads) k_conv(BatchArgs b, ConvIO io) {
   extern __shared__ float smem[];
   const int tile = blockIdx.x, slot = blockIdx.y;
   const int s = b.out_tiles[tile];
   const EvalDev& e = b.evals[s * 2 + slot];
   const int ops = e.ops;
   double* tacc = b.tile_acc + ((int64_t)tile * 2 + slot) * kNacc;
-  if (!ops) return;
+  if (!ops) return;  // uniform per block
   const StampDev& st = b.stamps[s];
   const int local = tile - st.tile_o0;
-  const int tx = threadIdx.x & (kTile - 1), ty = threadIdx.x / kTile;
-  const int x0 = (local % st.nto_x) * kTile, y0 = (local / st.nto_x) * kTile;
-  const int x = x0 + tx, y = y0 + ty;
-  const bool valid = (x < st.nx) && (y < st.ny);
+  const int tx = threadIdx.x & 31, tg = threadIdx.x >> 5;
+  const int x0 = (local % st.nto_x) * kOutTileX, y0 = (local / st.nto_x) * kOutTileY;
+  const int x = x0 + tx, yb = y0 + tg * kConvRows;
   const bool jac = (ops & OP_JAC) != 0;
   const bool shiftmode = (b.psf_mode == AP_PSF_FULL);
 
-  // conv results: [0] model, [1] d/dshift_x, [2] d/dshift_y, [3+q] plane q+1 convolved
-  float cv[3 + NGRAD];
+  // conv results per row: [0] model, [1] d/dshift_x, [2] d/dshift_y, [3+q] partial plane q
+  float cv[3 + NGRAD][kConvRows];
 #pragma unroll
-  for (int k = 0; k < 3 + NGRAD; ++k) cv[k] = 0.f;
+  for (int k = 0; k < 3 + NGRAD; ++k)
+#pragma unroll
+    for (int o = 0; o < kConvRows; ++o) cv[k][o] = 0.f;
 
   const int nplanes = jac ? 1 + NGRAD : 1;
   if (b.psf_mode == AP_PSF_NONE) {
-    if (valid) {
-      const int64_t wp = st.work_off + (int64_t)y * st.wnx + x;
-      cv[0] = b.work[work_plane(b, slot, 0) + wp];
-      for (int q = 0; q < nplanes - 1; ++q) cv[3 + q] = b.work[work_plane(b, slot, 1 + q) + wp];
+#pragma unroll
+    for (int o = 0; o < kConvRows; ++o) {
+      const int y = yb + o;
+      if (x < st.nx && y < st.ny) {
+        const int64_t wp = st.work_off + (int64_t)y * st.wnx + x;
+        cv[0][o] = b.work[work_plane(b, slot, 0) + wp];
+        if (jac) {
+#pragma unroll
+          for (int q = 0; q < NGRAD; ++q) cv[3 + q][o] = b.work[work_plane(b, slot, 1 + q) + wp];
+        }
+      }
     }
   } else {
     const int kpx = st.kpx, kpy = st.kpy, kp2 = kpx * kpy;
     const int cx = (kpx - 1) / 2, cy = (kpy - 1) / 2;
-    const int TW = kTile + kpx - 1, TH = kTile + kpy - 1;
-    float* K = smem;              // up to 3 kernels
-    float* Tt = smem + 3 * kp2;   // input tile
+    const int TW = kOutTileX + kpx - 1, TH = kOutTileY + kpy - 1;
+    float* K = smem;             // up to 3 kernels
+    float* Tt = smem + 3 * kp2;  // input tile
     const float* ksrc = b.spsf + st.spsf_off + (int64_t)slot * 3 * kp2;
     const int nk = (jac && shiftmode) ? 3 : 1;
     for (int idx = threadIdx.x; idx < nk * kp2; idx += blockDim.x) K[idx] = ksrc[idx];
@@ -693,7 +868,7 @@ __global__ void __launch_bounds__(256) k_conv(BatchArgs b, ConvIO io) {
       __syncthreads();
       const float* src = b.work + work_plane(b, slot, pl) + st.work_off;
       for (int idx = threadIdx.x; idx < TW * TH; idx += blockDim.x) {
-        const int r = idx / TW, c = idx % TW;
+        const int r = idx / TW, c = idx - r * TW;
         const int wr = row0 + r, wc = col0 + c;
         Tt[idx] = (wr >= 0 && wr < st.wny && wc >= 0 && wc < st.wnx) ? src[(int64_t)wr * st.wnx + wc]
                                                                       : 0.f;
@@ -701,103 +876,97 @@ __global__ void __launch_bounds__(256) k_conv(BatchArgs b, ConvIO io) {
       __syncthreads();
       const int nkp = (pl == 0) ? nk : 1;
       for (int kk = 0; kk < nkp; ++kk) {
-        const float* Kk = K + kk * kp2;
-        float a = 0.f;
-        for (int v = 0; v < kpy; ++v) {
-          const float* trow = Tt + (ty + 2 * cy - v) * TW + tx + 2 * cx;
-          const float* krow = Kk + v * kpx;
-          for (int u = 0; u < kpx; ++u) a = fmaf(krow[u], trow[-u], a);
-        }
-        if (pl == 0)
-          cv[kk] = a;
-        else
-          cv[3 + (pl - 1)] = a;
+        float outv[kConvRows];
+        conv_col(Tt, TW, K + kk * kp2, kpx, kpy, tx, tg * kConvRows, outv);
+        const int dst = (pl == 0) ? kk : 3 + (pl - 1);
+#pragma unroll
+        for (int o = 0; o < kConvRows; ++o) cv[dst][o] = outv[o];
       }
     }
-  }
-
-  if (b.psf_mode != AP_PSF_NONE) {
     // algorithmic work: 2 FLOP per kernel tap per convolved plane per output pixel
     const int nconv = jac ? ((shiftmode ? 3 : 1) + (b.kind == AP_PROFILE_SERSIC ? 4 : 3) +
                              (shiftmode ? 0 : 2))
                           : 1;
-    const unsigned cnt = __popc(__ballot_sync(0xffffffffu, valid));
+    int nvalid = 0;
+#pragma unroll
+    for (int o = 0; o < kConvRows; ++o) nvalid += (x < st.nx && yb + o < st.ny) ? 1 : 0;
+    const int cnt = __reduce_add_sync(0xffffffffu, nvalid);
     if ((threadIdx.x & 31) == 0 && cnt)
-      atomicAdd(b.work_ctr, (unsigned long long)cnt * 2ull * (unsigned long long)(st.kpx * st.kpy) *
+      atomicAdd(b.work_ctr, (unsigned long long)cnt * 2ull * (unsigned long long)kp2 *
                                 (unsigned long long)nconv);
   }
-  // model and value-space Jacobian in full-vector order
-  const float mgal = cv[0];
-  const float m = mgal + e.sky;
-  float J[NPARAM];
-  if (jac) {
-    if (shiftmode) {
-      J[PX] = cv[1] * (float)st.Pinv[0] + cv[2] * (float)st.Pinv[2];
-      J[PY] = cv[1] * (float)st.Pinv[1] + cv[2] * (float)st.Pinv[3];
-    } else {
-      J[PX] = -cv[3 + GX];
-      J[PY] = -cv[3 + GY];
-    }
-    J[PQ] = cv[3 + GQ];
-    J[PPA] = cv[3 + GPA];
-    J[PN] = cv[3 + GN];
-    J[PRE] = cv[3 + GRE];
-    J[PIE] = kLn10f * mgal;
-    J[PF] = kLn10f * e.sky;
-    if (ops & OP_REP) {
-#pragma unroll
-      for (int k = 0; k < NPARAM; ++k) J[k] *= e.drep[k];
-    }
-  }
-  // compact fitted-slot columns
-  float Jc[NPARAM];
-  int nf = 0;
-  if (jac) {
-#pragma unroll
-    for (int k = 0; k < NPARAM; ++k)
-      if (b.free_mask & (1 << k)) Jc[nf++] = J[k];
-  }
-  const int64_t op = st.out_off + (int64_t)y * st.nx + x;
-  if (valid && (ops & OP_WRITE_MODEL)) io.model_out[op] = m;
-  if (valid && jac && (ops & OP_WRITE_JAC)) {
-    for (int k = 0; k < nf; ++k) io.jac_out[(int64_t)k * b.out_pixels + op] = Jc[k];
-  }
-  if (!(ops & (OP_CHI2 | OP_HG | OP_RPP))) return;
 
-  // fused reductions (fit/lm.py:374-406)
-  // masked pixels (mask != 0) are left out entirely: their data may be anything, NaN included
-  float w = 0.f, r = 0.f;
-  const bool use = valid && !(io.mask && io.mask[op]);
-  if (use) {
-    w = io.weight ? io.weight[op] : 1.f;
-    r = io.data[op] - m;
-  }
-  float vals[kNacc];
-  int nv = 0;
-  vals[nv++] = w * r * r;  // ACC_CHI2
   const int nfree = b.n_free;
-  if (ops & OP_HG) {
-    for (int k = 0; k < nfree; ++k) vals[nv++] = (use && jac) ? Jc[k] * w * r : 0.f;
-    for (int a = 0; a < nfree; ++a)
-      for (int c = a; c < nfree; ++c) vals[nv++] = (use && jac) ? Jc[a] * w * Jc[c] : 0.f;
-  }
-  if (ops & OP_RPP) {
-    float jh = 0.f, ebase = 0.f;
-    float Jb[NPARAM];
-    if (use) {
+  const bool acc_any = (ops & (OP_CHI2 | OP_HG | OP_RPP)) != 0;
+  float vals[kNacc];
+#pragma unroll
+  for (int k = 0; k < kNacc; ++k) vals[k] = 0.f;
+  const int n_hg = (ops & OP_HG) ? nfree + nfree * (nfree + 1) / 2 : 0;
+  const float d = (float)io.rpp_d;
+
+#pragma unroll
+  for (int o = 0; o < kConvRows; ++o) {
+    const int y = yb + o;
+    const bool valid = (x < st.nx) && (y < st.ny);
+    if (!valid) continue;
+    const float mgal = cv[0][o];
+    const float m = mgal + e.sky;
+    // model and value-space Jacobian in full-vector order, compacted to the fitted slots
+    float Jc[NPARAM];
+    int nf = 0;
+    if (jac) {
+      float J[NPARAM];
+      if (shiftmode) {
+        J[PX] = cv[1][o] * (float)st.Pinv[0] + cv[2][o] * (float)st.Pinv[2];
+        J[PY] = cv[1][o] * (float)st.Pinv[1] + cv[2][o] * (float)st.Pinv[3];
+      } else {
+        J[PX] = -cv[3 + GX][o];
+        J[PY] = -cv[3 + GY][o];
+      }
+      J[PQ] = cv[3 + GQ][o];
+      J[PPA] = cv[3 + GPA][o];
+      J[PN] = cv[3 + GN][o];
+      J[PRE] = cv[3 + GRE][o];
+      J[PIE] = kLn10f * mgal;
+      J[PF] = kLn10f * e.sky;
+#pragma unroll
+      for (int k = 0; k < NPARAM; ++k) {
+        if (b.free_mask & (1 << k)) Jc[nf++] = (ops & OP_REP) ? J[k] * e.drep[k] : J[k];
+      }
+    }
+    const int64_t op = st.out_off + (int64_t)y * st.nx + x;
+    if (ops & OP_WRITE_MODEL) io.model_out[op] = m;
+    if (jac && (ops & OP_WRITE_JAC)) {
+      for (int k = 0; k < nf; ++k) io.jac_out[(int64_t)k * b.out_pixels + op] = Jc[k];
+    }
+    if (!acc_any) continue;
+    // fused reductions (fit/lm.py:374-406); masked pixels are left out entirely
+    if (io.mask && io.mask[op]) continue;
+    const float w = io.weight ? io.weight[op] : 1.f;
+    const float r = io.data[op] - m;
+    vals[0] += w * r * r;  // chi2
+    int nv = 1;
+    if (ops & OP_HG) {
+      for (int k = 0; k < nfree; ++k) vals[nv++] += Jc[k] * w * r;
+      for (int a = 0; a < nfree; ++a)
+        for (int c = a; c < nfree; ++c) vals[nv++] += Jc[a] * w * Jc[c];
+    }
+    if (ops & OP_RPP) {
+      float Jb[NPARAM];
+      float jh = 0.f;
       for (int k = 0; k < nfree; ++k) {
         Jb[k] = io.jbase[(int64_t)k * b.out_pixels + op];
         jh = fmaf(Jb[k], (float)io.hvec[s * NPARAM + k], jh);
       }
-      const float d = (float)io.rpp_d;
       // (2/d) * ((rh - r)/d - W (J h)),  rh - r = W (Y1 - Y0)
-      ebase = (2.f / d) * ((w * (m - io.y0[op])) / d - w * jh);
+      const float ebase = (2.f / d) * ((w * (m - io.y0[op])) / d - w * jh);
+      for (int k = 0; k < nfree; ++k) vals[nv++] += Jb[k] * ebase;
     }
-    for (int k = 0; k < nfree; ++k) vals[nv++] = use ? Jb[k] * ebase : 0.f;
   }
-  __shared__ float shred[(kTile * kTile / 32) * kNacc];
-  __syncthreads();
-  tile_reduce(vals, nv, tacc, shred);
+  if (!acc_any) return;
+  int nv = 1 + n_hg + ((ops & OP_RPP) ? nfree : 0);
+  __shared__ float shred[kConvWarps * kNacc];
+  conv_tile_reduce(vals, nv, tacc, shred);
 }
 
 // per-stamp sums of the tile partials (fixed order: deterministic)
@@ -819,24 +988,27 @@ __global__ void k_reduce_acc(BatchArgs b) {
 // ---------------------------------------------------------------------------
 // stand-alone chi^2 of a given model (LM._chi2 numerator)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_chi2(BatchArgs b, ConvIO io, const float* model) {
+__global__ void __launch_bounds__(kConvThreads) k_chi2(BatchArgs b, ConvIO io, const float* model) {
   const int tile = blockIdx.x;
   const int s = b.out_tiles[tile];
   const StampDev& st = b.stamps[s];
   const int local = tile - st.tile_o0;
-  const int x = (local % st.nto_x) * kTile + (threadIdx.x & (kTile - 1));
-  const int y = (local / st.nto_x) * kTile + threadIdx.x / kTile;
+  const int x = (local % st.nto_x) * kOutTileX + (threadIdx.x & 31);
+  const int yb = (local / st.nto_x) * kOutTileY + (threadIdx.x >> 5) * kConvRows;
   float v = 0.f;
-  if (x < st.nx && y < st.ny) {
-    const int64_t op = st.out_off + (int64_t)y * st.nx + x;
-    if (!(io.mask && io.mask[op])) {
-      const float w = io.weight ? io.weight[op] : 1.f;
-      const float r = io.data[op] - model[op];
-      v = w * r * r;
+  for (int o = 0; o < kConvRows; ++o) {
+    const int y = yb + o;
+    if (x < st.nx && y < st.ny) {
+      const int64_t op = st.out_off + (int64_t)y * st.nx + x;
+      if (!(io.mask && io.mask[op])) {
+        const float w = io.weight ? io.weight[op] : 1.f;
+        const float r = io.data[op] - model[op];
+        v += w * r * r;
+      }
     }
   }
-  __shared__ float shred[(kTile * kTile / 32) * kNacc];
-  tile_reduce(&v, 1, b.tile_acc + (int64_t)tile * 2 * kNacc, shred);
+  __shared__ float shred[kConvWarps * kNacc];
+  conv_tile_reduce(&v, 1, b.tile_acc + (int64_t)tile * 2 * kNacc, shred);
 }
 
 __global__ void k_chi2_reduce(BatchArgs b, double* out) {
@@ -902,18 +1074,19 @@ cudaError_t launch_render_pass(const BatchArgs& b, const ConvIO& io, size_t conv
   k_sample<<<dim3(b.n_work_tiles, 2), kTile * kTile, 0, s>>>(b);
   E(t);
   if (b.integrate == AP_INTEGRATE_THRESHOLD) {
-    t = B(KC_SELECT);
-    k_select<<<dim3(b.n_work_tiles, 2), kTile * kTile, 0, s>>>(b);
-    E(t);
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    t = B(KC_SELECT);
+    k_select<<<dim3(b.n_work_tiles, 2), kTile * kTile, 0, s>>>(b);
+    k_recheck<<<nsm * 4, 256, 0, s>>>(b);
+    E(t);
     t = B(KC_INTEGRATE);
     k_integrate<<<nsm * 8, 256, 0, s>>>(b);
     E(t);
   }
   t = B(KC_CONV);
-  k_conv<<<dim3(b.n_out_tiles, 2), kTile * kTile, conv_smem, s>>>(b, io);
+  k_conv<<<dim3(b.n_out_tiles, 2), kConvThreads, conv_smem, s>>>(b, io);
   E(t);
   if (accumulate) {
     t = B(KC_REDUCE);
@@ -1009,7 +1182,7 @@ void Profiler::destroy() {
 
 cudaError_t launch_chi2_only(const BatchArgs& b, const ConvIO& io, const float* model,
                              double* out, cudaStream_t s) {
-  k_chi2<<<b.n_out_tiles, kTile * kTile, 0, s>>>(b, io, model);
+  k_chi2<<<b.n_out_tiles, kConvThreads, 0, s>>>(b, io, model);
   k_chi2_reduce<<<(b.n_stamps + 127) / 128, 128, 0, s>>>(b, out);
   return cudaGetLastError();
 }

@@ -11,7 +11,7 @@
 //
 // Rules of use
 //   - At most AP_NOALLOC_SCRATCH_BYTES (8 MiB) of scratch: working windows up to about
-//     90,000 pixels (e.g. a 256 x 256 stamp with a 21 x 21 PSF).  Larger stamps are rejected
+//     80,000 pixels (e.g. a 256 x 256 stamp with a 21 x 21 PSF).  Larger stamps are rejected
 //     with AP_ERR_WORKSPACE before any device work is queued.
 //   - The first call on each device resolves the array's device address (cudaGetSymbolAddress,
 //     with that device current); make that first call before any stream capture.
@@ -160,8 +160,8 @@ extern "C" int ap_render_noalloc(int32_t nx, int32_t ny, int32_t psf_kx, int32_t
   st.pixel_area = std::fabs(det);
   st.ntw_x = (st.wnx + kTile - 1) / kTile;
   st.ntw = st.ntw_x * ((st.wny + kTile - 1) / kTile);
-  st.nto_x = (nx + kTile - 1) / kTile;
-  st.nto = st.nto_x * ((ny + kTile - 1) / kTile);
+  st.nto_x = (nx + kOutTileX - 1) / kOutTileX;
+  st.nto = st.nto_x * ((ny + kOutTileY - 1) / kOutTileY);
   const int64_t wp = (int64_t)st.wnx * st.wny;
   const int64_t kp2 = (int64_t)st.kpx * st.kpy;
 
@@ -226,6 +226,7 @@ extern "C" int ap_render_noalloc(int32_t nx, int32_t ny, int32_t psf_kx, int32_t
   const int64_t o_aux = take(sizeof(float) * 2 * 2 * wp);
   const int64_t o_spsf = take(sizeof(float) * (kp2 > 0 ? 6 * kp2 : 1));
   const int64_t o_queue = take(sizeof(int64_t) * 2 * wp);
+  const int64_t o_recheck = take(sizeof(int64_t) * 2 * wp);
   const int64_t o_cnt = take(sizeof(uint32_t) * 16);
   const int64_t o_wctr = take(sizeof(unsigned long long) * 4);
   const int64_t o_mean = take(sizeof(double) * 2);
@@ -234,7 +235,7 @@ extern "C" int ap_render_noalloc(int32_t nx, int32_t ny, int32_t psf_kx, int32_t
   if (o > (int64_t)kScratchBytes) return AP_ERR_WORKSPACE;
   size_t conv_smem = 0;
   if (with_psf)
-    conv_smem = sizeof(float) * (3 * (size_t)kp2 + (size_t)(kTile + st.kpx - 1) * (kTile + st.kpy - 1));
+    conv_smem = conv_smem_bytes(st.kpx, st.kpy);
   if (conv_smem > 200 * 1024) return AP_ERR_UNSUPPORTED;
 
   // ---- device address of the scratch, once per device ----------------------------------------
@@ -290,6 +291,7 @@ extern "C" int ap_render_noalloc(int32_t nx, int32_t ny, int32_t psf_kx, int32_t
   A.aux = (float*)(ws + o_aux);
   A.spsf = (float*)(ws + o_spsf);
   A.queue = (int64_t*)(ws + o_queue);
+  A.recheck = (int64_t*)(ws + o_recheck);
   A.counters = (uint32_t*)(ws + o_cnt);
   A.work_ctr = (unsigned long long*)(ws + o_wctr);
   A.mean_acc = (double*)(ws + o_mean);

@@ -164,8 +164,10 @@ int ap_lm_fit(ap_batch* batch, const float* data, const float* weight, const uin
 int ap_lm_history(const ap_batch* batch, const double** loss, const double** lambda_,
                   const double** states, int32_t* hist_len);
 
-/* Diagnostics of the last call: integration queue length, FP64 re-decisions, rounds. */
-int ap_batch_stats(const ap_batch* batch, int64_t* stats_out /* [4] */);
+/* Diagnostics of the last call: [0] integration queue length, [1] selection decisions made
+ * in float64 (cumulative), [2] overflow flags, [3] LM rounds, [4] integration-level
+ * decisions made in float64 (cumulative). */
+int ap_batch_stats(const ap_batch* batch, int64_t* stats_out /* [5] */);
 
 /* Per-kernel CUDA-event timing.  ap_batch_profile(b, 1) clears the totals and records an
  * event pair around every kernel this batch launches from then on (also inside the LM's
@@ -194,7 +196,7 @@ int ap_fma_probe(float* scratch, int32_t iters, int32_t blocks, ap_stream_t stre
  * instead of a caller workspace.  geometry / options are host pointers (8 doubles as in
  * ap_batch_create); params[8] (value space), psf[psf_ky * psf_kx] (NULL without a PSF) and
  * model[ny * nx] are device pointers.  Working windows that need more than
- * AP_NOALLOC_SCRATCH_BYTES of scratch (about 90,000 pixels, e.g. 256 x 256 with a 21 x 21
+ * AP_NOALLOC_SCRATCH_BYTES of scratch (about 80,000 pixels, e.g. 256 x 256 with a 21 x 21
  * PSF) are rejected with AP_ERR_WORKSPACE.  The first call on each device resolves the
  * array's address; make it before any stream capture.  All calls on a device share the
  * array, so calls that overlap on the GPU race.  Calls no cudaMalloc / cudaFree. */

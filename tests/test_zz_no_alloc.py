@@ -36,6 +36,7 @@ def assert_image_close(got, ref, rel=1e-5, pix=1e-4):
 
 
 def noalloc_render(N, nx, ny, psf, psf_shape, geometry, opts, params):
+    assert params.dtype == torch.float64 and params.is_contiguous()  # the C ABI reads double[8]
     model = torch.full((ny * nx,), float("nan"), dtype=torch.float32, device="cuda")
     g = np.ascontiguousarray(geometry, dtype=np.float64)
     kx, ky = psf_shape
@@ -79,7 +80,7 @@ def test_noalloc_matches_batch_render_twice(N, name):
 def test_noalloc_rejects_windows_beyond_its_scratch(N):
     opts = N.make_options(psf_mode="full")
     psf = torch.ones(21 * 21, dtype=torch.float32, device="cuda") / 441
-    params = torch.tensor([300.0, 300.0, 0.5, 1.0, 2.0, 10.0, 1.0, 0.0], device="cuda")
+    params = torch.tensor([300.0, 300.0, 0.5, 1.0, 2.0, 10.0, 1.0, 0.0], dtype=torch.float64, device="cuda")
     model = torch.zeros(600 * 600, dtype=torch.float32, device="cuda")
     g = np.ascontiguousarray(N.scale_geometry(1)[0])
     rc = N.lib().ap_render_noalloc(600, 600, 21, 21, g.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
@@ -87,3 +88,16 @@ def test_noalloc_rejects_windows_beyond_its_scratch(N):
                                    ctypes.c_void_p(psf.data_ptr()), ctypes.c_void_p(model.data_ptr()),
                                    ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
     assert rc == N.AP_ERR_WORKSPACE
+
+
+def test_noalloc_handles_the_largest_cutout(N):
+    """A 256 x 256 stamp with a 21 x 21 PSF (the largest of the cutout workload) fits."""
+    opts = N.make_options(psf_mode="full")
+    psf_np = np.ones((21, 21)) / 441.0
+    geom = N.scale_geometry(1)
+    batch = N.StampBatch([(256, 256)], [(21, 21)], geom, opts)
+    psf = batch.pack_psf([psf_np])
+    params = torch.tensor([[128.3, 127.6, 0.5, 1.0, 2.0, 12.0, 1.0, 0.0]], dtype=torch.float64, device="cuda")
+    want = batch.unpack(batch.render(params, psf))[0]
+    got = noalloc_render(N, 256, 256, psf, (21, 21), geom[0], opts, params[0].contiguous())
+    assert_image_close(got, want)
