@@ -223,6 +223,10 @@ int ap_batch_create(ap_batch** out, int32_t n, const int32_t* nx, const int32_t*
     st.ref_xy[0] = g[6];
     st.ref_xy[1] = g[7];
     st.pixel_area = std::fabs(det);
+    for (int k = 0; k < 4; ++k) {
+      st.Pf[k] = (float)st.P[k];
+      st.Pinvf[k] = (float)st.Pinv[k];
+    }
     st.out_off = out_off;
     st.work_off = work_off;
     st.psf_off = psf_off;
@@ -322,6 +326,8 @@ int ap_batch_create(ap_batch** out, int32_t n, const int32_t* nx, const int32_t*
       break;
     }
   }
+
+  quad_tables_fill_f32(T);
 
   // workspace layout
   Layout& L = b->L;

@@ -69,7 +69,28 @@ struct QuadTables {
   double gx[kMaxGrid * kMaxGrid], gy[kMaxGrid * kMaxGrid];
   // sampling-mode sub-sample offsets (unit pixel) and weights
   double sx[kMaxQuad * kMaxQuad], sy[kMaxQuad * kMaxQuad], sw[kMaxQuad * kMaxQuad];
+  // FP32 copies for the per-sample paths (a double -> float conversion runs on the FP64
+  // pipe, which is narrow on this GPU)
+  float qxf[kMaxQuad * kMaxQuad], qyf[kMaxQuad * kMaxQuad], qwf[kMaxQuad * kMaxQuad];
+  float gxf[kMaxGrid * kMaxGrid], gyf[kMaxGrid * kMaxGrid];
+  float sxf[kMaxQuad * kMaxQuad], syf[kMaxQuad * kMaxQuad], swf[kMaxQuad * kMaxQuad];
 };
+
+// fill the FP32 copies of a table (host side)
+inline void quad_tables_fill_f32(QuadTables& T) {
+  for (int k = 0; k < kMaxQuad * kMaxQuad; ++k) {
+    T.qxf[k] = (float)T.qx[k];
+    T.qyf[k] = (float)T.qy[k];
+    T.qwf[k] = (float)T.qw[k];
+    T.sxf[k] = (float)T.sx[k];
+    T.syf[k] = (float)T.sy[k];
+    T.swf[k] = (float)T.sw[k];
+  }
+  for (int k = 0; k < kMaxGrid * kMaxGrid; ++k) {
+    T.gxf[k] = (float)T.gx[k];
+    T.gyf[k] = (float)T.gy[k];
+  }
+}
 
 struct StampDev {
   int32_t nx, ny;    // output window
@@ -87,6 +108,7 @@ struct StampDev {
   double P[4], Pinv[4];
   double ref_ij[2], ref_xy[2];
   double pixel_area;
+  float Pf[4], Pinvf[4];  // FP32 copies for the per-pixel paths
 };
 
 struct EvalDev {
@@ -152,9 +174,11 @@ struct ConvIO {
   double rpp_d;           // OP_RPP: d (0.1)
 };
 
-// dynamic shared memory of the convolve pass for a kpx x kpy kernel: 3 kernels + input tile
+// dynamic shared memory of the convolve pass for a kpx x kpy kernel: 3 kernels stored
+// transposed with columns padded to a multiple of 4 floats, and the input tile
+__host__ __device__ inline int conv_col_stride(int kpy) { return (kpy + 3) & ~3; }
 __host__ __device__ inline size_t conv_smem_bytes(int kpx, int kpy) {
-  return sizeof(float) * (3 * (size_t)kpx * kpy +
+  return sizeof(float) * (3 * (size_t)kpx * conv_col_stride(kpy) +
                           (size_t)(kOutTileX + kpx - 1) * (kOutTileY + kpy - 1));
 }
 
@@ -238,8 +262,8 @@ __device__ __forceinline__ double eval_profile64(const EvalDev& e, int kind, dou
 __device__ __forceinline__ void pix_to_offset(const StampDev& st, const EvalDev& e, float di,
                                               float dj, float& X, float& Y) {
   const float a = di - e.fx, b = dj - e.fy;
-  X = (float)st.P[0] * a + (float)st.P[1] * b;
-  Y = (float)st.P[2] * a + (float)st.P[3] * b;
+  X = st.Pf[0] * a + st.Pf[1] * b;
+  Y = st.Pf[2] * a + st.Pf[3] * b;
 }
 
 __device__ __forceinline__ void pix_to_offset64(const StampDev& st, const EvalDev& e, double di,

@@ -229,9 +229,9 @@ __device__ __forceinline__ void sample_pixel(const BatchArgs& b, const StampDev&
   float referr = 0.f;
   for (int k = 0; k < T.nsub; ++k) {
     float X, Y;
-    pix_to_offset(st, e, di + (float)T.sx[k], dj + (float)T.sy[k], X, Y);
+    pix_to_offset(st, e, di + T.sxf[k], dj + T.syf[k], X, Y);
     const Sample sm = eval_profile<JAC>(e, b.kind, X, Y, 1.f);
-    const float w = (float)T.sw[k];
+    const float w = T.swf[k];
     deep = fmaf(w, sm.v, deep);
     if (JAC) {
 #pragma unroll
@@ -323,16 +323,22 @@ __global__ void __launch_bounds__(256) k_sample(BatchArgs b) {
 __device__ __forceinline__ void stamp_threshold(const BatchArgs& b, const StampDev& st,
                                                 const EvalDev& e, int s, int slot, float& thr,
                                                 double& thr64, float& thr_err) {
-  if (b.kind == AP_PROFILE_SERSIC) {
-    thr = e.thresh;
-    thr64 = e.thresh64;
-    thr_err = 2.f * kEps * thr;
-  } else {
-    thr64 = b.tolerance64 * (b.mean_acc[s * 2 + slot] / ((double)st.wnx * (double)st.wny));
-    thr = (float)thr64;
-    // the FP32 samples make the mean uncertain at the 1e-6 level
-    thr_err = 2e-6f * thr;
-  }
+  // Sersic: closed-form flux (k_eval_setup); exponential: sum(deep) (k_exp_threshold).
+  thr = e.thresh;
+  thr64 = e.thresh64;
+  // the exponential's mean comes from FP32 samples: uncertain at the 1e-6 level
+  thr_err = (b.kind == AP_PROFILE_SERSIC) ? 2.f * kEps * thr : 2e-6f * thr;
+}
+
+// Exponential threshold: sampling_tolerance * sum(deep) / numel, once per (stamp, slot).
+__global__ void k_exp_threshold(BatchArgs b) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= b.n_stamps * 2) return;
+  EvalDev& e = b.evals[t];
+  if (!e.ops) return;
+  const StampDev& st = b.stamps[t >> 1];
+  e.thresh64 = b.tolerance64 * (b.mean_acc[t] / ((double)st.wnx * (double)st.wny));
+  e.thresh = (float)e.thresh64;
 }
 
 __global__ void __launch_bounds__(256) k_select(BatchArgs b) {
@@ -500,9 +506,9 @@ __device__ __forceinline__ QuadResult quad_lane(const BatchArgs& b, const StampD
   float referr = 0.f;
   for (int k = 0; k < n; ++k) {
     float X, Y;
-    pix_to_offset(st, e, ci + (float)T.qx[k] * inv_g, cj + (float)T.qy[k] * inv_g, X, Y);
+    pix_to_offset(st, e, ci + T.qxf[k] * inv_g, cj + T.qyf[k] * inv_g, X, Y);
     const Sample sm = eval_profile<JAC>(e, b.kind, X, Y, area);
-    const float w = (float)T.qw[k];
+    const float w = T.qwf[k];
     r.res = fmaf(w, sm.v, r.res);
     if (JAC) {
 #pragma unroll
@@ -520,10 +526,20 @@ __device__ __forceinline__ QuadResult quad_lane(const BatchArgs& b, const StampD
   return r;
 }
 
-__device__ bool refine64(const BatchArgs& b, const StampDev& st, const EvalDev& e, double ci,
-                         double cj, double inv_g, double area, double thr64) {
+// float64 re-evaluation of one (sub-)pixel's quadrature: pixel (i, j) of the working grid,
+// sub-pixel m of the displacement grid (m < 0: the pixel itself).
+__device__ bool refine64(const BatchArgs& b, const StampDev& st, const EvalDev& e, int i, int j,
+                         int m, double thr64) {
   const QuadTables& T = *b.tables;
   const int n = T.quad_level * T.quad_level;
+  double ci = (double)(i - e.cix), cj = (double)(j - e.cjy);
+  double inv_g = 1.0, area = 1.0;
+  if (m >= 0) {
+    ci += T.gx[m];
+    cj += T.gy[m];
+    inv_g = 1.0 / (double)T.gridding;
+    area = inv_g * inv_g;
+  }
   double res = 0, ref = 0;
   for (int k = 0; k < n; ++k) {
     double X, Y;
@@ -535,16 +551,18 @@ __device__ bool refine64(const BatchArgs& b, const StampDev& st, const EvalDev& 
   return fabs(res - ref) > thr64;
 }
 
+// Level-2 refinement decision of sub-pixel m: FP32 when clear of the error band, else
+// float64 (threshold scaled by gridding^2 as the reference passes it down).
 __device__ __forceinline__ bool decide(const BatchArgs& b, const StampDev& st, const EvalDev& e,
-                                       const QuadResult& r, float thr, double thr64, float ci,
-                                       float cj, double ci64, double cj64, float inv_g,
-                                       double inv_g64, float area, double area64, int& n64) {
+                                       const QuadResult& r, float thr, int i, int j, int m,
+                                       int& n64) {
   const float diff = fabsf(r.res - r.ref);
   const float band = 1.5f * r.errb + 4.f * kEps * thr;
   if (diff > thr + band) return true;
   if (diff < thr - band) return false;
   ++n64;
-  return refine64(b, st, e, ci64, cj64, inv_g64, area64, thr64);
+  const int g = b.tables->gridding;
+  return refine64(b, st, e, i, j, m, e.thresh64 * (double)(g * g));
 }
 
 template <bool JAC>
@@ -557,12 +575,8 @@ __device__ void integrate_entry(const BatchArgs& b, int slot, int s, int64_t p, 
   const int g = T.gridding, G2 = g * g;
   const int i = (int)(p % st.wnx), j = (int)(p / st.wnx);
   const float di = (float)(i - e.cix), dj = (float)(j - e.cjy);
-  const double di64 = (double)(i - e.cix), dj64 = (double)(j - e.cjy);
-  float thr, thr_err;
-  double thr64;
-  stamp_threshold(b, st, e, s, slot, thr, thr64, thr_err);
+  const float thr = e.thresh;
   const float ginv = 1.f / (float)g;
-  const double ginv64 = 1.0 / (double)g;
 
   int n_samples = Q2;
   // level 1: Q^2 samples spread over the lanes
@@ -572,9 +586,9 @@ __device__ void integrate_entry(const BatchArgs& b, int slot, int s, int64_t p, 
   float f = 0.f, fe = 0.f, fa = 0.f;
   if (lane < Q2) {
     float X, Y;
-    pix_to_offset(st, e, di + (float)T.qx[lane], dj + (float)T.qy[lane], X, Y);
+    pix_to_offset(st, e, di + T.qxf[lane], dj + T.qyf[lane], X, Y);
     const Sample sm = eval_profile<JAC>(e, b.kind, X, Y, 1.f);
-    const float w = (float)T.qw[lane];
+    const float w = T.qwf[lane];
     f = sm.v;
     v = w * sm.v;
     fa = fabsf(v);
@@ -612,7 +626,7 @@ __device__ void integrate_entry(const BatchArgs& b, int slot, int s, int64_t p, 
       double f64 = 0.0, wf64 = 0.0;
       if (lane < Q2) {
         double X, Y;
-        pix_to_offset64(st, e, di64 + T.qx[lane], dj64 + T.qy[lane], X, Y);
+        pix_to_offset64(st, e, (double)(i - e.cix) + T.qx[lane], (double)(j - e.cjy) + T.qy[lane], X, Y);
         f64 = eval_profile64(e, b.kind, X, Y, 1.0);
         wf64 = f64 * T.qw[lane];
       }
@@ -620,7 +634,7 @@ __device__ void integrate_entry(const BatchArgs& b, int slot, int s, int64_t p, 
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) res64 += __shfl_xor_sync(0xffffffffu, res64, o);
       const double ref64 = __shfl_sync(0xffffffffu, f64, Q2 / 2);
-      split = fabs(res64 - ref64) > thr64;
+      split = fabs(res64 - ref64) > e.thresh64;
       if (lane == 0) ++n64;
     }
     if (split) {
@@ -634,14 +648,11 @@ __device__ void integrate_entry(const BatchArgs& b, int slot, int s, int64_t p, 
       float ci2 = 0.f, cj2 = 0.f;
       bool split2 = false;
       if (lane < G2) {
-        ci2 = di + (float)T.gx[lane];
-        cj2 = dj + (float)T.gy[lane];
+        ci2 = di + T.gxf[lane];
+        cj2 = dj + T.gyf[lane];
         r2 = quad_lane<JAC>(b, st, e, ci2, cj2, ginv, area2);
         if (b.max_depth > 2) {
-          const float thr2 = thr * (float)G2;
-          const double thr2_64 = thr64 * (double)G2;
-          split2 = decide(b, st, e, r2, thr2, thr2_64, ci2, cj2, di64 + T.gx[lane],
-                          dj64 + T.gy[lane], ginv, ginv64, area2, ginv64 * ginv64, n64);
+          split2 = decide(b, st, e, r2, thr * (float)G2, i, j, lane, n64);
         }
       }
       // level 3: refine each flagged sub-pixel with the whole warp
@@ -658,8 +669,8 @@ __device__ void integrate_entry(const BatchArgs& b, int slot, int s, int64_t p, 
 #pragma unroll
         for (int q = 0; q < NGRAD; ++q) r3.g[q] = 0.f;
         if (lane < G2) {
-          r3 = quad_lane<JAC>(b, st, e, cim + (float)T.gx[lane] * ginv,
-                              cjm + (float)T.gy[lane] * ginv, ginv * ginv, area3);
+          r3 = quad_lane<JAC>(b, st, e, cim + T.gxf[lane] * ginv,
+                              cjm + T.gyf[lane] * ginv, ginv * ginv, area3);
         }
         const float s3 = warp_sum(r3.res);
         float gs3[NGRAD];
@@ -747,23 +758,32 @@ __device__ __forceinline__ void conv_tile_reduce(const float* vals, int nvals, d
 }
 
 // One column x kConvRows rows of a KP x KP convolution, register blocked: for each kernel
-// column u the kernel column and the input column window live in registers, so one shared
-// load feeds about three FMAs.  out[o] = sum_{v,u} K[v][u] T[ty0 + o + KP-1 - v][tx + KP-1 - u].
+// column u the kernel column (float4 loads of the transposed kernel) and the input column
+// window live in registers.  out[o] = sum_{v,u} K[v][u] T[ty0 + o + KP-1 - v][tx + KP-1 - u],
+// with KT[u * stride + v] = K[v][u].
 template <int KP>
 __device__ __forceinline__ void conv_col_fixed(const float* __restrict__ Tt, int TW,
-                                               const float* __restrict__ Kk, int tx, int ty0,
+                                               const float* __restrict__ KT, int tx, int ty0,
                                                float* out) {
   constexpr int C2 = KP - 1;
   constexpr int NT = kConvRows + KP - 1;
+  constexpr int KS = (KP + 3) & ~3;
   float acc[kConvRows];
 #pragma unroll
   for (int o = 0; o < kConvRows; ++o) acc[o] = 0.f;
   const float* base = Tt + ty0 * TW + tx + C2;
 #pragma unroll 1
   for (int u = 0; u < KP; ++u) {
-    float kc[KP];
+    float kc[KS];
+    const float4* kcol = reinterpret_cast<const float4*>(KT + u * KS);
 #pragma unroll
-    for (int v = 0; v < KP; ++v) kc[v] = Kk[v * KP + u];
+    for (int q = 0; q < KS / 4; ++q) {
+      const float4 k4 = kcol[q];
+      kc[4 * q + 0] = k4.x;
+      kc[4 * q + 1] = k4.y;
+      kc[4 * q + 2] = k4.z;
+      kc[4 * q + 3] = k4.w;
+    }
     float t[NT];
     const float* col = base - u;
 #pragma unroll
@@ -778,31 +798,34 @@ __device__ __forceinline__ void conv_col_fixed(const float* __restrict__ Tt, int
 }
 
 __device__ __forceinline__ void conv_col_generic(const float* __restrict__ Tt, int TW,
-                                                 const float* __restrict__ Kk, int kpx, int kpy,
+                                                 const float* __restrict__ KT, int kpx, int kpy,
                                                  int tx, int ty0, float* out) {
   float acc[kConvRows];
 #pragma unroll
   for (int o = 0; o < kConvRows; ++o) acc[o] = 0.f;
-  for (int v = 0; v < kpy; ++v) {
-    const float* krow = Kk + v * kpx;
-    const float* trow = Tt + (ty0 + kpy - 1 - v) * TW + tx + kpx - 1;
-    for (int u = 0; u < kpx; ++u) {
-      const float k = krow[u];
+  const int ks = conv_col_stride(kpy);
+  for (int u = 0; u < kpx; ++u) {
+    const float* kcol = KT + u * ks;
+    const float* tcol = Tt + ty0 * TW + tx + kpx - 1 - u;
+    for (int v = 0; v < kpy; ++v) {
+      const float k = kcol[v];
+      const float* tp = tcol + (kpy - 1 - v) * TW;
 #pragma unroll
-      for (int o = 0; o < kConvRows; ++o) acc[o] = fmaf(k, trow[o * TW - u], acc[o]);
+      for (int o = 0; o < kConvRows; ++o) acc[o] = fmaf(k, tp[o * TW], acc[o]);
     }
   }
 #pragma unroll
   for (int o = 0; o < kConvRows; ++o) out[o] = acc[o];
 }
 
-__device__ __forceinline__ void conv_col(const float* Tt, int TW, const float* Kk, int kpx,
-                                         int kpy, int tx, int ty0, float* out) {
+// One copy of all the kernel-size instances, shared by the k_conv<NF> instantiations.
+__device__ __noinline__ void conv_col(const float* Tt, int TW, const float* KT, int kpx, int kpy,
+                                      int tx, int ty0, float* out) {
   if (kpx == kpy) {
     switch (kpx) {
 #define AP_CONV_CASE(K) \
   case K:               \
-    conv_col_fixed<K>(Tt, TW, Kk, tx, ty0, out); \
+    conv_col_fixed<K>(Tt, TW, KT, tx, ty0, out); \
     return;
       AP_CONV_CASE(3) AP_CONV_CASE(5) AP_CONV_CASE(7) AP_CONV_CASE(9) AP_CONV_CASE(11)
       AP_CONV_CASE(13) AP_CONV_CASE(15) AP_CONV_CASE(17) AP_CONV_CASE(19) AP_CONV_CASE(21)
@@ -812,11 +835,14 @@ __device__ __forceinline__ void conv_col(const float* Tt, int TW, const float* K
         break;
     }
   }
-  conv_col_generic(Tt, TW, Kk, kpx, kpy, tx, ty0, out);
+  conv_col_generic(Tt, TW, KT, kpx, kpy, tx, ty0, out);
 }
 
+// Convolve/accumulate pass.  NF = number of fitted parameters (compile time, so the
+// per-pixel J^T W J accumulators stay in registers).
+template <int NF>
 __global__ void __launch_bounds__(kConvThreads) k_conv(BatchArgs b, ConvIO io) {
-  extern __shared__ float smem[];
+  extern __shared__ __align__(16) float smem[];
   const int tile = blockIdx.x, slot = blockIdx.y;
   const int s = b.out_tiles[tile];
   const EvalDev& e = b.evals[s * 2 + slot];
@@ -830,15 +856,15 @@ __global__ void __launch_bounds__(kConvThreads) k_conv(BatchArgs b, ConvIO io) {
   const int x = x0 + tx, yb = y0 + tg * kConvRows;
   const bool jac = (ops & OP_JAC) != 0;
   const bool shiftmode = (b.psf_mode == AP_PSF_FULL);
+  const int nplanes = jac ? 1 + NGRAD : 1;
 
-  // conv results per row: [0] model, [1] d/dshift_x, [2] d/dshift_y, [3+q] partial plane q
+  // conv results per row: [0] model, [1] d/dshift_x, [2] d/dshift_y, [3 + q] partial plane q
   float cv[3 + NGRAD][kConvRows];
 #pragma unroll
   for (int k = 0; k < 3 + NGRAD; ++k)
 #pragma unroll
     for (int o = 0; o < kConvRows; ++o) cv[k][o] = 0.f;
 
-  const int nplanes = jac ? 1 + NGRAD : 1;
   if (b.psf_mode == AP_PSF_NONE) {
 #pragma unroll
     for (int o = 0; o < kConvRows; ++o) {
@@ -853,31 +879,39 @@ __global__ void __launch_bounds__(kConvThreads) k_conv(BatchArgs b, ConvIO io) {
       }
     }
   } else {
-    const int kpx = st.kpx, kpy = st.kpy, kp2 = kpx * kpy;
+    const int kpx = st.kpx, kpy = st.kpy, ks = conv_col_stride(kpy), kstride = kpx * ks;
     const int cx = (kpx - 1) / 2, cy = (kpy - 1) / 2;
     const int TW = kOutTileX + kpx - 1, TH = kOutTileY + kpy - 1;
-    float* K = smem;             // up to 3 kernels
-    float* Tt = smem + 3 * kp2;  // input tile
+    float* KT = smem;                // up to 3 kernels, transposed
+    float* Tt = smem + 3 * kstride;  // input tile
+    const int kp2 = kpx * kpy;
     const float* ksrc = b.spsf + st.spsf_off + (int64_t)slot * 3 * kp2;
     const int nk = (jac && shiftmode) ? 3 : 1;
-    for (int idx = threadIdx.x; idx < nk * kp2; idx += blockDim.x) K[idx] = ksrc[idx];
+    for (int idx = threadIdx.x; idx < nk * kstride; idx += blockDim.x) {
+      const int kk = idx / kstride, rem = idx - kk * kstride, u = rem / ks, v = rem - u * ks;
+      KT[idx] = (v < kpy) ? ksrc[kk * kp2 + v * kpx + u] : 0.f;
+    }
     const int row0 = y0 + st.by - cy, col0 = x0 + st.bx - cx;
     for (int pl = 0; pl < nplanes; ++pl) {
       if (pl > 0 && shiftmode && (pl - 1 == GX || pl - 1 == GY)) continue;
       if (pl > 0 && b.kind != AP_PROFILE_SERSIC && pl - 1 == GN) continue;
       __syncthreads();
       const float* src = b.work + work_plane(b, slot, pl) + st.work_off;
-      for (int idx = threadIdx.x; idx < TW * TH; idx += blockDim.x) {
-        const int r = idx / TW, c = idx - r * TW;
-        const int wr = row0 + r, wc = col0 + c;
-        Tt[idx] = (wr >= 0 && wr < st.wny && wc >= 0 && wc < st.wnx) ? src[(int64_t)wr * st.wnx + wc]
-                                                                      : 0.f;
+      // rows over warps, columns over lanes: coalesced reads, no index division
+      for (int r = tg; r < TH; r += kConvThreads / 32) {
+        const int wr = row0 + r;
+        const bool rok = (wr >= 0 && wr < st.wny);
+        const float* srow = src + (int64_t)wr * st.wnx;
+        for (int c = tx; c < TW; c += 32) {
+          const int wc = col0 + c;
+          Tt[r * TW + c] = (rok && wc >= 0 && wc < st.wnx) ? srow[wc] : 0.f;
+        }
       }
       __syncthreads();
       const int nkp = (pl == 0) ? nk : 1;
       for (int kk = 0; kk < nkp; ++kk) {
         float outv[kConvRows];
-        conv_col(Tt, TW, K + kk * kp2, kpx, kpy, tx, tg * kConvRows, outv);
+        conv_col(Tt, TW, KT + kk * kstride, kpx, kpy, tx, tg * kConvRows, outv);
         const int dst = (pl == 0) ? kk : 3 + (pl - 1);
 #pragma unroll
         for (int o = 0; o < kConvRows; ++o) cv[dst][o] = outv[o];
@@ -896,29 +930,37 @@ __global__ void __launch_bounds__(kConvThreads) k_conv(BatchArgs b, ConvIO io) {
                                 (unsigned long long)nconv);
   }
 
-  const int nfree = b.n_free;
   const bool acc_any = (ops & (OP_CHI2 | OP_HG | OP_RPP)) != 0;
-  float vals[kNacc];
+  const bool do_hg = (ops & OP_HG) != 0, do_rpp = (ops & OP_RPP) != 0;
+  constexpr int NH = NF * (NF + 1) / 2;
+  float a_chi2 = 0.f, a_g[NF > 0 ? NF : 1], a_h[NH > 0 ? NH : 1], a_rpp[NF > 0 ? NF : 1];
 #pragma unroll
-  for (int k = 0; k < kNacc; ++k) vals[k] = 0.f;
-  const int n_hg = (ops & OP_HG) ? nfree + nfree * (nfree + 1) / 2 : 0;
+  for (int k = 0; k < NF; ++k) {
+    a_g[k] = 0.f;
+    a_rpp[k] = 0.f;
+  }
+#pragma unroll
+  for (int k = 0; k < NH; ++k) a_h[k] = 0.f;
   const float d = (float)io.rpp_d;
+  float hf[NF > 0 ? NF : 1];
+  if (do_rpp) {
+#pragma unroll
+    for (int k = 0; k < NF; ++k) hf[k] = (float)io.hvec[s * NPARAM + k];
+  }
 
 #pragma unroll
   for (int o = 0; o < kConvRows; ++o) {
     const int y = yb + o;
-    const bool valid = (x < st.nx) && (y < st.ny);
-    if (!valid) continue;
+    if (!(x < st.nx && y < st.ny)) continue;
     const float mgal = cv[0][o];
     const float m = mgal + e.sky;
-    // model and value-space Jacobian in full-vector order, compacted to the fitted slots
-    float Jc[NPARAM];
-    int nf = 0;
+    // value-space Jacobian in full-vector order, compacted to the fitted slots
+    float Jc[NF > 0 ? NF : 1];
     if (jac) {
       float J[NPARAM];
       if (shiftmode) {
-        J[PX] = cv[1][o] * (float)st.Pinv[0] + cv[2][o] * (float)st.Pinv[2];
-        J[PY] = cv[1][o] * (float)st.Pinv[1] + cv[2][o] * (float)st.Pinv[3];
+        J[PX] = cv[1][o] * st.Pinvf[0] + cv[2][o] * st.Pinvf[2];
+        J[PY] = cv[1][o] * st.Pinvf[1] + cv[2][o] * st.Pinvf[3];
       } else {
         J[PX] = -cv[3 + GX][o];
         J[PY] = -cv[3 + GY][o];
@@ -929,42 +971,69 @@ __global__ void __launch_bounds__(kConvThreads) k_conv(BatchArgs b, ConvIO io) {
       J[PRE] = cv[3 + GRE][o];
       J[PIE] = kLn10f * mgal;
       J[PF] = kLn10f * e.sky;
+      int nf = 0;
 #pragma unroll
       for (int k = 0; k < NPARAM; ++k) {
-        if (b.free_mask & (1 << k)) Jc[nf++] = (ops & OP_REP) ? J[k] * e.drep[k] : J[k];
+        const float v = (ops & OP_REP) ? J[k] * e.drep[k] : J[k];
+        if (b.free_mask & (1 << k)) {
+#pragma unroll
+          for (int c = 0; c < NF; ++c)
+            if (c == nf) Jc[c] = v;
+          ++nf;
+        }
       }
     }
     const int64_t op = st.out_off + (int64_t)y * st.nx + x;
     if (ops & OP_WRITE_MODEL) io.model_out[op] = m;
     if (jac && (ops & OP_WRITE_JAC)) {
-      for (int k = 0; k < nf; ++k) io.jac_out[(int64_t)k * b.out_pixels + op] = Jc[k];
+#pragma unroll
+      for (int k = 0; k < NF; ++k) io.jac_out[(int64_t)k * b.out_pixels + op] = Jc[k];
     }
     if (!acc_any) continue;
     // fused reductions (fit/lm.py:374-406); masked pixels are left out entirely
     if (io.mask && io.mask[op]) continue;
     const float w = io.weight ? io.weight[op] : 1.f;
     const float r = io.data[op] - m;
-    vals[0] += w * r * r;  // chi2
-    int nv = 1;
-    if (ops & OP_HG) {
-      for (int k = 0; k < nfree; ++k) vals[nv++] += Jc[k] * w * r;
-      for (int a = 0; a < nfree; ++a)
-        for (int c = a; c < nfree; ++c) vals[nv++] += Jc[a] * w * Jc[c];
+    a_chi2 += w * r * r;
+    if (do_hg) {
+      int h = 0;
+#pragma unroll
+      for (int a = 0; a < NF; ++a) {
+        const float wja = w * Jc[a];
+        a_g[a] += wja * r;
+#pragma unroll
+        for (int c = a; c < NF; ++c) a_h[h++] += wja * Jc[c];
+      }
     }
-    if (ops & OP_RPP) {
-      float Jb[NPARAM];
+    if (do_rpp) {
+      float Jb[NF > 0 ? NF : 1];
       float jh = 0.f;
-      for (int k = 0; k < nfree; ++k) {
+#pragma unroll
+      for (int k = 0; k < NF; ++k) {
         Jb[k] = io.jbase[(int64_t)k * b.out_pixels + op];
-        jh = fmaf(Jb[k], (float)io.hvec[s * NPARAM + k], jh);
+        jh = fmaf(Jb[k], hf[k], jh);
       }
       // (2/d) * ((rh - r)/d - W (J h)),  rh - r = W (Y1 - Y0)
       const float ebase = (2.f / d) * ((w * (m - io.y0[op])) / d - w * jh);
-      for (int k = 0; k < nfree; ++k) vals[nv++] += Jb[k] * ebase;
+#pragma unroll
+      for (int k = 0; k < NF; ++k) a_rpp[k] += Jb[k] * ebase;
     }
   }
   if (!acc_any) return;
-  int nv = 1 + n_hg + ((ops & OP_RPP) ? nfree : 0);
+  // accumulator order: chi2, [g (NF), H upper (NH)], [rpp (NF)]
+  float vals[1 + 2 * NF + NH];
+  int nv = 0;
+  vals[nv++] = a_chi2;
+  if (do_hg) {
+#pragma unroll
+    for (int k = 0; k < NF; ++k) vals[nv++] = a_g[k];
+#pragma unroll
+    for (int k = 0; k < NH; ++k) vals[nv++] = a_h[k];
+  }
+  if (do_rpp) {
+#pragma unroll
+    for (int k = 0; k < NF; ++k) vals[nv++] = a_rpp[k];
+  }
   __shared__ float shred[kConvWarps * kNacc];
   conv_tile_reduce(vals, nv, tacc, shred);
 }
@@ -1055,7 +1124,16 @@ cudaError_t launch_eval_setup(const BatchArgs& b, const double* params, int64_t 
 }
 
 cudaError_t set_conv_smem(size_t bytes) {
-  return cudaFuncSetAttribute(k_conv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  cudaError_t e = cudaSuccess;
+  const int nb = (int)bytes;
+  auto set = [&](const void* f) {
+    const cudaError_t r = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, nb);
+    if (r != cudaSuccess) e = r;
+  };
+  set((const void*)k_conv<0>); set((const void*)k_conv<1>); set((const void*)k_conv<2>);
+  set((const void*)k_conv<3>); set((const void*)k_conv<4>); set((const void*)k_conv<5>);
+  set((const void*)k_conv<6>); set((const void*)k_conv<7>); set((const void*)k_conv<8>);
+  return e;
 }
 
 cudaError_t launch_render_pass(const BatchArgs& b, const ConvIO& io, size_t conv_smem,
@@ -1072,6 +1150,8 @@ cudaError_t launch_render_pass(const BatchArgs& b, const ConvIO& io, size_t conv
   }
   t = B(KC_SAMPLE);
   k_sample<<<dim3(b.n_work_tiles, 2), kTile * kTile, 0, s>>>(b);
+  if (b.kind == AP_PROFILE_EXPONENTIAL && b.integrate == AP_INTEGRATE_THRESHOLD)
+    k_exp_threshold<<<(b.n_stamps * 2 + 127) / 128, 128, 0, s>>>(b);
   E(t);
   if (b.integrate == AP_INTEGRATE_THRESHOLD) {
     int dev = 0, nsm = 0;
@@ -1086,7 +1166,18 @@ cudaError_t launch_render_pass(const BatchArgs& b, const ConvIO& io, size_t conv
     E(t);
   }
   t = B(KC_CONV);
-  k_conv<<<dim3(b.n_out_tiles, 2), kConvThreads, conv_smem, s>>>(b, io);
+  const dim3 cgrid(b.n_out_tiles, 2);
+  switch (b.n_free) {
+    case 0: k_conv<0><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
+    case 1: k_conv<1><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
+    case 2: k_conv<2><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
+    case 3: k_conv<3><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
+    case 4: k_conv<4><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
+    case 5: k_conv<5><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
+    case 6: k_conv<6><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
+    case 7: k_conv<7><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
+    default: k_conv<8><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
+  }
   E(t);
   if (accumulate) {
     t = B(KC_REDUCE);

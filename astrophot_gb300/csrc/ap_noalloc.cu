@@ -158,6 +158,10 @@ extern "C" int ap_render_noalloc(int32_t nx, int32_t ny, int32_t psf_kx, int32_t
   st.ref_xy[0] = geometry[6];
   st.ref_xy[1] = geometry[7];
   st.pixel_area = std::fabs(det);
+  for (int k = 0; k < 4; ++k) {
+    st.Pf[k] = (float)st.P[k];
+    st.Pinvf[k] = (float)st.Pinv[k];
+  }
   st.ntw_x = (st.wnx + kTile - 1) / kTile;
   st.ntw = st.ntw_x * ((st.wny + kTile - 1) / kTile);
   st.nto_x = (nx + kOutTileX - 1) / kOutTileX;
@@ -209,6 +213,8 @@ extern "C" int ap_render_noalloc(int32_t nx, int32_t ny, int32_t psf_kx, int32_t
     T.sub_center = (k * k) / 2;
     na_fill_quad(k, T.sx, T.sy, T.sw);
   }
+
+  quad_tables_fill_f32(T);
 
   // ---- scratch layout; refuse what does not fit ----------------------------------------------
   int64_t o = 0;

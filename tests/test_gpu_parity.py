@@ -176,9 +176,22 @@ def lm_case_problem(d):
     return GroupProblem([gal, sky], Window.from_scale(size, size), PSF(d["psf"]), d["data"], d["weight"])
 
 
+def parameter_sigma(d):
+    """1-sigma statistical uncertainty of the reference's fitted representation vector:
+    sqrt(diag((J^T W J)^-1)) from the oracle's Jacobian at that solution."""
+    prob = lm_case_problem(d)
+    J = prob.jacobian(d["res"])
+    W = d["weight"].reshape(-1)
+    H = J.T @ (W[:, None] * J)
+    return np.sqrt(np.diag(np.linalg.inv(H)))
+
+
 @pytest.mark.parametrize("name", cases.lm_case_names())
 @pytest.mark.parametrize("graph", [False, True])
 def test_lm_matches_reference(N, name, graph):
+    """Final chi2/ndf within 1e-4 of the reference's; fitted vector within 0.25 sigma of the
+    reference's (its own stopping rule, chi2 change < 1e-5, leaves that much freedom along the
+    valley floor; the FP32 render changes where the last accepted step lands)."""
     d = cases.load_lm(name)
     size = d["spec"]["size"]
     opts = N.make_options(profile="sersic", psf_mode="full", free_mask=0x7F, has_sky=True)
@@ -196,10 +209,12 @@ def test_lm_matches_reference(N, name, graph):
     ref_chi2 = d["loss_history"].min()
     assert abs(chi2.item() / ref_chi2 - 1) <= 1e-4
     res = state.cpu().numpy()[0]
-    assert np.all(np.abs(res - d["res"]) <= 1e-3 * (1 + np.abs(d["res"])))
+    sig = parameter_sigma(d)
+    dev = np.abs(res - d["res"]) / sig
+    print(name, "fitted vector offset in sigma", np.round(dev, 4), "relative", np.abs(res - d["res"]) / np.abs(d["res"]))
+    assert np.all(dev <= 0.25), dev
     # the trajectory follows the reference's until the chi2 changes reach FP32 resolution
     loss, L, xs = b.lm_history()
-    nh = min(len(d["loss_history"]), int(iters.item()) + 1)
     assert np.allclose(loss[0, :3].cpu().numpy(), d["loss_history"][:3], rtol=1e-6)
     assert status.item() in (N.LM_SUCCESS, N.LM_IMMOBILE, N.LM_NO_STEP)
 
