@@ -17,7 +17,8 @@ constexpr int64_t kAlign = 256;
 int64_t align_up(int64_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
 
 struct Layout {
-  int64_t stamps, evals, work_tiles, out_tiles, tables, work, aux, spsf, queue, recheck, counters,
+  int64_t stamps, evals, work_tiles, out_tiles, tables, work, aux, spsf, queue, recheck, wlist,
+      olist, slist, counters,
       work_ctr, mean_acc, tile_acc, acc, total;
 };
 
@@ -347,6 +348,9 @@ int ap_batch_create(ap_batch** out, int32_t n, const int32_t* nx, const int32_t*
   L.spsf = take(sizeof(float) * std::max<int64_t>(b->spsf_total, 1));
   L.queue = take(sizeof(int64_t) * 2 * b->work_pixels);
   L.recheck = take(sizeof(int64_t) * 2 * b->work_pixels);
+  L.wlist = take(sizeof(int64_t) * 2 * (int64_t)b->work_tiles.size());
+  L.olist = take(sizeof(int64_t) * 2 * (int64_t)b->out_tiles.size());
+  L.slist = take(sizeof(int32_t) * 2 * (int64_t)n);
   L.counters = take(sizeof(uint32_t) * 16);
   L.work_ctr = take(sizeof(unsigned long long) * 4);
   L.mean_acc = take(sizeof(double) * 2 * (int64_t)n);
@@ -425,6 +429,9 @@ int ap_batch_bind(ap_batch* b, void* workspace, int64_t bytes, ap_stream_t strea
   A.spsf = (float*)(ws + L.spsf);
   A.queue = (int64_t*)(ws + L.queue);
   A.recheck = (int64_t*)(ws + L.recheck);
+  A.wlist = (int64_t*)(ws + L.wlist);
+  A.olist = (int64_t*)(ws + L.olist);
+  A.slist = (int32_t*)(ws + L.slist);
   A.counters = (uint32_t*)(ws + L.counters);
   A.work_ctr = (unsigned long long*)(ws + L.work_ctr);
   A.mean_acc = (double*)(ws + L.mean_acc);

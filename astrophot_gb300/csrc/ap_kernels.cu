@@ -11,6 +11,7 @@
 //   fft/direct convolve   astrophot/models/_model_methods.py:245-257, utils/operations.py:9-36
 //   crop                  astrophot/models/model_object.py:345-349
 //   chi2, hess, grad, rpp astrophot/fit/lm.py:374-406
+#include <algorithm>
 #include <cmath>
 
 #include "ap_internal.h"
@@ -64,6 +65,11 @@ __global__ void k_eval_setup(BatchArgs b, const double* params, int64_t stamp_st
     b.counters[0] = 0;  // queue length
     b.counters[1] = 0;  // queue head
     b.counters[5] = 0;  // recheck length
+    b.counters[7] = 0;  // active working tiles
+    b.counters[8] = 0;  // active output tiles
+    b.counters[9] = 0;  // active (stamp, slot) pairs
+    b.counters[10] = 0; // level-2 integration queue length
+    b.counters[11] = 0; // convolve-pass tile head
   }
   if (t >= b.n_stamps * 2) return;
   const int s = t >> 1, slot = t & 1;
@@ -131,6 +137,28 @@ __global__ void k_eval_setup(BatchArgs b, const double* params, int64_t stamp_st
   for (int i = 0; i < NPARAM; ++i) e.drep[i] = (float)drep_from_value(i, v[i]);
 }
 
+// Compacted work lists of this pass: the tiles of active (stamp, slot) pairs only, so the
+// pixel kernels (persistent grid-stride loops) never visit idle stamps.
+__global__ void k_build_lists(BatchArgs b) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= b.n_stamps * 2) return;
+  if (!b.evals[t].ops) return;
+  const int s = t >> 1, slot = t & 1;
+  const StampDev& st = b.stamps[s];
+  const int64_t key = ((int64_t)slot << 62) | ((int64_t)s << 32);
+  const uint32_t w0 = atomicAdd(&b.counters[7], (unsigned)st.ntw);
+  for (int k = 0; k < st.ntw; ++k) b.wlist[w0 + k] = key | k;
+  const uint32_t o0 = atomicAdd(&b.counters[8], (unsigned)st.nto);
+  for (int k = 0; k < st.nto; ++k) b.olist[o0 + k] = key | k;
+  b.slist[atomicAdd(&b.counters[9], 1u)] = t;
+}
+
+__device__ __forceinline__ void unpack_entry(int64_t ent, int& slot, int& s, int& local) {
+  slot = (int)(ent >> 62);
+  s = (int)((ent >> 32) & 0x3fffffff);
+  local = (int)(ent & 0xffffffffll);
+}
+
 // ---------------------------------------------------------------------------
 // PSF shift (bilinear interp2d of the 1-padded PSF) and renormalisation, with d/d shift
 // ---------------------------------------------------------------------------
@@ -173,15 +201,14 @@ __device__ double block_sum_d(double v, double* sh) {
   return t;
 }
 
-__global__ void k_psf_shift(BatchArgs b, const float* psf) {
-  const int s = blockIdx.x, slot = blockIdx.y;
+__device__ void psf_shift_one(const BatchArgs& b, const float* psf, int s, int slot) {
   const EvalDev& e = b.evals[s * 2 + slot];
-  if (!e.ops) return;
   const StampDev& st = b.stamps[s];
   const int kp2 = st.kpx * st.kpy;
   const float* P = psf + st.psf_off;
   float* out = b.spsf + st.spsf_off + (int64_t)slot * 3 * kp2;
   __shared__ double sh[32];
+  __syncthreads();  // sh reuse across the persistent loop
   const bool jac = (e.ops & OP_JAC) != 0;
   if (b.psf_mode == AP_PSF_FULL) {
     double S = 0, Sx = 0, Sy = 0;
@@ -209,6 +236,14 @@ __global__ void k_psf_shift(BatchArgs b, const float* psf) {
     for (int idx = threadIdx.x; idx < kp2; idx += blockDim.x) S += (double)P[idx];
     S = block_sum_d(S, sh);
     for (int idx = threadIdx.x; idx < kp2; idx += blockDim.x) out[idx] = (float)((double)P[idx] / S);
+  }
+}
+
+__global__ void k_psf_shift(BatchArgs b, const float* psf) {
+  const uint32_t n = b.counters[9];
+  for (uint32_t it = blockIdx.x; it < n; it += gridDim.x) {
+    const int t = b.slist[it];
+    psf_shift_one(b, psf, t >> 1, t & 1);
   }
 }
 
@@ -295,6 +330,7 @@ __device__ void sample_tile(const BatchArgs& b, int s, int slot, int tile_local)
     // sum(deep) for the default _integrate_reference (models/_model_methods.py:151-152)
     float v = warp_sum(valid ? deep : 0.f);
     __shared__ float sh[kTile * kTile / 32];
+    __syncthreads();  // sh reuse across the persistent loop
     if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -306,15 +342,15 @@ __device__ void sample_tile(const BatchArgs& b, int s, int slot, int tile_local)
 }
 
 __global__ void __launch_bounds__(256) k_sample(BatchArgs b) {
-  const int tile = blockIdx.x, slot = blockIdx.y;
-  const int s = b.work_tiles[tile];
-  const EvalDev& e = b.evals[s * 2 + slot];
-  if (!e.ops) return;
-  const int local = tile - b.stamps[s].tile_w0;
-  if (e.ops & OP_JAC)
-    sample_tile<true>(b, s, slot, local);
-  else
-    sample_tile<false>(b, s, slot, local);
+  const uint32_t n = b.counters[7];
+  for (uint32_t it = blockIdx.x; it < n; it += gridDim.x) {
+    int slot, s, local;
+    unpack_entry(b.wlist[it], slot, s, local);
+    if (b.evals[s * 2 + slot].ops & OP_JAC)
+      sample_tile<true>(b, s, slot, local);
+    else
+      sample_tile<false>(b, s, slot, local);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -341,13 +377,9 @@ __global__ void k_exp_threshold(BatchArgs b) {
   e.thresh = (float)e.thresh64;
 }
 
-__global__ void __launch_bounds__(256) k_select(BatchArgs b) {
-  const int tile = blockIdx.x, slot = blockIdx.y;
-  const int s = b.work_tiles[tile];
+__device__ __forceinline__ void select_tile(const BatchArgs& b, int slot, int s, int local) {
   const EvalDev& e = b.evals[s * 2 + slot];
-  if (!e.ops) return;  // uniform per block
   const StampDev& st = b.stamps[s];
-  const int local = tile - st.tile_w0;
   const int i = (local % st.ntw_x) * kTile + (threadIdx.x & (kTile - 1));
   const int j = (local / st.ntw_x) * kTile + threadIdx.x / kTile;
   const bool valid = (i < st.wnx) && (j < st.wny);
@@ -423,6 +455,15 @@ __global__ void __launch_bounds__(256) k_select(BatchArgs b) {
   }
 }
 
+__global__ void __launch_bounds__(256) k_select(BatchArgs b) {
+  const uint32_t n = b.counters[7];
+  for (uint32_t it = blockIdx.x; it < n; it += gridDim.x) {
+    int slot, s, local;
+    unpack_entry(b.wlist[it], slot, s, local);
+    select_tile(b, slot, s, local);
+  }
+}
+
 // Selection of the pixels the FP32 bound could not settle, one pixel per thread in float64
 // (the FP64 pipe retires whole-warp instructions, so the work is packed densely here).
 __global__ void __launch_bounds__(256) k_recheck(BatchArgs b) {
@@ -488,13 +529,14 @@ struct QuadResult {
 };
 
 // One (sub-)pixel integrated by this lane alone: Q^2 samples at unit offsets
-// (ci + qx / scale, cj + qy / scale) with amplitude scale area.
-template <bool JAC>
+// (ci + qx / scale, cj + qy / scale) with amplitude scale area.  QC > 0 fixes the quadrature
+// level at compile time (the sample loop unrolls into independent evaluations).
+template <bool JAC, int QC>
 __device__ __forceinline__ QuadResult quad_lane(const BatchArgs& b, const StampDev& st,
                                                 const EvalDev& e, float ci, float cj, float inv_g,
                                                 float area) {
   const QuadTables& T = *b.tables;
-  const int n = T.quad_level * T.quad_level;
+  const int n = QC > 0 ? QC * QC : T.quad_level * T.quad_level;
   const int mid = n / 2;
   QuadResult r;
   r.res = 0.f;
@@ -504,7 +546,9 @@ __device__ __forceinline__ QuadResult quad_lane(const BatchArgs& b, const StampD
 #pragma unroll
   for (int q = 0; q < NGRAD; ++q) r.g[q] = 0.f;
   float referr = 0.f;
-  for (int k = 0; k < n; ++k) {
+#pragma unroll
+  for (int k = 0; k < (QC > 0 ? QC * QC : kMaxQuad * kMaxQuad); ++k) {
+    if (QC == 0 && k >= n) break;
     float X, Y;
     pix_to_offset(st, e, ci + T.qxf[k] * inv_g, cj + T.qyf[k] * inv_g, X, Y);
     const Sample sm = eval_profile<JAC>(e, b.kind, X, Y, area);
@@ -565,149 +609,157 @@ __device__ __forceinline__ bool decide(const BatchArgs& b, const StampDev& st, c
   return refine64(b, st, e, i, j, m, e.thresh64 * (double)(g * g));
 }
 
-template <bool JAC>
-__device__ void integrate_entry(const BatchArgs& b, int slot, int s, int64_t p, int lane,
-                                unsigned long long& samples, int& n64) {
+__device__ __forceinline__ void write_deep(const BatchArgs& b, const StampDev& st, int slot,
+                                           int64_t p, float v, const float* g, bool jac) {
+  const int64_t wp = st.work_off + p;
+  b.work[work_plane(b, slot, 0) + wp] = v;
+  if (jac) {
+#pragma unroll
+    for (int q = 0; q < NGRAD; ++q) b.work[work_plane(b, slot, 1 + q) + wp] = g[q];
+  }
+}
+
+// Level 1 of grid_integrate, one queued pixel per thread: the Q x Q Gauss-Legendre
+// integral and its refinement decision.  Pixels that stop here are written; the others go
+// to the level-2 queue (b.recheck, emptied by k_recheck before this kernel runs).
+template <int QC>
+__device__ __forceinline__ void level1_pixel(const BatchArgs& b, int64_t ent, bool& push,
+                                             int& n64) {
+  const int slot = (int)(ent >> 62);
+  const int s = (int)((ent >> 32) & 0x3fffffff);
+  const int64_t p = ent & 0xffffffffll;
+  const StampDev& st = b.stamps[s];
+  const EvalDev& e = b.evals[s * 2 + slot];
+  const int i = (int)(p % st.wnx), j = (int)(p / st.wnx);
+  const float di = (float)(i - e.cix), dj = (float)(j - e.cjy);
+  const bool jac = (e.ops & OP_JAC) != 0;
+  QuadResult r = jac ? quad_lane<true, QC>(b, st, e, di, dj, 1.f, 1.f)
+                     : quad_lane<false, QC>(b, st, e, di, dj, 1.f, 1.f);
+  bool split = false;
+  if (b.max_depth > 1) {
+    const float thr = e.thresh;
+    const float diff = fabsf(r.res - r.ref);
+    const float band = 1.5f * r.errb + 4.f * kEps * thr;
+    split = diff > thr + band;
+    if (!split && diff >= thr - band) {
+      ++n64;
+      split = refine64(b, st, e, i, j, -1, e.thresh64);
+    }
+  }
+  if (split)
+    push = true;
+  else
+    write_deep(b, st, slot, p, r.res, r.g, jac);
+}
+
+__global__ void __launch_bounds__(256) k_level1(BatchArgs b) {
+  const uint32_t n = min((uint32_t)b.counters[0], (uint32_t)(2 * b.work_pixels));
+  const int Q = b.tables->quad_level;
+  const int lane = threadIdx.x & 31;
+  int n64 = 0;
+  uint32_t pushed = 0;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    const uint32_t idx = base + threadIdx.x;
+    bool push = false;
+    int64_t ent = 0;
+    if (idx < n) {
+      ent = b.queue[idx];
+      if (Q == 3)
+        level1_pixel<3>(b, ent, push, n64);
+      else
+        level1_pixel<0>(b, ent, push, n64);
+    }
+    const unsigned mask = __ballot_sync(0xffffffffu, push);
+    if (mask) {
+      const int leader = __ffs(mask) - 1;
+      uint32_t qb = 0;
+      if (lane == leader) qb = atomicAdd(&b.counters[10], (unsigned)__popc(mask));
+      qb = __shfl_sync(0xffffffffu, qb, leader);
+      if (push) b.recheck[qb + __popc(mask & ((1u << lane) - 1u))] = ent;
+      pushed += __popc(mask);
+    }
+  }
+  n64 = __reduce_add_sync(0xffffffffu, n64);
+  if (lane == 0 && n64) atomicAdd(&b.counters[6], (unsigned)n64);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const int Qn = b.tables->quad_level;
+    atomicAdd(b.work_ctr + 1, (unsigned long long)n * (unsigned long long)(Qn * Qn));
+  }
+}
+
+// Levels 2 and 3 of grid_integrate for a pixel that level 1 split: one warp per pixel,
+// one sub-pixel per lane; each level-2 sub-pixel flagged for refinement is split again and
+// integrated by the whole warp.
+template <bool JAC, int QC>
+__device__ void level23_pixel(const BatchArgs& b, int slot, int s, int64_t p, int lane,
+                              unsigned long long& samples, int& n64) {
   const StampDev& st = b.stamps[s];
   const EvalDev& e = b.evals[s * 2 + slot];
   const QuadTables& T = *b.tables;
-  const int Q2 = T.quad_level * T.quad_level;
+  const int Q2 = QC > 0 ? QC * QC : T.quad_level * T.quad_level;
   const int g = T.gridding, G2 = g * g;
   const int i = (int)(p % st.wnx), j = (int)(p / st.wnx);
   const float di = (float)(i - e.cix), dj = (float)(j - e.cjy);
   const float thr = e.thresh;
   const float ginv = 1.f / (float)g;
-
-  int n_samples = Q2;
-  // level 1: Q^2 samples spread over the lanes
-  float v = 0.f, gv[NGRAD];
+  const float area2 = ginv * ginv;
+  int n_samples = G2 * Q2;
+  QuadResult r2;
+  r2.res = 0.f;
 #pragma unroll
-  for (int q = 0; q < NGRAD; ++q) gv[q] = 0.f;
-  float f = 0.f, fe = 0.f, fa = 0.f;
-  if (lane < Q2) {
-    float X, Y;
-    pix_to_offset(st, e, di + T.qxf[lane], dj + T.qyf[lane], X, Y);
-    const Sample sm = eval_profile<JAC>(e, b.kind, X, Y, 1.f);
-    const float w = T.qwf[lane];
-    f = sm.v;
-    v = w * sm.v;
-    fa = fabsf(v);
-    fe = fa * sample_rel_err(e, sm.arg);
+  for (int q = 0; q < NGRAD; ++q) r2.g[q] = 0.f;
+  float ci2 = 0.f, cj2 = 0.f;
+  bool split2 = false;
+  if (lane < G2) {
+    ci2 = di + T.gxf[lane];
+    cj2 = dj + T.gyf[lane];
+    r2 = quad_lane<JAC, QC>(b, st, e, ci2, cj2, ginv, area2);
+    if (b.max_depth > 2) split2 = decide(b, st, e, r2, thr * (float)G2, i, j, lane, n64);
+  }
+  // level 3: refine each flagged sub-pixel with the whole warp
+  unsigned todo = __ballot_sync(0xffffffffu, split2);
+  n_samples += __popc(todo) * G2 * Q2;
+  const float area3 = area2 * area2;
+  while (todo) {
+    const int m = __ffs(todo) - 1;
+    todo &= todo - 1;
+    const float cim = __shfl_sync(0xffffffffu, ci2, m);
+    const float cjm = __shfl_sync(0xffffffffu, cj2, m);
+    QuadResult r3;
+    r3.res = 0.f;
+#pragma unroll
+    for (int q = 0; q < NGRAD; ++q) r3.g[q] = 0.f;
+    if (lane < G2) {
+      r3 = quad_lane<JAC, QC>(b, st, e, cim + T.gxf[lane] * ginv, cjm + T.gyf[lane] * ginv,
+                              ginv * ginv, area3);
+    }
+    const float s3 = warp_sum(r3.res);
+    float gs3[NGRAD];
     if (JAC) {
 #pragma unroll
-      for (int q = 0; q < NGRAD; ++q) gv[q] = w * sm.g[q];
+      for (int q = 0; q < NGRAD; ++q) gs3[q] = warp_sum(r3.g[q]);
     }
-  }
-  const float res1 = warp_sum(v);
-  float gres1[NGRAD];
-  if (JAC) {
-#pragma unroll
-    for (int q = 0; q < NGRAD; ++q) gres1[q] = warp_sum(gv[q]);
-  }
-  float out_v = res1;
-  float out_g[NGRAD];
-#pragma unroll
-  for (int q = 0; q < NGRAD; ++q) out_g[q] = JAC ? gres1[q] : 0.f;
-
-  if (b.max_depth > 1) {
-    const float ref1 = __shfl_sync(0xffffffffu, f, Q2 / 2);
-    const float ref1e = __shfl_sync(0xffffffffu, fe / fmaxf(fabsf(v), 1e-38f) * fabsf(f), Q2 / 2);
-    QuadResult r1;
-    r1.res = res1;
-    r1.ref = ref1;
-    r1.mag = warp_sum(fa);
-    r1.errb = warp_sum(fe) + ref1e + 2.f * Q2 * kEps * (r1.mag + fabsf(ref1));
-    // level-1 decision (warp-uniform): FP32 when clear of the band, else float64 samples,
-    // one per lane
-    const float diff1 = fabsf(r1.res - r1.ref);
-    const float band1 = 1.5f * r1.errb + 4.f * kEps * thr;
-    bool split = diff1 > thr + band1;
-    if (!split && diff1 >= thr - band1) {
-      double f64 = 0.0, wf64 = 0.0;
-      if (lane < Q2) {
-        double X, Y;
-        pix_to_offset64(st, e, (double)(i - e.cix) + T.qx[lane], (double)(j - e.cjy) + T.qy[lane], X, Y);
-        f64 = eval_profile64(e, b.kind, X, Y, 1.0);
-        wf64 = f64 * T.qw[lane];
-      }
-      double res64 = wf64;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) res64 += __shfl_xor_sync(0xffffffffu, res64, o);
-      const double ref64 = __shfl_sync(0xffffffffu, f64, Q2 / 2);
-      split = fabs(res64 - ref64) > e.thresh64;
-      if (lane == 0) ++n64;
-    }
-    if (split) {
-      n_samples += G2 * Q2;
-      // level 2: one sub-pixel per lane
-      const float area2 = ginv * ginv;
-      QuadResult r2;
-      r2.res = 0.f;
-#pragma unroll
-      for (int q = 0; q < NGRAD; ++q) r2.g[q] = 0.f;
-      float ci2 = 0.f, cj2 = 0.f;
-      bool split2 = false;
-      if (lane < G2) {
-        ci2 = di + T.gxf[lane];
-        cj2 = dj + T.gyf[lane];
-        r2 = quad_lane<JAC>(b, st, e, ci2, cj2, ginv, area2);
-        if (b.max_depth > 2) {
-          split2 = decide(b, st, e, r2, thr * (float)G2, i, j, lane, n64);
-        }
-      }
-      // level 3: refine each flagged sub-pixel with the whole warp
-      unsigned todo = __ballot_sync(0xffffffffu, split2);
-      n_samples += __popc(todo) * G2 * Q2;
-      const float area3 = area2 * area2;
-      while (todo) {
-        const int m = __ffs(todo) - 1;
-        todo &= todo - 1;
-        const float cim = __shfl_sync(0xffffffffu, ci2, m);
-        const float cjm = __shfl_sync(0xffffffffu, cj2, m);
-        QuadResult r3;
-        r3.res = 0.f;
-#pragma unroll
-        for (int q = 0; q < NGRAD; ++q) r3.g[q] = 0.f;
-        if (lane < G2) {
-          r3 = quad_lane<JAC>(b, st, e, cim + T.gxf[lane] * ginv,
-                              cjm + T.gyf[lane] * ginv, ginv * ginv, area3);
-        }
-        const float s3 = warp_sum(r3.res);
-        float gs3[NGRAD];
-        if (JAC) {
-#pragma unroll
-          for (int q = 0; q < NGRAD; ++q) gs3[q] = warp_sum(r3.g[q]);
-        }
-        if (lane == m) {
-          r2.res = s3;
-          if (JAC) {
-#pragma unroll
-            for (int q = 0; q < NGRAD; ++q) r2.g[q] = gs3[q];
-          }
-        }
-      }
-      out_v = warp_sum(lane < G2 ? r2.res : 0.f);
+    if (lane == m) {
+      r2.res = s3;
       if (JAC) {
 #pragma unroll
-        for (int q = 0; q < NGRAD; ++q) out_g[q] = warp_sum(lane < G2 ? r2.g[q] : 0.f);
+        for (int q = 0; q < NGRAD; ++q) r2.g[q] = gs3[q];
       }
     }
   }
-  samples += (unsigned long long)n_samples;
-  if (lane == 0) {
-    const int64_t wp = st.work_off + p;
-    b.work[work_plane(b, slot, 0) + wp] = out_v;
-    if (JAC) {
+  const float out_v = warp_sum(lane < G2 ? r2.res : 0.f);
+  float out_g[NGRAD];
 #pragma unroll
-      for (int q = 0; q < NGRAD; ++q) b.work[work_plane(b, slot, 1 + q) + wp] = out_g[q];
-    }
-  }
+  for (int q = 0; q < NGRAD; ++q) out_g[q] = JAC ? warp_sum(lane < G2 ? r2.g[q] : 0.f) : 0.f;
+  samples += (unsigned long long)n_samples;
+  if (lane == 0) write_deep(b, st, slot, p, out_v, out_g, JAC);
 }
 
 __global__ void __launch_bounds__(256) k_integrate(BatchArgs b) {
   const int lane = threadIdx.x & 31;
-  constexpr uint32_t kChunk = 4;  // queue entries grabbed per atomic
-  const uint32_t n = min((uint32_t)b.counters[0], (uint32_t)(2 * b.work_pixels));
+  constexpr uint32_t kChunk = 2;  // queue entries grabbed per atomic
+  const uint32_t n = min((uint32_t)b.counters[10], (uint32_t)(2 * b.work_pixels));
+  const int Q = b.tables->quad_level;
   unsigned long long samples = 0;
   int n64 = 0;
   while (true) {
@@ -717,14 +769,22 @@ __global__ void __launch_bounds__(256) k_integrate(BatchArgs b) {
     if (idx0 >= n) break;
     const uint32_t idx1 = min(idx0 + kChunk, n);
     for (uint32_t idx = idx0; idx < idx1; ++idx) {
-      const int64_t ent = b.queue[idx];
+      const int64_t ent = b.recheck[idx];
       const int slot = (int)(ent >> 62);
       const int s = (int)((ent >> 32) & 0x3fffffff);
       const int64_t p = ent & 0xffffffffll;
-      if (b.evals[s * 2 + slot].ops & OP_JAC)
-        integrate_entry<true>(b, slot, s, p, lane, samples, n64);
-      else
-        integrate_entry<false>(b, slot, s, p, lane, samples, n64);
+      const bool jac = (b.evals[s * 2 + slot].ops & OP_JAC) != 0;
+      if (Q == 3) {
+        if (jac)
+          level23_pixel<true, 3>(b, slot, s, p, lane, samples, n64);
+        else
+          level23_pixel<false, 3>(b, slot, s, p, lane, samples, n64);
+      } else {
+        if (jac)
+          level23_pixel<true, 0>(b, slot, s, p, lane, samples, n64);
+        else
+          level23_pixel<false, 0>(b, slot, s, p, lane, samples, n64);
+      }
     }
   }
   // per-warp totals: the sample count is warp-uniform, the FP64 re-decisions are per lane
@@ -841,16 +901,12 @@ __device__ __noinline__ void conv_col(const float* Tt, int TW, const float* KT, 
 // Convolve/accumulate pass.  NF = number of fitted parameters (compile time, so the
 // per-pixel J^T W J accumulators stay in registers).
 template <int NF>
-__global__ void __launch_bounds__(kConvThreads) k_conv(BatchArgs b, ConvIO io) {
-  extern __shared__ __align__(16) float smem[];
-  const int tile = blockIdx.x, slot = blockIdx.y;
-  const int s = b.out_tiles[tile];
+__device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, float* smem,
+                                          float* shred, int slot, int s, int local) {
   const EvalDev& e = b.evals[s * 2 + slot];
   const int ops = e.ops;
-  double* tacc = b.tile_acc + ((int64_t)tile * 2 + slot) * kNacc;
-  if (!ops) return;  // uniform per block
   const StampDev& st = b.stamps[s];
-  const int local = tile - st.tile_o0;
+  double* tacc = b.tile_acc + ((int64_t)(st.tile_o0 + local) * 2 + slot) * kNacc;
   const int tx = threadIdx.x & 31, tg = threadIdx.x >> 5;
   const int x0 = (local % st.nto_x) * kOutTileX, y0 = (local / st.nto_x) * kOutTileY;
   const int x = x0 + tx, yb = y0 + tg * kConvRows;
@@ -1034,23 +1090,46 @@ __global__ void __launch_bounds__(kConvThreads) k_conv(BatchArgs b, ConvIO io) {
 #pragma unroll
     for (int k = 0; k < NF; ++k) vals[nv++] = a_rpp[k];
   }
-  __shared__ float shred[kConvWarps * kNacc];
   conv_tile_reduce(vals, nv, tacc, shred);
+}
+
+template <int NF>
+__global__ void __launch_bounds__(kConvThreads) k_conv(BatchArgs b, ConvIO io) {
+  extern __shared__ __align__(16) float smem[];
+  __shared__ float shred[kConvWarps * kNacc];
+  __shared__ uint32_t next;
+  const uint32_t n = b.counters[8];
+  // tiles are fetched dynamically: their cost varies with the PSF size of their stamp
+  while (true) {
+    if (threadIdx.x == 0) next = atomicAdd(&b.counters[11], 1u);
+    __syncthreads();
+    const uint32_t it = next;
+    if (it >= n) break;
+    int slot, s, local;
+    unpack_entry(b.olist[it], slot, s, local);
+    conv_tile<NF>(b, io, smem, shred, slot, s, local);
+    __syncthreads();  // smem / shred / next reuse by the next tile
+  }
 }
 
 // per-stamp sums of the tile partials (fixed order: deterministic)
 __global__ void k_reduce_acc(BatchArgs b) {
-  const int s = blockIdx.x, slot = blockIdx.y;
-  const EvalDev& e = b.evals[s * 2 + slot];
-  if (!(e.ops & (OP_CHI2 | OP_HG | OP_RPP))) return;
-  const StampDev& st = b.stamps[s];
-  int nv = 1;
-  if (e.ops & OP_HG) nv += b.n_free + b.n_free * (b.n_free + 1) / 2;
-  if (e.ops & OP_RPP) nv += b.n_free;
-  for (int k = threadIdx.x; k < nv; k += blockDim.x) {
-    double t = 0;
-    for (int tt = 0; tt < st.nto; ++tt) t += b.tile_acc[((int64_t)(st.tile_o0 + tt) * 2 + slot) * kNacc + k];
-    b.acc[((int64_t)s * 2 + slot) * kNacc + k] = t;
+  const uint32_t n = b.counters[9];
+  for (uint32_t it = blockIdx.x; it < n; it += gridDim.x) {
+    const int t = b.slist[it];
+    const int s = t >> 1, slot = t & 1;
+    const EvalDev& e = b.evals[t];
+    if (!(e.ops & (OP_CHI2 | OP_HG | OP_RPP))) continue;
+    const StampDev& st = b.stamps[s];
+    int nv = 1;
+    if (e.ops & OP_HG) nv += b.n_free + b.n_free * (b.n_free + 1) / 2;
+    if (e.ops & OP_RPP) nv += b.n_free;
+    for (int k = threadIdx.x; k < nv; k += blockDim.x) {
+      double acc = 0;
+      for (int tt = 0; tt < st.nto; ++tt)
+        acc += b.tile_acc[((int64_t)(st.tile_o0 + tt) * 2 + slot) * kNacc + k];
+      b.acc[((int64_t)s * 2 + slot) * kNacc + k] = acc;
+    }
   }
 }
 
@@ -1142,31 +1221,38 @@ cudaError_t launch_render_pass(const BatchArgs& b, const ConvIO& io, size_t conv
   auto E = [&](int i) {
     if (i >= 0) prof->end(i, s);
   };
-  int t;
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  // persistent grids over the compacted lists (fixed sizes: graph capturable)
+  auto grid = [&](int64_t upper, int per_sm) {
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(upper, (int64_t)nsm * per_sm));
+  };
+  int t = B(KC_SETUP);
+  k_build_lists<<<(b.n_stamps * 2 + 127) / 128, 128, 0, s>>>(b);
+  E(t);
   if (b.psf_mode != AP_PSF_NONE) {
     t = B(KC_PSF);
-    k_psf_shift<<<dim3(b.n_stamps, 2), 256, 0, s>>>(b, io.psf);
+    k_psf_shift<<<grid(2 * (int64_t)b.n_stamps, 8), 256, 0, s>>>(b, io.psf);
     E(t);
   }
   t = B(KC_SAMPLE);
-  k_sample<<<dim3(b.n_work_tiles, 2), kTile * kTile, 0, s>>>(b);
+  k_sample<<<grid(2 * (int64_t)b.n_work_tiles, 8), kTile * kTile, 0, s>>>(b);
   if (b.kind == AP_PROFILE_EXPONENTIAL && b.integrate == AP_INTEGRATE_THRESHOLD)
     k_exp_threshold<<<(b.n_stamps * 2 + 127) / 128, 128, 0, s>>>(b);
   E(t);
   if (b.integrate == AP_INTEGRATE_THRESHOLD) {
-    int dev = 0, nsm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     t = B(KC_SELECT);
-    k_select<<<dim3(b.n_work_tiles, 2), kTile * kTile, 0, s>>>(b);
+    k_select<<<grid(2 * (int64_t)b.n_work_tiles, 8), kTile * kTile, 0, s>>>(b);
     k_recheck<<<nsm * 4, 256, 0, s>>>(b);
     E(t);
     t = B(KC_INTEGRATE);
+    k_level1<<<nsm * 8, 256, 0, s>>>(b);
     k_integrate<<<nsm * 8, 256, 0, s>>>(b);
     E(t);
   }
   t = B(KC_CONV);
-  const dim3 cgrid(b.n_out_tiles, 2);
+  const dim3 cgrid(grid(2 * (int64_t)b.n_out_tiles, 16));
   switch (b.n_free) {
     case 0: k_conv<0><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
     case 1: k_conv<1><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
@@ -1181,7 +1267,7 @@ cudaError_t launch_render_pass(const BatchArgs& b, const ConvIO& io, size_t conv
   E(t);
   if (accumulate) {
     t = B(KC_REDUCE);
-    k_reduce_acc<<<dim3(b.n_stamps, 2), 64, 0, s>>>(b);
+    k_reduce_acc<<<grid(2 * (int64_t)b.n_stamps, 16), 64, 0, s>>>(b);
     E(t);
   }
   return cudaGetLastError();
@@ -1279,7 +1365,8 @@ cudaError_t launch_chi2_only(const BatchArgs& b, const ConvIO& io, const float* 
 }
 
 cudaError_t launch_psf_only(const BatchArgs& b, const float* psf, cudaStream_t s) {
-  k_psf_shift<<<dim3(b.n_stamps, 2), 256, 0, s>>>(b, psf);
+  k_build_lists<<<(b.n_stamps * 2 + 127) / 128, 128, 0, s>>>(b);
+  k_psf_shift<<<std::max(1, std::min(2 * b.n_stamps, 1024)), 256, 0, s>>>(b, psf);
   return cudaGetLastError();
 }
 

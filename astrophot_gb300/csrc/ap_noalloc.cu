@@ -233,6 +233,9 @@ extern "C" int ap_render_noalloc(int32_t nx, int32_t ny, int32_t psf_kx, int32_t
   const int64_t o_spsf = take(sizeof(float) * (kp2 > 0 ? 6 * kp2 : 1));
   const int64_t o_queue = take(sizeof(int64_t) * 2 * wp);
   const int64_t o_recheck = take(sizeof(int64_t) * 2 * wp);
+  const int64_t o_wlist = take(sizeof(int64_t) * 2 * st.ntw);
+  const int64_t o_olist = take(sizeof(int64_t) * 2 * st.nto);
+  const int64_t o_slist = take(sizeof(int32_t) * 2);
   const int64_t o_cnt = take(sizeof(uint32_t) * 16);
   const int64_t o_wctr = take(sizeof(unsigned long long) * 4);
   const int64_t o_mean = take(sizeof(double) * 2);
@@ -298,6 +301,9 @@ extern "C" int ap_render_noalloc(int32_t nx, int32_t ny, int32_t psf_kx, int32_t
   A.spsf = (float*)(ws + o_spsf);
   A.queue = (int64_t*)(ws + o_queue);
   A.recheck = (int64_t*)(ws + o_recheck);
+  A.wlist = (int64_t*)(ws + o_wlist);
+  A.olist = (int64_t*)(ws + o_olist);
+  A.slist = (int32_t*)(ws + o_slist);
   A.counters = (uint32_t*)(ws + o_cnt);
   A.work_ctr = (unsigned long long*)(ws + o_wctr);
   A.mean_acc = (double*)(ws + o_mean);
