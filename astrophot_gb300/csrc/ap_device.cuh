@@ -123,7 +123,17 @@ struct EvalDev {
   double shift[2];
   double v[NPARAM];   // value-space parameters
   double amp64, bn64, c64, s64;
+  double invq64, invRe64, invn64;  // reciprocals for the float64 re-decisions
   float drep[NPARAM]; // d value / d representation
+};
+
+// The FP32 constants of one evaluation, held in registers by the pixel kernels (read once
+// per tile or queue entry instead of through a reference the compiler must re-load after
+// every store).
+struct EvalF {
+  float c, s, invq, invRe, invn, bn, dbn, amp, soft2, fx, fy;
+  float P0, P1, P2, P3;
+  int cix, cjy;
 };
 
 // everything the kernels need, passed by value
@@ -206,12 +216,12 @@ struct Sample {
 // log2 adds <= 2.4e-7 absolute, so t = 2^(log2(u)/n) has relative error <= 4e-7 + 5e-7/n;
 // the exponent b (t - 1) inherits b t times that, and the MUFU exp adds <= 3e-7 plus
 // 1.2e-7 per unit of exponent.  Hence |dI/I| <= 4e-7 + (|b (t - 1)| + b) (5e-7 + 5e-7/n).
-__device__ __forceinline__ float sample_rel_err(const EvalDev& e, float arg) {
+__device__ __forceinline__ float sample_rel_err(const EvalF& e, float arg) {
   return 4e-7f + (fabsf(arg) + e.bn) * (5e-7f + 5e-7f * e.invn);
 }
 
 template <bool GRAD>
-__device__ __forceinline__ Sample eval_profile(const EvalDev& e, int kind, float X, float Y,
+__device__ __forceinline__ Sample eval_profile(const EvalF& e, int kind, float X, float Y,
                                                float area_scale) {
   Sample out;
   const float Xr = e.c * X - e.s * Y;
@@ -254,22 +264,44 @@ __device__ __forceinline__ Sample eval_profile(const EvalDev& e, int kind, float
 __device__ __forceinline__ double eval_profile64(const EvalDev& e, int kind, double X, double Y,
                                                  double area_scale) {
   const double Xr = e.c64 * X - e.s64 * Y;
-  const double Yr = (e.s64 * X + e.c64 * Y) / e.v[PQ];
+  const double Yr = (e.s64 * X + e.c64 * Y) * e.invq64;
   const double R = sqrt(Xr * Xr + Yr * Yr + e.soft2_64);
   const double amp = e.amp64 * area_scale;
   if (kind == AP_PROFILE_SERSIC) {
-    return amp * exp(-e.bn64 * (exp(log(R / e.v[PRE]) * (1.0 / e.v[PN])) - 1.0));
+    return amp * exp(-e.bn64 * (exp(log(R * e.invRe64) * e.invn64) - 1.0));
   }
-  return amp * exp(-e.bn64 * ((R / e.v[PRE]) - 1.0));
+  return amp * exp(-e.bn64 * ((R * e.invRe64) - 1.0));
 }
 
 // Plane offset (X, Y) of a point given in working-pixel units relative to the
 // integer centre pixel, FP32 and FP64.
-__device__ __forceinline__ void pix_to_offset(const StampDev& st, const EvalDev& e, float di,
-                                              float dj, float& X, float& Y) {
+__device__ __forceinline__ void pix_to_offset(const EvalF& e, float di, float dj, float& X,
+                                              float& Y) {
   const float a = di - e.fx, b = dj - e.fy;
-  X = st.Pf[0] * a + st.Pf[1] * b;
-  Y = st.Pf[2] * a + st.Pf[3] * b;
+  X = e.P0 * a + e.P1 * b;
+  Y = e.P2 * a + e.P3 * b;
+}
+
+__device__ __forceinline__ EvalF load_evalf(const StampDev& st, const EvalDev& e) {
+  EvalF f;
+  f.c = __ldg(&e.c);
+  f.s = __ldg(&e.s);
+  f.invq = __ldg(&e.invq);
+  f.invRe = __ldg(&e.invRe);
+  f.invn = __ldg(&e.invn);
+  f.bn = __ldg(&e.bn);
+  f.dbn = __ldg(&e.dbn);
+  f.amp = __ldg(&e.amp);
+  f.soft2 = __ldg(&e.soft2);
+  f.fx = __ldg(&e.fx);
+  f.fy = __ldg(&e.fy);
+  f.P0 = __ldg(&st.Pf[0]);
+  f.P1 = __ldg(&st.Pf[1]);
+  f.P2 = __ldg(&st.Pf[2]);
+  f.P3 = __ldg(&st.Pf[3]);
+  f.cix = __ldg(&e.cix);
+  f.cjy = __ldg(&e.cjy);
+  return f;
 }
 
 __device__ __forceinline__ void pix_to_offset64(const StampDev& st, const EvalDev& e, double di,

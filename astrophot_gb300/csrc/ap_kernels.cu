@@ -109,11 +109,14 @@ __global__ void k_eval_setup(BatchArgs b, const double* params, int64_t stamp_st
   e.s64 = sin(theta);
   e.c = (float)e.c64;
   e.s = (float)e.s64;
-  e.invq = (float)(1.0 / v[PQ]);
+  e.invq64 = 1.0 / v[PQ];
+  e.invq = (float)e.invq64;
   e.Re = (float)v[PRE];
-  e.invRe = (float)(1.0 / v[PRE]);
+  e.invRe64 = 1.0 / v[PRE];
+  e.invRe = (float)e.invRe64;
   const double n = (b.kind == AP_PROFILE_SERSIC) ? v[PN] : 1.0;
-  e.invn = (float)(1.0 / n);
+  e.invn64 = 1.0 / n;
+  e.invn = (float)e.invn64;
   e.bn64 = sersic_b64(n);
   e.bn = (float)e.bn64;
   e.dbn = (float)sersic_db64(n);
@@ -151,6 +154,18 @@ __global__ void k_build_lists(BatchArgs b) {
   const uint32_t o0 = atomicAdd(&b.counters[8], (unsigned)st.nto);
   for (int k = 0; k < st.nto; ++k) b.olist[o0 + k] = key | k;
   b.slist[atomicAdd(&b.counters[9], 1u)] = t;
+  // algorithmic work of this evaluation (counted here, once, not per warp in the kernels):
+  // convolution = 2 FLOP per kernel tap per convolved plane per output pixel
+  const int ops = b.evals[t].ops;
+  if (b.psf_mode != AP_PSF_NONE) {
+    const bool jac = (ops & OP_JAC) != 0, shiftmode = (b.psf_mode == AP_PSF_FULL);
+    const int nconv = jac ? ((shiftmode ? 3 : 1) + (b.kind == AP_PROFILE_SERSIC ? 4 : 3) +
+                             (shiftmode ? 0 : 2))
+                          : 1;
+    atomicAdd(b.work_ctr, (unsigned long long)st.nx * st.ny * 2ull *
+                              (unsigned long long)(st.kpx * st.kpy) * (unsigned long long)nconv);
+  }
+  atomicAdd(b.work_ctr + 2, (unsigned long long)st.wnx * st.wny * (unsigned long long)b.tables->nsub);
 }
 
 __device__ __forceinline__ void unpack_entry(int64_t ent, int& slot, int& s, int& local) {
@@ -251,9 +266,8 @@ __global__ void k_psf_shift(BatchArgs b, const float* psf) {
 // sampling (_sample_init): deep value, partials, reference sub-sample, FP32 error bound
 // ---------------------------------------------------------------------------
 template <bool JAC>
-__device__ __forceinline__ void sample_pixel(const BatchArgs& b, const StampDev& st,
-                                             const EvalDev& e, int i, int j, float& deep,
-                                             float* g, float& refsub, float& errb) {
+__device__ __forceinline__ void sample_pixel(const BatchArgs& b, const EvalF& e, int i, int j,
+                                             float& deep, float* g, float& refsub, float& errb) {
   const QuadTables& T = *b.tables;
   const float di = (float)(i - e.cix), dj = (float)(j - e.cjy);
   deep = 0.f;
@@ -264,7 +278,7 @@ __device__ __forceinline__ void sample_pixel(const BatchArgs& b, const StampDev&
   float referr = 0.f;
   for (int k = 0; k < T.nsub; ++k) {
     float X, Y;
-    pix_to_offset(st, e, di + T.sxf[k], dj + T.syf[k], X, Y);
+    pix_to_offset(e, di + T.sxf[k], dj + T.syf[k], X, Y);
     const Sample sm = eval_profile<JAC>(e, b.kind, X, Y, 1.f);
     const float w = T.swf[k];
     deep = fmaf(w, sm.v, deep);
@@ -302,7 +316,7 @@ __device__ double sample_pixel64(const BatchArgs& b, const StampDev& st, const E
 template <bool JAC>
 __device__ void sample_tile(const BatchArgs& b, int s, int slot, int tile_local) {
   const StampDev& st = b.stamps[s];
-  const EvalDev& e = b.evals[s * 2 + slot];
+  const EvalF e = load_evalf(st, b.evals[s * 2 + slot]);
   const int tx = threadIdx.x & (kTile - 1), ty = threadIdx.x / kTile;
   const int i = (tile_local % st.ntw_x) * kTile + tx;
   const int j = (tile_local / st.ntw_x) * kTile + ty;
@@ -310,7 +324,7 @@ __device__ void sample_tile(const BatchArgs& b, int s, int slot, int tile_local)
   float deep = 0.f;
   if (valid) {
     float g[NGRAD], refsub, errb;
-    sample_pixel<JAC>(b, st, e, i, j, deep, g, refsub, errb);
+    sample_pixel<JAC>(b, e, i, j, deep, g, refsub, errb);
     const int64_t p = st.work_off + (int64_t)j * st.wnx + i;
     b.work[work_plane(b, slot, 0) + p] = deep;
     if (JAC) {
@@ -320,11 +334,6 @@ __device__ void sample_tile(const BatchArgs& b, int s, int slot, int tile_local)
     float* aux = b.aux + (int64_t)slot * 2 * b.work_pixels;
     aux[p] = refsub;
     aux[b.work_pixels + p] = errb;
-  }
-  {
-    const unsigned cnt = __popc(__ballot_sync(0xffffffffu, valid));
-    if ((threadIdx.x & 31) == 0 && cnt)
-      atomicAdd(b.work_ctr + 2, (unsigned long long)cnt * (unsigned long long)b.tables->nsub);
   }
   if (b.kind == AP_PROFILE_EXPONENTIAL && b.integrate == AP_INTEGRATE_THRESHOLD) {
     // sum(deep) for the default _integrate_reference (models/_model_methods.py:151-152)
@@ -532,9 +541,8 @@ struct QuadResult {
 // (ci + qx / scale, cj + qy / scale) with amplitude scale area.  QC > 0 fixes the quadrature
 // level at compile time (the sample loop unrolls into independent evaluations).
 template <bool JAC, int QC>
-__device__ __forceinline__ QuadResult quad_lane(const BatchArgs& b, const StampDev& st,
-                                                const EvalDev& e, float ci, float cj, float inv_g,
-                                                float area) {
+__device__ __forceinline__ QuadResult quad_lane(const BatchArgs& b, const EvalF& e, float ci,
+                                                float cj, float inv_g, float area) {
   const QuadTables& T = *b.tables;
   const int n = QC > 0 ? QC * QC : T.quad_level * T.quad_level;
   const int mid = n / 2;
@@ -550,7 +558,7 @@ __device__ __forceinline__ QuadResult quad_lane(const BatchArgs& b, const StampD
   for (int k = 0; k < (QC > 0 ? QC * QC : kMaxQuad * kMaxQuad); ++k) {
     if (QC == 0 && k >= n) break;
     float X, Y;
-    pix_to_offset(st, e, ci + T.qxf[k] * inv_g, cj + T.qyf[k] * inv_g, X, Y);
+    pix_to_offset(e, ci + T.qxf[k] * inv_g, cj + T.qyf[k] * inv_g, X, Y);
     const Sample sm = eval_profile<JAC>(e, b.kind, X, Y, area);
     const float w = T.qwf[k];
     r.res = fmaf(w, sm.v, r.res);
@@ -630,11 +638,12 @@ __device__ __forceinline__ void level1_pixel(const BatchArgs& b, int64_t ent, bo
   const int64_t p = ent & 0xffffffffll;
   const StampDev& st = b.stamps[s];
   const EvalDev& e = b.evals[s * 2 + slot];
+  const EvalF f = load_evalf(st, e);
   const int i = (int)(p % st.wnx), j = (int)(p / st.wnx);
-  const float di = (float)(i - e.cix), dj = (float)(j - e.cjy);
+  const float di = (float)(i - f.cix), dj = (float)(j - f.cjy);
   const bool jac = (e.ops & OP_JAC) != 0;
-  QuadResult r = jac ? quad_lane<true, QC>(b, st, e, di, dj, 1.f, 1.f)
-                     : quad_lane<false, QC>(b, st, e, di, dj, 1.f, 1.f);
+  QuadResult r = jac ? quad_lane<true, QC>(b, f, di, dj, 1.f, 1.f)
+                     : quad_lane<false, QC>(b, f, di, dj, 1.f, 1.f);
   bool split = false;
   if (b.max_depth > 1) {
     const float thr = e.thresh;
@@ -652,7 +661,7 @@ __device__ __forceinline__ void level1_pixel(const BatchArgs& b, int64_t ent, bo
     write_deep(b, st, slot, p, r.res, r.g, jac);
 }
 
-__global__ void __launch_bounds__(256) k_level1(BatchArgs b) {
+__global__ void __launch_bounds__(256, 3) k_level1(BatchArgs b) {
   const uint32_t n = min((uint32_t)b.counters[0], (uint32_t)(2 * b.work_pixels));
   const int Q = b.tables->quad_level;
   const int lane = threadIdx.x & 31;
@@ -698,8 +707,9 @@ __device__ void level23_pixel(const BatchArgs& b, int slot, int s, int64_t p, in
   const QuadTables& T = *b.tables;
   const int Q2 = QC > 0 ? QC * QC : T.quad_level * T.quad_level;
   const int g = T.gridding, G2 = g * g;
+  const EvalF f = load_evalf(st, e);
   const int i = (int)(p % st.wnx), j = (int)(p / st.wnx);
-  const float di = (float)(i - e.cix), dj = (float)(j - e.cjy);
+  const float di = (float)(i - f.cix), dj = (float)(j - f.cjy);
   const float thr = e.thresh;
   const float ginv = 1.f / (float)g;
   const float area2 = ginv * ginv;
@@ -713,7 +723,7 @@ __device__ void level23_pixel(const BatchArgs& b, int slot, int s, int64_t p, in
   if (lane < G2) {
     ci2 = di + T.gxf[lane];
     cj2 = dj + T.gyf[lane];
-    r2 = quad_lane<JAC, QC>(b, st, e, ci2, cj2, ginv, area2);
+    r2 = quad_lane<JAC, QC>(b, f, ci2, cj2, ginv, area2);
     if (b.max_depth > 2) split2 = decide(b, st, e, r2, thr * (float)G2, i, j, lane, n64);
   }
   // level 3: refine each flagged sub-pixel with the whole warp
@@ -730,7 +740,7 @@ __device__ void level23_pixel(const BatchArgs& b, int slot, int s, int64_t p, in
 #pragma unroll
     for (int q = 0; q < NGRAD; ++q) r3.g[q] = 0.f;
     if (lane < G2) {
-      r3 = quad_lane<JAC, QC>(b, st, e, cim + T.gxf[lane] * ginv, cjm + T.gyf[lane] * ginv,
+      r3 = quad_lane<JAC, QC>(b, f, cim + T.gxf[lane] * ginv, cjm + T.gyf[lane] * ginv,
                               ginv * ginv, area3);
     }
     const float s3 = warp_sum(r3.res);
@@ -973,17 +983,6 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
         for (int o = 0; o < kConvRows; ++o) cv[dst][o] = outv[o];
       }
     }
-    // algorithmic work: 2 FLOP per kernel tap per convolved plane per output pixel
-    const int nconv = jac ? ((shiftmode ? 3 : 1) + (b.kind == AP_PROFILE_SERSIC ? 4 : 3) +
-                             (shiftmode ? 0 : 2))
-                          : 1;
-    int nvalid = 0;
-#pragma unroll
-    for (int o = 0; o < kConvRows; ++o) nvalid += (x < st.nx && yb + o < st.ny) ? 1 : 0;
-    const int cnt = __reduce_add_sync(0xffffffffu, nvalid);
-    if ((threadIdx.x & 31) == 0 && cnt)
-      atomicAdd(b.work_ctr, (unsigned long long)cnt * 2ull * (unsigned long long)kp2 *
-                                (unsigned long long)nconv);
   }
 
   const bool acc_any = (ops & (OP_CHI2 | OP_HG | OP_RPP)) != 0;
@@ -1094,7 +1093,7 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
 }
 
 template <int NF>
-__global__ void __launch_bounds__(kConvThreads) k_conv(BatchArgs b, ConvIO io) {
+__global__ void __launch_bounds__(kConvThreads, 4) k_conv(BatchArgs b, ConvIO io) {
   extern __shared__ __align__(16) float smem[];
   __shared__ float shred[kConvWarps * kNacc];
   __shared__ uint32_t next;

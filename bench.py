@@ -398,6 +398,7 @@ def run_gpu(args):
         "fits": {"total": int(total_all), "converged": int(converged_all),
                  "mean_iterations": float(iters_h.mean()),
                  "status_counts": {N.LM_MESSAGES[k]: int(np.sum(status_h == k)) for k in np.unique(status_h)}},
+        "clocks": clk.summary(),
         "e2e": {"value": converged_all / (e2e_ms * 1e-3), "unit": "fits/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "wall_ms_per_step": e2e_wall_ms},
         "roofline": roof,
