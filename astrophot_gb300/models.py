@@ -1,0 +1,546 @@
+"""Model classes with the reference's construction API (``astrophot/models/``).
+
+``AstroPhot_Model(model_type=...)`` builds ``Sersic_Galaxy`` ("sersic galaxy model"),
+``Exponential_Galaxy`` ("exponential galaxy model"), ``Flat_Sky`` ("flat sky model") or
+``Group_Model`` ("group model") with the same parameters, limits, sampling knobs and
+defaults as the reference (``models/core_model.py:98-115``, ``model_object.py:57-111``,
+``galaxy_model_object.py:44-53``, ``sersic_model.py:61-66``, ``exponential_model.py:58-62``,
+``flatsky_model.py:23-26``, ``sky_model_object.py:16-35``, ``group_model_object.py``).
+
+Every image, Jacobian and fit is computed by the CUDA library through its C ABI
+(``_native``): a galaxy, alone or in a group with a flat sky, is one stamp of a
+``StampBatch`` whose window is the model's window.  There is no CPU fallback.
+"""
+
+from __future__ import annotations
+
+import math
+from copy import deepcopy
+from typing import Optional
+
+import numpy as np
+import torch
+
+from . import config
+from .errors import InvalidTarget, NameNotAllowed, SpecificationConflict, UnrecognizedModel, InvalidWindow
+from .image import Jacobian_Image, Model_Image, PSF_Image, Target_Image, Window
+from .param import Param_SoftLimits, Param_Unlock, Parameter_Node
+
+__all__ = (
+    "AstroPhot_Model",
+    "Component_Model",
+    "Galaxy_Model",
+    "Sersic_Galaxy",
+    "Exponential_Galaxy",
+    "Sky_Model",
+    "Flat_Sky",
+    "Group_Model",
+)
+
+# full parameter-vector slots of the C ABI
+SLOT = {"center": (0, 1), "q": (2,), "PA": (3,), "n": (4,), "Re": (5,), "Ie": (6,), "F": (7,)}
+
+
+def _all_subclasses(cls):
+    return set(cls.__subclasses__()).union(s for c in cls.__subclasses__() for s in _all_subclasses(c))
+
+
+class AstroPhot_Model:
+    """Factory and common plumbing (``models/core_model.py:26-502``)."""
+
+    model_type = "model"
+    model_names = []
+    special_kwargs = ["parameters", "filename", "model_type", "usable"]
+    usable = False
+
+    def __new__(cls, *, filename=None, model_type=None, **kwargs):
+        if model_type is not None:
+            for M in _all_subclasses(AstroPhot_Model):
+                if M.model_type == model_type:
+                    return super(AstroPhot_Model, cls).__new__(M)
+            raise UnrecognizedModel(f"Unknown AstroPhot model type: {model_type}")
+        return super().__new__(cls)
+
+    def __init__(self, *, name=None, target=None, window=None, locked=False, **kwargs):
+        self._window = None
+        self._target = None
+        self.name = name
+        self.parameters = Parameter_Node(self.name)
+        self.target = target
+        self.window = window
+        self._locked = locked
+        self.mask = kwargs.get("mask", None)
+        for k, v in kwargs.items():
+            if k in self.special_kwargs:
+                continue
+            setattr(self, k, v)
+
+    # names --------------------------------------------------------------------------------
+    @property
+    def name(self):
+        return self._name
+
+    @name.setter
+    def name(self, name):
+        if name is None:
+            i = 0
+            while f"{self.model_type} [{i}]" in AstroPhot_Model.model_names:
+                i += 1
+            name = f"{self.model_type} [{i}]"
+        if ":" in name or "|" in name:
+            raise NameNotAllowed("characters '|' and ':' are reserved for internal model operations")
+        self._name = name
+        AstroPhot_Model.model_names.append(name)
+
+    # target / window ---------------------------------------------------------------------
+    @property
+    def target(self):
+        return self._target
+
+    @target.setter
+    def target(self, tar):
+        if not (tar is None or isinstance(tar, Target_Image)):
+            raise InvalidTarget("AstroPhot_Model target must be a Target_Image instance.")
+        self._target = tar
+
+    @property
+    def window(self):
+        if self._window is None:
+            if self.target is None:
+                raise ValueError("This model has no target or window, these must be provided by the user")
+            return self.target.window.copy()
+        return self._window
+
+    @window.setter
+    def window(self, window):
+        if window is None:
+            self._window = None
+        elif isinstance(window, Window):
+            self._window = window
+        elif len(window) == 2:
+            self._window = self.target.window.copy().crop_to_pixel(window)
+        else:
+            raise InvalidWindow(f"Unrecognized window format: {window}")
+
+    @property
+    def locked(self):
+        return self._locked
+
+    @locked.setter
+    def locked(self, val):
+        self._locked = val
+
+    def __getitem__(self, key):
+        return self.parameters[key]
+
+    def __contains__(self, key):
+        return key in self.parameters
+
+    def make_model_image(self, window: Optional[Window] = None):
+        w = self.window if window is None else (self.window & window)
+        return self.target.model_image(w)
+
+    def __call__(self, image=None, parameters=None, window=None, as_representation=False, **kwargs):
+        """``core_model.py:484-502``: a tensor ``parameters`` is written into the model first."""
+        if isinstance(parameters, (torch.Tensor, np.ndarray, list, tuple)):
+            if as_representation:
+                self.parameters.vector_set_representation(parameters)
+            else:
+                self.parameters.vector_set_values(parameters)
+            parameters = None
+        return self.sample(image=image, window=window, parameters=parameters, **kwargs)
+
+    def negative_log_likelihood(self, parameters=None, as_representation=False):
+        """``core_model.py:220-256``: sum over unmasked pixels of W (model - data)^2 / 2."""
+        if parameters is not None:
+            (self.parameters.vector_set_representation if as_representation else self.parameters.vector_set_values)(parameters)
+        model = self.sample()
+        data = self.target[self.window]
+        r = (model.data - data.data) ** 2 * data.weight
+        if data.has_mask:
+            r = r[torch.logical_not(data.mask)]
+        return torch.sum(r) / 2.0
+
+    def get_state(self):
+        return {"name": self.name, "model_type": self.model_type, "parameters": self.parameters.get_state()}
+
+    @classmethod
+    def List_Model_Names(cls, usable=None):
+        return sorted(M.model_type for M in _all_subclasses(cls) if usable is None or M.usable is usable)
+
+
+class Component_Model(AstroPhot_Model):
+    """Single-component model with the reference's sampling knobs (``model_object.py:25-111``)."""
+
+    parameter_specs = {"center": {"units": "arcsec", "uncertainty": [0.1, 0.1]}}
+    _parameter_order = ("center",)
+    psf_mode = "none"
+    psf_convolve_mode = "fft"
+    psf_subpixel_shift = "bilinear"
+    sampling_mode = "midpoint"
+    sampling_tolerance = 1e-2
+    integrate_mode = "threshold"
+    integrate_max_depth = 3
+    integrate_gridding = 5
+    integrate_quad_level = 3
+    jacobian_chunksize = 10
+    image_chunksize = 1000
+    softening = 1e-3
+    usable = False
+
+    def __init__(self, *, name=None, **kwargs):
+        self._psf = None
+        super().__init__(name=name, **kwargs)
+        specs = self.build_parameter_specs(kwargs.get("parameters", None))
+        for p in self.__class__._parameter_order:
+            spec = specs[p]
+            if isinstance(spec, Parameter_Node):
+                self.parameters.link(spec)
+            else:
+                self.parameters.link(Parameter_Node(p, **spec))
+        self._plans = {}
+
+    @classmethod
+    def build_parameter_specs(cls, user_specs=None):
+        """``_model_methods.py:43-65``."""
+        specs = {}
+        for base in reversed(cls.__mro__):
+            if "parameter_specs" in base.__dict__:
+                specs.update(deepcopy(base.__dict__["parameter_specs"]))
+        if isinstance(user_specs, dict):
+            for p, v in user_specs.items():
+                if isinstance(v, Parameter_Node):
+                    specs[p] = v
+                elif isinstance(v, dict):
+                    specs[p].update(v)
+                else:
+                    specs[p]["value"] = v
+        return specs
+
+    @property
+    def psf(self):
+        if self._psf is None:
+            return None if self.target is None else self.target.psf
+        return self._psf
+
+    @psf.setter
+    def psf(self, val):
+        if val is None or isinstance(val, PSF_Image):
+            self._psf = val
+        else:
+            self._psf = PSF_Image(val, pixelscale=self.target.pixelscale)
+
+    @torch.no_grad()
+    def initialize(self, target=None, parameters=None, **kwargs):
+        """Centre defaults to the window centre (``model_object.py:180-205``); the reference's
+        profile heuristics are not part of this path, so other parameters must be given."""
+        c = self.parameters["center"]
+        if c.value is None:
+            with Param_Unlock(c), Param_SoftLimits(c):
+                c.value = self.window.center
+        missing = [p for p in self._parameter_order if self.parameters[p].value is None]
+        if missing:
+            raise SpecificationConflict(f"{self.name}: parameters without values: {sorted(set(missing))}")
+
+    # ---- rendering through the C ABI ----------------------------------------------------
+    def sample(self, image=None, window=None, parameters=None):
+        """``Component_Model.sample`` (``model_object.py:258-375``) on the CUDA path."""
+        return _sample_structure(self, [self], image, window)
+
+    def jacobian(self, parameters=None, as_representation=False, window=None, pass_jacobian=None, **kwargs):
+        """``_model_methods.py:260-347``: d(model)/d(vector) on the model window."""
+        if parameters is not None:
+            (self.parameters.vector_set_representation if as_representation else self.parameters.vector_set_values)(parameters)
+        return _jacobian_structure(self, [self], as_representation, window)
+
+
+class Galaxy_Model(Component_Model):
+    """q in (0, 1), PA cyclic in [0, pi) (``galaxy_model_object.py:21-53``)."""
+
+    model_type = f"galaxy {Component_Model.model_type}"
+    parameter_specs = {
+        "q": {"units": "b/a", "limits": (0, 1), "uncertainty": 0.03},
+        "PA": {"units": "radians", "limits": (0, math.pi), "cyclic": True, "uncertainty": 0.06},
+    }
+    _parameter_order = Component_Model._parameter_order + ("q", "PA")
+    usable = False
+
+
+class Sersic_Galaxy(Galaxy_Model):
+    """I(R) = 10^Ie exp(-b(n) ((R/Re)^(1/n) - 1)) (``sersic_model.py:41-91``)."""
+
+    model_type = f"sersic {Galaxy_Model.model_type}"
+    parameter_specs = {
+        "n": {"units": "none", "limits": (0.36, 8), "uncertainty": 0.05},
+        "Re": {"units": "arcsec", "limits": (0, None)},
+        "Ie": {"units": "log10(flux/arcsec^2)"},
+    }
+    _parameter_order = Galaxy_Model._parameter_order + ("n", "Re", "Ie")
+    usable = True
+    profile = "sersic"
+
+    def total_flux(self, parameters=None, window=None):
+        """``sersic_Ie_to_flux_torch`` (``utils/conversions/functions.py:168-190``)."""
+        p = self.parameters
+        n, Re, q, Ie = (p[k].value.item() for k in ("n", "Re", "q", "Ie"))
+        bn = 2 * n - 1 / 3 + 4 / (405 * n) + 46 / (25515 * n**2) + 131 / (1148175 * n**3) - 2194697 / (30690717750 * n**4)
+        return torch.tensor(2 * math.pi * 10**Ie * Re**2 * q * n * math.exp(bn) * bn ** (-2 * n) * math.exp(math.lgamma(2 * n)),
+                            dtype=config.ap_dtype)
+
+
+class Exponential_Galaxy(Galaxy_Model):
+    """I(R) = 10^Ie exp(-b(1) (R/Re - 1)) (``exponential_model.py:40-74``)."""
+
+    model_type = f"exponential {Galaxy_Model.model_type}"
+    parameter_specs = {
+        "Ie": {"units": "log10(flux/arcsec^2)"},
+        "Re": {"units": "arcsec", "limits": (0, None)},
+    }
+    _parameter_order = Galaxy_Model._parameter_order + ("Re", "Ie")
+    usable = True
+    profile = "exponential"
+
+
+class Sky_Model(Component_Model):
+    """Locked centre, no PSF, no integration (``sky_model_object.py:6-35``)."""
+
+    model_type = f"sky {Component_Model.model_type}"
+    parameter_specs = {"center": {"units": "arcsec", "locked": True, "uncertainty": 0.0}}
+    usable = False
+
+    @property
+    def psf_mode(self):
+        return "none"
+
+    @psf_mode.setter
+    def psf_mode(self, val):
+        pass
+
+    @property
+    def integrate_mode(self):
+        return "none"
+
+    @integrate_mode.setter
+    def integrate_mode(self, val):
+        pass
+
+
+class Flat_Sky(Sky_Model):
+    """pixel_area * 10^F everywhere (``flatsky_model.py:13-55``)."""
+
+    model_type = f"flat {Sky_Model.model_type}"
+    parameter_specs = {"F": {"units": "log10(flux/arcsec^2)"}}
+    _parameter_order = Sky_Model._parameter_order + ("F",)
+    usable = True
+
+    @torch.no_grad()
+    def initialize(self, target=None, parameters=None, **kwargs):
+        c = self.parameters["center"]
+        if c.value is None:
+            with Param_Unlock(c), Param_SoftLimits(c):
+                c.value = self.window.center
+        F = self.parameters["F"]
+        if F.value is None:
+            with Param_Unlock(F), Param_SoftLimits(F):
+                F.value = math.log10(abs(float(torch.median(self.target[self.window].data))) / self.target.pixel_area)
+
+
+class Group_Model(AstroPhot_Model):
+    """Sum of sub-models; its ``psf_mode`` is pushed onto every sub-model when they are added
+    (``group_model_object.py:88, 292-297``)."""
+
+    model_type = f"group {AstroPhot_Model.model_type}"
+    usable = True
+
+    def __init__(self, *, name=None, models=None, **kwargs):
+        self._psf_mode = "none"
+        self.models = {}
+        super().__init__(name=name, **kwargs)
+        if models is not None:
+            self.add_model(models)
+        self._plans = {}
+
+    def add_model(self, model):
+        if isinstance(model, (list, tuple)):
+            for m in model:
+                self.add_model(m)
+            return
+        if model.name in self.models and self.models[model.name] is not model:
+            raise KeyError(f"{self.name} already has model with name {model.name}, every model must have a unique name.")
+        self.models[model.name] = model
+        self.parameters.link(model.parameters)
+        self.psf_mode = self.psf_mode
+        if model.target is None:
+            model.target = self.target
+        self._window = None
+        self._plans = {}
+
+    @property
+    def psf_mode(self):
+        return self._psf_mode
+
+    @psf_mode.setter
+    def psf_mode(self, value):
+        self._psf_mode = value
+        for m in getattr(self, "models", {}).values():
+            m.psf_mode = value
+
+    @property
+    def window(self):
+        if self._window is not None:
+            return self._window
+        w = None
+        for m in self.models.values():
+            if m.locked:
+                continue
+            w = m.window.copy() if w is None else (w | m.window)
+        if w is None:
+            return self.target.window.copy()
+        return w
+
+    @window.setter
+    def window(self, window):
+        AstroPhot_Model.window.fset(self, window)
+
+    def __iter__(self):
+        return iter(self.models.values())
+
+    @torch.no_grad()
+    def initialize(self, target=None, parameters=None, **kwargs):
+        for m in self.models.values():
+            m.initialize()
+
+    def sample(self, image=None, window=None, parameters=None):
+        return _sample_structure(self, list(self.models.values()), image, window)
+
+    def jacobian(self, parameters=None, as_representation=False, pass_jacobian=None, window=None, **kwargs):
+        if parameters is not None:
+            (self.parameters.vector_set_representation if as_representation else self.parameters.vector_set_values)(parameters)
+        return _jacobian_structure(self, list(self.models.values()), as_representation, window)
+
+
+# ----------------------------------------------------------------------------------------
+# mapping supported structures onto one stamp of the C ABI
+# ----------------------------------------------------------------------------------------
+
+
+class _Structure:
+    """A galaxy (Sersic or exponential) and/or a flat sky rendered on one window."""
+
+    def __init__(self, owner, components):
+        gals = [c for c in components if isinstance(c, (Sersic_Galaxy, Exponential_Galaxy))]
+        skies = [c for c in components if isinstance(c, Flat_Sky)]
+        if len(gals) + len(skies) != len(components) or len(gals) > 1 or len(skies) > 1:
+            raise NotImplementedError(
+                "the CUDA render path covers one Sersic or exponential galaxy, optionally with one flat sky")
+        self.owner = owner
+        self.gal = gals[0] if gals else None
+        self.sky = skies[0] if skies else None
+        g = self.gal
+        if g is not None:
+            if g.psf_mode not in ("none", "full"):
+                raise SpecificationConflict(f"unknown psf_mode {g.psf_mode}")
+            if g.psf_mode == "full" and g.psf_convolve_mode not in ("fft", "direct"):
+                raise ValueError(f"unrecognized psf_convolve_mode: {g.psf_convolve_mode}")
+            if g.psf_mode == "full" and g.psf_subpixel_shift not in ("bilinear", "none"):
+                raise SpecificationConflict(f"unrecognized subpixel shift method: {g.psf_subpixel_shift}")
+
+    def options(self):
+        from . import _native as N
+
+        g = self.gal
+        free = 0
+        if g is not None:
+            for name, slots in SLOT.items():
+                if name in g.parameters and not g.parameters[name].locked:
+                    for sl in slots:
+                        free |= 1 << sl
+        if self.sky is not None and not self.sky.parameters["F"].locked:
+            free |= 1 << 7
+        if g is None:
+            return N.make_options(profile="sersic", sampling_mode="midpoint", integrate_mode="none", psf_mode="none",
+                                  free_mask=free, has_sky=True)
+        return N.make_options(
+            profile=g.profile, sampling_mode=g.sampling_mode, integrate_mode=g.integrate_mode, psf_mode=g.psf_mode,
+            psf_subpixel_shift=g.psf_subpixel_shift, integrate_max_depth=g.integrate_max_depth,
+            integrate_gridding=g.integrate_gridding, integrate_quad_level=g.integrate_quad_level,
+            sampling_tolerance=g.sampling_tolerance, softening=g.softening, free_mask=free,
+            has_sky=self.sky is not None)
+
+    def full_params(self):
+        v = np.zeros(8)
+        g = self.gal
+        if g is None:
+            v[:7] = [0.0, 0.0, 0.5, 0.0, 1.0, 1.0, -np.inf]
+        else:
+            p = g.parameters
+            v[0:2] = p["center"].value.numpy()
+            v[2] = p["q"].value.item()
+            v[3] = p["PA"].value.item()
+            v[4] = p["n"].value.item() if "n" in p else 1.0
+            v[5] = p["Re"].value.item()
+            v[6] = p["Ie"].value.item()
+        if self.sky is not None:
+            v[7] = self.sky.parameters["F"].value.item()
+        return v
+
+    def vector_order(self):
+        """For each element of ``owner.parameters.vector_values()``, its full-vector slot."""
+        out = []
+        comps = [c for c in ([self.gal] if self.gal is not None else []) + ([self.sky] if self.sky is not None else [])]
+        slot_of = {}
+        for c in comps:
+            for name, slots in SLOT.items():
+                if name in c.parameters:
+                    slot_of[c.parameters[name].identity] = slots
+        for node in self.owner.parameters.flat(include_locked=False).values():
+            slots = slot_of[node.identity]
+            mask = node.vector_mask().numpy()
+            out += [sl for sl, m in zip(slots, mask) if m]
+        return out
+
+
+def _plan(owner, struct: _Structure, window: Window):
+    from . import _native as N
+
+    opts = struct.options()
+    psf = struct.gal.psf if (struct.gal is not None and struct.gal.psf_mode == "full") else None
+    if psf is not None and abs(psf.pixel_length - window.pixel_length) > 1e-9 * window.pixel_length:
+        raise SpecificationConflict("PSFs finer than the image pixels are not supported by the CUDA path")
+    key = (tuple(window.pixel_shape), tuple(window.geometry_row()), None if psf is None else (id(psf), tuple(psf.data.shape)),
+           bytes(opts))
+    plans = owner.__dict__.setdefault("_plans", {})
+    if key not in plans:
+        batch = N.StampBatch([tuple(window.pixel_shape)], None if psf is None else [(psf.data.shape[1], psf.data.shape[0])],
+                             window.geometry_row()[None, :], opts, config.ap_device)
+        psf_d = None if psf is None else batch.pack_psf([psf.data.numpy()])
+        plans.clear()
+        plans[key] = (batch, psf_d)
+    return plans[key]
+
+
+def _sample_structure(owner, components, image, window):
+    struct = _Structure(owner, components)
+    w = owner.window if window is None else (owner.window & window)
+    if image is None:
+        image = owner.target.model_image(w)
+    batch, psf_d = _plan(owner, struct, w)
+    out = batch.render(torch.tensor(struct.full_params()[None, :]), psf_d)
+    img = Model_Image(torch.as_tensor(batch.unpack(out)[0], dtype=config.ap_dtype), w.copy())
+    image += img
+    return image
+
+
+def _jacobian_structure(owner, components, as_representation, window):
+    struct = _Structure(owner, components)
+    w = owner.window if window is None else (owner.window & window)
+    batch, psf_d = _plan(owner, struct, w)
+    _, jac = batch.jacobian(torch.tensor(struct.full_params()[None, :]), psf_d, as_representation=as_representation)
+    ny, nx = int(w.pixel_shape[1]), int(w.pixel_shape[0])
+    J = jac.cpu().numpy().reshape(batch.n_free, ny, nx).astype(np.float64)
+    # compact C-ABI columns (full-vector slot order) -> the model's vector order
+    compact = [i for i in range(8) if batch.options.free_mask & (1 << i)]
+    order = struct.vector_order()
+    cols = [J[compact.index(sl)] for sl in order]
+    data = np.stack(cols, -1) if cols else np.zeros((ny, nx, 0))
+    return Jacobian_Image(owner.parameters.vector_identities(), data, w.copy())

@@ -1,0 +1,172 @@
+"""The drop-in API on the GPU, written like the reference's own tests: models built with
+``AstroPhot_Model(model_type=...)`` on a ``Target_Image``, sampled, differentiated and fitted
+with ``fit.LM``; compared with the golden vectors recorded from the reference."""
+
+import math
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+import cases  # noqa: E402
+
+
+@pytest.fixture(scope="module")
+def ap():
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA GPU")
+    import astrophot_gb300
+
+    return astrophot_gb300
+
+
+def close(got, ref, rel=1e-5):
+    return np.max(np.abs(np.asarray(got) - ref)) <= rel * np.max(np.abs(ref))
+
+
+def model_from_case(ap, name, tag):
+    d = cases.load_render(name)
+    spec = d["spec"]
+    psf = d["psf"] if d["psf"].size else None
+    tar = ap.image.Target_Image(data=np.zeros((spec["ny"], spec["nx"])), pixelscale=spec["scale"], psf=psf)
+    kind = {"sersic": "sersic galaxy model", "exponential": "exponential galaxy model"}[spec["kind"]]
+    m = ap.models.AstroPhot_Model(name=f"api {name} {tag}", model_type=kind, target=tar, parameters=dict(spec["params"]),
+                                  **spec["knobs"])
+    return d, tar, m
+
+
+@pytest.mark.parametrize("name", cases.render_case_names())
+def test_model_call_and_jacobian_match_reference(ap, name):
+    d, tar, m = model_from_case(ap, name, "a")
+    img = m()
+    assert close(img.data.numpy(), d["model"])
+    J = m.jacobian(as_representation=True)
+    assert J.data.shape == d["jac_rep"].shape
+    for k in range(J.data.shape[-1]):
+        assert close(J.data[..., k].numpy(), d["jac_rep"][..., k], rel=2e-4)
+
+
+def test_group_with_sky_and_psf_mode_quirk(ap):
+    for tag, gmode, lock, F in (("locked", "full", True, 0.0), ("free", "full", False, 0.3), ("quirk", None, True, 0.0)):
+        d, tar, gal = model_from_case(ap, "sersic_psf_64", f"g {tag}")
+        sky = ap.models.AstroPhot_Model(name=f"api sky {tag}", model_type="flat sky model", target=tar,
+                                        parameters={"F": {"value": F, "locked": lock}})
+        sky.initialize()
+        kw = {} if gmode is None else {"psf_mode": gmode}
+        grp = ap.models.AstroPhot_Model(name=f"api grp {tag}", model_type="group model", target=tar, models=[gal, sky], **kw)
+        assert close(grp().data.numpy(), d[f"group_{tag}_model"])
+        J = grp.jacobian(as_representation=True).data.numpy()
+        ref = d[f"group_{tag}_jac_rep"]
+        assert J.shape == ref.shape
+        for k in range(ref.shape[-1]):
+            assert close(J[..., k], ref[..., k], rel=2e-4)
+
+
+def test_sky_first_group_keeps_vector_order(ap):
+    d, tar, gal = model_from_case(ap, "sersic_psf_64", "order")
+    sky = ap.models.AstroPhot_Model(name="api sky order", model_type="flat sky model", target=tar, parameters={"F": 0.3})
+    sky.initialize()
+    grp = ap.models.AstroPhot_Model(name="api grp order", model_type="group model", target=tar, models=[sky, gal],
+                                    psf_mode="full")
+    assert grp.parameters.vector_names()[0] == "F"
+    J = grp.jacobian(as_representation=True).data.numpy()
+    ref = d["group_free_jac_rep"]  # reference order: galaxy then sky
+    assert close(J[..., 0], ref[..., -1], rel=2e-4)
+    for k in range(7):
+        assert close(J[..., 1 + k], ref[..., k], rel=2e-4)
+
+
+def lm_target(ap, d, tag):
+    tar = ap.image.Target_Image(data=d["data"], pixelscale=1.0, psf=d["psf"], variance=1.0 / d["weight"])
+    cx, cy, q, PA, n, Re, Ie = d["init"]
+    gal = ap.models.AstroPhot_Model(name=f"lm gal {tag}", model_type="sersic galaxy model", target=tar, psf_mode="full",
+                                    parameters={"center": [cx, cy], "q": q, "PA": PA, "n": n, "Re": Re, "Ie": Ie})
+    sky = ap.models.AstroPhot_Model(name=f"lm sky {tag}", model_type="flat sky model", target=tar,
+                                    parameters={"F": {"value": 0.0, "locked": True}})
+    sky.initialize()
+    return ap.models.AstroPhot_Model(name=f"lm grp {tag}", model_type="group model", target=tar, models=[gal, sky],
+                                     psf_mode="full"), gal
+
+
+@pytest.mark.parametrize("name", cases.lm_case_names())
+def test_fit_lm_matches_reference(ap, name):
+    d = cases.load_lm(name)
+    grp, gal = lm_target(ap, d, name)
+    rep0 = grp.parameters.vector_representation().numpy()
+    assert np.allclose(rep0, d["rep0"], atol=1e-13)
+    res = ap.fit.LM(grp, initial_state=rep0).fit()
+    assert abs(min(res.loss_history) / d["loss_history"].min() - 1) <= 1e-4
+    assert np.allclose(res.loss_history[:3], d["loss_history"][:3], rtol=1e-6)
+    assert res.message in ("success", "success by immobility. Convergence not guaranteed",
+                           "fail. Could not find step to improve Chi^2")
+    # the model now holds res(); its vector agrees with the reference's fitted vector
+    got = grp.parameters.vector_representation().numpy()
+    assert np.allclose(got, res.res(), rtol=1e-12, atol=1e-12)
+    cov = res.covariance_matrix
+    sig = np.sqrt(np.diag(cov.numpy()))
+    vals = grp.parameters.vector_values().numpy()
+    ref_vals = d["final_values"]
+    assert np.all(np.abs(vals - ref_vals) <= 0.25 * sig)
+    res.update_uncertainty()
+    assert np.allclose(grp.parameters.vector_uncertainty().numpy(), sig)
+
+
+def test_fit_recovers_truth_like_the_reference_test(ap):
+    """tests/test_fit.py:71-161 style: noisy Sersic, LM from a nearby start recovers it."""
+    d = cases.load_lm("lm_c0_seed0")
+    grp, gal = lm_target(ap, d, "truth")
+    ap.fit.LM(grp).fit()
+    truth = d["truth"]
+    assert gal["center"].value[0].item() / truth[0] == pytest.approx(1, abs=1e-2)
+    assert gal["center"].value[1].item() / truth[1] == pytest.approx(1, abs=1e-2)
+    assert gal["n"].value.item() == pytest.approx(truth[4], abs=0.3)
+    assert gal["q"].value.item() == pytest.approx(truth[2], abs=0.05)
+    assert gal["Ie"].value.item() == pytest.approx(truth[6], abs=0.1)
+
+
+def test_batch_lm_equals_single_lm(ap):
+    names = cases.lm_case_names()
+    singles, batch_models = [], []
+    for name in names:
+        d = cases.load_lm(name)
+        g1, _ = lm_target(ap, d, f"s {name}")
+        singles.append(ap.fit.LM(g1, initial_state=d["rep0"]).fit())
+        g2, _ = lm_target(ap, d, f"b {name}")
+        batch_models.append(g2)
+    b = ap.fit.BatchLM(batch_models, initial_states=[cases.load_lm(n)["rep0"] for n in names]).fit()
+    for s, f in zip(singles, b.fits):
+        assert s.loss_history == f.loss_history
+        assert np.array_equal(np.asarray(s.res()), f.res_state.numpy())
+
+
+def test_bad_modes_raise(ap):
+    from astrophot_gb300.errors import SpecificationConflict
+
+    d, tar, m = model_from_case(ap, "sersic_nopsf", "bad")
+    m.sampling_mode = "bogus"
+    with pytest.raises(SpecificationConflict):
+        m()
+    m.sampling_mode = "midpoint"
+    m.integrate_mode = "full"
+    with pytest.raises(SpecificationConflict):
+        m()
+
+
+def test_model_window_inside_target(ap):
+    """A model on a sub-window of its target renders like the oracle on that window."""
+    from oracle.render import PSF, Component, Window, sample_component
+
+    d = cases.load_render("sersic_psf_64")
+    spec = d["spec"]
+    tar = ap.image.Target_Image(data=np.zeros((64, 64)), pixelscale=1.0, psf=d["psf"])
+    p = spec["params"]
+    m = ap.models.AstroPhot_Model(name="api win", model_type="sersic galaxy model", target=tar, psf_mode="full",
+                                  window=[[10, 50], [5, 58]], parameters=dict(p))
+    img = m().data.numpy()
+    assert img.shape == (53, 40)
+    comp = Component("sersic", {"center": np.array(p["center"]), "q": p["q"], "PA": p["PA"], "n": p["n"], "Re": p["Re"],
+                                "Ie": p["Ie"]}, psf_mode="full")
+    ref = sample_component(comp, Window(40, 53, np.eye(2), np.array([-10.5, -5.5]), np.zeros(2)), PSF(d["psf"])).model
+    assert close(img, ref)
