@@ -10,6 +10,6 @@ built library raises ImportError.
 """
 
 from . import config as AP_config  # noqa: F401
-from . import errors, fit, image, models, param, utils  # noqa: F401
+from . import autograd, errors, fit, image, models, param, utils  # noqa: F401
 
 __version__ = "0.1.0"

@@ -40,6 +40,7 @@ PROFILE = {"sersic": 0, "exponential": 1}
 SAMPLING = {"midpoint": 0, "simpsons": 1, "quad": 2, "trapezoid": 3}
 INTEGRATE = {"none": 0, "threshold": 1}
 PSF_NONE, PSF_FULL, PSF_FULL_NOSHIFT = 0, 1, 2
+VJP_REPRESENTATION, VJP_REFERENCE_CENTER = 1, 2
 
 LM_RUNNING, LM_SUCCESS, LM_IMMOBILE, LM_MAX_ITER, LM_NO_STEP, LM_LIMIT = range(6)
 LM_MESSAGES = {
@@ -103,6 +104,7 @@ EXPORTS = [
     ("ap_batch_bind", [_P, _P, _I64, _P]),
     ("ap_render", [_P, _P, _P, _P, _P]),
     ("ap_jacobian", [_P, _P, _P, _P, _P, _I32, _P]),
+    ("ap_render_vjp", [_P, _P, _P, _P, _I32, _P, _P]),
     ("ap_batch_psf_stride", [_P, _PI64]),
     ("ap_psf_shift", [_P, _P, _P, _P, _P, _P]),
     ("ap_chi2", [_P, _P, _P, _P, _P, _P, _P]),
@@ -365,6 +367,19 @@ class StampBatch:
             "ap_jacobian",
         )
         return model, jac[: self.n_free]
+
+    def vjp(self, params: torch.Tensor, psf: Optional[torch.Tensor], grad_model: torch.Tensor, as_representation=False,
+            reference_center=False):
+        """Adjoint of :meth:`render`: [n, n_free] float64 = sum_pixels grad_model * d model / d theta.
+        ``reference_center`` adds the sampling-coordinate path to the center entries under
+        PSF shift, as the reference's reverse-mode autograd does."""
+        params = params.to(self.device, torch.float64).contiguous()
+        g = grad_model.to(self.device, torch.float32).contiguous()
+        out = torch.empty((self.n, max(self.n_free, 1)), dtype=torch.float64, device=self.device)
+        flags = (VJP_REPRESENTATION if as_representation else 0) | (VJP_REFERENCE_CENTER if reference_center else 0)
+        check(self.lib.ap_render_vjp(self.handle, _ptr(params), _ptr(psf), _ptr(g), flags,
+                                     _ptr(out), _stream()), "ap_render_vjp")
+        return out[:, : self.n_free]
 
     def psf_shift(self, params: torch.Tensor, psf: torch.Tensor, derivatives=True):
         params = params.to(self.device, torch.float64).contiguous()

@@ -480,6 +480,26 @@ int ap_jacobian(ap_batch* b, const double* params, const float* psf, float* mode
   return render_common(b, params, psf, model, jac, ops, stream);
 }
 
+int ap_render_vjp(ap_batch* b, const double* params, const float* psf, const float* grad_model,
+                  int32_t flags, double* grad_params, ap_stream_t stream) {
+  if (!b || !params || !grad_model || !grad_params) return AP_ERR_ARG;
+  if (flags & ~(AP_VJP_REPRESENTATION | AP_VJP_REFERENCE_CENTER)) return AP_ERR_ARG;
+  if (!b->bound) return AP_ERR_NOT_BOUND;
+  if (b->opt.psf_mode != AP_PSF_NONE && !psf) return AP_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  int32_t ops = OP_FWD | OP_JAC | OP_VJP;
+  if (flags & AP_VJP_REPRESENTATION) ops |= OP_REP;
+  if ((flags & AP_VJP_REFERENCE_CENTER) && b->opt.psf_mode == AP_PSF_FULL) ops |= OP_VJP_COORD;
+  int rc = check_cuda(launch_eval_setup(b->args, params, NPARAM, 0, nullptr, ops, s));
+  if (rc) return rc;
+  ConvIO io{};
+  io.psf = psf;
+  io.vjp_in = grad_model;
+  rc = check_cuda(launch_render_pass(b->args, io, b->conv_smem, true, s, &b->prof));
+  if (rc) return rc;
+  return check_cuda(launch_gather_vjp(b->args, grad_params, s));
+}
+
 int ap_psf_shift(ap_batch* b, const double* params, const float* psf, float* out, float* d_out,
                  ap_stream_t stream) {
   if (!b || !params || !psf || !out) return AP_ERR_ARG;

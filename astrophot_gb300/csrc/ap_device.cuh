@@ -56,6 +56,8 @@ enum EvalOps : int32_t {
   OP_HG = 32,          // accumulate J^T W J and J^T W (y - m)
   OP_RPP = 64,         // accumulate J^T [(2/d)(W (m - Y0)/d - W J h)]
   OP_REP = 128,        // chain Jacobian columns to representation space
+  OP_VJP = 256,        // accumulate sum_pixels g * d model / d theta (adjoint of the render)
+  OP_VJP_COORD = 512,  // VJP in shift mode: add the sampling-coordinate path to the center
 };
 
 struct QuadTables {
@@ -188,6 +190,7 @@ struct ConvIO {
   const float* jbase;     // OP_RPP: Jacobian at the base point [n_free][out_pixels]
   const double* hvec;     // OP_RPP: h per stamp [n_stamps][8]
   double rpp_d;           // OP_RPP: d (0.1)
+  const float* vjp_in;    // OP_VJP: upstream gradient d loss / d model, output layout
 };
 
 // dynamic shared memory of the convolve pass for a kpx x kpy kernel: 3 kernels stored

@@ -160,7 +160,7 @@ __global__ void k_build_lists(BatchArgs b) {
   if (b.psf_mode != AP_PSF_NONE) {
     const bool jac = (ops & OP_JAC) != 0, shiftmode = (b.psf_mode == AP_PSF_FULL);
     const int nconv = jac ? ((shiftmode ? 3 : 1) + (b.kind == AP_PROFILE_SERSIC ? 4 : 3) +
-                             (shiftmode ? 0 : 2))
+                             ((shiftmode && !(ops & OP_VJP_COORD)) ? 0 : 2))
                           : 1;
     atomicAdd(b.work_ctr, (unsigned long long)st.nx * st.ny * 2ull *
                               (unsigned long long)(st.kpx * st.kpy) * (unsigned long long)nconv);
@@ -959,7 +959,7 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
     }
     const int row0 = y0 + st.by - cy, col0 = x0 + st.bx - cx;
     for (int pl = 0; pl < nplanes; ++pl) {
-      if (pl > 0 && shiftmode && (pl - 1 == GX || pl - 1 == GY)) continue;
+      if (pl > 0 && shiftmode && !(ops & OP_VJP_COORD) && (pl - 1 == GX || pl - 1 == GY)) continue;
       if (pl > 0 && b.kind != AP_PROFILE_SERSIC && pl - 1 == GN) continue;
       __syncthreads();
       const float* src = b.work + work_plane(b, slot, pl) + st.work_off;
@@ -985,8 +985,8 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
     }
   }
 
-  const bool acc_any = (ops & (OP_CHI2 | OP_HG | OP_RPP)) != 0;
-  const bool do_hg = (ops & OP_HG) != 0, do_rpp = (ops & OP_RPP) != 0;
+  const bool acc_any = (ops & (OP_CHI2 | OP_HG | OP_RPP | OP_VJP)) != 0;
+  const bool do_hg = (ops & OP_HG) != 0, do_rpp = (ops & OP_RPP) != 0, do_vjp = (ops & OP_VJP) != 0;
   constexpr int NH = NF * (NF + 1) / 2;
   float a_chi2 = 0.f, a_g[NF > 0 ? NF : 1], a_h[NH > 0 ? NH : 1], a_rpp[NF > 0 ? NF : 1];
 #pragma unroll
@@ -1016,6 +1016,10 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
       if (shiftmode) {
         J[PX] = cv[1][o] * st.Pinvf[0] + cv[2][o] * st.Pinvf[2];
         J[PY] = cv[1][o] * st.Pinvf[1] + cv[2][o] * st.Pinvf[3];
+        if (ops & OP_VJP_COORD) {
+          J[PX] -= cv[3 + GX][o];
+          J[PY] -= cv[3 + GY][o];
+        }
       } else {
         J[PX] = -cv[3 + GX][o];
         J[PY] = -cv[3 + GY][o];
@@ -1045,6 +1049,13 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
       for (int k = 0; k < NF; ++k) io.jac_out[(int64_t)k * b.out_pixels + op] = Jc[k];
     }
     if (!acc_any) continue;
+    if (do_vjp) {
+      // adjoint: the upstream gradient already carries weights and masks
+      const float gin = io.vjp_in[op];
+#pragma unroll
+      for (int k = 0; k < NF; ++k) a_g[k] += Jc[k] * gin;
+      continue;
+    }
     // fused reductions (fit/lm.py:374-406); masked pixels are left out entirely
     if (io.mask && io.mask[op]) continue;
     const float w = io.weight ? io.weight[op] : 1.f;
@@ -1079,9 +1090,11 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
   float vals[1 + 2 * NF + NH];
   int nv = 0;
   vals[nv++] = a_chi2;
-  if (do_hg) {
+  if (do_hg || do_vjp) {
 #pragma unroll
     for (int k = 0; k < NF; ++k) vals[nv++] = a_g[k];
+  }
+  if (do_hg) {
 #pragma unroll
     for (int k = 0; k < NH; ++k) vals[nv++] = a_h[k];
   }
@@ -1118,10 +1131,11 @@ __global__ void k_reduce_acc(BatchArgs b) {
     const int t = b.slist[it];
     const int s = t >> 1, slot = t & 1;
     const EvalDev& e = b.evals[t];
-    if (!(e.ops & (OP_CHI2 | OP_HG | OP_RPP))) continue;
+    if (!(e.ops & (OP_CHI2 | OP_HG | OP_RPP | OP_VJP))) continue;
     const StampDev& st = b.stamps[s];
     int nv = 1;
     if (e.ops & OP_HG) nv += b.n_free + b.n_free * (b.n_free + 1) / 2;
+    if (e.ops & OP_VJP) nv += b.n_free;
     if (e.ops & OP_RPP) nv += b.n_free;
     for (int k = threadIdx.x; k < nv; k += blockDim.x) {
       double acc = 0;
@@ -1354,6 +1368,20 @@ void Profiler::destroy() {
   ev = nullptr;
   kind = nullptr;
   cap = used = 0;
+}
+
+// grad[s][k] = accumulated VJP of stamp s (slot 0)
+__global__ void k_gather_vjp(BatchArgs b, double* grad) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= b.n_stamps * b.n_free) return;
+  const int s = t / b.n_free, k = t - s * b.n_free;
+  grad[t] = b.acc[((int64_t)s * 2 + 0) * kNacc + 1 + k];
+}
+
+cudaError_t launch_gather_vjp(const BatchArgs& b, double* grad, cudaStream_t s) {
+  const int n = b.n_stamps * b.n_free;
+  if (n > 0) k_gather_vjp<<<(n + 127) / 128, 128, 0, s>>>(b, grad);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_chi2_only(const BatchArgs& b, const ConvIO& io, const float* model,

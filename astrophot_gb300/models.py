@@ -150,8 +150,21 @@ class AstroPhot_Model:
             parameters = None
         return self.sample(image=image, window=window, parameters=parameters, **kwargs)
 
+    # the model's own render components (one galaxy and/or one flat sky)
+    def _components(self):
+        return [self]
+
+    # reverse-mode center gradients as the reference's autograd gives them under PSF shift
+    # (sub-pixel PSF shift path + sampling-coordinate path); False = the render's derivative
+    reference_center_gradient = True
+
     def negative_log_likelihood(self, parameters=None, as_representation=False):
-        """``core_model.py:220-256``: sum over unmasked pixels of W (model - data)^2 / 2."""
+        """``core_model.py:220-256``: sum over unmasked pixels of W (model - data)^2 / 2.
+
+        A ``parameters`` tensor that requires grad makes the result differentiable: its
+        backward is the library's adjoint (``ap_render_vjp``) of the CUDA render."""
+        if isinstance(parameters, torch.Tensor) and parameters.requires_grad:
+            return _NLLFunction.apply(parameters, self, bool(as_representation))
         if parameters is not None:
             (self.parameters.vector_set_representation if as_representation else self.parameters.vector_set_values)(parameters)
         model = self.sample()
@@ -410,6 +423,9 @@ class Group_Model(AstroPhot_Model):
         for m in self.models.values():
             m.initialize()
 
+    def _components(self):
+        return list(self.models.values())
+
     def sample(self, image=None, window=None, parameters=None):
         return _sample_structure(self, list(self.models.values()), image, window)
 
@@ -544,3 +560,39 @@ def _jacobian_structure(owner, components, as_representation, window):
     cols = [J[compact.index(sl)] for sl in order]
     data = np.stack(cols, -1) if cols else np.zeros((ny, nx, 0))
     return Jacobian_Image(owner.parameters.vector_identities(), data, w.copy())
+
+
+class _NLLFunction(torch.autograd.Function):
+    """nll(vector) with the adjoint of the CUDA render as its backward: d nll / d vector =
+    sum_pixels W (model - data) d model / d vector over unmasked pixels."""
+
+    @staticmethod
+    def forward(ctx, vec, owner, as_representation):
+        v = vec.detach().to("cpu", config.ap_dtype)
+        (owner.parameters.vector_set_representation if as_representation else owner.parameters.vector_set_values)(v)
+        struct = _Structure(owner, owner._components())
+        w = owner.window
+        batch, psf_d = _plan(owner, struct, w)
+        params = torch.tensor(struct.full_params()[None, :])
+        model = batch.render(params, psf_d).to(torch.float64)
+        data = owner.target[w]
+        d = batch.pack([data.data.numpy()], torch.float64)
+        wt = batch.pack([data.weight.numpy()], torch.float64)
+        r = model - d
+        if data.has_mask:
+            keep = torch.logical_not(batch.pack([data.mask.numpy().astype(np.uint8)], torch.uint8).bool())
+            r = torch.where(keep, r, torch.zeros_like(r))
+            wt = torch.where(keep, wt, torch.zeros_like(wt))
+        g = wt * r
+        ctx.owner, ctx.as_rep, ctx.struct = owner, as_representation, struct
+        ctx.batch, ctx.psf_d, ctx.params, ctx.g = batch, psf_d, params, g
+        return (0.5 * torch.sum(g * r)).to("cpu", vec.dtype)
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        batch = ctx.batch
+        gc = batch.vjp(ctx.params, ctx.psf_d, ctx.g.to(torch.float32), as_representation=ctx.as_rep,
+                       reference_center=bool(ctx.owner.reference_center_gradient))[0].cpu()
+        compact = [i for i in range(8) if batch.options.free_mask & (1 << i)]
+        grad = torch.tensor([float(gc[compact.index(sl)]) for sl in ctx.struct.vector_order()], dtype=config.ap_dtype)
+        return grad * grad_out.to("cpu", config.ap_dtype), None, None

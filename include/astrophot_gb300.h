@@ -129,6 +129,26 @@ int ap_render(ap_batch* batch, const double* params, const float* psf, float* mo
 int ap_jacobian(ap_batch* batch, const double* params, const float* psf, float* model,
                 float* jac, int32_t as_representation, ap_stream_t stream);
 
+/* Adjoint of the render (vector-Jacobian product): grad_params[n][n_free] (device, float64)
+ * = sum over each stamp's output pixels of grad_model * d model / d theta, theta the fitted
+ * slots in value space or, with AP_VJP_REPRESENTATION, in representation space.
+ * grad_model[out_pixels] (device, float32) is the upstream gradient d loss / d model in the
+ * output layout (weights and masks are the caller's).  The PSF-convolved derivative tiles are
+ * computed and reduced on the fly, never stored.  Replaces autograd's backward through
+ * Component_Model.sample (negative_log_likelihood().backward(),
+ * astrophot/models/core_model.py:220-256).
+ *
+ * Center columns under AP_PSF_FULL: the derivative of the render (what ap_jacobian returns, what
+ * the reference's forward-mode jacobian() returns, and what finite differences give) flows only
+ * through the sub-pixel PSF shift.  The reference's reverse-mode autograd adds the
+ * sampling-coordinate path -d profile / d(x, y) on top (the pixel_shift of the working window,
+ * astrophot/models/model_object.py:319-323, is not seen by backward); AP_VJP_REFERENCE_CENTER
+ * reproduces that value (two extra convolved planes). */
+#define AP_VJP_REPRESENTATION 1
+#define AP_VJP_REFERENCE_CENTER 2
+int ap_render_vjp(ap_batch* batch, const double* params, const float* psf, const float* grad_model,
+                  int32_t flags, double* grad_params, ap_stream_t stream);
+
 /* Shifted, renormalised PSF of every stamp for value-space params (device):
  * out[n][(ky+2)*(kx+2)] packed with stride max_kp2 = (max ky + 2) * (max kx + 2)
  * (see ap_batch_psf_stride).  d_out (optional, may be NULL) receives d/d shift_x and

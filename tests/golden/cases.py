@@ -35,3 +35,14 @@ def load_lm(name):
     d["spec"] = json.loads(str(d["spec"]))
     d["message"] = str(d["message"])
     return d
+
+
+def vjp_case_names():
+    return sorted(os.path.basename(p)[: -len(".npz")] for p in glob.glob(os.path.join(HERE, "vjp_*.npz")))
+
+
+def load_vjp(name):
+    z = np.load(os.path.join(HERE, f"{name}.npz"))
+    d = {k: z[k] for k in z.files}
+    d["spec"] = json.loads(str(d["spec"]))
+    return d

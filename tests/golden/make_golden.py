@@ -320,8 +320,64 @@ def run_lm_case(ap, key, case):
     )
 
 
+VJP_CASES = {
+    # negative_log_likelihood (models/core_model.py:220-256) and its autograd gradient with
+    # respect to the representation vector, Sersic + Moffat 25^2, 96 x 96 crop
+    "vjp_sersic_96": dict(size=96, seed=5, psf=MOFFAT_25, model="sersic"),
+    # exponential, no PSF, a masked block of pixels (center gradients from the coordinates)
+    "vjp_exp_mask_64": dict(size=64, seed=8, psf=None, model="exponential", mask=True),
+}
+
+
+def run_vjp_case(ap, key, case):
+    import torch
+
+    spec = synthetic.c0_stamp(case["seed"], size=case["size"])
+    psf = psf_array(case["psf"]) if case["psf"] is not None else None
+    psf_mode = "full" if psf is not None else "none"
+    mtype = f"{case['model']} galaxy model"
+    cx, cy, q, PA, n, Re, Ie = [float(v) for v in spec.truth]
+
+    def params(cx, cy, q, PA, n, Re, Ie):
+        p = {"center": [cx, cy], "q": q, "PA": PA, "Re": Re, "Ie": Ie}
+        if case["model"] == "sersic":
+            p["n"] = n
+        return p
+
+    kw = dict(pixelscale=1.0) if psf is None else dict(pixelscale=1.0, psf=psf)
+    target = ap.image.Target_Image(data=np.zeros((spec.ny, spec.nx)), **kw)
+    truth_model = ap.models.AstroPhot_Model(name=f"vjp truth {key}", model_type=mtype, target=target,
+                                            psf_mode=psf_mode, parameters=params(cx, cy, q, PA, n, Re, Ie))
+    truth_img = truth_model().data.detach().cpu().numpy()
+    data, weight = synthetic.add_noise(truth_img, spec.seed)
+    mask = np.zeros(data.shape, dtype=bool)
+    if case.get("mask"):
+        mask[5:17, 40:58] = True
+        mask[::7, ::5] = True
+    target = ap.image.Target_Image(data=data, variance=1.0 / weight, mask=mask, **kw)
+    cx, cy, q, PA, n, Re, Ie = [float(v) for v in spec.init]
+    model = ap.models.AstroPhot_Model(name=f"vjp {key}", model_type=mtype, target=target, psf_mode=psf_mode,
+                                      parameters=params(cx, cy, q, PA, n, Re, Ie))
+    rep = model.parameters.vector_representation().detach().clone().requires_grad_(True)
+    nll = model.negative_log_likelihood(parameters=rep, as_representation=True)
+    nll.backward()
+    # the same gradient from the reference's forward-mode jacobian() (what its LM uses)
+    rep0 = rep.detach().clone()
+    J = model.jacobian(parameters=rep0, as_representation=True).data.detach().numpy().reshape(-1, len(rep0))
+    m = model().data.detach().numpy().reshape(-1)
+    keep = np.logical_not(mask.reshape(-1))
+    grad_fwd = J[keep].T @ (weight.reshape(-1)[keep] * (m[keep] - data.reshape(-1)[keep]))
+    return dict(data=data, weight=weight, mask=mask, psf=psf if psf is not None else np.zeros((0, 0)), init=spec.init,
+                rep=rep.detach().numpy(), nll=np.array(nll.item()), grad=rep.grad.detach().numpy(), grad_fwd=grad_fwd,
+                spec=json.dumps(case))
+
+
 def main():
     ap = import_reference()
+    for key, case in VJP_CASES.items():
+        out = run_vjp_case(ap, key, case)
+        np.savez_compressed(os.path.join(HERE, f"{key}.npz"), **out)
+        print("vjp", key, out["nll"], out["grad"], out["grad_fwd"])
     for key, case in RENDER_CASES.items():
         out = run_render_case(ap, key, case)
         np.savez_compressed(os.path.join(HERE, f"render_{key}.npz"), **out)

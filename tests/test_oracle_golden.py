@@ -153,3 +153,91 @@ def test_representation_round_trip(name, vals):
     h = 1e-6 * np.maximum(1.0, np.abs(r))
     fd = (rep_to_value(name, r + h) - rep_to_value(name, r - h)) / (2 * h)
     assert np.allclose(drep_dvalue(name, r), fd, rtol=1e-6, atol=1e-9)
+
+
+# ---- adjoint: the gradient of the reference's negative log-likelihood -------------------
+
+
+def vjp_problem(d):
+    spec = d["spec"]
+    size = spec["size"]
+    cx, cy, q, PA, n, Re, Ie = d["init"]
+    params = {"center": [cx, cy], "q": q, "PA": PA, "Re": Re, "Ie": Ie}
+    if spec["model"] == "sersic":
+        params["n"] = n
+    psf = PSF(d["psf"]) if d["psf"].size else None
+    gal = Component(spec["model"], params, psf_mode="full" if psf is not None else "none")
+    mask = d["mask"] if d["mask"].any() else None
+    return GroupProblem([gal], Window.from_scale(size, size), psf, d["data"], d["weight"], mask)
+
+
+def oracle_nll(prob, rep):
+    """``negative_log_likelihood`` (models/core_model.py:220-256): sum(W (model - data)^2) / 2
+    over the unmasked pixels."""
+    m = prob.forward(rep)
+    keep = np.ones(m.shape, bool) if prob.mask is None else ~prob.mask.reshape(-1)
+    return 0.5 * float(np.sum((prob.W.reshape(-1) * (m - prob.Y.reshape(-1)) ** 2)[keep]))
+
+
+def oracle_nll_grad(prob, rep):
+    """J_rep^T W (model - data) over the unmasked pixels."""
+    J = prob.jacobian(rep)
+    m = prob.forward(rep)
+    keep = np.ones(m.shape, bool) if prob.mask is None else ~prob.mask.reshape(-1)
+    return J[keep].T @ (prob.W.reshape(-1)[keep] * (m - prob.Y.reshape(-1))[keep])
+
+
+@pytest.mark.parametrize("name", cases.vjp_case_names())
+def test_nll_gradient_matches_reference(name):
+    """The oracle's adjoint J_rep^T W (model - data) equals the reference's forward-mode
+    jacobian() contracted with the residual (``grad_fwd``) and the FP64 central difference of
+    the oracle's nll; it equals the reference's reverse-mode autograd gradient (``grad``) except
+    for the center under PSF shift, where reverse mode adds the sampling-coordinate path."""
+    d = cases.load_vjp(name)
+    prob = vjp_problem(d)
+    rep = prob.representation()
+    assert np.allclose(rep, d["rep"], rtol=0, atol=1e-13)
+    assert oracle_nll(prob, rep) == pytest.approx(float(d["nll"]), rel=1e-12)
+    g = oracle_nll_grad(prob, rep)
+    scale = np.max(np.abs(d["grad_fwd"]))
+    assert np.max(np.abs(g - d["grad_fwd"])) <= 1e-9 * scale, (g, d["grad_fwd"])
+    shifted = d["psf"].size > 0
+    rest = slice(2, None) if shifted else slice(None)
+    assert np.max(np.abs(g[rest] - d["grad"][rest])) <= 1e-9 * scale
+    fd = np.zeros_like(rep)
+    for k in range(len(rep)):
+        h = 1e-6 * max(1.0, abs(rep[k]))
+        rp, rm = rep.copy(), rep.copy()
+        rp[k] += h
+        rm[k] -= h
+        fd[k] = (oracle_nll(prob, rp) - oracle_nll(prob, rm)) / (2 * h)
+    assert np.max(np.abs(fd - d["grad_fwd"])) <= 1e-5 * scale, (fd, d["grad_fwd"])
+
+
+def test_reverse_mode_center_gradient_is_shift_plus_coordinate_path():
+    """Under PSF shift the reference's reverse-mode center gradient equals the derivative through
+    the sub-pixel PSF shift plus the sampling-coordinate path -d profile / d(x, y) (convolved with
+    the shifted PSF): the pixel_shift of the working window (models/model_object.py:319-323)
+    that cancels the coordinate path in the forward function is not seen by backward."""
+    import oracle.render as R
+
+    d = cases.load_vjp("vjp_sersic_96")
+    prob = vjp_problem(d)
+    prob.set_representation(prob.representation())
+    comp = prob.components[0]
+    captured = {}
+    orig = R._component_partials
+
+    def with_coords(comp_, deep, finish, from_coords, win):
+        jc = orig(comp_, deep, finish, True, win)
+        captured["coords"] = (jc[("center", 0)], jc[("center", 1)])
+        return orig(comp_, deep, finish, from_coords, win)
+
+    R._component_partials = with_coords
+    try:
+        r = R.sample_component(comp, prob.window, prob.psf, grad=True)
+    finally:
+        R._component_partials = orig
+    res = prob.W * (r.model - prob.Y)
+    gc = [np.sum(res * (r.jac[("center", k)] + captured["coords"][k])) for k in range(2)]
+    assert np.allclose(gc, d["grad"][:2], rtol=1e-11, atol=0)
