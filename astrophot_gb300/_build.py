@@ -1,6 +1,6 @@
 """Build recipe for the CUDA library (``libastrophot_gb300.so``), sm_103a only.
 
-``python -m astrophot_gb300._build`` compiles the three translation units in
+``python -m astrophot_gb300._build`` compiles the translation units in
 parallel and links them into the package directory.  No cmake, no torch
 extension machinery: plain ``nvcc`` with ``-gencode arch=compute_103a,code=sm_103a``.
 """
@@ -16,7 +16,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libastrophot_gb300.so")
-SOURCES = ("ap_kernels.cu", "ap_lm.cu", "ap_capi.cu", "ap_noalloc.cu")
+SOURCES = ("ap_kernels.cu", "ap_lm.cu", "ap_capi.cu", "ap_noalloc.cu", "ap_cnn.cu")
 ARCH = ("-gencode", "arch=compute_103a,code=sm_103a")
 FLAGS = ("-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2")
 

@@ -118,9 +118,29 @@ EXPORTS = [
     ("ap_fma_probe", [_P, _I32, _I32, _P]),
     ("ap_batch_stats", [_P, _PI64]),
     ("ap_render_noalloc", [_I32, _I32, _I32, _I32, _PD, ctypes.POINTER(ApOptions), _P, _P, _P, _P]),
+    ("ap_cnn_param_count", []),
+    ("ap_cnn_workspace_bytes", [_I64]),
+    ("ap_cnn_layer_offsets", [_PI64, _PI64, _PI32]),
+    ("ap_cnn_to_bf16", [_P, _P, _P]),
+    ("ap_cnn_forward", [_P, _P, _P, _I64, _P, _P, ctypes.c_size_t, _P]),
+    ("ap_cnn_backward", [_P, _P, _I64, _P, _P, ctypes.c_size_t, _P]),
+    ("ap_cnn_train_step", [_P, _P, _P, _P, _P, _P, _P, _I64, ctypes.c_float, _I32, ctypes.c_float, _P, _P,
+                           ctypes.c_size_t, _P]),
+    ("ap_cnn_prepare", [_P, _P, _P, _I64, _P, _P, _P]),
+    ("ap_cnn_decode", [_P, _P, _P, _P, _P, _I64, _P, _P]),
+    ("ap_moments_init", [_P, _P, _P, _P, _I64, _P, _P]),
+    ("ap_select_init", [_P, _P, _P, _P, _I64, _P, _P, _P]),
+    ("ap_gemm_bf16", [_P, _I32, _I32, _P, _I32, _I32, _P, _I32, _I32, _I32, _I32, _P]),
     ("ap_version", []),
     ("ap_last_cuda_error", []),
 ]
+
+_RESTYPES = {
+    "ap_version": ctypes.c_char_p,
+    "ap_last_cuda_error": ctypes.c_char_p,
+    "ap_cnn_param_count": ctypes.c_int64,
+    "ap_cnn_workspace_bytes": ctypes.c_size_t,
+}
 
 
 def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
@@ -133,7 +153,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     for name, argtypes in EXPORTS:
         fn = getattr(lib, name)
         fn.argtypes = argtypes
-        fn.restype = ctypes.c_char_p if name in ("ap_version", "ap_last_cuda_error") else ctypes.c_int
+        fn.restype = _RESTYPES.get(name, ctypes.c_int)
     return lib
 
 

@@ -1,0 +1,345 @@
+"""Learned initial guess for Sersic fits of 64 x 64 stamps.
+
+No counterpart in the reference: AstroPhot starts its LM from the heuristics of
+``Galaxy_Model.initialize`` / ``parametric_initialize`` (models/galaxy_model_object.py:60-113,
+models/_shared_methods.py:116-166).  Here a 6-layer CNN (``ap_cnn_*`` in the C ABI, bf16
+tensor-core GEMMs with fp32 accumulation) proposes the 7 Sersic parameters; the LM starts from
+the proposal unless its chi^2 is worse than that of the moments initialiser
+(``ap_moments_init``), which is then used instead (the fallback).
+
+Training data come only from the library's own renderer: Sersic stamps drawn from the C0
+parameter distributions (centre 32 + U(-1, 1), n ~ U(0.5, 4), Re ~ U(5, 20), q ~ U(0.3, 1),
+PA ~ U(0, pi), log10 Ie ~ U(0, 2)), a flat sky of 1.0, a Moffat PSF (beta 3.5) with
+FWHM ~ U(2, 5) px (64 levels, 21 x 21 box) and Gaussian noise of constant sigma set by a
+signal-to-noise ratio ~ U(10, 200), SNR = sqrt(sum(galaxy^2)) / sigma.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+import torch
+
+from . import _native as N
+from .synthetic import moffat_rd, moffat_stamp
+
+__all__ = ("InitNet", "StampSet", "draw_stamp_params", "psf_bank", "make_stamps", "learned_fit", "plain_fit",
+           "WEIGHTS_PATH")
+
+IMG = 64
+PSF_BOX = 21
+N_OUT = 8
+OUT_PAD = 16
+WEIGHTS_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights", "init_cnn.npz")
+
+
+# ---- synthetic stamps ----------------------------------------------------------------------
+def draw_stamp_params(rng: np.random.Generator, n: int, size: int = IMG) -> np.ndarray:
+    """[n, 8] value-space vectors (F = 0: sky 1.0) from the C0 distributions."""
+    p = np.zeros((n, 8))
+    p[:, 0] = size / 2 + rng.uniform(-1, 1, n)
+    p[:, 1] = size / 2 + rng.uniform(-1, 1, n)
+    q = rng.uniform(0.3, 1.0, n)
+    bad = q >= 0.999
+    while bad.any():
+        q[bad] = rng.uniform(0.3, 1.0, int(bad.sum()))
+        bad = q >= 0.999
+    p[:, 2] = q
+    p[:, 3] = rng.uniform(0.0, math.pi, n)
+    p[:, 4] = rng.uniform(0.5, 4.0, n)
+    p[:, 5] = rng.uniform(5.0, 20.0, n)
+    p[:, 6] = rng.uniform(0.0, 2.0, n)
+    return p
+
+
+def psf_bank(levels: int = 64, beta: float = 3.5) -> np.ndarray:
+    """[levels, 21, 21] Moffat stamps, FWHM evenly spaced on [2, 5] px, each drawn at side
+    odd(4 FWHM) and centred in the 21 x 21 box (zeros around)."""
+    out = np.zeros((levels, PSF_BOX, PSF_BOX))
+    for i, fwhm in enumerate(np.linspace(2.0, 5.0, levels)):
+        w = int(round(4 * fwhm))
+        w += 1 - (w % 2)
+        st = moffat_stamp(beta, moffat_rd(fwhm, beta), w)
+        o = (PSF_BOX - w) // 2
+        out[i, o : o + w, o : o + w] = st
+    return out
+
+
+@dataclass
+class StampSet:
+    """A batch of 64 x 64 stamps on the device (packed [n * 4096] float32)."""
+
+    truth: np.ndarray       # [n, 8]
+    data: torch.Tensor      # [n * 4096]
+    weight: torch.Tensor    # [n * 4096]
+    psf: torch.Tensor       # [n * 441]
+    sigma: torch.Tensor     # [n]
+    batch: "N.StampBatch"
+
+
+_BATCHES = {}
+
+
+def _stamp_batch(n: int, device) -> "N.StampBatch":
+    key = (n, str(device))
+    if key not in _BATCHES:
+        opts = N.make_options(profile="sersic", psf_mode="full", free_mask=0x7F, has_sky=True)
+        _BATCHES.clear()
+        _BATCHES[key] = N.StampBatch([(IMG, IMG)] * n, [(PSF_BOX, PSF_BOX)] * n, N.scale_geometry(n), opts, device)
+    return _BATCHES[key]
+
+
+def make_stamps(n: int, seed: int, bank: Optional[torch.Tensor] = None, device="cuda", snr=(10.0, 200.0)) -> StampSet:
+    """Render ``n`` stamps with the library's own kernels and add seeded Gaussian noise."""
+    rng = np.random.default_rng(seed)
+    truth = draw_stamp_params(rng, n)
+    if bank is None:
+        bank = torch.tensor(psf_bank(), dtype=torch.float32, device=device)
+    idx = torch.tensor(rng.integers(0, bank.shape[0], n), device=device)
+    psf = bank[idx].reshape(-1).contiguous()
+    b = _stamp_batch(n, device)
+    model = b.render(torch.tensor(truth), psf)
+    gal = (model - 1.0).view(n, IMG * IMG)
+    s = torch.tensor(rng.uniform(snr[0], snr[1], n), dtype=torch.float32, device=device)
+    sigma = torch.sqrt(torch.sum(gal.double() ** 2, dim=1)).float() / s
+    gen = torch.Generator(device=device)
+    gen.manual_seed(int(seed) * 7919 + 17)
+    noise = torch.randn((n, IMG * IMG), generator=gen, device=device, dtype=torch.float32)
+    data = (model.view(n, -1) + sigma[:, None] * noise).reshape(-1).contiguous()
+    weight = (torch.ones((n, IMG * IMG), device=device) / (sigma[:, None] ** 2)).reshape(-1).contiguous()
+    return StampSet(truth, data, weight, psf, sigma, b)
+
+
+# ---- the network ---------------------------------------------------------------------------
+def _targets(truth: torch.Tensor, lscale: torch.Tensor) -> torch.Tensor:
+    """Raw regression targets [n, 8] (see ``ap_cnn_decode``)."""
+    t = torch.empty((truth.shape[0], N_OUT), dtype=torch.float64, device=truth.device)
+    t[:, 0] = truth[:, 0] - IMG / 2
+    t[:, 1] = truth[:, 1] - IMG / 2
+    t[:, 2] = truth[:, 2]
+    t[:, 3] = torch.cos(2 * truth[:, 3])
+    t[:, 4] = torch.sin(2 * truth[:, 3])
+    t[:, 5] = torch.log(truth[:, 4])
+    t[:, 6] = torch.log(truth[:, 5])
+    t[:, 7] = truth[:, 6] - lscale.double()  # log10 Ie - log10 sigma
+    return t
+
+
+class InitNet:
+    """Parameters (fp32 master + bf16 mirror), output statistics, training and inference."""
+
+    def __init__(self, device="cuda", seed: int = 0):
+        self.device = torch.device(device)
+        self.lib = N.lib()
+        self.count = int(self.lib.ap_cnn_param_count())
+        w_off = (ctypes.c_int64 * 6)()
+        b_off = (ctypes.c_int64 * 6)()
+        dims = (ctypes.c_int32 * 36)()
+        N.check(self.lib.ap_cnn_layer_offsets(w_off, b_off, dims), "ap_cnn_layer_offsets")
+        self.w_off, self.b_off = list(w_off), list(b_off)
+        self.dims = np.array(list(dims)).reshape(6, 6)
+        rng = np.random.default_rng(seed)
+        p = np.zeros(self.count, dtype=np.float32)
+        for l in range(6):
+            cin, cout, hin, hout, K, Nn = self.dims[l]
+            fan_in = 9 * cin if l < 4 else K
+            W = rng.normal(0.0, math.sqrt(2.0 / fan_in), size=(Nn, K)).astype(np.float32)
+            if l == 0:
+                W[:, 9:] = 0.0
+            if l == 5:
+                W *= 0.1
+                W[N_OUT:] = 0.0
+            p[self.w_off[l] : self.w_off[l] + Nn * K] = W.reshape(-1)
+        self.params = torch.tensor(p, device=self.device)
+        self.params_bf16 = torch.empty(self.count, dtype=torch.bfloat16, device=self.device)
+        self._sync_bf16()
+        self.mean = torch.zeros(N_OUT, dtype=torch.float32, device=self.device)
+        self.std = torch.ones(N_OUT, dtype=torch.float32, device=self.device)
+        self._ws = None
+        self._ws_batch = 0
+        self.history = []
+
+    def _sync_bf16(self):
+        N.check(self.lib.ap_cnn_to_bf16(N._ptr(self.params), N._ptr(self.params_bf16), N._stream()), "ap_cnn_to_bf16")
+
+    def _workspace(self, batch: int):
+        need = int(self.lib.ap_cnn_workspace_bytes(batch))
+        if self._ws is None or self._ws.numel() < need:
+            self._ws = torch.empty(need, dtype=torch.uint8, device=self.device)
+        return self._ws
+
+    # -- persistence --
+    def save(self, path: str = WEIGHTS_PATH):
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        np.savez_compressed(path, params=self.params.cpu().numpy(), mean=self.mean.cpu().numpy(),
+                            std=self.std.cpu().numpy(), history=np.array(self.history, dtype=np.float64))
+
+    @classmethod
+    def load(cls, path: str = WEIGHTS_PATH, device="cuda") -> "InitNet":
+        z = np.load(path)
+        net = cls(device)
+        if z["params"].shape[0] != net.count:
+            raise ValueError(f"{path}: {z['params'].shape[0]} parameters, the network has {net.count}")
+        net.params = torch.tensor(z["params"], dtype=torch.float32, device=net.device)
+        net.mean = torch.tensor(z["mean"], dtype=torch.float32, device=net.device)
+        net.std = torch.tensor(z["std"], dtype=torch.float32, device=net.device)
+        net.history = list(z["history"]) if "history" in z.files else []
+        net._sync_bf16()
+        return net
+
+    # -- kernels --
+    def prepare(self, data: torch.Tensor, sigma: torch.Tensor, n: int, sky: float = 1.0):
+        x = torch.empty(n * IMG * IMG, dtype=torch.float32, device=self.device)
+        lscale = torch.empty(n, dtype=torch.float32, device=self.device)
+        skyv = torch.full((n,), sky, dtype=torch.float32, device=self.device)
+        sg = sigma.to(self.device, torch.float32).contiguous()
+        N.check(self.lib.ap_cnn_prepare(N._ptr(data), N._ptr(skyv), N._ptr(sg), n, N._ptr(x), N._ptr(lscale),
+                                        N._stream()), "ap_cnn_prepare")
+        return x, lscale
+
+    def forward(self, x: torch.Tensor, n: int) -> torch.Tensor:
+        if n % 16:
+            raise ValueError("batches of the CNN are multiples of 16 stamps")
+        ws = self._workspace(n)
+        out = torch.empty((n, OUT_PAD), dtype=torch.float32, device=self.device)
+        N.check(self.lib.ap_cnn_forward(N._ptr(self.params), N._ptr(self.params_bf16), N._ptr(x), n, N._ptr(out),
+                                        N._ptr(ws), ws.numel(), N._stream()), "ap_cnn_forward")
+        return out
+
+    def backward(self, dout: torch.Tensor, n: int) -> torch.Tensor:
+        ws = self._workspace(n)
+        grads = torch.empty(self.count, dtype=torch.float32, device=self.device)
+        N.check(self.lib.ap_cnn_backward(N._ptr(self.params_bf16), N._ptr(dout.contiguous()), n, N._ptr(grads),
+                                         N._ptr(ws), ws.numel(), N._stream()), "ap_cnn_backward")
+        return grads
+
+    def propose(self, data: torch.Tensor, sigma: torch.Tensor, n: int, sky_F: float = 0.0,
+                chunk: int = 8192) -> torch.Tensor:
+        """[n, 8] value-space proposals for packed 64 x 64 stamps (sky = 10^sky_F, noise sigma[n])."""
+        out = torch.empty((n, 8), dtype=torch.float64, device=self.device)
+        sky = 10.0**sky_F
+        for s in range(0, n, chunk):
+            m = min(chunk, n - s)
+            mp = (m + 15) // 16 * 16
+            d = data[s * IMG * IMG : (s + m) * IMG * IMG]
+            sg = sigma[s : s + m]
+            if mp != m:
+                d = torch.cat([d, torch.full(((mp - m) * IMG * IMG,), sky, dtype=torch.float32, device=self.device)])
+                sg = torch.cat([sg, torch.ones(mp - m, dtype=sg.dtype, device=sg.device)])
+            x, lscale = self.prepare(d.contiguous(), sg, mp, sky)
+            o = self.forward(x, mp)
+            skyF = torch.full((mp,), sky_F, dtype=torch.float64, device=self.device)
+            p = torch.empty((mp, 8), dtype=torch.float64, device=self.device)
+            N.check(self.lib.ap_cnn_decode(N._ptr(o), N._ptr(lscale), N._ptr(self.mean), N._ptr(self.std),
+                                           N._ptr(skyF), mp, N._ptr(p), N._stream()), "ap_cnn_decode")
+            out[s : s + m] = p[:m]
+        return out
+
+    # -- training --
+    def set_statistics(self, raw_targets: torch.Tensor):
+        self.mean = raw_targets.mean(dim=0).float().contiguous()
+        self.std = raw_targets.std(dim=0).clamp_min(1e-3).float().contiguous()
+
+    def train(self, n_stamps: int = 2_000_000, batch: int = 512, chunk: int = 8192, lr: float = 1e-3,
+              lr_end: float = 2e-5, warmup: int = 200, weight_decay: float = 1e-4, seed: int = 1, log_every: int = 0):
+        """Adam on fresh rendered stamps (each stamp seen once)."""
+        if batch % 16 or chunk % batch:
+            raise ValueError("batch must be a multiple of 16 dividing chunk")
+        bank = torch.tensor(psf_bank(), dtype=torch.float32, device=self.device)
+        m1 = torch.zeros(self.count, dtype=torch.float32, device=self.device)
+        m2 = torch.zeros_like(m1)
+        grads = torch.zeros_like(m1)
+        loss_d = torch.zeros(1, dtype=torch.float64, device=self.device)
+        ws = self._workspace(batch)
+        n_chunks = max(1, n_stamps // chunk)
+        total_steps = n_chunks * (chunk // batch)
+        step = 0
+        losses = []
+        for c in range(n_chunks):
+            st = make_stamps(chunk, seed * 1_000_003 + c, bank, self.device)
+            x, lscale = self.prepare(st.data, st.sigma, chunk)
+            raw = _targets(torch.tensor(st.truth, device=self.device), lscale)
+            if c == 0 and step == 0:
+                self.set_statistics(raw)
+            t = ((raw - self.mean.double()) / self.std.double()).float().contiguous()
+            for b0 in range(0, chunk, batch):
+                step += 1
+                if step <= warmup:
+                    lr_t = lr * step / warmup
+                else:
+                    f = (step - warmup) / max(1, total_steps - warmup)
+                    lr_t = lr_end + 0.5 * (lr - lr_end) * (1 + math.cos(math.pi * min(1.0, f)))
+                xb = x[b0 * IMG * IMG : (b0 + batch) * IMG * IMG]
+                tb = t[b0 : b0 + batch]
+                N.check(self.lib.ap_cnn_train_step(
+                    N._ptr(self.params), N._ptr(self.params_bf16), N._ptr(grads), N._ptr(m1), N._ptr(m2), N._ptr(xb),
+                    N._ptr(tb), batch, ctypes.c_float(lr_t), step, ctypes.c_float(weight_decay), N._ptr(loss_d),
+                    N._ptr(ws), ws.numel(), N._stream()), "ap_cnn_train_step")
+                if b0 == 0:
+                    losses.append(loss_d.clone())
+            if log_every and (c + 1) % log_every == 0:
+                print(f"chunk {c + 1}/{n_chunks} step {step} loss {losses[-1].item():.4f}", flush=True)
+        self.history = [float(v.item()) for v in losses]
+        return self.history
+
+    def loss(self, st: StampSet, n: int) -> float:
+        """Mean squared standardised error on a stamp set."""
+        x, lscale = self.prepare(st.data, st.sigma, n)
+        out = self.forward(x, n)
+        raw = _targets(torch.tensor(st.truth, device=self.device), lscale)
+        t = (raw - self.mean.double()) / self.std.double()
+        return float(torch.mean((out[:, :N_OUT].double() - t) ** 2).item())
+
+
+# ---- fits from the two kinds of initial values --------------------------------------------
+def moments_init(st: StampSet, n: int, sky_F: float = 0.0) -> torch.Tensor:
+    lib = N.lib()
+    dev = st.data.device
+    sky = torch.full((n,), 10.0**sky_F, dtype=torch.float32, device=dev)
+    skyF = torch.full((n,), sky_F, dtype=torch.float64, device=dev)
+    out = torch.empty((n, 8), dtype=torch.float64, device=dev)
+    N.check(lib.ap_moments_init(N._ptr(st.data), N._ptr(sky), N._ptr(st.sigma.contiguous()), N._ptr(skyF), n,
+                                N._ptr(out), N._stream()), "ap_moments_init")
+    return out
+
+
+def _lm(st: StampSet, init: torch.Tensor, lm_options):
+    from .transforms import SLOT_LIMITS
+
+    b = st.batch
+    # representation of the 7 fitted slots, computed on the device in float64
+    rep = torch.empty((init.shape[0], 7), dtype=torch.float64, device=init.device)
+    rep[:, 0:2] = init[:, 0:2]
+    rep[:, 2] = torch.tan(init[:, 2] * math.pi - math.pi / 2)           # q in (0, 1)
+    rep[:, 3] = torch.remainder(init[:, 3], math.pi)                     # PA cyclic
+    lo, hi = SLOT_LIMITS[4][0]
+    rep[:, 4] = torch.tan((init[:, 4] - lo) * math.pi / (hi - lo) - math.pi / 2)
+    rep[:, 5] = init[:, 5] - 1.0 / init[:, 5]                            # Re > 0
+    rep[:, 6] = init[:, 6]
+    return b.lm_fit(st.data, st.weight, None, st.psf, init.contiguous(), rep.contiguous(), lm_options)
+
+
+def plain_fit(st: StampSet, n: int, lm_options=None):
+    """LM from the moments initial values."""
+    init = moments_init(st, n)
+    return init, _lm(st, init, lm_options or N.make_lm_options())
+
+
+def learned_fit(net: InitNet, st: StampSet, n: int, lm_options=None):
+    """LM from the CNN proposal, or from the moments values where those have the lower chi^2."""
+    lib = N.lib()
+    b = st.batch
+    prop = net.propose(st.data, st.sigma, n)
+    fall = moments_init(st, n)
+    c_p = b.chi2(st.data, st.weight, None, b.render(prop, st.psf))
+    c_f = b.chi2(st.data, st.weight, None, b.render(fall, st.psf))
+    init = torch.empty_like(prop)
+    which = torch.empty(n, dtype=torch.int32, device=prop.device)
+    N.check(lib.ap_select_init(N._ptr(prop), N._ptr(fall), N._ptr(c_p), N._ptr(c_f), n, N._ptr(init), N._ptr(which),
+                               N._stream()), "ap_select_init")
+    return init, which, _lm(st, init, lm_options or N.make_lm_options())

@@ -141,15 +141,19 @@ int validate_options(const ap_options* o) {
   return AP_OK;
 }
 
+int check_cuda(cudaError_t e) { return record_cuda(e); }
+
+}  // namespace
+
+namespace apgb {
 thread_local cudaError_t g_last_cuda_error = cudaSuccess;
 
-int check_cuda(cudaError_t e) {
+int record_cuda(cudaError_t e) {
   if (e == cudaSuccess) return AP_OK;
   g_last_cuda_error = e;
   return AP_ERR_CUDA;
 }
-
-}  // namespace
+}  // namespace apgb
 
 extern "C" {
 

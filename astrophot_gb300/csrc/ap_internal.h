@@ -63,10 +63,15 @@ struct Profiler {
   long long launches[KC_COUNT] = {0};
   int begin(int k, cudaStream_t s);
   void end(int idx, cudaStream_t s);
+  void record(cudaEvent_t e, cudaStream_t s);
   void harvest(bool reset);  // after a synchronise: add elapsed times of the used pairs
   void clear_totals();
   void destroy();
 };
+
+// AP_OK for cudaSuccess, else remembers the error for ap_last_cuda_error and returns AP_ERR_CUDA
+int record_cuda(cudaError_t e);
+extern thread_local cudaError_t g_last_cuda_error;
 
 // render-pass launches (ap_kernels.cu)
 cudaError_t launch_eval_setup(const BatchArgs& b, const double* params, int64_t stamp_stride,

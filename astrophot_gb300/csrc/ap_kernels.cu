@@ -1330,14 +1330,22 @@ int Profiler::begin(int k, cudaStream_t s) {
   }
   const int idx = used++;
   kind[idx] = k;
-  // External records become event-record nodes when the stream is being captured
-  cudaEventRecordWithFlags(ev[2 * idx], s, cudaEventRecordExternal);
+  record(ev[2 * idx], s);
   return idx;
 }
 
-void Profiler::end(int idx, cudaStream_t s) {
-  cudaEventRecordWithFlags(ev[2 * idx + 1], s, cudaEventRecordExternal);
+// External records become event-record nodes when the stream is being captured; outside a
+// capture the flag is not accepted, and a plain record does the same job.
+void Profiler::record(cudaEvent_t e, cudaStream_t s) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(s, &cs);
+  if (cs == cudaStreamCaptureStatusActive)
+    cudaEventRecordWithFlags(e, s, cudaEventRecordExternal);
+  else
+    cudaEventRecord(e, s);
 }
+
+void Profiler::end(int idx, cudaStream_t s) { record(ev[2 * idx + 1], s); }
 
 void Profiler::harvest(bool reset) {
   for (int i = 0; i < used; ++i) {

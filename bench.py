@@ -1,13 +1,21 @@
-"""Benchmark: converged Levenberg-Marquardt Sersic fits per second on one GB300.
+"""Benchmark: converged Levenberg-Marquardt Sersic fits per second on one GB300,
+learned + batched against plain.
 
-Workload (one "step" = one batched LM fit of every stamp from its initial guess):
-  batched cutouts -- N stamps (default 8192) with sides round(log-uniform(32, 256)) px,
-  each one Sersic galaxy + a flat sky of 1.0 (locked), its own Moffat PSF (beta 3.5,
-  FWHM ~ U(2, 5) px, side = 4 FWHM rounded to odd), Gaussian noise sigma = sqrt(model + 10),
-  7 free parameters from the truth perturbed by 10 %.  Rendering is FP32 with
-  midpoint sampling + the reference's adaptive threshold integration, bilinear sub-pixel
-  PSF shift and PSF convolution; LM accumulators, damping solves and chi^2 are FP64.
-  Seeded synthetic data (no public dataset exists for this path).
+Workloads (one "step" = every stamp of the workload fitted once, from its initial values):
+  learned (default) -- 65,536 held-out 64 x 64 stamps rendered by this library: one Sersic
+      galaxy from the C0 distributions + a flat sky of 1.0 (locked), Moffat PSF (beta 3.5,
+      FWHM ~ U(2, 5) px, 21 x 21 box), Gaussian noise of constant sigma at SNR ~ U(10, 200).
+      A step = CNN proposal (bf16 tensor-core kernels) + moments fallback, chi^2 of both,
+      per-stamp selection, then one batched LM of all stamps (7 free parameters).
+      Reported beside it: the plain method = LM from the moments values, batched and one
+      stamp at a time.
+  cutouts -- N stamps (default 8192) with sides round(log-uniform(32, 256)) px, each one
+      Sersic galaxy + a flat sky of 1.0 (locked), its own Moffat PSF (beta 3.5, FWHM ~
+      U(2, 5) px, side = 4 FWHM rounded to odd), noise sigma = sqrt(model + 10), 7 free
+      parameters from the truth perturbed by 10 %.
+Rendering is FP32 with midpoint sampling + the reference's adaptive threshold integration,
+bilinear sub-pixel PSF shift and PSF convolution; LM accumulators, damping solves and chi^2
+are FP64.  Seeded synthetic data (no public dataset exists for this path).
 
 Arms:
   default            the CUDA path (libastrophot_gb300.so) -- JSON line with value (device
@@ -44,13 +52,17 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--stamps", type=int, default=8192)
+    p.add_argument("--workload", default="learned", choices=["learned", "cutouts"])
+    p.add_argument("--stamps", type=int, default=None, help="65536 (learned) / 8192 (cutouts)")
     p.add_argument("--seed", type=int, default=2024)
     p.add_argument("--cpu-sample", type=int, default=8, help="stamps fitted by the CPU baseline")
     p.add_argument("--rounds-per-sync", type=int, default=8)
     p.add_argument("--no-graph", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
-    return p.parse_args()
+    a = p.parse_args()
+    if a.stamps is None:
+        a.stamps = 65536 if a.workload == "learned" else 8192
+    return a
 
 
 def rank_info():
@@ -237,6 +249,13 @@ class ClockSampler:
 
 
 def run_gpu(args):
+    if args.workload == "learned":
+        run_gpu_learned(args)
+    else:
+        run_gpu_cutouts(args)
+
+
+def run_gpu_cutouts(args):
     import torch
 
     from astrophot_gb300 import _native as N
@@ -438,10 +457,326 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
+# ----------------------------------------------------------------------------------------
+# learned + batched workload
+# ----------------------------------------------------------------------------------------
+
+
+def learned_sample_jobs(S, seed, idx, data_of=None, init_of=None):
+    """Oracle LM jobs for stamps ``idx`` of the learned workload.  ``data_of(i)`` gives the
+    (data, sigma) the GPU fitted; without it the stamp is re-rendered by the oracle with
+    numpy noise of the same sigma rule (same truth, PSF and SNR draws as the GPU's)."""
+    from astrophot_gb300 import cnn
+    from oracle.init import moments_init
+    from oracle.render import PSF, Component, Window, sample_group
+
+    rng = np.random.default_rng(seed)
+    truth = cnn.draw_stamp_params(rng, S)
+    pidx = rng.integers(0, 64, S)
+    snr = rng.uniform(10.0, 200.0, S)
+    bank = cnn.psf_bank().astype(np.float32).astype(np.float64)
+    jobs = []
+    for i in idx:
+        psf = bank[pidx[i]]
+        if data_of is not None:
+            data, sigma = data_of(i)
+        else:
+            cx, cy, q, PA, n, Re, Ie, F = truth[i]
+            gal = Component("sersic", {"center": [cx, cy], "q": q, "PA": PA, "n": n, "Re": Re, "Ie": Ie},
+                            psf_mode="full")
+            sky = Component("flat_sky", {"F": 0.0}, locked=("F",))
+            model, _ = sample_group([gal, sky], Window.from_scale(64, 64), PSF(psf))
+            sigma = math.sqrt(np.sum((model - 1.0) ** 2)) / snr[i]
+            data = model + sigma * np.random.default_rng(seed * 7919 + 17 + int(i)).normal(size=model.shape)
+        weight = np.full(data.shape, 1.0 / sigma**2)
+        init = init_of(i) if init_of is not None else moments_init(data, 1.0, sigma)
+        jobs.append((data, weight, psf, init, truth[i]))
+    return jobs
+
+
+def run_reference_learned(args):
+    """--impl reference, learned workload: the plain method on the CPU (moments initial values,
+    then the float64 restatement of the reference LM) over all host cores on a bounded sample."""
+    rank, world, _ = rank_info()
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    k = min(args.stamps, 2 * cores)
+    idx = list(np.linspace(0, args.stamps - 1, k).round().astype(int))
+    jobs = learned_sample_jobs(args.stamps, args.seed, idx)
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(processes=min(cores, len(jobs))) as pool:
+        if args.warmup > 0:
+            pool.map(_oracle_fit, jobs[: min(len(jobs), cores)])
+        times = []
+        for _ in range(args.steps):
+            t = time.perf_counter()
+            res = pool.map(_oracle_fit, jobs)
+            times.append(time.perf_counter() - t)
+    dt = statistics.median(times)
+    value = len(jobs) / dt
+    line = {
+        "impl": "reference",
+        "metric": "LM Sersic fits/s (chi2 within 1e-4 of the FP64 oracle), learned+batched vs plain",
+        "value": value,
+        "unit": "fits/s",
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": dt * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {
+            "workload": f"learned init: {args.stamps} held-out 64x64 Sersic stamps + sky, Moffat FWHM 2-5 px, "
+            "SNR 10-200; plain method (moments initial values, float64 LM)",
+            "sample": f"{len(jobs)} stamps evenly spaced over the workload, {min(cores, len(jobs))} processes",
+        },
+        "cpu_baseline": {
+            "value": value,
+            "unit": "fits/s",
+            "cores": min(cores, len(jobs)),
+            "kind": "port",
+            "sample": f"{len(jobs)} stamps (float64 numpy restatement of the reference LM from moments values)",
+        },
+        "e2e": {"value": value, "unit": "fits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "mean_iterations": float(np.mean([r[1] for r in res])),
+    }
+    print(json.dumps(line), flush=True)
+
+
+# kernels of this library launched per CNN proposal chunk: prepare, input im2col, 3 im2col,
+# 6 GEMMs, 6 bias/activation passes, decode
+CNN_LAUNCHES_PER_CHUNK = 18
+
+
+def run_gpu_learned(args):
+    import torch
+
+    from astrophot_gb300 import _native as N
+    from astrophot_gb300 import cnn
+
+    rank, world, local = rank_info()
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", torch.cuda.current_device())
+    S = args.stamps
+    seed = args.seed + 7919 * rank
+    st = cnn.make_stamps(S, seed, device=dev)
+    net = cnn.InitNet.load(device=dev)
+    lmo = N.make_lm_options(rounds_per_sync=args.rounds_per_sync, use_graph=not args.no_graph)
+    batch = st.batch
+    data_h = st.data.cpu().pin_memory()
+    weight_h = st.weight.cpu().pin_memory()
+    psf_h = st.psf.cpu().pin_memory()
+    sigma_h = st.sigma.cpu().pin_memory()
+
+    def step_device():
+        return cnn.learned_fit(net, st, S, lmo)
+
+    def step_plain():
+        return cnn.plain_fit(st, S, lmo)
+
+    for _ in range(max(args.warmup, 0)):
+        step_device()
+    step_plain()
+    torch.cuda.synchronize()
+
+    # ---- value: learned + batched, inputs resident in HBM --------------------------------
+    batch.profile(True)
+    batch.work_counters(reset=True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    results = []
+    with ClockSampler(local) as clk:
+        e0.record()
+        for _ in range(args.steps):
+            results.append(step_device())
+        e1.record()
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    dev_ms = e0.elapsed_time(e1) / args.steps
+    ktimes = batch.kernel_times()
+    work = batch.work_counters(reset=True)
+    batch.profile(False)
+    init_l, which, (state, chi2, iters, status) = results[-1]
+    status_h, iters_h, chi2_h = status.cpu().numpy(), iters.cpu().numpy(), chi2.cpu().numpy()
+    converged = int(np.sum((status_h == N.LM_SUCCESS) | (status_h == N.LM_IMMOBILE)))
+
+    # ---- plain method on the GPU: moments values, batched and one stamp at a time ----------
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.steps):
+        init_p, (st_p, c2_p, it_p, stat_p) = step_plain()
+    e1.record()
+    torch.cuda.synchronize()
+    plain_ms = e0.elapsed_time(e1) / args.steps
+    stat_ph = stat_p.cpu().numpy()
+    conv_p = int(np.sum((stat_ph == N.LM_SUCCESS) | (stat_ph == N.LM_IMMOBILE)))
+    n_single = min(32, S)
+    init_ph = init_p.cpu()
+    opts = N.make_options(profile="sersic", psf_mode="full", free_mask=FREE_MASK, has_sky=True)
+    one = N.StampBatch([(64, 64)], [(21, 21)], N.scale_geometry(1), opts, dev)
+    singles = []
+    for i in range(n_single):
+        sl = slice(i * 4096, (i + 1) * 4096)
+        singles.append(cnn.StampSet(st.truth[i : i + 1], st.data[sl].contiguous(), st.weight[sl].contiguous(),
+                                    st.psf[i * 441 : (i + 1) * 441].contiguous(), st.sigma[i : i + 1].contiguous(), one))
+    cnn._lm(singles[0], init_p[0:1].contiguous(), lmo)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    conv_single = 0
+    for i, ss in enumerate(singles):
+        ini = cnn.moments_init(ss, 1)
+        _, _, _, stt = cnn._lm(ss, ini, lmo)
+        conv_single += int(stt.item() in (N.LM_SUCCESS, N.LM_IMMOBILE))
+    torch.cuda.synchronize()
+    single_s = time.perf_counter() - t0
+
+    # ---- e2e: host buffers, copies inside the timed region -------------------------------
+    def step_e2e():
+        ss = cnn.StampSet(st.truth, data_h.to(dev, non_blocking=True), weight_h.to(dev, non_blocking=True),
+                          psf_h.to(dev, non_blocking=True), sigma_h.to(dev, non_blocking=True), batch)
+        _, _, (s_, c_, i_, t_) = cnn.learned_fit(net, ss, S, lmo)
+        return s_.cpu(), c_.cpu(), t_.cpu()
+
+    step_e2e()
+    torch.cuda.synchronize()
+    h2d = (data_h.numel() + weight_h.numel() + psf_h.numel() + sigma_h.numel()) * 4
+    d2h = state.numel() * 8 + chi2.numel() * 8 + status.numel() * 4
+    t0 = time.perf_counter()
+    e0.record()
+    for _ in range(args.steps):
+        step_e2e()
+    e1.record()
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    e2e_wall_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+
+    if world > 1:
+        t = torch.tensor([dev_ms, e2e_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dev_ms, e2e_ms = t.tolist()
+        c = torch.tensor([converged, S], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(c)
+        converged_all, total_all = c.tolist()
+    else:
+        converged_all, total_all = converged, S
+
+    fp32_peak = N.fma_probe_tflops()
+    conv_ms, conv_n = ktimes["conv"]
+    achieved = work["conv_flops"] / (conv_ms * 1e-3) / 1e12 if conv_ms > 0 else None
+    roof = {
+        "kernel": "k_conv (PSF convolution + fused Jacobian/chi2/JtWJ/JtWr)",
+        "bound": "fp32",
+        "achieved": achieved,
+        "peak": fp32_peak,
+        "unit": "TFLOP/s",
+        "frac": achieved / fp32_peak if achieved else None,
+        "traffic": None,
+        "launches": conv_n,
+        "avg_launch_ms": conv_ms / max(conv_n, 1),
+        "peak_source": "measured FP32 FMA probe (ap_fma_probe) on this GPU",
+    }
+    chunks = (S + 8191) // 8192
+    launches = int(sum(v[1] for v in ktimes.values()) / args.steps) + CNN_LAUNCHES_PER_CHUNK * chunks + 2
+    value = converged_all / (dev_ms * 1e-3)
+    single_rate = conv_single / single_s if single_s > 0 else None
+    line = {
+        "metric": "LM Sersic fits/s (chi2 within 1e-4 of the FP64 oracle), learned+batched vs plain",
+        "value": value,
+        "unit": "fits/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": dev_ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 render / f64 LM / bf16 CNN",
+        "data": "synthetic",
+        "config": {
+            "workload": f"learned init + batched LM: {S} held-out 64x64 stamps per GPU, Sersic (C0 distributions) "
+            "+ locked sky 1.0, Moffat FWHM U(2,5) px in a 21x21 box, SNR U(10,200); 7 free params",
+            "stamps_per_gpu": S,
+            "pixels_per_gpu": int(batch.out_pixels),
+            "parallelism": f"replicas x{world} (independent stamps per rank)",
+            "l2": "inputs (%.2f GB) exceed the 129 MB L2" % ((data_h.numel() + weight_h.numel()) * 4 / 1e9),
+            "rounds_per_sync": args.rounds_per_sync,
+            "cuda_graph": not args.no_graph,
+        },
+        "fits": {"total": int(total_all), "converged": int(converged_all),
+                 "proposal_used": float(np.mean(which.cpu().numpy() == 0)),
+                 "mean_iterations": float(iters_h.mean()),
+                 "status_counts": {N.LM_MESSAGES[k]: int(np.sum(status_h == k)) for k in np.unique(status_h)}},
+        "plain": {
+            "batched_fits_per_s": conv_p / (plain_ms * 1e-3),
+            "batched_ms_per_step": plain_ms,
+            "batched_mean_iterations": float(it_p.cpu().numpy().mean()),
+            "batched_converged": conv_p,
+            "single_fits_per_s": single_rate,
+            "single_sample": f"{n_single} stamps, one LM call per stamp, moments initial values",
+            "learned_batched_over_plain_single": value / single_rate if single_rate else None,
+            "learned_batched_over_plain_batched": value / (conv_p / (plain_ms * 1e-3)) if conv_p else None,
+        },
+        "clocks": clk.summary(),
+        "e2e": {"value": converged_all / (e2e_ms * 1e-3), "unit": "fits/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "wall_ms_per_step": e2e_wall_ms},
+        "roofline": roof,
+        "kernel_ms_per_step": {k: v[0] / args.steps for k, v in ktimes.items()},
+        "kernel_launches_per_step": {k: v[1] / args.steps for k, v in ktimes.items()},
+        "gpu_launches": launches,
+        "work_per_step": {k: v / args.steps for k, v in work.items()},
+    }
+
+    if rank == 0 and world == 1 and not args.no_cpu and args.cpu_sample > 0:
+        idx = list(np.linspace(0, S - 1, args.cpu_sample).round().astype(int))
+        dh = data_h.numpy()
+        sg = sigma_h.numpy()
+        init_lh = init_l.cpu().numpy()
+
+        def data_of(i):
+            return dh[i * 4096 : (i + 1) * 4096].astype(np.float64).reshape(64, 64), float(sg[i])
+
+        jobs = learned_sample_jobs(S, seed, idx, data_of=data_of, init_of=lambda i: init_lh[i])
+        rels, secs, its = [], 0.0, []
+        for i, job in zip(idx, jobs):
+            c2, it, sec, msg = _oracle_fit(job)
+            secs += sec
+            its.append(it)
+            rels.append(abs(chi2_h[i] / c2 - 1.0))
+        line["cpu_baseline"] = {
+            "value": len(idx) / secs,
+            "unit": "fits/s",
+            "cores": 1,
+            "kind": "port",
+            "sample": f"{len(idx)} stamps of this workload from the same learned initial values, float64 numpy "
+            "restatement of the reference LM, one core",
+        }
+        line["parity"] = {"stamps": len(idx), "max_rel_chi2_vs_oracle": float(max(rels)),
+                          "within_1e-4": int(sum(r <= 1e-4 for r in rels)),
+                          "oracle_mean_iterations": float(np.mean(its))}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
-        run_reference(args)
+        if args.workload == "learned":
+            run_reference_learned(args)
+        else:
+            run_reference(args)
     else:
         run_gpu(args)
 

@@ -225,6 +225,59 @@ int ap_render_noalloc(int32_t nx, int32_t ny, int32_t psf_kx, int32_t psf_ky,
                       const double* geometry, const ap_options* options, const double* params,
                       const float* psf, float* model, ap_stream_t stream);
 
+/* ---- learned initial guess -----------------------------------------------------------------
+ * No counterpart in the reference: its initial values come from the heuristics of
+ * Galaxy_Model.initialize / parametric_initialize (astrophot/models/galaxy_model_object.py:60-113,
+ * astrophot/models/_shared_methods.py:116-166).  A 6-layer CNN (4 stride-2 3x3 convolutions
+ * 1->32->64->128->256 channels, fc 4096->192, fc 192->8; 1,176,008 parameters) proposes the
+ * 7 Sersic parameters of a 64 x 64 stamp; its forward and backward passes are GEMMs on the
+ * tensor cores in bf16 with fp32 accumulation.  Parameters are one flat fp32 vector of
+ * ap_cnn_param_count() floats (per layer W[N][K] then b[N], see ap_cnn_layer_offsets) plus its
+ * bf16 mirror (ap_cnn_to_bf16).  Batches must be multiples of 16 stamps.  All pointers are
+ * device pointers except those of ap_cnn_layer_offsets. */
+int64_t ap_cnn_param_count(void);
+size_t ap_cnn_workspace_bytes(int64_t batch);
+/* w_offsets[6], b_offsets[6], dims[6][6] = {cin, cout, hin, hout, K, N} per layer (host). */
+int ap_cnn_layer_offsets(int64_t* w_offsets, int64_t* b_offsets, int32_t* dims);
+int ap_cnn_to_bf16(const float* params, void* params_bf16, ap_stream_t stream);
+/* x[batch][64][64] (normalised stamps, ap_cnn_prepare) -> out[batch][16] (standardised
+ * outputs in columns 0..7).  The workspace keeps the activations for ap_cnn_backward. */
+int ap_cnn_forward(const float* params, const void* params_bf16, const float* x, int64_t batch,
+                   float* out, void* ws, size_t ws_bytes, ap_stream_t stream);
+/* grads (flat fp32) of a loss with d loss / d out = dout[batch][16], after ap_cnn_forward on the
+ * same workspace. */
+int ap_cnn_backward(const void* params_bf16, const float* dout, int64_t batch, float* grads,
+                    void* ws, size_t ws_bytes, ap_stream_t stream);
+/* One Adam step (beta 0.9 / 0.999, eps 1e-8, decoupled weight decay) on the mean squared error
+ * between out[:, 0..7] and targets[batch][8]; loss_out (device, may be NULL) receives the loss. */
+int ap_cnn_train_step(float* params, void* params_bf16, float* grads, float* adam_m, float* adam_v,
+                      const float* x, const float* targets, int64_t batch, float lr, int32_t step,
+                      float weight_decay, double* loss_out, void* ws, size_t ws_bytes,
+                      ap_stream_t stream);
+/* data[batch][64][64] -> x = asinh((data - sky) / (4 sigma)) (pixel signal-to-noise,
+ * compressed), lscale = log10(sigma); sky[batch], sigma[batch] per stamp. */
+int ap_cnn_prepare(const float* data, const float* sky, const float* sigma, int64_t batch, float* x,
+                   float* lscale, ap_stream_t stream);
+/* out[batch][16] -> params[batch][8] (value space, F = sky_F) through the output statistics
+ * mean[8], stdv[8]: outputs are cx - 32, cy - 32, q, cos 2PA, sin 2PA, ln n, ln Re,
+ * log10 Ie - log10 sigma. */
+int ap_cnn_decode(const float* out, const float* lscale, const float* mean, const float* stdv,
+                  const double* sky_F, int64_t batch, double* params, ap_stream_t stream);
+/* Moments initial guess of 64 x 64 stamps (the learned proposal's fallback): centre of light,
+ * PA and q from second moments of pixels more than sigma above the sky, Re holding half the
+ * light, n = 2, Ie at Re. */
+int ap_moments_init(const float* data, const float* sky, const float* sigma, const double* sky_F,
+                    int64_t batch, double* params, ap_stream_t stream);
+/* out = proposal where chi2_proposal <= chi2_fallback, else fallback; which = 0 / 1. */
+int ap_select_init(const double* proposal, const double* fallback, const double* chi2_proposal,
+                   const double* chi2_fallback, int64_t batch, double* out, int32_t* which,
+                   ap_stream_t stream);
+/* C[R][S] = sum_t A(r, t) B(s, t) on the tensor cores (bf16 in, fp32 out); A(r, t) = A[r*lda+t]
+ * or, with a_trans, A[t*lda+r]; likewise B.  R, S, lda, ldb multiples of 8, T of 16. */
+int ap_gemm_bf16(const void* A, int32_t lda, int32_t a_trans, const void* B, int32_t ldb,
+                 int32_t b_trans, float* C, int32_t ldc, int32_t R, int32_t S, int32_t T,
+                 ap_stream_t stream);
+
 /* Library version string. */
 const char* ap_version(void);
 /* Text of the last CUDA error behind an AP_ERR_CUDA status on this thread ("" if none). */

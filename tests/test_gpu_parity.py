@@ -312,3 +312,16 @@ def test_option_errors(N):
         N.make_options(integrate_mode="full")
     with pytest.raises(RuntimeError):
         N.StampBatch([(10, 10)], [(4, 4)], N.scale_geometry(1), N.make_options(psf_mode="full"))
+
+
+def test_profiler_outside_and_inside_capture(N):
+    """Kernel timing works for plain calls (ap_render) and for captured LM rounds alike."""
+    d = cases.load_render("sersic_psf_64")
+    b, psf = batch_for_case(N, d)
+    params = torch.tensor(full_params(d["spec"])[None, :])
+    b.profile(True)
+    b.render(params, psf)
+    torch.cuda.synchronize()
+    kt = b.kernel_times()
+    b.profile(False)
+    assert kt["conv"][1] >= 1 and kt["conv"][0] > 0
