@@ -177,88 +177,86 @@ __device__ __forceinline__ void unpack_entry(int64_t ent, int& slot, int& s, int
 // ---------------------------------------------------------------------------
 // PSF shift (bilinear interp2d of the 1-padded PSF) and renormalisation, with d/d shift
 // ---------------------------------------------------------------------------
-struct ShiftVal {
-  double v, dx, dy;
+// Bilinear interp2d of the 1-padded PSF at (ix - sx, iy - sy) (indices clamped, weights not:
+// the reference extrapolates at the edge) and its derivatives with respect to the shift.
+// FP32: the shifted values are stored as floats and the weights of a shift |s| <= 1/2 need no
+// more (relative error ~1e-7)
+struct ShiftValF {
+  float v, dx, dy;
 };
 
-__device__ __forceinline__ ShiftVal shifted_psf_at(const float* psf, int kx, int ky, int ix, int iy,
-                                                   double sx, double sy) {
+__device__ __forceinline__ ShiftValF shifted_psf_at_f(const float* psf, int kx, int ky, int ix, int iy,
+                                                      float sx, float sy) {
   const int w = kx + 2, h = ky + 2;
-  auto pad = [&](int r, int c) -> double {
+  auto pad = [&](int r, int c) -> float {
     const int rr = r - 1, cc = c - 1;
-    return (rr >= 0 && rr < ky && cc >= 0 && cc < kx) ? (double)psf[rr * kx + cc] : 0.0;
+    return (rr >= 0 && rr < ky && cc >= 0 && cc < kx) ? psf[rr * kx + cc] : 0.f;
   };
-  const double x = ix - sx, y = iy - sy;
-  int x0 = (int)floor(x), y0 = (int)floor(y);
+  const float x = (float)ix - sx, y = (float)iy - sy;
+  int x0 = (int)floorf(x), y0 = (int)floorf(y);
   int x1 = x0 + 1, y1 = y0 + 1;
   x0 = min(max(x0, 0), w - 2);
   x1 = min(max(x1, 1), w - 1);
   y0 = min(max(y0, 0), h - 2);
   y1 = min(max(y1, 1), h - 1);
-  const double fa = pad(y0, x0), fb = pad(y1, x0), fc = pad(y0, x1), fd = pad(y1, x1);
-  ShiftVal r;
-  r.v = fa * ((x1 - x) * (y1 - y)) + fb * ((x1 - x) * (y - y0)) + fc * ((x - x0) * (y1 - y)) +
-        fd * ((x - x0) * (y - y0));
-  r.dx = -(fa * (-(y1 - y)) + fb * (-(y - y0)) + fc * (y1 - y) + fd * (y - y0));
-  r.dy = -(fa * (-(x1 - x)) + fb * (x1 - x) + fc * (-(x - x0)) + fd * (x - x0));
+  const float fa = pad(y0, x0), fb = pad(y1, x0), fc = pad(y0, x1), fd = pad(y1, x1);
+  const float ax = (float)x1 - x, bx = x - (float)x0, ay = (float)y1 - y, by = y - (float)y0;
+  ShiftValF r;
+  r.v = fa * (ax * ay) + fb * (ax * by) + fc * (bx * ay) + fd * (bx * by);
+  r.dx = -(-fa * ay - fb * by + fc * ay + fd * by);
+  r.dy = -(-fa * ax + fb * ax - fc * bx + fd * bx);
   return r;
 }
 
-__device__ double block_sum_d(double v, double* sh) {
+__device__ __forceinline__ double warp_sum_d(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  __syncthreads();
-  if (lane == 0) sh[warp] = v;
-  __syncthreads();
-  double t = 0;
-  const int nw = (blockDim.x + 31) >> 5;
-  for (int i = 0; i < nw; ++i) t += sh[i];
-  return t;
+  return v;
 }
 
-__device__ void psf_shift_one(const BatchArgs& b, const float* psf, int s, int slot) {
+// one warp per (stamp, evaluation slot): sums in FP64 across the warp, values in FP32
+__device__ void psf_shift_warp(const BatchArgs& b, const float* psf, int s, int slot, int lane) {
   const EvalDev& e = b.evals[s * 2 + slot];
   const StampDev& st = b.stamps[s];
   const int kp2 = st.kpx * st.kpy;
   const float* P = psf + st.psf_off;
   float* out = b.spsf + st.spsf_off + (int64_t)slot * 3 * kp2;
-  __shared__ double sh[32];
-  __syncthreads();  // sh reuse across the persistent loop
   const bool jac = (e.ops & OP_JAC) != 0;
   if (b.psf_mode == AP_PSF_FULL) {
+    const float sx = (float)e.shift[0], sy = (float)e.shift[1];
     double S = 0, Sx = 0, Sy = 0;
-    for (int idx = threadIdx.x; idx < kp2; idx += blockDim.x) {
-      const ShiftVal r =
-          shifted_psf_at(P, st.kx, st.ky, idx % st.kpx, idx / st.kpx, e.shift[0], e.shift[1]);
+    for (int idx = lane; idx < kp2; idx += 32) {
+      const ShiftValF r = shifted_psf_at_f(P, st.kx, st.ky, idx % st.kpx, idx / st.kpx, sx, sy);
       S += r.v;
       Sx += r.dx;
       Sy += r.dy;
     }
-    S = block_sum_d(S, sh);
-    Sx = block_sum_d(Sx, sh);
-    Sy = block_sum_d(Sy, sh);
-    for (int idx = threadIdx.x; idx < kp2; idx += blockDim.x) {
-      const ShiftVal r =
-          shifted_psf_at(P, st.kx, st.ky, idx % st.kpx, idx / st.kpx, e.shift[0], e.shift[1]);
-      out[idx] = (float)(r.v / S);
+    S = warp_sum_d(S);
+    Sx = warp_sum_d(Sx);
+    Sy = warp_sum_d(Sy);
+    const float inv = (float)(1.0 / S), cx = (float)(Sx / (S * S)), cy = (float)(Sy / (S * S));
+    for (int idx = lane; idx < kp2; idx += 32) {
+      const ShiftValF r = shifted_psf_at_f(P, st.kx, st.ky, idx % st.kpx, idx / st.kpx, sx, sy);
+      out[idx] = r.v * inv;
       if (jac) {
-        out[kp2 + idx] = (float)(r.dx / S - r.v * Sx / (S * S));
-        out[2 * kp2 + idx] = (float)(r.dy / S - r.v * Sy / (S * S));
+        out[kp2 + idx] = r.dx * inv - r.v * cx;
+        out[2 * kp2 + idx] = r.dy * inv - r.v * cy;
       }
     }
   } else {
     double S = 0;
-    for (int idx = threadIdx.x; idx < kp2; idx += blockDim.x) S += (double)P[idx];
-    S = block_sum_d(S, sh);
-    for (int idx = threadIdx.x; idx < kp2; idx += blockDim.x) out[idx] = (float)((double)P[idx] / S);
+    for (int idx = lane; idx < kp2; idx += 32) S += (double)P[idx];
+    S = warp_sum_d(S);
+    const float inv = (float)(1.0 / S);
+    for (int idx = lane; idx < kp2; idx += 32) out[idx] = P[idx] * inv;
   }
 }
 
 __global__ void k_psf_shift(BatchArgs b, const float* psf) {
   const uint32_t n = b.counters[9];
-  for (uint32_t it = blockIdx.x; it < n; it += gridDim.x) {
+  const int wpb = blockDim.x >> 5, lane = threadIdx.x & 31;
+  for (uint32_t it = blockIdx.x * wpb + (threadIdx.x >> 5); it < n; it += gridDim.x * wpb) {
     const int t = b.slist[it];
-    psf_shift_one(b, psf, t >> 1, t & 1);
+    psf_shift_warp(b, psf, t >> 1, t & 1, lane);
   }
 }
 

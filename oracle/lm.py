@@ -38,10 +38,14 @@ class GroupProblem:
     Y: np.ndarray
     W: Optional[np.ndarray] = None
     mask: Optional[np.ndarray] = None
+    # (component, name) -> (component, name) of the node it points at (see ``sample_group``)
+    links: Optional[dict] = None
 
     def __post_init__(self):
         self.components = [copy.deepcopy(c) for c in self.components]
-        self.slots = [(ci, name, k) for ci, c in enumerate(self.components) for (name, k) in c.free_slots()]
+        self.links = dict(self.links or {})
+        self.slots = [(ci, name, k) for ci, c in enumerate(self.components) for (name, k) in c.free_slots()
+                      if (ci, name) not in self.links]
 
     # vector_values / vector_representation (param/parameter.py:169-214)
     def values(self):
@@ -58,13 +62,14 @@ class GroupProblem:
         for (ci, name, k), r in zip(self.slots, rep):
             v = rep_to_value(name, r)
             check_limits(name, v)
-            c = self.components[ci]
-            if name == "center":
-                arr = np.array(c.params["center"], dtype=float).copy()
-                arr[k] = v
-                c.params["center"] = arr
-            else:
-                c.params[name] = np.asarray(v, dtype=float)
+            for cj in [ci] + [a for (a, n), t in self.links.items() if t == (ci, name)]:
+                c = self.components[cj]
+                if name == "center":
+                    arr = np.array(c.params["center"], dtype=float).copy()
+                    arr[k] = v
+                    c.params["center"] = arr
+                else:
+                    c.params[name] = np.asarray(v, dtype=float)
 
     def forward(self, rep):
         self.set_representation(rep)
@@ -74,7 +79,7 @@ class GroupProblem:
     def jacobian(self, rep):
         """Representation-space Jacobian ``[N, P]`` (models/_model_methods.py:260-347)."""
         self.set_representation(rep)
-        _, J = sample_group(self.components, self.window, self.psf, grad=True)
+        _, J = sample_group(self.components, self.window, self.psf, grad=True, links=self.links)
         scale = np.array([drep_dvalue(name, r) for (ci, name, k), r in zip(self.slots, rep)])
         return J.reshape(-1, J.shape[-1]) * scale[None, :]
 

@@ -277,6 +277,9 @@ class Component:
     integrate_quad_level: int = 3
     softening: float = 1e-3
     locked: Tuple[str, ...] = ()
+    # pixel window [[x0, x1], [y0, y1]] inside the group's window (Model.window given in pixels,
+    # models/core_model.py:313-325 -> Window.crop_to_pixel); None = the whole window
+    window: Optional[Tuple[Tuple[int, int], Tuple[int, int]]] = None
 
     def __post_init__(self):
         self.params = {k: np.asarray(v, dtype=np.float64) for k, v in self.params.items()}
@@ -743,25 +746,75 @@ def _component_partials(comp, deep: Sampled, finish, center_from_coords, win):
     return jac
 
 
-def sample_group(components: List[Component], win: Window, psf: Optional[PSF], grad=False):
-    """``Group_Model.sample`` / ``jacobian`` (models/group_model_object.py:183-283) for
-    components that all cover ``win``: the model is the sum and the Jacobian columns are
-    the components' free parameters in order (``vector_identities``)."""
+def sub_window(win: Window, pix) -> Window:
+    """The window of pixels [[x0, x1], [y0, y1]] of ``win`` (``crop_to_pixel``)."""
+    (x0, x1), (y0, y1) = pix
+    w = win.copy()
+    w.nx, w.ny = int(x1 - x0), int(y1 - y0)
+    w.ref_ij = win.ref_ij - np.array([x0, y0], dtype=np.float64)
+    return w
+
+
+def sample_group_parts(components: List[Component], win: Window, psf: Optional[PSF], grad=False):
+    """Each component added into ``win`` (``Group_Model.sample``, models/group_model_object.py:
+    183-231) and, when ``grad``, its value-space partials placed on ``win``.
+
+    Reference quirk reproduced: inside a group a component with its own pixel window is
+    *evaluated on the group's window* (``model(window=group window)`` makes the working window
+    the group's, models/model_object.py:290-296, with the integration threshold and the PSF
+    convolution of that larger window) and only its own window is added
+    (``make_model_image`` = target[self.window & window], core_model.py:193-204); its Jacobian
+    is evaluated on its own window (``self.window & window``, models/_model_methods.py:293-298).
+    """
     total = np.zeros((win.ny, win.nx))
-    cols = []
+    parts = []
     for comp in components:
-        r = sample_component(comp, win, psf, grad)
-        total += r.model
+        if comp.window is None:
+            r = sample_component(comp, win, psf, grad)
+            total += r.model
+            parts.append(r.jac)
+            continue
+        (x0, x1), (y0, y1) = comp.window
         if grad:
-            for slot in comp.free_slots():
-                cols.append(r.jac[slot])
-    J = np.stack(cols, axis=-1) if (grad and cols) else None
+            r = sample_component(comp, sub_window(win, comp.window), psf, True)
+            total[y0:y1, x0:x1] += r.model
+            full = {}
+            for key, v in r.jac.items():
+                f = np.zeros((win.ny, win.nx))
+                f[y0:y1, x0:x1] = v
+                full[key] = f
+            parts.append(full)
+        else:
+            r = sample_component(comp, win, psf, False)
+            total[y0:y1, x0:x1] += r.model[y0:y1, x0:x1]
+            parts.append(None)
+    return total, parts
+
+
+def sample_group(components: List[Component], win: Window, psf: Optional[PSF], grad=False, links=None):
+    """``Group_Model.sample`` / ``jacobian`` (models/group_model_object.py:183-283): the model is
+    the sum of the components and the Jacobian columns are the components' free parameters in
+    order (``vector_identities``).  ``links`` maps (component, name) of a parameter whose node
+    points at another component's node (``value = node``, param/parameter.py:480-496) to that
+    (component, name): the linked node leaves the vector and its partials add into the column
+    of the node it points at (``Jacobian_Image`` merges columns by identity,
+    image/jacobian_image.py:36-37, 79-118)."""
+    links = links or {}
+    total, parts = sample_group_parts(components, win, psf, grad)
+    if not grad:
+        return total, None
+    cols = []
+    for ci, comp in enumerate(components):
+        for (name, k) in comp.free_slots():
+            if (ci, name) in links:
+                continue
+            col = parts[ci][(name, k)].copy()
+            for (cj, nj), target in links.items():
+                if target == (ci, name):
+                    col += parts[cj][(nj, k)]
+            cols.append(col)
+    J = np.stack(cols, axis=-1) if cols else None
     return total, J
-
-
-# ----------------------------------------------------------------------------
-# PSF stamp constructors (fixture generators)
-# ----------------------------------------------------------------------------
 
 
 def gaussian_psf(sigma, img_width, pixelscale, upsample=4, normalize=True):

@@ -46,3 +46,15 @@ def load_vjp(name):
     d = {k: z[k] for k in z.files}
     d["spec"] = json.loads(str(d["spec"]))
     return d
+
+
+def group_case_names():
+    return sorted(os.path.basename(p)[: -len(".npz")] for p in glob.glob(os.path.join(HERE, "group_*.npz")))
+
+
+def load_group(name):
+    z = np.load(os.path.join(HERE, f"{name}.npz"))
+    d = {k: z[k] for k in z.files}
+    d["spec"] = json.loads(str(d["spec"]))
+    d["message"] = str(d["message"])
+    return d

@@ -372,8 +372,88 @@ def run_vjp_case(ap, key, case):
                 spec=json.dumps(case))
 
 
+GROUP_CASES = {
+    # Group_Model of four components with their own pixel windows on one 96 x 96 image
+    # (models/group_model_object.py:183-283): a Sersic bulge and an exponential disk sharing
+    # one centre node (parameter link, param/parameter.py value = node), two more Sersic
+    # galaxies whose windows overlap the first pair's, a locked flat sky; group psf_mode
+    # "full" with a 25 x 25 Moffat.  Recorded: model, representation Jacobian (linked columns
+    # merged), vector names, and an LM trajectory.
+    "group_linked_96": dict(size=96, seed=13, psf=MOFFAT_25, max_iter=12),
+}
+
+GROUP_SOURCES = (
+    # name, kind, window [[x0, x1], [y0, y1]], truth (cx, cy, q, PA, n, Re, Ie), link
+    ("bulge", "sersic", [[8, 72], [10, 74]], (40.3, 42.6, 0.7, 0.8, 3.2, 5.0, 2.2), None),
+    ("disk", "exponential", [[8, 72], [10, 74]], (40.3, 42.6, 0.45, 0.9, 1.0, 12.0, 1.3), "bulge"),
+    ("east", "sersic", [[50, 96], [36, 90]], (72.4, 63.1, 0.6, 2.0, 1.5, 7.0, 1.8), None),
+    ("south", "sersic", [[0, 44], [52, 96]], (21.2, 73.8, 0.8, 0.3, 2.5, 4.0, 2.0), None),
+)
+
+
+def group_source_params(kind, vals, linked):
+    cx, cy, q, PA, n, Re, Ie = vals
+    p = {"q": q, "PA": PA, "Re": Re, "Ie": Ie}
+    if not linked:
+        p["center"] = [cx, cy]
+    if kind == "sersic":
+        p["n"] = n
+    return p
+
+
+def group_init_values(vals):
+    """Fixed 10-15 % perturbation of a truth vector (centre shifted by (0.8, -0.6) px)."""
+    cx, cy, q, PA, n, Re, Ie = vals
+    return (cx + 0.8, cy - 0.6, min(q * 1.1, 0.95), PA + 0.1, n * 0.85, Re * 1.15, Ie - 0.1)
+
+
+def build_group(ap, target, values, tag, psf_mode="full"):
+    models = {}
+    for (name, kind, window, _, link), vals in zip(GROUP_SOURCES, values):
+        m = ap.models.AstroPhot_Model(name=f"{tag} {name}", model_type=f"{kind} galaxy model", target=target,
+                                      window=window, parameters=group_source_params(kind, vals, link is not None))
+        if link is not None:
+            m.parameters["center"].value = models[link].parameters["center"]
+        models[name] = m
+    sky = ap.models.AstroPhot_Model(name=f"{tag} sky", model_type="flat sky model", target=target,
+                                    parameters={"F": {"value": 0.0, "locked": True}})
+    sky.initialize()  # sets the (unused) sky centre the sampler reads
+    group = ap.models.AstroPhot_Model(name=f"{tag} group", model_type="group model", target=target,
+                                      models=list(models.values()) + [sky], psf_mode=psf_mode)
+    return group
+
+
+def run_group_case(ap, key, case):
+    N = case["size"]
+    psf = psf_array(case["psf"])
+    target = ap.image.Target_Image(data=np.zeros((N, N)), pixelscale=1.0, psf=psf)
+    truth_vals = [src[3] for src in GROUP_SOURCES]
+    truth_group = build_group(ap, target, truth_vals, f"{key} truth")
+    truth_img = truth_group().data.detach().cpu().numpy()
+    data, weight = synthetic.add_noise(truth_img, case["seed"])
+    target = ap.image.Target_Image(data=data, pixelscale=1.0, psf=psf, variance=1.0 / weight)
+    init_vals = [group_init_values(v) for v in truth_vals]
+    group = build_group(ap, target, init_vals, key)
+    init_img = group().data.detach().cpu().numpy()
+    jac = group.jacobian(as_representation=True).data.detach().cpu().numpy()
+    names = [str(n) for n in group.parameters.vector_names()]
+    rep0 = group.parameters.vector_representation().detach().cpu().numpy().copy()
+    res = ap.fit.LM(group, initial_state=rep0, max_iter=case["max_iter"]).fit()
+    return dict(
+        psf=psf, data=data, weight=weight, truth_model=truth_img, init_model=init_img, jac_rep=jac,
+        names=np.array(names), rep0=rep0, init_values=np.array(init_vals), truth_values=np.array(truth_vals),
+        loss_history=np.array(res.loss_history), L_history=np.array(res.L_history),
+        lambda_history=np.array(res.lambda_history), res=np.array(res.res()), message=np.array(res.message),
+        spec=json.dumps(case),
+    )
+
+
 def main():
     ap = import_reference()
+    for key, case in GROUP_CASES.items():
+        out = run_group_case(ap, key, case)
+        np.savez_compressed(os.path.join(HERE, f"{key}.npz"), **out)
+        print("group", key, out["jac_rep"].shape, out["loss_history"], str(out["message"]))
     for key, case in VJP_CASES.items():
         out = run_vjp_case(ap, key, case)
         np.savez_compressed(os.path.join(HERE, f"{key}.npz"), **out)

@@ -241,3 +241,57 @@ def test_reverse_mode_center_gradient_is_shift_plus_coordinate_path():
     res = prob.W * (r.model - prob.Y)
     gc = [np.sum(res * (r.jac[("center", k)] + captured["coords"][k])) for k in range(2)]
     assert np.allclose(gc, d["grad"][:2], rtol=1e-11, atol=0)
+
+
+# ---- Group_Model with per-component windows and a linked centre ------------------------------
+
+
+def group_problem(d, values=None):
+    """The group of ``tests/golden/make_golden.py`` GROUP_SOURCES on the oracle."""
+    sources = (
+        ("sersic", ((8, 72), (10, 74)), None),
+        ("exponential", ((8, 72), (10, 74)), 0),
+        ("sersic", ((50, 96), (36, 90)), None),
+        ("sersic", ((0, 44), (52, 96)), None),
+    )
+    values = d["init_values"] if values is None else values
+    comps, links = [], {}
+    for ci, ((kind, win, link), v) in enumerate(zip(sources, values)):
+        cx, cy, q, PA, n, Re, Ie = v
+        p = {"center": [cx, cy], "q": q, "PA": PA, "Re": Re, "Ie": Ie}
+        if kind == "sersic":
+            p["n"] = n
+        comps.append(Component(kind, p, psf_mode="full", window=win))
+        if link is not None:
+            links[(ci, "center")] = (link, "center")
+    comps.append(Component("flat_sky", {"F": 0.0}, locked=("F",)))
+    N = d["spec"]["size"]
+    return GroupProblem(comps, Window.from_scale(N, N), PSF(d["psf"]), d["data"], d["weight"], links=links)
+
+
+@pytest.mark.parametrize("name", cases.group_case_names())
+def test_group_windows_links_match_reference(name):
+    d = cases.load_group(name)
+    prob = group_problem(d)
+    rep0 = prob.representation()
+    assert len(rep0) == len(d["names"]) == 25
+    assert np.allclose(rep0, d["rep0"], rtol=0, atol=1e-13)
+    m = prob.forward(rep0).reshape(d["init_model"].shape)
+    assert np.max(np.abs(m - d["init_model"])) <= 1e-12 * np.max(np.abs(d["init_model"]))
+    truth = group_problem(d, d["truth_values"])
+    mt = truth.forward(truth.representation()).reshape(d["truth_model"].shape)
+    assert np.max(np.abs(mt - d["truth_model"])) <= 1e-12 * np.max(np.abs(d["truth_model"]))
+    J = prob.jacobian(rep0).reshape(d["jac_rep"].shape)
+    for k in range(J.shape[-1]):
+        ref = d["jac_rep"][..., k]
+        assert np.max(np.abs(J[..., k] - ref)) <= 1e-11 * np.max(np.abs(ref)), k
+
+
+@pytest.mark.parametrize("name", cases.group_case_names())
+def test_group_lm_trajectory_matches_reference(name):
+    d = cases.load_group(name)
+    prob = group_problem(d)
+    lm = LMOracle(prob, prob.representation(), max_iter=d["spec"]["max_iter"]).fit()
+    assert lm.message == d["message"]
+    assert np.allclose(lm.loss_history, d["loss_history"], rtol=1e-10, atol=0)
+    assert np.allclose(lm.res(), d["res"], rtol=1e-8, atol=1e-10)
