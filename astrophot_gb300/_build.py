@@ -16,7 +16,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libastrophot_gb300.so")
-SOURCES = ("ap_kernels.cu", "ap_lm.cu", "ap_capi.cu", "ap_noalloc.cu", "ap_cnn.cu")
+SOURCES = ("ap_kernels.cu", "ap_lm.cu", "ap_capi.cu", "ap_noalloc.cu", "ap_cnn.cu", "ap_scene.cu")
 ARCH = ("-gencode", "arch=compute_103a,code=sm_103a")
 FLAGS = ("-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2")
 

@@ -118,6 +118,15 @@ EXPORTS = [
     ("ap_fma_probe", [_P, _I32, _I32, _P]),
     ("ap_batch_stats", [_P, _PI64]),
     ("ap_render_noalloc", [_I32, _I32, _I32, _I32, _PD, ctypes.POINTER(ApOptions), _P, _P, _P, _P]),
+    ("ap_scene_forward", [_P, _P, _P, _P, _I32, ctypes.c_float, _I32, _I32, _P, _P]),
+    ("ap_scene_jvp", [_P, _P, _P, _P, _P, _I32, _I32, _P, _P]),
+    ("ap_scene_jt", [_P, _I32, _P, _P, _I32, _I32, _P, _P]),
+    ("ap_scene_hess", [_P, _P, _I32, _P, _P, _P, _I32, _I32, _P, _P]),
+    ("ap_scene_chi2", [_P, _P, _P, _P, _I64, _P, _P]),
+    ("ap_scene_residual", [_P, _P, _P, _P, _I64, _P, _P]),
+    ("ap_scene_rpp_image", [_P, _P, _P, _P, _P, ctypes.c_double, _I64, _P, _P]),
+    ("ap_dense_solve_workspace_bytes", [_I32]),
+    ("ap_dense_damped_solve", [_I32, _P, _P, ctypes.c_double, _P, _P, ctypes.c_size_t, _P, _P]),
     ("ap_cnn_param_count", []),
     ("ap_cnn_workspace_bytes", [_I64]),
     ("ap_cnn_layer_offsets", [_PI64, _PI64, _PI32]),
@@ -140,6 +149,7 @@ _RESTYPES = {
     "ap_last_cuda_error": ctypes.c_char_p,
     "ap_cnn_param_count": ctypes.c_int64,
     "ap_cnn_workspace_bytes": ctypes.c_size_t,
+    "ap_dense_solve_workspace_bytes": ctypes.c_size_t,
 }
 
 
@@ -376,10 +386,15 @@ class StampBatch:
         check(self.lib.ap_render(self.handle, _ptr(params), _ptr(psf), _ptr(out), _stream()), "ap_render")
         return out
 
-    def jacobian(self, params: torch.Tensor, psf: Optional[torch.Tensor], as_representation=True):
+    def jacobian(self, params: torch.Tensor, psf: Optional[torch.Tensor], as_representation=True,
+                 model: Optional[torch.Tensor] = None, jac: Optional[torch.Tensor] = None):
+        """(model [out_pixels], jac [n_free][out_pixels]); ``model`` / ``jac`` may be given
+        (contiguous float32 of those sizes) to be written in place."""
         params = params.to(self.device, torch.float64).contiguous()
-        model = torch.empty(self.out_pixels, dtype=torch.float32, device=self.device)
-        jac = torch.empty((max(self.n_free, 1), self.out_pixels), dtype=torch.float32, device=self.device)
+        if model is None:
+            model = torch.empty(self.out_pixels, dtype=torch.float32, device=self.device)
+        if jac is None:
+            jac = torch.empty((max(self.n_free, 1), self.out_pixels), dtype=torch.float32, device=self.device)
         check(
             self.lib.ap_jacobian(
                 self.handle, _ptr(params), _ptr(psf), _ptr(model), _ptr(jac), 1 if as_representation else 0, _stream()

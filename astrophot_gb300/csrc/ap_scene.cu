@@ -1,0 +1,421 @@
+// Scenes: many sources on one image fitted jointly (Group_Model + LM over the joint vector).
+//
+// Each source is rendered by an ap_batch stamp (its own window for the Jacobian, the group's
+// window for the model image, as Group_Model.sample does).  These kernels combine the stamps:
+//   forward   image = sky + sum of the sources' renders inside their own windows
+//             (Group_Model.sample, astrophot/models/group_model_object.py:183-231)
+//   hess      H = J^T W J over the joint vector, one block per pair of overlapping windows
+//   jt        J^T v for an image v (gradient, geodesic-acceleration right-hand side)
+//   jvp       J h as an image
+//   chi2      sum of W (Y - M)^2 over unmasked pixels (LM._chi2, astrophot/fit/lm.py:374-378)
+//   solve     the damped system of LM._h (astrophot/fit/lm.py:361-371) for a dense P x P
+//             matrix: blocked Cholesky in FP64 plus two triangular solves
+// Linked parameters (one node shared by several sources) are one entry of the joint vector:
+// every source slot names its joint index, so their Jacobian columns add up (the merge by
+// identity of Jacobian_Image, astrophot/image/jacobian_image.py:36-37, 79-118).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ap_internal.h"
+
+using apgb::record_cuda;
+
+namespace {
+
+constexpr int kSceneTile = 32;
+constexpr int kMaxSlots = 8;
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ bool in_window(const ap_scene_source& s, int x, int y) {
+  return x >= s.x0 && x < s.x0 + s.wx && y >= s.y0 && y < s.y0 + s.wy;
+}
+
+// ---- forward: image = sky + sum over the tile's sources (fixed order: deterministic) -------------
+__global__ void k_scene_forward(const ap_scene_source* __restrict__ src, const int32_t* __restrict__ tile_ptr,
+                                const int32_t* __restrict__ tile_src, const float* __restrict__ fwd, float sky, int nx,
+                                int ny, int fwd_nx, float* __restrict__ image) {
+  const int tx = blockIdx.x % ((nx + kSceneTile - 1) / kSceneTile);
+  const int ty = blockIdx.x / ((nx + kSceneTile - 1) / kSceneTile);
+  const int t = blockIdx.x;
+  const int b = tile_ptr[t], e = tile_ptr[t + 1];
+  for (int i = threadIdx.x; i < kSceneTile * kSceneTile; i += blockDim.x) {
+    const int x = tx * kSceneTile + (i % kSceneTile), y = ty * kSceneTile + (i / kSceneTile);
+    if (x >= nx || y >= ny) continue;
+    float v = sky;
+    for (int k = b; k < e; ++k) {
+      const ap_scene_source& s = src[tile_src[k]];
+      if (in_window(s, x, y)) v += fwd[s.fwd_off + (int64_t)y * fwd_nx + x];
+    }
+    image[(int64_t)y * nx + x] = v;
+  }
+}
+
+// ---- jvp: out = J h on the image (own windows) -------------------------------------------------
+__global__ void k_scene_jvp(const ap_scene_source* __restrict__ src, const int32_t* __restrict__ tile_ptr,
+                            const int32_t* __restrict__ tile_src, const float* __restrict__ jac,
+                            const double* __restrict__ h, int nx, int ny, float* __restrict__ out) {
+  const int ntx = (nx + kSceneTile - 1) / kSceneTile;
+  const int tx = blockIdx.x % ntx, ty = blockIdx.x / ntx;
+  const int b = tile_ptr[blockIdx.x], e = tile_ptr[blockIdx.x + 1];
+  for (int i = threadIdx.x; i < kSceneTile * kSceneTile; i += blockDim.x) {
+    const int x = tx * kSceneTile + (i % kSceneTile), y = ty * kSceneTile + (i / kSceneTile);
+    if (x >= nx || y >= ny) continue;
+    float v = 0.f;
+    for (int k = b; k < e; ++k) {
+      const ap_scene_source& s = src[tile_src[k]];
+      if (!in_window(s, x, y)) continue;
+      const int64_t p = s.jac_off + (int64_t)(y - s.y0) * s.wx + (x - s.x0);
+      for (int c = 0; c < s.n_free; ++c) v = fmaf(jac[p + c * s.jac_stride], (float)h[s.gidx[c]], v);
+    }
+    out[(int64_t)y * nx + x] = v;
+  }
+}
+
+// ---- jt: out[g] += sum over the source's window of J_c(p) v(p) -----------------------------------
+__global__ void k_scene_jt(const ap_scene_source* __restrict__ src, const float* __restrict__ jac,
+                           const float* __restrict__ v, int nx, double* __restrict__ out) {
+  const ap_scene_source& s = src[blockIdx.x];
+  double acc[kMaxSlots];
+#pragma unroll
+  for (int c = 0; c < kMaxSlots; ++c) acc[c] = 0.0;
+  const int64_t n = (int64_t)s.wx * s.wy;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const int lx = (int)(i % s.wx), ly = (int)(i / s.wx);
+    const float vi = v[(int64_t)(s.y0 + ly) * nx + (s.x0 + lx)];
+#pragma unroll
+    for (int c = 0; c < kMaxSlots; ++c)
+      if (c < s.n_free) acc[c] += (double)(jac[s.jac_off + i + c * s.jac_stride] * vi);
+  }
+  __shared__ double sh[kMaxSlots][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int c = 0; c < kMaxSlots; ++c) {
+    const double r = warp_sum(acc[c]);
+    if (lane == 0) sh[c][w] = r;
+  }
+  __syncthreads();
+  if (threadIdx.x < s.n_free) {
+    double t = 0.0;
+    for (int k = 0; k < nw; ++k) t += sh[threadIdx.x][k];
+    atomicAdd(out + s.gidx[threadIdx.x], t);
+  }
+}
+
+// ---- hess: one block per overlapping pair (a <= b): H[ga][gb] += sum J_a W J_b --------------------
+__global__ void __launch_bounds__(256) k_scene_hess(const ap_scene_source* __restrict__ src,
+                                                    const int32_t* __restrict__ pairs, const float* __restrict__ jac,
+                                                    const float* __restrict__ weight, const uint8_t* __restrict__ mask,
+                                                    int nx, int P, double* __restrict__ H) {
+  const ap_scene_source& A = src[pairs[2 * blockIdx.x]];
+  const ap_scene_source& B = src[pairs[2 * blockIdx.x + 1]];
+  const bool same = pairs[2 * blockIdx.x] == pairs[2 * blockIdx.x + 1];
+  const int x0 = max(A.x0, B.x0), x1 = min(A.x0 + A.wx, B.x0 + B.wx);
+  const int y0 = max(A.y0, B.y0), y1 = min(A.y0 + A.wy, B.y0 + B.wy);
+  const int ow = x1 - x0, oh = y1 - y0;
+  float acc[kMaxSlots][kMaxSlots];
+#pragma unroll
+  for (int i = 0; i < kMaxSlots; ++i)
+#pragma unroll
+    for (int j = 0; j < kMaxSlots; ++j) acc[i][j] = 0.f;
+  if (ow > 0 && oh > 0) {
+    const int64_t n = (int64_t)ow * oh;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+      const int x = x0 + (int)(i % ow), y = y0 + (int)(i / ow);
+      const int64_t ip = (int64_t)y * nx + x;
+      if (mask && mask[ip]) continue;
+      const float w = weight ? weight[ip] : 1.f;
+      const int64_t pa = A.jac_off + (int64_t)(y - A.y0) * A.wx + (x - A.x0);
+      const int64_t pb = B.jac_off + (int64_t)(y - B.y0) * B.wx + (x - B.x0);
+      float ja[kMaxSlots], jb[kMaxSlots];
+#pragma unroll
+      for (int c = 0; c < kMaxSlots; ++c) {
+        ja[c] = c < A.n_free ? jac[pa + c * A.jac_stride] * w : 0.f;
+        jb[c] = c < B.n_free ? jac[pb + c * B.jac_stride] : 0.f;
+      }
+#pragma unroll
+      for (int a = 0; a < kMaxSlots; ++a)
+#pragma unroll
+        for (int c = 0; c < kMaxSlots; ++c) acc[a][c] = fmaf(ja[a], jb[c], acc[a][c]);
+    }
+  }
+  __shared__ double sh[kMaxSlots * kMaxSlots][8];
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int a = 0; a < kMaxSlots; ++a)
+#pragma unroll
+    for (int c = 0; c < kMaxSlots; ++c) {
+      const double r = warp_sum((double)acc[a][c]);
+      if (lane == 0) sh[a * kMaxSlots + c][wp] = r;
+    }
+  __syncthreads();
+  for (int k = threadIdx.x; k < kMaxSlots * kMaxSlots; k += blockDim.x) {
+    const int a = k / kMaxSlots, c = k % kMaxSlots;
+    if (a >= A.n_free || c >= B.n_free) continue;
+    double t = 0.0;
+    for (int q = 0; q < nw; ++q) t += sh[k][q];
+    const int ga = A.gidx[a], gb = B.gidx[c];
+    atomicAdd(H + (int64_t)ga * P + gb, t);
+    if (!same) atomicAdd(H + (int64_t)gb * P + ga, t);
+  }
+}
+
+// ---- chi2 and residual images --------------------------------------------------------------------
+__global__ void k_scene_chi2(const float* __restrict__ model, const float* __restrict__ data,
+                             const float* __restrict__ weight, const uint8_t* __restrict__ mask, int64_t n,
+                             double* __restrict__ out) {
+  double acc = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    if (mask && mask[i]) continue;
+    const double r = (double)data[i] - (double)model[i];
+    acc += (weight ? (double)weight[i] : 1.0) * r * r;
+  }
+  acc = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) atomicAdd(out, acc);
+}
+
+// r = W (Y - M) on unmasked pixels, 0 elsewhere (LM._r, astrophot/fit/lm.py:381-385)
+__global__ void k_scene_residual(const float* __restrict__ model, const float* __restrict__ data,
+                                 const float* __restrict__ weight, const uint8_t* __restrict__ mask, int64_t n,
+                                 float* __restrict__ r) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const bool m = mask && mask[i];
+    r[i] = m ? 0.f : (weight ? weight[i] : 1.f) * (data[i] - model[i]);
+  }
+}
+
+// geodesic-acceleration right-hand side image (astrophot/fit/lm.py:286-291):
+// out = (2/d) ((rh - r)/d - W (J h)) on unmasked pixels
+__global__ void k_scene_rpp(const float* __restrict__ r, const float* __restrict__ rh, const float* __restrict__ jh,
+                            const float* __restrict__ weight, const uint8_t* __restrict__ mask, double d, int64_t n,
+                            float* __restrict__ out) {
+  const float fd = (float)d;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const bool m = mask && mask[i];
+    const float w = weight ? weight[i] : 1.f;
+    out[i] = m ? 0.f : (2.f / fd) * ((rh[i] - r[i]) / fd - w * jh[i]);
+  }
+}
+
+// ---- dense damped solve ----------------------------------------------------------------------------
+// A = H o (I + D / (1 + L)) + L I (1 + diag H) (lower triangle written, used by the factorisation)
+__global__ void k_damp(const double* __restrict__ H, double L, int n, double* __restrict__ A) {
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(k / n), j = (int)(k % n);
+    const double h = H[k];
+    A[k] = (i == j) ? h + L * (1.0 + h) : h / (1.0 + L);
+  }
+}
+
+constexpr int kNB = 32;
+
+// factor the diagonal block [k0, k0 + nb) in place (lower Cholesky); info = 1 + row on failure
+__global__ void k_chol_diag(double* __restrict__ A, int n, int k0, int* __restrict__ info) {
+  __shared__ double S[kNB][kNB + 1];
+  const int nb = min(kNB, n - k0);
+  for (int i = threadIdx.x; i < nb * nb; i += blockDim.x) S[i / nb][i % nb] = A[(int64_t)(k0 + i / nb) * n + k0 + i % nb];
+  __syncthreads();
+  for (int j = 0; j < nb; ++j) {
+    if (threadIdx.x == 0) {
+      const double d = S[j][j];
+      if (!(d > 0.0) || !isfinite(d)) {
+        if (*info == 0) *info = 1 + k0 + j;
+        S[j][j] = 1.0;
+      } else {
+        S[j][j] = sqrt(d);
+      }
+    }
+    __syncthreads();
+    const double djj = S[j][j];
+    for (int i = j + 1 + threadIdx.x; i < nb; i += blockDim.x) S[i][j] /= djj;
+    __syncthreads();
+    for (int t = threadIdx.x; t < (nb - j - 1) * (nb - j - 1); t += blockDim.x) {
+      const int i = j + 1 + t / (nb - j - 1), c = j + 1 + t % (nb - j - 1);
+      if (c <= i) S[i][c] -= S[i][j] * S[c][j];
+    }
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < nb * nb; i += blockDim.x) {
+    const int r = i / nb, c = i % nb;
+    A[(int64_t)(k0 + r) * n + k0 + c] = (c <= r) ? S[r][c] : 0.0;
+  }
+}
+
+// panel below the diagonal block: X L^T = A[k0+nb:, k0:k0+nb]  (one thread per row)
+__global__ void k_chol_panel(double* __restrict__ A, int n, int k0) {
+  __shared__ double Ld[kNB][kNB + 1];
+  const int nb = min(kNB, n - k0);
+  for (int i = threadIdx.x; i < nb * nb; i += blockDim.x) Ld[i / nb][i % nb] = A[(int64_t)(k0 + i / nb) * n + k0 + i % nb];
+  __syncthreads();
+  const int r = k0 + nb + blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  double x[kNB];
+  double* row = A + (int64_t)r * n + k0;
+  for (int j = 0; j < nb; ++j) {
+    double v = row[j];
+    for (int c = 0; c < j; ++c) v -= x[c] * Ld[j][c];
+    x[j] = v / Ld[j][j];
+  }
+  for (int j = 0; j < nb; ++j) row[j] = x[j];
+}
+
+// trailing update: A[i][j] -= sum_c P[i][c] P[j][c] for k0 + nb <= j <= i (tiles of 32 x 32)
+__global__ void k_chol_update(double* __restrict__ A, int n, int k0) {
+  const int nb = min(kNB, n - k0);
+  const int base = k0 + nb;
+  const int ti = blockIdx.y, tj = blockIdx.x;
+  if (tj > ti) return;
+  __shared__ double Pi[kNB][kNB + 1], Pj[kNB][kNB + 1];
+  const int i0 = base + ti * kNB, j0 = base + tj * kNB;
+  for (int t = threadIdx.x; t < kNB * kNB; t += blockDim.x) {
+    const int r = t / kNB, c = t % kNB;
+    Pi[r][c] = (i0 + r < n && c < nb) ? A[(int64_t)(i0 + r) * n + k0 + c] : 0.0;
+    Pj[r][c] = (j0 + r < n && c < nb) ? A[(int64_t)(j0 + r) * n + k0 + c] : 0.0;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < kNB * kNB; t += blockDim.x) {
+    const int r = t / kNB, c = t % kNB;
+    const int i = i0 + r, j = j0 + c;
+    if (i >= n || j >= n || j > i) continue;
+    double s = 0.0;
+#pragma unroll 8
+    for (int q = 0; q < kNB; ++q) s += Pi[r][q] * Pj[c][q];
+    A[(int64_t)i * n + j] -= s;
+  }
+}
+
+// L y = b then L^T x = y, one block; x may alias b
+__global__ void k_chol_solve(const double* __restrict__ A, int n, const double* __restrict__ b, double* __restrict__ x,
+                             double* __restrict__ y) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) y[i] = b[i];
+  __syncthreads();
+  __shared__ double yj;
+  for (int j = 0; j < n; ++j) {
+    if (threadIdx.x == 0) {
+      yj = y[j] / A[(int64_t)j * n + j];
+      y[j] = yj;
+    }
+    __syncthreads();
+    const double v = yj;
+    for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) y[i] -= A[(int64_t)i * n + j] * v;
+    __syncthreads();
+  }
+  for (int j = n - 1; j >= 0; --j) {
+    if (threadIdx.x == 0) {
+      yj = y[j] / A[(int64_t)j * n + j];
+      y[j] = yj;
+    }
+    __syncthreads();
+    const double v = yj;
+    // row j of L^T is column j of L: y[i] -= L[j][i] * x[j] for i < j
+    for (int i = threadIdx.x; i < j; i += blockDim.x) y[i] -= A[(int64_t)j * n + i] * v;
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = y[i];
+}
+
+inline int egrid(int64_t n) {
+  int64_t g = (n + 255) / 256;
+  return (int)(g < 1 ? 1 : (g > 4096 ? 4096 : g));
+}
+
+}  // namespace
+
+extern "C" {
+
+int ap_scene_forward(const ap_scene_source* sources, const int32_t* tile_ptr, const int32_t* tile_src,
+                     const float* fwd, int32_t fwd_nx, float sky, int32_t nx, int32_t ny, float* image,
+                     ap_stream_t stream) {
+  if (!sources || !tile_ptr || !tile_src || !fwd || !image || nx <= 0 || ny <= 0 || fwd_nx < nx) return AP_ERR_ARG;
+  const int tiles = ((nx + kSceneTile - 1) / kSceneTile) * ((ny + kSceneTile - 1) / kSceneTile);
+  k_scene_forward<<<tiles, 256, 0, (cudaStream_t)stream>>>(sources, tile_ptr, tile_src, fwd, sky, nx, ny, fwd_nx,
+                                                           image);
+  return record_cuda(cudaGetLastError());
+}
+
+int ap_scene_jvp(const ap_scene_source* sources, const int32_t* tile_ptr, const int32_t* tile_src, const float* jac,
+                 const double* h, int32_t nx, int32_t ny, float* out, ap_stream_t stream) {
+  if (!sources || !tile_ptr || !tile_src || !jac || !h || !out || nx <= 0 || ny <= 0) return AP_ERR_ARG;
+  const int tiles = ((nx + kSceneTile - 1) / kSceneTile) * ((ny + kSceneTile - 1) / kSceneTile);
+  k_scene_jvp<<<tiles, 256, 0, (cudaStream_t)stream>>>(sources, tile_ptr, tile_src, jac, h, nx, ny, out);
+  return record_cuda(cudaGetLastError());
+}
+
+int ap_scene_jt(const ap_scene_source* sources, int32_t n_sources, const float* jac, const float* v, int32_t nx,
+                int32_t P, double* out, ap_stream_t stream) {
+  if (!sources || !jac || !v || !out || n_sources < 0 || P <= 0) return AP_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = record_cuda(cudaMemsetAsync(out, 0, sizeof(double) * P, st));
+  if (rc || n_sources == 0) return rc;
+  k_scene_jt<<<n_sources, 256, 0, st>>>(sources, jac, v, nx, out);
+  return record_cuda(cudaGetLastError());
+}
+
+int ap_scene_hess(const ap_scene_source* sources, const int32_t* pairs, int32_t n_pairs, const float* jac,
+                  const float* weight, const uint8_t* mask, int32_t nx, int32_t P, double* H, ap_stream_t stream) {
+  if (!sources || !jac || !H || n_pairs < 0 || P <= 0 || (n_pairs > 0 && !pairs)) return AP_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = record_cuda(cudaMemsetAsync(H, 0, sizeof(double) * P * P, st));
+  if (rc || n_pairs == 0) return rc;
+  k_scene_hess<<<n_pairs, 256, 0, st>>>(sources, pairs, jac, weight, mask, nx, P, H);
+  return record_cuda(cudaGetLastError());
+}
+
+int ap_scene_chi2(const float* model, const float* data, const float* weight, const uint8_t* mask, int64_t n,
+                  double* out, ap_stream_t stream) {
+  if (!model || !data || !out || n <= 0) return AP_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = record_cuda(cudaMemsetAsync(out, 0, sizeof(double), st));
+  if (rc) return rc;
+  k_scene_chi2<<<egrid(n), 256, 0, st>>>(model, data, weight, mask, n, out);
+  return record_cuda(cudaGetLastError());
+}
+
+int ap_scene_residual(const float* model, const float* data, const float* weight, const uint8_t* mask, int64_t n,
+                      float* r, ap_stream_t stream) {
+  if (!model || !data || !r || n <= 0) return AP_ERR_ARG;
+  k_scene_residual<<<egrid(n), 256, 0, (cudaStream_t)stream>>>(model, data, weight, mask, n, r);
+  return record_cuda(cudaGetLastError());
+}
+
+int ap_scene_rpp_image(const float* r, const float* rh, const float* jh, const float* weight, const uint8_t* mask,
+                       double d, int64_t n, float* out, ap_stream_t stream) {
+  if (!r || !rh || !jh || !out || n <= 0 || !(d > 0)) return AP_ERR_ARG;
+  k_scene_rpp<<<egrid(n), 256, 0, (cudaStream_t)stream>>>(r, rh, jh, weight, mask, d, n, out);
+  return record_cuda(cudaGetLastError());
+}
+
+size_t ap_dense_solve_workspace_bytes(int32_t n) {
+  if (n <= 0) return 0;
+  return sizeof(double) * ((size_t)n * n + n) + sizeof(int) * 4;
+}
+
+int ap_dense_damped_solve(int32_t n, const double* H, const double* g, double L, double* h, void* ws,
+                          size_t ws_bytes, int32_t* info, ap_stream_t stream) {
+  if (n <= 0 || !H || !g || !h || !ws || !info) return AP_ERR_ARG;
+  if (ws_bytes < ap_dense_solve_workspace_bytes(n)) return AP_ERR_WORKSPACE;
+  cudaStream_t st = (cudaStream_t)stream;
+  double* A = (double*)ws;
+  double* y = A + (size_t)n * n;
+  int rc = record_cuda(cudaMemsetAsync(info, 0, sizeof(int32_t), st));
+  if (rc) return rc;
+  k_damp<<<egrid((int64_t)n * n), 256, 0, st>>>(H, L, n, A);
+  for (int k0 = 0; k0 < n; k0 += kNB) {
+    k_chol_diag<<<1, 256, 0, st>>>(A, n, k0, info);
+    const int nb = n - k0 < kNB ? n - k0 : kNB;
+    const int rest = n - k0 - nb;
+    if (rest > 0) {
+      k_chol_panel<<<(rest + 127) / 128, 128, 0, st>>>(A, n, k0);
+      const int nt = (rest + kNB - 1) / kNB;
+      k_chol_update<<<dim3(nt, nt), 256, 0, st>>>(A, n, k0);
+    }
+  }
+  k_chol_solve<<<1, 1024, 0, st>>>(A, n, g, h, y);
+  return record_cuda(cudaGetLastError());
+}
+
+}  // extern "C"

@@ -1,0 +1,478 @@
+"""Scenes: many galaxies on one image, rendered and fitted jointly on the GPU.
+
+``Group_Model.sample`` / ``jacobian`` (models/group_model_object.py:183-283) and ``LM``
+(fit/lm.py) over the joint parameter vector when the sources share an image:
+
+* every source is a stamp of an ``ap_batch``: its Jacobian on its own pixel window
+  (``self.window & window``, models/_model_methods.py:293-298), its model image on the group's
+  window and then cropped to its own window (inside a group ``model(window=group window)``
+  makes the group window the working window, models/model_object.py:290-296, while only the
+  model's own window is added, core_model.py:193-204);
+* ``ap_scene_forward`` / ``ap_scene_hess`` / ``ap_scene_jt`` / ``ap_scene_jvp`` combine the
+  stamps over the image; ``ap_dense_damped_solve`` solves the joint damped system;
+* a source's centre may be linked to another source's centre (``value = node``,
+  param/parameter.py:480-496): one entry of the joint vector, Jacobian columns summed.
+
+``SceneLM`` is ``LM.fit`` / ``LM.step`` (fit/lm.py:249-357, 428-493) with these primitives:
+the damping search, geodesic right-hand side, curvature test, convergence rules and
+``res()`` of the reference, with all images, Jacobians and reductions on the device.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import math
+from dataclasses import dataclass, field
+from typing import List, Optional, Sequence
+
+import numpy as np
+import torch
+
+from . import _native as N
+from .transforms import SLOT_LIMITS, to_rep, to_value
+
+__all__ = ("SceneSource", "Scene", "SceneLM")
+
+TILE = 32
+_SLOTS_OF = {"sersic": (0, 1, 2, 3, 4, 5, 6), "exponential": (0, 1, 2, 3, 5, 6)}
+
+
+class ApSceneSource(ctypes.Structure):
+    _fields_ = [
+        ("fwd_off", ctypes.c_int64),
+        ("jac_off", ctypes.c_int64),
+        ("jac_stride", ctypes.c_int64),
+        ("x0", ctypes.c_int32),
+        ("y0", ctypes.c_int32),
+        ("wx", ctypes.c_int32),
+        ("wy", ctypes.c_int32),
+        ("n_free", ctypes.c_int32),
+        ("gidx", ctypes.c_int32 * 8),
+        ("reserved", ctypes.c_int32),
+    ]
+
+
+@dataclass
+class SceneSource:
+    """One galaxy: ``kind`` "sersic" or "exponential", value-space ``params``
+    [cx, cy, q, PA, n, Re, Ie] (n ignored for exponential), pixel ``window``
+    ((x0, x1), (y0, y1)) or None for the whole image, ``link_center`` = index of the source
+    whose centre node this one shares, ``locked`` = full-vector slots held fixed."""
+
+    kind: str
+    params: Sequence[float]
+    window: Optional[tuple] = None
+    link_center: Optional[int] = None
+    locked: tuple = ()
+
+
+class Scene:
+    """Sources on one ``nx`` x ``ny`` image (pixel scale ``scale``, the (0, 0) pixel corner at the
+    origin) with a locked flat sky ``sky`` (counts per pixel), one PSF (None: no convolution),
+    data / weight (1 / variance) / mask (True = ignored)."""
+
+    def __init__(self, nx: int, ny: int, sources: List[SceneSource], psf: Optional[np.ndarray], data, weight,
+                 mask=None, sky: float = 0.0, scale: float = 1.0, options: Optional[dict] = None,
+                 fwd_chunk: int = 64, device="cuda"):
+        self.nx, self.ny, self.scale = int(nx), int(ny), float(scale)
+        self.sources = list(sources)
+        self.device = torch.device(device)
+        self.sky = float(sky)
+        self.psf_np = None if psf is None else np.asarray(psf, dtype=np.float64)
+        opts_kw = dict(options or {})
+        dev = self.device
+        self.data = torch.as_tensor(np.asarray(data, dtype=np.float32).reshape(-1), device=dev).contiguous()
+        self.weight = torch.as_tensor(np.asarray(weight, dtype=np.float32).reshape(-1), device=dev).contiguous()
+        self.mask = None
+        if mask is not None and np.any(mask):
+            self.mask = torch.as_tensor(np.asarray(mask, dtype=np.uint8).reshape(-1), device=dev).contiguous()
+        n_used = self.nx * self.ny if self.mask is None else int((self.mask == 0).sum().item())
+
+        # ---- joint vector: sources in order, their free slots in parameter order --------------
+        self.slot_of = []  # per joint index: (source, full-vector slot)
+        self.gidx = []     # per source: {slot: joint index}
+        for si, src in enumerate(self.sources):
+            if src.kind not in _SLOTS_OF:
+                raise ValueError(f"unsupported source kind {src.kind}")
+            g = {}
+            for sl in _SLOTS_OF[src.kind]:
+                if sl in src.locked:
+                    continue
+                if sl in (0, 1) and src.link_center is not None:
+                    lead = src.link_center
+                    if lead >= si or sl not in self.gidx[lead]:
+                        raise ValueError("a linked centre must point at an earlier source's free centre")
+                    g[sl] = self.gidx[lead][sl]
+                    continue
+                g[sl] = len(self.slot_of)
+                self.slot_of.append((si, sl))
+            self.gidx.append(g)
+        self.P = len(self.slot_of)
+        self.ndf = max(1.0, n_used - self.P)
+
+        # ---- stamp batches, one per (kind, fitted slots) --------------------------------------
+        self.groups = {}
+        for si, src in enumerate(self.sources):
+            free = tuple(sl for sl in _SLOTS_OF[src.kind] if sl not in src.locked)
+            self.groups.setdefault((src.kind, free), []).append(si)
+        kpsf = None if psf is None else (self.psf_np.shape[1], self.psf_np.shape[0])
+        self._jac_parts = []
+        jac_total = 0
+        for (kind, free), members in self.groups.items():
+            mask_bits = sum(1 << sl for sl in free)
+            o = N.make_options(profile=kind, psf_mode="full" if psf is not None else "none", free_mask=mask_bits,
+                               has_sky=False, **opts_kw)
+            shapes, geoms = [], []
+            for si in members:
+                (x0, x1), (y0, y1) = self._window(si)
+                shapes.append((x1 - x0, y1 - y0))
+                geoms.append(N.scale_geometry(1, self.scale, (x0 * self.scale, y0 * self.scale))[0])
+            jb = N.StampBatch(shapes, None if kpsf is None else [kpsf] * len(members), np.array(geoms), o, dev)
+            jpsf = None if psf is None else jb.pack_psf([self.psf_np] * len(members))
+            nf = len(free)
+            self._jac_parts.append(dict(kind=kind, free=free, members=members, batch=jb, psf=jpsf, off=jac_total,
+                                        nf=nf))
+            jac_total += nf * jb.out_pixels
+        self.jac = torch.zeros(max(jac_total, 1), dtype=torch.float32, device=dev)
+
+        # model renders on the group window, in chunks of sources of one kind (same plan)
+        self._fwd_parts = []
+        self.fwd_chunk = max(1, int(fwd_chunk))
+        fwd_total = 0
+        for (kind, free), members in self.groups.items():
+            m = min(self.fwd_chunk, len(members))
+            o = N.make_options(profile=kind, psf_mode="full" if psf is not None else "none",
+                               free_mask=sum(1 << sl for sl in _SLOTS_OF[kind]), has_sky=False, **opts_kw)
+            fb = N.StampBatch([(self.nx, self.ny)] * m, None if kpsf is None else [kpsf] * m,
+                              N.scale_geometry(m, self.scale), o, dev)
+            fpsf = None if psf is None else fb.pack_psf([self.psf_np] * m)
+            self._fwd_parts.append(dict(kind=kind, members=members, batch=fb, psf=fpsf, off=fwd_total, m=m))
+            fwd_total += len(members) * self.nx * self.ny
+        self.fwd = torch.zeros(max(fwd_total, 1), dtype=torch.float32, device=dev)
+
+        # ---- source descriptors ----------------------------------------------------------------
+        desc = (ApSceneSource * len(self.sources))()
+        for part in self._fwd_parts:
+            for k, si in enumerate(part["members"]):
+                desc[si].fwd_off = part["off"] + k * self.nx * self.ny
+        for part in self._jac_parts:
+            b = part["batch"]
+            for k, si in enumerate(part["members"]):
+                d = desc[si]
+                (x0, x1), (y0, y1) = self._window(si)
+                d.jac_off = part["off"] + int(b.out_offsets[k])
+                d.jac_stride = int(b.out_pixels)
+                d.x0, d.y0, d.wx, d.wy = x0, y0, x1 - x0, y1 - y0
+                d.n_free = part["nf"]
+                for c, sl in enumerate(part["free"]):
+                    d.gidx[c] = self.gidx[si][sl]
+        raw = bytes(desc)
+        self.desc = torch.frombuffer(bytearray(raw), dtype=torch.uint8).to(dev)
+
+        # ---- tile lists and overlapping pairs (windows are fixed for the scene) -------------
+        ntx, nty = (self.nx + TILE - 1) // TILE, (self.ny + TILE - 1) // TILE
+        lists = [[] for _ in range(ntx * nty)]
+        for si in range(len(self.sources)):
+            (x0, x1), (y0, y1) = self._window(si)
+            for ty in range(y0 // TILE, (y1 - 1) // TILE + 1):
+                for tx in range(x0 // TILE, (x1 - 1) // TILE + 1):
+                    lists[ty * ntx + tx].append(si)
+        ptr = np.zeros(len(lists) + 1, dtype=np.int32)
+        ptr[1:] = np.cumsum([len(l) for l in lists])
+        flat = np.array([s for l in lists for s in l] or [0], dtype=np.int32)
+        self.tile_ptr = torch.tensor(ptr, device=dev)
+        self.tile_src = torch.tensor(flat, device=dev)
+        pairs = []
+        wins = [self._window(si) for si in range(len(self.sources))]
+        for a in range(len(self.sources)):
+            (ax0, ax1), (ay0, ay1) = wins[a]
+            for b in range(a, len(self.sources)):
+                (bx0, bx1), (by0, by1) = wins[b]
+                if max(ax0, bx0) < min(ax1, bx1) and max(ay0, by0) < min(ay1, by1):
+                    pairs.append((a, b))
+        self.n_pairs = len(pairs)
+        self.pairs = torch.tensor(np.array(pairs, dtype=np.int32).reshape(-1, 2), device=dev).contiguous()
+
+        self.lib = N.lib()
+        self._solve_ws = torch.empty(int(self.lib.ap_dense_solve_workspace_bytes(self.P)), dtype=torch.uint8,
+                                     device=dev)
+        self._info = torch.zeros(1, dtype=torch.int32, device=dev)
+        self._d64 = torch.zeros(1, dtype=torch.float64, device=dev)
+
+    # ---- geometry and parameters -----------------------------------------------------------
+    def _window(self, si):
+        w = self.sources[si].window
+        if w is None:
+            return (0, self.nx), (0, self.ny)
+        (x0, x1), (y0, y1) = w
+        x0, y0 = max(0, int(x0)), max(0, int(y0))
+        x1, y1 = min(self.nx, int(x1)), min(self.ny, int(y1))
+        if x1 <= x0 or y1 <= y0:
+            raise ValueError(f"source {si} window lies outside the image")
+        return (x0, x1), (y0, y1)
+
+    def values_matrix(self, rep: np.ndarray) -> np.ndarray:
+        """[n_sources, 8] value-space rows from a joint representation vector."""
+        V = np.zeros((len(self.sources), 8))
+        for si, src in enumerate(self.sources):
+            p = np.asarray(src.params, dtype=np.float64)
+            V[si, : len(p)] = p
+            if src.kind == "exponential":
+                V[si, 4] = 1.0
+            for sl, g in self.gidx[si].items():
+                V[si, sl] = to_value(*SLOT_LIMITS[sl], rep[g])
+        return V
+
+    def representation(self) -> np.ndarray:
+        rep = np.zeros(self.P)
+        for g, (si, sl) in enumerate(self.slot_of):
+            rep[g] = to_rep(*SLOT_LIMITS[sl], self.sources[si].params[sl])
+        return rep
+
+    def set_representation(self, rep):
+        V = self.values_matrix(np.asarray(rep, dtype=np.float64))
+        for si, src in enumerate(self.sources):
+            src.params = list(V[si, :7])
+
+    # ---- device primitives -----------------------------------------------------------------
+    def forward(self, rep: np.ndarray) -> torch.Tensor:
+        """Model image [ny * nx] (float32) at the joint representation vector."""
+        V = self.values_matrix(rep)
+        for part in self._fwd_parts:
+            b, m, mem = part["batch"], part["m"], part["members"]
+            for c0 in range(0, len(mem), m):
+                chunk = mem[c0 : c0 + m]
+                params = np.zeros((m, 8))
+                params[:, :] = V[chunk[0]]
+                params[: len(chunk)] = V[chunk]
+                out = self.fwd[part["off"] + c0 * self.nx * self.ny : part["off"] + (c0 + m) * self.nx * self.ny]
+                if out.numel() == m * self.nx * self.ny:
+                    b.render(torch.tensor(params), part["psf"], out=out)
+                else:
+                    tmp = b.render(torch.tensor(params), part["psf"])
+                    out.copy_(tmp[: out.numel()])
+        img = torch.empty(self.nx * self.ny, dtype=torch.float32, device=self.device)
+        N.check(self.lib.ap_scene_forward(N._ptr(self.desc), N._ptr(self.tile_ptr), N._ptr(self.tile_src),
+                                          N._ptr(self.fwd), self.nx, ctypes.c_float(self.sky), self.nx, self.ny,
+                                          N._ptr(img), N._stream()), "ap_scene_forward")
+        return img
+
+    def jacobian(self, rep: np.ndarray):
+        """Own-window representation-space Jacobians of every source into ``self.jac``."""
+        V = self.values_matrix(rep)
+        for part in self._jac_parts:
+            b = part["batch"]
+            n = len(part["members"])
+            jac = self.jac[part["off"] : part["off"] + part["nf"] * b.out_pixels].view(part["nf"], b.out_pixels)
+            b.jacobian(torch.tensor(V[part["members"]]), part["psf"], as_representation=True, jac=jac)
+        return self.jac
+
+    def jacobian_image(self, rep: np.ndarray) -> np.ndarray:
+        """Dense [ny, nx, P] Jacobian (for tests and small scenes)."""
+        self.jacobian(rep)
+        out = np.zeros((self.ny, self.nx, self.P))
+        jac = self.jac.cpu().numpy()
+        for part in self._jac_parts:
+            b = part["batch"]
+            for k, si in enumerate(part["members"]):
+                (x0, x1), (y0, y1) = self._window(si)
+                o = int(b.out_offsets[k])
+                for c, sl in enumerate(part["free"]):
+                    col = jac[part["off"] + c * b.out_pixels + o : part["off"] + c * b.out_pixels + o
+                              + (x1 - x0) * (y1 - y0)]
+                    out[y0:y1, x0:x1, self.gidx[si][sl]] += col.reshape(y1 - y0, x1 - x0)
+        return out
+
+    def hess(self) -> torch.Tensor:
+        H = torch.empty((self.P, self.P), dtype=torch.float64, device=self.device)
+        N.check(self.lib.ap_scene_hess(N._ptr(self.desc), N._ptr(self.pairs), self.n_pairs, N._ptr(self.jac),
+                                       N._ptr(self.weight), N._ptr(self.mask), self.nx, self.P, N._ptr(H),
+                                       N._stream()), "ap_scene_hess")
+        return H
+
+    def jt(self, img: torch.Tensor) -> torch.Tensor:
+        out = torch.empty(self.P, dtype=torch.float64, device=self.device)
+        N.check(self.lib.ap_scene_jt(N._ptr(self.desc), len(self.sources), N._ptr(self.jac), N._ptr(img), self.nx,
+                                     self.P, N._ptr(out), N._stream()), "ap_scene_jt")
+        return out
+
+    def jvp(self, h: torch.Tensor) -> torch.Tensor:
+        out = torch.empty(self.nx * self.ny, dtype=torch.float32, device=self.device)
+        N.check(self.lib.ap_scene_jvp(N._ptr(self.desc), N._ptr(self.tile_ptr), N._ptr(self.tile_src),
+                                      N._ptr(self.jac), N._ptr(h.contiguous()), self.nx, self.ny, N._ptr(out),
+                                      N._stream()), "ap_scene_jvp")
+        return out
+
+    def chi2(self, model: torch.Tensor) -> float:
+        N.check(self.lib.ap_scene_chi2(N._ptr(model), N._ptr(self.data), N._ptr(self.weight), N._ptr(self.mask),
+                                       self.nx * self.ny, N._ptr(self._d64), N._stream()), "ap_scene_chi2")
+        return float(self._d64.item())
+
+    def residual(self, model: torch.Tensor, data: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """W (data - model) on unmasked pixels."""
+        r = torch.empty(self.nx * self.ny, dtype=torch.float32, device=self.device)
+        d = self.data if data is None else data
+        N.check(self.lib.ap_scene_residual(N._ptr(model), N._ptr(d), N._ptr(self.weight), N._ptr(self.mask),
+                                           self.nx * self.ny, N._ptr(r), N._stream()), "ap_scene_residual")
+        return r
+
+    def rpp_image(self, r, rh, jh, d) -> torch.Tensor:
+        out = torch.empty(self.nx * self.ny, dtype=torch.float32, device=self.device)
+        N.check(self.lib.ap_scene_rpp_image(N._ptr(r), N._ptr(rh), N._ptr(jh), N._ptr(self.weight),
+                                            N._ptr(self.mask), float(d), self.nx * self.ny, N._ptr(out),
+                                            N._stream()), "ap_scene_rpp_image")
+        return out
+
+    def solve(self, H: torch.Tensor, g: torch.Tensor, L: float):
+        """Damped solve; None when the damped matrix is not positive definite."""
+        h = torch.empty(self.P, dtype=torch.float64, device=self.device)
+        N.check(self.lib.ap_dense_damped_solve(self.P, N._ptr(H), N._ptr(g.contiguous()), float(L), N._ptr(h),
+                                               N._ptr(self._solve_ws), self._solve_ws.numel(), N._ptr(self._info),
+                                               N._stream()), "ap_dense_damped_solve")
+        if int(self._info.item()) != 0:
+            return None
+        return h
+
+
+class OptimizeStop(Exception):
+    pass
+
+
+class SceneLM:
+    """``LM`` (fit/lm.py:15-539) over a scene's joint vector."""
+
+    def __init__(self, scene: Scene, initial_state=None, max_iter: int = 100, relative_tolerance: float = 1e-5,
+                 max_step_iter: int = 10, curvature_limit: float = 1.0, Lup: float = 11.0, Ldn: float = 9.0,
+                 L0: float = 1.0, acceleration: float = 0.0, ndf=None):
+        self.scene = scene
+        self.x = np.array(scene.representation() if initial_state is None else initial_state, dtype=np.float64)
+        self.max_iter, self.relative_tolerance = int(max_iter), float(relative_tolerance)
+        self.max_step_iter, self.curvature_limit = int(max_step_iter), float(curvature_limit)
+        self._Lup, self._Ldn, self.L, self.acceleration = float(Lup), float(Ldn), float(L0), float(acceleration)
+        self.ndf = scene.ndf if ndf is None else ndf
+        self.loss_history, self.L_history, self.lambda_history = [], [], []
+        self.message = ""
+        self.iterations = 0
+
+    def Lup(self):
+        self.L = min(1e9, self.L * self._Lup)
+
+    def Ldn(self):
+        self.L = max(1e-9, self.L / self._Ldn)
+
+    def _chi2(self, model):
+        return self.scene.chi2(model) / self.ndf
+
+    def step(self, chi2):
+        sc = self.scene
+        x = self.x
+        Y0 = sc.forward(x)
+        sc.jacobian(x)
+        hess = sc.hess()
+        resid = sc.residual(Y0)             # W (Y - Y0) = -r
+        grad = sc.jt(resid)                 # -J^T r
+        r = sc.residual(sc.data, Y0)        # W (Y0 - Y)
+        init_chi2 = chi2
+        nostep = True
+        best = (np.zeros_like(x), init_chi2, self.L)
+        scarry_best = (None, init_chi2, self.L)
+        direction = "none"
+        d = 0.1
+        for iteration in range(self.max_step_iter):
+            if iteration > self.max_step_iter / 2 and self.L < 1e-3:
+                self.L = 1.0
+            h = sc.solve(hess, grad, self.L)
+            if h is None:
+                self.Lup()
+                if direction == "better":
+                    break
+                direction = "worse"
+                continue
+            h_np = h.cpu().numpy()
+            Y1 = sc.forward(x + d * h_np)
+            rh = sc.residual(sc.data, Y1)   # W (Y1 - Y)
+            rpp = sc.jt(sc.rpp_image(r, rh, sc.jvp(h), d))
+            if self.L > 1e-4:
+                a_d = sc.solve(hess, rpp, self.L)
+                a = np.zeros_like(h_np) if a_d is None else -a_d.cpu().numpy() / 2
+            else:
+                a = np.zeros_like(h_np)
+            ha = h_np + a * self.acceleration
+            Y1 = sc.forward(x + ha)
+            chi2 = self._chi2(Y1)
+            if not np.isfinite(chi2):
+                self.Lup()
+                if direction == "better":
+                    break
+                direction = "worse"
+                continue
+            if chi2 <= scarry_best[1]:
+                scarry_best = (ha, chi2, self.L)
+            rho = np.linalg.norm(a) / np.linalg.norm(h_np)
+            if rho > self.curvature_limit:
+                self.Lup()
+                if direction == "better":
+                    break
+                direction = "worse"
+                continue
+            if chi2 < best[1]:
+                best = (ha, chi2, self.L)
+                nostep = False
+                self.Ldn()
+                if self.L <= 1e-8 or direction == "worse":
+                    break
+                direction = "better"
+            elif chi2 > best[1] and direction in ("none", "worse"):
+                self.Lup()
+                if self.L == 1e9:
+                    break
+                direction = "worse"
+            else:
+                break
+            if (best[1] - init_chi2) / init_chi2 < -0.1:
+                break
+        if nostep:
+            if scarry_best[0] is not None:
+                return scarry_best
+            raise OptimizeStop("Could not find step to improve chi^2")
+        return best
+
+    def fit(self):
+        if self.scene.P == 0:
+            return self
+        self.loss_history = [self._chi2(self.scene.forward(self.x))]
+        self.L_history = [self.L]
+        self.lambda_history = [self.x.copy()]
+        for iteration in range(self.max_iter):
+            self.iterations = iteration + 1
+            try:
+                res = self.step(chi2=self.loss_history[-1])
+            except OptimizeStop:
+                self.message = self.message + "fail. Could not find step to improve Chi^2"
+                break
+            self.L = res[2]
+            self.x = self.x + res[0]
+            self.L_history.append(self.L)
+            self.loss_history.append(res[1])
+            self.lambda_history.append(self.x.copy())
+            self.Ldn()
+            if len(self.loss_history) >= 3:
+                if (self.loss_history[-3] - self.loss_history[-1]) / self.loss_history[-1] < self.relative_tolerance \
+                        and self.L < 0.1:
+                    self.message = self.message + "success"
+                    break
+            if len(self.loss_history) > 10:
+                if (self.loss_history[-10] - self.loss_history[-1]) / self.loss_history[-1] < self.relative_tolerance:
+                    self.message = self.message + "success by immobility. Convergence not guaranteed"
+                    break
+        else:
+            self.message = self.message + "fail. Maximum iterations"
+        self.scene.set_representation(self.res())
+        return self
+
+    def res(self):
+        hist = np.array(self.loss_history)
+        ok = np.isfinite(hist)
+        if not ok.any():
+            return self.x.copy()
+        return np.array(self.lambda_history)[ok][np.argmin(hist[ok])]

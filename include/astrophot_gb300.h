@@ -225,6 +225,58 @@ int ap_render_noalloc(int32_t nx, int32_t ny, int32_t psf_kx, int32_t psf_ky,
                       const double* geometry, const ap_options* options, const double* params,
                       const float* psf, float* model, ap_stream_t stream);
 
+/* ---- scenes: many sources on one image, fitted jointly ----------------------------------------
+ * Group_Model.sample / jacobian (astrophot/models/group_model_object.py:183-283) over the joint
+ * parameter vector of LM (astrophot/fit/lm.py) when the sources share an image.  The sources are
+ * rendered by ap_batch stamps (ap_render for the model on the group's window, ap_jacobian on each
+ * source's own window, as the reference does); these entry points combine them.  One
+ * ap_scene_source per source (device array): */
+typedef struct ap_scene_source {
+  int64_t fwd_off;    /* element offset of the source's model render (group window, row stride
+                         fwd_nx) in the forward buffer */
+  int64_t jac_off;    /* element offset of its own-window Jacobian (compact slot 0) */
+  int64_t jac_stride; /* elements between its compact slots (the batch's output pixels) */
+  int32_t x0, y0;     /* own window: first pixel in the image */
+  int32_t wx, wy;     /* own window size */
+  int32_t n_free;     /* compact (fitted) slots of the source, <= 8 */
+  int32_t gidx[8];    /* joint-vector index of each compact slot (linked slots share one) */
+  int32_t reserved;
+} ap_scene_source;
+
+/* image = sky + sum of the sources' renders inside their own windows.  tile_ptr / tile_src: for
+ * every 32 x 32 image tile (row-major, ceil(nx/32) per row) the sources whose windows touch it
+ * (CSR; the order fixes the summation order). */
+int ap_scene_forward(const ap_scene_source* sources, const int32_t* tile_ptr, const int32_t* tile_src,
+                     const float* fwd, int32_t fwd_nx, float sky, int32_t nx, int32_t ny, float* image,
+                     ap_stream_t stream);
+/* out[ny][nx] = J h (h[P] float64), own windows, same tile lists. */
+int ap_scene_jvp(const ap_scene_source* sources, const int32_t* tile_ptr, const int32_t* tile_src,
+                 const float* jac, const double* h, int32_t nx, int32_t ny, float* out, ap_stream_t stream);
+/* out[P] = J^T v for an image v[ny][nx]. */
+int ap_scene_jt(const ap_scene_source* sources, int32_t n_sources, const float* jac, const float* v,
+                int32_t nx, int32_t P, double* out, ap_stream_t stream);
+/* H[P][P] = J^T W J; pairs[n_pairs][2] = every (a, b), a <= b, whose windows overlap (a = b
+ * included).  weight / mask (1 = ignored) may be NULL. */
+int ap_scene_hess(const ap_scene_source* sources, const int32_t* pairs, int32_t n_pairs,
+                  const float* jac, const float* weight, const uint8_t* mask, int32_t nx, int32_t P,
+                  double* H, ap_stream_t stream);
+/* out[0] = sum over unmasked pixels of W (data - model)^2 (float64). */
+int ap_scene_chi2(const float* model, const float* data, const float* weight, const uint8_t* mask,
+                  int64_t n, double* out, ap_stream_t stream);
+/* r = W (data - model) on unmasked pixels, 0 on masked ones (LM._r, fit/lm.py:381-385). */
+int ap_scene_residual(const float* model, const float* data, const float* weight,
+                      const uint8_t* mask, int64_t n, float* r, ap_stream_t stream);
+/* out = (2/d)((rh - r)/d - W jh): the image whose J^T is the geodesic-acceleration right-hand
+ * side of LM.step (fit/lm.py:286-291). */
+int ap_scene_rpp_image(const float* r, const float* rh, const float* jh, const float* weight,
+                       const uint8_t* mask, double d, int64_t n, float* out, ap_stream_t stream);
+/* h = solve(H o (I + D/(1+L)) + L I (1 + diag H), g) for one dense n x n system (LM._h,
+ * fit/lm.py:361-371): blocked FP64 Cholesky.  info (device) = 0, or 1 + the row whose pivot
+ * was not positive (the system is then not solved). */
+size_t ap_dense_solve_workspace_bytes(int32_t n);
+int ap_dense_damped_solve(int32_t n, const double* H, const double* g, double L, double* h,
+                          void* ws, size_t ws_bytes, int32_t* info, ap_stream_t stream);
+
 /* ---- learned initial guess -----------------------------------------------------------------
  * No counterpart in the reference: its initial values come from the heuristics of
  * Galaxy_Model.initialize / parametric_initialize (astrophot/models/galaxy_model_object.py:60-113,

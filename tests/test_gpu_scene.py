@@ -1,0 +1,104 @@
+"""Scenes on the GPU (many galaxies on one image, joint LM): against the reference's
+``Group_Model`` golden (per-component pixel windows, a bulge and a disk sharing one centre
+node, PSF convolution) recorded from the reference, and the scene primitives against numpy."""
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+import cases  # noqa: E402
+
+
+@pytest.fixture(scope="module")
+def S():
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA GPU")
+    from astrophot_gb300 import scene
+
+    return scene
+
+
+# the GROUP_SOURCES of tests/golden/make_golden.py
+WINDOWS = (((8, 72), (10, 74)), ((8, 72), (10, 74)), ((50, 96), (36, 90)), ((0, 44), (52, 96)))
+KINDS = ("sersic", "exponential", "sersic", "sersic")
+LINKS = (None, 0, None, None)
+
+
+def golden_scene(S, d, values=None):
+    values = d["init_values"] if values is None else values
+    srcs = [S.SceneSource(k, list(v), w, l) for k, v, w, l in zip(KINDS, values, WINDOWS, LINKS)]
+    N = d["spec"]["size"]
+    return S.Scene(N, N, srcs, d["psf"], d["data"], d["weight"], sky=1.0)
+
+
+@pytest.mark.parametrize("name", cases.group_case_names())
+def test_scene_model_and_jacobian_match_reference(S, name):
+    d = cases.load_group(name)
+    sc = golden_scene(S, d)
+    rep0 = sc.representation()
+    assert sc.P == 25
+    assert np.allclose(rep0, d["rep0"], rtol=0, atol=1e-12)
+    m = sc.forward(rep0).cpu().numpy().reshape(d["init_model"].shape)
+    ref = d["init_model"]
+    assert np.max(np.abs(m - ref)) <= 1e-5 * np.max(np.abs(ref)), np.max(np.abs(m - ref)) / np.max(np.abs(ref))
+    J = sc.jacobian_image(rep0)
+    for k in range(J.shape[-1]):
+        rk = d["jac_rep"][..., k]
+        err = np.max(np.abs(J[..., k] - rk)) / np.max(np.abs(rk))
+        assert err <= 2e-4, (k, err)
+
+
+@pytest.mark.parametrize("name", cases.group_case_names())
+def test_scene_primitives_match_numpy(S, name):
+    d = cases.load_group(name)
+    sc = golden_scene(S, d)
+    rep0 = sc.representation()
+    J = sc.jacobian_image(rep0).reshape(-1, sc.P)
+    W = d["weight"].astype(np.float32).astype(np.float64).reshape(-1)
+    H = sc.hess().cpu().numpy()
+    Hn = J.T @ (W[:, None] * J)
+    assert np.max(np.abs(H - Hn)) <= 1e-5 * np.max(np.abs(Hn))
+    rng = np.random.default_rng(3)
+    v = rng.normal(size=J.shape[0]).astype(np.float32)
+    jt = sc.jt(torch.tensor(v, device="cuda")).cpu().numpy()
+    want = J.T @ v.astype(np.float64)
+    assert np.max(np.abs(jt - want)) <= 1e-5 * np.max(np.abs(want))
+    h = rng.normal(size=sc.P)
+    jv = sc.jvp(torch.tensor(h, device="cuda")).cpu().numpy()
+    want = J @ h
+    assert np.max(np.abs(jv - want)) <= 1e-5 * np.max(np.abs(want))
+
+
+@pytest.mark.parametrize("n", [7, 32, 100, 257])
+def test_dense_damped_solve_matches_numpy(S, n):
+    rng = np.random.default_rng(n)
+    A = rng.normal(size=(n, 2 * n))
+    H = A @ A.T
+    g = rng.normal(size=n)
+    L = 0.37
+    I = np.eye(n)
+    D = np.ones_like(H) - I
+    M = H * (I + D / (1 + L)) + L * I * (1 + np.diag(H))
+    want = np.linalg.solve(M, g)
+    d = cases.load_group(cases.group_case_names()[0])
+    sc = golden_scene(S, d)
+    sc.P = n
+    sc._solve_ws = torch.empty(int(sc.lib.ap_dense_solve_workspace_bytes(n)), dtype=torch.uint8, device="cuda")
+    h = sc.solve(torch.tensor(H, device="cuda"), torch.tensor(g, device="cuda"), L).cpu().numpy()
+    assert np.allclose(h, want, rtol=1e-9, atol=1e-12 * np.max(np.abs(want)))
+    # not positive definite: reported, not solved
+    assert sc.solve(torch.tensor(-H, device="cuda"), torch.tensor(g, device="cuda"), 0.0) is None
+
+
+@pytest.mark.parametrize("name", cases.group_case_names())
+def test_scene_lm_matches_reference(S, name):
+    d = cases.load_group(name)
+    sc = golden_scene(S, d)
+    lm = S.SceneLM(sc, max_iter=d["spec"]["max_iter"]).fit()
+    print(name, lm.loss_history, d["loss_history"], lm.message)
+    assert lm.message == d["message"]
+    assert abs(min(lm.loss_history) / d["loss_history"].min() - 1) <= 1e-4
+    # the first steps follow the reference's trajectory
+    assert np.allclose(lm.loss_history[:3], d["loss_history"][:3], rtol=1e-5)
