@@ -102,6 +102,7 @@ EXPORTS = [
     ("ap_batch_sizes", [_P, _PI64, _PI64, _PI64]),
     ("ap_batch_offsets", [_P, _PI64, _PI64]),
     ("ap_batch_bind", [_P, _P, _I64, _P]),
+    ("ap_batch_set_threshold_numel", [_P, _PD]),
     ("ap_render", [_P, _P, _P, _P, _P]),
     ("ap_jacobian", [_P, _P, _P, _P, _P, _I32, _P]),
     ("ap_render_vjp", [_P, _P, _P, _P, _I32, _P, _P]),
@@ -118,7 +119,7 @@ EXPORTS = [
     ("ap_fma_probe", [_P, _I32, _I32, _P]),
     ("ap_batch_stats", [_P, _PI64]),
     ("ap_render_noalloc", [_I32, _I32, _I32, _I32, _PD, ctypes.POINTER(ApOptions), _P, _P, _P, _P]),
-    ("ap_scene_forward", [_P, _P, _P, _P, _I32, ctypes.c_float, _I32, _I32, _P, _P]),
+    ("ap_scene_forward", [_P, _P, _P, _P, ctypes.c_float, _I32, _I32, _P, _P]),
     ("ap_scene_jvp", [_P, _P, _P, _P, _P, _I32, _I32, _P, _P]),
     ("ap_scene_jt", [_P, _I32, _P, _P, _I32, _I32, _P, _P]),
     ("ap_scene_hess", [_P, _P, _I32, _P, _P, _P, _I32, _I32, _P, _P]),
@@ -385,6 +386,11 @@ class StampBatch:
             out = torch.empty(self.out_pixels, dtype=torch.float32, device=self.device)
         check(self.lib.ap_render(self.handle, _ptr(params), _ptr(psf), _ptr(out), _stream()), "ap_render")
         return out
+
+    def set_threshold_numel(self, numel):
+        """Pixel count of each stamp's integration threshold (see ap_batch_set_threshold_numel)."""
+        arr = np.ascontiguousarray(np.broadcast_to(np.asarray(numel, dtype=np.float64), (self.n,)))
+        check(self.lib.ap_batch_set_threshold_numel(self.handle, arr.ctypes.data_as(_PD)), "threshold numel")
 
     def jacobian(self, params: torch.Tensor, psf: Optional[torch.Tensor], as_representation=True,
                  model: Optional[torch.Tensor] = None, jac: Optional[torch.Tensor] = None):

@@ -232,6 +232,7 @@ int ap_batch_create(ap_batch** out, int32_t n, const int32_t* nx, const int32_t*
       st.Pf[k] = (float)st.P[k];
       st.Pinvf[k] = (float)st.Pinv[k];
     }
+    st.thr_numel = (double)st.wnx * (double)st.wny;
     st.out_off = out_off;
     st.work_off = work_off;
     st.psf_off = psf_off;
@@ -412,6 +413,18 @@ int ap_batch_offsets(const ap_batch* b, int64_t* out_offsets, int64_t* psf_offse
 int ap_batch_psf_stride(const ap_batch* b, int64_t* stride) {
   if (!b || !stride) return AP_ERR_ARG;
   *stride = b->max_kp2;
+  return AP_OK;
+}
+
+int ap_batch_set_threshold_numel(ap_batch* b, const double* numel) {
+  if (!b || !numel) return AP_ERR_ARG;
+  for (int i = 0; i < b->n; ++i)
+    if (!(numel[i] > 0)) return AP_ERR_ARG;
+  for (int i = 0; i < b->n; ++i) b->stamps[i].thr_numel = numel[i];
+  if (b->bound) {
+    const Layout& L = b->L;
+    return check_cuda(cudaMemcpy(b->ws + L.stamps, b->stamps.data(), sizeof(StampDev) * b->n, cudaMemcpyHostToDevice));
+  }
   return AP_OK;
 }
 

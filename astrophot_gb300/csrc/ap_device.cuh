@@ -111,6 +111,7 @@ struct StampDev {
   double ref_ij[2], ref_xy[2];
   double pixel_area;
   float Pf[4], Pinvf[4];  // FP32 copies for the per-pixel paths
+  double thr_numel;       // pixel count of the integration threshold (default: working window)
 };
 
 struct EvalDev {

@@ -132,7 +132,7 @@ __global__ void k_eval_setup(BatchArgs b, const double* params, int64_t stamp_st
     const double bn = e.bn64;
     const double flux = 2 * kPi * Ie * v[PRE] * v[PRE] * v[PQ] * n * (exp(bn) * pow(bn, -2 * n)) *
                         exp(lgamma(2 * n));
-    e.thresh64 = b.tolerance64 * (flux / ((double)st.wnx * (double)st.wny));
+    e.thresh64 = b.tolerance64 * (flux / st.thr_numel);
   } else {
     e.thresh64 = 0.0;
   }
@@ -380,7 +380,7 @@ __global__ void k_exp_threshold(BatchArgs b) {
   EvalDev& e = b.evals[t];
   if (!e.ops) return;
   const StampDev& st = b.stamps[t >> 1];
-  e.thresh64 = b.tolerance64 * (b.mean_acc[t] / ((double)st.wnx * (double)st.wny));
+  e.thresh64 = b.tolerance64 * (b.mean_acc[t] / st.thr_numel);
   e.thresh = (float)e.thresh64;
 }
 

@@ -162,6 +162,7 @@ extern "C" int ap_render_noalloc(int32_t nx, int32_t ny, int32_t psf_kx, int32_t
     st.Pf[k] = (float)st.P[k];
     st.Pinvf[k] = (float)st.Pinv[k];
   }
+  st.thr_numel = (double)st.wnx * (double)st.wny;
   st.ntw_x = (st.wnx + kTile - 1) / kTile;
   st.ntw = st.ntw_x * ((st.wny + kTile - 1) / kTile);
   st.nto_x = (nx + kOutTileX - 1) / kOutTileX;

@@ -37,7 +37,7 @@ __device__ __forceinline__ bool in_window(const ap_scene_source& s, int x, int y
 // ---- forward: image = sky + sum over the tile's sources (fixed order: deterministic) -------------
 __global__ void k_scene_forward(const ap_scene_source* __restrict__ src, const int32_t* __restrict__ tile_ptr,
                                 const int32_t* __restrict__ tile_src, const float* __restrict__ fwd, float sky, int nx,
-                                int ny, int fwd_nx, float* __restrict__ image) {
+                                int ny, float* __restrict__ image) {
   const int tx = blockIdx.x % ((nx + kSceneTile - 1) / kSceneTile);
   const int ty = blockIdx.x / ((nx + kSceneTile - 1) / kSceneTile);
   const int t = blockIdx.x;
@@ -48,7 +48,7 @@ __global__ void k_scene_forward(const ap_scene_source* __restrict__ src, const i
     float v = sky;
     for (int k = b; k < e; ++k) {
       const ap_scene_source& s = src[tile_src[k]];
-      if (in_window(s, x, y)) v += fwd[s.fwd_off + (int64_t)y * fwd_nx + x];
+      if (in_window(s, x, y)) v += fwd[s.fwd_off + (int64_t)(y - s.fwd_y0) * s.fwd_nx + (x - s.fwd_x0)];
     }
     image[(int64_t)y * nx + x] = v;
   }
@@ -328,12 +328,10 @@ inline int egrid(int64_t n) {
 extern "C" {
 
 int ap_scene_forward(const ap_scene_source* sources, const int32_t* tile_ptr, const int32_t* tile_src,
-                     const float* fwd, int32_t fwd_nx, float sky, int32_t nx, int32_t ny, float* image,
-                     ap_stream_t stream) {
-  if (!sources || !tile_ptr || !tile_src || !fwd || !image || nx <= 0 || ny <= 0 || fwd_nx < nx) return AP_ERR_ARG;
+                     const float* fwd, float sky, int32_t nx, int32_t ny, float* image, ap_stream_t stream) {
+  if (!sources || !tile_ptr || !tile_src || !fwd || !image || nx <= 0 || ny <= 0) return AP_ERR_ARG;
   const int tiles = ((nx + kSceneTile - 1) / kSceneTile) * ((ny + kSceneTile - 1) / kSceneTile);
-  k_scene_forward<<<tiles, 256, 0, (cudaStream_t)stream>>>(sources, tile_ptr, tile_src, fwd, sky, nx, ny, fwd_nx,
-                                                           image);
+  k_scene_forward<<<tiles, 256, 0, (cudaStream_t)stream>>>(sources, tile_ptr, tile_src, fwd, sky, nx, ny, image);
   return record_cuda(cudaGetLastError());
 }
 

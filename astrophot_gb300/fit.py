@@ -17,7 +17,7 @@ import torch
 
 from . import config
 from .errors import OptimizeStop
-from .models import _Structure, _plan
+from .models import _Structure, _make_scene, _needs_scene, _plan
 
 __all__ = ("LM", "BatchLM")
 
@@ -113,6 +113,24 @@ class LM:
         self.max_iter = max_iter
         self.relative_tolerance = relative_tolerance
         self.kwargs = dict(kwargs, max_iter=max_iter, relative_tolerance=relative_tolerance)
+        comps = list(model.models.values()) if hasattr(model, "models") else [model]
+        self._scene = None
+        if _needs_scene(model, comps):
+            # several galaxies on one image: joint LM over the scene (fit/lm.py over a Group_Model)
+            if initial_state is None:
+                model.initialize()
+                initial_state = model.parameters.vector_representation()
+            self._scene = _make_scene(model, comps)
+            self._scene_ndf = ndf
+            self.current_state = torch.as_tensor(initial_state, dtype=config.ap_dtype).flatten()
+            self.ndf = self._scene.ndf if ndf is None else ndf
+            self.message = ""
+            self.loss_history, self.L_history, self.lambda_history = [], [], []
+            self._covariance_matrix = None
+            tgt = model.target[model.window]
+            self.W = tgt.flatten("weight")
+            self.mask = None if not tgt.has_mask else torch.logical_not(tgt.flatten("mask"))
+            return
         self._fit = _Fit(model, initial_state)
         self.current_state = self._fit.current_state
         tgt = self._fit.target
@@ -131,6 +149,20 @@ class LM:
         if len(self.current_state) == 0:
             return self
         self._covariance_matrix = None
+        if self._scene is not None:
+            from .scene import SceneLM
+
+            kw = {k: self.kwargs[k] for k in ("max_step_iter", "curvature_limit", "Lup", "Ldn", "L0", "acceleration")
+                  if k in self.kwargs}
+            lm = SceneLM(self._scene, initial_state=self.current_state.numpy(), max_iter=self.max_iter,
+                         relative_tolerance=self.relative_tolerance, ndf=self._scene_ndf, **kw).fit()
+            self.loss_history, self.L_history = list(lm.loss_history), list(lm.L_history)
+            self.lambda_history = [np.array(v) for v in lm.lambda_history]
+            self.current_state = torch.tensor(lm.x)
+            self.message = self.message + lm.message
+            self.iterations = lm.iterations
+            self.model.parameters.vector_set_representation(torch.tensor(lm.res()))
+            return self
         _run([self._fit], self.kwargs)
         f = self._fit
         self.loss_history, self.L_history, self.lambda_history = f.loss_history, f.L_history, f.lambda_history

@@ -536,6 +536,8 @@ def _plan(owner, struct: _Structure, window: Window):
 
 
 def _sample_structure(owner, components, image, window):
+    if _needs_scene(owner, components):
+        return _sample_scene(owner, components, image, window)
     struct = _Structure(owner, components)
     w = owner.window if window is None else (owner.window & window)
     if image is None:
@@ -548,6 +550,8 @@ def _sample_structure(owner, components, image, window):
 
 
 def _jacobian_structure(owner, components, as_representation, window):
+    if _needs_scene(owner, components):
+        return _jacobian_scene(owner, components, as_representation, window)
     struct = _Structure(owner, components)
     w = owner.window if window is None else (owner.window & window)
     batch, psf_d = _plan(owner, struct, w)
@@ -596,3 +600,112 @@ class _NLLFunction(torch.autograd.Function):
         compact = [i for i in range(8) if batch.options.free_mask & (1 << i)]
         grad = torch.tensor([float(gc[compact.index(sl)]) for sl in ctx.struct.vector_order()], dtype=config.ap_dtype)
         return grad * grad_out.to("cpu", config.ap_dtype), None, None
+
+
+# ----------------------------------------------------------------------------------------
+# groups of several galaxies on one image: scenes (astrophot_gb300.scene)
+# ----------------------------------------------------------------------------------------
+def _galaxies(components):
+    return [c for c in components if isinstance(c, (Sersic_Galaxy, Exponential_Galaxy))]
+
+
+def _needs_scene(owner, components):
+    """More than one galaxy, or a galaxy whose own window is not the group's window."""
+    gals = _galaxies(components)
+    if len(gals) > 1:
+        return True
+    if gals and gals[0] is not owner and gals[0]._window is not None and not (gals[0].window == owner.window):
+        return True
+    return False
+
+
+_KNOBS = ("sampling_mode", "sampling_tolerance", "integrate_mode", "integrate_max_depth", "integrate_gridding",
+          "integrate_quad_level", "softening", "psf_subpixel_shift", "psf_mode")
+
+
+def _scene_spec(owner, components):
+    from .scene import SceneSource
+
+    w = owner.window
+    gals = _galaxies(components)
+    skies = [c for c in components if isinstance(c, Flat_Sky)]
+    if len(gals) + len(skies) != len(components) or len(skies) > 1:
+        raise NotImplementedError("the scene path covers Sersic / exponential galaxies and one flat sky")
+    sky = 0.0
+    if skies:
+        F = skies[0].parameters["F"]
+        if not F.locked:
+            raise NotImplementedError("a free sky in a group of several galaxies is not supported by the CUDA path")
+        sky = float(w.pixel_area) * 10.0 ** float(F.value.item())
+    knobs = {k: getattr(gals[0], k) for k in _KNOBS}
+    for g in gals[1:]:
+        if any(getattr(g, k) != knobs[k] for k in _KNOBS):
+            raise NotImplementedError("galaxies of one group must share their sampling / PSF settings on the CUDA path")
+    psf = gals[0].psf if knobs["psf_mode"] == "full" else None
+    if psf is not None and any(g.psf is not psf for g in gals[1:]):
+        raise NotImplementedError("galaxies of one group must share one PSF on the CUDA path")
+    center_owner = {}
+    sources = []
+    for gi, g in enumerate(gals):
+        p = g.parameters
+        c = p["center"]
+        link = None
+        if isinstance(c._value, Parameter_Node):
+            target = c._value
+            if id(target) not in center_owner:
+                raise NotImplementedError("a linked centre must point at the centre of an earlier galaxy of the group")
+            link = center_owner[id(target)]
+        else:
+            center_owner[id(c)] = gi
+        vals = [float(v) for v in c.value.numpy()] + [
+            p["q"].value.item(), p["PA"].value.item(), p["n"].value.item() if "n" in p else 1.0, p["Re"].value.item(),
+            p["Ie"].value.item()]
+        locked = tuple(sl for name, slots in SLOT.items() if name in p and name != "F"
+                       for sl in slots if p[name].locked and not (name == "center" and link is not None))
+        di, dj = g.window.offset_in(w)
+        win = ((di, di + int(g.window.pixel_shape[0])), (dj, dj + int(g.window.pixel_shape[1])))
+        sources.append(SceneSource(g.profile, vals, win, link, locked))
+    opts = {k: knobs[k] for k in _KNOBS if k != "psf_mode"}
+    return w, sources, psf, sky, opts
+
+
+def _make_scene(owner, components, with_data=True):
+    from .scene import Scene
+
+    w, sources, psf, sky, opts = _scene_spec(owner, components)
+    if abs(w.pixelscale[0, 1]) > 0 or abs(w.pixelscale[1, 0]) > 0 or abs(w.pixelscale[0, 0] - w.pixelscale[1, 1]) > 0:
+        raise NotImplementedError("scenes need a square, axis-aligned pixel grid on the CUDA path")
+    nx, ny = int(w.pixel_shape[0]), int(w.pixel_shape[1])
+    origin = w.pixel_to_plane(-0.5, -0.5)
+    if with_data:
+        tgt = owner.target[w]
+        data, weight = tgt.data.numpy(), tgt.weight.numpy()
+        mask = tgt.mask.numpy() if tgt.has_mask else None
+    else:
+        data = weight = np.zeros((ny, nx))
+        mask = None
+    scene = Scene(nx, ny, sources, None if psf is None else psf.data.numpy(), data, weight, mask=mask, sky=sky,
+                  scale=float(w.pixelscale[0, 0]), options=opts, origin=(float(origin[0]), float(origin[1])),
+                  device=config.ap_device)
+    if scene.P != len(owner.parameters.vector_values()):
+        raise NotImplementedError("this parameter structure has no joint-vector mapping on the CUDA path")
+    return scene
+
+
+def _sample_scene(owner, components, image, window):
+    w = owner.window if window is None else (owner.window & window)
+    if window is not None and not (w == owner.window):
+        raise NotImplementedError("sampling a sub-window of a multi-galaxy group is not supported by the CUDA path")
+    scene = _make_scene(owner, components, with_data=False)
+    img = scene.forward(scene.representation()).cpu().numpy().reshape(scene.ny, scene.nx).astype(np.float64)
+    if image is None:
+        image = owner.target.model_image(w)
+    image += Model_Image(torch.as_tensor(img, dtype=config.ap_dtype), w.copy())
+    return image
+
+
+def _jacobian_scene(owner, components, as_representation, window):
+    w = owner.window
+    scene = _make_scene(owner, components, with_data=False)
+    J = scene.jacobian_image(scene.representation(), as_representation=as_representation)
+    return Jacobian_Image(owner.parameters.vector_identities(), J, w.copy())

@@ -48,7 +48,9 @@ class ApSceneSource(ctypes.Structure):
         ("wy", ctypes.c_int32),
         ("n_free", ctypes.c_int32),
         ("gidx", ctypes.c_int32 * 8),
-        ("reserved", ctypes.c_int32),
+        ("fwd_x0", ctypes.c_int32),
+        ("fwd_y0", ctypes.c_int32),
+        ("fwd_nx", ctypes.c_int32),
     ]
 
 
@@ -73,8 +75,9 @@ class Scene:
 
     def __init__(self, nx: int, ny: int, sources: List[SceneSource], psf: Optional[np.ndarray], data, weight,
                  mask=None, sky: float = 0.0, scale: float = 1.0, options: Optional[dict] = None,
-                 fwd_chunk: int = 64, device="cuda"):
+                 fwd_chunk: int = 64, device="cuda", origin=(0.0, 0.0)):
         self.nx, self.ny, self.scale = int(nx), int(ny), float(scale)
+        self.origin = (float(origin[0]), float(origin[1]))
         self.sources = list(sources)
         self.device = torch.device(device)
         self.sky = float(sky)
@@ -126,7 +129,8 @@ class Scene:
             for si in members:
                 (x0, x1), (y0, y1) = self._window(si)
                 shapes.append((x1 - x0, y1 - y0))
-                geoms.append(N.scale_geometry(1, self.scale, (x0 * self.scale, y0 * self.scale))[0])
+                geoms.append(N.scale_geometry(1, self.scale, (self.origin[0] + x0 * self.scale,
+                                                              self.origin[1] + y0 * self.scale))[0])
             jb = N.StampBatch(shapes, None if kpsf is None else [kpsf] * len(members), np.array(geoms), o, dev)
             jpsf = None if psf is None else jb.pack_psf([self.psf_np] * len(members))
             nf = len(free)
@@ -135,26 +139,57 @@ class Scene:
             jac_total += nf * jb.out_pixels
         self.jac = torch.zeros(max(jac_total, 1), dtype=torch.float32, device=dev)
 
-        # model renders on the group window, in chunks of sources of one kind (same plan)
+        # model renders.  The reference evaluates a windowed source of a group on the group's
+        # window and keeps its own window.  A Sersic source is rendered on its own window with the
+        # group's working pixel count in its integration threshold, which gives the same pixels;
+        # an exponential source's threshold sums its samples over the whole group window, so it is
+        # rendered on the group window (in chunks of sources that share one plan).
         self._fwd_parts = []
         self.fwd_chunk = max(1, int(fwd_chunk))
+        bx = by = 0
+        if psf is not None:
+            ky_, kx_ = self.psf_np.shape
+            bx, by = int(math.ceil((1 + kx_) / 2)), int(math.ceil((1 + ky_) / 2))
+        group_numel = float((self.nx + 2 * bx) * (self.ny + 2 * by))
         fwd_total = 0
         for (kind, free), members in self.groups.items():
-            m = min(self.fwd_chunk, len(members))
-            o = N.make_options(profile=kind, psf_mode="full" if psf is not None else "none",
-                               free_mask=sum(1 << sl for sl in _SLOTS_OF[kind]), has_sky=False, **opts_kw)
-            fb = N.StampBatch([(self.nx, self.ny)] * m, None if kpsf is None else [kpsf] * m,
-                              N.scale_geometry(m, self.scale), o, dev)
-            fpsf = None if psf is None else fb.pack_psf([self.psf_np] * m)
-            self._fwd_parts.append(dict(kind=kind, members=members, batch=fb, psf=fpsf, off=fwd_total, m=m))
-            fwd_total += len(members) * self.nx * self.ny
+            fo = N.make_options(profile=kind, psf_mode="full" if psf is not None else "none",
+                                free_mask=sum(1 << sl for sl in _SLOTS_OF[kind]), has_sky=False, **opts_kw)
+            if kind == "sersic":
+                shapes, geoms = [], []
+                for si in members:
+                    (x0, x1), (y0, y1) = self._window(si)
+                    shapes.append((x1 - x0, y1 - y0))
+                    geoms.append(N.scale_geometry(1, self.scale, (self.origin[0] + x0 * self.scale,
+                                                                  self.origin[1] + y0 * self.scale))[0])
+                fb = N.StampBatch(shapes, None if kpsf is None else [kpsf] * len(members), np.array(geoms), fo, dev)
+                fb.set_threshold_numel(group_numel)
+                fpsf = None if psf is None else fb.pack_psf([self.psf_np] * len(members))
+                self._fwd_parts.append(dict(kind=kind, members=members, batch=fb, psf=fpsf, off=fwd_total,
+                                            m=len(members), own=True))
+                fwd_total += int(fb.out_pixels)
+            else:
+                m = min(self.fwd_chunk, len(members))
+                fb = N.StampBatch([(self.nx, self.ny)] * m, None if kpsf is None else [kpsf] * m,
+                                  N.scale_geometry(m, self.scale, self.origin), fo, dev)
+                fpsf = None if psf is None else fb.pack_psf([self.psf_np] * m)
+                self._fwd_parts.append(dict(kind=kind, members=members, batch=fb, psf=fpsf, off=fwd_total, m=m,
+                                            own=False))
+                fwd_total += len(members) * self.nx * self.ny
         self.fwd = torch.zeros(max(fwd_total, 1), dtype=torch.float32, device=dev)
 
         # ---- source descriptors ----------------------------------------------------------------
         desc = (ApSceneSource * len(self.sources))()
         for part in self._fwd_parts:
             for k, si in enumerate(part["members"]):
-                desc[si].fwd_off = part["off"] + k * self.nx * self.ny
+                d = desc[si]
+                if part["own"]:
+                    (x0, x1), (y0, y1) = self._window(si)
+                    d.fwd_off = part["off"] + int(part["batch"].out_offsets[k])
+                    d.fwd_x0, d.fwd_y0, d.fwd_nx = x0, y0, x1 - x0
+                else:
+                    d.fwd_off = part["off"] + k * self.nx * self.ny
+                    d.fwd_x0, d.fwd_y0, d.fwd_nx = 0, 0, self.nx
         for part in self._jac_parts:
             b = part["batch"]
             for k, si in enumerate(part["members"]):
@@ -240,6 +275,10 @@ class Scene:
         V = self.values_matrix(rep)
         for part in self._fwd_parts:
             b, m, mem = part["batch"], part["m"], part["members"]
+            if part["own"]:
+                out = self.fwd[part["off"] : part["off"] + b.out_pixels]
+                b.render(torch.tensor(V[mem]), part["psf"], out=out)
+                continue
             for c0 in range(0, len(mem), m):
                 chunk = mem[c0 : c0 + m]
                 params = np.zeros((m, 8))
@@ -253,23 +292,22 @@ class Scene:
                     out.copy_(tmp[: out.numel()])
         img = torch.empty(self.nx * self.ny, dtype=torch.float32, device=self.device)
         N.check(self.lib.ap_scene_forward(N._ptr(self.desc), N._ptr(self.tile_ptr), N._ptr(self.tile_src),
-                                          N._ptr(self.fwd), self.nx, ctypes.c_float(self.sky), self.nx, self.ny,
-                                          N._ptr(img), N._stream()), "ap_scene_forward")
+                                          N._ptr(self.fwd), ctypes.c_float(self.sky), self.nx, self.ny, N._ptr(img),
+                                          N._stream()), "ap_scene_forward")
         return img
 
-    def jacobian(self, rep: np.ndarray):
-        """Own-window representation-space Jacobians of every source into ``self.jac``."""
+    def jacobian(self, rep: np.ndarray, as_representation: bool = True):
+        """Own-window Jacobians of every source (representation or value space) into ``self.jac``."""
         V = self.values_matrix(rep)
         for part in self._jac_parts:
             b = part["batch"]
-            n = len(part["members"])
             jac = self.jac[part["off"] : part["off"] + part["nf"] * b.out_pixels].view(part["nf"], b.out_pixels)
-            b.jacobian(torch.tensor(V[part["members"]]), part["psf"], as_representation=True, jac=jac)
+            b.jacobian(torch.tensor(V[part["members"]]), part["psf"], as_representation=as_representation, jac=jac)
         return self.jac
 
-    def jacobian_image(self, rep: np.ndarray) -> np.ndarray:
-        """Dense [ny, nx, P] Jacobian (for tests and small scenes)."""
-        self.jacobian(rep)
+    def jacobian_image(self, rep: np.ndarray, as_representation: bool = True) -> np.ndarray:
+        """Dense [ny, nx, P] Jacobian (linked columns summed)."""
+        self.jacobian(rep, as_representation)
         out = np.zeros((self.ny, self.nx, self.P))
         jac = self.jac.cpu().numpy()
         for part in self._jac_parts:

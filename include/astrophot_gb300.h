@@ -115,6 +115,13 @@ int ap_batch_sizes(const ap_batch* batch, int64_t* out_pixels, int64_t* psf_pixe
 /* Per-stamp offsets (host arrays of n_stamps) into the packed output and PSF arrays. */
 int ap_batch_offsets(const ap_batch* batch, int64_t* out_offsets, int64_t* psf_offsets);
 
+/* Pixel count each stamp's adaptive-integration threshold divides by (default: its working
+ * window, as _integrate_reference / sampling_tolerance in the reference, models/sersic_model.py:
+ * 87-89).  A Sersic source of a Group_Model is evaluated by the reference on the group's window
+ * (models/model_object.py:290-296); rendering it on its own window with the group's working
+ * pixel count gives the same pixels inside its window.  numel[n] > 0, host; may follow bind. */
+int ap_batch_set_threshold_numel(ap_batch* batch, const double* numel);
+
 /* Attach caller-owned device workspace and upload the plan's tables into it
  * (synchronous with respect to the host for the table upload). */
 int ap_batch_bind(ap_batch* batch, void* workspace, int64_t workspace_bytes, ap_stream_t stream);
@@ -232,23 +239,22 @@ int ap_render_noalloc(int32_t nx, int32_t ny, int32_t psf_kx, int32_t psf_ky,
  * source's own window, as the reference does); these entry points combine them.  One
  * ap_scene_source per source (device array): */
 typedef struct ap_scene_source {
-  int64_t fwd_off;    /* element offset of the source's model render (group window, row stride
-                         fwd_nx) in the forward buffer */
+  int64_t fwd_off;    /* element offset of the source's model render in the forward buffer; image
+                         pixel (x, y) is at fwd_off + (y - fwd_y0) * fwd_nx + (x - fwd_x0) */
   int64_t jac_off;    /* element offset of its own-window Jacobian (compact slot 0) */
   int64_t jac_stride; /* elements between its compact slots (the batch's output pixels) */
   int32_t x0, y0;     /* own window: first pixel in the image */
   int32_t wx, wy;     /* own window size */
   int32_t n_free;     /* compact (fitted) slots of the source, <= 8 */
   int32_t gidx[8];    /* joint-vector index of each compact slot (linked slots share one) */
-  int32_t reserved;
+  int32_t fwd_x0, fwd_y0, fwd_nx; /* grid of the model render (group window or own window) */
 } ap_scene_source;
 
 /* image = sky + sum of the sources' renders inside their own windows.  tile_ptr / tile_src: for
  * every 32 x 32 image tile (row-major, ceil(nx/32) per row) the sources whose windows touch it
  * (CSR; the order fixes the summation order). */
 int ap_scene_forward(const ap_scene_source* sources, const int32_t* tile_ptr, const int32_t* tile_src,
-                     const float* fwd, int32_t fwd_nx, float sky, int32_t nx, int32_t ny, float* image,
-                     ap_stream_t stream);
+                     const float* fwd, float sky, int32_t nx, int32_t ny, float* image, ap_stream_t stream);
 /* out[ny][nx] = J h (h[P] float64), own windows, same tile lists. */
 int ap_scene_jvp(const ap_scene_source* sources, const int32_t* tile_ptr, const int32_t* tile_src,
                  const float* jac, const double* h, int32_t nx, int32_t ny, float* out, ap_stream_t stream);
