@@ -574,7 +574,23 @@ class _NLLFunction(torch.autograd.Function):
     def forward(ctx, vec, owner, as_representation):
         v = vec.detach().to("cpu", config.ap_dtype)
         (owner.parameters.vector_set_representation if as_representation else owner.parameters.vector_set_values)(v)
-        struct = _Structure(owner, owner._components())
+        ctx.owner, ctx.as_rep = owner, as_representation
+        comps = owner._components()
+        if _needs_scene(owner, comps):
+            scene = _make_scene(owner, comps)
+            rep = scene.representation()
+            model = scene.forward(rep).to(torch.float64)
+            r = model - scene.data.to(torch.float64)
+            wt = scene.weight.to(torch.float64)
+            if scene.mask is not None:
+                keep = scene.mask == 0
+                r = torch.where(keep, r, torch.zeros_like(r))
+                wt = torch.where(keep, wt, torch.zeros_like(wt))
+            g = wt * r
+            ctx.scene, ctx.rep, ctx.g = scene, rep, g
+            return (0.5 * torch.sum(g * r)).to("cpu", vec.dtype)
+        ctx.scene = None
+        struct = _Structure(owner, comps)
         w = owner.window
         batch, psf_d = _plan(owner, struct, w)
         params = torch.tensor(struct.full_params()[None, :])
@@ -588,12 +604,16 @@ class _NLLFunction(torch.autograd.Function):
             r = torch.where(keep, r, torch.zeros_like(r))
             wt = torch.where(keep, wt, torch.zeros_like(wt))
         g = wt * r
-        ctx.owner, ctx.as_rep, ctx.struct = owner, as_representation, struct
+        ctx.struct = struct
         ctx.batch, ctx.psf_d, ctx.params, ctx.g = batch, psf_d, params, g
         return (0.5 * torch.sum(g * r)).to("cpu", vec.dtype)
 
     @staticmethod
     def backward(ctx, grad_out):
+        if ctx.scene is not None:
+            grad = ctx.scene.vjp(ctx.rep, ctx.g.to(torch.float32), as_representation=ctx.as_rep,
+                                 reference_center=bool(ctx.owner.reference_center_gradient))
+            return grad.to(config.ap_dtype) * grad_out.to("cpu", config.ap_dtype), None, None
         batch = ctx.batch
         gc = batch.vjp(ctx.params, ctx.psf_d, ctx.g.to(torch.float32), as_representation=ctx.as_rep,
                        reference_center=bool(ctx.owner.reference_center_gradient))[0].cpu()

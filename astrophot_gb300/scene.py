@@ -31,7 +31,7 @@ import torch
 from . import _native as N
 from .transforms import SLOT_LIMITS, to_rep, to_value
 
-__all__ = ("SceneSource", "Scene", "SceneLM")
+__all__ = ("SceneSource", "Scene", "SceneLM", "SceneRenderFunction", "render")
 
 TILE = 32
 _SLOTS_OF = {"sersic": (0, 1, 2, 3, 4, 5, 6), "exponential": (0, 1, 2, 3, 5, 6)}
@@ -321,6 +321,58 @@ class Scene:
                     out[y0:y1, x0:x1, self.gidx[si][sl]] += col.reshape(y1 - y0, x1 - x0)
         return out
 
+    def _vjp_index(self, part):
+        """For an own-window forward batch: image index of every packed output pixel."""
+        if "vjp_idx" not in part:
+            b = part["batch"]
+            idx = np.empty(b.out_pixels, dtype=np.int64)
+            for k, si in enumerate(part["members"]):
+                (x0, x1), (y0, y1) = self._window(si)
+                yy, xx = np.mgrid[y0:y1, x0:x1]
+                o = int(b.out_offsets[k])
+                idx[o : o + (x1 - x0) * (y1 - y0)] = (yy * self.nx + xx).ravel()
+            part["vjp_idx"] = torch.tensor(idx, device=self.device)
+        return part["vjp_idx"]
+
+    def vjp(self, rep: np.ndarray, grad_image: torch.Tensor, as_representation: bool = True,
+            reference_center: bool = False) -> torch.Tensor:
+        """Adjoint of :meth:`forward`: [P] float64 = sum_pixels grad_image d image / d theta, by
+        ``ap_render_vjp`` of every source's model render (PSF-convolved derivative tiles are
+        recomputed and reduced on the fly, no Jacobian is stored).  ``reference_center`` gives
+        the centre entries the reference's reverse-mode autograd gives under PSF shift."""
+        V = self.values_matrix(rep)
+        g_img = grad_image.to(self.device, torch.float32).reshape(-1).contiguous()
+        out = np.zeros(self.P)
+        for part in self._fwd_parts:
+            b, m, mem = part["batch"], part["m"], part["members"]
+            slots = [sl for sl in range(8) if b.options.free_mask & (1 << sl)]
+            if part["own"]:
+                gp = g_img[self._vjp_index(part)].contiguous()
+                res = b.vjp(torch.tensor(V[mem]), part["psf"], gp, as_representation=as_representation,
+                            reference_center=reference_center).cpu().numpy()
+                rows = list(zip(mem, res))
+            else:
+                rows = []
+                img2 = g_img.view(self.ny, self.nx)
+                for c0 in range(0, len(mem), m):
+                    chunk = mem[c0 : c0 + m]
+                    gp = torch.zeros((m, self.ny, self.nx), dtype=torch.float32, device=self.device)
+                    for k, si in enumerate(chunk):
+                        (x0, x1), (y0, y1) = self._window(si)
+                        gp[k, y0:y1, x0:x1] = img2[y0:y1, x0:x1]
+                    params = np.zeros((m, 8))
+                    params[:, :] = V[chunk[0]]
+                    params[: len(chunk)] = V[chunk]
+                    res = b.vjp(torch.tensor(params), part["psf"], gp.reshape(-1), as_representation=as_representation,
+                                reference_center=reference_center).cpu().numpy()
+                    rows += list(zip(chunk, res[: len(chunk)]))
+            for si, r in rows:
+                for c, sl in enumerate(slots):
+                    gi = self.gidx[si].get(sl)
+                    if gi is not None:
+                        out[gi] += r[c]
+        return torch.tensor(out, dtype=torch.float64)
+
     def hess(self) -> torch.Tensor:
         H = torch.empty((self.P, self.P), dtype=torch.float64, device=self.device)
         N.check(self.lib.ap_scene_hess(N._ptr(self.desc), N._ptr(self.pairs), self.n_pairs, N._ptr(self.jac),
@@ -514,3 +566,24 @@ class SceneLM:
         if not ok.any():
             return self.x.copy()
         return np.array(self.lambda_history)[ok][np.argmin(hist[ok])]
+
+
+class SceneRenderFunction(torch.autograd.Function):
+    """image = scene.forward(rep) with the scene's adjoint as its backward."""
+
+    @staticmethod
+    def forward(ctx, rep, scene, reference_center):
+        ctx.scene, ctx.reference_center = scene, reference_center
+        ctx.save_for_backward(rep)
+        return scene.forward(rep.detach().cpu().numpy())
+
+    @staticmethod
+    def backward(ctx, grad_image):
+        (rep,) = ctx.saved_tensors
+        g = ctx.scene.vjp(rep.detach().cpu().numpy(), grad_image, reference_center=ctx.reference_center)
+        return g.to(rep.device, rep.dtype), None, None
+
+
+def render(scene: Scene, rep: torch.Tensor, reference_center: bool = False) -> torch.Tensor:
+    """Differentiable scene render from a joint representation vector (float64 tensor)."""
+    return SceneRenderFunction.apply(rep, scene, reference_center)

@@ -58,3 +58,15 @@ def load_group(name):
     d["spec"] = json.loads(str(d["spec"]))
     d["message"] = str(d["message"])
     return d
+
+
+def adjoint_case_names():
+    return sorted(os.path.basename(p)[: -len(".npz")] for p in glob.glob(os.path.join(HERE, "adjoint_*.npz")))
+
+
+def load_adjoint(name):
+    z = np.load(os.path.join(HERE, f"{name}.npz"))
+    d = {k: z[k] for k in z.files}
+    d["spec"] = json.loads(str(d["spec"]))
+    return d
+

@@ -448,8 +448,82 @@ def run_group_case(ap, key, case):
     )
 
 
+ADJOINT_CASES = {
+    # negative_log_likelihood().backward() of a Group_Model of three bulge (Sersic) + disk
+    # (exponential) pairs sharing their centre node, each with its own window, on a 256 x 256
+    # crop with a 65 x 65 Moffat PSF (FWHM 3, beta 3.5), locked sky: reverse-mode gradient
+    # (grad) and the forward-mode jacobian() contracted with the residual (grad_fwd)
+    "adjoint_bulge_disk_256": dict(size=256, seed=21, psf=("moffat", 3.5, 3.0, 65)),
+}
+
+ADJOINT_PAIRS = (
+    # centre, window [[x0, x1], [y0, y1]], bulge (q, PA, n, Re, Ie), disk (q, PA, Re, Ie)
+    ((80.3, 92.7), [[20, 150], [30, 160]], (0.8, 0.6, 3.5, 4.0, 2.0), (0.5, 0.7, 14.0, 1.1)),
+    ((170.6, 150.2), [[100, 240], [80, 220]], (0.7, 2.2, 2.4, 6.0, 1.7), (0.35, 2.1, 18.0, 0.9)),
+    ((120.4, 210.9), [[60, 190], [150, 256]], (0.9, 1.3, 4.5, 3.0, 2.3), (0.6, 1.4, 10.0, 1.3)),
+)
+
+
+def perturb_pair(c, b, dsk):
+    cx, cy = c
+    bq, bpa, bn, bre, bie = b
+    dq, dpa, dre, die = dsk
+    return ((cx + 0.7, cy - 0.5), (min(bq * 1.1, 0.95), bpa + 0.08, bn * 0.9, bre * 1.12, bie - 0.08),
+            (min(dq * 1.1, 0.95), dpa - 0.06, dre * 0.9, die + 0.07))
+
+
+def build_bulge_disk(ap, target, pairs, tag, perturb=False):
+    models = []
+    for k, (c, win, b, dsk) in enumerate(pairs):
+        if perturb:
+            c, b, dsk = perturb_pair(c, b, dsk)
+        cx, cy = c
+        bq, bpa, bn, bre, bie = b
+        dq, dpa, dre, die = dsk
+        bulge = ap.models.AstroPhot_Model(name=f"{tag} bulge {k}", model_type="sersic galaxy model", target=target,
+                                          window=win, parameters={"center": [cx, cy], "q": bq, "PA": bpa, "n": bn,
+                                                                  "Re": bre, "Ie": bie})
+        disk = ap.models.AstroPhot_Model(name=f"{tag} disk {k}", model_type="exponential galaxy model",
+                                         target=target, window=win,
+                                         parameters={"q": dq, "PA": dpa, "Re": dre, "Ie": die})
+        disk.parameters["center"].value = bulge.parameters["center"]
+        models += [bulge, disk]
+    sky = ap.models.AstroPhot_Model(name=f"{tag} sky", model_type="flat sky model", target=target,
+                                    parameters={"F": {"value": 0.0, "locked": True}})
+    sky.initialize()
+    return ap.models.AstroPhot_Model(name=f"{tag} group", model_type="group model", target=target,
+                                     models=models + [sky], psf_mode="full")
+
+
+def run_adjoint_case(ap, key, case):
+    N = case["size"]
+    psf = psf_array(case["psf"])
+    target = ap.image.Target_Image(data=np.zeros((N, N)), pixelscale=1.0, psf=psf)
+    truth_img = build_bulge_disk(ap, target, ADJOINT_PAIRS, f"{key} truth")().data.detach().cpu().numpy()
+    data, weight = synthetic.add_noise(truth_img, case["seed"])
+    target = ap.image.Target_Image(data=data, pixelscale=1.0, psf=psf, variance=1.0 / weight)
+    group = build_bulge_disk(ap, target, ADJOINT_PAIRS, key, perturb=True)
+    names = [str(n) for n in group.parameters.vector_names()]
+    rep = group.parameters.vector_representation().detach().clone().requires_grad_(True)
+    nll = group.negative_log_likelihood(parameters=rep, as_representation=True)
+    nll.backward()
+    rep0 = rep.detach().clone()
+    J = group.jacobian(parameters=rep0, as_representation=True).data.detach().cpu().numpy().reshape(-1, len(rep0))
+    m = group().data.detach().cpu().numpy().reshape(-1)
+    grad_fwd = J.T @ (weight.reshape(-1) * (m - data.reshape(-1)))
+    init = [perturb_pair(c, b, dsk) for c, _, b, dsk in ADJOINT_PAIRS]
+    return dict(psf=psf, data=data, weight=weight, names=np.array(names), rep=rep0.numpy(), nll=np.array(nll.item()),
+                grad=rep.grad.detach().numpy(), grad_fwd=grad_fwd, model=m.reshape(N, N), spec=json.dumps(case),
+                centers=np.array([i[0] for i in init]), bulges=np.array([i[1] for i in init]),
+                disks=np.array([i[2] for i in init]), windows=np.array([w for _, w, _, _ in ADJOINT_PAIRS]))
+
+
 def main():
     ap = import_reference()
+    for key, case in ADJOINT_CASES.items():
+        out = run_adjoint_case(ap, key, case)
+        np.savez_compressed(os.path.join(HERE, f"{key}.npz"), **out)
+        print("adjoint", key, out["nll"], out["grad"])
     for key, case in GROUP_CASES.items():
         out = run_group_case(ap, key, case)
         np.savez_compressed(os.path.join(HERE, f"{key}.npz"), **out)

@@ -295,3 +295,57 @@ def test_group_lm_trajectory_matches_reference(name):
     assert lm.message == d["message"]
     assert np.allclose(lm.loss_history, d["loss_history"], rtol=1e-10, atol=0)
     assert np.allclose(lm.res(), d["res"], rtol=1e-8, atol=1e-10)
+
+
+# ---- adjoint of a bulge + disk group (shared centres, windows, 65 x 65 PSF) -----------------
+
+
+def adjoint_problem(d):
+    comps, links = [], {}
+    for k, (c, w, b, dk) in enumerate(zip(d["centers"], d["windows"], d["bulges"], d["disks"])):
+        win = tuple(tuple(int(v) for v in r) for r in w)
+        q, PA, n, Re, Ie = b
+        comps.append(Component("sersic", {"center": list(c), "q": q, "PA": PA, "n": n, "Re": Re, "Ie": Ie},
+                               psf_mode="full", window=win))
+        q, PA, Re, Ie = dk
+        comps.append(Component("exponential", {"center": list(c), "q": q, "PA": PA, "Re": Re, "Ie": Ie},
+                               psf_mode="full", window=win))
+        links[(2 * k + 1, "center")] = (2 * k, "center")
+    comps.append(Component("flat_sky", {"F": 0.0}, locked=("F",)))
+    N = d["spec"]["size"]
+    return GroupProblem(comps, Window.from_scale(N, N), PSF(d["psf"]), d["data"], d["weight"], links=links)
+
+
+@pytest.mark.parametrize("name", cases.adjoint_case_names())
+def test_group_adjoint_golden_pins_the_oracle(name):
+    """nll of the group, the own-window Jacobian contracted with the residual (grad_fwd) and the
+    FP64 central differences (step 1e-6 relative) of the group-window forward, which the
+    reference's reverse-mode gradient equals away from the centres."""
+    d = cases.load_adjoint(name)
+    prob = adjoint_problem(d)
+    rep = prob.representation()
+    assert np.allclose(rep, d["rep"], rtol=0, atol=1e-12)
+    m = prob.forward(rep)
+    assert np.max(np.abs(m - d["model"].reshape(-1))) <= 1e-12 * np.max(d["model"])
+    W, Y = prob.W.reshape(-1), prob.Y.reshape(-1)
+    nll = 0.5 * float(np.sum(W * (m - Y) ** 2))
+    assert nll == pytest.approx(float(d["nll"]), rel=1e-12)
+    J = prob.jacobian(rep)
+    g = J.T @ (W * (prob.forward(rep) - Y))
+    scale = np.max(np.abs(d["grad_fwd"]))
+    assert np.max(np.abs(g - d["grad_fwd"])) <= 1e-9 * scale
+    # finite differences on two entries (a bulge axis ratio, a centre)
+    names = list(d["names"])
+    for k in (2, 0):
+        h = 1e-6 * max(1.0, abs(rep[k]))
+        rp, rm = rep.copy(), rep.copy()
+        rp[k] += h
+        rm[k] -= h
+        fp = 0.5 * float(np.sum(W * (prob.forward(rp) - Y) ** 2))
+        fm = 0.5 * float(np.sum(W * (prob.forward(rm) - Y) ** 2))
+        fd = (fp - fm) / (2 * h)
+        if names[k].startswith("center"):
+            # the reverse-mode centre adds the sampling-coordinate path: not the derivative
+            assert abs(fd - d["grad"][k]) > 1e-3 * abs(fd)
+        else:
+            assert abs(fd - d["grad"][k]) <= 1e-5 * scale, (k, names[k], fd, d["grad"][k])
