@@ -17,7 +17,7 @@ constexpr int64_t kAlign = 256;
 int64_t align_up(int64_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
 
 struct Layout {
-  int64_t stamps, evals, work_tiles, out_tiles, tables, work, aux, spsf, queue, recheck, wlist,
+  int64_t stamps, evals, work_tiles, out_tiles, tables, work, aux, spsf, queue, recheck, amb, wlist,
       olist, slist, counters,
       work_ctr, mean_acc, tile_acc, acc, total;
 };
@@ -353,6 +353,7 @@ int ap_batch_create(ap_batch** out, int32_t n, const int32_t* nx, const int32_t*
   L.spsf = take(sizeof(float) * std::max<int64_t>(b->spsf_total, 1));
   L.queue = take(sizeof(int64_t) * 2 * b->work_pixels);
   L.recheck = take(sizeof(int64_t) * 2 * b->work_pixels);
+  L.amb = take(sizeof(int64_t) * b->work_pixels);
   L.wlist = take(sizeof(int64_t) * 2 * (int64_t)b->work_tiles.size());
   L.olist = take(sizeof(int64_t) * 2 * (int64_t)b->out_tiles.size());
   L.slist = take(sizeof(int32_t) * 2 * (int64_t)n);
@@ -446,6 +447,8 @@ int ap_batch_bind(ap_batch* b, void* workspace, int64_t bytes, ap_stream_t strea
   A.spsf = (float*)(ws + L.spsf);
   A.queue = (int64_t*)(ws + L.queue);
   A.recheck = (int64_t*)(ws + L.recheck);
+  A.amb = (int64_t*)(ws + L.amb);
+  A.amb_cap = b->work_pixels;
   A.wlist = (int64_t*)(ws + L.wlist);
   A.olist = (int64_t*)(ws + L.olist);
   A.slist = (int32_t*)(ws + L.slist);

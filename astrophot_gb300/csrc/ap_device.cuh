@@ -165,11 +165,13 @@ struct BatchArgs {
   float* spsf;                // kernels
   int64_t* queue;             // [2 * work_pixels] pixels to integrate
   int64_t* recheck;           // [2 * work_pixels] pixels whose selection needs float64
+  int64_t* amb;               // [amb_cap] level-1 pixels whose split decision needs float64
+  int64_t amb_cap;            // 0: decided inline
   uint32_t* counters;         // [0] queue len, [1] queue head, [2] fp64 re-decisions (select),
                               // [3] errors, [4] active, [5] recheck len, [6] fp64 (integrate),
                               // [7] active working tiles, [8] active output tiles,
                               // [9] active (stamp, slot) pairs, [10] level-2 integration queue,
-                              // [11] convolve-pass tile head
+                              // [11] convolve-pass tile head, [12] level-1 float64 decisions
   int64_t* wlist;             // [2 * n_work_tiles] active working tiles: slot<<62 | stamp<<32 | tile
   int64_t* olist;             // [2 * n_out_tiles]  active output tiles, same packing
   int32_t* slist;             // [2 * n_stamps]     active (stamp * 2 + slot)

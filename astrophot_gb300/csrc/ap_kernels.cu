@@ -70,6 +70,7 @@ __global__ void k_eval_setup(BatchArgs b, const double* params, int64_t stamp_st
     b.counters[9] = 0;  // active (stamp, slot) pairs
     b.counters[10] = 0; // level-2 integration queue length
     b.counters[11] = 0; // convolve-pass tile head
+    b.counters[12] = 0; // level-1 float64 decisions
   }
   if (t >= b.n_stamps * 2) return;
   const int s = t >> 1, slot = t & 1;
@@ -629,7 +630,7 @@ __device__ __forceinline__ void write_deep(const BatchArgs& b, const StampDev& s
 // integral and its refinement decision.  Pixels that stop here are written; the others go
 // to the level-2 queue (b.recheck, emptied by k_recheck before this kernel runs).
 template <int QC>
-__device__ __forceinline__ void level1_pixel(const BatchArgs& b, int64_t ent, bool& push,
+__device__ __forceinline__ void level1_pixel(const BatchArgs& b, int64_t ent, bool& push, bool& amb,
                                              int& n64) {
   const int slot = (int)(ent >> 62);
   const int s = (int)((ent >> 32) & 0x3fffffff);
@@ -648,10 +649,10 @@ __device__ __forceinline__ void level1_pixel(const BatchArgs& b, int64_t ent, bo
     const float diff = fabsf(r.res - r.ref);
     const float band = 1.5f * r.errb + 4.f * kEps * thr;
     split = diff > thr + band;
-    if (!split && diff >= thr - band) {
-      ++n64;
-      split = refine64(b, st, e, i, j, -1, e.thresh64);
-    }
+    // inside the FP32 error band: the float64 decision is taken by k_level1_amb, densely
+    // (one pixel per lane), after this pixel's FP32 value is written; a split there
+    // overwrites it
+    if (!split && diff >= thr - band) amb = true;
   }
   if (split)
     push = true;
@@ -659,39 +660,79 @@ __device__ __forceinline__ void level1_pixel(const BatchArgs& b, int64_t ent, bo
     write_deep(b, st, slot, p, r.res, r.g, jac);
 }
 
+// warp-aggregated append of flagged entries to a list (counter, capacity); returns false for
+// the lanes whose entry did not fit
+__device__ __forceinline__ bool warp_append(bool flag, int64_t ent, int64_t* list, uint32_t* counter,
+                                            int64_t cap) {
+  const int lane = threadIdx.x & 31;
+  const unsigned mask = __ballot_sync(0xffffffffu, flag);
+  if (!mask) return true;
+  const int leader = __ffs(mask) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(counter, (unsigned)__popc(mask));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (!flag) return true;
+  const int64_t k = (int64_t)base + __popc(mask & ((1u << lane) - 1u));
+  if (k >= cap) return false;
+  list[k] = ent;
+  return true;
+}
+
 __global__ void __launch_bounds__(256, 3) k_level1(BatchArgs b) {
   const uint32_t n = min((uint32_t)b.counters[0], (uint32_t)(2 * b.work_pixels));
   const int Q = b.tables->quad_level;
-  const int lane = threadIdx.x & 31;
   int n64 = 0;
-  uint32_t pushed = 0;
   for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
     const uint32_t idx = base + threadIdx.x;
-    bool push = false;
+    bool push = false, amb = false;
     int64_t ent = 0;
     if (idx < n) {
       ent = b.queue[idx];
       if (Q == 3)
-        level1_pixel<3>(b, ent, push, n64);
+        level1_pixel<3>(b, ent, push, amb, n64);
       else
-        level1_pixel<0>(b, ent, push, n64);
+        level1_pixel<0>(b, ent, push, amb, n64);
     }
-    const unsigned mask = __ballot_sync(0xffffffffu, push);
-    if (mask) {
-      const int leader = __ffs(mask) - 1;
-      uint32_t qb = 0;
-      if (lane == leader) qb = atomicAdd(&b.counters[10], (unsigned)__popc(mask));
-      qb = __shfl_sync(0xffffffffu, qb, leader);
-      if (push) b.recheck[qb + __popc(mask & ((1u << lane) - 1u))] = ent;
-      pushed += __popc(mask);
+    if (!warp_append(amb, ent, b.amb, &b.counters[12], b.amb_cap)) {
+      // the dense list is full: decide here
+      const int slot = (int)(ent >> 62);
+      const int s = (int)((ent >> 32) & 0x3fffffff);
+      const int64_t p = ent & 0xffffffffll;
+      const StampDev& st = b.stamps[s];
+      ++n64;
+      push = refine64(b, st, b.evals[s * 2 + slot], (int)(p % st.wnx), (int)(p / st.wnx), -1,
+                      b.evals[s * 2 + slot].thresh64);
     }
+    warp_append(push, ent, b.recheck, &b.counters[10], (int64_t)2 * b.work_pixels);
   }
   n64 = __reduce_add_sync(0xffffffffu, n64);
-  if (lane == 0 && n64) atomicAdd(&b.counters[6], (unsigned)n64);
+  if ((threadIdx.x & 31) == 0 && n64) atomicAdd(&b.counters[6], (unsigned)n64);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     const int Qn = b.tables->quad_level;
     atomicAdd(b.work_ctr + 1, (unsigned long long)n * (unsigned long long)(Qn * Qn));
   }
+}
+
+// float64 split decisions of the level-1 pixels inside the FP32 error band, one per lane
+// (all lanes of a warp busy: the FP64 pipe is narrow); splits join the level-2 queue.
+__global__ void __launch_bounds__(256) k_level1_amb(BatchArgs b) {
+  const int64_t n = min((int64_t)b.counters[12], b.amb_cap);
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t idx = base + threadIdx.x;
+    bool push = false;
+    int64_t ent = 0;
+    if (idx < n) {
+      ent = b.amb[idx];
+      const int slot = (int)(ent >> 62);
+      const int s = (int)((ent >> 32) & 0x3fffffff);
+      const int64_t p = ent & 0xffffffffll;
+      const StampDev& st = b.stamps[s];
+      const EvalDev& e = b.evals[s * 2 + slot];
+      push = refine64(b, st, e, (int)(p % st.wnx), (int)(p / st.wnx), -1, e.thresh64);
+    }
+    warp_append(push, ent, b.recheck, &b.counters[10], (int64_t)2 * b.work_pixels);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0) atomicAdd(&b.counters[6], (unsigned)n);
 }
 
 // Levels 2 and 3 of grid_integrate for a pixel that level 1 split: one warp per pixel,
@@ -763,7 +804,7 @@ __device__ void level23_pixel(const BatchArgs& b, int slot, int s, int64_t p, in
   if (lane == 0) write_deep(b, st, slot, p, out_v, out_g, JAC);
 }
 
-__global__ void __launch_bounds__(256) k_integrate(BatchArgs b) {
+__global__ void __launch_bounds__(256, 3) k_integrate(BatchArgs b) {
   const int lane = threadIdx.x & 31;
   constexpr uint32_t kChunk = 2;  // queue entries grabbed per atomic
   const uint32_t n = min((uint32_t)b.counters[10], (uint32_t)(2 * b.work_pixels));
@@ -1259,6 +1300,7 @@ cudaError_t launch_render_pass(const BatchArgs& b, const ConvIO& io, size_t conv
     E(t);
     t = B(KC_INTEGRATE);
     k_level1<<<nsm * 8, 256, 0, s>>>(b);
+    if (b.amb_cap > 0) k_level1_amb<<<nsm * 4, 256, 0, s>>>(b);
     k_integrate<<<nsm * 8, 256, 0, s>>>(b);
     E(t);
   }

@@ -302,6 +302,8 @@ extern "C" int ap_render_noalloc(int32_t nx, int32_t ny, int32_t psf_kx, int32_t
   A.spsf = (float*)(ws + o_spsf);
   A.queue = (int64_t*)(ws + o_queue);
   A.recheck = (int64_t*)(ws + o_recheck);
+  A.amb = nullptr;  // level-1 float64 decisions inline (no dense list in the fixed scratch)
+  A.amb_cap = 0;
   A.wlist = (int64_t*)(ws + o_wlist);
   A.olist = (int64_t*)(ws + o_olist);
   A.slist = (int32_t*)(ws + o_slist);
