@@ -191,6 +191,21 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def aggregate_ranks(dev_ms, e2e_ms, converged, total, device):
+    """Max of the per-rank times, sum of the per-rank fit counts (independent stamps per rank:
+    weak scaling, no data-path collective; this is the only cross-rank step)."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return dev_ms, e2e_ms, converged, total
+    t = torch.tensor([dev_ms, e2e_ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    c = torch.tensor([converged, total], dtype=torch.float64, device=device)
+    dist.all_reduce(c)
+    return float(t[0]), float(t[1]), int(c[0]), int(c[1])
+
+
 # ----------------------------------------------------------------------------------------
 # GPU side
 # ----------------------------------------------------------------------------------------
@@ -361,15 +376,7 @@ def run_gpu_cutouts(args):
     e2e_wall_ms = (time.perf_counter() - t0) * 1e3 / args.steps
 
     # max over ranks
-    if world > 1:
-        t = torch.tensor([dev_ms, e2e_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dev_ms, e2e_ms = t.tolist()
-        c = torch.tensor([converged, S], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(c)
-        converged_all, total_all = c.tolist()
-    else:
-        converged_all, total_all = converged, S
+    dev_ms, e2e_ms, converged_all, total_all = aggregate_ranks(dev_ms, e2e_ms, converged, S, dev)
 
     # ---- roofline of the dominant kernel (live CUDA-event times over the timed region) ----
     dominant = max(ktimes, key=lambda k: ktimes[k][0])
@@ -665,15 +672,7 @@ def run_gpu_learned(args):
     e2e_ms = e0.elapsed_time(e1) / args.steps
     e2e_wall_ms = (time.perf_counter() - t0) * 1e3 / args.steps
 
-    if world > 1:
-        t = torch.tensor([dev_ms, e2e_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dev_ms, e2e_ms = t.tolist()
-        c = torch.tensor([converged, S], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(c)
-        converged_all, total_all = c.tolist()
-    else:
-        converged_all, total_all = converged, S
+    dev_ms, e2e_ms, converged_all, total_all = aggregate_ranks(dev_ms, e2e_ms, converged, S, dev)
 
     fp32_peak = N.fma_probe_tflops()
     conv_ms, conv_n = ktimes["conv"]
