@@ -106,6 +106,8 @@ EXPORTS = [
     ("ap_render", [_P, _P, _P, _P, _P]),
     ("ap_jacobian", [_P, _P, _P, _P, _P, _I32, _P]),
     ("ap_render_vjp", [_P, _P, _P, _P, _I32, _P, _P]),
+    ("ap_batch_autotune", [_P, _P, _P, _I32, _PI32, _PD, _P]),
+    ("ap_batch_set_grid", [_P, _PI32]),
     ("ap_batch_psf_stride", [_P, _PI64]),
     ("ap_psf_shift", [_P, _P, _P, _P, _P, _P]),
     ("ap_chi2", [_P, _P, _P, _P, _P, _P, _P]),
@@ -129,6 +131,7 @@ EXPORTS = [
     ("ap_dense_solve_workspace_bytes", [_I32]),
     ("ap_dense_damped_solve", [_I32, _P, _P, ctypes.c_double, _P, _P, ctypes.c_size_t, _P, _P]),
     ("ap_cnn_param_count", []),
+    ("ap_cnn_autotune", [_I32, _PI32]),
     ("ap_cnn_workspace_bytes", [_I64]),
     ("ap_cnn_layer_offsets", [_PI64, _PI64, _PI32]),
     ("ap_cnn_to_bf16", [_P, _P, _P]),
@@ -386,6 +389,21 @@ class StampBatch:
             out = torch.empty(self.out_pixels, dtype=torch.float32, device=self.device)
         check(self.lib.ap_render(self.handle, _ptr(params), _ptr(psf), _ptr(out), _stream()), "ap_render")
         return out
+
+    GRID_KNOBS = ("sample", "integrate", "conv", "psf")
+
+    def autotune(self, params: torch.Tensor, psf: Optional[torch.Tensor], jacobian: bool = True):
+        """Pick the persistent-grid sizes of the render pass by timing it (ap_batch_autotune)."""
+        params = params.to(self.device, torch.float64).contiguous()
+        chosen = (ctypes.c_int32 * 4)()
+        ms = ctypes.c_double()
+        check(self.lib.ap_batch_autotune(self.handle, _ptr(params), _ptr(psf), 1 if jacobian else 0, chosen,
+                                         ctypes.byref(ms), _stream()), "ap_batch_autotune")
+        return {"blocks_per_sm": dict(zip(self.GRID_KNOBS, list(chosen))), "render_pass_ms": ms.value}
+
+    def set_grid(self, blocks_per_sm):
+        arr = (ctypes.c_int32 * 4)(*[int(blocks_per_sm[k]) for k in self.GRID_KNOBS])
+        check(self.lib.ap_batch_set_grid(self.handle, arr), "ap_batch_set_grid")
 
     def set_threshold_numel(self, numel):
         """Pixel count of each stamp's integration threshold (see ap_batch_set_threshold_numel)."""

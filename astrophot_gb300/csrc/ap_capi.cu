@@ -520,6 +520,84 @@ int ap_render_vjp(ap_batch* b, const double* params, const float* psf, const flo
   return check_cuda(launch_gather_vjp(b->args, grad_params, s));
 }
 
+int ap_batch_autotune(ap_batch* b, const double* params, const float* psf, int32_t jacobian, int32_t* chosen,
+                      double* best_ms, ap_stream_t stream) {
+  if (!b || !params || !chosen) return AP_ERR_ARG;
+  if (!b->bound) return AP_ERR_NOT_BOUND;
+  if (b->opt.psf_mode != AP_PSF_NONE && !psf) return AP_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return AP_ERR_ARG;
+  const int32_t ops = jacobian ? (OP_FWD | OP_JAC) : OP_FWD;
+  // candidates (blocks per SM) of each persistent grid, tuned one knob at a time
+  static const int cand[GK_COUNT][5] = {{4, 8, 16, 0, 0}, {3, 6, 8, 12, 0}, {4, 8, 12, 16, 24}, {4, 8, 16, 0, 0}};
+  const int defaults[GK_COUNT] = {8, 8, 16, 8};
+  for (int k = 0; k < GK_COUNT; ++k) b->args.grid_mult[k] = defaults[k];
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess) return check_cuda(cudaGetLastError());
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return check_cuda(cudaGetLastError());
+  }
+  ConvIO io{};
+  io.psf = psf;
+  auto run = [&]() -> int {
+    int rc = check_cuda(launch_eval_setup(b->args, params, NPARAM, 0, nullptr, ops, s));
+    if (rc) return rc;
+    return check_cuda(launch_render_pass(b->args, io, b->conv_smem, false, s, nullptr));
+  };
+  auto time_it = [&](double& ms) -> int {
+    int rc = run();  // warm
+    if (rc) return rc;
+    float best = 1e30f;
+    for (int rep = 0; rep < 3; ++rep) {
+      cudaEventRecord(e0, s);
+      rc = run();
+      if (rc) return rc;
+      cudaEventRecord(e1, s);
+      rc = check_cuda(cudaEventSynchronize(e1));
+      if (rc) return rc;
+      float t = 0.f;
+      cudaEventElapsedTime(&t, e0, e1);
+      best = t < best ? t : best;
+    }
+    ms = best;
+    return AP_OK;
+  };
+  int rc = AP_OK;
+  double ms_best = 0.0;
+  rc = time_it(ms_best);
+  for (int k = 0; k < GK_COUNT && !rc; ++k) {
+    if (k == GK_PSF && b->opt.psf_mode == AP_PSF_NONE) continue;
+    if (k == GK_INTEGRATE && b->opt.integrate_mode != AP_INTEGRATE_THRESHOLD) continue;
+    int best = b->args.grid_mult[k];
+    for (int c = 0; c < 5 && cand[k][c] > 0 && !rc; ++c) {
+      if (cand[k][c] == best) continue;
+      b->args.grid_mult[k] = cand[k][c];
+      double ms = 0.0;
+      rc = time_it(ms);
+      if (!rc && ms < ms_best) {
+        ms_best = ms;
+        best = cand[k][c];
+      }
+    }
+    b->args.grid_mult[k] = best;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  for (int k = 0; k < GK_COUNT; ++k) chosen[k] = b->args.grid_mult[k];
+  if (best_ms) *best_ms = ms_best;
+  return rc;
+}
+
+int ap_batch_set_grid(ap_batch* b, const int32_t* blocks_per_sm) {
+  if (!b || !blocks_per_sm) return AP_ERR_ARG;
+  for (int k = 0; k < GK_COUNT; ++k)
+    if (blocks_per_sm[k] < 1 || blocks_per_sm[k] > 64) return AP_ERR_ARG;
+  for (int k = 0; k < GK_COUNT; ++k) b->args.grid_mult[k] = blocks_per_sm[k];
+  return AP_OK;
+}
+
 int ap_psf_shift(ap_batch* b, const double* params, const float* psf, float* out, float* d_out,
                  ap_stream_t stream) {
   if (!b || !params || !psf || !out) return AP_ERR_ARG;

@@ -19,6 +19,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <map>
+#include <mutex>
+#include <tuple>
+
 #include "ap_internal.h"
 
 using apgb::record_cuda;
@@ -228,6 +232,9 @@ __global__ void __launch_bounds__(WM* WN * 32) k_gemm(const bf16* __restrict__ A
 }
 
 int g_num_sms = 0;
+bool g_gemm_tune = false;
+std::mutex g_tune_mutex;
+std::map<std::tuple<int, int, int, int, int>, int> g_tuned;  // (A_T, B_T, R, S, T) -> tile shape
 
 template <bool A_T, bool B_T>
 cudaError_t gemm(const bf16* A, int lda, const bf16* B, int ldb, float* C, int ldc, int R, int S, int T,
@@ -261,9 +268,54 @@ cudaError_t gemm(const bf16* A, int lda, const bf16* B, int ldb, float* C, int l
     kern<<<dim3(gx, gy, split), threads, 0, st>>>(A, lda, B, ldb, C, ldc, R, S, T, t_split, split > 1 ? 1 : 0);
     return cudaGetLastError();
   };
-  if (S >= 128) return run(k_gemm<128, 128, 2, 4, A_T, B_T>, 128, 128, 256);
-  if (S >= 64) return run(k_gemm<128, 64, 4, 2, A_T, B_T>, 128, 64, 256);
-  return run(k_gemm<128, 32, 4, 1, A_T, B_T>, 128, 32, 128);
+  auto run_cfg = [&](int cfg) {
+    if (cfg == 0) return run(k_gemm<128, 128, 2, 4, A_T, B_T>, 128, 128, 256);
+    if (cfg == 1) return run(k_gemm<128, 64, 4, 2, A_T, B_T>, 128, 64, 256);
+    return run(k_gemm<128, 32, 4, 1, A_T, B_T>, 128, 32, 128);
+  };
+  const int heuristic = S >= 128 ? 0 : (S >= 64 ? 1 : 2);
+  if (!g_gemm_tune) return run_cfg(heuristic);
+  // in-project autotuner: the first call of each (layout, shape) times the three tile shapes
+  // (outside stream capture) and keeps the fastest for the later calls
+  const auto key = std::make_tuple((int)A_T, (int)B_T, R, S, T);
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    auto it = g_tuned.find(key);
+    if (it != g_tuned.end()) return run_cfg(it->second);
+  }
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return run_cfg(heuristic);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int best = heuristic;
+  float best_ms = 1e30f;
+  cudaError_t err = cudaSuccess;
+  for (int cfg = 0; cfg < 3 && err == cudaSuccess; ++cfg) {
+    err = run_cfg(cfg);  // warm
+    float ms_min = 1e30f;
+    for (int rep = 0; rep < 2 && err == cudaSuccess; ++rep) {
+      cudaEventRecord(e0, st);
+      err = run_cfg(cfg);
+      cudaEventRecord(e1, st);
+      if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      ms_min = ms < ms_min ? ms : ms_min;
+    }
+    if (ms_min < best_ms) {
+      best_ms = ms_min;
+      best = cfg;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (err != cudaSuccess) return err;
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    g_tuned[key] = best;
+  }
+  return run_cfg(best);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -640,6 +692,14 @@ cudaError_t backward(const bf16* wb, const float* dout, float* grads, int64_t B,
 extern "C" {
 
 int64_t ap_cnn_param_count(void) { return kParamCount; }
+
+int ap_cnn_autotune(int32_t enable, int32_t* tuned_shapes) {
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  g_gemm_tune = enable != 0;
+  if (enable < 0) g_tuned.clear();
+  if (tuned_shapes) *tuned_shapes = (int32_t)g_tuned.size();
+  return AP_OK;
+}
 
 size_t ap_cnn_workspace_bytes(int64_t batch) {
   if (batch <= 0) return 0;

@@ -140,7 +140,12 @@ struct EvalF {
 };
 
 // everything the kernels need, passed by value
+// persistent-grid sizes of the render pass, in blocks per SM (set by the in-project
+// autotuner, ap_batch_autotune)
+enum GridKnob { GK_SAMPLE = 0, GK_INTEGRATE = 1, GK_CONV = 2, GK_PSF = 3, GK_COUNT = 4 };
+
 struct BatchArgs {
+  int32_t grid_mult[GK_COUNT];  // blocks per SM of sample/select, level 1-3, convolve, PSF shift
   int32_t n_stamps;
   int32_t kind;         // AP_PROFILE_*
   int32_t sampling;     // AP_SAMPLING_*

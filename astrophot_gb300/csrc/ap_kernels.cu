@@ -1280,32 +1280,34 @@ cudaError_t launch_render_pass(const BatchArgs& b, const ConvIO& io, size_t conv
   auto grid = [&](int64_t upper, int per_sm) {
     return (unsigned)std::max<int64_t>(1, std::min<int64_t>(upper, (int64_t)nsm * per_sm));
   };
+  auto knob = [&](int k, int dflt) { return b.grid_mult[k] > 0 ? b.grid_mult[k] : dflt; };
   int t = B(KC_SETUP);
   k_build_lists<<<(b.n_stamps * 2 + 127) / 128, 128, 0, s>>>(b);
   E(t);
   if (b.psf_mode != AP_PSF_NONE) {
     t = B(KC_PSF);
-    k_psf_shift<<<grid(2 * (int64_t)b.n_stamps, 8), 256, 0, s>>>(b, io.psf);
+    k_psf_shift<<<grid(2 * (int64_t)b.n_stamps, knob(GK_PSF, 8)), 256, 0, s>>>(b, io.psf);
     E(t);
   }
   t = B(KC_SAMPLE);
-  k_sample<<<grid(2 * (int64_t)b.n_work_tiles, 8), kTile * kTile, 0, s>>>(b);
+  k_sample<<<grid(2 * (int64_t)b.n_work_tiles, knob(GK_SAMPLE, 8)), kTile * kTile, 0, s>>>(b);
   if (b.kind == AP_PROFILE_EXPONENTIAL && b.integrate == AP_INTEGRATE_THRESHOLD)
     k_exp_threshold<<<(b.n_stamps * 2 + 127) / 128, 128, 0, s>>>(b);
   E(t);
   if (b.integrate == AP_INTEGRATE_THRESHOLD) {
     t = B(KC_SELECT);
-    k_select<<<grid(2 * (int64_t)b.n_work_tiles, 8), kTile * kTile, 0, s>>>(b);
+    k_select<<<grid(2 * (int64_t)b.n_work_tiles, knob(GK_SAMPLE, 8)), kTile * kTile, 0, s>>>(b);
     k_recheck<<<nsm * 4, 256, 0, s>>>(b);
     E(t);
     t = B(KC_INTEGRATE);
-    k_level1<<<nsm * 8, 256, 0, s>>>(b);
+    const int gi = nsm * knob(GK_INTEGRATE, 8);
+    k_level1<<<gi, 256, 0, s>>>(b);
     if (b.amb_cap > 0) k_level1_amb<<<nsm * 4, 256, 0, s>>>(b);
-    k_integrate<<<nsm * 8, 256, 0, s>>>(b);
+    k_integrate<<<gi, 256, 0, s>>>(b);
     E(t);
   }
   t = B(KC_CONV);
-  const dim3 cgrid(grid(2 * (int64_t)b.n_out_tiles, 16));
+  const dim3 cgrid(grid(2 * (int64_t)b.n_out_tiles, knob(GK_CONV, 16)));
   switch (b.n_free) {
     case 0: k_conv<0><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
     case 1: k_conv<1><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;

@@ -271,7 +271,7 @@ extern "C" int ap_render_noalloc(int32_t nx, int32_t ny, int32_t psf_kx, int32_t
     return AP_ERR_CUDA;
   if (conv_smem > 48 * 1024 && set_conv_smem(200 * 1024) != cudaSuccess) return AP_ERR_CUDA;
 
-  BatchArgs A;
+  BatchArgs A{};
   std::memset(&A, 0, sizeof(A));
   A.n_stamps = 1;
   A.kind = options->profile;

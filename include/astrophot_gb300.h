@@ -156,6 +156,15 @@ int ap_jacobian(ap_batch* batch, const double* params, const float* psf, float* 
 int ap_render_vjp(ap_batch* batch, const double* params, const float* psf, const float* grad_model,
                   int32_t flags, double* grad_params, ap_stream_t stream);
 
+/* In-project autotuner of the render pass: times the full render pass (forward, or with the
+ * Jacobian when jacobian != 0) at params[n][8] for candidate persistent-grid sizes of each
+ * kernel group (blocks per SM of sample/select, integration, convolution, PSF shift), one group
+ * at a time, keeps the fastest and returns them in chosen[4] (best_ms: the pass time).  Not
+ * inside a stream capture; synchronises the stream.  ap_batch_set_grid sets them directly. */
+int ap_batch_autotune(ap_batch* batch, const double* params, const float* psf, int32_t jacobian,
+                      int32_t* chosen, double* best_ms, ap_stream_t stream);
+int ap_batch_set_grid(ap_batch* batch, const int32_t* blocks_per_sm);
+
 /* Shifted, renormalised PSF of every stamp for value-space params (device):
  * out[n][(ky+2)*(kx+2)] packed with stride max_kp2 = (max ky + 2) * (max kx + 2)
  * (see ap_batch_psf_stride).  d_out (optional, may be NULL) receives d/d shift_x and
@@ -294,6 +303,10 @@ int ap_dense_damped_solve(int32_t n, const double* H, const double* g, double L,
  * bf16 mirror (ap_cnn_to_bf16).  Batches must be multiples of 16 stamps.  All pointers are
  * device pointers except those of ap_cnn_layer_offsets. */
 int64_t ap_cnn_param_count(void);
+/* In-project autotuner of the CNN GEMM tiles: with enable != 0 the first GEMM of each
+ * (layout, shape) times the 128x128 / 128x64 / 128x32 tiles and keeps the fastest; enable < 0
+ * also forgets the choices made so far.  tuned_shapes (may be NULL) = shapes tuned so far. */
+int ap_cnn_autotune(int32_t enable, int32_t* tuned_shapes);
 size_t ap_cnn_workspace_bytes(int64_t batch);
 /* w_offsets[6], b_offsets[6], dims[6][6] = {cin, cout, hin, hout, K, N} per layer (host). */
 int ap_cnn_layer_offsets(int64_t* w_offsets, int64_t* b_offsets, int32_t* dims);

@@ -224,3 +224,23 @@ def test_moments_initialiser_matches_oracle(N):
     # Re and Ie come from fp32 histograms: a pixel on a bin edge may land in the next bin
     close = np.isclose(got[:, 5], want[:, 5], rtol=1e-3) & np.isclose(got[:, 6], want[:, 6], atol=1e-3)
     assert close.mean() >= 0.95
+
+
+def test_gemm_autotuner_keeps_results(N):
+    """The CNN GEMM autotuner picks a tile shape per GEMM shape; the forward pass agrees with
+    the untuned one to fp32 summation order."""
+    from astrophot_gb300 import cnn
+    import ctypes
+
+    net = cnn.InitNet(seed=4)
+    x = torch.randn(64 * 64 * 64, device="cuda")
+    lib = N.lib()
+    lib.ap_cnn_autotune(0, None)
+    ref = net.forward(x, 64).clone()
+    n = ctypes.c_int32()
+    lib.ap_cnn_autotune(-1, ctypes.byref(n))
+    lib.ap_cnn_autotune(1, ctypes.byref(n))
+    out = net.forward(x, 64)
+    lib.ap_cnn_autotune(0, ctypes.byref(n))
+    assert n.value >= 6
+    assert torch.allclose(out, ref, rtol=1e-3, atol=1e-3 * ref.abs().max().item())

@@ -325,3 +325,26 @@ def test_profiler_outside_and_inside_capture(N):
     kt = b.kernel_times()
     b.profile(False)
     assert kt["conv"][1] >= 1 and kt["conv"][0] > 0
+
+
+def test_autotuned_grid_gives_identical_renders(N):
+    """The render-pass autotuner changes only persistent-grid sizes: the renders, Jacobians and
+    LM results stay bit for bit the same (every reduction has a fixed order)."""
+    from astrophot_gb300 import synthetic
+
+    specs = synthetic.cutout_stamps(12, seed=5, lo=24, hi=96)
+    opts = N.make_options(profile="sersic", psf_mode="full", free_mask=0x7F, has_sky=True)
+    b = N.StampBatch([(s.nx, s.ny) for s in specs], [(s.psf.shape[1], s.psf.shape[0]) for s in specs],
+                     N.scale_geometry(len(specs)), opts)
+    psf = b.pack_psf([s.psf for s in specs])
+    params = torch.tensor(np.array([np.r_[s.init, 0.0] for s in specs]))
+    m0, j0 = b.jacobian(params, psf)
+    m0, j0 = m0.clone(), j0.clone()
+    res = b.autotune(params, psf, jacobian=True)
+    assert set(res["blocks_per_sm"]) == {"sample", "integrate", "conv", "psf"}
+    assert all(1 <= v <= 64 for v in res["blocks_per_sm"].values()) and res["render_pass_ms"] > 0
+    m1, j1 = b.jacobian(params, psf)
+    assert torch.equal(m0, m1) and torch.equal(j0, j1)
+    b.set_grid({"sample": 3, "integrate": 2, "conv": 5, "psf": 1})
+    m2, j2 = b.jacobian(params, psf)
+    assert torch.equal(m0, m2) and torch.equal(j0, j2)

@@ -102,3 +102,53 @@ def test_scene_lm_matches_reference(S, name):
     assert abs(min(lm.loss_history) / d["loss_history"].min() - 1) <= 1e-4
     # the first steps follow the reference's trajectory
     assert np.allclose(lm.loss_history[:3], d["loss_history"][:3], rtol=1e-5)
+
+
+def test_scene_with_mask_and_no_psf_matches_oracle(S):
+    """Masked pixels and no PSF: model, Jacobian and the joint LM against the oracle."""
+    from oracle.lm import GroupProblem, LMOracle
+    from oracle.render import Component, Window
+
+    rng = np.random.default_rng(17)
+    N = 72
+    wins = (((0, 48), (4, 60)), ((20, 72), (10, 72)), ((10, 70), (30, 72)))
+    truth = ((22.3, 30.8, 0.6, 0.9, 2.2, 6.0, 1.9), (47.1, 40.2, 0.45, 2.3, 1.0, 9.0, 1.6),
+             (39.6, 55.4, 0.8, 0.4, 3.1, 4.0, 2.1))
+    kinds = ("sersic", "exponential", "sersic")
+
+    def comps(values):
+        out = []
+        for k, v, w in zip(kinds, values, wins):
+            p = {"center": [v[0], v[1]], "q": v[2], "PA": v[3], "Re": v[5], "Ie": v[6]}
+            if k == "sersic":
+                p["n"] = v[4]
+            out.append(Component(k, p, window=w))
+        out.append(Component("flat_sky", {"F": 0.0}, locked=("F",)))
+        return out
+
+    prob_t = GroupProblem(comps(truth), Window.from_scale(N, N), None, np.zeros((N, N)))
+    img = prob_t.forward(prob_t.representation()).reshape(N, N)
+    var = img + 10.0
+    data = img + np.sqrt(var) * rng.normal(size=img.shape)
+    weight = 1.0 / var
+    mask = np.zeros((N, N), bool)
+    mask[30:38, 5:30] = True
+    mask[::9, ::7] = True
+    init = [tuple(np.array(v) * np.array([1, 1, 1.08, 1, 0.9, 1.1, 1]) + np.array([0.5, -0.4, 0, 0.05, 0, 0, -0.05]))
+            for v in truth]
+    prob = GroupProblem(comps(init), Window.from_scale(N, N), None, data, weight, mask)
+    srcs = [S.SceneSource(k, list(v), w) for k, v, w in zip(kinds, init, wins)]
+    sc = S.Scene(N, N, srcs, None, data, weight, mask=mask, sky=1.0)
+    rep = sc.representation()
+    assert np.allclose(rep, prob.representation(), atol=1e-12)
+    m = sc.forward(rep).cpu().numpy()
+    ref = prob.forward(rep)
+    assert np.max(np.abs(m - ref)) <= 1e-5 * np.max(np.abs(ref))
+    J = sc.jacobian_image(rep).reshape(-1, sc.P)
+    Jr = prob.jacobian(rep)
+    for k in range(sc.P):
+        assert np.max(np.abs(J[:, k] - Jr[:, k])) <= 2e-4 * np.max(np.abs(Jr[:, k])), k
+    lm = S.SceneLM(sc, max_iter=15).fit()
+    lmo = LMOracle(prob, rep, max_iter=15).fit()
+    print(lm.loss_history, lmo.loss_history)
+    assert abs(min(lm.loss_history) / min(lmo.loss_history) - 1) <= 1e-4
