@@ -313,9 +313,8 @@ __device__ double sample_pixel64(const BatchArgs& b, const StampDev& st, const E
 }
 
 template <bool JAC>
-__device__ void sample_tile(const BatchArgs& b, int s, int slot, int tile_local) {
+__device__ void sample_tile(const BatchArgs& b, const EvalF& e, int s, int slot, int tile_local) {
   const StampDev& st = b.stamps[s];
-  const EvalF e = load_evalf(st, b.evals[s * 2 + slot]);
   const int tx = threadIdx.x & (kTile - 1), ty = threadIdx.x / kTile;
   const int i = (tile_local % st.ntw_x) * kTile + tx;
   const int j = (tile_local / st.ntw_x) * kTile + ty;
@@ -349,15 +348,38 @@ __device__ void sample_tile(const BatchArgs& b, int s, int slot, int tile_local)
   }
 }
 
+// Each block takes a contiguous chunk of the working-tile list: a stamp's tiles are
+// consecutive there, so its evaluation constants are loaded once per run of tiles instead of
+// once per tile, and the next list entry is fetched while a tile is sampled.
+__device__ __forceinline__ void tile_chunk(uint32_t n, uint32_t& c0, uint32_t& c1) {
+  const uint32_t per = (n + gridDim.x - 1) / gridDim.x;
+  c0 = min(n, blockIdx.x * per);
+  c1 = min(n, c0 + per);
+}
+
 __global__ void __launch_bounds__(256) k_sample(BatchArgs b) {
   const uint32_t n = b.counters[7];
-  for (uint32_t it = blockIdx.x; it < n; it += gridDim.x) {
+  uint32_t c0, c1;
+  tile_chunk(n, c0, c1);
+  int cur = -1;
+  bool jac = false;
+  EvalF e{};
+  int64_t next = (c0 < c1) ? b.wlist[c0] : 0;
+  for (uint32_t it = c0; it < c1; ++it) {
+    const int64_t ent = next;
+    if (it + 1 < c1) next = b.wlist[it + 1];
     int slot, s, local;
-    unpack_entry(b.wlist[it], slot, s, local);
-    if (b.evals[s * 2 + slot].ops & OP_JAC)
-      sample_tile<true>(b, s, slot, local);
+    unpack_entry(ent, slot, s, local);
+    if (s * 2 + slot != cur) {
+      cur = s * 2 + slot;
+      const EvalDev& ed = b.evals[cur];
+      e = load_evalf(b.stamps[s], ed);
+      jac = (ed.ops & OP_JAC) != 0;
+    }
+    if (jac)
+      sample_tile<true>(b, e, s, slot, local);
     else
-      sample_tile<false>(b, s, slot, local);
+      sample_tile<false>(b, e, s, slot, local);
   }
 }
 
@@ -465,9 +487,14 @@ __device__ __forceinline__ void select_tile(const BatchArgs& b, int slot, int s,
 
 __global__ void __launch_bounds__(256) k_select(BatchArgs b) {
   const uint32_t n = b.counters[7];
-  for (uint32_t it = blockIdx.x; it < n; it += gridDim.x) {
+  uint32_t c0, c1;
+  tile_chunk(n, c0, c1);
+  int64_t next = (c0 < c1) ? b.wlist[c0] : 0;
+  for (uint32_t it = c0; it < c1; ++it) {
+    const int64_t ent = next;
+    if (it + 1 < c1) next = b.wlist[it + 1];
     int slot, s, local;
-    unpack_entry(b.wlist[it], slot, s, local);
+    unpack_entry(ent, slot, s, local);
     select_tile(b, slot, s, local);
   }
 }
