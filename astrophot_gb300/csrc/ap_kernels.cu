@@ -1172,7 +1172,7 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
 }
 
 template <int NF>
-__global__ void __launch_bounds__(kConvThreads, 4) k_conv(BatchArgs b, ConvIO io) {
+__global__ void __launch_bounds__(kConvThreads, 5) k_conv(BatchArgs b, ConvIO io) {
   extern __shared__ __align__(16) float smem[];
   __shared__ float shred[kConvWarps * kNacc];
   __shared__ uint32_t next;
