@@ -204,9 +204,17 @@ struct ConvIO {
 // dynamic shared memory of the convolve pass for a kpx x kpy kernel: 3 kernels stored
 // transposed with columns padded to a multiple of 4 floats, and the input tile
 __host__ __device__ inline int conv_col_stride(int kpy) { return (kpy + 3) & ~3; }
+// Row pitch of the column-major input tile: at least its kOutTileY + kpy - 1 rows plus the
+// 2 rows that the last float4 of a column may overrun, and 4 mod 8 so that the 8 lanes of a
+// quarter-warp read 16-byte slots in 8 different bank groups
+__host__ __device__ inline int conv_tile_pitch(int kpy) {
+  const int th = kOutTileY + kpy - 1 + 2;
+  return th + ((4 - th % 8) + 8) % 8;
+}
+
 __host__ __device__ inline size_t conv_smem_bytes(int kpx, int kpy) {
   return sizeof(float) * (3 * (size_t)kpx * conv_col_stride(kpy) +
-                          (size_t)(kOutTileX + kpx - 1) * (kOutTileY + kpy - 1));
+                          (size_t)(kOutTileX + kpx - 1) * conv_tile_pitch(kpy));
 }
 
 __host__ __device__ inline int64_t work_plane(const BatchArgs& b, int slot, int plane) {

@@ -898,16 +898,18 @@ __device__ __forceinline__ void conv_tile_reduce(const float* vals, int nvals, d
 // window live in registers.  out[o] = sum_{v,u} K[v][u] T[ty0 + o + KP-1 - v][tx + KP-1 - u],
 // with KT[u * stride + v] = K[v][u].
 template <int KP>
-__device__ __forceinline__ void conv_col_fixed(const float* __restrict__ Tt, int TW,
+__device__ __forceinline__ void conv_col_fixed(const float* __restrict__ Tt, int TP,
                                                const float* __restrict__ KT, int tx, int ty0,
                                                float* out) {
   constexpr int C2 = KP - 1;
   constexpr int NT = kConvRows + KP - 1;
   constexpr int KS = (KP + 3) & ~3;
+  constexpr int NT4 = (NT + 3) / 4;
   float acc[kConvRows];
 #pragma unroll
   for (int o = 0; o < kConvRows; ++o) acc[o] = 0.f;
-  const float* base = Tt + ty0 * TW + tx + C2;
+  // column-major tile (pitch TP): a thread's input column is contiguous, read as float4
+  const float* base = Tt + (tx + C2) * TP + ty0;
 #pragma unroll 1
   for (int u = 0; u < KP; ++u) {
     float kc[KS];
@@ -920,10 +922,16 @@ __device__ __forceinline__ void conv_col_fixed(const float* __restrict__ Tt, int
       kc[4 * q + 2] = k4.z;
       kc[4 * q + 3] = k4.w;
     }
-    float t[NT];
-    const float* col = base - u;
+    float t[4 * NT4];
+    const float4* col = reinterpret_cast<const float4*>(base - u * TP);
 #pragma unroll
-    for (int r = 0; r < NT; ++r) t[r] = col[r * TW];
+    for (int q = 0; q < NT4; ++q) {
+      const float4 c4 = col[q];
+      t[4 * q + 0] = c4.x;
+      t[4 * q + 1] = c4.y;
+      t[4 * q + 2] = c4.z;
+      t[4 * q + 3] = c4.w;
+    }
 #pragma unroll
     for (int v = 0; v < KP; ++v)
 #pragma unroll
@@ -933,7 +941,7 @@ __device__ __forceinline__ void conv_col_fixed(const float* __restrict__ Tt, int
   for (int o = 0; o < kConvRows; ++o) out[o] = acc[o];
 }
 
-__device__ __forceinline__ void conv_col_generic(const float* __restrict__ Tt, int TW,
+__device__ __forceinline__ void conv_col_generic(const float* __restrict__ Tt, int TP,
                                                  const float* __restrict__ KT, int kpx, int kpy,
                                                  int tx, int ty0, float* out) {
   float acc[kConvRows];
@@ -942,12 +950,12 @@ __device__ __forceinline__ void conv_col_generic(const float* __restrict__ Tt, i
   const int ks = conv_col_stride(kpy);
   for (int u = 0; u < kpx; ++u) {
     const float* kcol = KT + u * ks;
-    const float* tcol = Tt + ty0 * TW + tx + kpx - 1 - u;
+    const float* tcol = Tt + (tx + kpx - 1 - u) * TP + ty0;
     for (int v = 0; v < kpy; ++v) {
       const float k = kcol[v];
-      const float* tp = tcol + (kpy - 1 - v) * TW;
+      const float* tp = tcol + (kpy - 1 - v);
 #pragma unroll
-      for (int o = 0; o < kConvRows; ++o) acc[o] = fmaf(k, tp[o * TW], acc[o]);
+      for (int o = 0; o < kConvRows; ++o) acc[o] = fmaf(k, tp[o], acc[o]);
     }
   }
 #pragma unroll
@@ -955,13 +963,13 @@ __device__ __forceinline__ void conv_col_generic(const float* __restrict__ Tt, i
 }
 
 // One copy of all the kernel-size instances, shared by the k_conv<NF> instantiations.
-__device__ __noinline__ void conv_col(const float* Tt, int TW, const float* KT, int kpx, int kpy,
+__device__ __noinline__ void conv_col(const float* Tt, int TP, const float* KT, int kpx, int kpy,
                                       int tx, int ty0, float* out) {
   if (kpx == kpy) {
     switch (kpx) {
 #define AP_CONV_CASE(K) \
   case K:               \
-    conv_col_fixed<K>(Tt, TW, KT, tx, ty0, out); \
+    conv_col_fixed<K>(Tt, TP, KT, tx, ty0, out); \
     return;
       AP_CONV_CASE(3) AP_CONV_CASE(5) AP_CONV_CASE(7) AP_CONV_CASE(9) AP_CONV_CASE(11)
       AP_CONV_CASE(13) AP_CONV_CASE(15) AP_CONV_CASE(17) AP_CONV_CASE(19) AP_CONV_CASE(21)
@@ -971,7 +979,7 @@ __device__ __noinline__ void conv_col(const float* Tt, int TW, const float* KT, 
         break;
     }
   }
-  conv_col_generic(Tt, TW, KT, kpx, kpy, tx, ty0, out);
+  conv_col_generic(Tt, TP, KT, kpx, kpy, tx, ty0, out);
 }
 
 // Convolve/accumulate pass.  NF = number of fitted parameters (compile time, so the
@@ -1013,7 +1021,7 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
   } else {
     const int kpx = st.kpx, kpy = st.kpy, ks = conv_col_stride(kpy), kstride = kpx * ks;
     const int cx = (kpx - 1) / 2, cy = (kpy - 1) / 2;
-    const int TW = kOutTileX + kpx - 1, TH = kOutTileY + kpy - 1;
+    const int TW = kOutTileX + kpx - 1, TH = kOutTileY + kpy - 1, TP = conv_tile_pitch(kpy);
     float* KT = smem;                // up to 3 kernels, transposed
     float* Tt = smem + 3 * kstride;  // input tile
     const int kp2 = kpx * kpy;
@@ -1029,21 +1037,22 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
       if (pl > 0 && b.kind != AP_PROFILE_SERSIC && pl - 1 == GN) continue;
       __syncthreads();
       const float* src = b.work + work_plane(b, slot, pl) + st.work_off;
-      // rows over warps, columns over lanes: coalesced reads, no index division
-      for (int r = tg; r < TH; r += kConvThreads / 32) {
+      // rows over warps, columns over lanes: coalesced reads; stored column-major (pitch TP,
+      // rows TH..TP-1 zero)
+      for (int r = tg; r < TP; r += kConvThreads / 32) {
         const int wr = row0 + r;
-        const bool rok = (wr >= 0 && wr < st.wny);
+        const bool rok = (r < TH && wr >= 0 && wr < st.wny);
         const float* srow = src + (int64_t)wr * st.wnx;
         for (int c = tx; c < TW; c += 32) {
           const int wc = col0 + c;
-          Tt[r * TW + c] = (rok && wc >= 0 && wc < st.wnx) ? srow[wc] : 0.f;
+          Tt[c * TP + r] = (rok && wc >= 0 && wc < st.wnx) ? srow[wc] : 0.f;
         }
       }
       __syncthreads();
       const int nkp = (pl == 0) ? nk : 1;
       for (int kk = 0; kk < nkp; ++kk) {
         float outv[kConvRows];
-        conv_col(Tt, TW, KT + kk * kstride, kpx, kpy, tx, tg * kConvRows, outv);
+        conv_col(Tt, TP, KT + kk * kstride, kpx, kpy, tx, tg * kConvRows, outv);
         const int dst = (pl == 0) ? kk : 3 + (pl - 1);
 #pragma unroll
         for (int o = 0; o < kConvRows; ++o) cv[dst][o] = outv[o];
