@@ -348,3 +348,64 @@ def test_autotuned_grid_gives_identical_renders(N):
     b.set_grid({"sample": 3, "integrate": 2, "conv": 5, "psf": 1})
     m2, j2 = b.jacobian(params, psf)
     assert torch.equal(m0, m2) and torch.equal(j0, j2)
+
+
+LM_VARIANTS = {
+    # profile, psf, sampling, free sky, mask
+    "exponential_no_psf": ("exponential", False, "midpoint", False, False),
+    "sersic_simpsons_psf": ("sersic", True, "simpsons", False, False),
+    "sersic_free_sky_mask": ("sersic", True, "midpoint", True, True),
+    "exponential_psf_trapezoid": ("exponential", True, "trapezoid", False, False),
+}
+
+
+@pytest.mark.parametrize("name", sorted(LM_VARIANTS))
+def test_lm_variants_match_oracle(N, name):
+    """Batched LM with other options (profile, PSF, sampling mode, free sky, masked pixels):
+    final chi2/ndf against the float64 oracle LM from the same data and initial vector."""
+    from astrophot_gb300 import synthetic
+    from astrophot_gb300.transforms import slots_to_rep
+
+    kind, with_psf, sampling, free_sky, with_mask = LM_VARIANTS[name]
+    size = 48
+    rng = np.random.default_rng(sum(map(ord, name)))
+    truth = synthetic.draw_sersic(rng, size, size)
+    truth[5] = min(truth[5], 9.0)
+    if kind == "exponential":
+        truth[4] = 1.0
+    init = synthetic.perturb_sersic(rng, truth)
+    if kind == "exponential":
+        init[4] = 1.0
+    F_true, F_init = (0.2, 0.15) if free_sky else (0.0, 0.0)
+    psf = synthetic.moffat_stamp(3.5, synthetic.moffat_rd(3.0, 3.5), 15) if with_psf else None
+    slots = [0, 1, 2, 3, 4, 5, 6] if kind == "sersic" else [0, 1, 2, 3, 5, 6]
+    if free_sky:
+        slots.append(7)
+    fmask = sum(1 << s for s in slots)
+    opts = N.make_options(profile=kind, psf_mode="full" if with_psf else "none", sampling_mode=sampling,
+                          free_mask=fmask, has_sky=True)
+    b = N.StampBatch([(size, size)], [(15, 15)] if with_psf else None, N.scale_geometry(1), opts)
+    psf_d = b.pack_psf([psf]) if with_psf else None
+    t8 = np.r_[truth, F_true]
+    model = b.unpack(b.render(torch.tensor(t8[None, :]), psf_d))[0].astype(np.float64)
+    data, weight = synthetic.add_noise(model, 11)
+    mask = np.zeros((size, size), dtype=np.uint8)
+    if with_mask:
+        mask[5:14, 20:31] = 1
+        mask[::6, ::5] = 1
+    i8 = np.r_[init, F_init]
+    state, chi2, iters, status = b.lm_fit(
+        b.pack([data]), b.pack([weight]), b.pack([mask], torch.uint8) if with_mask else None, psf_d,
+        torch.tensor(i8[None, :]), torch.tensor(slots_to_rep(i8[None, :], fmask)), N.make_lm_options())
+    p = {"center": [init[0], init[1]], "q": init[2], "PA": init[3], "Re": init[5], "Ie": init[6]}
+    if kind == "sersic":
+        p["n"] = init[4]
+    gal = Component(kind, p, psf_mode="full" if with_psf else "none", sampling_mode=sampling)
+    sky = Component("flat_sky", {"F": F_init}, locked=() if free_sky else ("F",))
+    psf32 = None if psf is None else PSF(psf.astype(np.float32).astype(np.float64))
+    prob = GroupProblem([gal, sky], Window.from_scale(size, size), psf32,
+                        data.astype(np.float32).astype(np.float64), weight.astype(np.float32).astype(np.float64),
+                        mask.astype(bool) if with_mask else None)
+    lm = LMOracle(prob, prob.representation()).fit()
+    print(name, chi2.item(), lm.res_loss(), iters.item(), lm.iterations, N.LM_MESSAGES[status.item()], lm.message)
+    assert abs(chi2.item() / lm.res_loss() - 1) <= 1e-4
