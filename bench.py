@@ -52,7 +52,7 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default="learned", choices=["learned", "cutouts"])
+    p.add_argument("--workload", default="learned", choices=["learned", "cutouts", "crowded"])
     p.add_argument("--stamps", type=int, default=None, help="65536 (learned) / 8192 (cutouts)")
     p.add_argument("--seed", type=int, default=2024)
     p.add_argument("--cpu-sample", type=int, default=8, help="stamps fitted by the CPU baseline")
@@ -270,6 +270,12 @@ class ClockSampler:
 def run_gpu(args):
     if args.workload == "learned":
         run_gpu_learned(args)
+    elif args.workload == "crowded":
+        import torch
+
+        if rank_info()[0] == 0:
+            print(json.dumps({"workload": "crowded", "crowded_field": crowded_block(args, torch.device("cuda"))}),
+                  flush=True)
     else:
         run_gpu_cutouts(args)
 
@@ -689,9 +695,13 @@ def run_gpu_learned(args):
         "peak": fp32_peak,
         "unit": "TFLOP/s",
         "frac": achieved / fp32_peak if achieved else None,
-        "traffic": None,
+        # DRAM bytes per launch from one ncu capture of the 4096-stamp case (mean over all
+        # k_conv launches, 108.2 MB), scaled by the stamps per launch (profiles/k_conv_learned_init_4096.md)
+        "traffic": 108.2e6 * S / 4096,
+        "traffic_unit": "bytes per launch (ncu, 4096-stamp capture scaled by stamps)",
         "launches": conv_n,
         "avg_launch_ms": conv_ms / max(conv_n, 1),
+        "algorithmic_flop_per_launch": work["conv_flops"] / max(conv_n, 1),
         "peak_source": "measured FP32 FMA probe (ap_fma_probe) on this GPU",
     }
     chunks = (S + 8191) // 8192
@@ -864,6 +874,9 @@ def main():
     if args.impl == "reference":
         if args.workload == "learned":
             run_reference_learned(args)
+        elif args.workload == "crowded":
+            print(json.dumps({"impl": "reference", "workload": "crowded",
+                              "unavailable": "the crowded-field block is a GPU-only secondary measurement"}))
         else:
             run_reference(args)
     else:
