@@ -10,8 +10,8 @@ the proposal unless its chi^2 is worse than that of the moments initialiser
 Training data come only from the library's own renderer: Sersic stamps drawn from the C0
 parameter distributions (centre 32 + U(-1, 1), n ~ U(0.5, 4), Re ~ U(5, 20), q ~ U(0.3, 1),
 PA ~ U(0, pi), log10 Ie ~ U(0, 2)), a flat sky of 1.0, a Moffat PSF (beta 3.5) with
-FWHM ~ U(2, 5) px (64 levels, 21 x 21 box) and Gaussian noise of constant sigma set by a
-signal-to-noise ratio ~ U(10, 200), SNR = sqrt(sum(galaxy^2)) / sigma.
+FWHM ~ U(2, 5) px (64 levels, side 4 FWHM rounded to odd: 9 to 21 px) and Gaussian noise of
+constant sigma set by a signal-to-noise ratio ~ U(10, 200), SNR = sqrt(sum(galaxy^2)) / sigma.
 """
 
 from __future__ import annotations
@@ -32,7 +32,6 @@ __all__ = ("InitNet", "StampSet", "draw_stamp_params", "psf_bank", "make_stamps"
            "WEIGHTS_PATH")
 
 IMG = 64
-PSF_BOX = 21
 N_OUT = 8
 OUT_PAD = 16
 WEIGHTS_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights", "init_cnn.npz")
@@ -57,16 +56,13 @@ def draw_stamp_params(rng: np.random.Generator, n: int, size: int = IMG) -> np.n
     return p
 
 
-def psf_bank(levels: int = 64, beta: float = 3.5) -> np.ndarray:
-    """[levels, 21, 21] Moffat stamps, FWHM evenly spaced on [2, 5] px, each drawn at side
-    odd(4 FWHM) and centred in the 21 x 21 box (zeros around)."""
-    out = np.zeros((levels, PSF_BOX, PSF_BOX))
-    for i, fwhm in enumerate(np.linspace(2.0, 5.0, levels)):
+def psf_bank(levels: int = 64, beta: float = 3.5) -> list:
+    """[levels] Moffat stamps, FWHM evenly spaced on [2, 5] px, each of side odd(4 FWHM)."""
+    out = []
+    for fwhm in np.linspace(2.0, 5.0, levels):
         w = int(round(4 * fwhm))
         w += 1 - (w % 2)
-        st = moffat_stamp(beta, moffat_rd(fwhm, beta), w)
-        o = (PSF_BOX - w) // 2
-        out[i, o : o + w, o : o + w] = st
+        out.append(moffat_stamp(beta, moffat_rd(fwhm, beta), w))
     return out
 
 
@@ -77,32 +73,27 @@ class StampSet:
     truth: np.ndarray       # [n, 8]
     data: torch.Tensor      # [n * 4096]
     weight: torch.Tensor    # [n * 4096]
-    psf: torch.Tensor       # [n * 441]
+    psf: torch.Tensor       # packed PSFs (batch.pack_psf layout)
     sigma: torch.Tensor     # [n]
     batch: "N.StampBatch"
 
 
-_BATCHES = {}
+def _stamp_batch(kshapes, device) -> "N.StampBatch":
+    """A plan for len(kshapes) 64 x 64 stamps with these PSF shapes."""
+    opts = N.make_options(profile="sersic", psf_mode="full", free_mask=0x7F, has_sky=True)
+    n = len(kshapes)
+    return N.StampBatch([(IMG, IMG)] * n, list(kshapes), N.scale_geometry(n), opts, device)
 
 
-def _stamp_batch(n: int, device) -> "N.StampBatch":
-    key = (n, str(device))
-    if key not in _BATCHES:
-        opts = N.make_options(profile="sersic", psf_mode="full", free_mask=0x7F, has_sky=True)
-        _BATCHES.clear()
-        _BATCHES[key] = N.StampBatch([(IMG, IMG)] * n, [(PSF_BOX, PSF_BOX)] * n, N.scale_geometry(n), opts, device)
-    return _BATCHES[key]
-
-
-def make_stamps(n: int, seed: int, bank: Optional[torch.Tensor] = None, device="cuda", snr=(10.0, 200.0)) -> StampSet:
+def make_stamps(n: int, seed: int, bank: Optional[list] = None, device="cuda", snr=(10.0, 200.0)) -> StampSet:
     """Render ``n`` stamps with the library's own kernels and add seeded Gaussian noise."""
     rng = np.random.default_rng(seed)
     truth = draw_stamp_params(rng, n)
     if bank is None:
-        bank = torch.tensor(psf_bank(), dtype=torch.float32, device=device)
-    idx = torch.tensor(rng.integers(0, bank.shape[0], n), device=device)
-    psf = bank[idx].reshape(-1).contiguous()
-    b = _stamp_batch(n, device)
+        bank = psf_bank()
+    idx = rng.integers(0, len(bank), n)
+    b = _stamp_batch([bank[k].shape[::-1] for k in idx], device)
+    psf = b.pack_psf([bank[k] for k in idx])
     model = b.render(torch.tensor(truth), psf)
     gal = (model - 1.0).view(n, IMG * IMG)
     s = torch.tensor(rng.uniform(snr[0], snr[1], n), dtype=torch.float32, device=device)
@@ -250,7 +241,7 @@ class InitNet:
         """Adam on fresh rendered stamps (each stamp seen once)."""
         if batch % 16 or chunk % batch:
             raise ValueError("batch must be a multiple of 16 dividing chunk")
-        bank = torch.tensor(psf_bank(), dtype=torch.float32, device=self.device)
+        bank = psf_bank()
         m1 = torch.zeros(self.count, dtype=torch.float32, device=self.device)
         m2 = torch.zeros_like(m1)
         grads = torch.zeros_like(m1)

@@ -4,7 +4,8 @@ learned + batched against plain.
 Workloads (one "step" = every stamp of the workload fitted once, from its initial values):
   learned (default) -- 65,536 held-out 64 x 64 stamps rendered by this library: one Sersic
       galaxy from the C0 distributions + a flat sky of 1.0 (locked), Moffat PSF (beta 3.5,
-      FWHM ~ U(2, 5) px, 21 x 21 box), Gaussian noise of constant sigma at SNR ~ U(10, 200).
+      FWHM ~ U(2, 5) px, side 4 FWHM rounded to odd), Gaussian noise of constant sigma at
+      SNR ~ U(10, 200).
       A step = CNN proposal (bf16 tensor-core kernels) + moments fallback, chi^2 of both,
       per-stamp selection, then one batched LM of all stamps (7 free parameters).
       Reported beside it: the plain method = LM from the moments values, batched and one
@@ -491,7 +492,7 @@ def learned_sample_jobs(S, seed, idx, data_of=None, init_of=None):
     truth = cnn.draw_stamp_params(rng, S)
     pidx = rng.integers(0, 64, S)
     snr = rng.uniform(10.0, 200.0, S)
-    bank = cnn.psf_bank().astype(np.float32).astype(np.float64)
+    bank = [k.astype(np.float32).astype(np.float64) for k in cnn.psf_bank()]
     jobs = []
     for i in idx:
         psf = bank[pidx[i]]
@@ -646,12 +647,16 @@ def run_gpu_learned(args):
     n_single = min(32, S)
     init_ph = init_p.cpu()
     opts = N.make_options(profile="sersic", psf_mode="full", free_mask=FREE_MASK, has_sky=True)
-    one = N.StampBatch([(64, 64)], [(21, 21)], N.scale_geometry(1), opts, dev)
     singles = []
+    psf_off = [0]
+    for kx, ky in batch.psf_shapes:
+        psf_off.append(psf_off[-1] + kx * ky)
     for i in range(n_single):
         sl = slice(i * 4096, (i + 1) * 4096)
+        one = N.StampBatch([(64, 64)], [batch.psf_shapes[i]], N.scale_geometry(1), opts, dev)
         singles.append(cnn.StampSet(st.truth[i : i + 1], st.data[sl].contiguous(), st.weight[sl].contiguous(),
-                                    st.psf[i * 441 : (i + 1) * 441].contiguous(), st.sigma[i : i + 1].contiguous(), one))
+                                    st.psf[psf_off[i] : psf_off[i + 1]].contiguous(), st.sigma[i : i + 1].contiguous(),
+                                    one))
     cnn._lm(singles[0], init_p[0:1].contiguous(), lmo)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -723,7 +728,7 @@ def run_gpu_learned(args):
         "data": "synthetic",
         "config": {
             "workload": f"learned init + batched LM: {S} held-out 64x64 stamps per GPU, Sersic (C0 distributions) "
-            "+ locked sky 1.0, Moffat FWHM U(2,5) px in a 21x21 box, SNR U(10,200); 7 free params",
+            "+ locked sky 1.0, Moffat FWHM U(2,5) px of side odd(4 FWHM) = 9-21 px, SNR U(10,200); 7 free params",
             "stamps_per_gpu": S,
             "pixels_per_gpu": int(batch.out_pixels),
             "parallelism": f"replicas x{world} (independent stamps per rank)",
