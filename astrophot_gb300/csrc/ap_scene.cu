@@ -288,31 +288,60 @@ __global__ void k_chol_update(double* __restrict__ A, int n, int k0) {
   }
 }
 
-// L y = b then L^T x = y, one block; x may alias b
-__global__ void k_chol_solve(const double* __restrict__ A, int n, const double* __restrict__ b, double* __restrict__ x,
-                             double* __restrict__ y) {
+// L y = b then L^T x = y, one block, in 32-row blocks: warp 0 solves a diagonal block with
+// shuffles (no block barrier per row), then all threads apply it to the remaining rows
+__global__ void k_chol_solve(const double* __restrict__ A, int n, const double* __restrict__ b,
+                             double* __restrict__ x, double* __restrict__ y) {
+  __shared__ double yb[kNB];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int i = threadIdx.x; i < n; i += blockDim.x) y[i] = b[i];
   __syncthreads();
-  __shared__ double yj;
-  for (int j = 0; j < n; ++j) {
-    if (threadIdx.x == 0) {
-      yj = y[j] / A[(int64_t)j * n + j];
-      y[j] = yj;
+  for (int kb = 0; kb < n; kb += kNB) {
+    const int nb = min(kNB, n - kb);
+    if (warp == 0) {
+      double v = lane < nb ? y[kb + lane] : 0.0;
+      for (int c = 0; c < nb; ++c) {
+        if (lane == c) v = v / A[(int64_t)(kb + c) * n + kb + c];
+        const double vc = __shfl_sync(0xffffffffu, v, c);
+        if (lane > c && lane < nb) v -= A[(int64_t)(kb + lane) * n + kb + c] * vc;
+      }
+      if (lane < nb) {
+        y[kb + lane] = v;
+        yb[lane] = v;
+      }
     }
     __syncthreads();
-    const double v = yj;
-    for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) y[i] -= A[(int64_t)i * n + j] * v;
+    for (int i = kb + nb + threadIdx.x; i < n; i += blockDim.x) {
+      const double* row = A + (int64_t)i * n + kb;
+      double acc = 0.0;
+      for (int c = 0; c < nb; ++c) acc += row[c] * yb[c];
+      y[i] -= acc;
+    }
     __syncthreads();
   }
-  for (int j = n - 1; j >= 0; --j) {
-    if (threadIdx.x == 0) {
-      yj = y[j] / A[(int64_t)j * n + j];
-      y[j] = yj;
+  const int last = ((n - 1) / kNB) * kNB;
+  for (int kb = last; kb >= 0; kb -= kNB) {
+    const int nb = min(kNB, n - kb);
+    if (warp == 0) {
+      // L^T block is upper triangular: rows from the bottom up
+      double v = lane < nb ? y[kb + lane] : 0.0;
+      for (int c = nb - 1; c >= 0; --c) {
+        if (lane == c) v = v / A[(int64_t)(kb + c) * n + kb + c];
+        const double vc = __shfl_sync(0xffffffffu, v, c);
+        if (lane < c) v -= A[(int64_t)(kb + c) * n + kb + lane] * vc;
+      }
+      if (lane < nb) {
+        y[kb + lane] = v;
+        yb[lane] = v;
+      }
     }
     __syncthreads();
-    const double v = yj;
-    // row j of L^T is column j of L: y[i] -= L[j][i] * x[j] for i < j
-    for (int i = threadIdx.x; i < j; i += blockDim.x) y[i] -= A[(int64_t)j * n + i] * v;
+    // rows above: y[i] -= sum_c L[kb + c][i] x[kb + c]  (coalesced over i)
+    for (int i = threadIdx.x; i < kb; i += blockDim.x) {
+      double acc = 0.0;
+      for (int c = 0; c < nb; ++c) acc += A[(int64_t)(kb + c) * n + i] * yb[c];
+      y[i] -= acc;
+    }
     __syncthreads();
   }
   for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = y[i];
