@@ -701,8 +701,8 @@ def run_gpu_learned(args):
         "unit": "TFLOP/s",
         "frac": achieved / fp32_peak if achieved else None,
         # DRAM bytes per launch from one ncu capture of the 4096-stamp case (mean over all
-        # k_conv launches, 108.2 MB), scaled by the stamps per launch (profiles/k_conv_learned_init_4096.md)
-        "traffic": 108.2e6 * S / 4096,
+        # k_conv launches, 99.9 MB), scaled by the stamps per launch (profiles/k_conv_learned_init_4096.md)
+        "traffic": 99.9e6 * S / 4096,
         "traffic_unit": "bytes per launch (ncu, 4096-stamp capture scaled by stamps)",
         "launches": conv_n,
         "avg_launch_ms": conv_ms / max(conv_n, 1),
