@@ -108,6 +108,7 @@ EXPORTS = [
     ("ap_render_vjp", [_P, _P, _P, _P, _I32, _P, _P]),
     ("ap_batch_autotune", [_P, _P, _P, _I32, _PI32, _PD, _P]),
     ("ap_batch_set_grid", [_P, _PI32]),
+    ("ap_values_to_rep", [_P, _I32, _I32, _P, _P]),
     ("ap_batch_psf_stride", [_P, _PI64]),
     ("ap_psf_shift", [_P, _P, _P, _P, _P, _P]),
     ("ap_chi2", [_P, _P, _P, _P, _P, _P, _P]),
@@ -545,6 +546,15 @@ def fma_probe_tflops(iters=4096, blocks=None) -> float:
         flops = 2.0 * 8 * 16 * iters * blocks * 256
         best = max(best, flops / (ms * 1e-3) / 1e12)
     return best
+
+
+def values_to_rep(values: torch.Tensor, free_mask: int) -> torch.Tensor:
+    """[n, 8] value-space rows (device) -> [n, n_free] representation rows, on the device."""
+    values = values.to(torch.float64).contiguous()
+    n = values.shape[0]
+    out = torch.empty((n, bin(free_mask).count("1")), dtype=torch.float64, device=values.device)
+    check(lib().ap_values_to_rep(_ptr(values), n, int(free_mask), _ptr(out), _stream()), "ap_values_to_rep")
+    return out
 
 
 def damped_solve(hess: torch.Tensor, grad: torch.Tensor, L: torch.Tensor) -> torch.Tensor:

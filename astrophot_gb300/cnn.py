@@ -300,19 +300,9 @@ def moments_init(st: StampSet, n: int, sky_F: float = 0.0) -> torch.Tensor:
 
 
 def _lm(st: StampSet, init: torch.Tensor, lm_options):
-    from .transforms import SLOT_LIMITS
-
     b = st.batch
-    # representation of the 7 fitted slots, computed on the device in float64
-    rep = torch.empty((init.shape[0], 7), dtype=torch.float64, device=init.device)
-    rep[:, 0:2] = init[:, 0:2]
-    rep[:, 2] = torch.tan(init[:, 2] * math.pi - math.pi / 2)           # q in (0, 1)
-    rep[:, 3] = torch.remainder(init[:, 3], math.pi)                     # PA cyclic
-    lo, hi = SLOT_LIMITS[4][0]
-    rep[:, 4] = torch.tan((init[:, 4] - lo) * math.pi / (hi - lo) - math.pi / 2)
-    rep[:, 5] = init[:, 5] - 1.0 / init[:, 5]                            # Re > 0
-    rep[:, 6] = init[:, 6]
-    return b.lm_fit(st.data, st.weight, None, st.psf, init.contiguous(), rep.contiguous(), lm_options)
+    rep = N.values_to_rep(init, 0x7F)
+    return b.lm_fit(st.data, st.weight, None, st.psf, init.contiguous(), rep, lm_options)
 
 
 def plain_fit(st: StampSet, n: int, lm_options=None):

@@ -590,6 +590,11 @@ int ap_batch_autotune(ap_batch* b, const double* params, const float* psf, int32
   return rc;
 }
 
+int ap_values_to_rep(const double* values, int32_t n, int32_t free_mask, double* rep, ap_stream_t stream) {
+  if (!values || !rep || n < 0 || (free_mask & ~0xff)) return AP_ERR_ARG;
+  return check_cuda(launch_values_to_rep(values, n, free_mask, rep, (cudaStream_t)stream));
+}
+
 int ap_batch_set_grid(ap_batch* b, const int32_t* blocks_per_sm) {
   if (!b || !blocks_per_sm) return AP_ERR_ARG;
   for (int k = 0; k < GK_COUNT; ++k)

@@ -85,6 +85,7 @@ cudaError_t launch_chi2_only(const BatchArgs& b, const ConvIO& io, const float* 
                              double* out, cudaStream_t s);
 cudaError_t launch_psf_only(const BatchArgs& b, const float* psf, cudaStream_t s);
 cudaError_t launch_gather_vjp(const BatchArgs& b, double* grad, cudaStream_t s);
+cudaError_t launch_values_to_rep(const double* values, int32_t n, int32_t free_mask, double* rep, cudaStream_t st);
 cudaError_t launch_damped_solve(int m, int p, const double* hess, const double* grad,
                                 const double* L, double* h, cudaStream_t s);
 cudaError_t launch_psf_export(const BatchArgs& b, float* out, float* d_out, int64_t stride,

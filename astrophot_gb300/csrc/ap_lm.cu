@@ -38,6 +38,38 @@ __device__ __forceinline__ bool rep_to_value(int slot, double r, double& v) {
   }
 }
 
+// value -> representation (utils/conversions/optimization.py:6-16,42-48): the inverse of
+// rep_to_value for the fitted slots
+__device__ __forceinline__ double value_to_rep(int slot, double v) {
+  switch (slot) {
+    case PQ:
+      return tan((v - 0.0) * kPi / (1.0 - 0.0) - kPi / 2);
+    case PN:
+      return tan((v - 0.36) * kPi / (8.0 - 0.36) - kPi / 2);
+    case PRE:
+      return v - 1.0 / (v - 0.0);
+    case PPA:
+      return 0.0 + (v - 0.0) - kPi * floor((v - 0.0) / kPi);
+    default:
+      return v;
+  }
+}
+
+__global__ void k_values_to_rep(const double* __restrict__ values, int32_t n, int32_t free_mask,
+                                double* __restrict__ rep) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  int k = 0;
+  const int nf = __popc(free_mask & 0xff);
+  for (int i = 0; i < NPARAM; ++i)
+    if (free_mask & (1 << i)) rep[(int64_t)s * nf + k++] = value_to_rep(i, values[(int64_t)s * NPARAM + i]);
+}
+
+cudaError_t launch_values_to_rep(const double* values, int32_t n, int32_t free_mask, double* rep, cudaStream_t st) {
+  if (n > 0) k_values_to_rep<<<(n + 127) / 128, 128, 0, st>>>(values, n, free_mask, rep);
+  return cudaGetLastError();
+}
+
 __device__ bool write_eval(const BatchArgs& b, const LMArgs& lm, int s, int slot, const double* x,
                            int32_t ops) {
   double* out = lm.params_next + ((int64_t)s * 2 + slot) * NPARAM;

@@ -790,6 +790,15 @@ def run_gpu_learned(args):
         line["parity"] = {"stamps": len(idx), "max_rel_chi2_vs_oracle": float(max(rels)),
                           "within_1e-4": int(sum(r <= 1e-4 for r in rels)),
                           "oracle_mean_iterations": float(np.mean(its))}
+        # the fits that ended with "could not find step" (not counted in value): their chi2
+        # against the oracle's from the same initial values, on a few of them
+        ns = [int(i) for i in np.flatnonzero(status_h == N.LM_NO_STEP)[: max(2, args.cpu_sample // 2)]]
+        if ns:
+            jobs = learned_sample_jobs(S, seed, ns, data_of=data_of, init_of=lambda i: init_lh[i])
+            rel_ns = [abs(chi2_h[i] / _oracle_fit(job)[0] - 1.0) for i, job in zip(ns, jobs)]
+            line["parity"]["no_step_stamps"] = len(ns)
+            line["parity"]["no_step_within_1e-4"] = int(sum(r <= 1e-4 for r in rel_ns))
+            line["parity"]["no_step_max_rel_chi2"] = float(max(rel_ns))
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -165,6 +165,12 @@ int ap_batch_autotune(ap_batch* batch, const double* params, const float* psf, i
                       int32_t* chosen, double* best_ms, ap_stream_t stream);
 int ap_batch_set_grid(ap_batch* batch, const int32_t* blocks_per_sm);
 
+/* Value -> representation of the fitted slots (boundaries / cyclic_boundaries,
+ * astrophot/utils/conversions/optimization.py:6-54): values[n][8] -> rep[n][popcount(free_mask)],
+ * device pointers; the representation vector ap_lm_fit starts from. */
+int ap_values_to_rep(const double* values, int32_t n, int32_t free_mask, double* rep,
+                     ap_stream_t stream);
+
 /* Shifted, renormalised PSF of every stamp for value-space params (device):
  * out[n][(ky+2)*(kx+2)] packed with stride max_kp2 = (max ky + 2) * (max kx + 2)
  * (see ap_batch_psf_stride).  d_out (optional, may be NULL) receives d/d shift_x and

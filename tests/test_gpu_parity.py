@@ -409,3 +409,16 @@ def test_lm_variants_match_oracle(N, name):
     lm = LMOracle(prob, prob.representation()).fit()
     print(name, chi2.item(), lm.res_loss(), iters.item(), lm.iterations, N.LM_MESSAGES[status.item()], lm.message)
     assert abs(chi2.item() / lm.res_loss() - 1) <= 1e-4
+
+
+def test_values_to_rep_matches_host_transforms(N):
+    from astrophot_gb300.transforms import slots_to_rep
+    from astrophot_gb300 import synthetic
+
+    rng = np.random.default_rng(12)
+    rows = np.array([np.r_[synthetic.draw_sersic(rng, 64, 64), 0.1] for _ in range(50)])
+    rows[:, 3] += np.pi * rng.integers(-2, 3, 50)  # PA outside [0, pi): the cyclic map wraps it
+    for mask in (0x7F, 0xFF, 0x6F):
+        got = N.values_to_rep(torch.tensor(rows, device="cuda"), mask).cpu().numpy()
+        want = slots_to_rep(rows, mask)
+        assert np.allclose(got, want, rtol=1e-12, atol=1e-12)
