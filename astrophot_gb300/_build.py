@@ -16,7 +16,9 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libastrophot_gb300.so")
-SOURCES = ("ap_kernels.cu", "ap_lm.cu", "ap_capi.cu", "ap_noalloc.cu", "ap_cnn.cu", "ap_scene.cu")
+SOURCES = ("ap_kernels.cu", "ap_lm.cu", "ap_capi.cu", "ap_noalloc.cu", "ap_cnn.cu", "ap_scene.cu", "ap_refinit.cu")
+# per-file flags: the initial-value heuristics round like numpy (no FMA contraction)
+EXTRA = {"ap_refinit.cu": ("-fmad=false",)}
 ARCH = ("-gencode", "arch=compute_103a,code=sm_103a")
 FLAGS = ("-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2")
 
@@ -50,7 +52,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     def compile_one(src):
         obj = os.path.join(build_dir, src.replace(".cu", ".o"))
-        cmd = [cc, *ARCH, *FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [cc, *ARCH, *FLAGS, *EXTRA.get(src, ()), "-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:
             print(" ".join(cmd), flush=True)
         subprocess.run(cmd, check=True)

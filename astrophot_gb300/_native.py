@@ -41,6 +41,8 @@ SAMPLING = {"midpoint": 0, "simpsons": 1, "quad": 2, "trapezoid": 3}
 INTEGRATE = {"none": 0, "threshold": 1}
 PSF_NONE, PSF_FULL, PSF_FULL_NOSHIFT = 0, 1, 2
 VJP_REPRESENTATION, VJP_REFERENCE_CENTER = 1, 2
+# ap_reference_init status bits
+INIT_CENTRE_EDGE, INIT_FIT_LIMIT, INIT_NO_ISOPHOTE, INIT_NO_PROFILE = 1, 2, 4, 8
 
 LM_RUNNING, LM_SUCCESS, LM_IMMOBILE, LM_MAX_ITER, LM_NO_STEP, LM_LIMIT = range(6)
 LM_MESSAGES = {
@@ -109,6 +111,8 @@ EXPORTS = [
     ("ap_batch_autotune", [_P, _P, _P, _I32, _PI32, _PD, _P]),
     ("ap_batch_set_grid", [_P, _PI32]),
     ("ap_values_to_rep", [_P, _I32, _I32, _P, _P]),
+    ("ap_reference_init_workspace_bytes", [_P, _PI64]),
+    ("ap_reference_init", [_P, _P, _P, _I32, _P, _P, _P, _I64, _P]),
     ("ap_batch_psf_stride", [_P, _PI64]),
     ("ap_psf_shift", [_P, _P, _P, _P, _P, _P]),
     ("ap_chi2", [_P, _P, _P, _P, _P, _P, _P]),
@@ -440,6 +444,24 @@ class StampBatch:
         check(self.lib.ap_render_vjp(self.handle, _ptr(params), _ptr(psf), _ptr(g), flags,
                                      _ptr(out), _stream()), "ap_render_vjp")
         return out[:, : self.n_free]
+
+    def reference_init(self, data: torch.Tensor, mask: Optional[torch.Tensor] = None,
+                       params: Optional[torch.Tensor] = None, known_mask: int = 0):
+        """The reference's ``initialize()`` values of every stamp (see ap_reference_init):
+        returns (params [n, 8] float64 value space, status [n] int32 of AP_INIT_* bits).
+        ``params`` supplies the slots whose bit is set in ``known_mask``."""
+        data = data.to(self.device, torch.float32).contiguous()
+        if mask is not None:
+            mask = mask.to(self.device, torch.uint8).contiguous()
+        out = (torch.zeros((self.n, 8), dtype=torch.float64, device=self.device) if params is None
+               else params.to(self.device, torch.float64).clone().contiguous())
+        status = torch.zeros(self.n, dtype=torch.int32, device=self.device)
+        nbytes = ctypes.c_int64(0)
+        check(self.lib.ap_reference_init_workspace_bytes(self.handle, ctypes.byref(nbytes)), "init workspace")
+        ws = torch.empty(max(int(nbytes.value), 1), dtype=torch.uint8, device=self.device)
+        check(self.lib.ap_reference_init(self.handle, _ptr(data), _ptr(mask), int(known_mask), _ptr(out), _ptr(status),
+                                         _ptr(ws), ws.numel(), _stream()), "ap_reference_init")
+        return out, status
 
     def psf_shift(self, params: torch.Tensor, psf: torch.Tensor, derivatives=True):
         params = params.to(self.device, torch.float64).contiguous()

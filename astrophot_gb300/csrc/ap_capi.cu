@@ -595,6 +595,34 @@ int ap_values_to_rep(const double* values, int32_t n, int32_t free_mask, double*
   return check_cuda(launch_values_to_rep(values, n, free_mask, rep, (cudaStream_t)stream));
 }
 
+namespace {
+int refinit_geometry_ok(const ap_batch* b) {
+  for (int i = 0; i < b->n; ++i) {
+    const StampDev& s = b->stamps[i];
+    if (!(s.P[0] > 0) || s.P[0] != s.P[3] || s.P[1] != 0 || s.P[2] != 0) return AP_ERR_UNSUPPORTED;
+  }
+  return AP_OK;
+}
+}  // namespace
+
+int ap_reference_init_workspace_bytes(const ap_batch* b, int64_t* bytes) {
+  if (!b || !bytes) return AP_ERR_ARG;
+  const RefInitPlan P = plan_reference_init(b->stamps.data(), b->n);
+  *bytes = P.scratch_bytes;
+  return AP_OK;
+}
+
+int ap_reference_init(ap_batch* b, const float* data, const uint8_t* mask, int32_t known_mask, double* params,
+                      int32_t* status, void* workspace, int64_t workspace_bytes, ap_stream_t stream) {
+  if (!b || !data || !params || !status || (known_mask & ~0xff)) return AP_ERR_ARG;
+  if (!b->bound) return AP_ERR_NOT_BOUND;
+  if (int rc = refinit_geometry_ok(b)) return rc;
+  const RefInitPlan P = plan_reference_init(b->stamps.data(), b->n);
+  if (P.scratch_bytes > 0 && (!workspace || workspace_bytes < P.scratch_bytes)) return AP_ERR_WORKSPACE;
+  return check_cuda(launch_reference_init(P, b->args.stamps, b->n, b->opt.profile, known_mask, data, mask, params,
+                                          status, workspace, (cudaStream_t)stream));
+}
+
 int ap_batch_set_grid(ap_batch* b, const int32_t* blocks_per_sm) {
   if (!b || !blocks_per_sm) return AP_ERR_ARG;
   for (int k = 0; k < GK_COUNT; ++k)

@@ -91,6 +91,21 @@ cudaError_t launch_damped_solve(int m, int p, const double* hess, const double* 
 cudaError_t launch_psf_export(const BatchArgs& b, float* out, float* d_out, int64_t stride,
                               cudaStream_t s);
 
+// the reference's initial-value heuristics (ap_refinit.cu)
+constexpr size_t kRefInitSmemBudget = 200 * 1024;  // dynamic shared memory per CTA at most
+struct RefInitPlan {
+  int iso_cap = 0;         // isophote samples per CTA (power of two)
+  int pix_cap = 0;         // pixel sort buffer (power of two >= pixels and edge pixels per stamp)
+  bool pix_in_smem = false;
+  size_t smem = 0;         // dynamic shared memory per CTA
+  int grid = 0;            // persistent CTAs
+  int64_t scratch_bytes = 0;  // global pixel buffers when they do not fit in shared memory
+};
+RefInitPlan plan_reference_init(const StampDev* host_stamps, int32_t n);
+cudaError_t launch_reference_init(const RefInitPlan& P, const StampDev* stamps, int32_t n, int32_t kind,
+                                  int32_t known, const float* data, const uint8_t* mask, double* params,
+                                  int32_t* status, void* scratch, cudaStream_t st);
+
 // LM launches (ap_lm.cu)
 cudaError_t launch_lm_init(const BatchArgs& b, const LMArgs& lm, const double* state0,
                            const uint8_t* mask, cudaStream_t s);

@@ -278,6 +278,50 @@ class Galaxy_Model(Component_Model):
     _parameter_order = Component_Model._parameter_order + ("q", "PA")
     usable = False
 
+    @torch.no_grad()
+    def initialize(self, target=None, parameters=None, **kwargs):
+        """``initialize()`` of a Sérsic / exponential galaxy on the CUDA path
+        (``ap_reference_init``): every parameter without a value gets the reference's own
+        heuristic value, the centre of light (``model_object.py:180-233``), the angular centre
+        PA and the flattest-isophote q (``galaxy_model_object.py:60-113``), and n / Re / Ie from
+        Nelder-Mead on the binned median profile (``_shared_methods.py:123-166``); parameters
+        with values are inputs.  Uncertainties are left as they are."""
+        from . import _native as N
+
+        order = self._parameter_order
+        missing = [p for p in order if self.parameters[p].value is None]
+        if not missing:
+            return
+        target = self.target if target is None else target
+        area = target[self.window]
+        c = self.parameters["center"]
+        if c.value is None and c.locked:  # model_object.py:209-210: the window centre, no search
+            with Param_Unlock(c), Param_SoftLimits(c):
+                c.value = self.window.center
+        vec = np.zeros((1, 8))
+        known = 0
+        for name in order:
+            node = self.parameters[name]
+            if node.value is None:
+                continue
+            for k, slot in enumerate(SLOT[name]):
+                vec[0, slot] = float(node.value.reshape(-1)[k])
+                known |= 1 << slot
+        opts = N.make_options(profile=self.profile, free_mask=0x7F if self.profile == "sersic" else 0x6F)
+        w = area.window
+        batch = N.StampBatch([tuple(w.pixel_shape)], None, w.geometry_row()[None, :], opts, config.ap_device)
+        data = batch.pack([area.data.detach().cpu().numpy()])
+        mask = batch.pack([area.mask.detach().cpu().numpy()], torch.uint8) if area.has_mask else None
+        out, status = batch.reference_init(data, mask, torch.tensor(vec), known)
+        if int(status.item()) & (N.INIT_NO_ISOPHOTE | N.INIT_NO_PROFILE):
+            raise ValueError(f"{self.name}: unable to recover isophotes or a radial profile, provide initial values")
+        out = out.cpu().numpy()[0]
+        for name in missing:
+            node = self.parameters[name]
+            val = out[SLOT[name]] if len(SLOT[name]) > 1 else out[SLOT[name][0]]
+            with Param_Unlock(node), Param_SoftLimits(node):
+                node.value = torch.as_tensor(val, dtype=config.ap_dtype)
+
 
 class Sersic_Galaxy(Galaxy_Model):
     """I(R) = 10^Ie exp(-b(n) ((R/Re)^(1/n) - 1)) (``sersic_model.py:41-91``)."""

@@ -171,6 +171,25 @@ int ap_batch_set_grid(ap_batch* batch, const int32_t* blocks_per_sm);
 int ap_values_to_rep(const double* values, int32_t n, int32_t free_mask, double* rep,
                      ap_stream_t stream);
 
+/* The reference's own initial values of a Sérsic / exponential galaxy on every stamp of a bound
+ * batch: what ``Model.initialize()`` finds for the parameters that have no value
+ * (astrophot/models/model_object.py:180-233 centre of light,
+ * astrophot/models/galaxy_model_object.py:60-113 PA and isophote q,
+ * astrophot/models/_shared_methods.py:71-166 n / Re / Ie by Nelder-Mead on the binned median
+ * profile), float64, one CTA per stamp.  data (and mask, optional, 1 = masked) use the batch's
+ * output-pixel packing; pixels must be square and unrotated (P = s I).  params[n][8] (value
+ * space, device): slots with their bit set in known_mask are inputs, the others are written;
+ * status[n] receives AP_INIT_* bits.  workspace (may be NULL when
+ * ap_reference_init_workspace_bytes gives 0) holds per-CTA pixel buffers of large stamps. */
+#define AP_INIT_CENTRE_EDGE 1  /* the centre-of-light box reached the image edge: window centre kept */
+#define AP_INIT_FIT_LIMIT 2    /* Nelder-Mead stopped at its iteration limit: its start kept */
+#define AP_INIT_NO_ISOPHOTE 4  /* no isophote had 3 samples (the reference raises): q = 0.9 */
+#define AP_INIT_NO_PROFILE 8   /* no positive profile bin (the reference raises) */
+int ap_reference_init_workspace_bytes(const ap_batch* batch, int64_t* bytes);
+int ap_reference_init(ap_batch* batch, const float* data, const uint8_t* mask, int32_t known_mask,
+                      double* params, int32_t* status, void* workspace, int64_t workspace_bytes,
+                      ap_stream_t stream);
+
 /* Shifted, renormalised PSF of every stamp for value-space params (device):
  * out[n][(ky+2)*(kx+2)] packed with stride max_kp2 = (max ky + 2) * (max kx + 2)
  * (see ap_batch_psf_stride).  d_out (optional, may be NULL) receives d/d shift_x and

@@ -70,3 +70,17 @@ def load_adjoint(name):
     d["spec"] = json.loads(str(d["spec"]))
     return d
 
+
+
+def init_case_names():
+    return sorted(os.path.basename(p)[: -len(".npz")] for p in glob.glob(os.path.join(HERE, "init_*.npz")))
+
+
+def load_init(name):
+    """A reference ``initialize()`` case: data, mask (None when absent), spec (kind, nx, ny,
+    scale, given values) and the reference's values under ``value_<name>``."""
+    z = np.load(os.path.join(HERE, f"{name}.npz"))
+    d = {k: z[k] for k in z.files}
+    d["spec"] = json.loads(str(d["spec"]))
+    d["mask"] = d["mask"] if d["mask"].size else None
+    return d

@@ -3,7 +3,8 @@
 Run in a container that has the reference checkout (default path below, or
 ``ASTROPHOT_REFERENCE=<path>``):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py          # every case
+    python tests/golden/make_golden.py init     # only the initial-value cases
 
 The reference (AstroPhot 0.x) is imported through a ``sys.modules`` shim for
 the optional packages it imports at module level but never calls on this
@@ -518,8 +519,86 @@ def run_adjoint_case(ap, key, case):
                 disks=np.array([i[2] for i in init]), windows=np.array([w for _, w, _, _ in ADJOINT_PAIRS]))
 
 
+# --------------------------------------------------------------------------
+# the reference's initial-value heuristics (Model.initialize) on noisy stamps
+# --------------------------------------------------------------------------
+
+# truth rendered by the reference (PSF convolved) + flat sky, Gaussian noise; data rounded to
+# float32 so every implementation reads the same numbers; ``mask`` names a mask pattern.
+INIT_CASES = {
+    "init_sersic_64": dict(kind="sersic", nx=64, ny=64, scale=1.0, sky=1.0, noise=0.05, seed=11,
+                           params={"center": [31.7, 32.4], "q": 0.55, "PA": 0.9, "n": 2.5, "Re": 8.0, "Ie": 0.2}),
+    "init_sersic_offcentre": dict(kind="sersic", nx=64, ny=64, scale=1.0, sky=1.0, noise=0.05, seed=12,
+                                  params={"center": [24.3, 38.9], "q": 0.35, "PA": 2.6, "n": 1.2, "Re": 5.0, "Ie": 0.4}),
+    "init_sersic_rect": dict(kind="sersic", nx=64, ny=48, scale=1.0, sky=1.0, noise=0.03, seed=13,
+                             params={"center": [33.1, 23.6], "q": 0.8, "PA": 0.3, "n": 4.0, "Re": 6.0, "Ie": -0.3}),
+    "init_sersic_mask": dict(kind="sersic", nx=64, ny=64, scale=1.0, sky=1.0, noise=0.05, seed=14, mask="rows",
+                             params={"center": [30.6, 33.2], "q": 0.65, "PA": 1.9, "n": 1.8, "Re": 9.0, "Ie": 0.0}),
+    "init_exp_64": dict(kind="exponential", nx=64, ny=64, scale=1.0, sky=1.0, noise=0.05, seed=15,
+                        params={"center": [32.4, 31.1], "q": 0.5, "PA": 1.7, "Re": 7.0, "Ie": 0.3}),
+    "init_sersic_scale08": dict(kind="sersic", nx=56, ny=56, scale=0.8, sky=1.0, noise=0.05, seed=16,
+                                params={"center": [22.5, 21.9], "q": 0.7, "PA": 0.6, "n": 3.0, "Re": 5.0, "Ie": 0.1}),
+    "init_sersic_big": dict(kind="sersic", nx=96, ny=96, scale=1.0, sky=1.0, noise=0.02, seed=17,
+                            params={"center": [47.8, 48.3], "q": 0.6, "PA": 2.2, "n": 3.5, "Re": 16.0, "Ie": -0.2}),
+    "init_sersic_compact": dict(kind="sersic", nx=48, ny=48, scale=1.0, sky=1.0, noise=0.1, seed=18,
+                                params={"center": [23.9, 24.6], "q": 0.9, "PA": 0.1, "n": 1.0, "Re": 2.0, "Ie": 0.8}),
+    # parameters with values are inputs: no centre of light, no PA, the fit starts from n
+    "init_sersic_given": dict(kind="sersic", nx=64, ny=64, scale=1.0, sky=1.0, noise=0.05, seed=19,
+                              params={"center": [29.4, 35.2], "q": 0.45, "PA": 2.3, "n": 3.0, "Re": 7.0, "Ie": 0.1},
+                              given={"center": [29.5, 35.0], "PA": 2.25, "n": 2.8}),
+}
+
+
+def init_mask(kind, ny, nx, rng):
+    if kind is None:
+        return None
+    m = np.zeros((ny, nx), dtype=bool)
+    m[40:44, 10:50] = True
+    m[rng.integers(0, ny, 60), rng.integers(0, nx, 60)] = True
+    return m
+
+
+def run_init_case(ap, key, case):
+    """``model.initialize()`` of a Sérsic / exponential galaxy with no parameter values: the
+    centre-of-light, angular-centre PA, isophote q and binned-profile Nelder-Mead heuristics."""
+    from astrophot.models._shared_methods import _sample_image
+
+    rng = np.random.default_rng(case["seed"])
+    nx, ny, scale = case["nx"], case["ny"], case["scale"]
+    psf = psf_array(("moffat", 3.5, 3.0, 13), scale)
+    model_type = {"sersic": "sersic galaxy model", "exponential": "exponential galaxy model"}[case["kind"]]
+    blank = ap.image.Target_Image(data=np.zeros((ny, nx)), pixelscale=scale, psf=psf)
+    truth = ap.models.AstroPhot_Model(name=f"init truth {key}", model_type=model_type, target=blank,
+                                      parameters=dict(case["params"]), psf_mode="full")
+    img = truth().data.detach().cpu().numpy() + case["sky"] * scale**2
+    data = (img + case["noise"] * rng.normal(size=img.shape)).astype(np.float32).astype(np.float64)
+    mask = init_mask(case.get("mask"), ny, nx, rng)
+    kw = {} if mask is None else {"mask": mask}
+    target = ap.image.Target_Image(data=data, pixelscale=scale, psf=psf,
+                                   variance=np.full(data.shape, case["noise"] ** 2), **kw)
+    model = ap.models.AstroPhot_Model(name=f"init {key}", model_type=model_type, target=target, psf_mode="full",
+                                      parameters={k: (list(v) if isinstance(v, list) else v)
+                                                  for k, v in case.get("given", {}).items()})
+    model.initialize()
+    names = ["center", "q", "PA", "n", "Re", "Ie"] if case["kind"] == "sersic" else ["center", "q", "PA", "Re", "Ie"]
+    vals = {k: model[k].value.detach().cpu().numpy() for k in names}
+    R, I, S = _sample_image(target[model.window], model.transform_coordinates, model.radius_metric, model.parameters)
+    out = dict(data=data, mask=np.zeros((0, 0), bool) if mask is None else mask, profile_R=R, profile_I=I,
+               spec=json.dumps(case))
+    for k, v in vals.items():
+        out[f"value_{k}"] = v
+    return out
+
+
 def main():
     ap = import_reference()
+    only = sys.argv[1] if len(sys.argv) > 1 else None
+    for key, case in INIT_CASES.items():
+        out = run_init_case(ap, key, case)
+        np.savez_compressed(os.path.join(HERE, f"{key}.npz"), **out)
+        print("init", key, {k: out[k] for k in out if k.startswith("value_")})
+    if only == "init":
+        return
     for key, case in ADJOINT_CASES.items():
         out = run_adjoint_case(ap, key, case)
         np.savez_compressed(os.path.join(HERE, f"{key}.npz"), **out)

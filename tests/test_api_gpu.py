@@ -217,3 +217,23 @@ def test_multi_galaxy_group_matches_reference(ap, name):
     res = ap.fit.LM(grp, max_iter=d["spec"]["max_iter"]).fit()
     assert res.message == d["message"]
     assert abs(min(res.loss_history) / d["loss_history"].min() - 1) <= 1e-4
+
+
+@pytest.mark.parametrize("name", cases.init_case_names())
+def test_initialize_matches_reference(ap, name):
+    """``model.initialize()`` with no (or some) parameter values, as the reference's
+    ``tests/golden/init_*`` recorded it: centre of light, PA, isophote q, profile fit."""
+    d = cases.load_init(name)
+    spec = d["spec"]
+    kw = {} if d["mask"] is None else {"mask": d["mask"]}
+    tar = ap.image.Target_Image(data=d["data"], pixelscale=spec["scale"], variance=np.full(d["data"].shape, 0.0025), **kw)
+    kind = {"sersic": "sersic galaxy model", "exponential": "exponential galaxy model"}[spec["kind"]]
+    given = {k: (list(v) if isinstance(v, list) else v) for k, v in spec.get("given", {}).items()}
+    m = ap.models.AstroPhot_Model(name=f"api init {name}", model_type=kind, target=tar, parameters=given)
+    m.initialize()
+    names = ["center", "q", "PA", "n", "Re", "Ie"] if spec["kind"] == "sersic" else ["center", "q", "PA", "Re", "Ie"]
+    for k in names:
+        got = m[k].value.detach().cpu().numpy()
+        ref = d[f"value_{k}"]
+        tol = 1e-9 if k in ("center", "PA", "q") else 1e-3
+        assert np.max(np.abs(got - ref) / np.maximum(1.0, np.abs(ref))) <= tol, (k, got, ref)
