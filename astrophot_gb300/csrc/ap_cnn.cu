@@ -123,6 +123,14 @@ CnnWs cnn_layout(char* base, int64_t B) {
 constexpr int kBK = 32;
 constexpr int kSK = kBK + 8;  // smem row stride (bf16): 80 bytes, ldmatrix rows stay 16B aligned
 
+// Optional fused epilogue of a non-split GEMM: v = C + bias[s], ReLU, stored as bf16 into act
+// (same row stride as C) instead of C; or, without act, v = C + bias stored into C.
+struct GemmEpilogue {
+  const float* bias = nullptr;  // null: plain store of C
+  bf16* act = nullptr;
+  int relu = 0;
+};
+
 __device__ __forceinline__ void ldsm_x4(uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3, const void* p) {
   const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
   asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
@@ -168,7 +176,7 @@ __device__ __forceinline__ void load_tile(bf16 (*S)[kSK], const bf16* __restrict
 template <int BM, int BN, int WM, int WN, bool A_T, bool B_T>
 __global__ void __launch_bounds__(WM* WN * 32) k_gemm(const bf16* __restrict__ A, int lda, const bf16* __restrict__ B,
                                                       int ldb, float* __restrict__ C, int ldc, int R, int S, int T,
-                                                      int t_split, int atomic) {
+                                                      int t_split, int atomic, GemmEpilogue ep) {
   constexpr int NT = WM * WN * 32;
   constexpr int WTM = BM / WM, WTN = BN / WN;
   constexpr int TM = WTM / 16, TN = WTN / 8;
@@ -221,12 +229,20 @@ __global__ void __launch_bounds__(WM* WN * 32) k_gemm(const bf16* __restrict__ A
 #pragma unroll
         for (int e = 0; e < 2; ++e) {
           if (s + e >= S) continue;
-          float* p = C + (int64_t)r * ldc + s + e;
-          const float v = acc[i][j][h * 2 + e];
-          if (atomic)
-            atomicAdd(p, v);
-          else
-            *p = v;
+          const int64_t o = (int64_t)r * ldc + s + e;
+          float v = acc[i][j][h * 2 + e];
+          if (atomic) {
+            atomicAdd(C + o, v);
+          } else if (ep.bias) {
+            v += ep.bias[s + e];
+            if (ep.relu) v = fmaxf(v, 0.f);
+            if (ep.act)
+              ep.act[o] = __float2bfloat16(v);
+            else
+              C[o] = v;
+          } else {
+            C[o] = v;
+          }
         }
       }
 }
@@ -236,9 +252,11 @@ bool g_gemm_tune = false;
 std::mutex g_tune_mutex;
 std::map<std::tuple<int, int, int, int, int>, int> g_tuned;  // (A_T, B_T, R, S, T) -> tile shape
 
+// ep.bias set: the epilogue is fused when the reduction is not split; *fused tells the caller
 template <bool A_T, bool B_T>
 cudaError_t gemm(const bf16* A, int lda, const bf16* B, int ldb, float* C, int ldc, int R, int S, int T,
-                 cudaStream_t st) {
+                 cudaStream_t st, GemmEpilogue ep = GemmEpilogue(), bool* fused = nullptr) {
+  if (fused) *fused = false;
   if (R <= 0 || S <= 0 || T <= 0) return cudaSuccess;
   if (!g_num_sms) {
     int dev = 0;
@@ -265,7 +283,9 @@ cudaError_t gemm(const bf16* A, int lda, const bf16* B, int ldb, float* C, int l
       cudaError_t e = cudaMemsetAsync(C, 0, sizeof(float) * ((size_t)(R - 1) * ldc + S), st);
       if (e != cudaSuccess) return e;
     }
-    kern<<<dim3(gx, gy, split), threads, 0, st>>>(A, lda, B, ldb, C, ldc, R, S, T, t_split, split > 1 ? 1 : 0);
+    const GemmEpilogue use = split > 1 ? GemmEpilogue() : ep;
+    if (fused) *fused = (split == 1) && ep.bias != nullptr;
+    kern<<<dim3(gx, gy, split), threads, 0, st>>>(A, lda, B, ldb, C, ldc, R, S, T, t_split, split > 1 ? 1 : 0, use);
     return cudaGetLastError();
   };
   auto run_cfg = [&](int cfg) {
@@ -646,11 +666,19 @@ cudaError_t forward(const float* params, const bf16* wb, const float* x, int64_t
       const LayerDim dp = layer_dim(l - 1);
       k_im2col<<<grid_for(M * 9 * (d.cin / 8)), 256, 0, st>>>(w.act[l - 1], w.col[l], B, dp.hout, d.cin);
     }
-    e = gemm<false, false>(w.col[l], d.K, wb + w_off(l), d.K, w.pre[l], d.N, (int)M, d.N, d.K, st);
-    if (e != cudaSuccess) return e;
     const bool last = (l == kLayers - 1);
-    k_bias_act<<<grid_for(M * d.N), 256, 0, st>>>(w.pre[l], params + b_off(l), last ? nullptr : w.act[l],
-                                                  last ? w.out : nullptr, M, d.N, last ? 0 : 1);
+    // bias + ReLU + bf16 fused into the GEMM epilogue when the reduction is not split
+    GemmEpilogue ep;
+    ep.bias = params + b_off(l);
+    ep.act = last ? nullptr : w.act[l];
+    ep.relu = last ? 0 : 1;
+    float* cout = last ? w.out : w.pre[l];
+    bool fused = false;
+    e = gemm<false, false>(w.col[l], d.K, wb + w_off(l), d.K, cout, d.N, (int)M, d.N, d.K, st, ep, &fused);
+    if (e != cudaSuccess) return e;
+    if (!fused)
+      k_bias_act<<<grid_for(M * d.N), 256, 0, st>>>(cout, params + b_off(l), last ? nullptr : w.act[l],
+                                                    last ? w.out : nullptr, M, d.N, last ? 0 : 1);
   }
   return cudaGetLastError();
 }
