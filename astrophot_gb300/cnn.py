@@ -299,6 +299,16 @@ def moments_init(st: StampSet, n: int, sky_F: float = 0.0) -> torch.Tensor:
     return out
 
 
+def heuristic_init(st: StampSet, n: int, sky_F: float = 0.0) -> torch.Tensor:
+    """The reference's own initial values of every stamp (``Model.initialize()``: centre of
+    light, angular-centre PA, flattest-isophote q, n / Re / Ie from Nelder-Mead on the binned
+    median profile), computed by ``ap_reference_init``; the sky slot holds ``sky_F``."""
+    vals = torch.zeros((n, 8), dtype=torch.float64, device=st.data.device)
+    vals[:, 7] = sky_F
+    out, _ = st.batch.reference_init(st.data, None, vals, 0)
+    return out
+
+
 def _lm(st: StampSet, init: torch.Tensor, lm_options):
     b = st.batch
     rep = N.values_to_rep(init, 0x7F)
@@ -306,8 +316,8 @@ def _lm(st: StampSet, init: torch.Tensor, lm_options):
 
 
 def plain_fit(st: StampSet, n: int, lm_options=None):
-    """LM from the moments initial values."""
-    init = moments_init(st, n)
+    """The plain method: LM from the reference's heuristic initial values."""
+    init = heuristic_init(st, n)
     return init, _lm(st, init, lm_options or N.make_lm_options())
 
 

@@ -28,7 +28,7 @@
 namespace apgb {
 namespace {
 
-constexpr int kInitThreads = 256;
+constexpr int kInitThreads = 128;
 constexpr int kInitWarps = kInitThreads / 32;
 constexpr int kBins = 10;
 constexpr int kQSamples = 15;
@@ -41,7 +41,17 @@ struct InitGeom {
   double s, ox, oy, area;
 };
 
+// one stamp of a chunk waiting for its profile fit (each warp fits one stamp of the chunk)
+struct ChunkSlot {
+  double R[kBins], I[kBins], x0[3];
+  double cx, cy, q, PA;
+  int st;        // stamp index, -1: empty
+  int status;
+  int need_fit;
+};
+
 struct InitShared {
+  ChunkSlot slot[kInitWarps];
   double red[kInitWarps * 4];
   int ired[kInitWarps + 1];
   double d[8];
@@ -155,37 +165,62 @@ __device__ __forceinline__ int pow2_at_least(int n) {
   return p;
 }
 
+// Sorting runs on order-preserving 64-bit integer keys of the doubles (integer compares keep the
+// narrow FP64 pipe free): negative values map to ~bits, the rest to bits | sign; a positive NaN
+// sorts after +inf, as numpy's NaN-last order.
+__device__ __forceinline__ unsigned long long okey(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double okey_inv(unsigned long long k) {
+  return __longlong_as_double((long long)((k >> 63) ? (k & 0x7fffffffffffffffull) : ~k));
+}
+
+__device__ void to_keys(double* a, int P) {
+  unsigned long long* k = (unsigned long long*)a;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) k[i] = okey(a[i]);
+  __syncthreads();
+}
+__device__ void from_keys(double* a, int P) {
+  unsigned long long* k = (unsigned long long*)a;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) a[i] = okey_inv(k[i]);
+  __syncthreads();
+}
+
 // ascending bitonic sort of a[0, P) (P a power of two), NaN last
 __device__ void sort_keys(double* a, int P) {
-  for (int k = 2; k <= P; k <<= 1)
-    for (int j = k >> 1; j > 0; j >>= 1) {
+  to_keys(a, P);
+  unsigned long long* k = (unsigned long long*)a;
+  for (int sz = 2; sz <= P; sz <<= 1)
+    for (int j = sz >> 1; j > 0; j >>= 1) {
       for (int i = threadIdx.x; i < P; i += blockDim.x) {
         const int l = i ^ j;
         if (l > i) {
-          const double x = a[i], y = a[l];
-          const bool up = (i & k) == 0;
-          if (up ? lt_nan(y, x) : lt_nan(x, y)) {
-            a[i] = y;
-            a[l] = x;
+          const unsigned long long x = k[i], y = k[l];
+          if (((i & sz) == 0) ? (y < x) : (x < y)) {
+            k[i] = y;
+            k[l] = x;
           }
         }
       }
       __syncthreads();
     }
+  from_keys(a, P);
 }
 
 // ascending sort of (key, value) pairs by key
 __device__ void sort_pairs(double* key, double* val, int P) {
-  for (int k = 2; k <= P; k <<= 1)
-    for (int j = k >> 1; j > 0; j >>= 1) {
+  to_keys(key, P);
+  unsigned long long* k = (unsigned long long*)key;
+  for (int sz = 2; sz <= P; sz <<= 1)
+    for (int j = sz >> 1; j > 0; j >>= 1) {
       for (int i = threadIdx.x; i < P; i += blockDim.x) {
         const int l = i ^ j;
         if (l > i) {
-          const double x = key[i], y = key[l];
-          const bool up = (i & k) == 0;
-          if (up ? lt_nan(y, x) : lt_nan(x, y)) {
-            key[i] = y;
-            key[l] = x;
+          const unsigned long long x = k[i], y = k[l];
+          if (((i & sz) == 0) ? (y < x) : (x < y)) {
+            k[i] = y;
+            k[l] = x;
             const double t = val[i];
             val[i] = val[l];
             val[l] = t;
@@ -194,30 +229,33 @@ __device__ void sort_pairs(double* key, double* val, int P) {
       }
       __syncthreads();
     }
+  from_keys(key, P);
 }
 
 // ascending sort of (bin, value) pairs, bins first
 __device__ void sort_binned(uint8_t* bin, double* val, int P) {
-  for (int k = 2; k <= P; k <<= 1)
-    for (int j = k >> 1; j > 0; j >>= 1) {
+  to_keys(val, P);
+  unsigned long long* k = (unsigned long long*)val;
+  for (int sz = 2; sz <= P; sz <<= 1)
+    for (int j = sz >> 1; j > 0; j >>= 1) {
       for (int i = threadIdx.x; i < P; i += blockDim.x) {
         const int l = i ^ j;
         if (l > i) {
           const uint8_t bx = bin[i], by = bin[l];
-          const double x = val[i], y = val[l];
-          const bool lx = bx < by || (bx == by && lt_nan(x, y));  // (bx, x) < (by, y)
-          const bool ly = by < bx || (by == bx && lt_nan(y, x));
-          const bool up = (i & k) == 0;
-          if (up ? ly : lx) {
+          const unsigned long long x = k[i], y = k[l];
+          const bool lx = bx < by || (bx == by && x < y);  // (bx, x) < (by, y)
+          const bool ly = by < bx || (by == bx && y < x);
+          if (((i & sz) == 0) ? ly : lx) {
             bin[i] = by;
             bin[l] = bx;
-            val[i] = y;
-            val[l] = x;
+            k[i] = y;
+            k[l] = x;
           }
         }
       }
       __syncthreads();
     }
+  from_keys(val, P);
 }
 
 // ``Sigma_Clip_Upper`` on sorted values (one thread): lim = median + nsigma iqr/2 of the
@@ -294,88 +332,100 @@ __device__ double interp_periodic(double x, const double* xp, const double* fp, 
 // -- the isophote sampler -------------------------------------------------------------------
 
 struct IsoBuf {
-  double *x, *y, *th, *fl, *srt, *k2, *v2;  // [cap] each
+  double *x, *y, *t, *fl, *srt, *k2, *v2;  // [cap] each; t = ellipse parameter of the sample
   int cap;
 };
 
-__device__ __forceinline__ double img_at(const float* d, int nx, int r, int c, double sub) {
-  return (double)d[(int64_t)r * nx + c] - sub;
+// Python's a % 2pi for a in (-2pi, 4pi): fmod is exact there, so this is the same number
+__device__ __forceinline__ double mod_2pi(double a) {
+  if (a < 0) return a + kTwoPi;
+  if (a >= kTwoPi) return a - kTwoPi;
+  return a;
 }
 
-// normalised Lanczos (scale 5) at (X, Y) of img = data - sub (``interpolate_Lanczos``)
-__device__ double lanczos5(const InitShared& S, const float* d, int nx, int ny, double sub, double X, double Y) {
+// the reference's isophote angle of ellipse parameter t: atan(q tan t) (+ pi where cos t < 0),
+// rotated by pa, mod 2 pi (extract.py:136, 148)
+__device__ __forceinline__ double iso_theta(double t, double q, double pa) {
+  double st, ct;
+  sincos(t, &st, &ct);
+  const double th = atan(q * (st / ct)) + kPi * (ct < 0 ? 1.0 : 0.0);
+  return mod_2pi(th + pa);
+}
+
+// normalised Lanczos (scale 5) at (X, Y) of the float64 image img (``interpolate_Lanczos``):
+// separable weights sinc(u) sinc(u / 5), u = (k - X) + floor(X), k = -4..5, over the taps that
+// fall inside the image.  sin(pi u) = -(-1)^k sin(pi f) and sin(pi u / 5) by angle addition; the
+// ten reciprocals of one axis come from one division (running products).
+__device__ double lanczos5(const InitShared& S, const double* img, int nx, int ny, double X, double Y) {
   const double fx = floor(X), fy = floor(Y);
   const int ix = (int)fx, iy = (int)fy;
-  const int bx0 = max(0, ix - 4), bx1 = min(nx, ix + 6);
-  const int by0 = max(0, iy - 4), by1 = min(ny, iy + 6);
-  // sinc(t) sinc(t / 5) at t = (k - X) + floor(X), k = -4..5, from sin(pi t) = -(-1)^k sin(pi f)
-  // and sin(pi t / 5) by angle addition
   double L[2][10];
-  const double f[2] = {X - fx, Y - fy};
 #pragma unroll
   for (int a = 0; a < 2; ++a) {
     const double base = a == 0 ? X : Y;
     const double fl = a == 0 ? fx : fy;
-    const double sp = sinpi(f[a]);
+    const double f = base - fl;
+    const double sp = sinpi(f);
     double s5, c5;
-    sincospi(f[a] / 5.0, &s5, &c5);
+    sincospi(f / 5.0, &s5, &c5);
+    double num[10], den[10], pre[10];
+    double run = 1.0;
 #pragma unroll
     for (int k = 0; k < 10; ++k) {
-      const double t = ((double)(k - 4) - base) + fl;
-      if (t == 0.0) {
-        L[a][k] = 1.0;
-      } else {
-        const double sgn = ((k - 4) & 1) ? 1.0 : -1.0;  // -(-1)^k
-        const double st = sgn * sp;
-        const double st5 = S.sin5[k] * c5 - S.cos5[k] * s5;  // sin(pi (k - f) / 5)
-        const double y1 = kPi * t, y5 = kPi * (t / 5.0);
-        L[a][k] = (st / y1) * (st5 / y5);
-      }
+      const double u = ((double)(k - 4) - base) + fl;
+      const double sgn = ((k - 4) & 1) ? 1.0 : -1.0;  // -(-1)^k
+      num[k] = (sgn * sp) * (S.sin5[k] * c5 - S.cos5[k] * s5);
+      den[k] = u == 0.0 ? 1.0 : (kPi * u) * (kPi * (u / 5.0));
+      if (u == 0.0) num[k] = 1.0;
+      pre[k] = run;
+      run *= den[k];
+    }
+    double inv = 1.0 / run;
+#pragma unroll
+    for (int k = 9; k >= 0; --k) {
+      L[a][k] = num[k] * (inv * pre[k]);
+      inv *= den[k];
     }
   }
-  double num = 0.0, den = 0.0;
+  const int bx0 = max(0, ix - 4), bx1 = min(nx, ix + 6);
+  const int by0 = max(0, iy - 4), by1 = min(ny, iy + 6);
+  double sx = 0.0, sy = 0.0, acc = 0.0;
+  for (int c = bx0; c < bx1; ++c) sx += L[0][c - (ix - 4)];
   for (int r = by0; r < by1; ++r) {
+    const double* row = img + (int64_t)r * nx;
+    double rs = 0.0;
+    for (int c = bx0; c < bx1; ++c) rs = fma(L[0][c - (ix - 4)], row[c], rs);
     const double ly = L[1][r - (iy - 4)];
-    for (int c = bx0; c < bx1; ++c) {
-      const double w = L[0][c - (ix - 4)] * ly;
-      num += img_at(d, nx, r, c, sub) * w;
-      den += w;
-    }
+    acc = fma(ly, rs, acc);
+    sy += ly;
   }
-  return num / den;
+  return acc / (sx * sy);
 }
 
-// ``_iso_extract`` with sigma clipping (nsigma 3): fills B.fl[0, n) (and B.th) in ellipse order
-// and B.srt[0, n) with the same fluxes sorted; returns n.  *n_keep receives the number of
-// values the reference keeps (values below the clip limit: a prefix of srt), or n when it keeps
-// all.  With interp, clipped fluxes are replaced by periodic interpolation in angle (and srt is
-// not re-sorted: callers sort again).
-__device__ int iso_extract(InitShared& S, IsoBuf& B, const float* d, int nx, int ny, double sub, double sma,
-                           double q, double pa, double cx, double cy, bool interp, int* n_keep) {
+// ``_iso_extract`` with sigma clipping (nsigma 3) on img = data - edge median (float64, row-major):
+// fills B.fl[0, n) in ellipse order and B.srt[0, n) with the same fluxes sorted; returns n.
+// *n_keep receives the number of values the reference keeps (those below the clip limit: a
+// prefix of srt), or n when it keeps all.  With interp, clipped fluxes are replaced by periodic
+// interpolation in angle (srt is then stale: callers sort again).  Sample points are
+// sma (cos t, q sin t) rotated by pa, the reference's superellipse point for C = 2.
+__device__ int iso_extract(InitShared& S, IsoBuf& B, const double* img, int nx, int ny, double sma, double q,
+                           double pa, double cx, double cy, bool interp, int* n_keep) {
   const int N = max(15, (int)(((0.9 * 2) * kPi) * sma));
   const double stop = (2 * kPi) * (1.0 - 1.0 / N);
   const double step = stop / (double)(N - 1);
   const double sa = sin(pa), ca = cos(pa);
-  const double e = 1.0 - q;
-  const double a = 1.0 - e;
   int base = 0;
   for (int c0 = 0; c0 < N; c0 += blockDim.x) {
     const int k = c0 + threadIdx.x;
     bool keep = false;
-    double X = 0, Y = 0, th = 0;
+    double X = 0, Y = 0, t = 0;
     if (k < N) {
-      const double t = (k == N - 1) ? stop : (double)k * step;
-      const double ct = cos(t);
-      th = atan(q * tan(t)) + kPi * (ct < 0 ? 1.0 : 0.0);
-      const double cth = cos(th), sth = sin(th);
-      const double u = fabs(a * cth), v = fabs(sth);
-      const double rs = a / sqrt(u * u + v * v);
-      const double x0 = sma * (rs * cth), y0 = sma * (rs * sth);
-      X = ca * x0 - sa * y0;
-      Y = ca * y0 + sa * x0;
-      th = pymod(th + pa, kTwoPi);
-      X = X + cx;
-      Y = Y + cy;
+      t = (k == N - 1) ? stop : (double)k * step;
+      double st, ct;
+      sincos(t, &st, &ct);
+      const double x0 = sma * ct, y0 = sma * (q * st);
+      X = (ca * x0 - sa * y0) + cx;
+      Y = (ca * y0 + sa * x0) + cy;
       keep = X >= 0 && X < nx - 1 && Y >= 0 && Y < ny - 1;
     }
     int tot;
@@ -383,7 +433,7 @@ __device__ int iso_extract(InitShared& S, IsoBuf& B, const float* d, int nx, int
     if (keep) {
       B.x[base + slot] = X;
       B.y[base + slot] = Y;
-      B.th[base + slot] = th;
+      B.t[base + slot] = t;
     }
     base += tot;
   }
@@ -394,9 +444,9 @@ __device__ int iso_extract(InitShared& S, IsoBuf& B, const float* d, int nx, int
     double f = INFINITY;
     if (i < n) {
       if (sma < 30)
-        f = lanczos5(S, d, nx, ny, sub, B.x[i], B.y[i]);
+        f = lanczos5(S, img, nx, ny, B.x[i], B.y[i]);
       else
-        f = img_at(d, nx, (int)rint(B.y[i]), (int)rint(B.x[i]), sub);
+        f = img[(int64_t)(int)rint(B.y[i]) * nx + (int)rint(B.x[i])];
       B.fl[i] = f;
     }
     B.srt[i] = f;
@@ -430,7 +480,7 @@ __device__ int iso_extract(InitShared& S, IsoBuf& B, const float* d, int nx, int
       int tot;
       const int slot = block_compact(S, kp, tot);
       if (kp) {
-        B.k2[base2 + slot] = B.th[i];
+        B.k2[base2 + slot] = iso_theta(B.t[i], q, pa);
         B.v2[base2 + slot] = B.fl[i];
       }
       base2 += tot;
@@ -444,24 +494,34 @@ __device__ int iso_extract(InitShared& S, IsoBuf& B, const float* d, int nx, int
     __syncthreads();
     sort_pairs(B.k2, B.v2, P2);
     for (int i = threadIdx.x; i < n; i += blockDim.x)
-      if (!(B.fl[i] < lim)) B.fl[i] = interp_periodic(B.th[i], B.k2, B.v2, m);
+      if (!(B.fl[i] < lim)) B.fl[i] = interp_periodic(iso_theta(B.t[i], q, pa), B.k2, B.v2, m);
     __syncthreads();
   }
   return n;
 }
 
-// -- Nelder-Mead on the binned profile (warp 0, lanes 0-9 hold the bins) -----------------
+// -- Nelder-Mead on the binned profile (one warp per stamp) --------------------------------
+// The warp evaluates up to three simplex points at once: lanes 10 g .. 10 g + 9 hold the ten
+// profile bins of point g (g = 0, 1, 2).  The points an iteration may need (reflection,
+// expansion, outside contraction; the shrink's vertices) are evaluated side by side and used
+// in the order the sequential method asks for them, so the path and the evaluation count are
+// those of the sequential method.
 
 __device__ __forceinline__ double sersic_b(double n) {
-  return 2 * n - 1.0 / 3 + 4 / (405 * n) + 46 / (25515 * (n * n)) + 131 / (1148175 * pow(n, 3.0)) -
-         2194697 / (30690717750.0 * pow(n, 4.0));
+  // the n^3, n^4 terms are below 1e-4 of b(n): a last-bit difference there does not reach b(n)
+  const double n2 = n * n;
+  return 2 * n - 1.0 / 3 + 4 / (405 * n) + 46 / (25515 * n2) + 131 / (1148175 * (n2 * n)) -
+         2194697 / (30690717750.0 * (n2 * n2));
 }
 
-// mean of the 8 smallest squared log residuals (numpy: sort, drop the 2 largest, pairwise mean)
-__device__ double nm_objective(int kind, double R, double I, const double* x) {
+// mean of the 8 smallest squared log residuals of this lane group's point x (numpy: sort,
+// drop the 2 largest, pairwise mean); valid in the lanes of groups 0-2
+__device__ double nm_objective3(int kind, double R, double I, const double* x) {
   const int lane = threadIdx.x & 31;
+  const int g = lane / kBins, b = lane - g * kBins, base = g * kBins;
+  const bool live = g < 3;
   double r = INFINITY;
-  if (lane < kBins) {
+  if (live) {
     double lp;
     if (kind == AP_PROFILE_SERSIC) {
       const double n = x[0], Re = x[1], Ie = pow(10.0, x[2]);
@@ -477,17 +537,19 @@ __device__ double nm_objective(int kind, double R, double I, const double* x) {
     const double dlt = I - lp;
     r = dlt * dlt;
   }
-  // rank of each residual (NaN last, ties by lane)
+  // rank within the group on order-preserving integer keys (NaN last), ties by lane
+  const unsigned long long key = okey(r);
   int rank = 0;
   for (int m = 0; m < kBins; ++m) {
-    const double o = __shfl_sync(0xffffffffu, r, m);
-    if (lane < kBins && (lt_nan(o, r) || (m < lane && !lt_nan(r, o) && !lt_nan(o, r)))) ++rank;
+    const unsigned long long o = __shfl_sync(0xffffffffu, key, min(base + m, 31));
+    if (live && (o < key || (o == key && m < b))) ++rank;
   }
+  const unsigned gmask = live ? (0x3ffu << base) : 0u;
   double s[8];
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
-    const unsigned b = __ballot_sync(0xffffffffu, lane < kBins && rank == k);
-    s[k] = __shfl_sync(0xffffffffu, r, __ffs(b) - 1);
+    const unsigned bal = __ballot_sync(0xffffffffu, live && rank == k) & gmask;
+    s[k] = __shfl_sync(0xffffffffu, r, bal ? __ffs(bal) - 1 : lane);
   }
   return (((s[0] + s[1]) + (s[2] + s[3])) + ((s[4] + s[5]) + (s[6] + s[7]))) / 8.0;
 }
@@ -501,15 +563,23 @@ struct NMResult {
 __device__ NMResult nelder_mead(int kind, int dim, double R, double I, const double* x0) {
   constexpr double xatol = 1e-4, fatol = 1e-4;
   const int maxiter = 200 * dim, maxfev = 200 * dim;
+  const int g = (threadIdx.x & 31) / kBins;
   double sim[4][3], fs[4];
   int calls = 0;
   for (int j = 0; j <= dim; ++j)
-    for (int k = 0; k < dim; ++k) sim[j][k] = x0[k];
+    for (int k = 0; k < 3; ++k) sim[j][k] = k < dim ? x0[k] : 0.0;
   for (int k = 0; k < dim; ++k) sim[k + 1][k] = sim[k + 1][k] != 0 ? 1.05 * sim[k + 1][k] : 0.00025;
-  for (int j = 0; j <= dim; ++j) {
-    fs[j] = nm_objective(kind, R, I, sim[j]);
-    ++calls;
+  double cand[3];
+  // the first simplex: points 0-2 together, then point 3
+  for (int k = 0; k < 3; ++k) cand[k] = sim[min(g, dim)][k];
+  double f = nm_objective3(kind, R, I, cand);
+  for (int j = 0; j <= min(dim, 2); ++j) fs[j] = __shfl_sync(0xffffffffu, f, j * kBins);
+  if (dim == 3) {
+    for (int k = 0; k < 3; ++k) cand[k] = sim[3][k];
+    f = nm_objective3(kind, R, I, cand);
+    fs[3] = __shfl_sync(0xffffffffu, f, 0);
   }
+  calls = dim + 1;
   auto order = [&]() {  // stable insertion sort by value, NaN last
     for (int a = 1; a <= dim; ++a) {
       double fv = fs[a], xv[3];
@@ -526,7 +596,7 @@ __device__ NMResult nelder_mead(int kind, int dim, double R, double I, const dou
   };
   order();
   int it = 1;
-  double xr[3], xe[3], xc[3], xbar[3];
+  double xr[3], xe[3], xc[3], xbar[3], nsim[4][3];
   while (calls < maxfev && it < maxiter) {
     // convergence (np.max propagates NaN: then not converged)
     double dx = 0.0, df = 0.0;
@@ -543,61 +613,74 @@ __device__ NMResult nelder_mead(int kind, int dim, double R, double I, const dou
     }
     if (!nanx && dx <= xatol && df <= fatol) break;
     bool spent = false;
-    for (int k = 0; k < dim; ++k) {
-      double t = sim[0][k];
-      for (int j = 1; j < dim; ++j) t += sim[j][k];
-      xbar[k] = t / dim;
-      xr[k] = (1 + 1) * xbar[k] - 1 * sim[dim][k];
+    for (int k = 0; k < 3; ++k) {
+      if (k < dim) {
+        double t = sim[0][k];
+        for (int j = 1; j < dim; ++j) t += sim[j][k];
+        xbar[k] = t / dim;
+        xr[k] = (1 + 1) * xbar[k] - 1 * sim[dim][k];
+        xe[k] = (1 + 1 * 2) * xbar[k] - 1 * 2 * sim[dim][k];
+        xc[k] = (1 + 0.5 * 1) * xbar[k] - 0.5 * 1 * sim[dim][k];
+      } else {
+        xbar[k] = xr[k] = xe[k] = xc[k] = 0.0;
+      }
     }
-    const double fr = nm_objective(kind, R, I, xr);
+    for (int k = 0; k < 3; ++k) cand[k] = g == 0 ? xr[k] : (g == 1 ? xe[k] : xc[k]);
+    f = nm_objective3(kind, R, I, cand);
+    const double fr = __shfl_sync(0xffffffffu, f, 0);
+    const double fe = __shfl_sync(0xffffffffu, f, kBins);
+    const double fc = __shfl_sync(0xffffffffu, f, 2 * kBins);
     ++calls;
     if (fr < fs[0]) {
-      for (int k = 0; k < dim; ++k) xe[k] = (1 + 1 * 2) * xbar[k] - 1 * 2 * sim[dim][k];
       if (calls >= maxfev) {
         spent = true;
       } else {
-        const double fe = nm_objective(kind, R, I, xe);
         ++calls;
         const bool take_e = fe < fr;
-        for (int k = 0; k < dim; ++k) sim[dim][k] = take_e ? xe[k] : xr[k];
+        for (int k = 0; k < 3; ++k) sim[dim][k] = take_e ? xe[k] : xr[k];
         fs[dim] = take_e ? fe : fr;
       }
     } else if (fr < fs[dim - 1]) {
-      for (int k = 0; k < dim; ++k) sim[dim][k] = xr[k];
+      for (int k = 0; k < 3; ++k) sim[dim][k] = xr[k];
       fs[dim] = fr;
     } else {
       bool shrink = false;
       if (calls >= maxfev) {
         spent = true;
       } else if (fr < fs[dim]) {
-        for (int k = 0; k < dim; ++k) xc[k] = (1 + 0.5 * 1) * xbar[k] - 0.5 * 1 * sim[dim][k];
-        const double fc = nm_objective(kind, R, I, xc);
         ++calls;
         if (fc <= fr) {
-          for (int k = 0; k < dim; ++k) sim[dim][k] = xc[k];
+          for (int k = 0; k < 3; ++k) sim[dim][k] = xc[k];
           fs[dim] = fc;
         } else {
           shrink = true;
         }
       } else {
-        for (int k = 0; k < dim; ++k) xc[k] = (1 - 0.5) * xbar[k] + 0.5 * sim[dim][k];
-        const double fc = nm_objective(kind, R, I, xc);
+        double xcc[3];
+        for (int k = 0; k < 3; ++k) xcc[k] = k < dim ? (1 - 0.5) * xbar[k] + 0.5 * sim[dim][k] : 0.0;
+        f = nm_objective3(kind, R, I, xcc);
+        const double fcc = __shfl_sync(0xffffffffu, f, 0);
         ++calls;
-        if (fc < fs[dim]) {
-          for (int k = 0; k < dim; ++k) sim[dim][k] = xc[k];
-          fs[dim] = fc;
+        if (fcc < fs[dim]) {
+          for (int k = 0; k < 3; ++k) sim[dim][k] = xcc[k];
+          fs[dim] = fcc;
         } else {
           shrink = true;
         }
       }
       if (shrink) {
-        for (int j = 1; j <= dim && !spent; ++j) {
-          for (int k = 0; k < dim; ++k) sim[j][k] = sim[0][k] + 0.5 * (sim[j][k] - sim[0][k]);
+        for (int j = 1; j <= dim; ++j)
+          for (int k = 0; k < 3; ++k) nsim[j][k] = k < dim ? sim[0][k] + 0.5 * (sim[j][k] - sim[0][k]) : 0.0;
+        for (int k = 0; k < 3; ++k) cand[k] = nsim[min(g, dim - 1) + 1][k];
+        f = nm_objective3(kind, R, I, cand);
+        for (int j = 1; j <= dim; ++j) {
+          const double fj = __shfl_sync(0xffffffffu, f, (j - 1) * kBins);
+          for (int k = 0; k < 3; ++k) sim[j][k] = nsim[j][k];
           if (calls >= maxfev) {
             spent = true;
             break;
           }
-          fs[j] = nm_objective(kind, R, I, sim[j]);
+          fs[j] = fj;
           ++calls;
         }
       }
@@ -633,7 +716,7 @@ struct InitArgs {
   uint8_t* pix_bin_g;    // [grid][pix_cap]
 };
 
-__global__ void __launch_bounds__(kInitThreads) k_reference_init(InitArgs A) {
+__global__ void __launch_bounds__(kInitThreads, 4) k_reference_init(InitArgs A) {
   __shared__ InitShared S;
   extern __shared__ __align__(16) unsigned char dyn[];
   IsoBuf B;
@@ -641,7 +724,7 @@ __global__ void __launch_bounds__(kInitThreads) k_reference_init(InitArgs A) {
   double* dp = (double*)dyn;
   B.x = dp;
   B.y = dp + B.cap;
-  B.th = dp + 2 * B.cap;
+  B.t = dp + 2 * B.cap;
   B.fl = dp + 3 * B.cap;
   B.srt = dp + 4 * B.cap;
   B.k2 = dp + 5 * B.cap;
@@ -664,7 +747,15 @@ __global__ void __launch_bounds__(kInitThreads) k_reference_init(InitArgs A) {
   __syncthreads();
   const int lane = threadIdx.x & 31;
 
-  for (int st = blockIdx.x; st < A.n; st += gridDim.x) {
+  // chunks of kInitWarps stamps: every stage but the profile fit runs CTA-wide stamp by stamp,
+  // then the chunk's fits run side by side, one warp per stamp
+  for (int chunk = blockIdx.x; chunk * kInitWarps < A.n; chunk += gridDim.x) {
+  for (int j = 0; j < kInitWarps; ++j) {
+    const int st = chunk * kInitWarps + j;
+    if (st >= A.n) {
+      if (threadIdx.x == 0) S.slot[j].st = -1;
+      continue;
+    }
     const StampDev& sd = A.stamps[st];
     InitGeom g;
     g.nx = sd.nx;
@@ -782,9 +873,12 @@ __global__ void __launch_bounds__(kInitThreads) k_reference_init(InitArgs A) {
         const int r = i / nx, c = i % nx;
         const double X = ((c + 0.5) * g.s + g.ox) - cx, Y = ((r + 0.5) * g.s + g.oy) - cy;
         const double w = dat(r, c) - edge_avg;
-        const double t = atan2(Y, X);
-        v[0] += w * cos(2 * t);
-        v[1] += w * sin(2 * t);
+        // cos 2θ, sin 2θ of θ = atan2(Y, X) as (X² - Y²) / r², 2XY / r² (θ = 0 at r = 0)
+        const double r2 = X * X + Y * Y;
+        const double c2 = r2 > 0 ? (X * X - Y * Y) / r2 : 1.0;
+        const double s2 = r2 > 0 ? (2 * X * Y) / r2 : 0.0;
+        v[0] += w * c2;
+        v[1] += w * s2;
         v[2] += w;
       }
       block_sum4(S, v, 3);
@@ -800,13 +894,16 @@ __global__ void __launch_bounds__(kInitThreads) k_reference_init(InitArgs A) {
       const double ccx = icy, ccy = icx;  // the reference's transposed centre
       const double thr = 3 * edge_scatter;
       const double qmax = 0.9;
+      // the isophotes read data - edge median (raw data: masked pixels keep their values)
+      for (int i = threadIdx.x; i < npix; i += blockDim.x) pv[i] = (double)d[i] - edge_avg;
+      __syncthreads();
       double r = 1.0;
       int count = 1;
       while (r < fmax((double)nx, (double)ny) / 2) {
         r = r * (1 + 0.2);
         ++count;
         int nk;
-        const int n = iso_extract(S, B, d, nx, ny, edge_avg, r, qmax, pa, ccx, ccy, false, &nk);
+        const int n = iso_extract(S, B, pv, nx, ny, r, qmax, pa, ccx, ccy, false, &nk);
         if (nk < 3) continue;
         const double q80 = pct_sorted(B.srt, nk, 0.8);
         __syncthreads();
@@ -820,7 +917,7 @@ __global__ void __launch_bounds__(kInitThreads) k_reference_init(InitArgs A) {
       for (int qi = 0; qi < kQSamples; ++qi) {
         const double qv = qi == kQSamples - 1 ? 0.9 : qi * qstep + 0.2;
         int nk;
-        const int n = iso_extract(S, B, d, nx, ny, edge_avg, R, qv, pa, ccx, ccy, true, &nk);
+        const int n = iso_extract(S, B, pv, nx, ny, R, qv, pa, ccx, ccy, true, &nk);
         if (n < 3) {
           short_mask |= 1u << qi;
           continue;
@@ -887,6 +984,7 @@ __global__ void __launch_bounds__(kInitThreads) k_reference_init(InitArgs A) {
         const double X = ((c + 0.5) * g.s + g.ox) - cx, Y = ((r + 0.5) * g.s + g.oy) - cy;
         const double Xr = ca * X - sa * Y, Yr = (sa * X + ca * Y) / q;
         const double R = sqrt((Xr * Xr + Yr * Yr) + soft2);
+        pv[i] = R;  // read back by the binning pass (same thread, same index)
         mn = fmin(mn, R);
         mx = fmax(mx, R);
       }
@@ -905,9 +1003,7 @@ __global__ void __launch_bounds__(kInitThreads) k_reference_init(InitArgs A) {
         double v = INFINITY;
         if (i < npix) {
           const int r = i / nx, c = i % nx;
-          const double X = ((c + 0.5) * g.s + g.ox) - cx, Y = ((r + 0.5) * g.s + g.oy) - cy;
-          const double Xr = ca * X - sa * Y, Yr = (sa * X + ca * Y) / q;
-          const double R = sqrt((Xr * Xr + Yr * Yr) + soft2);
+          const double R = pv[i];
           int k = 0;  // searchsorted(edges, R, 'right') - 1
           while (k < kBins && S.edges[k + 1] <= R) ++k;
           if (R < S.edges[0]) k = -1;
@@ -963,55 +1059,83 @@ __global__ void __launch_bounds__(kInitThreads) k_reference_init(InitArgs A) {
       }
       __syncthreads();
       status |= S.i[2];
-      if (threadIdx.x < 32) {
-        double x0[3];
-        if (A.kind == AP_PROFILE_SERSIC) {
-          x0[0] = 2.0;
-          x0[1] = S.prof_R[4];
-          x0[2] = S.prof_I[4];
-        } else {
-          x0[0] = S.prof_R[4];
-          x0[1] = S.prof_I[4];
-          x0[2] = 0.0;
-        }
-        for (int k = 0; k < dim; ++k)
-          if ((A.known >> fslot[k]) & 1) x0[k] = prm[fslot[k]];
-        const double Rb = lane < kBins ? S.prof_R[lane] : 0.0;
-        const double Ib = lane < kBins ? S.prof_I[lane] : 0.0;
-        const NMResult res = nelder_mead(A.kind, dim, Rb, Ib, x0);
-        if (lane == 0) {
-          double fit[3];
-          for (int k = 0; k < 3; ++k) fit[k] = res.success ? res.x[k] : x0[k];
-          if (!res.success) S.i[3] = AP_INIT_FIT_LIMIT;
-          else S.i[3] = 0;
-          if (A.kind == AP_PROFILE_SERSIC) {
-            S.d[4] = soft_hi(soft_lo(fit[0], 0.36), 8.0);
-            S.d[5] = soft_lo(fit[1], 0.0);
-            S.d[6] = fit[2];
-          } else {
-            S.d[5] = soft_lo(fit[0], 0.0);
-            S.d[6] = fit[1];
-          }
-        }
-      }
-      __syncthreads();
-      status |= S.i[3];
     }
 
-    // 6. write the values that were not given
+    // 6. park the stamp until its chunk's fits run
     if (threadIdx.x == 0) {
-      if (!know_c) {
-        prm[PX] = cx;
-        prm[PY] = cy;
-      }
-      if (!know_pa) prm[PPA] = PA;
-      if (!know_q) prm[PQ] = q;
-      if (need_fit)
+      ChunkSlot& cs = S.slot[j];
+      cs.st = st;
+      cs.cx = cx;
+      cs.cy = cy;
+      cs.q = q;
+      cs.PA = PA;
+      cs.status = status;
+      cs.need_fit = need_fit ? 1 : 0;
+      if (need_fit) {
+        for (int k = 0; k < kBins; ++k) {
+          cs.R[k] = S.prof_R[k];
+          cs.I[k] = S.prof_I[k];
+        }
+        if (A.kind == AP_PROFILE_SERSIC) {
+          cs.x0[0] = 2.0;
+          cs.x0[1] = S.prof_R[4];
+          cs.x0[2] = S.prof_I[4];
+        } else {
+          cs.x0[0] = S.prof_R[4];
+          cs.x0[1] = S.prof_I[4];
+          cs.x0[2] = 0.0;
+        }
         for (int k = 0; k < dim; ++k)
-          if (!((A.known >> fslot[k]) & 1)) prm[fslot[k]] = S.d[4 + (fslot[k] - PN)];
-      A.status[st] = status;
+          if ((A.known >> fslot[k]) & 1) cs.x0[k] = prm[fslot[k]];
+      }
     }
     __syncthreads();
+  }
+
+  __syncthreads();
+  // 7. Nelder-Mead on the binned profiles, one warp per stamp, and the values written out
+  {
+    const int w = threadIdx.x >> 5;
+    const ChunkSlot& cs = S.slot[w];
+    if (cs.st >= 0) {
+      const int dim = A.kind == AP_PROFILE_SERSIC ? 3 : 2;
+      const int pslot[3] = {PN, PRE, PIE};
+      const int* fslot = A.kind == AP_PROFILE_SERSIC ? pslot : pslot + 1;
+      double* prm = A.params + (int64_t)cs.st * NPARAM;
+      int status = cs.status;
+      double fitv[3] = {0, 0, 0};
+      if (cs.need_fit) {
+        // lanes 10 g + b hold bin b for the point of lane group g
+        const double Rb = lane < 3 * kBins ? cs.R[lane % kBins] : 0.0;
+        const double Ib = lane < 3 * kBins ? cs.I[lane % kBins] : 0.0;
+        const NMResult res = nelder_mead(A.kind, dim, Rb, Ib, cs.x0);
+        double fit[3];
+        for (int k = 0; k < 3; ++k) fit[k] = res.success ? res.x[k] : cs.x0[k];
+        if (!res.success) status |= AP_INIT_FIT_LIMIT;
+        if (A.kind == AP_PROFILE_SERSIC) {
+          fitv[0] = soft_hi(soft_lo(fit[0], 0.36), 8.0);
+          fitv[1] = soft_lo(fit[1], 0.0);
+          fitv[2] = fit[2];
+        } else {
+          fitv[0] = soft_lo(fit[0], 0.0);
+          fitv[1] = fit[1];
+        }
+      }
+      if (lane == 0) {
+        if ((A.known & 3) != 3) {
+          prm[PX] = cs.cx;
+          prm[PY] = cs.cy;
+        }
+        if (!((A.known >> PPA) & 1)) prm[PPA] = cs.PA;
+        if (!((A.known >> PQ) & 1)) prm[PQ] = cs.q;
+        if (cs.need_fit)
+          for (int k = 0; k < dim; ++k)
+            if (!((A.known >> fslot[k]) & 1)) prm[fslot[k]] = fitv[k];
+        A.status[cs.st] = status;
+      }
+    }
+  }
+  __syncthreads();
   }
 }
 
@@ -1051,7 +1175,8 @@ RefInitPlan plan_reference_init(const StampDev* host_stamps, int32_t n) {
       per < 1)
     per = 1;
   if (sms < 1) sms = 1;
-  P.grid = (int)std::max<long long>(1, std::min<long long>((long long)sms * per, n));
+  const long long chunks = ((long long)n + kInitWarps - 1) / kInitWarps;
+  P.grid = (int)std::max<long long>(1, std::min<long long>((long long)sms * per, chunks));
   P.scratch_bytes = P.pix_in_smem ? 0 : (int64_t)pix_bytes * P.grid;
   return P;
 }

@@ -318,7 +318,7 @@ class Galaxy_Model(Component_Model):
         out = out.cpu().numpy()[0]
         for name in missing:
             node = self.parameters[name]
-            val = out[SLOT[name]] if len(SLOT[name]) > 1 else out[SLOT[name][0]]
+            val = out[list(SLOT[name])] if len(SLOT[name]) > 1 else out[SLOT[name][0]]
             with Param_Unlock(node), Param_SoftLimits(node):
                 node.value = torch.as_tensor(val, dtype=config.ap_dtype)
 

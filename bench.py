@@ -109,11 +109,18 @@ def sample_indices(specs, k):
 
 
 def _oracle_fit(args):
-    """One LM fit with the oracle: (data, weight, psf, init8, truth8) -> (chi2, iters, seconds)."""
+    """One fit with the oracle: (data, weight, psf, init8, truth8) -> (chi2, iters, seconds).
+    Without init8 the fit starts from the reference's own ``initialize()`` heuristics (restated
+    in float64), as a reference user's fit does."""
     data, weight, psf, init, _ = args
     from oracle.lm import GroupProblem, LMOracle
     from oracle.render import PSF, Component, Window
 
+    if init is None:
+        from oracle.refinit import initialize
+
+        o = initialize(data, "sersic", 1.0)
+        init = (o["center"][0], o["center"][1], o["q"], o["PA"], o["n"], o["Re"], o["Ie"], 0.0)
     cx, cy, q, PA, n, Re, Ie, F = init
     gal = Component("sersic", {"center": [cx, cy], "q": q, "PA": PA, "n": n, "Re": Re, "Ie": Ie}, psf_mode="full")
     sky = Component("flat_sky", {"F": F}, locked=("F",))
@@ -483,9 +490,10 @@ def run_gpu_cutouts(args):
 def learned_sample_jobs(S, seed, idx, data_of=None, init_of=None):
     """Oracle LM jobs for stamps ``idx`` of the learned workload.  ``data_of(i)`` gives the
     (data, sigma) the GPU fitted; without it the stamp is re-rendered by the oracle with
-    numpy noise of the same sigma rule (same truth, PSF and SNR draws as the GPU's)."""
+    numpy noise of the same sigma rule (same truth, PSF and SNR draws as the GPU's).
+    ``init_of(i)`` gives the initial values; without it the fit starts from the reference's
+    ``initialize()`` heuristics, computed inside the timed worker."""
     from astrophot_gb300 import cnn
-    from oracle.init import moments_init
     from oracle.render import PSF, Component, Window, sample_group
 
     rng = np.random.default_rng(seed)
@@ -507,14 +515,15 @@ def learned_sample_jobs(S, seed, idx, data_of=None, init_of=None):
             sigma = math.sqrt(np.sum((model - 1.0) ** 2)) / snr[i]
             data = model + sigma * np.random.default_rng(seed * 7919 + 17 + int(i)).normal(size=model.shape)
         weight = np.full(data.shape, 1.0 / sigma**2)
-        init = init_of(i) if init_of is not None else moments_init(data, 1.0, sigma)
+        init = init_of(i) if init_of is not None else None  # None: the worker runs initialize()
         jobs.append((data, weight, psf, init, truth[i]))
     return jobs
 
 
 def run_reference_learned(args):
-    """--impl reference, learned workload: the plain method on the CPU (moments initial values,
-    then the float64 restatement of the reference LM) over all host cores on a bounded sample."""
+    """--impl reference, learned workload: the plain method on the CPU (the reference's
+    ``initialize()`` heuristics, then its LM, both restated in float64) over all host cores on a
+    bounded sample."""
     rank, world, _ = rank_info()
     if rank != 0:
         return
@@ -549,7 +558,7 @@ def run_reference_learned(args):
         "data": "synthetic",
         "config": {
             "workload": f"learned init: {args.stamps} held-out 64x64 Sersic stamps + sky, Moffat FWHM 2-5 px, "
-            "SNR 10-200; plain method (moments initial values, float64 LM)",
+            "SNR 10-200; plain method (the reference's initialize() heuristics, then float64 LM)",
             "sample": f"{len(jobs)} stamps evenly spaced over the workload, {min(cores, len(jobs))} processes",
         },
         "cpu_baseline": {
@@ -557,7 +566,7 @@ def run_reference_learned(args):
             "unit": "fits/s",
             "cores": min(cores, len(jobs)),
             "kind": "port",
-            "sample": f"{len(jobs)} stamps (float64 numpy restatement of the reference LM from moments values)",
+            "sample": f"{len(jobs)} stamps (float64 numpy restatement of the reference initialize() + LM)",
         },
         "e2e": {"value": value, "unit": "fits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "mean_iterations": float(np.mean([r[1] for r in res])),
