@@ -5,7 +5,9 @@ No counterpart in the reference: AstroPhot starts its LM from the heuristics of
 models/_shared_methods.py:116-166).  Here a 6-layer CNN (``ap_cnn_*`` in the C ABI, bf16
 tensor-core GEMMs with fp32 accumulation) proposes the 7 Sersic parameters; the LM starts from
 the proposal unless its chi^2 is worse than that of the moments initialiser
-(``ap_moments_init``), which is then used instead (the fallback).
+(``ap_moments_init``), which is then used instead.  LM's final chi^2 judges the outcome: a
+stamp left with a poor fit is fitted again by the plain method, LM from the reference's own
+heuristic initial values (``ap_reference_init``), and keeps the better of the two.
 
 Training data come only from the library's own renderer: Sersic stamps drawn from the C0
 parameter distributions (centre 32 + U(-1, 1), n ~ U(0.5, 4), Re ~ U(5, 20), q ~ U(0.3, 1),
@@ -29,6 +31,7 @@ from . import _native as N
 from .synthetic import moffat_rd, moffat_stamp
 
 __all__ = ("InitNet", "StampSet", "draw_stamp_params", "psf_bank", "make_stamps", "learned_fit", "plain_fit",
+           "heuristic_init", "subset",
            "WEIGHTS_PATH")
 
 IMG = 64
@@ -321,10 +324,29 @@ def plain_fit(st: StampSet, n: int, lm_options=None):
     return init, _lm(st, init, lm_options or N.make_lm_options())
 
 
-def learned_fit(net: InitNet, st: StampSet, n: int, lm_options=None):
-    """LM from the CNN proposal, or from the moments values where those have the lower chi^2."""
+def subset(st: StampSet, idx) -> StampSet:
+    """The stamps ``idx`` (host indices) of ``st`` as their own StampSet and plan."""
+    idx = np.asarray(idx, dtype=np.int64)
+    dev = st.data.device
+    shapes = st.batch.psf_shapes
+    off = np.concatenate([[0], np.cumsum([kx * ky for kx, ky in shapes])])
+    b = _stamp_batch([shapes[i] for i in idx], dev)
+    pix = torch.as_tensor((idx[:, None] * IMG * IMG + np.arange(IMG * IMG)[None, :]).reshape(-1), device=dev)
+    psf_idx = torch.as_tensor(np.concatenate([np.arange(off[i], off[i + 1]) for i in idx]), device=dev)
+    t = torch.as_tensor(idx, device=dev)
+    return StampSet(st.truth[idx], st.data[pix].contiguous(), st.weight[pix].contiguous(), st.psf[psf_idx].contiguous(),
+                    st.sigma[t].contiguous(), b)
+
+
+def learned_fit(net: InitNet, st: StampSet, n: int, lm_options=None, judge_sigma: float = 5.0):
+    """LM from the CNN proposal, or from the moments values where those have the lower chi^2;
+    then LM's final chi^2 judges the result: a stamp whose chi^2/ndf ends more than
+    ``judge_sigma`` standard deviations (sqrt(2 / ndf)) above 1 is fitted again by the plain
+    method (LM from the reference's heuristic initial values) and keeps the better fit.
+    Returns (initial values, which [0 proposal, 1 moments, 2 plain refit], LM results)."""
     lib = N.lib()
     b = st.batch
+    lmo = lm_options or N.make_lm_options()
     prop = net.propose(st.data, st.sigma, n)
     fall = moments_init(st, n)
     c_p = b.chi2(st.data, st.weight, None, b.render(prop, st.psf))
@@ -333,4 +355,22 @@ def learned_fit(net: InitNet, st: StampSet, n: int, lm_options=None):
     which = torch.empty(n, dtype=torch.int32, device=prop.device)
     N.check(lib.ap_select_init(N._ptr(prop), N._ptr(fall), N._ptr(c_p), N._ptr(c_f), n, N._ptr(init), N._ptr(which),
                                N._stream()), "ap_select_init")
-    return init, which, _lm(st, init, lm_options or N.make_lm_options())
+    state, chi2, iters, status = _lm(st, init, lmo)
+    ndf = IMG * IMG - 7  # unmasked pixels - free parameters
+    bad = torch.nonzero(chi2 > 1.0 + judge_sigma * math.sqrt(2.0 / ndf)).reshape(-1)
+    if bad.numel():
+        idx = bad.cpu().numpy()
+        sub = subset(st, idx)
+        h = heuristic_init(sub, len(idx))
+        s2, c2, i2, t2 = _lm(sub, h, lmo)
+        better = c2 < chi2[bad]
+        keep = bad[better]
+        if keep.numel():
+            sel = better.nonzero().reshape(-1)
+            state[keep] = s2[sel]
+            chi2[keep] = c2[sel]
+            iters[keep] = iters[keep] + i2[sel]
+            status[keep] = t2[sel]
+            init[keep] = h[sel]
+            which[keep] = 2
+    return init, which, (state, chi2, iters, status)

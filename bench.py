@@ -7,9 +7,12 @@ Workloads (one "step" = every stamp of the workload fitted once, from its initia
       FWHM ~ U(2, 5) px, side 4 FWHM rounded to odd), Gaussian noise of constant sigma at
       SNR ~ U(10, 200).
       A step = CNN proposal (bf16 tensor-core kernels) + moments fallback, chi^2 of both,
-      per-stamp selection, then one batched LM of all stamps (7 free parameters).
-      Reported beside it: the plain method = LM from the moments values, batched and one
-      stamp at a time.
+      per-stamp selection, one batched LM of all stamps (7 free parameters), then LM's final
+      chi^2 as the judge: stamps left more than 5 sigma above chi^2/ndf = 1 are fitted again by
+      the plain method and keep the better fit.
+      Reported beside it: the plain method = LM from the reference's own heuristic initial
+      values (initialize(): centre of light, PA, isophote q, profile Nelder-Mead, computed by
+      ap_reference_init), batched and one stamp at a time.
   cutouts -- N stamps (default 8192) with sides round(log-uniform(32, 256)) px, each one
       Sersic galaxy + a flat sky of 1.0 (locked), its own Moffat PSF (beta 3.5, FWHM ~
       U(2, 5) px, side = 4 FWHM rounded to odd), noise sigma = sqrt(model + 10), 7 free
@@ -643,7 +646,8 @@ def run_gpu_learned(args):
     status_h, iters_h, chi2_h = status.cpu().numpy(), iters.cpu().numpy(), chi2.cpu().numpy()
     converged = int(np.sum((status_h == N.LM_SUCCESS) | (status_h == N.LM_IMMOBILE)))
 
-    # ---- plain method on the GPU: moments values, batched and one stamp at a time ----------
+    # ---- plain method on the GPU: the reference's heuristic values, batched and one stamp at
+    # a time (the heuristic initialiser is inside the timed region) ----------------------------
     torch.cuda.synchronize()
     e0.record()
     for _ in range(args.steps):
@@ -651,6 +655,11 @@ def run_gpu_learned(args):
     e1.record()
     torch.cuda.synchronize()
     plain_ms = e0.elapsed_time(e1) / args.steps
+    e0.record()
+    cnn.heuristic_init(st, S)
+    e1.record()
+    torch.cuda.synchronize()
+    heur_ms = e0.elapsed_time(e1)
     stat_ph = stat_p.cpu().numpy()
     conv_p = int(np.sum((stat_ph == N.LM_SUCCESS) | (stat_ph == N.LM_IMMOBILE)))
     n_single = min(32, S)
@@ -671,7 +680,7 @@ def run_gpu_learned(args):
     t0 = time.perf_counter()
     conv_single = 0
     for i, ss in enumerate(singles):
-        ini = cnn.moments_init(ss, 1)
+        ini = cnn.heuristic_init(ss, 1)
         _, _, _, stt = cnn._lm(ss, ini, lmo)
         conv_single += int(stt.item() in (N.LM_SUCCESS, N.LM_IMMOBILE))
     torch.cuda.synchronize()
@@ -747,15 +756,17 @@ def run_gpu_learned(args):
         },
         "fits": {"total": int(total_all), "converged": int(converged_all),
                  "proposal_used": float(np.mean(which.cpu().numpy() == 0)),
+                 "plain_refits": int(np.sum(which.cpu().numpy() == 2)),
                  "mean_iterations": float(iters_h.mean()),
                  "status_counts": {N.LM_MESSAGES[k]: int(np.sum(status_h == k)) for k in np.unique(status_h)}},
         "plain": {
             "batched_fits_per_s": conv_p / (plain_ms * 1e-3),
             "batched_ms_per_step": plain_ms,
+            "heuristic_init_ms": heur_ms,
             "batched_mean_iterations": float(it_p.cpu().numpy().mean()),
             "batched_converged": conv_p,
             "single_fits_per_s": single_rate,
-            "single_sample": f"{n_single} stamps, one LM call per stamp, moments initial values",
+            "single_sample": f"{n_single} stamps, one initialiser + LM call per stamp, the reference's heuristic initial values",
             "learned_batched_over_plain_single": value / single_rate if single_rate else None,
             "learned_batched_over_plain_batched": value / (conv_p / (plain_ms * 1e-3)) if conv_p else None,
         },

@@ -244,3 +244,25 @@ def test_gemm_autotuner_keeps_results(N):
     lib.ap_cnn_autotune(0, ctypes.byref(n))
     assert n.value >= 6
     assert torch.allclose(out, ref, rtol=1e-3, atol=1e-3 * ref.abs().max().item())
+
+
+def test_learned_fit_refits_poor_stamps_with_the_plain_method(N):
+    """LM's final chi^2 judges the learned fit: flagged stamps are refitted from the reference's
+    heuristic values (``ap_reference_init``) and keep the better fit.  A threshold below every
+    chi^2 flags all stamps: each result is then the better of the two runs."""
+    from astrophot_gb300 import cnn
+
+    net = cnn.InitNet.load()
+    n = 48
+    st = cnn.make_stamps(n, seed=31337)
+    _, w0, (s0, c0, i0, t0) = cnn.learned_fit(net, st, n, judge_sigma=1e9)
+    assert not bool((w0 == 2).any())
+    init, w1, (s1, c1, i1, t1) = cnn.learned_fit(net, st, n, judge_sigma=-1e9)
+    _, (sp, cp, ip, tp) = cnn.plain_fit(st, n)
+    c0, c1, cp = c0.cpu().numpy(), c1.cpu().numpy(), cp.cpu().numpy()
+    w1 = w1.cpu().numpy()
+    assert np.allclose(c1, np.minimum(c0, cp), rtol=1e-12, atol=0)
+    refit = w1 == 2
+    assert np.array_equal(refit, cp < c0)
+    h = cnn.heuristic_init(st, n)
+    assert torch.equal(init[torch.as_tensor(refit, device=init.device)], h[torch.as_tensor(refit, device=h.device)])
