@@ -13,6 +13,8 @@ Workloads (one "step" = every stamp of the workload fitted once, from its initia
       Reported beside it: the plain method = LM from the reference's own heuristic initial
       values (initialize(): centre of light, PA, isophote q, profile Nelder-Mead, computed by
       ap_reference_init), batched and one stamp at a time.
+  init -- the reference's initial-value heuristics (initialize(), ap_reference_init) on the
+      learned workload's stamps: stamps/s, parity and the CPU oracle beside it.
   cutouts -- N stamps (default 8192) with sides round(log-uniform(32, 256)) px, each one
       Sersic galaxy + a flat sky of 1.0 (locked), its own Moffat PSF (beta 3.5, FWHM ~
       U(2, 5) px, side = 4 FWHM rounded to odd), noise sigma = sqrt(model + 10), 7 free
@@ -56,8 +58,8 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default="learned", choices=["learned", "cutouts", "crowded"])
-    p.add_argument("--stamps", type=int, default=None, help="65536 (learned) / 8192 (cutouts)")
+    p.add_argument("--workload", default="learned", choices=["learned", "cutouts", "crowded", "init"])
+    p.add_argument("--stamps", type=int, default=None, help="65536 (learned, init) / 8192 (cutouts)")
     p.add_argument("--seed", type=int, default=2024)
     p.add_argument("--cpu-sample", type=int, default=8, help="stamps fitted by the CPU baseline")
     p.add_argument("--rounds-per-sync", type=int, default=8)
@@ -69,7 +71,7 @@ def parse():
     p.add_argument("--crowded-iters", type=int, default=20)
     a = p.parse_args()
     if a.stamps is None:
-        a.stamps = 65536 if a.workload == "learned" else 8192
+        a.stamps = 65536 if a.workload in ("learned", "init") else 8192
     return a
 
 
@@ -281,6 +283,8 @@ class ClockSampler:
 def run_gpu(args):
     if args.workload == "learned":
         run_gpu_learned(args)
+    elif args.workload == "init":
+        run_gpu_init(args)
     elif args.workload == "crowded":
         import torch
 
@@ -903,11 +907,147 @@ def crowded_block(args, dev):
     }
 
 
+def _oracle_init(data):
+    """The reference's initialize() heuristics restated in float64 (oracle) on one stamp."""
+    from oracle.refinit import initialize
+
+    t = time.perf_counter()
+    o = initialize(data, "sersic", 1.0)
+    v = np.r_[o["center"], o["q"], o["PA"], o["n"], o["Re"], o["Ie"]]
+    return v, time.perf_counter() - t
+
+
+INIT_METRIC = "initial-value heuristics (the reference's initialize()) stamps/s"
+
+
+def run_gpu_init(args):
+    """--workload init: the reference's initialiser (``ap_reference_init``) on the learned
+    workload's stamps; value = stamps/s with the stamps resident in HBM, e2e through host
+    buffers; parity and the CPU baseline from the float64 oracle on --cpu-sample stamps."""
+    import torch
+
+    from astrophot_gb300 import cnn
+
+    rank, world, local = rank_info()
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", torch.cuda.current_device())
+    S = args.stamps
+    st = cnn.make_stamps(S, args.seed + 7919 * rank, device=dev)
+    data_h = st.data.cpu().pin_memory()
+    for _ in range(max(args.warmup, 0)):
+        cnn.heuristic_init(st, S)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record()
+        for _ in range(args.steps):
+            vals = cnn.heuristic_init(st, S)
+        e1.record()
+        torch.cuda.synchronize()
+    dev_ms = e0.elapsed_time(e1) / args.steps
+
+    def step_e2e():
+        ss = cnn.StampSet(st.truth, data_h.to(dev, non_blocking=True), st.weight, st.psf, st.sigma, st.batch)
+        return cnn.heuristic_init(ss, S).cpu()
+
+    step_e2e()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.steps):
+        step_e2e()
+    e1.record()
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    dev_ms, e2e_ms, _, total = aggregate_ranks(dev_ms, e2e_ms, S, S, dev)
+    if rank != 0:
+        return
+    line = {
+        "metric": INIT_METRIC,
+        "value": total / (dev_ms * 1e-3),
+        "unit": "stamps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": dev_ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": f"reference initialiser on {S} held-out 64x64 stamps of the learned workload per GPU",
+                   "stamps_per_gpu": S, "l2": "the stamps (1 GB at 65536) exceed the 129 MB L2"},
+        "clocks": clk.summary(),
+        "e2e": {"value": total / (e2e_ms * 1e-3), "unit": "stamps/s", "h2d_bytes_per_step": int(data_h.numel() * 4),
+                "d2h_bytes_per_step": int(S * 8 * 8)},
+        "gpu_launches": args.steps,
+    }
+    if not args.no_cpu:
+        k = min(args.cpu_sample, S)
+        idx = np.linspace(0, S - 1, k).round().astype(int)
+        data = st.data.view(S, 64, 64)[torch.as_tensor(idx, device=dev)].cpu().numpy().astype(np.float64)
+        got = vals.cpu().numpy()[idx, :7]
+        res = [_oracle_init(d) for d in data]
+        ref = np.array([r[0] for r in res])
+        secs = sum(r[1] for r in res)
+        err = np.abs(got - ref) / np.maximum(1.0, np.abs(ref))
+        line["cpu_baseline"] = {"value": k / secs, "unit": "stamps/s", "cores": 1, "kind": "port",
+                                "sample": f"{k} stamps, float64 numpy restatement of the reference initialize(), one core"}
+        line["parity"] = {"stamps": int(k), "q_equal": int(np.sum(got[:, 2] == ref[:, 2])),
+                          "max_rel_err_centre_pa": float(err[:, [0, 1, 3]].max()),
+                          "max_rel_err_n_re_ie": float(err[:, 4:].max())}
+    print(json.dumps(line), flush=True)
+
+
+def run_reference_init(args):
+    """--impl reference --workload init: the float64 restatement of the reference's initialize()
+    over all host cores on a bounded sample of the same stamps."""
+    rank, world, _ = rank_info()
+    if rank != 0:
+        return
+    from astrophot_gb300 import cnn  # noqa: F401  (stamp draws only; no GPU work)
+
+    cores = os.cpu_count() or 1
+    k = min(args.stamps, 4 * cores)
+    idx = list(np.linspace(0, args.stamps - 1, k).round().astype(int))
+    jobs = learned_sample_jobs(args.stamps, args.seed, idx)
+    datas = [j[0] for j in jobs]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(processes=min(cores, len(datas))) as pool:
+        if args.warmup > 0:
+            pool.map(_oracle_init, datas[: min(len(datas), cores)])
+        times = []
+        for _ in range(args.steps):
+            t = time.perf_counter()
+            pool.map(_oracle_init, datas)
+            times.append(time.perf_counter() - t)
+    dt = statistics.median(times)
+    value = len(datas) / dt
+    line = {
+        "impl": "reference", "metric": INIT_METRIC, "value": value, "unit": "stamps/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"reference initialiser on {args.stamps} held-out 64x64 stamps of the learned workload",
+                   "sample": f"{len(datas)} stamps evenly spaced over the workload, {min(cores, len(datas))} processes"},
+        "cpu_baseline": {"value": value, "unit": "stamps/s", "cores": min(cores, len(datas)), "kind": "port",
+                         "sample": f"{len(datas)} stamps (float64 numpy restatement of the reference initialize())"},
+        "e2e": {"value": value, "unit": "stamps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         if args.workload == "learned":
             run_reference_learned(args)
+        elif args.workload == "init":
+            run_reference_init(args)
         elif args.workload == "crowded":
             print(json.dumps({"impl": "reference", "workload": "crowded",
                               "unavailable": "the crowded-field block is a GPU-only secondary measurement"}))
