@@ -41,6 +41,9 @@ SAMPLING = {"midpoint": 0, "simpsons": 1, "quad": 2, "trapezoid": 3}
 INTEGRATE = {"none": 0, "threshold": 1}
 PSF_NONE, PSF_FULL, PSF_FULL_NOSHIFT = 0, 1, 2
 VJP_REPRESENTATION, VJP_REFERENCE_CENTER = 1, 2
+# psf_convolve_mode "fft": stamps whose convolution kernel side (PSF side + 2 with the bilinear
+# shift) is at least this are convolved by FFT, smaller ones directly (same numbers either way)
+FFT_MIN_KERNEL = 33
 # ap_reference_init status bits
 INIT_CENTRE_EDGE, INIT_FIT_LIMIT, INIT_NO_ISOPHOTE, INIT_NO_PROFILE = 1, 2, 4, 8
 
@@ -72,6 +75,7 @@ class ApOptions(ctypes.Structure):
         ("softening", ctypes.c_double),
         ("free_mask", ctypes.c_int32),
         ("has_sky", ctypes.c_int32),
+        ("fft_min_kernel", ctypes.c_int32),
     ]
 
 
@@ -226,6 +230,8 @@ def make_options(
     softening=1e-3,
     free_mask=0x7F,
     has_sky=False,
+    psf_convolve_mode="direct",
+    fft_min_kernel=None,
 ) -> ApOptions:
     o = ApOptions()
     if profile not in PROFILE:
@@ -264,6 +270,11 @@ def make_options(
     o.softening = float(softening)
     o.free_mask = int(free_mask)
     o.has_sky = 1 if has_sky else 0
+    if psf_convolve_mode not in ("fft", "direct"):
+        raise SpecificationConflict(f"unrecognized psf_convolve_mode: {psf_convolve_mode}")
+    if fft_min_kernel is None:
+        fft_min_kernel = FFT_MIN_KERNEL if psf_convolve_mode == "fft" else 0
+    o.fft_min_kernel = int(fft_min_kernel)
     return o
 
 

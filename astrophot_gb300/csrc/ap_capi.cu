@@ -19,7 +19,7 @@ int64_t align_up(int64_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
 struct Layout {
   int64_t stamps, evals, work_tiles, out_tiles, tables, work, aux, spsf, queue, recheck, amb, wlist,
       olist, slist, counters,
-      work_ctr, mean_acc, tile_acc, acc, total;
+      work_ctr, mean_acc, tile_acc, acc, fft_lists, fft_buf, preconv, total;
 };
 
 // Gauss-Legendre nodes (ascending) and weights for 1..5 points, closed forms.
@@ -98,6 +98,8 @@ struct ap_batch {
   int64_t out_pixels = 0, psf_pixels = 0, work_pixels = 0, spsf_total = 0;
   int32_t max_kp2 = 0;
   size_t conv_smem = 0;
+  std::vector<int32_t> fft_lists;  // stamp list, then the row / column-group / output-row prefixes
+  int64_t fft_buf_elems = 0, preconv_elems = 0;
   Layout L{};
   BatchArgs args{};
   bool bound = false;
@@ -120,6 +122,7 @@ namespace {
 
 int validate_options(const ap_options* o) {
   if (!o) return AP_ERR_ARG;
+  if (o->fft_min_kernel < 0) return AP_ERR_ARG;
   if (o->profile != AP_PROFILE_SERSIC && o->profile != AP_PROFILE_EXPONENTIAL) return AP_ERR_UNSUPPORTED;
   if (o->sampling_mode < AP_SAMPLING_MIDPOINT || o->sampling_mode > AP_SAMPLING_TRAPEZOID)
     return AP_ERR_UNSUPPORTED;
@@ -257,7 +260,25 @@ int ap_batch_create(ap_batch** out, int32_t n, const int32_t* nx, const int32_t*
     for (int t = 0; t < st.nto; ++t) b->out_tiles.push_back(s);
     tw += st.ntw;
     to += st.nto;
-    if (psf) {
+    if (psf && options->fft_min_kernel > 0 && std::max(st.kpx, st.kpy) >= options->fft_min_kernel) {
+      // FFT sides: powers of two >= working window + kernel - 1 (no wrap into the crop)
+      auto pow2 = [](int v) {
+        int p = 8;
+        while (p < v) p <<= 1;
+        return p;
+      };
+      const int fx = pow2(st.wnx + st.kpx - 1), fy = pow2(st.wny + st.kpy - 1);
+      if (fx <= kFftMaxSide && fy <= kFftMaxSide) {
+        st.fft_nx = fx;
+        st.fft_ny = fy;
+        st.fft_off = b->fft_buf_elems;
+        st.pre_off = b->preconv_elems;
+        b->fft_buf_elems += 2 * 6 * (int64_t)fx * fy;
+        b->preconv_elems += 2 * (3 + NGRAD) * (int64_t)st.nx * st.ny;
+        b->fft_lists.push_back(s);
+      }
+    }
+    if (psf && st.fft_nx == 0) {
       const size_t need = conv_smem_bytes(st.kpx, st.kpy);
       smem = std::max(smem, need);
     }
@@ -275,6 +296,28 @@ int ap_batch_create(ap_batch** out, int32_t n, const int32_t* nx, const int32_t*
   b->work_pixels = work_off;
   b->psf_pixels = psf_off;
   b->spsf_total = spsf_off;
+  // FFT work lists: [stamps (n_fft)] [row prefix (n_fft + 1)] [column-group prefix] [output-row prefix]
+  const int32_t n_fft = (int32_t)b->fft_lists.size();
+  int32_t fft_rows = 0, fft_cols = 0, fft_outs = 0, fft_max_nx = 0, fft_max_ny = 0;
+  if (n_fft > 0) {
+    std::vector<int32_t> lists(b->fft_lists);
+    std::vector<int32_t> rp(1, 0), cp(1, 0), op(1, 0);
+    for (int32_t s : b->fft_lists) {
+      const StampDev& st = b->stamps[s];
+      rp.push_back(rp.back() + st.fft_ny);
+      cp.push_back(cp.back() + st.fft_nx / 8);
+      op.push_back(op.back() + st.ny);
+      fft_max_nx = std::max(fft_max_nx, st.fft_nx);
+      fft_max_ny = std::max(fft_max_ny, st.fft_ny);
+    }
+    fft_rows = rp.back();
+    fft_cols = cp.back();
+    fft_outs = op.back();
+    lists.insert(lists.end(), rp.begin(), rp.end());
+    lists.insert(lists.end(), cp.begin(), cp.end());
+    lists.insert(lists.end(), op.begin(), op.end());
+    b->fft_lists = lists;
+  }
 
   // quadrature tables
   QuadTables& T = b->tables;
@@ -362,6 +405,9 @@ int ap_batch_create(ap_batch** out, int32_t n, const int32_t* nx, const int32_t*
   L.mean_acc = take(sizeof(double) * 2 * (int64_t)n);
   L.tile_acc = take(sizeof(double) * 2 * kNacc * (int64_t)b->out_tiles.size());
   L.acc = take(sizeof(double) * 2 * kNacc * (int64_t)n);
+  L.fft_lists = take(sizeof(int32_t) * std::max<int64_t>((int64_t)b->fft_lists.size(), 1));
+  L.fft_buf = take(sizeof(float2) * std::max<int64_t>(b->fft_buf_elems, 1));
+  L.preconv = take(sizeof(float) * std::max<int64_t>(b->preconv_elems, 1));
   L.total = o;
 
   BatchArgs& A = b->args;
@@ -384,6 +430,12 @@ int ap_batch_create(ap_batch** out, int32_t n, const int32_t* nx, const int32_t*
   A.softening64 = options->softening;
   A.work_pixels = b->work_pixels;
   A.out_pixels = b->out_pixels;
+  A.n_fft = n_fft;
+  A.fft_rows = fft_rows;
+  A.fft_cols = fft_cols;
+  A.fft_outs = fft_outs;
+  A.fft_max_nx = fft_max_nx;
+  A.fft_max_ny = fft_max_ny;
   *out = b;
   return AP_OK;
 }
@@ -457,6 +509,15 @@ int ap_batch_bind(ap_batch* b, void* workspace, int64_t bytes, ap_stream_t strea
   A.mean_acc = (double*)(ws + L.mean_acc);
   A.tile_acc = (double*)(ws + L.tile_acc);
   A.acc = (double*)(ws + L.acc);
+  if (A.n_fft > 0) {
+    const int32_t* fl = (const int32_t*)(ws + L.fft_lists);
+    A.fft_stamp = fl;
+    A.fft_row_pre = fl + A.n_fft;
+    A.fft_col_pre = fl + 2 * A.n_fft + 1;
+    A.fft_out_pre = fl + 3 * A.n_fft + 2;
+    A.fft_buf = (float2*)(ws + L.fft_buf);
+    A.preconv = (float*)(ws + L.preconv);
+  }
   int rc = AP_OK;
   rc = rc ? rc : check_cuda(cudaMemcpyAsync(ws + L.stamps, b->stamps.data(), sizeof(StampDev) * b->n, cudaMemcpyHostToDevice, s));
   rc = rc ? rc : check_cuda(cudaMemcpyAsync(ws + L.work_tiles, b->work_tiles.data(), sizeof(int32_t) * b->work_tiles.size(), cudaMemcpyHostToDevice, s));
@@ -465,6 +526,12 @@ int ap_batch_bind(ap_batch* b, void* workspace, int64_t bytes, ap_stream_t strea
   rc = rc ? rc : check_cuda(cudaMemsetAsync(ws + L.counters, 0, sizeof(uint32_t) * 16, s));
   rc = rc ? rc : check_cuda(cudaMemsetAsync(ws + L.work_ctr, 0, sizeof(unsigned long long) * 4, s));
   rc = rc ? rc : check_cuda(cudaMemsetAsync(ws + L.evals, 0, sizeof(EvalDev) * 2 * b->n, s));
+  if (A.n_fft > 0) {
+    rc = rc ? rc : check_cuda(cudaMemcpyAsync(ws + L.fft_lists, b->fft_lists.data(),
+                                              sizeof(int32_t) * b->fft_lists.size(), cudaMemcpyHostToDevice, s));
+    rc = rc ? rc : check_cuda(fft_upload_twiddles(s));
+    rc = rc ? rc : check_cuda(set_fft_smem());
+  }
   rc = rc ? rc : check_cuda(cudaStreamSynchronize(s));
   if (!rc && b->conv_smem > 48 * 1024) rc = check_cuda(set_conv_smem(b->conv_smem));
   b->ws = ws;

@@ -112,6 +112,12 @@ struct StampDev {
   double pixel_area;
   float Pf[4], Pinvf[4];  // FP32 copies for the per-pixel paths
   double thr_numel;       // pixel count of the integration threshold (default: working window)
+  // PSF convolution by FFT (large kernels): transform sides (powers of two, 0 = direct
+  // convolution), offset of the stamp's complex buffers [2 slots][6][fft_ny][fft_nx] and of its
+  // convolved planes [2 slots][3 + NGRAD][ny][nx]
+  int32_t fft_nx, fft_ny;
+  int64_t fft_off;
+  int64_t pre_off;
 };
 
 struct EvalDev {
@@ -184,6 +190,17 @@ struct BatchArgs {
   double* mean_acc;           // [n_stamps][2]
   double* tile_acc;           // [n_out_tiles][2][kNacc]
   double* acc;                // [n_stamps][2][kNacc]
+  // stamps convolved by FFT (ap_fft.cu): their list and prefix sums of transform rows, column
+  // groups and output rows; complex buffers and the convolved planes read by the convolve pass
+  int32_t n_fft;
+  int32_t fft_rows, fft_cols, fft_outs;  // totals of the three prefix lists
+  int32_t fft_max_nx, fft_max_ny;
+  const int32_t* fft_stamp;   // [n_fft]
+  const int32_t* fft_row_pre; // [n_fft + 1]
+  const int32_t* fft_col_pre; // [n_fft + 1]
+  const int32_t* fft_out_pre; // [n_fft + 1]
+  float2* fft_buf;
+  float* preconv;
 };
 
 // buffers of the convolve/accumulate pass

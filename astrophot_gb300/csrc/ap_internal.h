@@ -91,6 +91,13 @@ cudaError_t launch_damped_solve(int m, int p, const double* hess, const double* 
 cudaError_t launch_psf_export(const BatchArgs& b, float* out, float* d_out, int64_t stride,
                               cudaStream_t s);
 
+// PSF convolution by FFT (ap_fft.cu)
+constexpr int kFftMaxSide = 1024;  // largest transform side
+cudaError_t fft_upload_twiddles(cudaStream_t st);
+cudaError_t set_fft_smem();
+cudaError_t launch_fft_conv(const BatchArgs& b, int total_rows, int total_cols, int total_out, int max_nx,
+                            int max_ny, cudaStream_t s);
+
 // the reference's initial-value heuristics (ap_refinit.cu)
 constexpr size_t kRefInitSmemBudget = 200 * 1024;  // dynamic shared memory per CTA at most
 struct RefInitPlan {

@@ -158,7 +158,7 @@ __global__ void k_build_lists(BatchArgs b) {
   // algorithmic work of this evaluation (counted here, once, not per warp in the kernels):
   // convolution = 2 FLOP per kernel tap per convolved plane per output pixel
   const int ops = b.evals[t].ops;
-  if (b.psf_mode != AP_PSF_NONE) {
+  if (b.psf_mode != AP_PSF_NONE && st.fft_nx == 0) {  // (FFT-convolved stamps: not k_conv's work)
     const bool jac = (ops & OP_JAC) != 0, shiftmode = (b.psf_mode == AP_PSF_FULL);
     const int nconv = jac ? ((shiftmode ? 3 : 1) + (b.kind == AP_PROFILE_SERSIC ? 4 : 3) +
                              ((shiftmode && !(ops & OP_VJP_COORD)) ? 0 : 2))
@@ -1018,6 +1018,29 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
         }
       }
     }
+  } else if (st.fft_nx > 0) {
+    // planes convolved by the FFT pass (ap_fft.cu), same indices as below
+    const int64_t npix = (int64_t)st.nx * st.ny;
+    const float* pre = b.preconv + st.pre_off + (int64_t)slot * (3 + NGRAD) * npix;
+#pragma unroll
+    for (int o = 0; o < kConvRows; ++o) {
+      const int y = yb + o;
+      if (!(x < st.nx && y < st.ny)) continue;
+      const int64_t i = (int64_t)y * st.nx + x;
+      cv[0][o] = pre[i];
+      if (jac) {
+        if (shiftmode) {
+          cv[1][o] = pre[npix + i];
+          cv[2][o] = pre[2 * npix + i];
+        }
+#pragma unroll
+        for (int q = 0; q < NGRAD; ++q) {
+          if (shiftmode && !(ops & OP_VJP_COORD) && (q == GX || q == GY)) continue;
+          if (b.kind != AP_PROFILE_SERSIC && q == GN) continue;
+          cv[3 + q][o] = pre[(int64_t)(3 + q) * npix + i];
+        }
+      }
+    }
   } else {
     const int kpx = st.kpx, kpy = st.kpy, ks = conv_col_stride(kpy), kstride = kpx * ks;
     const int cx = (kpx - 1) / 2, cy = (kpy - 1) / 2;
@@ -1343,6 +1366,10 @@ cudaError_t launch_render_pass(const BatchArgs& b, const ConvIO& io, size_t conv
     E(t);
   }
   t = B(KC_CONV);
+  if (b.n_fft > 0) {
+    const cudaError_t fe = launch_fft_conv(b, b.fft_rows, b.fft_cols, b.fft_outs, b.fft_max_nx, b.fft_max_ny, s);
+    if (fe != cudaSuccess) return fe;
+  }
   const dim3 cgrid(grid(2 * (int64_t)b.n_out_tiles, knob(GK_CONV, 16)));
   switch (b.n_free) {
     case 0: k_conv<0><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;

@@ -525,7 +525,7 @@ class _Structure:
             psf_subpixel_shift=g.psf_subpixel_shift, integrate_max_depth=g.integrate_max_depth,
             integrate_gridding=g.integrate_gridding, integrate_quad_level=g.integrate_quad_level,
             sampling_tolerance=g.sampling_tolerance, softening=g.softening, free_mask=free,
-            has_sky=self.sky is not None)
+            has_sky=self.sky is not None, psf_convolve_mode=g.psf_convolve_mode)
 
     def full_params(self):
         v = np.zeros(8)
@@ -684,7 +684,7 @@ def _needs_scene(owner, components):
 
 
 _KNOBS = ("sampling_mode", "sampling_tolerance", "integrate_mode", "integrate_max_depth", "integrate_gridding",
-          "integrate_quad_level", "softening", "psf_subpixel_shift", "psf_mode")
+          "integrate_quad_level", "softening", "psf_subpixel_shift", "psf_convolve_mode", "psf_mode")
 
 
 def _scene_spec(owner, components):

@@ -837,7 +837,9 @@ def run_gpu_learned(args):
 def crowded_block(args, dev):
     """200 Sersic galaxies on a 1024 x 1024 image, 51 x 51 Gaussian PSF (sigma 2), sky 5.0,
     noise sigma = sqrt(model + 10), explicit per-galaxy windows; 1400 parameters fitted jointly
-    for 20 LM iterations.  Reports render Mpix/s, Jacobian build time and the LM run."""
+    for 20 LM iterations with the PSF convolved by FFT (the reference's default mode).  Reports
+    render Mpix/s, Jacobian build time and the LM run, and the same render / Jacobian with
+    direct convolution beside them."""
     import torch
 
     from astrophot_gb300 import scene as SC
@@ -853,28 +855,37 @@ def crowded_block(args, dev):
     data, weight = synthetic.add_noise(model, args.seed)
     del sc_t
     src_i = [SC.SceneSource("sersic", list(t), w) for t, w in zip(init, windows)]
-    sc = SC.Scene(size, size, src_i, psf, data, weight, sky=sky, device=dev)
-    rep = sc.representation()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    for _ in range(2):
-        sc.forward(rep)
-        sc.jacobian(rep)
-        sc.hess()
-    torch.cuda.synchronize()
     reps = 5
-    e0.record()
-    for _ in range(reps):
-        sc.forward(rep)
-    e1.record()
-    torch.cuda.synchronize()
-    fwd_ms = e0.elapsed_time(e1) / reps
-    e0.record()
-    for _ in range(reps):
-        sc.jacobian(rep)
-        H = sc.hess()
-    e1.record()
-    torch.cuda.synchronize()
-    jac_ms = e0.elapsed_time(e1) / reps
+
+    def timed(sc, rep):
+        for _ in range(2):
+            sc.forward(rep)
+            sc.jacobian(rep)
+            sc.hess()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            sc.forward(rep)
+        e1.record()
+        torch.cuda.synchronize()
+        fwd = e0.elapsed_time(e1) / reps
+        e0.record()
+        for _ in range(reps):
+            sc.jacobian(rep)
+            H = sc.hess()
+        e1.record()
+        torch.cuda.synchronize()
+        return fwd, e0.elapsed_time(e1) / reps, H
+
+    sc_d = SC.Scene(size, size, src_i, psf, data, weight, sky=sky, device=dev, options={"psf_convolve_mode": "direct"})
+    rep = sc_d.representation()
+    fwd_d, jac_d, _ = timed(sc_d, rep)
+    chi2_d = float(sc_d.chi2(sc_d.forward(rep)))
+    del sc_d
+    sc = SC.Scene(size, size, src_i, psf, data, weight, sky=sky, device=dev, options={"psf_convolve_mode": "fft"})
+    fwd_ms, jac_ms, H = timed(sc, rep)
+    chi2_f = float(sc.chi2(sc.forward(rep)))
     g = sc.jt(sc.residual(sc.forward(rep)))
     torch.cuda.synchronize()
     e0.record()
@@ -889,7 +900,7 @@ def crowded_block(args, dev):
     torch.cuda.synchronize()
     lm_s = time.perf_counter() - t0
     return {
-        "workload": f"{n_src} Sersic galaxies on a {size}x{size} image, 51x51 Gaussian PSF (sigma 2, direct "
+        "workload": f"{n_src} Sersic galaxies on a {size}x{size} image, 51x51 Gaussian PSF (sigma 2, FFT "
         "convolution), sky 5.0, explicit windows (half-size 4 Re + 3 sigma + 2), noise sqrt(model + 10); "
         f"{sc.P} parameters fitted jointly",
         "parameters": sc.P,
@@ -897,6 +908,8 @@ def crowded_block(args, dev):
         "render_ms": fwd_ms,
         "render_mpix_per_s": size * size / (fwd_ms * 1e-3) / 1e6,
         "jacobian_build_ms": jac_ms,
+        "direct_convolution": {"render_ms": fwd_d, "jacobian_build_ms": jac_d,
+                               "chi2_rel_diff_vs_fft": abs(chi2_f / chi2_d - 1)},
         "damped_solve_ms": solve_ms,
         "lm_iterations": lm.iterations,
         "lm_seconds": lm_s,

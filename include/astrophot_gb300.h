@@ -83,6 +83,10 @@ typedef struct ap_options {
   double softening;             /* reference default 1e-3 */
   int32_t free_mask;            /* bit i set: full-vector slot i is fitted */
   int32_t has_sky;              /* 1: a flat sky 10^F * pixel_area is added */
+  int32_t fft_min_kernel;       /* stamps whose convolution kernel side (with the shift
+                                   padding) is at least this are convolved by FFT
+                                   (psf_convolve_mode "fft", models/_model_methods.py:245-257);
+                                   0 = direct convolution for every stamp */
 } ap_options;
 
 typedef struct ap_lm_options {
