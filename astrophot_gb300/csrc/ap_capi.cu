@@ -296,7 +296,8 @@ int ap_batch_create(ap_batch** out, int32_t n, const int32_t* nx, const int32_t*
   b->work_pixels = work_off;
   b->psf_pixels = psf_off;
   b->spsf_total = spsf_off;
-  // FFT work lists: [stamps (n_fft)] [row prefix (n_fft + 1)] [column-group prefix] [output-row prefix]
+  // FFT work lists: [stamps (n_fft)] [row-block prefix (n_fft + 1)] [column-group prefix]
+  // [output row-block prefix]
   const int32_t n_fft = (int32_t)b->fft_lists.size();
   int32_t fft_rows = 0, fft_cols = 0, fft_outs = 0, fft_max_nx = 0, fft_max_ny = 0;
   if (n_fft > 0) {
@@ -304,9 +305,10 @@ int ap_batch_create(ap_batch** out, int32_t n, const int32_t* nx, const int32_t*
     std::vector<int32_t> rp(1, 0), cp(1, 0), op(1, 0);
     for (int32_t s : b->fft_lists) {
       const StampDev& st = b->stamps[s];
-      rp.push_back(rp.back() + st.fft_ny);
+      const int rb = fft_rows_per_block(st.fft_nx);
+      rp.push_back(rp.back() + (st.fft_ny + rb - 1) / rb);
       cp.push_back(cp.back() + st.fft_nx / 8);
-      op.push_back(op.back() + st.ny);
+      op.push_back(op.back() + (st.ny + rb - 1) / rb);
       fft_max_nx = std::max(fft_max_nx, st.fft_nx);
       fft_max_ny = std::max(fft_max_ny, st.fft_ny);
     }

@@ -150,6 +150,9 @@ struct EvalF {
 // autotuner, ap_batch_autotune)
 enum GridKnob { GK_SAMPLE = 0, GK_INTEGRATE = 1, GK_CONV = 2, GK_PSF = 3, GK_COUNT = 4 };
 
+// rows of an FFT side-nx transform taken by one CTA of the row passes (1024 complex values)
+__host__ __device__ inline int fft_rows_per_block(int nx) { return nx >= 1024 ? 1 : 1024 / nx; }
+
 struct BatchArgs {
   int32_t grid_mult[GK_COUNT];  // blocks per SM of sample/select, level 1-3, convolve, PSF shift
   int32_t n_stamps;
@@ -193,12 +196,13 @@ struct BatchArgs {
   // stamps convolved by FFT (ap_fft.cu): their list and prefix sums of transform rows, column
   // groups and output rows; complex buffers and the convolved planes read by the convolve pass
   int32_t n_fft;
-  int32_t fft_rows, fft_cols, fft_outs;  // totals of the three prefix lists
+  int32_t fft_rows, fft_cols, fft_outs;  // totals of the three prefix lists (row blocks of
+                                         // fft_rows_per_block rows, 8-column groups, row blocks)
   int32_t fft_max_nx, fft_max_ny;
   const int32_t* fft_stamp;   // [n_fft]
-  const int32_t* fft_row_pre; // [n_fft + 1]
+  const int32_t* fft_row_pre; // [n_fft + 1] transform row blocks
   const int32_t* fft_col_pre; // [n_fft + 1]
-  const int32_t* fft_out_pre; // [n_fft + 1]
+  const int32_t* fft_out_pre; // [n_fft + 1] output row blocks
   float2* fft_buf;
   float* preconv;
 };

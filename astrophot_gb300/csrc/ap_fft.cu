@@ -14,8 +14,10 @@
 // accumulations afterwards).
 //
 // Transforms are radix-2, decimation in time, in shared memory after a bit-reversed load: one
-// CTA per row of one buffer, then one CTA per group of 8 columns.  FP32 with FP64-computed
-// twiddles.
+// CTA per transform row (every active buffer of both evaluation slots in turn; the inputs are
+// built in place), one CTA per group of 8 columns, the spectra products per row, the inverse
+// columns, and the inverse rows only for the kept rows, written straight into the convolved
+// planes.  FP32 with FP64-computed twiddles.
 #include <cmath>
 #include <vector>
 
@@ -84,198 +86,216 @@ __device__ __forceinline__ float2* fft_buffer(const BatchArgs& b, const StampDev
   return b.fft_buf + st.fft_off + (int64_t)(slot * kFftBufs + k) * st.fft_ny * st.fft_nx;
 }
 
-// in-place radix-2 DIT on n points of a bit-reversed array (one transform per block; thread t of
-// nt takes butterflies t, t + nt, ...); sign -1 forward, +1 inverse
-__device__ void dit_stages(float2* a, int n, bool inverse, int t, int nt) {
+// in-place radix-2 DIT of rows bit-reversed rows of n points each, back to back in a (thread t of
+// nt takes butterflies t, t + nt, ... over all rows); sign -1 forward, +1 inverse
+__device__ void dit_rows(float2* a, int n, int rows, bool inverse, int t, int nt) {
+  const int hn = n >> 1;
   for (int L = 2; L <= n; L <<= 1) {
     const int half = L >> 1;
     const int step = kFftMaxSide / L;
-    for (int j = t; j < n / 2; j += nt) {
+    for (int jj = t; jj < rows * hn; jj += nt) {
+      const int r = jj / hn, j = jj - r * hn;
       const int g = j / half, k = j - g * half;
+      float2* ar = a + r * n;
       const int i0 = g * L + k, i1 = i0 + half;
       float2 w = c_tw[k * step];
       if (inverse) w.y = -w.y;
-      const float2 u = a[i0], v = cmul(a[i1], w);
-      a[i0] = make_float2(u.x + v.x, u.y + v.y);
-      a[i1] = make_float2(u.x - v.x, u.y - v.y);
+      const float2 u = ar[i0], v = cmul(ar[i1], w);
+      ar[i0] = make_float2(u.x + v.x, u.y + v.y);
+      ar[i1] = make_float2(u.x - v.x, u.y - v.y);
     }
     __syncthreads();
   }
 }
 
-// -- pack the planes and kernels ------------------------------------------------------------
-__global__ void __launch_bounds__(kFftThreads) k_fft_pack(BatchArgs b) {
+// value of buffer k at transform position (y, x) before the transforms (kernels centred at 0,
+// planes at their working-window position, zero elsewhere)
+__device__ __forceinline__ float2 fft_input(const BatchArgs& b, const StampDev& st, const FftUse& u, int slot, int k,
+                                            int y, int x) {
+  if (k == FB_K0 || k == FB_K1) {
+    const int v = (y + st.kpy / 2) % st.fft_ny, uu = (x + st.kpx / 2) % st.fft_nx;  // y = (v - cy) mod Ny
+    if (v >= st.kpy || uu >= st.kpx) return make_float2(0.f, 0.f);
+    const int kp2 = st.kpx * st.kpy, ki = v * st.kpx + uu;
+    const float* ksrc = b.spsf + st.spsf_off + (int64_t)slot * 3 * kp2;
+    if (k == FB_K1) return make_float2(ksrc[2 * kp2 + ki], 0.f);
+    return make_float2(ksrc[ki], (u.jac && u.shift) ? ksrc[kp2 + ki] : 0.f);
+  }
+  if (y >= st.wny || x >= st.wnx) return make_float2(0.f, 0.f);
+  const float* w = b.work + st.work_off + (int64_t)y * st.wnx + x;
+  if (k == FB_D) return make_float2(w[work_plane(b, slot, 0)], 0.f);
+  const int p = k - FB_P1;
+  const int qa = u.part[2 * p];
+  const int qb = 2 * p + 1 < u.npart ? u.part[2 * p + 1] : -1;
+  return make_float2(w[work_plane(b, slot, 1 + qa)], qb >= 0 ? w[work_plane(b, slot, 1 + qb)] : 0.f);
+}
+
+// -- forward row transforms, the inputs built in place: one CTA per (stamp, block of rows) ---
+__global__ void __launch_bounds__(kFftThreads) k_fft_rows_fwd(BatchArgs b) {
+  extern __shared__ float2 sm[];
   const int j = fft_find(b.fft_row_pre, b.n_fft, blockIdx.x);
-  const int s = b.fft_stamp[j], slot = blockIdx.y;
-  const int ops = b.evals[s * 2 + slot].ops;
-  if (!ops) return;
+  const int s = b.fft_stamp[j];
   const StampDev& st = b.stamps[s];
-  const FftUse u = fft_use(b, ops);
-  const int y = blockIdx.x - b.fft_row_pre[j];
-  const int Nx = st.fft_nx, Ny = st.fft_ny;
-  const int kp2 = st.kpx * st.kpy;
-  const float* ksrc = b.spsf + st.spsf_off + (int64_t)slot * 3 * kp2;
-  const int cx = (st.kpx - 1) / 2, cy = (st.kpy - 1) / 2;
-  const int v = (y + cy) % Ny;  // kernel row at this transform row: y = (v - cy) mod Ny
-  const bool vrow = v < st.kpy;
-  const bool wrow = y < st.wny;
-  const float* work = b.work + st.work_off + (int64_t)y * st.wnx;
-  float2* K0 = fft_buffer(b, st, slot, FB_K0) + (int64_t)y * Nx;
-  float2* K1 = fft_buffer(b, st, slot, FB_K1) + (int64_t)y * Nx;
-  float2* D = fft_buffer(b, st, slot, FB_D) + (int64_t)y * Nx;
-  const bool two_k = u.jac && u.shift;
-  for (int x = threadIdx.x; x < Nx; x += blockDim.x) {
-    const int uu = (x + cx) % Nx;
-    const bool kin = vrow && uu < st.kpx;
-    const int ki = v * st.kpx + uu;
-    K0[x] = kin ? make_float2(ksrc[ki], two_k ? ksrc[kp2 + ki] : 0.f) : make_float2(0.f, 0.f);
-    if (two_k) K1[x] = make_float2(kin ? ksrc[2 * kp2 + ki] : 0.f, 0.f);
-    const bool win = wrow && x < st.wnx;
-    D[x] = make_float2(win ? work[work_plane(b, slot, 0) + x] : 0.f, 0.f);
-    for (int p = 0; p < (u.npart + 1) / 2; ++p) {
-      const int qa = u.part[2 * p];
-      const int qb = 2 * p + 1 < u.npart ? u.part[2 * p + 1] : -1;
-      float2* P = fft_buffer(b, st, slot, FB_P1 + p) + (int64_t)y * Nx;
-      const float a = win ? work[work_plane(b, slot, 1 + qa) + x] : 0.f;
-      const float c = (win && qb >= 0) ? work[work_plane(b, slot, 1 + qb) + x] : 0.f;
-      P[x] = make_float2(a, c);
+  const int Nx = st.fft_nx, bits = 31 - __clz(Nx);
+  const int rb = fft_rows_per_block(Nx);
+  const int y0 = (blockIdx.x - b.fft_row_pre[j]) * rb;
+  const int rows = min(rb, st.fft_ny - y0);
+  for (int slot = 0; slot < 2; ++slot) {
+    const int ops = b.evals[s * 2 + slot].ops;
+    if (!ops) continue;
+    const FftUse u = fft_use(b, ops);
+    for (int k = 0; k < kFftBufs; ++k) {
+      if (!((u.fwd >> k) & 1u)) continue;
+      float2* buf = fft_buffer(b, st, slot, k) + (int64_t)y0 * Nx;
+      for (int e = threadIdx.x; e < rows * Nx; e += blockDim.x) {
+        const int r = e / Nx, x = e - r * Nx;
+        sm[r * Nx + (__brev(x) >> (32 - bits))] = fft_input(b, st, u, slot, k, y0 + r, x);
+      }
+      __syncthreads();
+      dit_rows(sm, Nx, rows, false, threadIdx.x, blockDim.x);
+      for (int e = threadIdx.x; e < rows * Nx; e += blockDim.x) buf[e] = sm[e];
+      __syncthreads();
     }
   }
 }
 
-// -- row transforms: one CTA per (row, slot * kFftBufs + buffer) ----------------------------
-__global__ void __launch_bounds__(kFftThreads) k_fft_rows(BatchArgs b, int inverse) {
-  extern __shared__ float2 sm[];
-  const int j = fft_find(b.fft_row_pre, b.n_fft, blockIdx.x);
-  const int s = b.fft_stamp[j];
-  const int slot = blockIdx.y / kFftBufs, k = blockIdx.y - slot * kFftBufs;
-  const int ops = b.evals[s * 2 + slot].ops;
-  if (!ops) return;
-  const FftUse u = fft_use(b, ops);
-  if (!(((inverse ? u.inv : u.fwd) >> k) & 1u)) return;
-  const StampDev& st = b.stamps[s];
-  const int y = blockIdx.x - b.fft_row_pre[j];
-  const int Nx = st.fft_nx;
-  const int bits = 31 - __clz(Nx);
-  float2* row = fft_buffer(b, st, slot, k) + (int64_t)y * Nx;
-  for (int x = threadIdx.x; x < Nx; x += blockDim.x) sm[__brev(x) >> (32 - bits)] = row[x];
-  __syncthreads();
-  dit_stages(sm, Nx, inverse != 0, threadIdx.x, blockDim.x);
-  for (int x = threadIdx.x; x < Nx; x += blockDim.x) row[x] = sm[x];
-}
-
-// -- column transforms: one CTA per (group of 8 columns, slot * kFftBufs + buffer) ---------
+// -- column transforms: one CTA per (stamp, group of 8 columns), every active buffer ---------
 __global__ void __launch_bounds__(kFftThreads) k_fft_cols(BatchArgs b, int inverse) {
   extern __shared__ float2 sm[];
   const int j = fft_find(b.fft_col_pre, b.n_fft, blockIdx.x);
   const int s = b.fft_stamp[j];
-  const int slot = blockIdx.y / kFftBufs, k = blockIdx.y - slot * kFftBufs;
-  const int ops = b.evals[s * 2 + slot].ops;
-  if (!ops) return;
-  const FftUse u = fft_use(b, ops);
-  if (!(((inverse ? u.inv : u.fwd) >> k) & 1u)) return;
   const StampDev& st = b.stamps[s];
   const int x0 = (blockIdx.x - b.fft_col_pre[j]) * kColGroup;
   const int Nx = st.fft_nx, Ny = st.fft_ny;
   const int bits = 31 - __clz(Ny);
-  float2* buf = fft_buffer(b, st, slot, k);
-  // column c of the group lives at sm[c * Ny ...], rows bit-reversed
-  for (int e = threadIdx.x; e < kColGroup * Ny; e += blockDim.x) {
-    const int r = e / kColGroup, c = e - r * kColGroup;
-    sm[c * Ny + (__brev(r) >> (32 - bits))] = buf[(int64_t)r * Nx + x0 + c];
-  }
-  __syncthreads();
-  // the 8 columns' butterflies together: thread t takes column t % 8
   const int c = threadIdx.x % kColGroup, t = threadIdx.x / kColGroup, nt = blockDim.x / kColGroup;
-  float2* a = sm + c * Ny;
-  for (int L = 2; L <= Ny; L <<= 1) {
-    const int half = L >> 1;
-    const int step = kFftMaxSide / L;
-    for (int jj = t; jj < Ny / 2; jj += nt) {
-      const int g = jj / half, kk = jj - g * half;
-      const int i0 = g * L + kk, i1 = i0 + half;
-      float2 w = c_tw[kk * step];
-      if (inverse) w.y = -w.y;
-      const float2 p = a[i0], q = cmul(a[i1], w);
-      a[i0] = make_float2(p.x + q.x, p.y + q.y);
-      a[i1] = make_float2(p.x - q.x, p.y - q.y);
+  for (int slot = 0; slot < 2; ++slot) {
+    const int ops = b.evals[s * 2 + slot].ops;
+    if (!ops) continue;
+    const FftUse u = fft_use(b, ops);
+    for (int k = 0; k < kFftBufs; ++k) {
+      if (!(((inverse ? u.inv : u.fwd) >> k) & 1u)) continue;
+      float2* buf = fft_buffer(b, st, slot, k);
+      // column cc of the group lives at sm[cc * Ny ...], rows bit-reversed
+      for (int e = threadIdx.x; e < kColGroup * Ny; e += blockDim.x) {
+        const int r = e / kColGroup, cc = e - r * kColGroup;
+        sm[cc * Ny + (__brev(r) >> (32 - bits))] = buf[(int64_t)r * Nx + x0 + cc];
+      }
+      __syncthreads();
+      float2* a = sm + c * Ny;
+      for (int L = 2; L <= Ny; L <<= 1) {
+        const int half = L >> 1;
+        const int step = kFftMaxSide / L;
+        for (int jj = t; jj < Ny / 2; jj += nt) {
+          const int g = jj / half, kk = jj - g * half;
+          const int i0 = g * L + kk, i1 = i0 + half;
+          float2 w = c_tw[kk * step];
+          if (inverse) w.y = -w.y;
+          const float2 p = a[i0], q = cmul(a[i1], w);
+          a[i0] = make_float2(p.x + q.x, p.y + q.y);
+          a[i1] = make_float2(p.x - q.x, p.y - q.y);
+        }
+        __syncthreads();
+      }
+      for (int e = threadIdx.x; e < kColGroup * Ny; e += blockDim.x) {
+        const int r = e / kColGroup, cc = e - r * kColGroup;
+        buf[(int64_t)r * Nx + x0 + cc] = sm[cc * Ny + r];
+      }
+      __syncthreads();
     }
-    __syncthreads();
-  }
-  for (int e = threadIdx.x; e < kColGroup * Ny; e += blockDim.x) {
-    const int r = e / kColGroup, cc = e - r * kColGroup;
-    buf[(int64_t)r * Nx + x0 + cc] = sm[cc * Ny + r];
   }
 }
 
-// -- spectra products -----------------------------------------------------------------------
+// -- spectra products: one CTA per (stamp, block of rows) ----------------------------------
 __global__ void __launch_bounds__(kFftThreads) k_fft_mul(BatchArgs b) {
   const int j = fft_find(b.fft_row_pre, b.n_fft, blockIdx.x);
-  const int s = b.fft_stamp[j], slot = blockIdx.y;
-  const int ops = b.evals[s * 2 + slot].ops;
-  if (!ops) return;
+  const int s = b.fft_stamp[j];
   const StampDev& st = b.stamps[s];
-  const FftUse u = fft_use(b, ops);
-  const int y = blockIdx.x - b.fft_row_pre[j];
   const int Nx = st.fft_nx, Ny = st.fft_ny;
-  const int ym = (Ny - y) % Ny;
-  const float2* K0 = fft_buffer(b, st, slot, FB_K0);
-  float2* K1 = fft_buffer(b, st, slot, FB_K1) + (int64_t)y * Nx;
-  float2* D = fft_buffer(b, st, slot, FB_D) + (int64_t)y * Nx;
-  const bool two_k = u.jac && u.shift;
-  const int pairs = (u.npart + 1) / 2;
-  for (int x = threadIdx.x; x < Nx; x += blockDim.x) {
-    const int xm = (Nx - x) % Nx;
-    const float2 z = K0[(int64_t)y * Nx + x];
-    float2 FK = z, FX = make_float2(0.f, 0.f);
-    if (two_k) {
-      const float2 zm = K0[(int64_t)ym * Nx + xm];
-      // K^ = (Z(k) + conj Z(-k)) / 2, dKx^ = (Z(k) - conj Z(-k)) / 2i
-      FK = make_float2(0.5f * (z.x + zm.x), 0.5f * (z.y - zm.y));
-      FX = make_float2(0.5f * (z.y + zm.y), -0.5f * (z.x - zm.x));
-    }
-    const float2 d = D[x];
-    if (two_k) {
-      K1[x] = cmul(d, K1[x]);
-      const float2 m = make_float2(FK.x - FX.y, FK.y + FX.x);  // K^ + i dKx^
-      D[x] = cmul(d, m);
-    } else {
-      D[x] = cmul(d, FK);
-    }
-    for (int p = 0; p < pairs; ++p) {
-      float2* P = fft_buffer(b, st, slot, FB_P1 + p) + (int64_t)y * Nx;
-      P[x] = cmul(P[x], FK);
+  const int rb = fft_rows_per_block(Nx);
+  const int y0 = (blockIdx.x - b.fft_row_pre[j]) * rb;
+  const int rows = min(rb, Ny - y0);
+  for (int slot = 0; slot < 2; ++slot) {
+    const int ops = b.evals[s * 2 + slot].ops;
+    if (!ops) continue;
+    const FftUse u = fft_use(b, ops);
+    const float2* K0 = fft_buffer(b, st, slot, FB_K0);
+    float2* K1 = fft_buffer(b, st, slot, FB_K1);
+    float2* D = fft_buffer(b, st, slot, FB_D);
+    const bool two_k = u.jac && u.shift;
+    const int pairs = (u.npart + 1) / 2;
+    for (int e = threadIdx.x; e < rows * Nx; e += blockDim.x) {
+      const int r = e / Nx, x = e - r * Nx;
+      const int y = y0 + r;
+      const int64_t i = (int64_t)y * Nx + x;
+      const float2 z = K0[i];
+      float2 FK = z, FX = make_float2(0.f, 0.f);
+      if (two_k) {
+        const float2 zm = K0[(int64_t)((Ny - y) % Ny) * Nx + (Nx - x) % Nx];
+        // K^ = (Z(k) + conj Z(-k)) / 2, dKx^ = (Z(k) - conj Z(-k)) / 2i
+        FK = make_float2(0.5f * (z.x + zm.x), 0.5f * (z.y - zm.y));
+        FX = make_float2(0.5f * (z.y + zm.y), -0.5f * (z.x - zm.x));
+      }
+      const float2 d = D[i];
+      if (two_k) {
+        K1[i] = cmul(d, K1[i]);
+        D[i] = cmul(d, make_float2(FK.x - FX.y, FK.y + FX.x));  // d (K^ + i dKx^)
+      } else {
+        D[i] = cmul(d, FK);
+      }
+      for (int p = 0; p < pairs; ++p) {
+        float2* P = fft_buffer(b, st, slot, FB_P1 + p);
+        P[i] = cmul(P[i], FK);
+      }
     }
   }
 }
 
-// -- convolved planes on the output grid ----------------------------------------------------
-__global__ void __launch_bounds__(kFftThreads) k_fft_extract(BatchArgs b) {
+// -- inverse row transforms of the kept rows, written as convolved planes: one CTA per
+// (stamp, block of output rows) ---------------------------------------------------------------
+__global__ void __launch_bounds__(kFftThreads) k_fft_rows_inv(BatchArgs b) {
+  extern __shared__ float2 sm[];
   const int j = fft_find(b.fft_out_pre, b.n_fft, blockIdx.x);
-  const int s = b.fft_stamp[j], slot = blockIdx.y;
-  const int ops = b.evals[s * 2 + slot].ops;
-  if (!ops) return;
+  const int s = b.fft_stamp[j];
   const StampDev& st = b.stamps[s];
-  const FftUse u = fft_use(b, ops);
-  const int Y = blockIdx.x - b.fft_out_pre[j];
-  const int Nx = st.fft_nx, Ny = st.fft_ny;
+  const int Nx = st.fft_nx, Ny = st.fft_ny, bits = 31 - __clz(Nx);
+  const int rb = fft_rows_per_block(Nx);
+  const int Y0 = (blockIdx.x - b.fft_out_pre[j]) * rb;
+  const int rows = min(rb, st.ny - Y0);
   const float scale = 1.f / ((float)Nx * (float)Ny);
   const int64_t npix = (int64_t)st.nx * st.ny;
-  float* pre = b.preconv + st.pre_off + (int64_t)slot * (3 + NGRAD) * npix + (int64_t)Y * st.nx;
-  const int64_t wrow = (int64_t)(Y + st.by) * Nx + st.bx;
-  const float2* D = fft_buffer(b, st, slot, FB_D) + wrow;
-  const float2* K1 = fft_buffer(b, st, slot, FB_K1) + wrow;
-  const bool two_k = u.jac && u.shift;
-  for (int X = threadIdx.x; X < st.nx; X += blockDim.x) {
-    const float2 d = D[X];
-    pre[X] = d.x * scale;
-    if (two_k) {
-      pre[npix + X] = d.y * scale;
-      pre[2 * npix + X] = K1[X].x * scale;
-    }
-    for (int p = 0; p < u.npart; ++p) {
-      const float2 v = fft_buffer(b, st, slot, FB_P1 + p / 2)[wrow + X];
-      pre[(int64_t)(3 + u.part[p]) * npix + X] = ((p & 1) ? v.y : v.x) * scale;
+  for (int slot = 0; slot < 2; ++slot) {
+    const int ops = b.evals[s * 2 + slot].ops;
+    if (!ops) continue;
+    const FftUse u = fft_use(b, ops);
+    float* pre = b.preconv + st.pre_off + (int64_t)slot * (3 + NGRAD) * npix + (int64_t)Y0 * st.nx;
+    for (int k = 0; k < kFftBufs; ++k) {
+      if (!((u.inv >> k) & 1u)) continue;
+      const float2* buf = fft_buffer(b, st, slot, k) + (int64_t)(Y0 + st.by) * Nx;
+      for (int e = threadIdx.x; e < rows * Nx; e += blockDim.x) {
+        const int r = e / Nx, x = e - r * Nx;
+        sm[r * Nx + (__brev(x) >> (32 - bits))] = buf[e];
+      }
+      __syncthreads();
+      dit_rows(sm, Nx, rows, true, threadIdx.x, blockDim.x);
+      // planes: D -> model (re), d/dshift_x (im); K1 -> d/dshift_y (re); P -> a pair of partials
+      int pr = -1, pi = -1;
+      if (k == FB_D) {
+        pr = 0;
+        pi = (u.jac && u.shift) ? 1 : -1;
+      } else if (k == FB_K1) {
+        pr = 2;
+      } else {
+        const int p = k - FB_P1;
+        pr = 3 + u.part[2 * p];
+        pi = 2 * p + 1 < u.npart ? 3 + u.part[2 * p + 1] : -1;
+      }
+      for (int e = threadIdx.x; e < rows * st.nx; e += blockDim.x) {
+        const int r = e / st.nx, X = e - r * st.nx;
+        const float2 v = sm[r * Nx + X + st.bx];
+        pre[(int64_t)pr * npix + (int64_t)r * st.nx + X] = v.x * scale;
+        if (pi >= 0) pre[(int64_t)pi * npix + (int64_t)r * st.nx + X] = v.y * scale;
+      }
+      __syncthreads();
     }
   }
 }
@@ -297,22 +317,23 @@ cudaError_t set_fft_smem() {
   cudaError_t e = cudaFuncSetAttribute(k_fft_cols, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)(sizeof(float2) * kColGroup * kFftMaxSide));
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_fft_rows, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  e = cudaFuncSetAttribute(k_fft_rows_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)(sizeof(float2) * kFftMaxSide));
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_fft_rows_inv, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)(sizeof(float2) * kFftMaxSide));
 }
 
 cudaError_t launch_fft_conv(const BatchArgs& b, int total_rows, int total_cols, int total_out, int max_nx,
                             int max_ny, cudaStream_t s) {
   if (b.n_fft <= 0) return cudaSuccess;
-  const size_t row_smem = sizeof(float2) * (size_t)max_nx;
+  const size_t row_smem = sizeof(float2) * (size_t)kFftMaxSide;  // fft_rows_per_block rows of max_nx
   const size_t col_smem = sizeof(float2) * kColGroup * (size_t)max_ny;
-  k_fft_pack<<<dim3(total_rows, 2), kFftThreads, 0, s>>>(b);
-  k_fft_rows<<<dim3(total_rows, 2 * kFftBufs), kFftThreads, row_smem, s>>>(b, 0);
-  k_fft_cols<<<dim3(total_cols, 2 * kFftBufs), kFftThreads, col_smem, s>>>(b, 0);
-  k_fft_mul<<<dim3(total_rows, 2), kFftThreads, 0, s>>>(b);
-  k_fft_cols<<<dim3(total_cols, 2 * kFftBufs), kFftThreads, col_smem, s>>>(b, 1);
-  k_fft_rows<<<dim3(total_rows, 2 * kFftBufs), kFftThreads, row_smem, s>>>(b, 1);
-  k_fft_extract<<<dim3(total_out, 2), kFftThreads, 0, s>>>(b);
+  k_fft_rows_fwd<<<total_rows, kFftThreads, row_smem, s>>>(b);
+  k_fft_cols<<<total_cols, kFftThreads, col_smem, s>>>(b, 0);
+  k_fft_mul<<<total_rows, kFftThreads, 0, s>>>(b);
+  k_fft_cols<<<total_cols, kFftThreads, col_smem, s>>>(b, 1);
+  k_fft_rows_inv<<<total_out, kFftThreads, row_smem, s>>>(b);
   return cudaGetLastError();
 }
 
