@@ -6,6 +6,8 @@ keeps the reference's knobs (``max_step_iter``, ``curvature_limit``, ``Lup``, ``
 ``acceleration``), its outputs (``loss_history``, ``L_history``, ``lambda_history``,
 ``message``, ``res()``, ``covariance_matrix``, ``update_uncertainty()``) and its messages.
 ``BatchLM(models)`` fits many independent models (cutouts) in one device run.
+``Iter_LM(model, chunks=50, method="random")`` runs LM on chunks of the parameter vector in
+turn (``astrophot/fit/iterative.py:177-338``).
 """
 
 from __future__ import annotations
@@ -19,7 +21,7 @@ from . import config
 from .errors import OptimizeStop
 from .models import _Structure, _make_scene, _needs_scene, _plan
 
-__all__ = ("LM", "BatchLM")
+__all__ = ("LM", "BatchLM", "Iter_LM")
 
 
 def _setup(model, initial_state):
@@ -236,3 +238,63 @@ class BatchLM:
 
     def res(self):
         return [f.res_state.numpy() for f in self.fits]
+
+
+class Iter_LM:
+    """``Iter_LM`` (fit/iterative.py:177-338) on the CUDA path: sweeps of LMs on chunks of the
+    model's parameter vector, the other entries held, each chunk's LM with the whole problem's
+    degrees of freedom, until the sweep loss settles twice or ``max_iter`` sweeps.  ``chunks``:
+    an int (chunks of that many entries, drawn by ``random.sample`` with ``method="random"`` or
+    taken in order with ``"sequential"``) or a tuple of index tuples into the vector.  Runs over
+    the model's scene (its galaxies with their windows and the locked sky); ``LM_kwargs`` go to
+    each chunk's LM."""
+
+    def __init__(self, model, initial_state: Sequence = None, chunks=50, max_iter: int = 100, method: str = "random",
+                 LM_kwargs: Optional[dict] = None, relative_tolerance: float = 1e-3, **kwargs):
+        if method not in ("random", "sequential"):
+            raise ValueError(f"unrecognized Iter_LM method: {method}")
+        if not isinstance(chunks, (int, tuple, list)):
+            raise ValueError(f"Unrecognized chunks value, should be one of int, tuple. not: {type(chunks)}")
+        self.model = model
+        comps = list(model.models.values()) if hasattr(model, "models") else [model]
+        if initial_state is None:
+            model.initialize()
+            initial_state = model.parameters.vector_representation()
+        self.current_state = torch.as_tensor(initial_state, dtype=config.ap_dtype).flatten()
+        self._scene = _make_scene(model, comps)
+        self.chunks, self.method, self.max_iter = chunks, method, max_iter
+        self.relative_tolerance = relative_tolerance
+        self.LM_kwargs = dict(LM_kwargs or {})
+        self.loss_history, self.lambda_history = [], []
+        self.message = ""
+        self.iteration = 0
+        self.ndf = None
+
+    def fit(self):
+        from .scene import SceneIterLM
+
+        it = SceneIterLM(self._scene, initial_state=self.current_state.numpy(), chunks=self.chunks,
+                         max_iter=self.max_iter, method=self.method, relative_tolerance=self.relative_tolerance,
+                         LM_kwargs=self.LM_kwargs).fit()
+        self.ndf = it.ndf
+        self.loss_history = list(it.loss_history)
+        self.lambda_history = [np.array(v) for v in it.lambda_history]
+        self.iteration = it.iteration
+        self.message = self.message + it.message
+        self.current_state = torch.tensor(it.x)
+        self.model.parameters.vector_set_representation(torch.tensor(it.res()))
+        return self
+
+    def res(self):
+        hist = np.array(self.loss_history)
+        N = np.isfinite(hist)
+        if len(hist) == 0 or not N.any():
+            return self.current_state.numpy()
+        return np.array(self.lambda_history)[N][np.argmin(hist[N])]
+
+    def res_loss(self):
+        hist = np.array(self.loss_history)
+        return float(np.min(hist[np.isfinite(hist)]))
+
+    def chi2min(self):
+        return float(np.nanmin(self.loss_history))

@@ -414,9 +414,11 @@ class Scene:
         return out
 
     def solve(self, H: torch.Tensor, g: torch.Tensor, L: float):
-        """Damped solve; None when the damped matrix is not positive definite."""
-        h = torch.empty(self.P, dtype=torch.float64, device=self.device)
-        N.check(self.lib.ap_dense_damped_solve(self.P, N._ptr(H), N._ptr(g.contiguous()), float(L), N._ptr(h),
+        """Damped solve of the n x n system H (n = H's side, at most P); None when the damped
+        matrix is not positive definite."""
+        n = int(H.shape[0])
+        h = torch.empty(n, dtype=torch.float64, device=self.device)
+        N.check(self.lib.ap_dense_damped_solve(n, N._ptr(H.contiguous()), N._ptr(g.contiguous()), float(L), N._ptr(h),
                                                N._ptr(self._solve_ws), self._solve_ws.numel(), N._ptr(self._info),
                                                N._stream()), "ap_dense_damped_solve")
         if int(self._info.item()) != 0:
@@ -429,13 +431,17 @@ class OptimizeStop(Exception):
 
 
 class SceneLM:
-    """``LM`` (fit/lm.py:15-539) over a scene's joint vector."""
+    """``LM`` (fit/lm.py:15-539) over a scene's joint vector, or over the entries ``free`` of
+    it with the others held (the LM ``Iter_LM`` runs under ``Param_Mask``,
+    fit/iterative.py:291-296)."""
 
     def __init__(self, scene: Scene, initial_state=None, max_iter: int = 100, relative_tolerance: float = 1e-5,
                  max_step_iter: int = 10, curvature_limit: float = 1.0, Lup: float = 11.0, Ldn: float = 9.0,
-                 L0: float = 1.0, acceleration: float = 0.0, ndf=None):
+                 L0: float = 1.0, acceleration: float = 0.0, ndf=None, free=None):
         self.scene = scene
         self.x = np.array(scene.representation() if initial_state is None else initial_state, dtype=np.float64)
+        self.free = None if free is None else np.asarray(free, dtype=np.int64)
+        self._free_t = None if free is None else torch.as_tensor(self.free, device=scene.device)
         self.max_iter, self.relative_tolerance = int(max_iter), float(relative_tolerance)
         self.max_step_iter, self.curvature_limit = int(max_step_iter), float(curvature_limit)
         self._Lup, self._Ldn, self.L, self.acceleration = float(Lup), float(Ldn), float(L0), float(acceleration)
@@ -453,14 +459,26 @@ class SceneLM:
     def _chi2(self, model):
         return self.scene.chi2(model) / self.ndf
 
+    def _sub(self, v):  # entries of the fitted chunk
+        return v if self._free_t is None else v[self._free_t]
+
+    def _full(self, v):  # a chunk vector as a joint vector (zeros elsewhere)
+        if self._free_t is None:
+            return v
+        out = torch.zeros(self.scene.P, dtype=v.dtype, device=v.device)
+        out[self._free_t] = v
+        return out
+
     def step(self, chi2):
         sc = self.scene
         x = self.x
         Y0 = sc.forward(x)
         sc.jacobian(x)
         hess = sc.hess()
+        if self._free_t is not None:
+            hess = hess[self._free_t][:, self._free_t].contiguous()
         resid = sc.residual(Y0)             # W (Y - Y0) = -r
-        grad = sc.jt(resid)                 # -J^T r
+        grad = self._sub(sc.jt(resid))      # -J^T r
         r = sc.residual(sc.data, Y0)        # W (Y0 - Y)
         init_chi2 = chi2
         nostep = True
@@ -478,13 +496,14 @@ class SceneLM:
                     break
                 direction = "worse"
                 continue
+            h = self._full(h)
             h_np = h.cpu().numpy()
             Y1 = sc.forward(x + d * h_np)
             rh = sc.residual(sc.data, Y1)   # W (Y1 - Y)
-            rpp = sc.jt(sc.rpp_image(r, rh, sc.jvp(h), d))
+            rpp = self._sub(sc.jt(sc.rpp_image(r, rh, sc.jvp(h), d)))
             if self.L > 1e-4:
                 a_d = sc.solve(hess, rpp, self.L)
-                a = np.zeros_like(h_np) if a_d is None else -a_d.cpu().numpy() / 2
+                a = np.zeros_like(h_np) if a_d is None else -self._full(a_d).cpu().numpy() / 2
             else:
                 a = np.zeros_like(h_np)
             ha = h_np + a * self.acceleration
@@ -528,7 +547,7 @@ class SceneLM:
         return best
 
     def fit(self):
-        if self.scene.P == 0:
+        if self.scene.P == 0 or (self.free is not None and len(self.free) == 0):
             return self
         self.loss_history = [self._chi2(self.scene.forward(self.x))]
         self.L_history = [self.L]
@@ -557,6 +576,84 @@ class SceneLM:
                     break
         else:
             self.message = self.message + "fail. Maximum iterations"
+        self.scene.set_representation(self.res())
+        return self
+
+    def res(self):
+        hist = np.array(self.loss_history)
+        ok = np.isfinite(hist)
+        if not ok.any():
+            return self.x.copy()
+        return np.array(self.lambda_history)[ok][np.argmin(hist[ok])]
+
+
+class SceneIterLM:
+    """``Iter_LM`` (fit/iterative.py:177-338) over a scene: sweeps of LMs on chunks of the joint
+    vector (the rest held, the full problem's degrees of freedom), until the sweep loss settles
+    twice (relative change in (-tol 1e-3, tol / 10)) or ``max_iter`` sweeps.  ``chunks`` an int:
+    chunks of that many entries in order (``method="sequential"``) or drawn by ``random.sample``
+    (``"random"``, Python's ``random`` module, as the reference draws them); or a sequence of
+    index lists."""
+
+    def __init__(self, scene: Scene, initial_state=None, chunks=50, max_iter: int = 100, method: str = "random",
+                 relative_tolerance: float = 1e-3, LM_kwargs: Optional[dict] = None):
+        self.scene = scene
+        self.x = np.array(scene.representation() if initial_state is None else initial_state, dtype=np.float64)
+        self.chunks, self.method, self.max_iter = chunks, method, int(max_iter)
+        self.relative_tolerance = float(relative_tolerance)
+        self.LM_kwargs = dict(LM_kwargs or {})
+        n_used = scene.nx * scene.ny if scene.mask is None else int((scene.mask == 0).sum().item())
+        self.ndf = n_used - scene.P
+        self.loss_history, self.lambda_history = [], []
+        self.message = ""
+        self.iteration = 0
+        self._count_finish = 0
+
+    def _chunk_list(self):
+        import random
+
+        if isinstance(self.chunks, int):
+            ids = list(range(self.scene.P))
+            while ids:
+                take = random.sample(ids, min(len(ids), self.chunks)) if self.method == "random" else ids[: self.chunks]
+                for t in sorted(take):
+                    ids.pop(ids.index(t))
+                yield sorted(take)
+        else:
+            order = list(range(len(self.chunks)))
+            while order:
+                k = random.choice(order) if self.method == "random" else order[0]
+                order.pop(order.index(k))
+                yield sorted(int(i) for i in self.chunks[k])
+
+    def step(self):
+        res = None
+        for chunk in self._chunk_list():
+            res = SceneLM(self.scene, initial_state=self.x, ndf=self.ndf, free=chunk, **self.LM_kwargs).fit()
+            self.x = np.array(res.res(), dtype=np.float64)
+        self.loss_history.append(min(v for v in res.loss_history if np.isfinite(v)))
+        self.lambda_history.append(self.x.copy())
+        if self.iteration >= 2 and (
+            (-self.relative_tolerance * 1e-3)
+            < ((self.loss_history[-2] - self.loss_history[-1]) / self.loss_history[-1])
+            < (self.relative_tolerance / 10)
+        ):
+            self._count_finish += 1
+        else:
+            self._count_finish = 0
+        self.iteration += 1
+
+    def fit(self):
+        if self.scene.P == 0:
+            return self
+        while True:
+            self.step()
+            if self.iteration > 2 and self._count_finish >= 2:
+                self.message = self.message + "success"
+                break
+            if self.iteration >= self.max_iter:
+                self.message = self.message + f"fail max iterations reached: {self.iteration}"
+                break
         self.scene.set_representation(self.res())
         return self
 

@@ -274,3 +274,114 @@ class LMOracle:
     def res_loss(self):
         hist = np.array(self.loss_history)
         return float(np.min(hist[np.isfinite(hist)]))
+
+
+class ChunkProblem:
+    """A :class:`GroupProblem` restricted to the joint-vector entries ``idx``, the others held at
+    their current values: what ``Param_Mask(parameters, chunk)`` shows the LM
+    (param/param_context.py:62-90, fit/iterative.py:291-296)."""
+
+    def __init__(self, problem: GroupProblem, idx):
+        self.problem = problem
+        self.idx = np.asarray(idx, dtype=np.int64)
+        self.base = np.array(problem.representation(), dtype=np.float64)
+        self.Y, self.W, self.mask = problem.Y, problem.W, problem.mask
+
+    def full(self, sub):
+        x = self.base.copy()
+        x[self.idx] = sub
+        return x
+
+    def representation(self):
+        return self.base[self.idx].copy()
+
+    def set_representation(self, sub):
+        self.problem.set_representation(self.full(sub))
+        self.base = np.array(self.problem.representation(), dtype=np.float64)
+
+    def forward(self, sub):
+        return self.problem.forward(self.full(sub))
+
+    def jacobian(self, sub):
+        return self.problem.jacobian(self.full(sub))[:, self.idx]
+
+
+class IterLMOracle:
+    """``Iter_LM`` (fit/iterative.py:177-338): LM on chunks of the joint vector in turn, the
+    rest held, until the loss of two successive sweeps settles (or ``max_iter`` sweeps).
+    ``chunks`` an int: chunks of that many entries, in order (``method="sequential"``) or drawn
+    with ``random.sample`` (``"random"``, Python's ``random`` module as the reference uses it);
+    or a tuple of index lists.  Each chunk's LM uses the full problem's degrees of freedom."""
+
+    def __init__(self, problem: GroupProblem, initial_state=None, chunks=50, max_iter=100, method="random",
+                 relative_tolerance=1e-3, LM_kwargs=None):
+        self.problem = problem
+        if initial_state is not None:
+            problem.set_representation(np.asarray(initial_state, dtype=np.float64))
+        self.current_state = np.array(problem.representation(), dtype=np.float64)
+        self.chunks, self.method, self.max_iter = chunks, method, max_iter
+        self.relative_tolerance = relative_tolerance
+        self.LM_kwargs = dict(LM_kwargs or {})
+        n = problem.Y.size
+        self.ndf = n - len(self.current_state)
+        if problem.mask is not None:
+            self.ndf -= int(np.sum(problem.mask))
+        self.loss_history, self.lambda_history = [], []
+        self.message = ""
+        self.iteration = 0
+        self._count_finish = 0
+
+    def _chunk_list(self):
+        P = len(self.current_state)
+        if isinstance(self.chunks, int):
+            import random
+
+            ids = list(range(P))
+            while ids:
+                take = random.sample(ids, min(len(ids), self.chunks)) if self.method == "random" else ids[: self.chunks]
+                for t in sorted(take):
+                    ids.pop(ids.index(t))
+                yield sorted(take)
+        else:
+            import random
+
+            order = list(range(len(self.chunks)))
+            while order:
+                k = random.choice(order) if self.method == "random" else order[0]
+                order.pop(order.index(k))
+                yield sorted(self.chunks[k])
+
+    def step(self):
+        res = None
+        for chunk in self._chunk_list():
+            res = LMOracle(ChunkProblem(self.problem, chunk), ndf=self.ndf, **self.LM_kwargs).fit()
+        self.loss_history.append(res.res_loss())
+        self.lambda_history.append(np.array(self.problem.representation(), dtype=np.float64))
+        if self.iteration >= 2 and (
+            (-self.relative_tolerance * 1e-3)
+            < ((self.loss_history[-2] - self.loss_history[-1]) / self.loss_history[-1])
+            < (self.relative_tolerance / 10)
+        ):
+            self._count_finish += 1
+        else:
+            self._count_finish = 0
+        self.iteration += 1
+
+    def fit(self):
+        while True:
+            self.step()
+            if self.iteration > 2 and self._count_finish >= 2:
+                self.message = self.message + "success"
+                break
+            if self.iteration >= self.max_iter:
+                self.message = self.message + f"fail max iterations reached: {self.iteration}"
+                break
+        self.problem.set_representation(self.res())
+        return self
+
+    def res(self):
+        hist = np.array(self.loss_history)
+        N = np.isfinite(hist)
+        if not N.any():
+            return self.current_state.copy()
+        return np.array(self.lambda_history)[N][np.argmin(hist[N])]

@@ -84,3 +84,17 @@ def load_init(name):
     d["spec"] = json.loads(str(d["spec"]))
     d["mask"] = d["mask"] if d["mask"].size else None
     return d
+
+
+def iter_case_names():
+    return sorted(os.path.basename(p)[: -len(".npz")] for p in glob.glob(os.path.join(HERE, "iterlm_*.npz")))
+
+
+def load_iter(name):
+    """An ``Iter_LM`` case: its spec (group case, chunks, method, max_iter) and the reference's
+    outer loss / state histories, final state and message."""
+    z = np.load(os.path.join(HERE, f"{name}.npz"))
+    d = {k: z[k] for k in z.files}
+    d["spec"] = json.loads(str(d["spec"]))
+    d["message"] = str(d["message"])
+    return d

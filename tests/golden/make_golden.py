@@ -5,6 +5,7 @@ Run in a container that has the reference checkout (default path below, or
 
     python tests/golden/make_golden.py          # every case
     python tests/golden/make_golden.py init     # only the initial-value cases
+    python tests/golden/make_golden.py iter     # the initial-value and Iter_LM cases
 
 The reference (AstroPhot 0.x) is imported through a ``sys.modules`` shim for
 the optional packages it imports at module level but never calls on this
@@ -449,6 +450,30 @@ def run_group_case(ap, key, case):
     )
 
 
+ITER_CASES = {
+    # fit.Iter_LM over the group_linked_96 group from its perturbed start: the joint vector in
+    # sequential chunks of 7 parameters, each chunk a full LM with the others fixed
+    "iterlm_linked_96": dict(group="group_linked_96", chunks=7, method="sequential", max_iter=5),
+}
+
+
+def run_iter_case(ap, key, case):
+    gcase = GROUP_CASES[case["group"]]
+    N = gcase["size"]
+    psf = psf_array(gcase["psf"])
+    target = ap.image.Target_Image(data=np.zeros((N, N)), pixelscale=1.0, psf=psf)
+    truth_vals = [src[3] for src in GROUP_SOURCES]
+    truth_img = build_group(ap, target, truth_vals, f"{key} truth")().data.detach().cpu().numpy()
+    data, weight = synthetic.add_noise(truth_img, gcase["seed"])
+    target = ap.image.Target_Image(data=data, pixelscale=1.0, psf=psf, variance=1.0 / weight)
+    group = build_group(ap, target, [group_init_values(v) for v in truth_vals], key)
+    rep0 = group.parameters.vector_representation().detach().cpu().numpy().copy()
+    res = ap.fit.Iter_LM(group, initial_state=rep0, chunks=case["chunks"], method=case["method"],
+                         max_iter=case["max_iter"]).fit()
+    return dict(rep0=rep0, loss_history=np.array(res.loss_history), lambda_history=np.array(res.lambda_history),
+                res=np.array(res.res()), message=np.array(res.message), ndf=np.array(res.ndf), spec=json.dumps(case))
+
+
 ADJOINT_CASES = {
     # negative_log_likelihood().backward() of a Group_Model of three bulge (Sersic) + disk
     # (exponential) pairs sharing their centre node, each with its own window, on a 256 x 256
@@ -598,6 +623,12 @@ def main():
         np.savez_compressed(os.path.join(HERE, f"{key}.npz"), **out)
         print("init", key, {k: out[k] for k in out if k.startswith("value_")})
     if only == "init":
+        return
+    for key, case in ITER_CASES.items():
+        out = run_iter_case(ap, key, case)
+        np.savez_compressed(os.path.join(HERE, f"{key}.npz"), **out)
+        print("iter", key, out["loss_history"], str(out["message"]))
+    if only == "iter":
         return
     for key, case in ADJOINT_CASES.items():
         out = run_adjoint_case(ap, key, case)

@@ -152,3 +152,50 @@ def test_scene_with_mask_and_no_psf_matches_oracle(S):
     lmo = LMOracle(prob, rep, max_iter=15).fit()
     print(lm.loss_history, lmo.loss_history)
     assert abs(min(lm.loss_history) / min(lmo.loss_history) - 1) <= 1e-4
+
+
+@pytest.mark.parametrize("name", cases.iter_case_names())
+def test_scene_iter_lm_matches_reference(S, name):
+    """``Iter_LM`` (sequential chunks of 7 over the linked group's 25 entries, 5 sweeps) on the
+    scene: the reference's sweep losses, message and final state."""
+    d = cases.load_iter(name)
+    g = cases.load_group(d["spec"]["group"])
+    sc = golden_scene(S, g)
+    assert np.allclose(sc.representation(), d["rep0"], atol=1e-12)
+    it = S.SceneIterLM(sc, chunks=d["spec"]["chunks"], method=d["spec"]["method"], max_iter=d["spec"]["max_iter"]).fit()
+    print(it.loss_history, d["loss_history"])
+    assert it.ndf == int(d["ndf"])
+    assert it.message == d["message"]
+    assert np.allclose(it.loss_history, d["loss_history"], rtol=1e-5, atol=0)
+    assert np.max(np.abs(it.res() - d["res"])) <= 1e-3
+
+
+def test_iter_lm_drop_in_api(S):
+    """``fit.Iter_LM`` on a drop-in group model built like the reference's tests."""
+    import astrophot_gb300 as ap
+
+    d = cases.load_iter(cases.iter_case_names()[0])
+    g = cases.load_group(d["spec"]["group"])
+    N = g["spec"]["size"]
+    tar = ap.image.Target_Image(data=g["data"], pixelscale=1.0, psf=g["psf"], variance=1.0 / g["weight"])
+    models = []
+    for i, (k, v, w, l) in enumerate(zip(KINDS, g["init_values"], WINDOWS, LINKS)):
+        cx, cy, q, PA, n, Re, Ie = v
+        p = {"q": q, "PA": PA, "Re": Re, "Ie": Ie}
+        if l is None:
+            p["center"] = [cx, cy]
+        if k == "sersic":
+            p["n"] = n
+        m = ap.models.AstroPhot_Model(name=f"iterlm {i}", model_type=f"{k} galaxy model", target=tar,
+                                      window=[list(w[0]), list(w[1])], parameters=p)
+        if l is not None:
+            m.parameters["center"].value = models[l].parameters["center"]
+        models.append(m)
+    sky = ap.models.AstroPhot_Model(name="iterlm sky", model_type="flat sky model", target=tar,
+                                    parameters={"F": {"value": 0.0, "locked": True}})
+    sky.initialize()
+    grp = ap.models.AstroPhot_Model(name="iterlm group", model_type="group model", target=tar,
+                                    models=models + [sky], psf_mode="full")
+    res = ap.fit.Iter_LM(grp, chunks=7, method="sequential", max_iter=2).fit()
+    assert np.allclose(res.loss_history, d["loss_history"][:2], rtol=1e-5)
+    assert res.message == "fail max iterations reached: 2"

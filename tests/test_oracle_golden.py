@@ -349,3 +349,23 @@ def test_group_adjoint_golden_pins_the_oracle(name):
             assert abs(fd - d["grad"][k]) > 1e-3 * abs(fd)
         else:
             assert abs(fd - d["grad"][k]) <= 1e-5 * scale, (k, names[k], fd, d["grad"][k])
+
+
+# ---- Iter_LM: LM on chunks of the joint vector ----------------------------------------------
+
+
+@pytest.mark.parametrize("name", cases.iter_case_names())
+def test_iter_lm_first_sweep_matches_reference(name):
+    """The first sweep of ``Iter_LM`` (four chunk LMs over the 25-entry vector of the linked
+    group) against the reference's: the sweep loss and the state after it.  (The full five-sweep
+    run, 2 minutes on the oracle, agrees to 1e-10 in loss and 3e-10 in state; the GPU test runs
+    it through the library.)"""
+    from oracle.lm import IterLMOracle
+
+    d = cases.load_iter(name)
+    g = cases.load_group(d["spec"]["group"])
+    prob = group_problem(g)
+    it = IterLMOracle(prob, d["rep0"], chunks=d["spec"]["chunks"], method=d["spec"]["method"], max_iter=1).fit()
+    assert it.ndf == int(d["ndf"])
+    assert np.isclose(it.loss_history[0], d["loss_history"][0], rtol=1e-10, atol=0)
+    assert np.allclose(it.lambda_history[0], d["lambda_history"][0], rtol=1e-8, atol=1e-10)
