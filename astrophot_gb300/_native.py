@@ -118,6 +118,10 @@ EXPORTS = [
     ("ap_batch_set_grid", [_P, _PI32]),
     ("ap_values_to_rep", [_P, _I32, _I32, _P, _P]),
     ("ap_reference_init_workspace_bytes", [_P, _PI64]),
+    ("ap_segmap_range", [_P, _I64, _P, _P]),
+    ("ap_segmap_present", [_P, _I64, _I32, _P, _P]),
+    ("ap_segmap_stats", [_P, _P, _I32, _I32, _P, _I32, ctypes.c_double, _P, _P, _P, _P, _P, _P, _P, _P]),
+    ("ap_window_flux", [_P, _I32, _I32, _P, _I32, _P, _P]),
     ("ap_reference_init", [_P, _P, _P, _I32, _P, _P, _P, _I64, _P]),
     ("ap_batch_psf_stride", [_P, _PI64]),
     ("ap_psf_shift", [_P, _P, _P, _P, _P, _P]),

@@ -692,6 +692,32 @@ int ap_reference_init(ap_batch* b, const float* data, const uint8_t* mask, int32
                                           status, workspace, (cudaStream_t)stream));
 }
 
+int ap_segmap_range(const int32_t* seg, int64_t npix, int32_t* min_max, ap_stream_t stream) {
+  if (!seg || !min_max || npix <= 0) return AP_ERR_ARG;
+  return check_cuda(launch_seg_range(seg, npix, min_max, (cudaStream_t)stream));
+}
+
+int ap_segmap_present(const int32_t* seg, int64_t npix, int32_t max_id, uint8_t* present, ap_stream_t stream) {
+  if (!seg || !present || npix <= 0 || max_id < 0) return AP_ERR_ARG;
+  return check_cuda(launch_seg_mark(seg, npix, present, max_id, (cudaStream_t)stream));
+}
+
+int ap_segmap_stats(const int32_t* seg, const float* image, int32_t nx, int32_t ny, const int32_t* index,
+                    int32_t n_seg, double north, const double* centroid_in, const double* pa_in, double* acc,
+                    int32_t* bbox, double* centroid, double* pa, double* q, ap_stream_t stream) {
+  if (!seg || !image || !index || !acc || !bbox || !centroid || !pa || !q || nx <= 0 || ny <= 0 || n_seg < 0)
+    return AP_ERR_ARG;
+  if (n_seg == 0) return AP_OK;
+  return check_cuda(launch_seg_stats(seg, image, nx, ny, index, n_seg, north, centroid_in, pa_in, acc, bbox,
+                                     centroid, pa, q, (cudaStream_t)stream));
+}
+
+int ap_window_flux(const float* image, int32_t nx, int32_t ny, const int32_t* windows, int32_t n, double* flux,
+                   ap_stream_t stream) {
+  if (!image || !windows || !flux || nx <= 0 || ny <= 0 || n < 0) return AP_ERR_ARG;
+  return check_cuda(launch_window_flux(image, nx, ny, windows, n, flux, (cudaStream_t)stream));
+}
+
 int ap_batch_set_grid(ap_batch* b, const int32_t* blocks_per_sm) {
   if (!b || !blocks_per_sm) return AP_ERR_ARG;
   for (int k = 0; k < GK_COUNT; ++k)

@@ -98,6 +98,15 @@ cudaError_t set_fft_smem();
 cudaError_t launch_fft_conv(const BatchArgs& b, int total_rows, int total_cols, int total_out, int max_nx,
                             int max_ny, cudaStream_t s);
 
+// segmentation-map statistics (ap_segmap.cu)
+cudaError_t launch_seg_range(const int32_t* seg, int64_t n, int32_t* mm, cudaStream_t s);
+cudaError_t launch_seg_mark(const int32_t* seg, int64_t n, uint8_t* present, int32_t max_id, cudaStream_t s);
+cudaError_t launch_seg_stats(const int32_t* seg, const float* img, int nx, int ny, const int32_t* index, int n_seg,
+                             double north, const double* cen_in, const double* pa_in, double* acc, int32_t* bbox,
+                             double* cen, double* pa, double* q, cudaStream_t s);
+cudaError_t launch_window_flux(const float* img, int nx, int ny, const int32_t* wins, int n, double* out,
+                               cudaStream_t s);
+
 // the reference's initial-value heuristics (ap_refinit.cu)
 constexpr size_t kRefInitSmemBudget = 200 * 1024;  // dynamic shared memory per CTA at most
 struct RefInitPlan {

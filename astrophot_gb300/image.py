@@ -10,6 +10,8 @@ Pixel data are float64 host tensors ``[ny, nx]``.
 
 from __future__ import annotations
 
+import ast
+
 import math
 from typing import Optional
 
@@ -179,7 +181,10 @@ class Target_Image(_Image):
     """Data with optional variance/weight, mask and PSF (``image/target_image.py:17-342``)."""
 
     def __init__(self, data=None, pixelscale=1.0, psf=None, variance=None, weight=None, mask=None, zeropoint=None,
-                 origin=None, window=None, psf_upscale=1, **kwargs):
+                 origin=None, window=None, psf_upscale=1, filename=None, **kwargs):
+        if filename is not None:
+            self._load_states(filename)
+            return
         data = _t(data)
         if window is None:
             window = Window((data.shape[1], data.shape[0]), pixelscale, origin=origin)
@@ -258,6 +263,77 @@ class Target_Image(_Image):
         out._weight = None if self._weight is None else self._weight.clone()
         out._mask = None if self._mask is None else self._mask.clone()
         return out
+
+    # -- FITS (image/image_object.py:400-428, image/target_image.py:503-532) -------------------
+    @staticmethod
+    def _window_keys(w: Window, shape_xy):
+        return {"PROJ": "gnomonic", "REFRADEC": str([0.0, 0.0]), "REFPLNXY": str([0.0, 0.0]),
+                "PXLSCALE": str(np.asarray(w.pixelscale, dtype=np.float64).tolist()),
+                "REFIMGIJ": str(np.asarray(w.reference_imageij, dtype=np.float64).tolist()),
+                "REFIMGXY": str(np.asarray(w.reference_imagexy, dtype=np.float64).tolist()),
+                "PXL_SHPE": str([float(v) for v in shape_xy])}
+
+    def get_fits_state(self):
+        """[(data, header)]: PRIMARY (with the window and zeropoint keys), WEIGHT, MASK, PSF."""
+        head = self._window_keys(self.window, self.window.pixel_shape)
+        if self.zeropoint is not None:
+            head["ZEROPNT"] = str(float(self.zeropoint))
+        head["IMAGE"] = "PRIMARY"
+        states = [(self.data.detach().cpu().numpy().astype(np.float64), head)]
+        if self.has_weight:
+            states.append((self._weight.detach().cpu().numpy().astype(np.float64), {"IMAGE": "WEIGHT"}))
+        if self.has_mask:
+            states.append((self._mask.detach().cpu().numpy().astype(np.int64), {"IMAGE": "MASK"}))
+        if self.has_psf:
+            ky, kx = self.psf.data.shape
+            pw = Window((kx, ky), self.psf.pixelscale)
+            ph = self._window_keys(pw, (kx, ky))
+            ph["IMAGE"] = "PSF"
+            states.append((self.psf.data.detach().cpu().numpy().astype(np.float64), ph))
+        return states
+
+    def save(self, filename=None, overwrite=True):
+        """Write the HDU list the reference writes (primary image + WEIGHT / MASK / PSF images)."""
+        import os
+
+        from .fits_io import write_hdus
+
+        if filename is None:
+            return self.get_fits_state()
+        if os.path.exists(filename) and not overwrite:
+            raise OSError(f"{filename} exists")
+        write_hdus(filename, self.get_fits_state())
+        return self.get_fits_state()
+
+    def _load_states(self, filename):
+        from .fits_io import read_hdus
+
+        hdus = read_hdus(filename)
+        prim = next((d, h) for d, h in hdus if str(h.get("IMAGE", "")).strip() == "PRIMARY")
+        data, head = prim
+        lit = ast.literal_eval  # the reference writes Python list literals into these keys
+        P = np.array(lit(str(head["PXLSCALE"])), dtype=np.float64)
+        shape = [int(round(v)) for v in lit(str(head["PXL_SHPE"]))]
+        w = Window(shape, P, reference_imageij=lit(str(head["REFIMGIJ"])), reference_imagexy=lit(str(head["REFIMGXY"])))
+        _Image.__init__(self, _t(np.asarray(data, dtype=np.float64)), w)
+        self.zeropoint = float(lit(str(head["ZEROPNT"]))) if "ZEROPNT" in head else None
+        self._weight = None
+        self._mask = None
+        self.psf = None
+        for d, h in hdus:
+            tag = str(h.get("IMAGE", "")).strip()
+            if tag == "WEIGHT":
+                self._weight = _t(np.asarray(d, dtype=np.float64))
+            # the reference's set_fits_state looks for "mask" in lower case while it writes
+            # "MASK" (image/target_image.py:517, 529): a saved mask does not come back on load
+            if tag == "mask":
+                self._mask = torch.as_tensor(np.asarray(d, dtype=bool))
+            if tag == "PSF":
+                Pp = np.array(lit(str(h["PXLSCALE"])), dtype=np.float64)
+                self.psf = PSF_Image(np.asarray(d, dtype=np.float64), pixelscale=Pp)
+
+    def load(self, filename):
+        self._load_states(filename)
 
 
 class Model_Image(_Image):

@@ -1,6 +1,7 @@
 """Helpers mirroring ``astrophot.utils`` for the render path: PSF stamp constructors
-(``utils/initialize/construct_psf.py:8-65``) and the Sersic b(n) polynomial
-(``utils/conversions/functions.py:7-22``)."""
+(``utils/initialize/construct_psf.py:8-65``), the Sersic b(n) polynomial
+(``utils/conversions/functions.py:7-22``) and the segmentation-map window helpers
+(``utils/initialize/segmentation_map.py``, in ``segmap.py``)."""
 
 from types import SimpleNamespace
 
@@ -23,5 +24,9 @@ def sersic_n_to_b(n):
             - 2194697 / (30690717750 * n**4))
 
 
-initialize = SimpleNamespace(moffat_psf=moffat_psf, gaussian_psf=gaussian_psf)
+from . import segmap as _segmap  # noqa: E402
+
+initialize = SimpleNamespace(moffat_psf=moffat_psf, gaussian_psf=gaussian_psf,
+                             segmentation_map=_segmap,
+                             **{name: getattr(_segmap, name) for name in _segmap.__all__})
 conversions = SimpleNamespace(functions=SimpleNamespace(sersic_n_to_b=sersic_n_to_b))

@@ -194,6 +194,26 @@ int ap_reference_init(ap_batch* batch, const float* data, const uint8_t* mask, i
                       double* params, int32_t* status, void* workspace, int64_t workspace_bytes,
                       ap_stream_t stream);
 
+/* Segmentation maps (astrophot/utils/initialize/segmentation_map.py:33-293), device pointers,
+ * seg[ny][nx] int32 ids >= 0, image[ny][nx] float32.
+ * ap_segmap_range: min_max[2] = (smallest, largest id).
+ * ap_segmap_present: present[id] = 1 for every id in the map (present: max_id + 1 bytes).
+ * ap_segmap_stats: per segment k (index[id] = k, -1 for ids left out; n_seg segments): bbox[k] =
+ *   (xmin, xmax, ymin, ymax) (windows_from_segmentation_map), centroid[k] = flux-weighted (x, y)
+ *   (centroids_from_segmentation_map), pa[k] = angular centre of light + north
+ *   (PA_from_segmentation_map), q[k] = axis_ratio_com at pa + north (q_from_segmentation_map);
+ *   centroid_in / pa_in (may be NULL): caller's centroids / PAs used instead of computed ones (the
+ *   reference functions' centroids= / PAs= arguments); acc: n_seg * 5 doubles of workspace.
+ * ap_window_flux: flux[w] = sum of the image over windows[w] = (x0, x1, y0, y1), half-open, clipped
+ *   to the image (filter_windows' flux). */
+int ap_segmap_range(const int32_t* seg, int64_t npix, int32_t* min_max, ap_stream_t stream);
+int ap_segmap_present(const int32_t* seg, int64_t npix, int32_t max_id, uint8_t* present, ap_stream_t stream);
+int ap_segmap_stats(const int32_t* seg, const float* image, int32_t nx, int32_t ny, const int32_t* index,
+                    int32_t n_seg, double north, const double* centroid_in, const double* pa_in, double* acc,
+                    int32_t* bbox, double* centroid, double* pa, double* q, ap_stream_t stream);
+int ap_window_flux(const float* image, int32_t nx, int32_t ny, const int32_t* windows, int32_t n, double* flux,
+                   ap_stream_t stream);
+
 /* Shifted, renormalised PSF of every stamp for value-space params (device):
  * out[n][(ky+2)*(kx+2)] packed with stride max_kp2 = (max ky + 2) * (max kx + 2)
  * (see ap_batch_psf_stride).  d_out (optional, may be NULL) receives d/d shift_x and

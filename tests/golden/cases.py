@@ -98,3 +98,15 @@ def load_iter(name):
     d["spec"] = json.loads(str(d["spec"]))
     d["message"] = str(d["message"])
     return d
+
+
+def segmap_case_names():
+    return sorted(os.path.basename(p)[: -len(".npz")] for p in glob.glob(os.path.join(HERE, "segmap_*.npz")))
+
+
+def load_segmap(name):
+    """A segmentation-map case: seg (int32), image, and the reference helpers' outputs per id."""
+    z = np.load(os.path.join(HERE, f"{name}.npz"))
+    d = {k: z[k] for k in z.files}
+    d["spec"] = json.loads(str(d["spec"]))
+    return d

@@ -6,6 +6,7 @@ Run in a container that has the reference checkout (default path below, or
     python tests/golden/make_golden.py          # every case
     python tests/golden/make_golden.py init     # only the initial-value cases
     python tests/golden/make_golden.py iter     # the initial-value and Iter_LM cases
+    python tests/golden/make_golden.py segmap   # only the segmentation-map case
 
 The reference (AstroPhot 0.x) is imported through a ``sys.modules`` shim for
 the optional packages it imports at module level but never calls on this
@@ -474,6 +475,58 @@ def run_iter_case(ap, key, case):
                 res=np.array(res.res()), message=np.array(res.message), ndf=np.array(res.ndf), spec=json.dumps(case))
 
 
+SEGMAP_CASES = {
+    # the segmentation-map helpers (utils/initialize/segmentation_map.py) on a 240 x 200 image of
+    # seven noisy Sersic galaxies whose segments (ids 1-6 and 9; 0 = background, skipped) are
+    # their isophote regions above 3 sigma, one of them clipped at the image edge
+    "segmap_240x200": dict(nx=240, ny=200, seed=31, noise=0.05),
+}
+
+SEGMAP_GALAXIES = (  # id, centre, q, PA, n, Re, Ie
+    (1, (40.3, 52.7), 0.6, 0.4, 2.0, 6.0, 0.5),
+    (2, (120.6, 95.2), 0.35, 2.1, 1.2, 10.0, 0.3),
+    (3, (190.1, 40.8), 0.8, 1.0, 3.5, 5.0, 0.6),
+    (4, (70.4, 160.3), 0.5, 2.8, 1.0, 8.0, 0.2),
+    (5, (210.7, 150.9), 0.7, 0.2, 2.5, 7.0, 0.4),
+    (6, (3.2, 110.5), 0.9, 1.6, 1.5, 6.0, 0.5),
+    (9, (150.3, 175.6), 0.45, 1.3, 4.0, 4.0, 0.7),
+)
+
+
+def run_segmap_case(ap, key, case):
+    from astrophot.utils.initialize import segmentation_map as sm
+
+    rng = np.random.default_rng(case["seed"])
+    nx, ny = case["nx"], case["ny"]
+    blank = ap.image.Target_Image(data=np.zeros((ny, nx)), pixelscale=1.0)
+    image = np.zeros((ny, nx))
+    seg = np.zeros((ny, nx), dtype=np.int32)
+    best = np.zeros((ny, nx))
+    for sid, c, q, PA, n, Re, Ie in SEGMAP_GALAXIES:
+        m = ap.models.AstroPhot_Model(name=f"{key} {sid}", model_type="sersic galaxy model", target=blank,
+                                      parameters={"center": list(c), "q": q, "PA": PA, "n": n, "Re": Re, "Ie": Ie})
+        img = m().data.detach().cpu().numpy()
+        image += img
+        own = (img > 3 * case["noise"]) & (img > best)
+        seg[own] = sid
+        best = np.maximum(best, img)
+    image = (image + case["noise"] * rng.normal(size=image.shape)).astype(np.float32).astype(np.float64)
+    cen = sm.centroids_from_segmentation_map(seg, image)
+    pas = sm.PA_from_segmentation_map(seg, image, cen)
+    qs = sm.q_from_segmentation_map(seg, image, cen, pas)
+    win = sm.windows_from_segmentation_map(seg)
+    scaled = sm.scale_windows(win, image_shape=image.shape, expand_scale=1.5, expand_border=3)
+    filt = sm.filter_windows(scaled, min_size=30, max_area=3800, min_flux=700.0, image=image)
+    ids = np.array(sorted(int(i) for i in cen))
+    return dict(
+        seg=seg, image=image, ids=ids,
+        centroids=np.array([cen[i] for i in ids]), pas=np.array([pas[i] for i in ids]),
+        qs=np.array([qs[i] for i in ids]), windows=np.array([win[i] for i in ids]),
+        scaled=np.array([scaled[i] for i in ids]), filtered_ids=np.array(sorted(int(i) for i in filt)),
+        spec=json.dumps(case),
+    )
+
+
 ADJOINT_CASES = {
     # negative_log_likelihood().backward() of a Group_Model of three bulge (Sersic) + disk
     # (exponential) pairs sharing their centre node, each with its own window, on a 256 x 256
@@ -618,17 +671,23 @@ def run_init_case(ap, key, case):
 def main():
     ap = import_reference()
     only = sys.argv[1] if len(sys.argv) > 1 else None
-    for key, case in INIT_CASES.items():
+    for key, case in (INIT_CASES if only != "segmap" else {}).items():
         out = run_init_case(ap, key, case)
         np.savez_compressed(os.path.join(HERE, f"{key}.npz"), **out)
         print("init", key, {k: out[k] for k in out if k.startswith("value_")})
     if only == "init":
         return
-    for key, case in ITER_CASES.items():
+    for key, case in (ITER_CASES if only != "segmap" else {}).items():
         out = run_iter_case(ap, key, case)
         np.savez_compressed(os.path.join(HERE, f"{key}.npz"), **out)
         print("iter", key, out["loss_history"], str(out["message"]))
     if only == "iter":
+        return
+    for key, case in SEGMAP_CASES.items():
+        out = run_segmap_case(ap, key, case)
+        np.savez_compressed(os.path.join(HERE, f"{key}.npz"), **out)
+        print("segmap", key, out["ids"], out["filtered_ids"])
+    if only == "segmap":
         return
     for key, case in ADJOINT_CASES.items():
         out = run_adjoint_case(ap, key, case)
