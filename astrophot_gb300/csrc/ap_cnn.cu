@@ -252,10 +252,12 @@ bool g_gemm_tune = false;
 std::mutex g_tune_mutex;
 std::map<std::tuple<int, int, int, int, int>, int> g_tuned;  // (A_T, B_T, R, S, T) -> tile shape
 
-// ep.bias set: the epilogue is fused when the reduction is not split; *fused tells the caller
+// ep.bias set: the epilogue is fused when the reduction is not split; *fused tells the caller.
+// allow_split = false keeps every reduction in one CTA (no float atomics: results independent of
+// scheduling, as the forward pass needs for reproducible proposals)
 template <bool A_T, bool B_T>
 cudaError_t gemm(const bf16* A, int lda, const bf16* B, int ldb, float* C, int ldc, int R, int S, int T,
-                 cudaStream_t st, GemmEpilogue ep = GemmEpilogue(), bool* fused = nullptr) {
+                 cudaStream_t st, GemmEpilogue ep = GemmEpilogue(), bool* fused = nullptr, bool allow_split = true) {
   if (fused) *fused = false;
   if (R <= 0 || S <= 0 || T <= 0) return cudaSuccess;
   if (!g_num_sms) {
@@ -270,7 +272,7 @@ cudaError_t gemm(const bf16* A, int lda, const bf16* B, int ldb, float* C, int l
     // split the reduction when the output tiles alone cannot fill the GPU
     int split = 1;
     const int want = 2 * g_num_sms;
-    if (tiles < want) {
+    if (allow_split && tiles < want) {
       const int max_split = (T + 8 * kBK - 1) / (8 * kBK);  // at least 8 k-steps per split
       split = (want + tiles - 1) / tiles;
       if (split > max_split) split = max_split;
@@ -544,6 +546,7 @@ __global__ void k_moments_init(const float* __restrict__ data, const float* __re
   const float sk = sky[b], thr = 1.0f * sigma[b];
   __shared__ double red[6][8];
   __shared__ float hist_f[kMomBins], hist_n[kMomBins];
+  __shared__ float whist_f[8][kMomBins], whist_n[8][kMomBins];  // per-warp histograms (256 threads)
   __shared__ double sh_par[6];
   double S = 0, Sx = 0, Sy = 0;
   for (int i = threadIdx.x; i < kImg * kImg; i += blockDim.x) {
@@ -596,21 +599,51 @@ __global__ void k_moments_init(const float* __restrict__ data, const float* __re
     sh_par[2] = q;
     sh_par[3] = pa;
   }
-  for (int k = threadIdx.x; k < kMomBins; k += blockDim.x) {
-    hist_f[k] = 0.f;
-    hist_n[k] = 0.f;
+  for (int k = threadIdx.x; k < 8 * kMomBins; k += blockDim.x) {
+    whist_f[k / kMomBins][k % kMomBins] = 0.f;
+    whist_n[k / kMomBins][k % kMomBins] = 0.f;
   }
   __syncthreads();
   const double q = sh_par[2], pa = sh_par[3];
   const double ca = cos(pa - 1.5707963267948966), sa = sin(pa - 1.5707963267948966);
   const float rmax = 0.75f * kImg;
-  for (int i = threadIdx.x; i < kImg * kImg; i += blockDim.x) {
-    const double x = (i % kImg) + 0.5 - sh_par[0], y = (i / kImg) + 0.5 - sh_par[1];
-    const double u = x * ca + y * sa, v = (-x * sa + y * ca) / q;
-    const float r = (float)sqrt(u * u + v * v);
-    const int k = min(kMomBins - 1, (int)(r / rmax * kMomBins));
-    atomicAdd(&hist_f[k], d[i] - sk);
-    atomicAdd(&hist_n[k], 1.f);
+  // radial histogram in a fixed summation order (no float atomics): each warp walks its 512
+  // pixels 32 at a time; the lanes of one bin sum their values in lane order and the lowest of
+  // them adds the sum to the warp's histogram; the 8 warp histograms are then added in order
+  {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int per_warp = kImg * kImg / 8;
+    for (int base = warp * per_warp; base < (warp + 1) * per_warp; base += 32) {
+      const int i = base + lane;
+      const double x = (i % kImg) + 0.5 - sh_par[0], y = (i / kImg) + 0.5 - sh_par[1];
+      const double u = x * ca + y * sa, v = (-x * sa + y * ca) / q;
+      const float r = (float)sqrt(u * u + v * v);
+      const int k = min(kMomBins - 1, (int)(r / rmax * kMomBins));
+      const float val = d[i] - sk;
+      const unsigned same = __match_any_sync(0xffffffffu, k);
+      float acc = 0.f, cnt = 0.f;
+      for (int src = 0; src < 32; ++src) {
+        const float vs = __shfl_sync(0xffffffffu, val, src);
+        if ((same >> src) & 1u) {
+          acc += vs;
+          cnt += 1.f;
+        }
+      }
+      if (lane == __ffs(same) - 1) {
+        whist_f[warp][k] += acc;
+        whist_n[warp][k] += cnt;
+      }
+    }
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < kMomBins; k += blockDim.x) {
+    float f = 0.f, c = 0.f;
+    for (int w = 0; w < 8; ++w) {
+      f += whist_f[w][k];
+      c += whist_n[w][k];
+    }
+    hist_f[k] = f;
+    hist_n[k] = c;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -674,7 +707,7 @@ cudaError_t forward(const float* params, const bf16* wb, const float* x, int64_t
     ep.relu = last ? 0 : 1;
     float* cout = last ? w.out : w.pre[l];
     bool fused = false;
-    e = gemm<false, false>(w.col[l], d.K, wb + w_off(l), d.K, cout, d.N, (int)M, d.N, d.K, st, ep, &fused);
+    e = gemm<false, false>(w.col[l], d.K, wb + w_off(l), d.K, cout, d.N, (int)M, d.N, d.K, st, ep, &fused, false);
     if (e != cudaSuccess) return e;
     if (!fused)
       k_bias_act<<<grid_for(M * d.N), 256, 0, st>>>(cout, params + b_off(l), last ? nullptr : w.act[l],
