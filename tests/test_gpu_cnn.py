@@ -266,3 +266,23 @@ def test_learned_fit_refits_poor_stamps_with_the_plain_method(N):
     assert np.array_equal(refit, cp < c0)
     h = cnn.heuristic_init(st, n)
     assert torch.equal(init[torch.as_tensor(refit, device=init.device)], h[torch.as_tensor(refit, device=h.device)])
+
+
+def test_learned_fit_is_reproducible(N):
+    """Proposal, moments values and the LM results are bitwise the same from run to run and for
+    a stamp fitted in a smaller batch (fixed summation orders, no float atomics)."""
+    from astrophot_gb300 import cnn
+
+    net = cnn.InitNet.load()
+    n = 64
+    st = cnn.make_stamps(n, seed=99)
+    assert torch.equal(net.propose(st.data, st.sigma, n), net.propose(st.data, st.sigma, n))
+    assert torch.equal(cnn.moments_init(st, n), cnn.moments_init(st, n))
+    a = cnn.learned_fit(net, st, n)
+    b = cnn.learned_fit(net, st, n)
+    assert torch.equal(a[0], b[0]) and torch.equal(a[2][1], b[2][1]) and torch.equal(a[2][3], b[2][3])
+    idx = np.arange(0, n, 4)
+    sub = cnn.subset(st, idx)
+    c = cnn.learned_fit(net, sub, len(idx))
+    t = torch.as_tensor(idx, device=a[2][1].device)
+    assert torch.equal(c[2][1], a[2][1][t])
