@@ -8,7 +8,7 @@ Workloads (one "step" = every stamp of the workload fitted once, from its initia
       SNR ~ U(10, 200).
       A step = CNN proposal (bf16 tensor-core kernels) + moments fallback, chi^2 of both,
       per-stamp selection, one batched LM of all stamps (7 free parameters), then LM's final
-      chi^2 as the judge: stamps left more than 5 sigma above chi^2/ndf = 1 are fitted again by
+      chi^2 decides: stamps left more than 5 sigma above chi^2/ndf = 1 are fitted again by
       the plain method and keep the better fit.
       Reported beside it: the plain method = LM from the reference's own heuristic initial
       values (initialize(): centre of light, PA, isophote q, profile Nelder-Mead, computed by
