@@ -36,7 +36,7 @@ _ERR_NAMES = {
     AP_ERR_NOT_BOUND: "batch not bound to a workspace",
 }
 
-PROFILE = {"sersic": 0, "exponential": 1}
+PROFILE = {"sersic": 0, "exponential": 1, "moffat": 2}
 SAMPLING = {"midpoint": 0, "simpsons": 1, "quad": 2, "trapezoid": 3}
 INTEGRATE = {"none": 0, "threshold": 1}
 PSF_NONE, PSF_FULL, PSF_FULL_NOSHIFT = 0, 1, 2
@@ -113,6 +113,8 @@ EXPORTS = [
     ("ap_batch_set_threshold_numel", [_P, _PD]),
     ("ap_render", [_P, _P, _P, _P, _P]),
     ("ap_jacobian", [_P, _P, _P, _P, _P, _I32, _P]),
+    ("ap_render_psf_derivative", [_P, _P, _P, _P, _P, _P]),
+    ("ap_psf_normalize", [_I32, _I32, _P, _P, _P, _P, _P]),
     ("ap_render_vjp", [_P, _P, _P, _P, _I32, _P, _P]),
     ("ap_batch_autotune", [_P, _P, _P, _I32, _PI32, _PD, _P]),
     ("ap_batch_set_grid", [_P, _PI32]),
@@ -410,6 +412,16 @@ class StampBatch:
         if out is None:
             out = torch.empty(self.out_pixels, dtype=torch.float32, device=self.device)
         check(self.lib.ap_render(self.handle, _ptr(params), _ptr(psf), _ptr(out), _stream()), "ap_render")
+        return out
+
+    def render_psf_derivative(self, params: torch.Tensor, psf: torch.Tensor, dpsf: torch.Tensor,
+                              out: Optional[torch.Tensor] = None):
+        """d model / d theta for a PSF change dpsf = d psf / d theta (ap_render_psf_derivative)."""
+        params = params.to(self.device, torch.float64).contiguous()
+        if out is None:
+            out = torch.empty(self.out_pixels, dtype=torch.float32, device=self.device)
+        check(self.lib.ap_render_psf_derivative(self.handle, _ptr(params), _ptr(psf), _ptr(dpsf.contiguous()),
+                                                _ptr(out), _stream()), "ap_render_psf_derivative")
         return out
 
     GRID_KNOBS = ("sample", "integrate", "conv", "psf")

@@ -123,7 +123,8 @@ namespace {
 int validate_options(const ap_options* o) {
   if (!o) return AP_ERR_ARG;
   if (o->fft_min_kernel < 0) return AP_ERR_ARG;
-  if (o->profile != AP_PROFILE_SERSIC && o->profile != AP_PROFILE_EXPONENTIAL) return AP_ERR_UNSUPPORTED;
+  if (o->profile != AP_PROFILE_SERSIC && o->profile != AP_PROFILE_EXPONENTIAL && o->profile != AP_PROFILE_MOFFAT)
+    return AP_ERR_UNSUPPORTED;
   if (o->sampling_mode < AP_SAMPLING_MIDPOINT || o->sampling_mode > AP_SAMPLING_TRAPEZOID)
     return AP_ERR_UNSUPPORTED;
   if (o->sampling_mode == AP_SAMPLING_QUAD &&
@@ -569,6 +570,21 @@ int ap_jacobian(ap_batch* b, const double* params, const float* psf, float* mode
   return render_common(b, params, psf, model, jac, ops, stream);
 }
 
+int ap_render_psf_derivative(ap_batch* b, const double* params, const float* psf, const float* dpsf,
+                             float* model, ap_stream_t stream) {
+  if (!b || !params || !psf || !dpsf || !model) return AP_ERR_ARG;
+  if (!b->bound) return AP_ERR_NOT_BOUND;
+  if (b->opt.psf_mode == AP_PSF_NONE || b->opt.has_sky) return AP_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = check_cuda(launch_eval_setup(b->args, params, NPARAM, 0, nullptr, OP_FWD | OP_WRITE_MODEL, s));
+  if (rc) return rc;
+  ConvIO io{};
+  io.psf = dpsf;
+  io.psf_base = psf;
+  io.model_out = model;
+  return check_cuda(launch_render_pass(b->args, io, b->conv_smem, false, s, &b->prof));
+}
+
 int ap_render_vjp(ap_batch* b, const double* params, const float* psf, const float* grad_model,
                   int32_t flags, double* grad_params, ap_stream_t stream) {
   if (!b || !params || !grad_model || !grad_params) return AP_ERR_ARG;
@@ -685,6 +701,7 @@ int ap_reference_init(ap_batch* b, const float* data, const uint8_t* mask, int32
                       int32_t* status, void* workspace, int64_t workspace_bytes, ap_stream_t stream) {
   if (!b || !data || !params || !status || (known_mask & ~0xff)) return AP_ERR_ARG;
   if (!b->bound) return AP_ERR_NOT_BOUND;
+  if (b->opt.profile == AP_PROFILE_MOFFAT) return AP_ERR_UNSUPPORTED;
   if (int rc = refinit_geometry_ok(b)) return rc;
   const RefInitPlan P = plan_reference_init(b->stamps.data(), b->n);
   if (P.scratch_bytes > 0 && (!workspace || workspace_bytes < P.scratch_bytes)) return AP_ERR_WORKSPACE;
@@ -815,6 +832,8 @@ int ap_lm_fit(ap_batch* b, const float* data, const float* weight, const uint8_t
   if (!b || !data || !fixed_params || !state || !lm_ws || !chi2_out || !iters_out || !status_out)
     return AP_ERR_ARG;
   if (!b->bound) return AP_ERR_NOT_BOUND;
+  // the device LM's representation maps carry the Sersic index limits (0.36, 8)
+  if (b->opt.profile == AP_PROFILE_MOFFAT) return AP_ERR_UNSUPPORTED;
   int rc = lm_validate(lm);
   if (rc) return rc;
   if (b->opt.psf_mode != AP_PSF_NONE && !psf) return AP_ERR_ARG;

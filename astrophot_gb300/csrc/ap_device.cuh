@@ -210,6 +210,8 @@ struct BatchArgs {
 // buffers of the convolve/accumulate pass
 struct ConvIO {
   const float* psf;       // packed raw PSFs
+  const float* psf_base;  // non-null: psf is a perturbation of these raw PSFs and the render
+                          // convolves with the derivative of the renormalised shifted kernel
   const float* data;      // packed output pixels (may be null)
   const float* weight;    // (null = 1)
   const uint8_t* mask;    // (null = none)
@@ -256,6 +258,10 @@ struct Sample {
 // log2 adds <= 2.4e-7 absolute, so t = 2^(log2(u)/n) has relative error <= 4e-7 + 5e-7/n;
 // the exponent b (t - 1) inherits b t times that, and the MUFU exp adds <= 3e-7 plus
 // 1.2e-7 per unit of exponent.  Hence |dI/I| <= 4e-7 + (|b (t - 1)| + b) (5e-7 + 5e-7/n).
+// Moffat (e.bn = n, e.invn = 1): ln(1 + u^2) carries <= 2.4e-7 absolute from the log2, 6e-8
+// from rounding 1 + u^2 and 3e-7 from u's own error, n times that in the exponent n ln(1 + u^2),
+// plus 2.4e-7 relative from its rounding and the exp's 1.4e-7 per unit: the same formula with
+// invn = 1 gives 4e-7 + (|arg| + n) 1e-6, above that bound.
 __device__ __forceinline__ float sample_rel_err(const EvalF& e, float arg) {
   return 4e-7f + (fabsf(arg) + e.bn) * (5e-7f + 5e-7f * e.invn);
 }
@@ -270,12 +276,19 @@ __device__ __forceinline__ Sample eval_profile(const EvalF& e, int kind, float X
   const float R = sqrtf(fmaf(Xr, Xr, fmaf(Yr, Yr, e.soft2)));
   const float u = R * e.invRe;
   const float amp = e.amp * area_scale;
-  float t = u, lu2 = 0.f;
-  if (kind == AP_PROFILE_SERSIC) {
-    lu2 = __log2f(u);
-    t = exp2f(lu2 * e.invn);
+  float t = u, lu2 = 0.f, w = 1.f, arg;
+  if (kind == AP_PROFILE_MOFFAT) {
+    // I0 / (1 + u^2)^n = I0 exp(-n ln(1 + u^2)); e.bn holds n
+    w = fmaf(u, u, 1.f);
+    lu2 = __log2f(w);
+    arg = e.bn * (lu2 * 0.6931471805599453f);
+  } else {
+    if (kind == AP_PROFILE_SERSIC) {
+      lu2 = __log2f(u);
+      t = exp2f(lu2 * e.invn);
+    }
+    arg = e.bn * (t - 1.f);
   }
-  const float arg = e.bn * (t - 1.f);
   const float I = amp * __expf(-arg);
   out.v = I;
   out.arg = arg;
@@ -287,6 +300,11 @@ __device__ __forceinline__ Sample eval_profile(const EvalF& e, int kind, float X
       dIdR = -I * bt * invR;
       out.g[GRE] = I * bt * e.invRe;
       out.g[GN] = I * (-e.dbn * (t - 1.f) + bt * (lu2 * 0.6931471805599453f) * e.invn);
+    } else if (kind == AP_PROFILE_MOFFAT) {
+      const float nu = 2.f * e.bn * u / w;  // -d ln I / d u
+      dIdR = -I * nu * e.invRe;
+      out.g[GRE] = I * nu * u * e.invRe;
+      out.g[GN] = -I * (lu2 * 0.6931471805599453f);
     } else {
       dIdR = -I * e.bn * e.invRe;
       out.g[GRE] = I * e.bn * u * e.invRe;
@@ -309,6 +327,10 @@ __device__ __forceinline__ double eval_profile64(const EvalDev& e, int kind, dou
   const double amp = e.amp64 * area_scale;
   if (kind == AP_PROFILE_SERSIC) {
     return amp * exp(-e.bn64 * (exp(log(R * e.invRe64) * e.invn64) - 1.0));
+  }
+  if (kind == AP_PROFILE_MOFFAT) {
+    const double u = R * e.invRe64;
+    return amp / pow(1.0 + u * u, e.bn64);
   }
   return amp * exp(-e.bn64 * ((R * e.invRe64) - 1.0));
 }

@@ -36,13 +36,18 @@ __device__ __forceinline__ double sersic_db64(double n) {
 }
 
 // d value / d representation (utils/conversions/optimization.py:40-47), from the value.
-__device__ __forceinline__ double drep_from_value(int slot, double v) {
+__device__ __forceinline__ double drep_from_value(int kind, int slot, double v) {
   switch (slot) {
     case PQ: {  // limits (0, 1)
       const double r = tan((v - 0.0) * kPi / 1.0 - kPi / 2);
       return 1.0 / (kPi * (r * r + 1));
     }
-    case PN: {  // limits (0.36, 8)
+    case PN: {
+      if (kind == AP_PROFILE_MOFFAT) {  // limits (0.1, 10), models/moffat_model.py:89
+        const double r = tan((v - 0.1) * kPi / (10.0 - 0.1) - kPi / 2);
+        return (10.0 - 0.1) / (kPi * (r * r + 1));
+      }
+      // limits (0.36, 8)
       const double r = tan((v - 0.36) * kPi / (8.0 - 0.36) - kPi / 2);
       return (8.0 - 0.36) / (kPi * (r * r + 1));
     }
@@ -115,19 +120,28 @@ __global__ void k_eval_setup(BatchArgs b, const double* params, int64_t stamp_st
   e.Re = (float)v[PRE];
   e.invRe64 = 1.0 / v[PRE];
   e.invRe = (float)e.invRe64;
-  const double n = (b.kind == AP_PROFILE_SERSIC) ? v[PN] : 1.0;
-  e.invn64 = 1.0 / n;
-  e.invn = (float)e.invn64;
-  e.bn64 = sersic_b64(n);
-  e.bn = (float)e.bn64;
-  e.dbn = (float)sersic_db64(n);
+  const double n = (b.kind != AP_PROFILE_EXPONENTIAL) ? v[PN] : 1.0;
+  if (b.kind == AP_PROFILE_MOFFAT) {  // I0 / (1 + (R/Rd)^2)^n: the power in bn, Rd in Re
+    e.invn64 = 1.0 / n;
+    e.invn = 1.f;  // (FP32 error bound of eval_profile)
+    e.bn64 = n;
+    e.bn = (float)n;
+    e.dbn = 0.f;
+  } else {
+    e.invn64 = 1.0 / n;
+    e.invn = (float)e.invn64;
+    e.bn64 = sersic_b64(n);
+    e.bn = (float)e.bn64;
+    e.dbn = (float)sersic_db64(n);
+  }
   e.amp64 = st.pixel_area * pow(10.0, v[PIE]);
   e.amp = (float)e.amp64;
   e.sky = b.has_sky ? (float)(st.pixel_area * pow(10.0, v[PF])) : 0.f;
   e.soft2_64 = b.softening64 * b.softening64;
   e.soft2 = (float)e.soft2_64;
   // integration reference: Sersic total flux / numel (models/sersic_model.py:78-89,
-  // utils/conversions/functions.py:168-190); exponential uses sum(deep) / numel later
+  // utils/conversions/functions.py:168-190); exponential and Moffat use sum(deep) / numel
+  // later (the default _integrate_reference, models/_model_methods.py:151-152)
   if (b.kind == AP_PROFILE_SERSIC) {
     const double Ie = pow(10.0, v[PIE]);
     const double bn = e.bn64;
@@ -138,7 +152,7 @@ __global__ void k_eval_setup(BatchArgs b, const double* params, int64_t stamp_st
     e.thresh64 = 0.0;
   }
   e.thresh = (float)e.thresh64;
-  for (int i = 0; i < NPARAM; ++i) e.drep[i] = (float)drep_from_value(i, v[i]);
+  for (int i = 0; i < NPARAM; ++i) e.drep[i] = (float)drep_from_value(b.kind, i, v[i]);
 }
 
 // Compacted work lists of this pass: the tiles of active (stamp, slot) pairs only, so the
@@ -160,7 +174,7 @@ __global__ void k_build_lists(BatchArgs b) {
   const int ops = b.evals[t].ops;
   if (b.psf_mode != AP_PSF_NONE && st.fft_nx == 0) {  // (FFT-convolved stamps: not k_conv's work)
     const bool jac = (ops & OP_JAC) != 0, shiftmode = (b.psf_mode == AP_PSF_FULL);
-    const int nconv = jac ? ((shiftmode ? 3 : 1) + (b.kind == AP_PROFILE_SERSIC ? 4 : 3) +
+    const int nconv = jac ? ((shiftmode ? 3 : 1) + (b.kind != AP_PROFILE_EXPONENTIAL ? 4 : 3) +
                              ((shiftmode && !(ops & OP_VJP_COORD)) ? 0 : 2))
                           : 1;
     atomicAdd(b.work_ctr, (unsigned long long)st.nx * st.ny * 2ull *
@@ -214,6 +228,34 @@ __device__ __forceinline__ double warp_sum_d(double v) {
   return v;
 }
 
+// Derivative of the shifted, renormalised kernel N(K) = S(K) / sum S(K) (S: the shift, linear)
+// along a perturbation D of the raw kernel K:
+//   dN = (S(D) - N(K) sum S(D)) / sum S(K),
+// so that a render with dN in place of N(K) is d model / d (PSF parameter) when D = dK/dtheta.
+__device__ void psf_derivative_warp(const BatchArgs& b, const float* D, const float* K, int s, int slot,
+                                    int lane) {
+  const EvalDev& e = b.evals[s * 2 + slot];
+  const StampDev& st = b.stamps[s];
+  const int kp2 = st.kpx * st.kpy;
+  const float* Pd = D + st.psf_off;
+  const float* Pk = K + st.psf_off;
+  float* out = b.spsf + st.spsf_off + (int64_t)slot * 3 * kp2;
+  const bool shift = (b.psf_mode == AP_PSF_FULL);
+  const float sx = (float)e.shift[0], sy = (float)e.shift[1];
+  auto val = [&](const float* P, int idx) -> float {
+    return shift ? shifted_psf_at_f(P, st.kx, st.ky, idx % st.kpx, idx / st.kpx, sx, sy).v : P[idx];
+  };
+  double SK = 0, SD = 0;
+  for (int idx = lane; idx < kp2; idx += 32) {
+    SK += val(Pk, idx);
+    SD += val(Pd, idx);
+  }
+  SK = warp_sum_d(SK);
+  SD = warp_sum_d(SD);
+  const float inv = (float)(1.0 / SK), c = (float)(SD / (SK * SK));
+  for (int idx = lane; idx < kp2; idx += 32) out[idx] = val(Pd, idx) * inv - val(Pk, idx) * c;
+}
+
 // one warp per (stamp, evaluation slot): sums in FP64 across the warp, values in FP32
 __device__ void psf_shift_warp(const BatchArgs& b, const float* psf, int s, int slot, int lane) {
   const EvalDev& e = b.evals[s * 2 + slot];
@@ -252,12 +294,17 @@ __device__ void psf_shift_warp(const BatchArgs& b, const float* psf, int s, int 
   }
 }
 
-__global__ void k_psf_shift(BatchArgs b, const float* psf) {
+// psf_base == nullptr: the shifted, renormalised kernels of psf; otherwise psf is a
+// perturbation of psf_base and the kernels are the derivatives of psf_derivative_warp
+__global__ void k_psf_shift(BatchArgs b, const float* psf, const float* psf_base) {
   const uint32_t n = b.counters[9];
   const int wpb = blockDim.x >> 5, lane = threadIdx.x & 31;
   for (uint32_t it = blockIdx.x * wpb + (threadIdx.x >> 5); it < n; it += gridDim.x * wpb) {
     const int t = b.slist[it];
-    psf_shift_warp(b, psf, t >> 1, t & 1, lane);
+    if (psf_base)
+      psf_derivative_warp(b, psf, psf_base, t >> 1, t & 1, lane);
+    else
+      psf_shift_warp(b, psf, t >> 1, t & 1, lane);
   }
 }
 
@@ -333,7 +380,7 @@ __device__ void sample_tile(const BatchArgs& b, const EvalF& e, int s, int slot,
     aux[p] = refsub;
     aux[b.work_pixels + p] = errb;
   }
-  if (b.kind == AP_PROFILE_EXPONENTIAL && b.integrate == AP_INTEGRATE_THRESHOLD) {
+  if (b.kind != AP_PROFILE_SERSIC && b.integrate == AP_INTEGRATE_THRESHOLD) {
     // sum(deep) for the default _integrate_reference (models/_model_methods.py:151-152)
     float v = warp_sum(valid ? deep : 0.f);
     __shared__ float sh[kTile * kTile / 32];
@@ -1036,7 +1083,7 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
 #pragma unroll
         for (int q = 0; q < NGRAD; ++q) {
           if (shiftmode && !(ops & OP_VJP_COORD) && (q == GX || q == GY)) continue;
-          if (b.kind != AP_PROFILE_SERSIC && q == GN) continue;
+          if (b.kind == AP_PROFILE_EXPONENTIAL && q == GN) continue;
           cv[3 + q][o] = pre[(int64_t)(3 + q) * npix + i];
         }
       }
@@ -1057,7 +1104,7 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
     const int row0 = y0 + st.by - cy, col0 = x0 + st.bx - cx;
     for (int pl = 0; pl < nplanes; ++pl) {
       if (pl > 0 && shiftmode && !(ops & OP_VJP_COORD) && (pl - 1 == GX || pl - 1 == GY)) continue;
-      if (pl > 0 && b.kind != AP_PROFILE_SERSIC && pl - 1 == GN) continue;
+      if (pl > 0 && b.kind == AP_PROFILE_EXPONENTIAL && pl - 1 == GN) continue;
       __syncthreads();
       const float* src = b.work + work_plane(b, slot, pl) + st.work_off;
       // rows over warps, columns over lanes: coalesced reads; stored column-major (pitch TP,
@@ -1345,12 +1392,12 @@ cudaError_t launch_render_pass(const BatchArgs& b, const ConvIO& io, size_t conv
   E(t);
   if (b.psf_mode != AP_PSF_NONE) {
     t = B(KC_PSF);
-    k_psf_shift<<<grid(2 * (int64_t)b.n_stamps, knob(GK_PSF, 8)), 256, 0, s>>>(b, io.psf);
+    k_psf_shift<<<grid(2 * (int64_t)b.n_stamps, knob(GK_PSF, 8)), 256, 0, s>>>(b, io.psf, io.psf_base);
     E(t);
   }
   t = B(KC_SAMPLE);
   k_sample<<<grid(2 * (int64_t)b.n_work_tiles, knob(GK_SAMPLE, 8)), kTile * kTile, 0, s>>>(b);
-  if (b.kind == AP_PROFILE_EXPONENTIAL && b.integrate == AP_INTEGRATE_THRESHOLD)
+  if (b.kind != AP_PROFILE_SERSIC && b.integrate == AP_INTEGRATE_THRESHOLD)
     k_exp_threshold<<<(b.n_stamps * 2 + 127) / 128, 128, 0, s>>>(b);
   E(t);
   if (b.integrate == AP_INTEGRATE_THRESHOLD) {
@@ -1506,7 +1553,7 @@ cudaError_t launch_chi2_only(const BatchArgs& b, const ConvIO& io, const float* 
 
 cudaError_t launch_psf_only(const BatchArgs& b, const float* psf, cudaStream_t s) {
   k_build_lists<<<(b.n_stamps * 2 + 127) / 128, 128, 0, s>>>(b);
-  k_psf_shift<<<std::max(1, std::min(2 * b.n_stamps, 1024)), 256, 0, s>>>(b, psf);
+  k_psf_shift<<<std::max(1, std::min(2 * b.n_stamps, 1024)), 256, 0, s>>>(b, psf, nullptr);
   return cudaGetLastError();
 }
 

@@ -352,9 +352,52 @@ inline int egrid(int64_t n) {
   return (int)(g < 1 ? 1 : (g > 4096 ? 4096 : g));
 }
 
+// ---- PSF model normalisation: K / sum K and its derivatives (one block) ---------------------------
+__global__ void k_psf_normalize(int n, int m, const float* __restrict__ img, const float* __restrict__ dimg,
+                                float* __restrict__ out, float* __restrict__ dout) {
+  constexpr int kMaxDir = 8;
+  double acc[1 + kMaxDir];
+#pragma unroll
+  for (int c = 0; c <= kMaxDir; ++c) acc[c] = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    acc[0] += (double)img[i];
+#pragma unroll
+    for (int c = 0; c < kMaxDir; ++c)
+      if (c < m) acc[1 + c] += (double)dimg[(int64_t)c * n + i];
+  }
+  __shared__ double sh[1 + kMaxDir][32];
+  __shared__ double tot[1 + kMaxDir];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int c = 0; c <= kMaxDir; ++c) {
+    const double r = warp_sum(acc[c]);
+    if (lane == 0) sh[c][w] = r;
+  }
+  __syncthreads();
+  if (threadIdx.x <= kMaxDir) {
+    double t = 0.0;
+    for (int k = 0; k < nw; ++k) t += sh[threadIdx.x][k];
+    tot[threadIdx.x] = t;
+  }
+  __syncthreads();
+  const double S = tot[0];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double k = (double)img[i] / S;
+    out[i] = (float)k;
+    for (int c = 0; c < m; ++c) dout[(int64_t)c * n + i] = (float)(((double)dimg[(int64_t)c * n + i] - k * tot[1 + c]) / S);
+  }
+}
+
 }  // namespace
 
 extern "C" {
+
+int ap_psf_normalize(int32_t n_pix, int32_t n_dir, const float* img, const float* dimg, float* out, float* dout,
+                     ap_stream_t stream) {
+  if (n_pix <= 0 || n_dir < 0 || n_dir > 8 || !img || !out || (n_dir > 0 && (!dimg || !dout))) return AP_ERR_ARG;
+  k_psf_normalize<<<1, 1024, 0, (cudaStream_t)stream>>>(n_pix, n_dir, img, dimg, out, dout);
+  return record_cuda(cudaGetLastError());
+}
 
 int ap_scene_forward(const ap_scene_source* sources, const int32_t* tile_ptr, const int32_t* tile_src,
                      const float* fwd, float sky, int32_t nx, int32_t ny, float* image, ap_stream_t stream) {

@@ -1,7 +1,8 @@
 """Model classes with the reference's construction API (``astrophot/models/``).
 
 ``AstroPhot_Model(model_type=...)`` builds ``Sersic_Galaxy`` ("sersic galaxy model"),
-``Exponential_Galaxy`` ("exponential galaxy model"), ``Flat_Sky`` ("flat sky model") or
+``Exponential_Galaxy`` ("exponential galaxy model"), ``Flat_Sky`` ("flat sky model"),
+``Moffat_PSF`` ("moffat psf model", a live PSF when given as a galaxy's ``psf``) or
 ``Group_Model`` ("group model") with the same parameters, limits, sampling knobs and
 defaults as the reference (``models/core_model.py:98-115``, ``model_object.py:57-111``,
 ``galaxy_model_object.py:44-53``, ``sersic_model.py:61-66``, ``exponential_model.py:58-62``,
@@ -35,6 +36,8 @@ __all__ = (
     "Sky_Model",
     "Flat_Sky",
     "Group_Model",
+    "PSF_Model",
+    "Moffat_PSF",
 )
 
 # full parameter-vector slots of the C ABI
@@ -240,8 +243,18 @@ class Component_Model(AstroPhot_Model):
     def psf(self, val):
         if val is None or isinstance(val, PSF_Image):
             self._psf = val
+        elif isinstance(val, PSF_Model):
+            self.set_aux_psf(val)
         else:
             self._psf = PSF_Image(val, pixelscale=self.target.pixelscale)
+
+    def set_aux_psf(self, aux_psf, add_parameters=True):
+        """``set_aux_psf`` (``model_object.py:133-149``): a PSF model sampled at every evaluation,
+        its parameters linked into this model's (ahead of the model's own, which are added
+        after the constructor's keyword arguments)."""
+        self._psf = aux_psf
+        if add_parameters:
+            self.parameters.link(aux_psf.parameters)
 
     @torch.no_grad()
     def initialize(self, target=None, parameters=None, **kwargs):
@@ -321,6 +334,87 @@ class Galaxy_Model(Component_Model):
             val = out[list(SLOT[name])] if len(SLOT[name]) > 1 else out[SLOT[name][0]]
             with Param_Unlock(node), Param_SoftLimits(node):
                 node.value = torch.as_tensor(val, dtype=config.ap_dtype)
+
+
+class PSF_Model(Component_Model):
+    """A point-source profile sampled on a PSF image (``psf_model_object.py:21-264``): centred on
+    the image's (0, 0), Simpson sampling at tolerance 1e-3 with threshold integration, the
+    image normalised to unit sum.  Its target is a ``PSF_Image``."""
+
+    parameter_specs = {"center": {"units": "arcsec", "value": (0.0, 0.0), "uncertainty": (0.1, 0.1),
+                                  "locked": True}}
+    _parameter_order = ("center",)
+    model_type = f"psf {AstroPhot_Model.model_type}"
+    sampling_mode = "simpsons"
+    sampling_tolerance = 1e-3
+    normalize_psf = True
+    usable = False
+
+    @property
+    def target(self):
+        return self._target
+
+    @target.setter
+    def target(self, tar):
+        if not (tar is None or isinstance(tar, PSF_Image)):
+            raise InvalidTarget("PSF_Model target must be a PSF_Image instance.")
+        self._target = tar
+
+
+class Moffat_PSF(PSF_Model):
+    """I(R) = 10^I0 / (1 + (R/Rd)^2)^n on the PSF image (``moffat_model.py:71-120``), I0 locked
+    at 0 by default.  As a galaxy's ``psf`` it is a live PSF: re-sampled from its parameters at
+    every evaluation and fitted with the galaxy (``astrophot_gb300.scene.LivePSF``)."""
+
+    model_type = f"moffat {PSF_Model.model_type}"
+    parameter_specs = {
+        "n": {"units": "none", "limits": (0.1, 10), "uncertainty": 0.05},
+        "Rd": {"units": "arcsec", "limits": (0, None)},
+        "I0": {"units": "log10(flux/arcsec^2)", "value": 0.0, "locked": True},
+    }
+    _parameter_order = PSF_Model._parameter_order + ("n", "Rd", "I0")
+    usable = True
+
+    def initialize(self, target=None, parameters=None, **kwargs):
+        missing = [p for p in ("n", "Rd", "I0") if self.parameters[p].value is None]
+        if missing:
+            raise SpecificationConflict(f"{self.name}: parameters without values: {missing}")
+
+    def live_psf(self, device=None):
+        """A :class:`~astrophot_gb300.scene.LivePSF` at the current values; its free parameters
+        are the unlocked ones of n, Rd, I0."""
+        from .scene import LivePSF
+
+        if self.normalize_psf is not True:
+            raise NotImplementedError("an unnormalised PSF model is not supported by the CUDA path")
+        if self.sampling_mode not in ("midpoint", "simpsons", "trapezoid") and not self.sampling_mode.startswith("quad"):
+            raise SpecificationConflict(f"unknown sampling mode: {self.sampling_mode}")
+        p = self.parameters
+        vals = {k: float(p[k].value.item()) for k in ("n", "Rd", "I0")}
+        free = tuple(k for k in ("n", "Rd", "I0") if not p[k].locked)
+        knobs = {k: getattr(self, k) for k in ("sampling_mode", "sampling_tolerance", "integrate_mode",
+                                               "integrate_max_depth", "integrate_gridding", "integrate_quad_level",
+                                               "softening")}
+        return LivePSF(vals, tuple(self.target.data.shape), self.target.pixel_length, free, knobs,
+                       config.ap_device if device is None else device)
+
+    def sample(self, image=None, window=None, parameters=None):
+        """``PSF_Model.sample``: the normalised PSF image, sampled on the GPU."""
+        img = self.live_psf().image()
+        return PSF_Image(torch.as_tensor(img, dtype=config.ap_dtype), pixelscale=self.target.pixelscale)
+
+    def jacobian(self, parameters=None, as_representation=False, window=None, pass_jacobian=None, **kwargs):
+        """d(normalised PSF image) / d(free parameters): [ky, kx, n_free]."""
+        if parameters is not None:
+            (self.parameters.vector_set_representation if as_representation else self.parameters.vector_set_values)(parameters)
+        live = self.live_psf()
+        _, dK = live.render(True)
+        if dK is None:
+            return torch.zeros(live.ky, live.kx, 0, dtype=config.ap_dtype)
+        J = dK.cpu().numpy().astype(np.float64).reshape(-1, live.ky, live.kx).transpose(1, 2, 0)
+        if as_representation:
+            J = J * live.drep(live.representation())[None, None, :]
+        return torch.as_tensor(J, dtype=config.ap_dtype)
 
 
 class Sersic_Galaxy(Galaxy_Model):
@@ -674,9 +768,12 @@ def _galaxies(components):
 
 
 def _needs_scene(owner, components):
-    """More than one galaxy, or a galaxy whose own window is not the group's window."""
+    """More than one galaxy, a galaxy whose own window is not the group's window, or a galaxy
+    convolved with a live PSF model."""
     gals = _galaxies(components)
     if len(gals) > 1:
+        return True
+    if gals and gals[0].psf_mode == "full" and isinstance(gals[0].psf, PSF_Model):
         return True
     if gals and gals[0] is not owner and gals[0]._window is not None and not (gals[0].window == owner.window):
         return True
@@ -708,6 +805,8 @@ def _scene_spec(owner, components):
     psf = gals[0].psf if knobs["psf_mode"] == "full" else None
     if psf is not None and any(g.psf is not psf for g in gals[1:]):
         raise NotImplementedError("galaxies of one group must share one PSF on the CUDA path")
+    if isinstance(psf, PSF_Model) and not isinstance(psf, Moffat_PSF):
+        raise NotImplementedError("the CUDA path's live PSF models are Moffat PSFs")
     center_owner = {}
     sources = []
     for gi, g in enumerate(gals):
@@ -748,9 +847,12 @@ def _make_scene(owner, components, with_data=True):
     else:
         data = weight = np.zeros((ny, nx))
         mask = None
-    scene = Scene(nx, ny, sources, None if psf is None else psf.data.numpy(), data, weight, mask=mask, sky=sky,
-                  scale=float(w.pixelscale[0, 0]), options=opts, origin=(float(origin[0]), float(origin[1])),
-                  device=config.ap_device)
+    live = psf.live_psf() if isinstance(psf, PSF_Model) else None
+    if live is not None and abs(live.scale - float(w.pixelscale[0, 0])) > 1e-9 * live.scale:
+        raise NotImplementedError("a live PSF needs the image's pixel scale on the CUDA path")
+    scene = Scene(nx, ny, sources, None if (psf is None or live is not None) else psf.data.numpy(), data, weight,
+                  mask=mask, sky=sky, scale=float(w.pixelscale[0, 0]), options=opts,
+                  origin=(float(origin[0]), float(origin[1])), device=config.ap_device, psf_model=live)
     if scene.P != len(owner.parameters.vector_values()):
         raise NotImplementedError("this parameter structure has no joint-vector mapping on the CUDA path")
     return scene

@@ -16,6 +16,13 @@
 ``SceneLM`` is ``LM.fit`` / ``LM.step`` (fit/lm.py:249-357, 428-493) with these primitives:
 the damping search, geodesic right-hand side, curvature test, convergence rules and
 ``res()`` of the reference, with all images, Jacobians and reductions on the device.
+
+A scene's PSF may be a live Moffat PSF model (``set_aux_psf``, models/model_object.py:133-149)
+instead of a fixed image: :class:`LivePSF` samples it on its PSF image at every evaluation, its
+free parameters lead the joint vector (the linked PSF node comes before the galaxy's own
+parameters), and their Jacobian columns are image-wide: every source's pre-convolution image
+convolved with the derivative of its shifted, renormalised kernel (``ap_render_psf_derivative``),
+summed over the image like the model.
 """
 
 from __future__ import annotations
@@ -29,12 +36,76 @@ import numpy as np
 import torch
 
 from . import _native as N
-from .transforms import SLOT_LIMITS, to_rep, to_value
+from .transforms import SLOT_LIMITS, drep_dvalue, to_rep, to_value
 
 __all__ = ("SceneSource", "Scene", "SceneLM", "SceneRenderFunction", "render")
 
 TILE = 32
 _SLOTS_OF = {"sersic": (0, 1, 2, 3, 4, 5, 6), "exponential": (0, 1, 2, 3, 5, 6)}
+
+# Moffat_PSF parameters: limits (models/moffat_model.py:88-92) and their slots in the render
+PSF_MODEL_LIMITS = {"n": ((0.1, 10.0), False), "Rd": ((0.0, None), False), "I0": ((None, None), False)}
+_PSF_SLOT = {"n": 4, "Rd": 5, "I0": 6}
+# PSF_Model class knobs (models/psf_model_object.py:50-80)
+PSF_MODEL_KNOBS = dict(sampling_mode="simpsons", sampling_tolerance=1e-3, integrate_mode="threshold",
+                       integrate_max_depth=3, integrate_gridding=5, integrate_quad_level=3, softening=1e-3)
+
+
+class LivePSF:
+    """A Moffat PSF model (I0 / (1 + (R/Rd)^2)^n, centred on its PSF image) sampled on the device
+    as ``PSF_Model.sample`` does (models/psf_model_object.py:180-264: sampling and threshold
+    integration, then ``normalize_psf``), with the derivatives of the normalised image with
+    respect to its ``free`` parameters (``ap_psf_normalize``)."""
+
+    def __init__(self, params: dict, shape, scale: float = 1.0, free=("n", "Rd"), knobs: Optional[dict] = None,
+                 device="cuda"):
+        self.params = {k: float(params.get(k, 0.0)) for k in ("n", "Rd", "I0")}
+        self.ky, self.kx = int(shape[0]), int(shape[1])
+        self.scale = float(scale)
+        self.free = tuple(free)
+        if any(f not in _PSF_SLOT for f in self.free):
+            raise ValueError(f"unknown Moffat PSF parameter in {self.free}")
+        kn = dict(PSF_MODEL_KNOBS)
+        kn.update(knobs or {})
+        mask = sum(1 << _PSF_SLOT[f] for f in self.free)
+        o = N.make_options(profile="moffat", psf_mode="none", free_mask=mask, has_sky=False, **kn)
+        origin = (-self.kx * self.scale / 2, -self.ky * self.scale / 2)  # the image centred on (0, 0)
+        self.device = torch.device(device)
+        self.batch = N.StampBatch([(self.kx, self.ky)], None, N.scale_geometry(1, self.scale, origin), o, self.device)
+        self.npix = self.kx * self.ky
+        self.K = torch.empty(self.npix, dtype=torch.float32, device=self.device)
+        self.dK = torch.empty((max(len(self.free), 1), self.npix), dtype=torch.float32, device=self.device)
+        self.lib = N.lib()
+
+    def _row(self):
+        p = self.params  # q = 1 and PA = pi/2 make the inclined transform the identity
+        return torch.tensor([[0.0, 0.0, 1.0, math.pi / 2, p["n"], p["Rd"], p["I0"], 0.0]], dtype=torch.float64)
+
+    def representation(self):
+        return np.array([to_rep(*PSF_MODEL_LIMITS[f], self.params[f]) for f in self.free])
+
+    def set_representation(self, rep):
+        for f, r in zip(self.free, rep):
+            self.params[f] = float(to_value(*PSF_MODEL_LIMITS[f], r))
+
+    def drep(self, rep):
+        """d value / d representation of the free parameters."""
+        return np.array([float(drep_dvalue(*PSF_MODEL_LIMITS[f], r)) for f, r in zip(self.free, rep)])
+
+    def render(self, grad: bool = False):
+        """(K [ky * kx], dK [n_free][ky * kx] or None): the normalised PSF image and its
+        value-space derivatives."""
+        m = len(self.free) if grad else 0
+        if m:
+            model, jac = self.batch.jacobian(self._row(), None, as_representation=False)
+        else:
+            model, jac = self.batch.render(self._row(), None), None
+        N.check(self.lib.ap_psf_normalize(self.npix, m, N._ptr(model), N._ptr(jac), N._ptr(self.K), N._ptr(self.dK),
+                                          N._stream()), "ap_psf_normalize")
+        return self.K, (self.dK[:m] if m else None)
+
+    def image(self) -> np.ndarray:
+        return self.render(False)[0].cpu().numpy().reshape(self.ky, self.kx).astype(np.float64)
 
 
 class ApSceneSource(ctypes.Structure):
@@ -70,17 +141,23 @@ class SceneSource:
 
 class Scene:
     """Sources on one ``nx`` x ``ny`` image (pixel scale ``scale``, the (0, 0) pixel corner at the
-    origin) with a locked flat sky ``sky`` (counts per pixel), one PSF (None: no convolution),
-    data / weight (1 / variance) / mask (True = ignored)."""
+    origin) with a locked flat sky ``sky`` (counts per pixel), one PSF (None: no convolution) or
+    a live PSF model ``psf_model`` (:class:`LivePSF`, its free parameters first in the joint
+    vector), data / weight (1 / variance) / mask (True = ignored)."""
 
     def __init__(self, nx: int, ny: int, sources: List[SceneSource], psf: Optional[np.ndarray], data, weight,
                  mask=None, sky: float = 0.0, scale: float = 1.0, options: Optional[dict] = None,
-                 fwd_chunk: int = 64, device="cuda", origin=(0.0, 0.0)):
+                 fwd_chunk: int = 64, device="cuda", origin=(0.0, 0.0), psf_model: Optional[LivePSF] = None):
         self.nx, self.ny, self.scale = int(nx), int(ny), float(scale)
         self.origin = (float(origin[0]), float(origin[1]))
         self.sources = list(sources)
         self.device = torch.device(device)
         self.sky = float(sky)
+        self.live_psf = psf_model
+        if psf_model is not None:
+            if psf is not None:
+                raise ValueError("a scene takes a fixed PSF image or a live PSF model, not both")
+            psf = psf_model.image()
         self.psf_np = None if psf is None else np.asarray(psf, dtype=np.float64)
         opts_kw = dict(options or {})
         dev = self.device
@@ -91,8 +168,11 @@ class Scene:
             self.mask = torch.as_tensor(np.asarray(mask, dtype=np.uint8).reshape(-1), device=dev).contiguous()
         n_used = self.nx * self.ny if self.mask is None else int((self.mask == 0).sum().item())
 
-        # ---- joint vector: sources in order, their free slots in parameter order --------------
-        self.slot_of = []  # per joint index: (source, full-vector slot)
+        # ---- joint vector: a live PSF's free parameters, then the sources in order and their
+        # free slots in parameter order --------------------------------------------------------
+        self.n_psf = 0 if psf_model is None else len(psf_model.free)
+        # per joint index: (source, full-vector slot), (-1, PSF parameter name) for the live PSF
+        self.slot_of = [(-1, f) for f in (psf_model.free if psf_model is not None else ())]
         self.gidx = []     # per source: {slot: joint index}
         for si, src in enumerate(self.sources):
             if src.kind not in _SLOTS_OF:
@@ -137,6 +217,9 @@ class Scene:
             self._jac_parts.append(dict(kind=kind, free=free, members=members, batch=jb, psf=jpsf, off=jac_total,
                                         nf=nf))
             jac_total += nf * jb.out_pixels
+        # live PSF columns: image-wide, one [ny * nx] plane per free PSF parameter
+        self.psf_jac_off = jac_total
+        jac_total += self.n_psf * self.nx * self.ny
         self.jac = torch.zeros(max(jac_total, 1), dtype=torch.float32, device=dev)
 
         # model renders.  The reference evaluates a windowed source of a group on the group's
@@ -177,9 +260,18 @@ class Scene:
                                             own=False))
                 fwd_total += len(members) * self.nx * self.ny
         self.fwd = torch.zeros(max(fwd_total, 1), dtype=torch.float32, device=dev)
+        self.fwd_d = torch.zeros_like(self.fwd) if psf_model is not None else None
 
-        # ---- source descriptors ----------------------------------------------------------------
-        desc = (ApSceneSource * len(self.sources))()
+        # ---- source descriptors (+ one whole-image entry carrying the live PSF columns) --------
+        ns = len(self.sources)
+        desc = (ApSceneSource * (ns + (1 if self.n_psf else 0)))()
+        if self.n_psf:
+            d = desc[ns]
+            d.jac_off, d.jac_stride = self.psf_jac_off, self.nx * self.ny
+            d.x0, d.y0, d.wx, d.wy = 0, 0, self.nx, self.ny
+            d.n_free = self.n_psf
+            for c in range(self.n_psf):
+                d.gidx[c] = c
         for part in self._fwd_parts:
             for k, si in enumerate(part["members"]):
                 d = desc[si]
@@ -217,6 +309,14 @@ class Scene:
         flat = np.array([s for l in lists for s in l] or [0], dtype=np.int32)
         self.tile_ptr = torch.tensor(ptr, device=dev)
         self.tile_src = torch.tensor(flat, device=dev)
+        # J h also sums the live PSF columns: the whole-image entry in every tile
+        self.jtile_ptr, self.jtile_src = self.tile_ptr, self.tile_src
+        if self.n_psf:
+            jl = [l + [ns] for l in lists]
+            jptr = np.zeros(len(jl) + 1, dtype=np.int32)
+            jptr[1:] = np.cumsum([len(l) for l in jl])
+            self.jtile_ptr = torch.tensor(jptr, device=dev)
+            self.jtile_src = torch.tensor(np.array([x for l in jl for x in l], dtype=np.int32), device=dev)
         pairs = []
         wins = [self._window(si) for si in range(len(self.sources))]
         for a in range(len(self.sources)):
@@ -225,6 +325,8 @@ class Scene:
                 (bx0, bx1), (by0, by1) = wins[b]
                 if max(ax0, bx0) < min(ax1, bx1) and max(ay0, by0) < min(ay1, by1):
                     pairs.append((a, b))
+        if self.n_psf:
+            pairs += [(a, ns) for a in range(ns)] + [(ns, ns)]
         self.n_pairs = len(pairs)
         self.pairs = torch.tensor(np.array(pairs, dtype=np.int32).reshape(-1, 2), device=dev).contiguous()
 
@@ -261,48 +363,87 @@ class Scene:
     def representation(self) -> np.ndarray:
         rep = np.zeros(self.P)
         for g, (si, sl) in enumerate(self.slot_of):
+            if si < 0:
+                continue
             rep[g] = to_rep(*SLOT_LIMITS[sl], self.sources[si].params[sl])
+        if self.n_psf:
+            rep[: self.n_psf] = self.live_psf.representation()
         return rep
 
     def set_representation(self, rep):
-        V = self.values_matrix(np.asarray(rep, dtype=np.float64))
+        rep = np.asarray(rep, dtype=np.float64)
+        V = self.values_matrix(rep)
         for si, src in enumerate(self.sources):
             src.params = list(V[si, :7])
+        if self.n_psf:
+            self.live_psf.set_representation(rep[: self.n_psf])
+
+    def _refresh_psf(self, rep, grad: bool):
+        """Sample the live PSF at ``rep`` and copy it into every batch's packed PSF; returns its
+        value-space derivatives when ``grad``."""
+        self.live_psf.set_representation(np.asarray(rep, dtype=np.float64)[: self.n_psf])
+        K, dK = self.live_psf.render(grad)
+        for part in self._jac_parts + self._fwd_parts:
+            if part["psf"] is not None:
+                part["psf"].copy_(K.repeat(part["psf"].numel() // K.numel()))
+        return dK
 
     # ---- device primitives -----------------------------------------------------------------
-    def forward(self, rep: np.ndarray) -> torch.Tensor:
-        """Model image [ny * nx] (float32) at the joint representation vector."""
-        V = self.values_matrix(rep)
+    def _render_sources(self, V, buf, render):
+        """Every source's model render into ``buf`` (the layout of ``self.fwd``) by
+        ``render(batch, params, packed psf, out)``."""
         for part in self._fwd_parts:
             b, m, mem = part["batch"], part["m"], part["members"]
             if part["own"]:
-                out = self.fwd[part["off"] : part["off"] + b.out_pixels]
-                b.render(torch.tensor(V[mem]), part["psf"], out=out)
+                render(b, torch.tensor(V[mem]), part["psf"], buf[part["off"] : part["off"] + b.out_pixels])
                 continue
             for c0 in range(0, len(mem), m):
                 chunk = mem[c0 : c0 + m]
                 params = np.zeros((m, 8))
                 params[:, :] = V[chunk[0]]
                 params[: len(chunk)] = V[chunk]
-                out = self.fwd[part["off"] + c0 * self.nx * self.ny : part["off"] + (c0 + m) * self.nx * self.ny]
+                out = buf[part["off"] + c0 * self.nx * self.ny : part["off"] + (c0 + m) * self.nx * self.ny]
                 if out.numel() == m * self.nx * self.ny:
-                    b.render(torch.tensor(params), part["psf"], out=out)
+                    render(b, torch.tensor(params), part["psf"], out)
                 else:
-                    tmp = b.render(torch.tensor(params), part["psf"])
+                    tmp = torch.empty(b.out_pixels, dtype=torch.float32, device=self.device)
+                    render(b, torch.tensor(params), part["psf"], tmp)
                     out.copy_(tmp[: out.numel()])
-        img = torch.empty(self.nx * self.ny, dtype=torch.float32, device=self.device)
+
+    def _combine(self, buf, sky, img):
         N.check(self.lib.ap_scene_forward(N._ptr(self.desc), N._ptr(self.tile_ptr), N._ptr(self.tile_src),
-                                          N._ptr(self.fwd), ctypes.c_float(self.sky), self.nx, self.ny, N._ptr(img),
+                                          N._ptr(buf), ctypes.c_float(sky), self.nx, self.ny, N._ptr(img),
                                           N._stream()), "ap_scene_forward")
         return img
 
+    def forward(self, rep: np.ndarray) -> torch.Tensor:
+        """Model image [ny * nx] (float32) at the joint representation vector."""
+        if self.n_psf:
+            self._refresh_psf(rep, False)
+        V = self.values_matrix(rep)
+        self._render_sources(V, self.fwd, lambda b, p, k, out: b.render(p, k, out=out))
+        img = torch.empty(self.nx * self.ny, dtype=torch.float32, device=self.device)
+        return self._combine(self.fwd, self.sky, img)
+
     def jacobian(self, rep: np.ndarray, as_representation: bool = True):
-        """Own-window Jacobians of every source (representation or value space) into ``self.jac``."""
+        """Own-window Jacobians of every source (representation or value space) into ``self.jac``,
+        and the image-wide columns of a live PSF's parameters."""
+        dK = self._refresh_psf(rep, True) if self.n_psf else None
         V = self.values_matrix(rep)
         for part in self._jac_parts:
             b = part["batch"]
             jac = self.jac[part["off"] : part["off"] + part["nf"] * b.out_pixels].view(part["nf"], b.out_pixels)
             b.jacobian(torch.tensor(V[part["members"]]), part["psf"], as_representation=as_representation, jac=jac)
+        if self.n_psf:
+            scale = self.live_psf.drep(np.asarray(rep, dtype=np.float64)[: self.n_psf]) if as_representation else \
+                np.ones(self.n_psf)
+            npx = self.nx * self.ny
+            for j in range(self.n_psf):
+                D = dK[j] * float(scale[j])
+                self._render_sources(V, self.fwd_d, lambda b, p, k, out: b.render_psf_derivative(
+                    p, k, D.repeat(k.numel() // D.numel()), out=out))
+                col = self.jac[self.psf_jac_off + j * npx : self.psf_jac_off + (j + 1) * npx]
+                self._combine(self.fwd_d, 0.0, col)
         return self.jac
 
     def jacobian_image(self, rep: np.ndarray, as_representation: bool = True) -> np.ndarray:
@@ -319,6 +460,9 @@ class Scene:
                     col = jac[part["off"] + c * b.out_pixels + o : part["off"] + c * b.out_pixels + o
                               + (x1 - x0) * (y1 - y0)]
                     out[y0:y1, x0:x1, self.gidx[si][sl]] += col.reshape(y1 - y0, x1 - x0)
+        npx = self.nx * self.ny
+        for j in range(self.n_psf):
+            out[:, :, j] += jac[self.psf_jac_off + j * npx : self.psf_jac_off + (j + 1) * npx].reshape(self.ny, self.nx)
         return out
 
     def _vjp_index(self, part):
@@ -340,6 +484,8 @@ class Scene:
         ``ap_render_vjp`` of every source's model render (PSF-convolved derivative tiles are
         recomputed and reduced on the fly, no Jacobian is stored).  ``reference_center`` gives
         the centre entries the reference's reverse-mode autograd gives under PSF shift."""
+        if self.n_psf:
+            raise NotImplementedError("the adjoint of a scene with a live PSF model is not implemented")
         V = self.values_matrix(rep)
         g_img = grad_image.to(self.device, torch.float32).reshape(-1).contiguous()
         out = np.zeros(self.P)
@@ -382,13 +528,14 @@ class Scene:
 
     def jt(self, img: torch.Tensor) -> torch.Tensor:
         out = torch.empty(self.P, dtype=torch.float64, device=self.device)
-        N.check(self.lib.ap_scene_jt(N._ptr(self.desc), len(self.sources), N._ptr(self.jac), N._ptr(img), self.nx,
+        N.check(self.lib.ap_scene_jt(N._ptr(self.desc), len(self.sources) + (1 if self.n_psf else 0), N._ptr(self.jac),
+                                     N._ptr(img), self.nx,
                                      self.P, N._ptr(out), N._stream()), "ap_scene_jt")
         return out
 
     def jvp(self, h: torch.Tensor) -> torch.Tensor:
         out = torch.empty(self.nx * self.ny, dtype=torch.float32, device=self.device)
-        N.check(self.lib.ap_scene_jvp(N._ptr(self.desc), N._ptr(self.tile_ptr), N._ptr(self.tile_src),
+        N.check(self.lib.ap_scene_jvp(N._ptr(self.desc), N._ptr(self.jtile_ptr), N._ptr(self.jtile_src),
                                       N._ptr(self.jac), N._ptr(h.contiguous()), self.nx, self.ny, N._ptr(out),
                                       N._stream()), "ap_scene_jvp")
         return out

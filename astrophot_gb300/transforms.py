@@ -54,6 +54,20 @@ def to_value(limits, cyclic, rep):
     return (np.arctan(rep) + np.pi / 2) * (hi - lo) / np.pi + lo
 
 
+def drep_dvalue(limits, cyclic, rep):
+    """d value / d representation (``d_inv_boundaries_dval``, optimization.py:40-47); 1 for
+    cyclic and unbounded parameters."""
+    lo, hi = limits
+    rep = np.asarray(rep, dtype=np.float64)
+    if cyclic or (lo is None and hi is None):
+        return np.ones_like(rep)
+    if lo is None:
+        return 0.5 - 0.5 * (rep - hi) / np.sqrt((rep - hi) ** 2 + 4)
+    if hi is None:
+        return 0.5 + 0.5 * (rep - lo) / np.sqrt((rep - lo) ** 2 + 4)
+    return (hi - lo) / (np.pi * (rep**2 + 1))
+
+
 def slots_to_rep(values: np.ndarray, free_mask: int) -> np.ndarray:
     """[n, 8] value-space rows -> [n, n_free] representation rows (fitted slots, in order)."""
     values = np.atleast_2d(np.asarray(values, dtype=np.float64))

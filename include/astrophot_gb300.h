@@ -49,6 +49,11 @@ typedef struct CUstream_st* ap_stream_t; /* same handle as cudaStream_t */
 /* ap_options.profile */
 #define AP_PROFILE_SERSIC 0
 #define AP_PROFILE_EXPONENTIAL 1
+/* Moffat (Moffat_PSF / Moffat_Galaxy, astrophot/models/moffat_model.py:71-120):
+ * I0 / (1 + (R/Rd)^2)^n with n in slot n, Rd in slot Re, log10 I0 in slot Ie; limits of n
+ * (0.1, 10).  Render, Jacobian and adjoint only (ap_lm_fit and ap_reference_init return
+ * AP_ERR_UNSUPPORTED): a fitted PSF's parameters are fitted by the scene LM. */
+#define AP_PROFILE_MOFFAT 2
 /* ap_options.sampling_mode */
 #define AP_SAMPLING_MIDPOINT 0
 #define AP_SAMPLING_SIMPSONS 1
@@ -139,6 +144,25 @@ int ap_render(ap_batch* batch, const double* params, const float* psf, float* mo
  * as_representation != 0 gives d model / d representation (the LM's space). */
 int ap_jacobian(ap_batch* batch, const double* params, const float* psf, float* model,
                 float* jac, int32_t as_representation, ap_stream_t stream);
+
+/* Derivative of the render along a change of the PSF image (a fitted PSF model's parameter):
+ * with N(K) = S(K) / sum S(K) the shifted, renormalised kernel of a raw PSF K (S: the bilinear
+ * shift, or the identity under AP_PSF_FULL_NOSHIFT), model[out_pixels] = the stamp's
+ * pre-convolution image convolved with dN = (S(dpsf) - N(psf) sum S(dpsf)) / sum S(psf), i.e.
+ * d model / d theta for dpsf = d psf / d theta.  psf and dpsf are packed like ap_render's psf.
+ * Needs psf_mode != AP_PSF_NONE and no sky (the sky does not depend on the PSF).  Replaces
+ * autograd through the live PSF of a model with an auxiliary PSF model: the PSF image sampled
+ * each evaluation (astrophot/models/model_object.py:133-149, 306-312) and convolved by
+ * _sample_convolve (astrophot/models/_model_methods.py:233-257). */
+int ap_render_psf_derivative(ap_batch* batch, const double* params, const float* psf, const float* dpsf,
+                             float* model, ap_stream_t stream);
+
+/* A PSF model's normalisation (PSF_Model.sample, normalize_psf: the image divided by its sum,
+ * astrophot/models/psf_model_object.py:250-252) and its derivative: out = img / S and
+ * dout[c] = (dimg[c] - out sum dimg[c]) / S for n_dir <= 8 directions, S = sum img (float64
+ * sums).  img[n_pix], dimg[n_dir][n_pix], out, dout: device. */
+int ap_psf_normalize(int32_t n_pix, int32_t n_dir, const float* img, const float* dimg, float* out, float* dout,
+                     ap_stream_t stream);
 
 /* Adjoint of the render (vector-Jacobian product): grad_params[n][n_free] (device, float64)
  * = sum over each stamp's output pixels of grad_model * d model / d theta, theta the fitted

@@ -40,7 +40,17 @@ PARAM_SPECS = {
     "Re": ((0.0, None), False),
     "Ie": ((None, None), False),
     "F": ((None, None), False),
+    # Moffat (models/moffat_model.py:88-92); its n takes KIND_SPECS' limits
+    "Rd": ((0.0, None), False),
+    "I0": ((None, None), False),
 }
+
+# per-kind overrides of PARAM_SPECS: Moffat_PSF's n, models/moffat_model.py:89
+KIND_SPECS = {"moffat": {"n": ((0.1, 10.0), False)}}
+
+
+def _spec(name, kind=None):
+    return KIND_SPECS.get(kind, {}).get(name, PARAM_SPECS[name])
 
 PARAM_ORDER = {
     # astrophot/models/model_object.py:61, galaxy_model_object.py:53,
@@ -48,12 +58,14 @@ PARAM_ORDER = {
     "sersic": ("center", "q", "PA", "n", "Re", "Ie"),
     "exponential": ("center", "q", "PA", "Re", "Ie"),
     "flat_sky": ("F",),
+    # psf_model_object.py:45, moffat_model.py:93
+    "moffat": ("center", "n", "Rd", "I0"),
 }
 
 
-def value_to_rep(name: str, val):
+def value_to_rep(name: str, val, kind=None):
     """``boundaries`` / ``cyclic_boundaries``: utils/conversions/optimization.py:6-14,50-54."""
-    (lo, hi), cyclic = PARAM_SPECS[name]
+    (lo, hi), cyclic = _spec(name, kind)
     val = np.asarray(val, dtype=np.float64)
     if cyclic:
         return lo + np.mod(val - lo, hi - lo)
@@ -66,9 +78,9 @@ def value_to_rep(name: str, val):
     return np.tan((val - lo) * np.pi / (hi - lo) - np.pi / 2)
 
 
-def rep_to_value(name: str, rep):
+def rep_to_value(name: str, rep, kind=None):
     """``inv_boundaries`` / ``cyclic_boundaries``: utils/conversions/optimization.py:17-25,50-54."""
-    (lo, hi), cyclic = PARAM_SPECS[name]
+    (lo, hi), cyclic = _spec(name, kind)
     rep = np.asarray(rep, dtype=np.float64)
     if cyclic:
         return lo + np.mod(rep - lo, hi - lo)
@@ -81,11 +93,11 @@ def rep_to_value(name: str, rep):
     return (np.arctan(rep) + np.pi / 2) * (hi - lo) / np.pi + lo
 
 
-def drep_dvalue(name: str, rep):
+def drep_dvalue(name: str, rep, kind=None):
     """d(value)/d(representation), i.e. ``d_inv_boundaries_dval``
     (utils/conversions/optimization.py:40-47); 1 for cyclic and free parameters
     (forward-mode AD of ``remainder`` has unit slope)."""
-    (lo, hi), cyclic = PARAM_SPECS[name]
+    (lo, hi), cyclic = _spec(name, kind)
     rep = np.asarray(rep, dtype=np.float64)
     if cyclic or (lo is None and hi is None):
         return np.ones_like(rep)
@@ -96,9 +108,9 @@ def drep_dvalue(name: str, rep):
     return (hi - lo) / (np.pi * (rep**2 + 1))
 
 
-def check_limits(name: str, val) -> None:
+def check_limits(name: str, val, kind=None) -> None:
     """``Parameter_Node._set_val_self`` limit check, astrophot/param/parameter.py:436-450."""
-    (lo, hi), cyclic = PARAM_SPECS[name]
+    (lo, hi), cyclic = _spec(name, kind)
     if cyclic:
         return
     val = np.asarray(val)
@@ -306,7 +318,7 @@ class Component:
 # brightness evaluation with analytic partials
 # ----------------------------------------------------------------------------
 
-GRAD_KEYS = ("X", "Y", "q", "PA", "n", "Re", "Ie", "F")
+GRAD_KEYS = ("X", "Y", "q", "PA", "n", "Re", "Ie", "F", "Rd", "I0")
 
 
 def eval_brightness(comp: Component, X, Y, pixel_area, grad: bool):
@@ -327,6 +339,19 @@ def eval_brightness(comp: Component, X, Y, pixel_area, grad: bool):
         if not grad:
             return I, None
         return I, {"F": I * np.log(10.0)}
+    if comp.kind == "moffat":
+        # Moffat_PSF: radial_evaluate_model on untransformed coordinates
+        # (models/_shared_methods.py:275-283, psf_model_object.py:140-142) -> moffat_torch
+        # (utils/parametric_profiles.py:89-100) with I0 * pixel_area (_shared_methods.py:355-361)
+        n, Rd = p["n"], p["Rd"]
+        R = np.sqrt(X**2 + Y**2 + comp.softening**2)
+        w = 1 + (R / Rd) ** 2
+        I = (pixel_area * 10 ** p["I0"]) / w**n
+        if not grad:
+            return I, None
+        dI_dR = -I * n * 2 * R / (Rd * Rd * w)
+        return I, {"n": -I * np.log(w), "Rd": I * n * 2 * R * R / (Rd**3 * w), "I0": I * np.log(10.0),
+                   "X": dI_dR * X / R, "Y": dI_dR * Y / R}
 
     q = p["q"]
     PA = p["PA"]
@@ -654,10 +679,14 @@ class Rendered:
     working_shape: Tuple[int, int] = (0, 0)
 
 
-def sample_component(comp: Component, win: Window, psf: Optional[PSF] = None, grad: bool = False) -> Rendered:
+def sample_component(comp: Component, win: Window, psf: Optional[PSF] = None, grad: bool = False,
+                     psf_dirs: Optional[dict] = None) -> Rendered:
     """Render one component on ``win`` (its own window) and, when ``grad``, the value-space
     Jacobian with respect to every parameter element (locked ones included; the caller
-    selects).  Follows ``Component_Model.sample`` (models/model_object.py:258-375)."""
+    selects).  Follows ``Component_Model.sample`` (models/model_object.py:258-375).
+    ``psf_dirs`` {name: d psf / d theta} (a live PSF model's parameters) adds the columns
+    ("psf", name): the pre-convolution image convolved with the derivative of the shifted,
+    renormalised kernel (models/_model_methods.py:233-243) along each."""
     p = comp.params
     center = p["center"] if "center" in p else np.zeros(2)
     center_partials_from_coords = True
@@ -707,6 +736,10 @@ def sample_component(comp: Component, win: Window, psf: Optional[PSF] = None, gr
                 dmod = [_reduce(conv(deep.val, k)[by : ny - by, bx : nx - bx], upscale) for k in dk]
                 jac[("center", 0)] = dmod[0] * Pi[0, 0] + dmod[1] * Pi[1, 0]
                 jac[("center", 1)] = dmod[0] * Pi[0, 1] + dmod[1] * Pi[1, 1]
+            for name, D in (psf_dirs or {}).items():
+                SD = shift_psf_bilinear(D, shift, False)[0] if shift is not None else D
+                dk = SD / norm - spsf * np.sum(SD) / norm**2
+                jac[("psf", name)] = _reduce(conv(deep.val, dk)[by : ny - by, bx : nx - bx], upscale)
         return Rendered(model, jac, select, (ny, nx))
 
     reference, deep = sample_init(comp, win.copy(), center, grad)

@@ -7,6 +7,7 @@ Run in a container that has the reference checkout (default path below, or
     python tests/golden/make_golden.py init     # only the initial-value cases
     python tests/golden/make_golden.py iter     # the initial-value and Iter_LM cases
     python tests/golden/make_golden.py segmap   # only the segmentation-map case
+    python tests/golden/make_golden.py auxpsf   # only the live-PSF-model case
 
 The reference (AstroPhot 0.x) is imported through a ``sys.modules`` shim for
 the optional packages it imports at module level but never calls on this
@@ -603,6 +604,54 @@ def run_adjoint_case(ap, key, case):
 
 # truth rendered by the reference (PSF convolved) + flat sky, Gaussian noise; data rounded to
 # float32 so every implementation reads the same numbers; ``mask`` names a mask pattern.
+AUXPSF_CASES = {
+    # a compact Sersic galaxy (Re 1.5 px, so the PSF shape is well constrained) on 48 x 48
+    # convolved with a live Moffat PSF model on a 15 x 15 PSF image
+    # (set_aux_psf, models/model_object.py:133-149): the PSF's n and Rd fitted with the galaxy
+    "auxpsf_48": dict(size=48, psf_size=15, seed=21,
+                      truth=dict(psf=dict(n=2.5, Rd=2.2), gal=[24.3, 23.6, 0.7, 1.0, 1.5, 1.5, 2.5]),
+                      init=dict(psf=dict(n=2.0, Rd=2.6), gal=[24.0, 24.0, 0.75, 0.9, 1.8, 1.8, 2.4])),
+}
+
+
+def build_auxpsf(ap, target, psf_target, vals, tag):
+    live = ap.models.AstroPhot_Model(name=f"psf {tag}", model_type="moffat psf model", target=psf_target,
+                                     parameters=dict(vals["psf"]))
+    cx, cy, q, PA, n, Re, Ie = vals["gal"]
+    gal = ap.models.AstroPhot_Model(name=f"gal {tag}", model_type="sersic galaxy model", target=target,
+                                    psf_mode="full", psf=live,
+                                    parameters={"center": [cx, cy], "q": q, "PA": PA, "n": n, "Re": Re, "Ie": Ie})
+    return live, gal
+
+
+def run_auxpsf_case(ap, key, case):
+    size, k = case["size"], case["psf_size"]
+    psf_target = ap.image.PSF_Image(data=np.ones((k, k)) / k**2, pixelscale=1.0)
+    blank = ap.image.Target_Image(data=np.zeros((size, size)), pixelscale=1.0)
+    live_t, gal_t = build_auxpsf(ap, blank, psf_target, case["truth"], f"truth {key}")
+    truth_img = gal_t().data.detach().cpu().numpy()
+    truth_psf = live_t().data.detach().cpu().numpy()
+    data, weight = synthetic.add_noise(truth_img, case["seed"])
+    target = ap.image.Target_Image(data=data, pixelscale=1.0, variance=1.0 / weight)
+    live, gal = build_auxpsf(ap, target, psf_target, case["init"], f"fit {key}")
+    names = [str(v) for v in gal.parameters.vector_names()]
+    psf0 = live().data.detach().cpu().numpy()
+    model0 = gal().data.detach().cpu().numpy()
+    J_rep = gal.jacobian(as_representation=True).data.detach().cpu().numpy()
+    J_val = gal.jacobian(as_representation=False).data.detach().cpu().numpy()
+    rep0 = gal.parameters.vector_representation().detach().cpu().numpy().copy()
+    val0 = gal.parameters.vector_values().detach().cpu().numpy().copy()
+    res = ap.fit.LM(gal, initial_state=rep0).fit()
+    return dict(
+        names=np.array(names), truth_model=truth_img, truth_psf=truth_psf, data=data, weight=weight,
+        psf0=psf0, model0=model0, jac_rep=J_rep, jac_val=J_val, rep0=rep0, val0=val0,
+        loss_history=np.array(res.loss_history), lambda_history=np.array(res.lambda_history),
+        L_history=np.array(res.L_history), res=np.array(res.res()),
+        final_values=gal.parameters.vector_values().detach().cpu().numpy(), message=np.array(res.message),
+        spec=json.dumps(case),
+    )
+
+
 INIT_CASES = {
     "init_sersic_64": dict(kind="sersic", nx=64, ny=64, scale=1.0, sky=1.0, noise=0.05, seed=11,
                            params={"center": [31.7, 32.4], "q": 0.55, "PA": 0.9, "n": 2.5, "Re": 8.0, "Ie": 0.2}),
@@ -671,6 +720,12 @@ def run_init_case(ap, key, case):
 def main():
     ap = import_reference()
     only = sys.argv[1] if len(sys.argv) > 1 else None
+    if only == "auxpsf":
+        for key, case in AUXPSF_CASES.items():
+            out = run_auxpsf_case(ap, key, case)
+            np.savez_compressed(os.path.join(HERE, f"{key}.npz"), **out)
+            print("auxpsf", key, out["names"], out["loss_history"], str(out["message"]), out["final_values"])
+        return
     for key, case in (INIT_CASES if only != "segmap" else {}).items():
         out = run_init_case(ap, key, case)
         np.savez_compressed(os.path.join(HERE, f"{key}.npz"), **out)

@@ -1,0 +1,114 @@
+"""Fitted parametric PSFs on the GPU against the reference's own outputs
+(``tests/golden/auxpsf_48.npz``): the Moffat PSF model sampled and normalised on the device, a
+Sersic galaxy convolved with it (model and Jacobian, the PSF's n and Rd leading the vector), the
+scene LM fitting PSF and galaxy together, and the same through the drop-in model API."""
+
+import json
+import os
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "auxpsf_48.npz")
+
+
+@pytest.fixture(scope="module")
+def case():
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA GPU")
+    d = np.load(GOLDEN)
+    return d, json.loads(str(d["spec"]))
+
+
+def make_scene(d, spec, mode="direct"):
+    from astrophot_gb300.scene import LivePSF, Scene, SceneSource
+
+    ini = spec["init"]
+    k, size = spec["psf_size"], spec["size"]
+    live = LivePSF(dict(ini["psf"], I0=0.0), (k, k))
+    src = SceneSource("sersic", list(ini["gal"]))
+    return Scene(size, size, [src], None, d["data"], d["weight"], psf_model=live,
+                 options=dict(psf_convolve_mode=mode))
+
+
+def test_live_psf_image_matches_reference(case):
+    from astrophot_gb300.scene import LivePSF
+
+    d, spec = case
+    for key, img in (("init", d["psf0"]), ("truth", d["truth_psf"])):
+        live = LivePSF(dict(spec[key]["psf"], I0=0.0), img.shape)
+        K = live.image()
+        assert np.max(np.abs(K - img)) <= 2e-6 * np.max(img), key
+    # d(normalised image) / d(n, Rd) against central differences of the float64 oracle
+    from oracle.psfmodel import render_psf
+
+    p = dict(spec["init"]["psf"], I0=0.0)
+    live = LivePSF(p, d["psf0"].shape)
+    _, dK = live.render(True)
+    dK = dK.cpu().numpy().reshape(2, *d["psf0"].shape)
+    for j, name in enumerate(("n", "Rd")):
+        h = 1e-5 * p[name]
+        pp, pm = dict(p), dict(p)
+        pp[name] += h
+        pm[name] -= h
+        fd = (render_psf(pp, d["psf0"].shape)[0] - render_psf(pm, d["psf0"].shape)[0]) / (2 * h)
+        assert np.max(np.abs(dK[j] - fd)) <= 2e-4 * np.max(np.abs(fd)), name
+
+
+@pytest.mark.parametrize("mode", ["direct", "fft"])
+def test_scene_with_live_psf_matches_reference(case, mode):
+    d, spec = case
+    sc = make_scene(d, spec, mode)
+    rep0 = d["rep0"]
+    assert np.allclose(sc.representation(), rep0, atol=1e-12)
+    m = sc.forward(rep0).cpu().numpy().reshape(d["model0"].shape)
+    assert np.max(np.abs(m - d["model0"])) <= 1e-5 * np.max(d["model0"])
+    J = sc.jacobian_image(rep0)
+    for k in range(J.shape[-1]):
+        ref = d["jac_rep"][..., k]
+        err = np.max(np.abs(J[..., k] - ref)) / np.max(np.abs(ref))
+        assert err <= 2e-4, (k, str(d["names"][k]), err)
+
+
+def test_scene_lm_with_live_psf_matches_reference(case):
+    from astrophot_gb300.scene import SceneLM
+
+    d, spec = case
+    sc = make_scene(d, spec)
+    lm = SceneLM(sc, initial_state=d["rep0"].copy()).fit()
+    ref_loss = float(np.min(d["loss_history"]))
+    got = float(np.min(lm.loss_history))
+    assert abs(got / ref_loss - 1) <= 1e-4, (got, ref_loss)
+    assert lm.message == str(d["message"])
+    vals = np.concatenate([[sc.live_psf.params["n"], sc.live_psf.params["Rd"]], np.asarray(sc.sources[0].params)])
+    assert np.allclose(vals, d["final_values"], rtol=2e-3, atol=2e-3), (vals, d["final_values"])
+
+
+def test_api_galaxy_with_moffat_psf_model_fits_like_reference(case):
+    """The reference's construction: ``psf=`` a "moffat psf model" on a PSF_Image, ``LM().fit()``."""
+    import astrophot_gb300 as ap
+
+    d, spec = case
+    ini = spec["init"]
+    k = spec["psf_size"]
+    psf_t = ap.image.PSF_Image(data=np.ones((k, k)) / k**2, pixelscale=1.0)
+    live = ap.models.AstroPhot_Model(name="api psf", model_type="moffat psf model", target=psf_t,
+                                     parameters=dict(ini["psf"]))
+    assert np.max(np.abs(live().data.numpy() - d["psf0"])) <= 2e-6 * np.max(d["psf0"])
+    cx, cy, q, PA, n, Re, Ie = ini["gal"]
+    tgt = ap.image.Target_Image(data=d["data"], pixelscale=1.0, variance=1.0 / d["weight"])
+    gal = ap.models.AstroPhot_Model(name="api gal", model_type="sersic galaxy model", target=tgt, psf_mode="full",
+                                    psf=live, parameters={"center": [cx, cy], "q": q, "PA": PA, "n": n, "Re": Re,
+                                                          "Ie": Ie})
+    img = gal().data.numpy()
+    assert np.max(np.abs(img - d["model0"])) <= 1e-5 * np.max(d["model0"])
+    J = gal.jacobian(as_representation=True).data.numpy()
+    assert J.shape == d["jac_rep"].shape
+    assert np.max(np.abs(J - d["jac_rep"])) <= 2e-4 * np.max(np.abs(d["jac_rep"]))
+    res = ap.fit.LM(gal).fit()
+    assert res.message == str(d["message"])
+    assert np.allclose(gal.parameters.vector_values().numpy(), d["final_values"], rtol=2e-3, atol=2e-3)
+    assert abs(live["n"].value.item() - d["final_values"][0]) <= 2e-3 * d["final_values"][0]

@@ -1,0 +1,84 @@
+"""The live-PSF oracle (``oracle/psfmodel.py``) pinned to the reference's own outputs in
+``tests/golden/auxpsf_48.npz``: a Moffat PSF model sampled on a 15 x 15 PSF image, a Sersic
+galaxy convolved with it, the Jacobian over [PSF n, PSF Rd, galaxy parameters] and the LM fit of
+all of them (``set_aux_psf``, models/model_object.py:133-149).  Also the host-side parameter
+order of the drop-in API for the same construction."""
+
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle.lm import LMOracle
+from oracle.psfmodel import LivePSFProblem, render_psf
+from oracle.render import Component, Window
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "auxpsf_48.npz")
+
+
+@pytest.fixture(scope="module")
+def case():
+    d = np.load(GOLDEN)
+    return d, json.loads(str(d["spec"]))
+
+
+def problem(d, spec):
+    ini = spec["init"]
+    cx, cy, q, PA, n, Re, Ie = ini["gal"]
+    gal = Component("sersic", {"center": [cx, cy], "q": q, "PA": PA, "n": n, "Re": Re, "Ie": Ie}, psf_mode="full")
+    size, k = spec["size"], spec["psf_size"]
+    return LivePSFProblem(gal, Window.from_scale(size, size), dict(ini["psf"], I0=0.0), (k, k), d["data"], d["weight"])
+
+
+def test_oracle_psf_image_matches_reference(case):
+    d, spec = case
+    K, _ = render_psf(dict(spec["init"]["psf"], I0=0.0), d["psf0"].shape)
+    assert np.max(np.abs(K - d["psf0"])) <= 1e-12 * np.max(d["psf0"])
+    Kt, _ = render_psf(dict(spec["truth"]["psf"], I0=0.0), d["truth_psf"].shape)
+    assert np.max(np.abs(Kt - d["truth_psf"])) <= 1e-12 * np.max(d["truth_psf"])
+
+
+def test_oracle_live_psf_model_and_jacobian_match_reference(case):
+    d, spec = case
+    pr = problem(d, spec)
+    assert np.allclose(pr.representation(), d["rep0"], rtol=0, atol=1e-12)
+    m = pr.forward(d["rep0"]).reshape(d["model0"].shape)
+    assert np.max(np.abs(m - d["model0"])) <= 1e-12 * np.max(d["model0"])
+    J = pr.jacobian(d["rep0"]).reshape(d["jac_rep"].shape)
+    for k in range(J.shape[-1]):
+        ref = d["jac_rep"][..., k]
+        assert np.max(np.abs(J[..., k] - ref)) <= 1e-10 * np.max(np.abs(ref)), (k, str(d["names"][k]))
+
+
+def test_oracle_lm_with_live_psf_matches_reference(case):
+    d, spec = case
+    pr = problem(d, spec)
+    lm = LMOracle(pr, initial_state=d["rep0"].copy())
+    lm.fit()
+    assert lm.message == str(d["message"])
+    assert np.allclose(lm.loss_history, d["loss_history"], rtol=1e-10, atol=0)
+    assert np.allclose(pr.values(), d["final_values"], rtol=1e-8, atol=1e-10)
+
+
+def test_api_vector_order_puts_the_live_psf_first(case):
+    """Host logic only: a galaxy built with a Moffat PSF model as its ``psf`` links the PSF's
+    parameters ahead of its own, as the reference's vector_names show."""
+    torch = pytest.importorskip("torch")
+    import astrophot_gb300 as ap
+
+    d, spec = case
+    ini = spec["init"]
+    k = spec["psf_size"]
+    psf_t = ap.image.PSF_Image(data=np.ones((k, k)) / k**2, pixelscale=1.0)
+    live = ap.models.AstroPhot_Model(name="order psf", model_type="moffat psf model", target=psf_t,
+                                     parameters=dict(ini["psf"]))
+    cx, cy, q, PA, n, Re, Ie = ini["gal"]
+    tgt = ap.image.Target_Image(data=d["data"], pixelscale=1.0, variance=1.0 / d["weight"])
+    gal = ap.models.AstroPhot_Model(name="order gal", model_type="sersic galaxy model", target=tgt, psf_mode="full",
+                                    psf=live, parameters={"center": [cx, cy], "q": q, "PA": PA, "n": n, "Re": Re,
+                                                          "Ie": Ie})
+    assert [str(x) for x in gal.parameters.vector_names()] == [str(x) for x in d["names"]]
+    assert np.allclose(gal.parameters.vector_values().numpy(), d["val0"])
+    assert np.allclose(gal.parameters.vector_representation().numpy(), d["rep0"], atol=1e-12)
+    assert isinstance(gal.psf, ap.models.Moffat_PSF) and torch.is_tensor(gal["order psf"]["n"].value)
