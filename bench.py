@@ -15,6 +15,11 @@ Workloads (one "step" = every stamp of the workload fitted once, from its initia
       ap_reference_init), batched and one stamp at a time.
   init -- the reference's initial-value heuristics (initialize(), ap_reference_init) on the
       learned workload's stamps: stamps/s, parity and the CPU oracle beside it.
+  livepsf -- fitted PSF models: 64 x 64 stamps of a compact Sersic galaxy convolved with a live
+      Moffat PSF model on a 15 x 15 PSF image (set_aux_psf), PSF n and Rd fitted with the
+      galaxy's 7 parameters by the scene LM, one stamp after another: fits/s, parity and the
+      CPU oracle beside it; plus 200 galaxies on 1024 x 1024 sharing one live 31 x 31 Moffat
+      PSF (1402 parameters) fitted jointly.
   cutouts -- N stamps (default 8192) with sides round(log-uniform(32, 256)) px, each one
       Sersic galaxy + a flat sky of 1.0 (locked), its own Moffat PSF (beta 3.5, FWHM ~
       U(2, 5) px, side = 4 FWHM rounded to odd), noise sigma = sqrt(model + 10), 7 free
@@ -58,8 +63,8 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default="learned", choices=["learned", "cutouts", "crowded", "init"])
-    p.add_argument("--stamps", type=int, default=None, help="65536 (learned, init) / 8192 (cutouts)")
+    p.add_argument("--workload", default="learned", choices=["learned", "cutouts", "crowded", "init", "livepsf"])
+    p.add_argument("--stamps", type=int, default=None, help="65536 (learned, init) / 32 (livepsf) / 8192 (cutouts)")
     p.add_argument("--seed", type=int, default=2024)
     p.add_argument("--cpu-sample", type=int, default=8, help="stamps fitted by the CPU baseline")
     p.add_argument("--rounds-per-sync", type=int, default=8)
@@ -71,7 +76,7 @@ def parse():
     p.add_argument("--crowded-iters", type=int, default=20)
     a = p.parse_args()
     if a.stamps is None:
-        a.stamps = 65536 if a.workload in ("learned", "init") else 8192
+        a.stamps = 65536 if a.workload in ("learned", "init") else (32 if a.workload == "livepsf" else 8192)
     return a
 
 
@@ -285,6 +290,8 @@ def run_gpu(args):
         run_gpu_learned(args)
     elif args.workload == "init":
         run_gpu_init(args)
+    elif args.workload == "livepsf":
+        run_gpu_livepsf(args)
     elif args.workload == "crowded":
         import torch
 
@@ -1059,6 +1066,272 @@ def run_reference_init(args):
     print(json.dumps(line), flush=True)
 
 
+# ----------------------------------------------------------------------------------------
+# fitted PSF models
+# ----------------------------------------------------------------------------------------
+LIVEPSF_METRIC = "LM fits/s of galaxy + live Moffat PSF model (9 parameters, chi2 within 1e-4 of the FP64 oracle)"
+LIVEPSF_SIZE, LIVEPSF_K = 64, 15
+
+
+def livepsf_specs(n, seed):
+    """Truth and initial values of ``n`` stamps: (psf {n, Rd}, galaxy [cx, cy, q, PA, n, Re, Ie])."""
+    rng = np.random.default_rng(seed + 104729)
+    out = []
+    c = LIVEPSF_SIZE / 2
+    for i in range(n):
+        tp = dict(n=float(rng.uniform(2.0, 4.0)), Rd=float(rng.uniform(1.5, 2.8)))
+        tg = [c + rng.uniform(-1, 1), c + rng.uniform(-1, 1), rng.uniform(0.5, 0.85), rng.uniform(0.2, 2.9),
+              rng.uniform(1.0, 3.0), rng.uniform(1.2, 2.5), rng.uniform(2.0, 2.8)]
+        ip = dict(n=tp["n"] * 0.85, Rd=tp["Rd"] * 1.15)
+        ig = [tg[0] + 0.3, tg[1] - 0.3, min(tg[2] * 1.08, 0.95), tg[3] + 0.1, tg[4] * 1.15, tg[5] * 1.15, tg[6] - 0.1]
+        out.append(dict(truth=dict(psf=tp, gal=[float(v) for v in tg]), init=dict(psf=ip, gal=[float(v) for v in ig]),
+                        seed=seed + 31 * i))
+    return out
+
+
+def _oracle_livepsf(job):
+    """(final chi2/ndf, final vector, seconds) of the float64 oracle LM on one stamp."""
+    from oracle.lm import LMOracle
+    from oracle.psfmodel import LivePSFProblem
+    from oracle.render import Component, Window
+
+    data, weight, init = job
+    cx, cy, q, PA, n, Re, Ie = init["gal"]
+    gal = Component("sersic", {"center": [cx, cy], "q": q, "PA": PA, "n": n, "Re": Re, "Ie": Ie}, psf_mode="full")
+    t = time.perf_counter()
+    pr = LivePSFProblem(gal, Window.from_scale(LIVEPSF_SIZE, LIVEPSF_SIZE), dict(init["psf"], I0=0.0),
+                        (LIVEPSF_K, LIVEPSF_K), data, weight)
+    lm = LMOracle(pr)
+    lm.fit()
+    return float(np.min(lm.loss_history)), pr.values(), time.perf_counter() - t
+
+
+def _oracle_livepsf_truth(spec):
+    """Noisy data of one stamp rendered by the float64 restatement (the reference arm's input)."""
+    from oracle.psfmodel import LivePSFProblem
+    from oracle.render import Component, Window
+
+    from astrophot_gb300 import synthetic
+
+    cx, cy, q, PA, n, Re, Ie = spec["truth"]["gal"]
+    gal = Component("sersic", {"center": [cx, cy], "q": q, "PA": PA, "n": n, "Re": Re, "Ie": Ie}, psf_mode="full")
+    z = np.zeros((LIVEPSF_SIZE, LIVEPSF_SIZE))
+    pr = LivePSFProblem(gal, Window.from_scale(LIVEPSF_SIZE, LIVEPSF_SIZE), dict(spec["truth"]["psf"], I0=0.0),
+                        (LIVEPSF_K, LIVEPSF_K), z, z + 1)
+    img = pr.forward(pr.representation()).reshape(LIVEPSF_SIZE, LIVEPSF_SIZE)
+    return synthetic.add_noise(img, spec["seed"])
+
+
+def crowded_live_psf_block(args, dev):
+    """200 Sersic galaxies on 1024 x 1024 convolved with one live 31 x 31 Moffat PSF model whose n
+    and Rd are fitted with them (1402 parameters): Jacobian build (with the two image-wide PSF
+    columns) and the scene LM."""
+    import torch
+
+    from astrophot_gb300 import scene as SC
+    from astrophot_gb300 import synthetic
+
+    size, n_src = args.crowded_size, args.crowded_sources
+    truth, init, windows, _ = synthetic.crowded_field(args.seed, size, n_src)
+    sky = 5.0
+    tp, ip = dict(n=3.0, Rd=2.5, I0=0.0), dict(n=2.6, Rd=2.8, I0=0.0)
+    zeros = np.zeros((size, size))
+    sc_t = SC.Scene(size, size, [SC.SceneSource("sersic", list(t), w) for t, w in zip(truth, windows)], None, zeros,
+                    zeros + 1, sky=sky, device=dev, psf_model=SC.LivePSF(tp, (31, 31), device=dev))
+    model = sc_t.forward(sc_t.representation()).cpu().numpy().astype(np.float64).reshape(size, size)
+    data, weight = synthetic.add_noise(model, args.seed)
+    del sc_t
+    sc = SC.Scene(size, size, [SC.SceneSource("sersic", list(t), w) for t, w in zip(init, windows)], None, data,
+                  weight, sky=sky, device=dev, options={"psf_convolve_mode": "fft"},
+                  psf_model=SC.LivePSF(ip, (31, 31), device=dev))
+    rep = sc.representation()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(2):
+        sc.forward(rep)
+        sc.jacobian(rep)
+        sc.hess()
+    torch.cuda.synchronize()
+    reps = 5
+    e0.record()
+    for _ in range(reps):
+        sc.forward(rep)
+    e1.record()
+    torch.cuda.synchronize()
+    fwd_ms = e0.elapsed_time(e1) / reps
+    e0.record()
+    for _ in range(reps):
+        sc.jacobian(rep)
+        sc.hess()
+    e1.record()
+    torch.cuda.synchronize()
+    jac_ms = e0.elapsed_time(e1) / reps
+    t0 = time.perf_counter()
+    lm = SC.SceneLM(sc, initial_state=rep, max_iter=args.crowded_iters).fit()
+    torch.cuda.synchronize()
+    lm_s = time.perf_counter() - t0
+    return {
+        "workload": f"{n_src} Sersic galaxies on a {size}x{size} image sharing one live 31x31 Moffat PSF model "
+        f"(truth n 3.0, Rd 2.5; start 2.6, 2.8), sky 5.0, explicit windows; {sc.P} parameters fitted jointly",
+        "parameters": sc.P,
+        "render_ms": fwd_ms,
+        "jacobian_and_hessian_ms": jac_ms,
+        "lm_iterations": lm.iterations,
+        "lm_seconds": lm_s,
+        "lm_ms_per_iteration": lm_s * 1e3 / max(lm.iterations, 1),
+        "chi2_ndf_start": lm.loss_history[0],
+        "chi2_ndf_end": min(lm.loss_history),
+        "psf_fitted": {"n": sc.live_psf.params["n"], "Rd": sc.live_psf.params["Rd"], "truth_n": 3.0, "truth_Rd": 2.5},
+        "lm_message": lm.message,
+    }
+
+
+def run_gpu_livepsf(args):
+    """--workload livepsf: fits/s of galaxy + live PSF stamps, each fitted by the scene LM
+    (device-resident data: value; host data copied in and the fitted vector read back: e2e)."""
+    import torch
+
+    from astrophot_gb300 import scene as SC
+    from astrophot_gb300 import synthetic
+
+    rank, world, local = rank_info()
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", torch.cuda.current_device())
+    S = args.stamps
+    specs = livepsf_specs(S, args.seed + 7919 * rank)
+    z = np.zeros((LIVEPSF_SIZE, LIVEPSF_SIZE))
+    scenes, inits, hosts = [], [], []
+    for sp in specs:
+        sc_t = SC.Scene(LIVEPSF_SIZE, LIVEPSF_SIZE, [SC.SceneSource("sersic", sp["truth"]["gal"])], None, z, z + 1,
+                        device=dev, psf_model=SC.LivePSF(dict(sp["truth"]["psf"], I0=0.0), (LIVEPSF_K, LIVEPSF_K),
+                                                         device=dev))
+        img = sc_t.forward(sc_t.representation()).cpu().numpy().astype(np.float64).reshape(LIVEPSF_SIZE, LIVEPSF_SIZE)
+        data, weight = synthetic.add_noise(img, sp["seed"])
+        sc = SC.Scene(LIVEPSF_SIZE, LIVEPSF_SIZE, [SC.SceneSource("sersic", sp["init"]["gal"])], None, data, weight,
+                      device=dev, psf_model=SC.LivePSF(dict(sp["init"]["psf"], I0=0.0), (LIVEPSF_K, LIVEPSF_K),
+                                                       device=dev))
+        scenes.append(sc)
+        inits.append(sc.representation())
+        hosts.append(torch.from_numpy(data.astype(np.float32).reshape(-1)).pin_memory())
+
+    def step(e2e=False):
+        out = []
+        for sc, x0, h in zip(scenes, inits, hosts):
+            if e2e:
+                sc.data.copy_(h, non_blocking=True)
+            lm = SC.SceneLM(sc, initial_state=x0.copy()).fit()
+            out.append((min(lm.loss_history), lm.res(), lm.message))
+        return out
+
+    for _ in range(max(args.warmup, 0)):
+        res = step()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record()
+        for _ in range(args.steps):
+            res = step()
+        e1.record()
+        torch.cuda.synchronize()
+    dev_ms = e0.elapsed_time(e1) / args.steps
+    e0.record()
+    for _ in range(args.steps):
+        step(e2e=True)
+    e1.record()
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    converged = sum(1 for r in res if r[2].startswith("success"))
+    dev_ms, e2e_ms, converged, total = aggregate_ranks(dev_ms, e2e_ms, converged, S, dev)
+    if rank != 0:
+        return
+    line = {
+        "metric": LIVEPSF_METRIC,
+        "value": converged / (dev_ms * 1e-3),
+        "unit": "fits/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": dev_ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 render / f64 LM",
+        "data": "synthetic",
+        "config": {"workload": f"{S} stamps of {LIVEPSF_SIZE}x{LIVEPSF_SIZE} per GPU, compact Sersic (Re 1.2-2.5 px) "
+                   f"convolved with a live Moffat PSF model on {LIVEPSF_K}x{LIVEPSF_K} (truth n 2-4, Rd 1.5-2.8), "
+                   "noise sqrt(model + 10); PSF n, Rd + 7 galaxy parameters fitted by the scene LM, one stamp after "
+                   "another", "stamps_per_gpu": S,
+                   "l2": "small stamps: resident in L2 (a host-driven LM per stamp, latency-bound)"},
+        "fits": {"total": total, "converged": converged,
+                 "messages": {m: sum(1 for r in res if r[2] == m) for m in sorted({r[2] for r in res})}},
+        "clocks": clk.summary(),
+        "e2e": {"value": converged / (e2e_ms * 1e-3), "unit": "fits/s",
+                "h2d_bytes_per_step": int(S * LIVEPSF_SIZE * LIVEPSF_SIZE * 4), "d2h_bytes_per_step": int(S * 9 * 8)},
+        "roofline": None,
+        "roofline_note": "each LM iteration launches ~40 small kernels on a 64x64 stamp and reads the damped step "
+                         "back to the host: bound by launch latency and host round trips, not by a unit",
+    }
+    if not args.no_crowded:
+        line["crowded_live_psf"] = crowded_live_psf_block(args, dev)
+    if not args.no_cpu:
+        k = min(args.cpu_sample, S)
+        idx = list(np.linspace(0, S - 1, k).round().astype(int))
+        jobs = [(scenes[i].data.cpu().numpy().astype(np.float64).reshape(LIVEPSF_SIZE, LIVEPSF_SIZE),
+                 scenes[i].weight.cpu().numpy().astype(np.float64).reshape(LIVEPSF_SIZE, LIVEPSF_SIZE),
+                 specs[i]["init"]) for i in idx]
+        out = [_oracle_livepsf(j) for j in jobs]
+        secs = sum(o[2] for o in out)
+        rel = [abs(res[i][0] / o[0] - 1) for i, o in zip(idx, out)]
+        line["cpu_baseline"] = {"value": k / secs, "unit": "fits/s", "cores": 1, "kind": "port",
+                                "sample": f"{k} stamps of this workload, float64 numpy restatement of the reference "
+                                          "(live PSF sampling + LM), one core"}
+        line["parity"] = {"stamps": k, "max_rel_chi2_vs_oracle": float(max(rel)),
+                          "within_1e-4": int(sum(r <= 1e-4 for r in rel))}
+    print(json.dumps(line), flush=True)
+
+
+def run_reference_livepsf(args):
+    """--impl reference --workload livepsf: the float64 restatement (live PSF sampling + LM) on
+    all host cores, on the same stamps (rendered and noised by the restatement)."""
+    rank, world, _ = rank_info()
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    specs = livepsf_specs(args.stamps, args.seed)
+    k = min(args.stamps, 2 * cores)
+    specs = [specs[i] for i in np.linspace(0, args.stamps - 1, k).round().astype(int)]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(processes=min(cores, len(specs))) as pool:
+        dw = pool.map(_oracle_livepsf_truth, specs)
+        jobs = [(d, w, sp["init"]) for (d, w), sp in zip(dw, specs)]
+        if args.warmup > 0:
+            pool.map(_oracle_livepsf, jobs[: min(len(jobs), cores)])
+        times = []
+        for _ in range(args.steps):
+            t = time.perf_counter()
+            pool.map(_oracle_livepsf, jobs)
+            times.append(time.perf_counter() - t)
+    dt = statistics.median(times)
+    value = len(jobs) / dt
+    line = {
+        "impl": "reference", "metric": LIVEPSF_METRIC, "value": value, "unit": "fits/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{args.stamps} stamps of {LIVEPSF_SIZE}x{LIVEPSF_SIZE}, Sersic + live Moffat PSF model "
+                               f"on {LIVEPSF_K}x{LIVEPSF_K}, 9 parameters fitted",
+                   "sample": f"{len(jobs)} stamps evenly spaced over the workload, {min(cores, len(jobs))} processes"},
+        "cpu_baseline": {"value": value, "unit": "fits/s", "cores": min(cores, len(jobs)), "kind": "port",
+                         "sample": f"{len(jobs)} stamps (float64 numpy restatement of live PSF sampling + LM)"},
+        "e2e": {"value": value, "unit": "fits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -1066,6 +1339,8 @@ def main():
             run_reference_learned(args)
         elif args.workload == "init":
             run_reference_init(args)
+        elif args.workload == "livepsf":
+            run_reference_livepsf(args)
         elif args.workload == "crowded":
             print(json.dumps({"impl": "reference", "workload": "crowded",
                               "unavailable": "the crowded-field block is a GPU-only secondary measurement"}))
