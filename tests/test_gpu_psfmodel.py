@@ -112,3 +112,48 @@ def test_api_galaxy_with_moffat_psf_model_fits_like_reference(case):
     assert res.message == str(d["message"])
     assert np.allclose(gal.parameters.vector_values().numpy(), d["final_values"], rtol=2e-3, atol=2e-3)
     assert abs(live["n"].value.item() - d["final_values"][0]) <= 2e-3 * d["final_values"][0]
+
+
+def test_live_psf_columns_add_over_sources_and_feed_the_normal_equations(case):
+    """Two overlapping galaxies sharing one live PSF: the PSF columns of the pair are the sums of
+    each galaxy's own (the model is a sum), and the device J^T W J, J^T v and J h over the joint
+    vector (PSF entries first) equal the dense products of the assembled Jacobian."""
+    from astrophot_gb300.scene import LivePSF, Scene, SceneSource
+
+    d, spec = case
+    rng = np.random.default_rng(3)
+    size = 64
+    gals = [[24.3, 27.6, 0.7, 1.0, 1.5, 2.5, 2.2], [37.1, 33.4, 0.5, 2.2, 2.5, 3.5, 1.8]]
+    wins = [((8, 44), (10, 46)), ((20, 60), (14, 54))]
+    data = rng.normal(size=(size, size)) + 1.0
+    weight = rng.uniform(0.5, 1.5, size=(size, size))
+    psf = dict(n=2.7, Rd=2.1, I0=0.0)
+
+    def scene(idx):
+        return Scene(size, size, [SceneSource("sersic", gals[i], wins[i]) for i in idx], None, data, weight,
+                     psf_model=LivePSF(psf, (15, 15)))
+
+    both, one, two = scene([0, 1]), scene([0]), scene([1])
+    Jb = both.jacobian_image(both.representation())
+    J1 = one.jacobian_image(one.representation())
+    J2 = two.jacobian_image(two.representation())
+    for c in range(2):
+        ref = J1[..., c] + J2[..., c]
+        assert np.max(np.abs(Jb[..., c] - ref)) <= 1e-5 * np.max(np.abs(ref)), c
+    assert np.allclose(Jb[..., 2:9], J1[..., 2:], rtol=0, atol=1e-6 * np.abs(J1).max())
+    assert np.allclose(Jb[..., 9:], J2[..., 2:], rtol=0, atol=1e-6 * np.abs(J2).max())
+    # normal equations on the device against the dense Jacobian
+    both.jacobian(both.representation())
+    H = both.hess().cpu().numpy()
+    Jf = Jb.reshape(-1, both.P).astype(np.float64)
+    w = weight.reshape(-1)
+    Href = Jf.T @ (Jf * w[:, None])
+    assert np.max(np.abs(H - Href)) <= 1e-4 * np.max(np.abs(Href))
+    v = torch.tensor(rng.normal(size=size * size), dtype=torch.float32, device="cuda")
+    g = both.jt(v).cpu().numpy()
+    gref = Jf.T @ v.cpu().numpy().astype(np.float64)
+    assert np.max(np.abs(g - gref)) <= 1e-4 * np.max(np.abs(gref))
+    h = torch.tensor(rng.normal(size=both.P), dtype=torch.float64, device="cuda")
+    jh = both.jvp(h).cpu().numpy()
+    jhref = Jf @ h.cpu().numpy()
+    assert np.max(np.abs(jh - jhref)) <= 1e-4 * np.max(np.abs(jhref))
