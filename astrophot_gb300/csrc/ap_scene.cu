@@ -167,14 +167,22 @@ __global__ void __launch_bounds__(256) k_scene_hess(const ap_scene_source* __res
 __global__ void k_scene_chi2(const float* __restrict__ model, const float* __restrict__ data,
                              const float* __restrict__ weight, const uint8_t* __restrict__ mask, int64_t n,
                              double* __restrict__ out) {
+  // one block, partial sums added in a fixed order: the same chi^2 bits on every run
   double acc = 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
     if (mask && mask[i]) continue;
     const double r = (double)data[i] - (double)model[i];
     acc += (weight ? (double)weight[i] : 1.0) * r * r;
   }
   acc = warp_sum(acc);
-  if ((threadIdx.x & 31) == 0) atomicAdd(out, acc);
+  __shared__ double sh[32];
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w];
+    *out = t;
+  }
 }
 
 // r = W (Y - M) on unmasked pixels, 0 elsewhere (LM._r, astrophot/fit/lm.py:381-385)
@@ -441,7 +449,7 @@ int ap_scene_chi2(const float* model, const float* data, const float* weight, co
   cudaStream_t st = (cudaStream_t)stream;
   int rc = record_cuda(cudaMemsetAsync(out, 0, sizeof(double), st));
   if (rc) return rc;
-  k_scene_chi2<<<egrid(n), 256, 0, st>>>(model, data, weight, mask, n, out);
+  k_scene_chi2<<<1, 1024, 0, st>>>(model, data, weight, mask, n, out);
   return record_cuda(cudaGetLastError());
 }
 

@@ -38,7 +38,7 @@ import torch
 from . import _native as N
 from .transforms import SLOT_LIMITS, drep_dvalue, to_rep, to_value
 
-__all__ = ("SceneSource", "Scene", "SceneLM", "SceneRenderFunction", "render")
+__all__ = ("SceneSource", "Scene", "SceneLM", "LivePSF", "fit_scenes", "SceneRenderFunction", "render")
 
 TILE = 32
 _SLOTS_OF = {"sersic": (0, 1, 2, 3, 4, 5, 6), "exponential": (0, 1, 2, 3, 5, 6)}
@@ -732,6 +732,39 @@ class SceneLM:
         if not ok.any():
             return self.x.copy()
         return np.array(self.lambda_history)[ok][np.argmin(hist[ok])]
+
+
+def fit_scenes(scenes: Sequence[Scene], initial_states=None, workers: int = 8, **lm_kwargs) -> List[SceneLM]:
+    """Independent scene LMs (``LM(model).fit()`` of separate models) run concurrently: each of
+    ``workers`` host threads drives its share of the scenes on its own CUDA stream, so that one
+    fit's host round trips (damped-solve status, chi^2) overlap the kernels of the others.
+    Every scene must own its batches (no scene shared between two entries).  Returns the
+    :class:`SceneLM` of every scene, in order; each fit is the same as run alone."""
+    import concurrent.futures as cf
+
+    n = len(scenes)
+    if len({id(sc) for sc in scenes}) != n:
+        raise ValueError("fit_scenes needs distinct scenes")
+    inits = [None] * n if initial_states is None else list(initial_states)
+    nw = max(1, min(int(workers), n))
+    streams = [torch.cuda.Stream(device=scenes[0].device) for _ in range(nw)] if n else []
+    out: List[Optional[SceneLM]] = [None] * n
+    caller = torch.cuda.current_stream()
+    for st in streams:
+        st.wait_stream(caller)
+
+    def work(w):
+        with torch.cuda.stream(streams[w]):
+            for i in range(w, n, nw):
+                x0 = None if inits[i] is None else np.array(inits[i], dtype=np.float64)
+                out[i] = SceneLM(scenes[i], initial_state=x0, **lm_kwargs).fit()
+        streams[w].synchronize()
+
+    with cf.ThreadPoolExecutor(max_workers=nw) as ex:
+        list(ex.map(work, range(nw)))
+    for st in streams:
+        caller.wait_stream(st)
+    return out
 
 
 class SceneIterLM:

@@ -157,3 +157,23 @@ def test_live_psf_columns_add_over_sources_and_feed_the_normal_equations(case):
     jh = both.jvp(h).cpu().numpy()
     jhref = Jf @ h.cpu().numpy()
     assert np.max(np.abs(jh - jhref)) <= 1e-4 * np.max(np.abs(jhref))
+
+
+def test_concurrent_scene_fits_equal_sequential_ones(case):
+    """fit_scenes: independent live-PSF fits on worker streams end exactly where the same fits
+    run one after another end."""
+    from astrophot_gb300.scene import SceneLM, fit_scenes
+
+    d, spec = case
+    scenes = [make_scene(d, spec) for _ in range(4)]
+    x0 = d["rep0"].copy()
+    for k, sc in enumerate(scenes):  # four different starting points
+        x0k = x0.copy()
+        x0k[2] += 0.1 * k
+        scenes[k]._x0 = x0k
+    seq = [SceneLM(sc, initial_state=sc._x0.copy()).fit() for sc in scenes]
+    con = fit_scenes(scenes, [sc._x0 for sc in scenes], workers=4)
+    for a, b in zip(seq, con):
+        assert a.message == b.message
+        assert np.array_equal(np.asarray(a.loss_history), np.asarray(b.loss_history))
+        assert np.array_equal(a.res(), b.res())
