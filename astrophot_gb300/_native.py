@@ -36,7 +36,7 @@ _ERR_NAMES = {
     AP_ERR_NOT_BOUND: "batch not bound to a workspace",
 }
 
-PROFILE = {"sersic": 0, "exponential": 1, "moffat": 2}
+PROFILE = {"sersic": 0, "exponential": 1, "moffat": 2, "gaussian": 3}
 SAMPLING = {"midpoint": 0, "simpsons": 1, "quad": 2, "trapezoid": 3}
 INTEGRATE = {"none": 0, "threshold": 1}
 PSF_NONE, PSF_FULL, PSF_FULL_NOSHIFT = 0, 1, 2

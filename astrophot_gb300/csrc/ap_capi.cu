@@ -123,8 +123,7 @@ namespace {
 int validate_options(const ap_options* o) {
   if (!o) return AP_ERR_ARG;
   if (o->fft_min_kernel < 0) return AP_ERR_ARG;
-  if (o->profile != AP_PROFILE_SERSIC && o->profile != AP_PROFILE_EXPONENTIAL && o->profile != AP_PROFILE_MOFFAT)
-    return AP_ERR_UNSUPPORTED;
+  if (o->profile < AP_PROFILE_SERSIC || o->profile > AP_PROFILE_GAUSSIAN) return AP_ERR_UNSUPPORTED;
   if (o->sampling_mode < AP_SAMPLING_MIDPOINT || o->sampling_mode > AP_SAMPLING_TRAPEZOID)
     return AP_ERR_UNSUPPORTED;
   if (o->sampling_mode == AP_SAMPLING_QUAD &&
@@ -139,7 +138,7 @@ int validate_options(const ap_options* o) {
     if (o->integrate_quad_level < 1 || o->integrate_quad_level > kMaxQuad) return AP_ERR_UNSUPPORTED;
   }
   if (o->free_mask & ~0xff) return AP_ERR_ARG;
-  if (o->profile == AP_PROFILE_EXPONENTIAL && (o->free_mask & (1 << PN))) return AP_ERR_ARG;
+  if (!profile_has_n(o->profile) && (o->free_mask & (1 << PN))) return AP_ERR_ARG;
   if (!o->has_sky && (o->free_mask & (1 << PF))) return AP_ERR_ARG;
   if (!(o->softening >= 0.0) || !(o->sampling_tolerance >= 0.0)) return AP_ERR_ARG;
   return AP_OK;
@@ -701,7 +700,7 @@ int ap_reference_init(ap_batch* b, const float* data, const uint8_t* mask, int32
                       int32_t* status, void* workspace, int64_t workspace_bytes, ap_stream_t stream) {
   if (!b || !data || !params || !status || (known_mask & ~0xff)) return AP_ERR_ARG;
   if (!b->bound) return AP_ERR_NOT_BOUND;
-  if (b->opt.profile == AP_PROFILE_MOFFAT) return AP_ERR_UNSUPPORTED;
+  if (b->opt.profile != AP_PROFILE_SERSIC && b->opt.profile != AP_PROFILE_EXPONENTIAL) return AP_ERR_UNSUPPORTED;
   if (int rc = refinit_geometry_ok(b)) return rc;
   const RefInitPlan P = plan_reference_init(b->stamps.data(), b->n);
   if (P.scratch_bytes > 0 && (!workspace || workspace_bytes < P.scratch_bytes)) return AP_ERR_WORKSPACE;
@@ -833,7 +832,7 @@ int ap_lm_fit(ap_batch* b, const float* data, const float* weight, const uint8_t
     return AP_ERR_ARG;
   if (!b->bound) return AP_ERR_NOT_BOUND;
   // the device LM's representation maps carry the Sersic index limits (0.36, 8)
-  if (b->opt.profile == AP_PROFILE_MOFFAT) return AP_ERR_UNSUPPORTED;
+  if (b->opt.profile != AP_PROFILE_SERSIC && b->opt.profile != AP_PROFILE_EXPONENTIAL) return AP_ERR_UNSUPPORTED;
   int rc = lm_validate(lm);
   if (rc) return rc;
   if (b->opt.psf_mode != AP_PSF_NONE && !psf) return AP_ERR_ARG;

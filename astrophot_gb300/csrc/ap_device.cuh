@@ -244,6 +244,11 @@ __host__ __device__ inline int64_t work_plane(const BatchArgs& b, int slot, int 
   return ((int64_t)slot * kNumPlanes + plane) * b.work_pixels;
 }
 
+// profiles with an index n (slot PN) and its Jacobian plane
+__host__ __device__ inline bool profile_has_n(int kind) {
+  return kind == AP_PROFILE_SERSIC || kind == AP_PROFILE_MOFFAT;
+}
+
 // ---------------------------------------------------------------------------
 // sample evaluation
 // ---------------------------------------------------------------------------
@@ -262,6 +267,8 @@ struct Sample {
 // from rounding 1 + u^2 and 3e-7 from u's own error, n times that in the exponent n ln(1 + u^2),
 // plus 2.4e-7 relative from its rounding and the exp's 1.4e-7 per unit: the same formula with
 // invn = 1 gives 4e-7 + (|arg| + n) 1e-6, above that bound.
+// Gaussian (arg = u^2 / 2, e.bn = e.invn = 1): u^2 carries ~5 ulp (6e-7 relative of arg) and
+// the exp adds 2.4e-7 plus 1.4e-7 per unit: below 4e-7 + (|arg| + 1) 1e-6.
 __device__ __forceinline__ float sample_rel_err(const EvalF& e, float arg) {
   return 4e-7f + (fabsf(arg) + e.bn) * (5e-7f + 5e-7f * e.invn);
 }
@@ -282,6 +289,9 @@ __device__ __forceinline__ Sample eval_profile(const EvalF& e, int kind, float X
     w = fmaf(u, u, 1.f);
     lu2 = __log2f(w);
     arg = e.bn * (lu2 * 0.6931471805599453f);
+  } else if (kind == AP_PROFILE_GAUSSIAN) {
+    // I0 / sqrt(2 pi sigma^2) exp(-u^2 / 2), u = R / sigma: the prefactor is in amp
+    arg = 0.5f * u * u;
   } else {
     if (kind == AP_PROFILE_SERSIC) {
       lu2 = __log2f(u);
@@ -305,6 +315,10 @@ __device__ __forceinline__ Sample eval_profile(const EvalF& e, int kind, float X
       dIdR = -I * nu * e.invRe;
       out.g[GRE] = I * nu * u * e.invRe;
       out.g[GN] = -I * (lu2 * 0.6931471805599453f);
+    } else if (kind == AP_PROFILE_GAUSSIAN) {
+      dIdR = -I * u * e.invRe;
+      out.g[GRE] = I * (u * u - 1.f) * e.invRe;  // the prefactor's 1/sigma included
+      out.g[GN] = 0.f;
     } else {
       dIdR = -I * e.bn * e.invRe;
       out.g[GRE] = I * e.bn * u * e.invRe;
@@ -331,6 +345,10 @@ __device__ __forceinline__ double eval_profile64(const EvalDev& e, int kind, dou
   if (kind == AP_PROFILE_MOFFAT) {
     const double u = R * e.invRe64;
     return amp / pow(1.0 + u * u, e.bn64);
+  }
+  if (kind == AP_PROFILE_GAUSSIAN) {
+    const double u = R * e.invRe64;
+    return amp * exp(-0.5 * (u * u));
   }
   return amp * exp(-e.bn64 * ((R * e.invRe64) - 1.0));
 }

@@ -49,7 +49,7 @@ __device__ FftUse fft_use(const BatchArgs& b, int ops) {
   if (u.jac) {
     for (int q = 0; q < NGRAD; ++q) {
       if (u.shift && !(ops & OP_VJP_COORD) && (q == GX || q == GY)) continue;
-      if (b.kind == AP_PROFILE_EXPONENTIAL && q == GN) continue;
+      if (!profile_has_n(b.kind) && q == GN) continue;
       u.part[u.npart++] = q;
     }
   }

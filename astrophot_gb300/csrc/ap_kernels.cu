@@ -120,8 +120,14 @@ __global__ void k_eval_setup(BatchArgs b, const double* params, int64_t stamp_st
   e.Re = (float)v[PRE];
   e.invRe64 = 1.0 / v[PRE];
   e.invRe = (float)e.invRe64;
-  const double n = (b.kind != AP_PROFILE_EXPONENTIAL) ? v[PN] : 1.0;
-  if (b.kind == AP_PROFILE_MOFFAT) {  // I0 / (1 + (R/Rd)^2)^n: the power in bn, Rd in Re
+  const double n = profile_has_n(b.kind) ? v[PN] : 1.0;
+  if (b.kind == AP_PROFILE_GAUSSIAN) {  // (FP32 error bound of eval_profile: bn = invn = 1)
+    e.invn64 = 1.0;
+    e.invn = 1.f;
+    e.bn64 = 1.0;
+    e.bn = 1.f;
+    e.dbn = 0.f;
+  } else if (b.kind == AP_PROFILE_MOFFAT) {  // I0 / (1 + (R/Rd)^2)^n: the power in bn, Rd in Re
     e.invn64 = 1.0 / n;
     e.invn = 1.f;  // (FP32 error bound of eval_profile)
     e.bn64 = n;
@@ -135,6 +141,8 @@ __global__ void k_eval_setup(BatchArgs b, const double* params, int64_t stamp_st
     e.dbn = (float)sersic_db64(n);
   }
   e.amp64 = st.pixel_area * pow(10.0, v[PIE]);
+  // gaussian_torch (utils/parametric_profiles.py:39-48): I0 / sqrt(2 pi sigma^2), sigma in slot Re
+  if (b.kind == AP_PROFILE_GAUSSIAN) e.amp64 = e.amp64 / sqrt(2 * kPi * v[PRE] * v[PRE]);
   e.amp = (float)e.amp64;
   e.sky = b.has_sky ? (float)(st.pixel_area * pow(10.0, v[PF])) : 0.f;
   e.soft2_64 = b.softening64 * b.softening64;
@@ -174,7 +182,7 @@ __global__ void k_build_lists(BatchArgs b) {
   const int ops = b.evals[t].ops;
   if (b.psf_mode != AP_PSF_NONE && st.fft_nx == 0) {  // (FFT-convolved stamps: not k_conv's work)
     const bool jac = (ops & OP_JAC) != 0, shiftmode = (b.psf_mode == AP_PSF_FULL);
-    const int nconv = jac ? ((shiftmode ? 3 : 1) + (b.kind != AP_PROFILE_EXPONENTIAL ? 4 : 3) +
+    const int nconv = jac ? ((shiftmode ? 3 : 1) + (profile_has_n(b.kind) ? 4 : 3) +
                              ((shiftmode && !(ops & OP_VJP_COORD)) ? 0 : 2))
                           : 1;
     atomicAdd(b.work_ctr, (unsigned long long)st.nx * st.ny * 2ull *
@@ -1083,7 +1091,7 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
 #pragma unroll
         for (int q = 0; q < NGRAD; ++q) {
           if (shiftmode && !(ops & OP_VJP_COORD) && (q == GX || q == GY)) continue;
-          if (b.kind == AP_PROFILE_EXPONENTIAL && q == GN) continue;
+          if (!profile_has_n(b.kind) && q == GN) continue;
           cv[3 + q][o] = pre[(int64_t)(3 + q) * npix + i];
         }
       }
@@ -1104,7 +1112,7 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
     const int row0 = y0 + st.by - cy, col0 = x0 + st.bx - cx;
     for (int pl = 0; pl < nplanes; ++pl) {
       if (pl > 0 && shiftmode && !(ops & OP_VJP_COORD) && (pl - 1 == GX || pl - 1 == GY)) continue;
-      if (pl > 0 && b.kind == AP_PROFILE_EXPONENTIAL && pl - 1 == GN) continue;
+      if (pl > 0 && !profile_has_n(b.kind) && pl - 1 == GN) continue;
       __syncthreads();
       const float* src = b.work + work_plane(b, slot, pl) + st.work_off;
       // rows over warps, columns over lanes: coalesced reads; stored column-major (pitch TP,

@@ -38,6 +38,7 @@ __all__ = (
     "Group_Model",
     "PSF_Model",
     "Moffat_PSF",
+    "Gaussian_PSF",
 )
 
 # full parameter-vector slots of the C ABI
@@ -360,46 +361,38 @@ class PSF_Model(Component_Model):
             raise InvalidTarget("PSF_Model target must be a PSF_Image instance.")
         self._target = tar
 
-
-class Moffat_PSF(PSF_Model):
-    """I(R) = 10^I0 / (1 + (R/Rd)^2)^n on the PSF image (``moffat_model.py:71-120``), I0 locked
-    at 0 by default.  As a galaxy's ``psf`` it is a live PSF: re-sampled from its parameters at
-    every evaluation and fitted with the galaxy (``astrophot_gb300.scene.LivePSF``)."""
-
-    model_type = f"moffat {PSF_Model.model_type}"
-    parameter_specs = {
-        "n": {"units": "none", "limits": (0.1, 10), "uncertainty": 0.05},
-        "Rd": {"units": "arcsec", "limits": (0, None)},
-        "I0": {"units": "log10(flux/arcsec^2)", "value": 0.0, "locked": True},
-    }
-    _parameter_order = PSF_Model._parameter_order + ("n", "Rd", "I0")
-    usable = True
+    _live_kind = None  # LivePSF kind of a concrete PSF model
 
     def initialize(self, target=None, parameters=None, **kwargs):
-        missing = [p for p in ("n", "Rd", "I0") if self.parameters[p].value is None]
+        missing = [p for p in self._parameter_order[1:] if self.parameters[p].value is None]
         if missing:
             raise SpecificationConflict(f"{self.name}: parameters without values: {missing}")
 
     def live_psf(self, device=None):
         """A :class:`~astrophot_gb300.scene.LivePSF` at the current values; its free parameters
-        are the unlocked ones of n, Rd, I0."""
+        are the unlocked ones of the profile's parameters."""
         from .scene import LivePSF
 
+        if self._live_kind is None:
+            raise NotImplementedError(f"{self.model_type} has no CUDA sampler")
         if self.normalize_psf is not True:
             raise NotImplementedError("an unnormalised PSF model is not supported by the CUDA path")
         if self.sampling_mode not in ("midpoint", "simpsons", "trapezoid") and not self.sampling_mode.startswith("quad"):
             raise SpecificationConflict(f"unknown sampling mode: {self.sampling_mode}")
         p = self.parameters
-        vals = {k: float(p[k].value.item()) for k in ("n", "Rd", "I0")}
-        free = tuple(k for k in ("n", "Rd", "I0") if not p[k].locked)
+        names = self._parameter_order[1:]
+        vals = {k: float(p[k].value.item()) for k in names}
+        free = tuple(k for k in names if not p[k].locked)
         knobs = {k: getattr(self, k) for k in ("sampling_mode", "sampling_tolerance", "integrate_mode",
                                                "integrate_max_depth", "integrate_gridding", "integrate_quad_level",
                                                "softening")}
         return LivePSF(vals, tuple(self.target.data.shape), self.target.pixel_length, free, knobs,
-                       config.ap_device if device is None else device)
+                       config.ap_device if device is None else device, kind=self._live_kind)
 
     def sample(self, image=None, window=None, parameters=None):
         """``PSF_Model.sample``: the normalised PSF image, sampled on the GPU."""
+        if isinstance(parameters, (torch.Tensor, np.ndarray, list, tuple)):
+            self.parameters.vector_set_values(parameters)
         img = self.live_psf().image()
         return PSF_Image(torch.as_tensor(img, dtype=config.ap_dtype), pixelscale=self.target.pixelscale)
 
@@ -415,6 +408,36 @@ class Moffat_PSF(PSF_Model):
         if as_representation:
             J = J * live.drep(live.representation())[None, None, :]
         return torch.as_tensor(J, dtype=config.ap_dtype)
+
+
+class Moffat_PSF(PSF_Model):
+    """I(R) = 10^I0 / (1 + (R/Rd)^2)^n on the PSF image (``moffat_model.py:71-120``), I0 locked
+    at 0 by default.  As a galaxy's ``psf`` it is a live PSF: re-sampled from its parameters at
+    every evaluation and fitted with the galaxy (``astrophot_gb300.scene.LivePSF``)."""
+
+    model_type = f"moffat {PSF_Model.model_type}"
+    parameter_specs = {
+        "n": {"units": "none", "limits": (0.1, 10), "uncertainty": 0.05},
+        "Rd": {"units": "arcsec", "limits": (0, None)},
+        "I0": {"units": "log10(flux/arcsec^2)", "value": 0.0, "locked": True},
+    }
+    _parameter_order = PSF_Model._parameter_order + ("n", "Rd", "I0")
+    _live_kind = "moffat"
+    usable = True
+
+
+class Gaussian_PSF(PSF_Model):
+    """I(R) = 10^flux exp(-R^2 / (2 sigma^2)) / sqrt(2 pi sigma^2) on the PSF image
+    (``gaussian_model.py:255-290``), flux locked at 0 by default; live like ``Moffat_PSF``."""
+
+    model_type = f"gaussian {PSF_Model.model_type}"
+    parameter_specs = {
+        "sigma": {"units": "arcsec", "limits": (0, None)},
+        "flux": {"units": "log10(flux)", "value": 0.0, "locked": True},
+    }
+    _parameter_order = PSF_Model._parameter_order + ("sigma", "flux")
+    _live_kind = "gaussian"
+    usable = True
 
 
 class Sersic_Galaxy(Galaxy_Model):
@@ -805,8 +828,8 @@ def _scene_spec(owner, components):
     psf = gals[0].psf if knobs["psf_mode"] == "full" else None
     if psf is not None and any(g.psf is not psf for g in gals[1:]):
         raise NotImplementedError("galaxies of one group must share one PSF on the CUDA path")
-    if isinstance(psf, PSF_Model) and not isinstance(psf, Moffat_PSF):
-        raise NotImplementedError("the CUDA path's live PSF models are Moffat PSFs")
+    if isinstance(psf, PSF_Model) and psf._live_kind is None:
+        raise NotImplementedError("the CUDA path's live PSF models are Moffat and Gaussian PSFs")
     center_owner = {}
     sources = []
     for gi, g in enumerate(gals):

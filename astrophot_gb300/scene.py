@@ -43,32 +43,42 @@ __all__ = ("SceneSource", "Scene", "SceneLM", "LivePSF", "fit_scenes", "SceneRen
 TILE = 32
 _SLOTS_OF = {"sersic": (0, 1, 2, 3, 4, 5, 6), "exponential": (0, 1, 2, 3, 5, 6)}
 
-# Moffat_PSF parameters: limits (models/moffat_model.py:88-92) and their slots in the render
-PSF_MODEL_LIMITS = {"n": ((0.1, 10.0), False), "Rd": ((0.0, None), False), "I0": ((None, None), False)}
-_PSF_SLOT = {"n": 4, "Rd": 5, "I0": 6}
+# PSF model parameters per kind: limits (Moffat_PSF models/moffat_model.py:88-92, Gaussian_PSF
+# models/gaussian_model.py:272-275) and their slots in the render
+PSF_MODEL_LIMITS = {
+    "moffat": {"n": ((0.1, 10.0), False), "Rd": ((0.0, None), False), "I0": ((None, None), False)},
+    "gaussian": {"sigma": ((0.0, None), False), "flux": ((None, None), False)},
+}
+_PSF_SLOT = {"moffat": {"n": 4, "Rd": 5, "I0": 6}, "gaussian": {"sigma": 5, "flux": 6}}
+_PSF_DEFAULT_FREE = {"moffat": ("n", "Rd"), "gaussian": ("sigma",)}
 # PSF_Model class knobs (models/psf_model_object.py:50-80)
 PSF_MODEL_KNOBS = dict(sampling_mode="simpsons", sampling_tolerance=1e-3, integrate_mode="threshold",
                        integrate_max_depth=3, integrate_gridding=5, integrate_quad_level=3, softening=1e-3)
 
 
 class LivePSF:
-    """A Moffat PSF model (I0 / (1 + (R/Rd)^2)^n, centred on its PSF image) sampled on the device
-    as ``PSF_Model.sample`` does (models/psf_model_object.py:180-264: sampling and threshold
+    """A PSF model centred on its PSF image -- ``kind`` "moffat" (I0 / (1 + (R/Rd)^2)^n) or
+    "gaussian" (10^flux / sqrt(2 pi sigma^2) exp(-R^2 / (2 sigma^2))) -- sampled on the device as
+    ``PSF_Model.sample`` does (models/psf_model_object.py:180-264: sampling and threshold
     integration, then ``normalize_psf``), with the derivatives of the normalised image with
     respect to its ``free`` parameters (``ap_psf_normalize``)."""
 
-    def __init__(self, params: dict, shape, scale: float = 1.0, free=("n", "Rd"), knobs: Optional[dict] = None,
-                 device="cuda"):
-        self.params = {k: float(params.get(k, 0.0)) for k in ("n", "Rd", "I0")}
+    def __init__(self, params: dict, shape, scale: float = 1.0, free=None, knobs: Optional[dict] = None,
+                 device="cuda", kind: str = "moffat"):
+        if kind not in _PSF_SLOT:
+            raise ValueError(f"unsupported PSF model kind {kind}")
+        self.kind = kind
+        self.limits = PSF_MODEL_LIMITS[kind]
+        self.params = {k: float(params.get(k, 0.0)) for k in _PSF_SLOT[kind]}
         self.ky, self.kx = int(shape[0]), int(shape[1])
         self.scale = float(scale)
-        self.free = tuple(free)
-        if any(f not in _PSF_SLOT for f in self.free):
-            raise ValueError(f"unknown Moffat PSF parameter in {self.free}")
+        self.free = tuple(_PSF_DEFAULT_FREE[kind] if free is None else free)
+        if any(f not in _PSF_SLOT[kind] for f in self.free):
+            raise ValueError(f"unknown {kind} PSF parameter in {self.free}")
         kn = dict(PSF_MODEL_KNOBS)
         kn.update(knobs or {})
-        mask = sum(1 << _PSF_SLOT[f] for f in self.free)
-        o = N.make_options(profile="moffat", psf_mode="none", free_mask=mask, has_sky=False, **kn)
+        mask = sum(1 << _PSF_SLOT[kind][f] for f in self.free)
+        o = N.make_options(profile=kind, psf_mode="none", free_mask=mask, has_sky=False, **kn)
         origin = (-self.kx * self.scale / 2, -self.ky * self.scale / 2)  # the image centred on (0, 0)
         self.device = torch.device(device)
         self.batch = N.StampBatch([(self.kx, self.ky)], None, N.scale_geometry(1, self.scale, origin), o, self.device)
@@ -78,19 +88,21 @@ class LivePSF:
         self.lib = N.lib()
 
     def _row(self):
-        p = self.params  # q = 1 and PA = pi/2 make the inclined transform the identity
-        return torch.tensor([[0.0, 0.0, 1.0, math.pi / 2, p["n"], p["Rd"], p["I0"], 0.0]], dtype=torch.float64)
+        row = [0.0, 0.0, 1.0, math.pi / 2, 1.0, 1.0, 0.0, 0.0]  # q = 1, PA = pi/2: no inclination
+        for k, v in self.params.items():
+            row[_PSF_SLOT[self.kind][k]] = v
+        return torch.tensor([row], dtype=torch.float64)
 
     def representation(self):
-        return np.array([to_rep(*PSF_MODEL_LIMITS[f], self.params[f]) for f in self.free])
+        return np.array([to_rep(*self.limits[f], self.params[f]) for f in self.free])
 
     def set_representation(self, rep):
         for f, r in zip(self.free, rep):
-            self.params[f] = float(to_value(*PSF_MODEL_LIMITS[f], r))
+            self.params[f] = float(to_value(*self.limits[f], r))
 
     def drep(self, rep):
         """d value / d representation of the free parameters."""
-        return np.array([float(drep_dvalue(*PSF_MODEL_LIMITS[f], r)) for f, r in zip(self.free, rep)])
+        return np.array([float(drep_dvalue(*self.limits[f], r)) for f, r in zip(self.free, rep)])
 
     def render(self, grad: bool = False):
         """(K [ky * kx], dK [n_free][ky * kx] or None): the normalised PSF image and its

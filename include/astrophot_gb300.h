@@ -54,6 +54,10 @@ typedef struct CUstream_st* ap_stream_t; /* same handle as cudaStream_t */
  * (0.1, 10).  Render, Jacobian and adjoint only (ap_lm_fit and ap_reference_init return
  * AP_ERR_UNSUPPORTED): a fitted PSF's parameters are fitted by the scene LM. */
 #define AP_PROFILE_MOFFAT 2
+/* Gaussian (Gaussian_PSF, astrophot/models/gaussian_model.py:255-290): 10^flux / sqrt(2 pi
+ * sigma^2) exp(-R^2 / (2 sigma^2)) with sigma in slot Re and flux in slot Ie; no n.  Render,
+ * Jacobian and adjoint only, like the Moffat profile. */
+#define AP_PROFILE_GAUSSIAN 3
 /* ap_options.sampling_mode */
 #define AP_SAMPLING_MIDPOINT 0
 #define AP_SAMPLING_SIMPSONS 1

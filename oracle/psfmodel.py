@@ -1,7 +1,8 @@
 """Fitted parametric PSFs restated in float64 numpy.  TEST INFRASTRUCTURE ONLY (the checker
 of the CUDA path's live PSF models; see ``oracle/__init__``).
 
-* ``render_psf``: a Moffat PSF model sampled on its PSF image and normalised to unit sum
+* ``render_psf``: a Moffat (models/moffat_model.py:71-120) or Gaussian
+  (models/gaussian_model.py:255-290) PSF model sampled on its PSF image and normalised to unit sum
   (``PSF_Model.sample``, astrophot/models/psf_model_object.py:180-264, with the class knobs of
   psf_model_object.py:50-80: Simpson sampling, tolerance 1e-3, threshold integration), and the
   derivatives of the normalised image with respect to the PSF parameters.
@@ -11,7 +12,8 @@ of the CUDA path's live PSF models; see ``oracle/__init__``).
   node is added to the galaxy's parameters before the galaxy's own, so the PSF parameters lead
   the vector.  It has the interface ``LMOracle`` expects.
 
-Pinned by ``tests/golden/auxpsf_48.npz``, recorded from the reference itself.
+Pinned by ``tests/golden/auxpsf_48.npz`` (Moffat) and ``auxpsf_gauss_48.npz`` (Gaussian),
+recorded from the reference itself.
 """
 
 from __future__ import annotations
@@ -26,7 +28,8 @@ from .render import PSF, Component, Window, check_limits, drep_dvalue, rep_to_va
 # PSF_Model class attributes (astrophot/models/psf_model_object.py:50-80)
 PSF_KNOBS = dict(sampling_mode="simpsons", sampling_tolerance=1e-3, integrate_mode="threshold",
                  integrate_max_depth=3, integrate_gridding=5, integrate_quad_level=3, softening=1e-3)
-MOFFAT_PSF_ORDER = ("n", "Rd", "I0")
+PSF_ORDER = {"moffat": ("n", "Rd", "I0"), "gaussian": ("sigma", "flux")}
+DEFAULT_FREE = {"moffat": ("n", "Rd"), "gaussian": ("sigma",)}
 
 
 def psf_window(kx: int, ky: int, scale: float = 1.0) -> Window:
@@ -35,11 +38,12 @@ def psf_window(kx: int, ky: int, scale: float = 1.0) -> Window:
 
 
 def render_psf(params: Dict[str, float], shape, scale: float = 1.0, grad: bool = False,
-               free: Sequence[str] = ("n", "Rd")):
-    """(K / sum K, {name: d(K / sum K) / d name}) of a Moffat PSF model on a ``shape`` = (ky, kx)
-    PSF image."""
+               free: Optional[Sequence[str]] = None, kind: str = "moffat"):
+    """(K / sum K, {name: d(K / sum K) / d name}) of a Moffat or Gaussian PSF model on a
+    ``shape`` = (ky, kx) PSF image."""
     ky, kx = shape
-    comp = Component("moffat", {"center": np.zeros(2), **{k: params[k] for k in MOFFAT_PSF_ORDER}}, **PSF_KNOBS)
+    free = DEFAULT_FREE[kind] if free is None else free
+    comp = Component(kind, {"center": np.zeros(2), **{k: params[k] for k in PSF_ORDER[kind]}}, **PSF_KNOBS)
     r = sample_component(comp, psf_window(kx, ky, scale), None, grad)
     S = np.sum(r.model)
     Kn = r.model / S
@@ -53,24 +57,26 @@ def render_psf(params: Dict[str, float], shape, scale: float = 1.0, grad: bool =
 
 
 class LivePSFProblem:
-    """One galaxy (``psf_mode`` "full") with a live Moffat PSF on ``window``, against data ``Y``
-    with weights ``W``."""
+    """One galaxy (``psf_mode`` "full") with a live Moffat or Gaussian PSF (``psf_kind``) on
+    ``window``, against data ``Y`` with weights ``W``."""
 
     def __init__(self, galaxy: Component, window: Window, psf_params: Dict[str, float], psf_shape,
                  Y: np.ndarray, W: Optional[np.ndarray] = None, psf_scale: float = 1.0,
-                 psf_free: Sequence[str] = ("n", "Rd"), mask: Optional[np.ndarray] = None):
+                 psf_free: Optional[Sequence[str]] = None, mask: Optional[np.ndarray] = None,
+                 psf_kind: str = "moffat"):
         self.galaxy = copy.deepcopy(galaxy)
         self.window = window
         self.psf_params = {k: float(v) for k, v in psf_params.items()}
         self.psf_shape = tuple(psf_shape)
         self.psf_scale = float(psf_scale)
-        self.psf_free = tuple(psf_free)
+        self.psf_kind = psf_kind
+        self.psf_free = tuple(DEFAULT_FREE[psf_kind] if psf_free is None else psf_free)
         self.Y, self.W, self.mask = Y, W, mask
         self.slots = [("psf", name, 0) for name in self.psf_free] + [("gal", name, k)
                                                                     for name, k in self.galaxy.free_slots()]
 
     def _kind(self, who):
-        return "moffat" if who == "psf" else None
+        return self.psf_kind if who == "psf" else None
 
     def _get(self, who, name, k):
         if who == "psf":
@@ -97,7 +103,7 @@ class LivePSFProblem:
                 self.galaxy.params[name] = np.asarray(v, dtype=float)
 
     def psf_image(self, grad=False):
-        return render_psf(self.psf_params, self.psf_shape, self.psf_scale, grad, self.psf_free)
+        return render_psf(self.psf_params, self.psf_shape, self.psf_scale, grad, self.psf_free, self.psf_kind)
 
     def forward(self, rep):
         self.set_representation(rep)

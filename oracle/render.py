@@ -43,6 +43,9 @@ PARAM_SPECS = {
     # Moffat (models/moffat_model.py:88-92); its n takes KIND_SPECS' limits
     "Rd": ((0.0, None), False),
     "I0": ((None, None), False),
+    # Gaussian_PSF (models/gaussian_model.py:272-275)
+    "sigma": ((0.0, None), False),
+    "flux": ((None, None), False),
 }
 
 # per-kind overrides of PARAM_SPECS: Moffat_PSF's n, models/moffat_model.py:89
@@ -60,6 +63,8 @@ PARAM_ORDER = {
     "flat_sky": ("F",),
     # psf_model_object.py:45, moffat_model.py:93
     "moffat": ("center", "n", "Rd", "I0"),
+    # gaussian_model.py:276
+    "gaussian": ("center", "sigma", "flux"),
 }
 
 
@@ -318,7 +323,7 @@ class Component:
 # brightness evaluation with analytic partials
 # ----------------------------------------------------------------------------
 
-GRAD_KEYS = ("X", "Y", "q", "PA", "n", "Re", "Ie", "F", "Rd", "I0")
+GRAD_KEYS = ("X", "Y", "q", "PA", "n", "Re", "Ie", "F", "Rd", "I0", "sigma", "flux")
 
 
 def eval_brightness(comp: Component, X, Y, pixel_area, grad: bool):
@@ -352,6 +357,17 @@ def eval_brightness(comp: Component, X, Y, pixel_area, grad: bool):
         dI_dR = -I * n * 2 * R / (Rd * Rd * w)
         return I, {"n": -I * np.log(w), "Rd": I * n * 2 * R * R / (Rd**3 * w), "I0": I * np.log(10.0),
                    "X": dI_dR * X / R, "Y": dI_dR * Y / R}
+    if comp.kind == "gaussian":
+        # Gaussian_PSF: radial_evaluate_model -> gaussian_torch (utils/parametric_profiles.py:39-48)
+        # with 10^flux * pixel_area (models/_shared_methods.py:403-408)
+        sig = p["sigma"]
+        R = np.sqrt(X**2 + Y**2 + comp.softening**2)
+        I = (pixel_area * 10 ** p["flux"]) / np.sqrt(2 * np.pi * sig**2) * np.exp(-0.5 * (R / sig) ** 2)
+        if not grad:
+            return I, None
+        dI_dR = -I * R / sig**2
+        return I, {"sigma": I * (R * R / sig**3 - 1 / sig), "flux": I * np.log(10.0), "X": dI_dR * X / R,
+                   "Y": dI_dR * Y / R}
 
     q = p["q"]
     PA = p["PA"]

@@ -611,11 +611,15 @@ AUXPSF_CASES = {
     "auxpsf_48": dict(size=48, psf_size=15, seed=21,
                       truth=dict(psf=dict(n=2.5, Rd=2.2), gal=[24.3, 23.6, 0.7, 1.0, 1.5, 1.5, 2.5]),
                       init=dict(psf=dict(n=2.0, Rd=2.6), gal=[24.0, 24.0, 0.75, 0.9, 1.8, 1.8, 2.4])),
+    # the same galaxy with a live Gaussian PSF model (sigma fitted, flux locked)
+    "auxpsf_gauss_48": dict(size=48, psf_size=15, seed=22, psf_kind="gaussian",
+                            truth=dict(psf=dict(sigma=1.6), gal=[24.3, 23.6, 0.7, 1.0, 1.5, 1.5, 2.5]),
+                            init=dict(psf=dict(sigma=2.0), gal=[24.0, 24.0, 0.75, 0.9, 1.8, 1.8, 2.4])),
 }
 
 
-def build_auxpsf(ap, target, psf_target, vals, tag):
-    live = ap.models.AstroPhot_Model(name=f"psf {tag}", model_type="moffat psf model", target=psf_target,
+def build_auxpsf(ap, target, psf_target, vals, tag, kind="moffat"):
+    live = ap.models.AstroPhot_Model(name=f"psf {tag}", model_type=f"{kind} psf model", target=psf_target,
                                      parameters=dict(vals["psf"]))
     cx, cy, q, PA, n, Re, Ie = vals["gal"]
     gal = ap.models.AstroPhot_Model(name=f"gal {tag}", model_type="sersic galaxy model", target=target,
@@ -628,12 +632,13 @@ def run_auxpsf_case(ap, key, case):
     size, k = case["size"], case["psf_size"]
     psf_target = ap.image.PSF_Image(data=np.ones((k, k)) / k**2, pixelscale=1.0)
     blank = ap.image.Target_Image(data=np.zeros((size, size)), pixelscale=1.0)
-    live_t, gal_t = build_auxpsf(ap, blank, psf_target, case["truth"], f"truth {key}")
+    kind = case.get("psf_kind", "moffat")
+    live_t, gal_t = build_auxpsf(ap, blank, psf_target, case["truth"], f"truth {key}", kind)
     truth_img = gal_t().data.detach().cpu().numpy()
     truth_psf = live_t().data.detach().cpu().numpy()
     data, weight = synthetic.add_noise(truth_img, case["seed"])
     target = ap.image.Target_Image(data=data, pixelscale=1.0, variance=1.0 / weight)
-    live, gal = build_auxpsf(ap, target, psf_target, case["init"], f"fit {key}")
+    live, gal = build_auxpsf(ap, target, psf_target, case["init"], f"fit {key}", kind)
     names = [str(v) for v in gal.parameters.vector_names()]
     psf0 = live().data.detach().cpu().numpy()
     model0 = gal().data.detach().cpu().numpy()

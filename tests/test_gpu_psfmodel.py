@@ -1,7 +1,8 @@
 """Fitted parametric PSFs on the GPU against the reference's own outputs
-(``tests/golden/auxpsf_48.npz``): the Moffat PSF model sampled and normalised on the device, a
-Sersic galaxy convolved with it (model and Jacobian, the PSF's n and Rd leading the vector), the
-scene LM fitting PSF and galaxy together, and the same through the drop-in model API."""
+(``tests/golden/auxpsf_48.npz``, Moffat; ``auxpsf_gauss_48.npz``, Gaussian): the PSF model sampled
+and normalised on the device, a Sersic galaxy convolved with it (model and Jacobian, the PSF's
+parameters leading the vector), the scene LM fitting PSF and galaxy together, and the same
+through the drop-in model API."""
 
 import json
 import os
@@ -12,15 +13,24 @@ import pytest
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
-GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "auxpsf_48.npz")
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+LOCKED = {"moffat": {"I0": 0.0}, "gaussian": {"flux": 0.0}}
 
 
-@pytest.fixture(scope="module")
-def case():
+@pytest.fixture(scope="module", params=["auxpsf_48", "auxpsf_gauss_48"])
+def case(request):
     if not torch.cuda.is_available():
         pytest.skip("needs a CUDA GPU")
-    d = np.load(GOLDEN)
+    d = np.load(os.path.join(GOLDEN, f"{request.param}.npz"))
     return d, json.loads(str(d["spec"]))
+
+
+def kind_of(spec):
+    return spec.get("psf_kind", "moffat")
+
+
+def psf_params(spec, which):
+    return dict(spec[which]["psf"], **LOCKED[kind_of(spec)])
 
 
 def make_scene(d, spec, mode="direct"):
@@ -28,7 +38,7 @@ def make_scene(d, spec, mode="direct"):
 
     ini = spec["init"]
     k, size = spec["psf_size"], spec["size"]
-    live = LivePSF(dict(ini["psf"], I0=0.0), (k, k))
+    live = LivePSF(psf_params(spec, "init"), (k, k), kind=kind_of(spec))
     src = SceneSource("sersic", list(ini["gal"]))
     return Scene(size, size, [src], None, d["data"], d["weight"], psf_model=live,
                  options=dict(psf_convolve_mode=mode))
@@ -38,23 +48,24 @@ def test_live_psf_image_matches_reference(case):
     from astrophot_gb300.scene import LivePSF
 
     d, spec = case
+    kind = kind_of(spec)
     for key, img in (("init", d["psf0"]), ("truth", d["truth_psf"])):
-        live = LivePSF(dict(spec[key]["psf"], I0=0.0), img.shape)
+        live = LivePSF(psf_params(spec, key), img.shape, kind=kind)
         K = live.image()
         assert np.max(np.abs(K - img)) <= 2e-6 * np.max(img), key
-    # d(normalised image) / d(n, Rd) against central differences of the float64 oracle
+    # d(normalised image) / d(free parameters) against central differences of the float64 oracle
     from oracle.psfmodel import render_psf
 
-    p = dict(spec["init"]["psf"], I0=0.0)
-    live = LivePSF(p, d["psf0"].shape)
+    p = psf_params(spec, "init")
+    live = LivePSF(p, d["psf0"].shape, kind=kind)
     _, dK = live.render(True)
-    dK = dK.cpu().numpy().reshape(2, *d["psf0"].shape)
-    for j, name in enumerate(("n", "Rd")):
+    dK = dK.cpu().numpy().reshape(len(live.free), *d["psf0"].shape)
+    for j, name in enumerate(live.free):
         h = 1e-5 * p[name]
         pp, pm = dict(p), dict(p)
         pp[name] += h
         pm[name] -= h
-        fd = (render_psf(pp, d["psf0"].shape)[0] - render_psf(pm, d["psf0"].shape)[0]) / (2 * h)
+        fd = (render_psf(pp, d["psf0"].shape, kind=kind)[0] - render_psf(pm, d["psf0"].shape, kind=kind)[0]) / (2 * h)
         assert np.max(np.abs(dK[j] - fd)) <= 2e-4 * np.max(np.abs(fd)), name
 
 
@@ -83,19 +94,20 @@ def test_scene_lm_with_live_psf_matches_reference(case):
     got = float(np.min(lm.loss_history))
     assert abs(got / ref_loss - 1) <= 1e-4, (got, ref_loss)
     assert lm.message == str(d["message"])
-    vals = np.concatenate([[sc.live_psf.params["n"], sc.live_psf.params["Rd"]], np.asarray(sc.sources[0].params)])
+    vals = np.concatenate([[sc.live_psf.params[f] for f in sc.live_psf.free], np.asarray(sc.sources[0].params)])
     assert np.allclose(vals, d["final_values"], rtol=2e-3, atol=2e-3), (vals, d["final_values"])
 
 
-def test_api_galaxy_with_moffat_psf_model_fits_like_reference(case):
-    """The reference's construction: ``psf=`` a "moffat psf model" on a PSF_Image, ``LM().fit()``."""
+def test_api_galaxy_with_psf_model_fits_like_reference(case):
+    """The reference's construction: ``psf=`` a "moffat psf model" / "gaussian psf model" on a
+    PSF_Image, ``LM().fit()``."""
     import astrophot_gb300 as ap
 
     d, spec = case
     ini = spec["init"]
     k = spec["psf_size"]
     psf_t = ap.image.PSF_Image(data=np.ones((k, k)) / k**2, pixelscale=1.0)
-    live = ap.models.AstroPhot_Model(name="api psf", model_type="moffat psf model", target=psf_t,
+    live = ap.models.AstroPhot_Model(name="api psf", model_type=f"{kind_of(spec)} psf model", target=psf_t,
                                      parameters=dict(ini["psf"]))
     assert np.max(np.abs(live().data.numpy() - d["psf0"])) <= 2e-6 * np.max(d["psf0"])
     cx, cy, q, PA, n, Re, Ie = ini["gal"]
@@ -111,7 +123,8 @@ def test_api_galaxy_with_moffat_psf_model_fits_like_reference(case):
     res = ap.fit.LM(gal).fit()
     assert res.message == str(d["message"])
     assert np.allclose(gal.parameters.vector_values().numpy(), d["final_values"], rtol=2e-3, atol=2e-3)
-    assert abs(live["n"].value.item() - d["final_values"][0]) <= 2e-3 * d["final_values"][0]
+    first = "n" if kind_of(spec) == "moffat" else "sigma"
+    assert abs(live[first].value.item() - d["final_values"][0]) <= 2e-3 * d["final_values"][0]
 
 
 def test_live_psf_columns_add_over_sources_and_feed_the_normal_equations(case):
@@ -127,21 +140,23 @@ def test_live_psf_columns_add_over_sources_and_feed_the_normal_equations(case):
     wins = [((8, 44), (10, 46)), ((20, 60), (14, 54))]
     data = rng.normal(size=(size, size)) + 1.0
     weight = rng.uniform(0.5, 1.5, size=(size, size))
-    psf = dict(n=2.7, Rd=2.1, I0=0.0)
+    kind = kind_of(spec)
+    psf = dict(n=2.7, Rd=2.1, I0=0.0) if kind == "moffat" else dict(sigma=1.8, flux=0.0)
 
     def scene(idx):
         return Scene(size, size, [SceneSource("sersic", gals[i], wins[i]) for i in idx], None, data, weight,
-                     psf_model=LivePSF(psf, (15, 15)))
+                     psf_model=LivePSF(psf, (15, 15), kind=kind))
 
     both, one, two = scene([0, 1]), scene([0]), scene([1])
     Jb = both.jacobian_image(both.representation())
     J1 = one.jacobian_image(one.representation())
     J2 = two.jacobian_image(two.representation())
-    for c in range(2):
+    m = both.n_psf
+    for c in range(m):
         ref = J1[..., c] + J2[..., c]
         assert np.max(np.abs(Jb[..., c] - ref)) <= 1e-5 * np.max(np.abs(ref)), c
-    assert np.allclose(Jb[..., 2:9], J1[..., 2:], rtol=0, atol=1e-6 * np.abs(J1).max())
-    assert np.allclose(Jb[..., 9:], J2[..., 2:], rtol=0, atol=1e-6 * np.abs(J2).max())
+    assert np.allclose(Jb[..., m : m + 7], J1[..., m:], rtol=0, atol=1e-6 * np.abs(J1).max())
+    assert np.allclose(Jb[..., m + 7 :], J2[..., m:], rtol=0, atol=1e-6 * np.abs(J2).max())
     # normal equations on the device against the dense Jacobian
     both.jacobian(both.representation())
     H = both.hess().cpu().numpy()

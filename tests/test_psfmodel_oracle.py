@@ -1,5 +1,6 @@
 """The live-PSF oracle (``oracle/psfmodel.py``) pinned to the reference's own outputs in
-``tests/golden/auxpsf_48.npz``: a Moffat PSF model sampled on a 15 x 15 PSF image, a Sersic
+``tests/golden/auxpsf_48.npz`` and ``auxpsf_gauss_48.npz``: a Moffat or Gaussian PSF model
+sampled on a 15 x 15 PSF image, a Sersic
 galaxy convolved with it, the Jacobian over [PSF n, PSF Rd, galaxy parameters] and the LM fit of
 all of them (``set_aux_psf``, models/model_object.py:133-149).  Also the host-side parameter
 order of the drop-in API for the same construction."""
@@ -14,13 +15,23 @@ from oracle.lm import LMOracle
 from oracle.psfmodel import LivePSFProblem, render_psf
 from oracle.render import Component, Window
 
-GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "auxpsf_48.npz")
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+CASES = ["auxpsf_48", "auxpsf_gauss_48"]
+LOCKED = {"moffat": {"I0": 0.0}, "gaussian": {"flux": 0.0}}
 
 
-@pytest.fixture(scope="module")
-def case():
-    d = np.load(GOLDEN)
+@pytest.fixture(scope="module", params=CASES)
+def case(request):
+    d = np.load(os.path.join(GOLDEN, f"{request.param}.npz"))
     return d, json.loads(str(d["spec"]))
+
+
+def kind_of(spec):
+    return spec.get("psf_kind", "moffat")
+
+
+def psf_params(spec, which):
+    return dict(spec[which]["psf"], **LOCKED[kind_of(spec)])
 
 
 def problem(d, spec):
@@ -28,14 +39,15 @@ def problem(d, spec):
     cx, cy, q, PA, n, Re, Ie = ini["gal"]
     gal = Component("sersic", {"center": [cx, cy], "q": q, "PA": PA, "n": n, "Re": Re, "Ie": Ie}, psf_mode="full")
     size, k = spec["size"], spec["psf_size"]
-    return LivePSFProblem(gal, Window.from_scale(size, size), dict(ini["psf"], I0=0.0), (k, k), d["data"], d["weight"])
+    return LivePSFProblem(gal, Window.from_scale(size, size), psf_params(spec, "init"), (k, k), d["data"],
+                          d["weight"], psf_kind=kind_of(spec))
 
 
 def test_oracle_psf_image_matches_reference(case):
     d, spec = case
-    K, _ = render_psf(dict(spec["init"]["psf"], I0=0.0), d["psf0"].shape)
+    K, _ = render_psf(psf_params(spec, "init"), d["psf0"].shape, kind=kind_of(spec))
     assert np.max(np.abs(K - d["psf0"])) <= 1e-12 * np.max(d["psf0"])
-    Kt, _ = render_psf(dict(spec["truth"]["psf"], I0=0.0), d["truth_psf"].shape)
+    Kt, _ = render_psf(psf_params(spec, "truth"), d["truth_psf"].shape, kind=kind_of(spec))
     assert np.max(np.abs(Kt - d["truth_psf"])) <= 1e-12 * np.max(d["truth_psf"])
 
 
@@ -71,7 +83,7 @@ def test_api_vector_order_puts_the_live_psf_first(case):
     ini = spec["init"]
     k = spec["psf_size"]
     psf_t = ap.image.PSF_Image(data=np.ones((k, k)) / k**2, pixelscale=1.0)
-    live = ap.models.AstroPhot_Model(name="order psf", model_type="moffat psf model", target=psf_t,
+    live = ap.models.AstroPhot_Model(name="order psf", model_type=f"{kind_of(spec)} psf model", target=psf_t,
                                      parameters=dict(ini["psf"]))
     cx, cy, q, PA, n, Re, Ie = ini["gal"]
     tgt = ap.image.Target_Image(data=d["data"], pixelscale=1.0, variance=1.0 / d["weight"])
@@ -81,4 +93,5 @@ def test_api_vector_order_puts_the_live_psf_first(case):
     assert [str(x) for x in gal.parameters.vector_names()] == [str(x) for x in d["names"]]
     assert np.allclose(gal.parameters.vector_values().numpy(), d["val0"])
     assert np.allclose(gal.parameters.vector_representation().numpy(), d["rep0"], atol=1e-12)
-    assert isinstance(gal.psf, ap.models.Moffat_PSF) and torch.is_tensor(gal["order psf"]["n"].value)
+    first = "n" if kind_of(spec) == "moffat" else "sigma"
+    assert isinstance(gal.psf, ap.models.PSF_Model) and torch.is_tensor(gal["order psf"][first].value)
