@@ -496,11 +496,23 @@ class Scene:
         ``ap_render_vjp`` of every source's model render (PSF-convolved derivative tiles are
         recomputed and reduced on the fly, no Jacobian is stored).  ``reference_center`` gives
         the centre entries the reference's reverse-mode autograd gives under PSF shift."""
-        if self.n_psf:
-            raise NotImplementedError("the adjoint of a scene with a live PSF model is not implemented")
-        V = self.values_matrix(rep)
         g_img = grad_image.to(self.device, torch.float32).reshape(-1).contiguous()
         out = np.zeros(self.P)
+        if self.n_psf:
+            # a live PSF's entries: the upstream gradient against each image-wide PSF column
+            # (the render's derivative along d psf / d theta); the sources below see the current PSF
+            dK = self._refresh_psf(rep, True)
+            scale = self.live_psf.drep(np.asarray(rep, dtype=np.float64)[: self.n_psf]) if as_representation else \
+                np.ones(self.n_psf)
+            V = self.values_matrix(rep)
+            col = torch.empty(self.nx * self.ny, dtype=torch.float32, device=self.device)
+            for j in range(self.n_psf):
+                D = dK[j] * float(scale[j])
+                self._render_sources(V, self.fwd_d, lambda b, p, k, o: b.render_psf_derivative(
+                    p, k, D.repeat(k.numel() // D.numel()), out=o))
+                self._combine(self.fwd_d, 0.0, col)
+                out[j] = float(torch.dot(col.to(torch.float64), g_img.to(torch.float64)).item())
+        V = self.values_matrix(rep)
         for part in self._fwd_parts:
             b, m, mem = part["batch"], part["m"], part["members"]
             slots = [sl for sl in range(8) if b.options.free_mask & (1 << sl)]

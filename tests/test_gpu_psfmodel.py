@@ -192,3 +192,34 @@ def test_concurrent_scene_fits_equal_sequential_ones(case):
         assert a.message == b.message
         assert np.array_equal(np.asarray(a.loss_history), np.asarray(b.loss_history))
         assert np.array_equal(a.res(), b.res())
+
+
+def test_adjoint_with_live_psf_matches_reference_jacobian(case):
+    """The scene adjoint with a live PSF (PSF entries included) equals J^T g of the reference's
+    Jacobian, and the drop-in nll().backward() gives the reference's gradient sum W (M - D) dM."""
+    import astrophot_gb300 as ap
+
+    d, spec = case
+    sc = make_scene(d, spec)
+    rng = np.random.default_rng(9)
+    g = rng.normal(size=d["model0"].shape)
+    got = sc.vjp(d["rep0"], torch.tensor(g, dtype=torch.float32)).numpy()
+    ref = np.einsum("yxk,yx->k", d["jac_rep"], g)
+    assert np.max(np.abs(got - ref)) <= 1e-4 * np.max(np.abs(ref)), (got, ref)
+
+    ini = spec["init"]
+    k = spec["psf_size"]
+    psf_t = ap.image.PSF_Image(data=np.ones((k, k)) / k**2, pixelscale=1.0)
+    live = ap.models.AstroPhot_Model(name="nll psf", model_type=f"{kind_of(spec)} psf model", target=psf_t,
+                                     parameters=dict(ini["psf"]))
+    cx, cy, q, PA, n, Re, Ie = ini["gal"]
+    tgt = ap.image.Target_Image(data=d["data"], pixelscale=1.0, variance=1.0 / d["weight"])
+    gal = ap.models.AstroPhot_Model(name="nll gal", model_type="sersic galaxy model", target=tgt, psf_mode="full",
+                                    psf=live, parameters={"center": [cx, cy], "q": q, "PA": PA, "n": n, "Re": Re,
+                                                          "Ie": Ie})
+    gal.reference_center_gradient = False  # the render's derivative, which the Jacobian holds
+    vec = torch.tensor(d["rep0"], dtype=torch.float64, requires_grad=True)
+    nll = gal.negative_log_likelihood(parameters=vec, as_representation=True)
+    nll.backward()
+    gref = np.einsum("yxk,yx->k", d["jac_rep"], d["weight"] * (d["model0"] - d["data"]))
+    assert np.max(np.abs(vec.grad.numpy() - gref)) <= 1e-3 * np.max(np.abs(gref)), (vec.grad.numpy(), gref)
