@@ -273,7 +273,9 @@ __device__ __forceinline__ float sample_rel_err(const EvalF& e, float arg) {
   return 4e-7f + (fabsf(arg) + e.bn) * (5e-7f + 5e-7f * e.invn);
 }
 
-template <bool GRAD>
+// EXT: the PSF-model profiles (Moffat, Gaussian) are compiled in; galaxy batches use EXT = false
+// and get the Sersic / exponential code alone
+template <bool GRAD, bool EXT>
 __device__ __forceinline__ Sample eval_profile(const EvalF& e, int kind, float X, float Y,
                                                float area_scale) {
   Sample out;
@@ -284,12 +286,12 @@ __device__ __forceinline__ Sample eval_profile(const EvalF& e, int kind, float X
   const float u = R * e.invRe;
   const float amp = e.amp * area_scale;
   float t = u, lu2 = 0.f, w = 1.f, arg;
-  if (kind == AP_PROFILE_MOFFAT) {
+  if (EXT && kind == AP_PROFILE_MOFFAT) {
     // I0 / (1 + u^2)^n = I0 exp(-n ln(1 + u^2)); e.bn holds n
     w = fmaf(u, u, 1.f);
     lu2 = __log2f(w);
     arg = e.bn * (lu2 * 0.6931471805599453f);
-  } else if (kind == AP_PROFILE_GAUSSIAN) {
+  } else if (EXT && kind == AP_PROFILE_GAUSSIAN) {
     // I0 / sqrt(2 pi sigma^2) exp(-u^2 / 2), u = R / sigma: the prefactor is in amp
     arg = 0.5f * u * u;
   } else {
@@ -310,12 +312,12 @@ __device__ __forceinline__ Sample eval_profile(const EvalF& e, int kind, float X
       dIdR = -I * bt * invR;
       out.g[GRE] = I * bt * e.invRe;
       out.g[GN] = I * (-e.dbn * (t - 1.f) + bt * (lu2 * 0.6931471805599453f) * e.invn);
-    } else if (kind == AP_PROFILE_MOFFAT) {
+    } else if (EXT && kind == AP_PROFILE_MOFFAT) {
       const float nu = 2.f * e.bn * u / w;  // -d ln I / d u
       dIdR = -I * nu * e.invRe;
       out.g[GRE] = I * nu * u * e.invRe;
       out.g[GN] = -I * (lu2 * 0.6931471805599453f);
-    } else if (kind == AP_PROFILE_GAUSSIAN) {
+    } else if (EXT && kind == AP_PROFILE_GAUSSIAN) {
       dIdR = -I * u * e.invRe;
       out.g[GRE] = I * (u * u - 1.f) * e.invRe;  // the prefactor's 1/sigma included
       out.g[GN] = 0.f;
@@ -333,6 +335,7 @@ __device__ __forceinline__ Sample eval_profile(const EvalF& e, int kind, float X
 }
 
 // float64 value, same operation order as the reference.
+template <bool EXT>
 __device__ __forceinline__ double eval_profile64(const EvalDev& e, int kind, double X, double Y,
                                                  double area_scale) {
   const double Xr = e.c64 * X - e.s64 * Y;
@@ -342,11 +345,11 @@ __device__ __forceinline__ double eval_profile64(const EvalDev& e, int kind, dou
   if (kind == AP_PROFILE_SERSIC) {
     return amp * exp(-e.bn64 * (exp(log(R * e.invRe64) * e.invn64) - 1.0));
   }
-  if (kind == AP_PROFILE_MOFFAT) {
+  if (EXT && kind == AP_PROFILE_MOFFAT) {
     const double u = R * e.invRe64;
     return amp / pow(1.0 + u * u, e.bn64);
   }
-  if (kind == AP_PROFILE_GAUSSIAN) {
+  if (EXT && kind == AP_PROFILE_GAUSSIAN) {
     const double u = R * e.invRe64;
     return amp * exp(-0.5 * (u * u));
   }

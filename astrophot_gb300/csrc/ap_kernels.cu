@@ -319,7 +319,7 @@ __global__ void k_psf_shift(BatchArgs b, const float* psf, const float* psf_base
 // ---------------------------------------------------------------------------
 // sampling (_sample_init): deep value, partials, reference sub-sample, FP32 error bound
 // ---------------------------------------------------------------------------
-template <bool JAC>
+template <bool JAC, bool EXT>
 __device__ __forceinline__ void sample_pixel(const BatchArgs& b, const EvalF& e, int i, int j,
                                              float& deep, float* g, float& refsub, float& errb) {
   const QuadTables& T = *b.tables;
@@ -333,7 +333,7 @@ __device__ __forceinline__ void sample_pixel(const BatchArgs& b, const EvalF& e,
   for (int k = 0; k < T.nsub; ++k) {
     float X, Y;
     pix_to_offset(e, di + T.sxf[k], dj + T.syf[k], X, Y);
-    const Sample sm = eval_profile<JAC>(e, b.kind, X, Y, 1.f);
+    const Sample sm = eval_profile<JAC, EXT>(e, b.kind, X, Y, 1.f);
     const float w = T.swf[k];
     deep = fmaf(w, sm.v, deep);
     if (JAC) {
@@ -352,6 +352,7 @@ __device__ __forceinline__ void sample_pixel(const BatchArgs& b, const EvalF& e,
   errb = absb + 2.f * (float)T.nsub * kEps * mag + referr;
 }
 
+template <bool EXT>
 __device__ double sample_pixel64(const BatchArgs& b, const StampDev& st, const EvalDev& e, int i,
                                  int j, double* refsub) {
   const QuadTables& T = *b.tables;
@@ -360,14 +361,14 @@ __device__ double sample_pixel64(const BatchArgs& b, const StampDev& st, const E
   for (int k = 0; k < T.nsub; ++k) {
     double X, Y;
     pix_to_offset64(st, e, di + T.sx[k], dj + T.sy[k], X, Y);
-    const double f = eval_profile64(e, b.kind, X, Y, 1.0);
+    const double f = eval_profile64<EXT>(e, b.kind, X, Y, 1.0);
     deep += T.sw[k] * f;
     if (k == T.sub_center && refsub) *refsub = f;
   }
   return deep;
 }
 
-template <bool JAC>
+template <bool JAC, bool EXT>
 __device__ void sample_tile(const BatchArgs& b, const EvalF& e, int s, int slot, int tile_local) {
   const StampDev& st = b.stamps[s];
   const int tx = threadIdx.x & (kTile - 1), ty = threadIdx.x / kTile;
@@ -377,7 +378,7 @@ __device__ void sample_tile(const BatchArgs& b, const EvalF& e, int s, int slot,
   float deep = 0.f;
   if (valid) {
     float g[NGRAD], refsub, errb;
-    sample_pixel<JAC>(b, e, i, j, deep, g, refsub, errb);
+    sample_pixel<JAC, EXT>(b, e, i, j, deep, g, refsub, errb);
     const int64_t p = st.work_off + (int64_t)j * st.wnx + i;
     b.work[work_plane(b, slot, 0) + p] = deep;
     if (JAC) {
@@ -412,6 +413,7 @@ __device__ __forceinline__ void tile_chunk(uint32_t n, uint32_t& c0, uint32_t& c
   c1 = min(n, c0 + per);
 }
 
+template <bool EXT>
 __global__ void __launch_bounds__(256) k_sample(BatchArgs b) {
   const uint32_t n = b.counters[7];
   uint32_t c0, c1;
@@ -432,9 +434,9 @@ __global__ void __launch_bounds__(256) k_sample(BatchArgs b) {
       jac = (ed.ops & OP_JAC) != 0;
     }
     if (jac)
-      sample_tile<true>(b, e, s, slot, local);
+      sample_tile<true, EXT>(b, e, s, slot, local);
     else
-      sample_tile<false>(b, e, s, slot, local);
+      sample_tile<false, EXT>(b, e, s, slot, local);
   }
 }
 
@@ -556,6 +558,7 @@ __global__ void __launch_bounds__(256) k_select(BatchArgs b) {
 
 // Selection of the pixels the FP32 bound could not settle, one pixel per thread in float64
 // (the FP64 pipe retires whole-warp instructions, so the work is packed densely here).
+template <bool EXT>
 __global__ void __launch_bounds__(256) k_recheck(BatchArgs b) {
   const uint32_t n = min((uint32_t)b.counters[5], (uint32_t)(2 * b.work_pixels));
   const int lane = threadIdx.x & 31;
@@ -577,17 +580,17 @@ __global__ void __launch_bounds__(256) k_recheck(BatchArgs b) {
       double err64;
       if (b.sampling == AP_SAMPLING_MIDPOINT || b.sampling == AP_SAMPLING_TRAPEZOID) {
         const int ic = min(max(i, 1), st.wnx - 2), jc = min(max(j, 1), st.wny - 2);
-        const double m0 = sample_pixel64(b, st, e, i, j, nullptr);
-        const double u = sample_pixel64(b, st, e, ic, jc - 1, nullptr);
-        const double l = sample_pixel64(b, st, e, ic - 1, jc, nullptr);
-        const double m = (ic == i && jc == j) ? m0 : sample_pixel64(b, st, e, ic, jc, nullptr);
-        const double r = sample_pixel64(b, st, e, ic + 1, jc, nullptr);
-        const double dn = sample_pixel64(b, st, e, ic, jc + 1, nullptr);
+        const double m0 = sample_pixel64<EXT>(b, st, e, i, j, nullptr);
+        const double u = sample_pixel64<EXT>(b, st, e, ic, jc - 1, nullptr);
+        const double l = sample_pixel64<EXT>(b, st, e, ic - 1, jc, nullptr);
+        const double m = (ic == i && jc == j) ? m0 : sample_pixel64<EXT>(b, st, e, ic, jc, nullptr);
+        const double r = sample_pixel64<EXT>(b, st, e, ic + 1, jc, nullptr);
+        const double dn = sample_pixel64<EXT>(b, st, e, ic, jc + 1, nullptr);
         const double lap = u + l + (-4.0) * m + r + dn;
         err64 = fabs(m0 - (m0 + lap));
       } else {
         double ref64 = 0;
-        const double deep64 = sample_pixel64(b, st, e, i, j, &ref64);
+        const double deep64 = sample_pixel64<EXT>(b, st, e, i, j, &ref64);
         err64 = fabs(deep64 - ref64);
       }
       sel = err64 > thr64;
@@ -621,7 +624,7 @@ struct QuadResult {
 // One (sub-)pixel integrated by this lane alone: Q^2 samples at unit offsets
 // (ci + qx / scale, cj + qy / scale) with amplitude scale area.  QC > 0 fixes the quadrature
 // level at compile time (the sample loop unrolls into independent evaluations).
-template <bool JAC, int QC>
+template <bool JAC, int QC, bool EXT>
 __device__ __forceinline__ QuadResult quad_lane(const BatchArgs& b, const EvalF& e, float ci,
                                                 float cj, float inv_g, float area) {
   const QuadTables& T = *b.tables;
@@ -640,7 +643,7 @@ __device__ __forceinline__ QuadResult quad_lane(const BatchArgs& b, const EvalF&
     if (QC == 0 && k >= n) break;
     float X, Y;
     pix_to_offset(e, ci + T.qxf[k] * inv_g, cj + T.qyf[k] * inv_g, X, Y);
-    const Sample sm = eval_profile<JAC>(e, b.kind, X, Y, area);
+    const Sample sm = eval_profile<JAC, EXT>(e, b.kind, X, Y, area);
     const float w = T.qwf[k];
     r.res = fmaf(w, sm.v, r.res);
     if (JAC) {
@@ -661,6 +664,7 @@ __device__ __forceinline__ QuadResult quad_lane(const BatchArgs& b, const EvalF&
 
 // float64 re-evaluation of one (sub-)pixel's quadrature: pixel (i, j) of the working grid,
 // sub-pixel m of the displacement grid (m < 0: the pixel itself).
+template <bool EXT>
 __device__ bool refine64(const BatchArgs& b, const StampDev& st, const EvalDev& e, int i, int j,
                          int m, double thr64) {
   const QuadTables& T = *b.tables;
@@ -677,7 +681,7 @@ __device__ bool refine64(const BatchArgs& b, const StampDev& st, const EvalDev& 
   for (int k = 0; k < n; ++k) {
     double X, Y;
     pix_to_offset64(st, e, ci + T.qx[k] * inv_g, cj + T.qy[k] * inv_g, X, Y);
-    const double f = eval_profile64(e, b.kind, X, Y, area);
+    const double f = eval_profile64<EXT>(e, b.kind, X, Y, area);
     res += f * T.qw[k];
     if (k == n / 2) ref = f;
   }
@@ -686,6 +690,7 @@ __device__ bool refine64(const BatchArgs& b, const StampDev& st, const EvalDev& 
 
 // Level-2 refinement decision of sub-pixel m: FP32 when clear of the error band, else
 // float64 (threshold scaled by gridding^2 as the reference passes it down).
+template <bool EXT>
 __device__ __forceinline__ bool decide(const BatchArgs& b, const StampDev& st, const EvalDev& e,
                                        const QuadResult& r, float thr, int i, int j, int m,
                                        int& n64) {
@@ -695,7 +700,7 @@ __device__ __forceinline__ bool decide(const BatchArgs& b, const StampDev& st, c
   if (diff < thr - band) return false;
   ++n64;
   const int g = b.tables->gridding;
-  return refine64(b, st, e, i, j, m, e.thresh64 * (double)(g * g));
+  return refine64<EXT>(b, st, e, i, j, m, e.thresh64 * (double)(g * g));
 }
 
 __device__ __forceinline__ void write_deep(const BatchArgs& b, const StampDev& st, int slot,
@@ -711,7 +716,7 @@ __device__ __forceinline__ void write_deep(const BatchArgs& b, const StampDev& s
 // Level 1 of grid_integrate, one queued pixel per thread: the Q x Q Gauss-Legendre
 // integral and its refinement decision.  Pixels that stop here are written; the others go
 // to the level-2 queue (b.recheck, emptied by k_recheck before this kernel runs).
-template <int QC>
+template <int QC, bool EXT>
 __device__ __forceinline__ void level1_pixel(const BatchArgs& b, int64_t ent, bool& push, bool& amb,
                                              int& n64) {
   const int slot = (int)(ent >> 62);
@@ -723,8 +728,8 @@ __device__ __forceinline__ void level1_pixel(const BatchArgs& b, int64_t ent, bo
   const int i = (int)(p % st.wnx), j = (int)(p / st.wnx);
   const float di = (float)(i - f.cix), dj = (float)(j - f.cjy);
   const bool jac = (e.ops & OP_JAC) != 0;
-  QuadResult r = jac ? quad_lane<true, QC>(b, f, di, dj, 1.f, 1.f)
-                     : quad_lane<false, QC>(b, f, di, dj, 1.f, 1.f);
+  QuadResult r = jac ? quad_lane<true, QC, EXT>(b, f, di, dj, 1.f, 1.f)
+                     : quad_lane<false, QC, EXT>(b, f, di, dj, 1.f, 1.f);
   bool split = false;
   if (b.max_depth > 1) {
     const float thr = e.thresh;
@@ -760,6 +765,7 @@ __device__ __forceinline__ bool warp_append(bool flag, int64_t ent, int64_t* lis
   return true;
 }
 
+template <bool EXT>
 __global__ void __launch_bounds__(256, 3) k_level1(BatchArgs b) {
   const uint32_t n = min((uint32_t)b.counters[0], (uint32_t)(2 * b.work_pixels));
   const int Q = b.tables->quad_level;
@@ -771,9 +777,9 @@ __global__ void __launch_bounds__(256, 3) k_level1(BatchArgs b) {
     if (idx < n) {
       ent = b.queue[idx];
       if (Q == 3)
-        level1_pixel<3>(b, ent, push, amb, n64);
+        level1_pixel<3, EXT>(b, ent, push, amb, n64);
       else
-        level1_pixel<0>(b, ent, push, amb, n64);
+        level1_pixel<0, EXT>(b, ent, push, amb, n64);
     }
     if (!warp_append(amb, ent, b.amb, &b.counters[12], b.amb_cap)) {
       // the dense list is full: decide here
@@ -782,7 +788,7 @@ __global__ void __launch_bounds__(256, 3) k_level1(BatchArgs b) {
       const int64_t p = ent & 0xffffffffll;
       const StampDev& st = b.stamps[s];
       ++n64;
-      push = refine64(b, st, b.evals[s * 2 + slot], (int)(p % st.wnx), (int)(p / st.wnx), -1,
+      push = refine64<EXT>(b, st, b.evals[s * 2 + slot], (int)(p % st.wnx), (int)(p / st.wnx), -1,
                       b.evals[s * 2 + slot].thresh64);
     }
     warp_append(push, ent, b.recheck, &b.counters[10], (int64_t)2 * b.work_pixels);
@@ -797,6 +803,7 @@ __global__ void __launch_bounds__(256, 3) k_level1(BatchArgs b) {
 
 // float64 split decisions of the level-1 pixels inside the FP32 error band, one per lane
 // (all lanes of a warp busy: the FP64 pipe is narrow); splits join the level-2 queue.
+template <bool EXT>
 __global__ void __launch_bounds__(256) k_level1_amb(BatchArgs b) {
   const int64_t n = min((int64_t)b.counters[12], b.amb_cap);
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
@@ -810,7 +817,7 @@ __global__ void __launch_bounds__(256) k_level1_amb(BatchArgs b) {
       const int64_t p = ent & 0xffffffffll;
       const StampDev& st = b.stamps[s];
       const EvalDev& e = b.evals[s * 2 + slot];
-      push = refine64(b, st, e, (int)(p % st.wnx), (int)(p / st.wnx), -1, e.thresh64);
+      push = refine64<EXT>(b, st, e, (int)(p % st.wnx), (int)(p / st.wnx), -1, e.thresh64);
     }
     warp_append(push, ent, b.recheck, &b.counters[10], (int64_t)2 * b.work_pixels);
   }
@@ -820,7 +827,7 @@ __global__ void __launch_bounds__(256) k_level1_amb(BatchArgs b) {
 // Levels 2 and 3 of grid_integrate for a pixel that level 1 split: one warp per pixel,
 // one sub-pixel per lane; each level-2 sub-pixel flagged for refinement is split again and
 // integrated by the whole warp.
-template <bool JAC, int QC>
+template <bool JAC, int QC, bool EXT>
 __device__ void level23_pixel(const BatchArgs& b, int slot, int s, int64_t p, int lane,
                               unsigned long long& samples, int& n64) {
   const StampDev& st = b.stamps[s];
@@ -844,8 +851,8 @@ __device__ void level23_pixel(const BatchArgs& b, int slot, int s, int64_t p, in
   if (lane < G2) {
     ci2 = di + T.gxf[lane];
     cj2 = dj + T.gyf[lane];
-    r2 = quad_lane<JAC, QC>(b, f, ci2, cj2, ginv, area2);
-    if (b.max_depth > 2) split2 = decide(b, st, e, r2, thr * (float)G2, i, j, lane, n64);
+    r2 = quad_lane<JAC, QC, EXT>(b, f, ci2, cj2, ginv, area2);
+    if (b.max_depth > 2) split2 = decide<EXT>(b, st, e, r2, thr * (float)G2, i, j, lane, n64);
   }
   // level 3: refine each flagged sub-pixel with the whole warp
   unsigned todo = __ballot_sync(0xffffffffu, split2);
@@ -861,7 +868,7 @@ __device__ void level23_pixel(const BatchArgs& b, int slot, int s, int64_t p, in
 #pragma unroll
     for (int q = 0; q < NGRAD; ++q) r3.g[q] = 0.f;
     if (lane < G2) {
-      r3 = quad_lane<JAC, QC>(b, f, cim + T.gxf[lane] * ginv, cjm + T.gyf[lane] * ginv,
+      r3 = quad_lane<JAC, QC, EXT>(b, f, cim + T.gxf[lane] * ginv, cjm + T.gyf[lane] * ginv,
                               ginv * ginv, area3);
     }
     const float s3 = warp_sum(r3.res);
@@ -886,6 +893,7 @@ __device__ void level23_pixel(const BatchArgs& b, int slot, int s, int64_t p, in
   if (lane == 0) write_deep(b, st, slot, p, out_v, out_g, JAC);
 }
 
+template <bool EXT>
 __global__ void __launch_bounds__(256, 3) k_integrate(BatchArgs b) {
   const int lane = threadIdx.x & 31;
   constexpr uint32_t kChunk = 2;  // queue entries grabbed per atomic
@@ -907,14 +915,14 @@ __global__ void __launch_bounds__(256, 3) k_integrate(BatchArgs b) {
       const bool jac = (b.evals[s * 2 + slot].ops & OP_JAC) != 0;
       if (Q == 3) {
         if (jac)
-          level23_pixel<true, 3>(b, slot, s, p, lane, samples, n64);
+          level23_pixel<true, 3, EXT>(b, slot, s, p, lane, samples, n64);
         else
-          level23_pixel<false, 3>(b, slot, s, p, lane, samples, n64);
+          level23_pixel<false, 3, EXT>(b, slot, s, p, lane, samples, n64);
       } else {
         if (jac)
-          level23_pixel<true, 0>(b, slot, s, p, lane, samples, n64);
+          level23_pixel<true, 0, EXT>(b, slot, s, p, lane, samples, n64);
         else
-          level23_pixel<false, 0>(b, slot, s, p, lane, samples, n64);
+          level23_pixel<false, 0, EXT>(b, slot, s, p, lane, samples, n64);
       }
     }
   }
@@ -1404,20 +1412,35 @@ cudaError_t launch_render_pass(const BatchArgs& b, const ConvIO& io, size_t conv
     E(t);
   }
   t = B(KC_SAMPLE);
-  k_sample<<<grid(2 * (int64_t)b.n_work_tiles, knob(GK_SAMPLE, 8)), kTile * kTile, 0, s>>>(b);
+  // PSF-model profiles take the kernels compiled with them; galaxies the Sersic/exponential ones
+  const bool ext = b.kind == AP_PROFILE_MOFFAT || b.kind == AP_PROFILE_GAUSSIAN;
+  const unsigned sgrid = grid(2 * (int64_t)b.n_work_tiles, knob(GK_SAMPLE, 8));
+  if (ext)
+    k_sample<true><<<sgrid, kTile * kTile, 0, s>>>(b);
+  else
+    k_sample<false><<<sgrid, kTile * kTile, 0, s>>>(b);
   if (b.kind != AP_PROFILE_SERSIC && b.integrate == AP_INTEGRATE_THRESHOLD)
     k_exp_threshold<<<(b.n_stamps * 2 + 127) / 128, 128, 0, s>>>(b);
   E(t);
   if (b.integrate == AP_INTEGRATE_THRESHOLD) {
     t = B(KC_SELECT);
     k_select<<<grid(2 * (int64_t)b.n_work_tiles, knob(GK_SAMPLE, 8)), kTile * kTile, 0, s>>>(b);
-    k_recheck<<<nsm * 4, 256, 0, s>>>(b);
+    if (ext)
+      k_recheck<true><<<nsm * 4, 256, 0, s>>>(b);
+    else
+      k_recheck<false><<<nsm * 4, 256, 0, s>>>(b);
     E(t);
     t = B(KC_INTEGRATE);
     const int gi = nsm * knob(GK_INTEGRATE, 8);
-    k_level1<<<gi, 256, 0, s>>>(b);
-    if (b.amb_cap > 0) k_level1_amb<<<nsm * 4, 256, 0, s>>>(b);
-    k_integrate<<<gi, 256, 0, s>>>(b);
+    if (ext) {
+      k_level1<true><<<gi, 256, 0, s>>>(b);
+      if (b.amb_cap > 0) k_level1_amb<true><<<nsm * 4, 256, 0, s>>>(b);
+      k_integrate<true><<<gi, 256, 0, s>>>(b);
+    } else {
+      k_level1<false><<<gi, 256, 0, s>>>(b);
+      if (b.amb_cap > 0) k_level1_amb<false><<<nsm * 4, 256, 0, s>>>(b);
+      k_integrate<false><<<gi, 256, 0, s>>>(b);
+    }
     E(t);
   }
   t = B(KC_CONV);

@@ -69,6 +69,8 @@ def parse():
     p.add_argument("--seed", type=int, default=2024)
     p.add_argument("--cpu-sample", type=int, default=8, help="stamps fitted by the CPU baseline")
     p.add_argument("--rounds-per-sync", type=int, default=8)
+    p.add_argument("--grid", default=None,
+                   help="blocks per SM of sample,integrate,conv,psf (default: the autotuner picks them)")
     p.add_argument("--livepsf-workers", type=int, default=16, help="concurrent fits (host threads / streams)")
     p.add_argument("--no-graph", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
@@ -622,7 +624,12 @@ def run_gpu_learned(args):
     # in-project autotuners (outside the timed region): CNN GEMM tile shapes per layer shape,
     # persistent-grid sizes of the render pass
     N.lib().ap_cnn_autotune(1, None)
-    tuned = batch.autotune(cnn.moments_init(st, S), st.psf, jacobian=True)
+    if args.grid:
+        grid = dict(zip(N.StampBatch.GRID_KNOBS, (int(v) for v in args.grid.split(","))))
+        batch.set_grid(grid)
+        tuned = {"blocks_per_sm": grid, "render_pass_ms": None, "fixed": True}
+    else:
+        tuned = batch.autotune(cnn.moments_init(st, S), st.psf, jacobian=True)
 
     def step_device():
         return cnn.learned_fit(net, st, S, lmo)
