@@ -739,7 +739,7 @@ def run_gpu_learned(args):
         "unit": "TFLOP/s",
         "frac": achieved / fp32_peak if achieved else None,
         # DRAM bytes per launch from one ncu capture of the 4096-stamp case (mean over all
-        # k_conv launches, 99.9 MB), scaled by the stamps per launch (profiles/k_conv_learned_init_4096.md)
+        # k_conv launches, 99.9 MB), scaled by the stamps per launch (the k_conv summary in profiles/)
         "traffic": 99.9e6 * S / 4096,
         "traffic_unit": "bytes per launch (ncu, 4096-stamp capture scaled by stamps)",
         "launches": conv_n,
