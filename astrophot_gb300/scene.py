@@ -397,7 +397,7 @@ class Scene:
         K, dK = self.live_psf.render(grad)
         for part in self._jac_parts + self._fwd_parts:
             if part["psf"] is not None:
-                part["psf"].copy_(K.repeat(part["psf"].numel() // K.numel()))
+                part["psf"].view(-1, K.numel()).copy_(K.expand(part["psf"].numel() // K.numel(), -1))
         return dK
 
     # ---- device primitives -----------------------------------------------------------------
@@ -437,6 +437,16 @@ class Scene:
         img = torch.empty(self.nx * self.ny, dtype=torch.float32, device=self.device)
         return self._combine(self.fwd, self.sky, img)
 
+    def _psf_column(self, V, rep, dK, j, as_representation, out):
+        """Image-wide column ``j`` of a live PSF into ``out`` [ny * nx]: every source rendered
+        with the derivative of its kernel along d psf / d theta_j, summed like the model."""
+        scale = float(self.live_psf.drep(np.asarray(rep, dtype=np.float64)[: self.n_psf])[j]) \
+            if as_representation else 1.0
+        D = dK[j] * scale
+        self._render_sources(V, self.fwd_d, lambda b, p, k, o: b.render_psf_derivative(
+            p, k, D.repeat(k.numel() // D.numel()), out=o))
+        return self._combine(self.fwd_d, 0.0, out)
+
     def jacobian(self, rep: np.ndarray, as_representation: bool = True):
         """Own-window Jacobians of every source (representation or value space) into ``self.jac``,
         and the image-wide columns of a live PSF's parameters."""
@@ -446,16 +456,10 @@ class Scene:
             b = part["batch"]
             jac = self.jac[part["off"] : part["off"] + part["nf"] * b.out_pixels].view(part["nf"], b.out_pixels)
             b.jacobian(torch.tensor(V[part["members"]]), part["psf"], as_representation=as_representation, jac=jac)
-        if self.n_psf:
-            scale = self.live_psf.drep(np.asarray(rep, dtype=np.float64)[: self.n_psf]) if as_representation else \
-                np.ones(self.n_psf)
-            npx = self.nx * self.ny
-            for j in range(self.n_psf):
-                D = dK[j] * float(scale[j])
-                self._render_sources(V, self.fwd_d, lambda b, p, k, out: b.render_psf_derivative(
-                    p, k, D.repeat(k.numel() // D.numel()), out=out))
-                col = self.jac[self.psf_jac_off + j * npx : self.psf_jac_off + (j + 1) * npx]
-                self._combine(self.fwd_d, 0.0, col)
+        npx = self.nx * self.ny
+        for j in range(self.n_psf):
+            self._psf_column(V, rep, dK, j, as_representation,
+                             self.jac[self.psf_jac_off + j * npx : self.psf_jac_off + (j + 1) * npx])
         return self.jac
 
     def jacobian_image(self, rep: np.ndarray, as_representation: bool = True) -> np.ndarray:
@@ -502,15 +506,10 @@ class Scene:
             # a live PSF's entries: the upstream gradient against each image-wide PSF column
             # (the render's derivative along d psf / d theta); the sources below see the current PSF
             dK = self._refresh_psf(rep, True)
-            scale = self.live_psf.drep(np.asarray(rep, dtype=np.float64)[: self.n_psf]) if as_representation else \
-                np.ones(self.n_psf)
             V = self.values_matrix(rep)
             col = torch.empty(self.nx * self.ny, dtype=torch.float32, device=self.device)
             for j in range(self.n_psf):
-                D = dK[j] * float(scale[j])
-                self._render_sources(V, self.fwd_d, lambda b, p, k, o: b.render_psf_derivative(
-                    p, k, D.repeat(k.numel() // D.numel()), out=o))
-                self._combine(self.fwd_d, 0.0, col)
+                self._psf_column(V, rep, dK, j, as_representation, col)
                 out[j] = float(torch.dot(col.to(torch.float64), g_img.to(torch.float64)).item())
         V = self.values_matrix(rep)
         for part in self._fwd_parts:
