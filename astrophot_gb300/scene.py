@@ -85,6 +85,7 @@ class LivePSF:
         self.npix = self.kx * self.ky
         self.K = torch.empty(self.npix, dtype=torch.float32, device=self.device)
         self.dK = torch.empty((max(len(self.free), 1), self.npix), dtype=torch.float32, device=self.device)
+        self.row_d = torch.zeros((1, 8), dtype=torch.float64, device=self.device)  # staged parameter row
         self.lib = N.lib()
 
     def _row(self):
@@ -104,14 +105,20 @@ class LivePSF:
         """d value / d representation of the free parameters."""
         return np.array([float(drep_dvalue(*self.limits[f], r)) for f, r in zip(self.free, rep)])
 
-    def render(self, grad: bool = False):
+    def stage(self):
+        """Copy the current parameter row to the device (``render(staged=True)`` reads it)."""
+        self.row_d.copy_(self._row())
+
+    def render(self, grad: bool = False, staged: bool = False):
         """(K [ky * kx], dK [n_free][ky * kx] or None): the normalised PSF image and its
-        value-space derivatives."""
+        value-space derivatives; ``staged`` reads the parameters :meth:`stage` copied (no
+        host-to-device copy, so the call can be captured in a CUDA graph)."""
         m = len(self.free) if grad else 0
+        row = self.row_d if staged else self._row()
         if m:
-            model, jac = self.batch.jacobian(self._row(), None, as_representation=False)
+            model, jac = self.batch.jacobian(row, None, as_representation=False)
         else:
-            model, jac = self.batch.render(self._row(), None), None
+            model, jac = self.batch.render(row, None), None
         N.check(self.lib.ap_psf_normalize(self.npix, m, N._ptr(model), N._ptr(jac), N._ptr(self.K), N._ptr(self.dK),
                                           N._stream()), "ap_psf_normalize")
         return self.K, (self.dK[:m] if m else None)
@@ -159,7 +166,8 @@ class Scene:
 
     def __init__(self, nx: int, ny: int, sources: List[SceneSource], psf: Optional[np.ndarray], data, weight,
                  mask=None, sky: float = 0.0, scale: float = 1.0, options: Optional[dict] = None,
-                 fwd_chunk: int = 64, device="cuda", origin=(0.0, 0.0), psf_model: Optional[LivePSF] = None):
+                 fwd_chunk: int = 64, device="cuda", origin=(0.0, 0.0), psf_model: Optional[LivePSF] = None,
+                 graphs: bool = True):
         self.nx, self.ny, self.scale = int(nx), int(ny), float(scale)
         self.origin = (float(origin[0]), float(origin[1]))
         self.sources = list(sources)
@@ -273,6 +281,33 @@ class Scene:
                 fwd_total += len(members) * self.nx * self.ny
         self.fwd = torch.zeros(max(fwd_total, 1), dtype=torch.float32, device=dev)
         self.fwd_d = torch.zeros_like(self.fwd) if psf_model is not None else None
+
+        # staged parameters: every render's value rows, the live PSF's row and its column scales
+        # in one float64 buffer (one host-to-device copy per evaluation, by _stage); the render
+        # bodies read only device memory, so each is captured once and replayed as a CUDA graph
+        rows = 0
+        for part in self._jac_parts:
+            part["srow"] = (rows, len(part["members"]))
+            rows += len(part["members"])
+        for part in self._fwd_parts:
+            n_chunks = 1 if part["own"] else (len(part["members"]) + part["m"] - 1) // part["m"]
+            part["srow"] = [(rows + c * part["m"], len(part["members"]) if part["own"] else part["m"])
+                            for c in range(n_chunks)]
+            rows += n_chunks * (len(part["members"]) if part["own"] else part["m"])
+        self._psf_row = rows
+        rows += 1
+        self._stage_h = np.zeros((rows + 1, 8))  # last row: the PSF columns' d value / d rep
+        self._stage_d = torch.zeros((rows + 1, 8), dtype=torch.float64, device=dev)
+        for part in self._jac_parts:
+            r0, n = part["srow"]
+            part["dpar"] = self._stage_d[r0 : r0 + n]
+        for part in self._fwd_parts:
+            part["dpar"] = [self._stage_d[r0 : r0 + n] for r0, n in part["srow"]]
+        if psf_model is not None:
+            psf_model.row_d = self._stage_d[self._psf_row : self._psf_row + 1]
+        self._img = torch.empty(self.nx * self.ny, dtype=torch.float32, device=dev)
+        self.use_graphs = bool(graphs)
+        self._graphs, self._graph_failed = {}, set()
 
         # ---- source descriptors (+ one whole-image entry carrying the live PSF columns) --------
         ns = len(self.sources)
@@ -390,36 +425,82 @@ class Scene:
         if self.n_psf:
             self.live_psf.set_representation(rep[: self.n_psf])
 
-    def _refresh_psf(self, rep, grad: bool):
-        """Sample the live PSF at ``rep`` and copy it into every batch's packed PSF; returns its
-        value-space derivatives when ``grad``."""
-        self.live_psf.set_representation(np.asarray(rep, dtype=np.float64)[: self.n_psf])
-        K, dK = self.live_psf.render(grad)
+    def _stage(self, rep, as_representation: bool = True):
+        """Every render's parameter rows (and a live PSF's row and column scales) at ``rep`` into
+        the device staging buffer, in one copy."""
+        rep = np.asarray(rep, dtype=np.float64)
+        V = self.values_matrix(rep)
+        H = self._stage_h
+        for part in self._jac_parts:
+            r0, n = part["srow"]
+            H[r0 : r0 + n] = V[part["members"]]
+        for part in self._fwd_parts:
+            mem, m = part["members"], part["m"]
+            if part["own"]:
+                r0, n = part["srow"][0]
+                H[r0 : r0 + n] = V[mem]
+                continue
+            for (r0, n), c0 in zip(part["srow"], range(0, len(mem), m)):
+                chunk = mem[c0 : c0 + m]
+                H[r0 : r0 + n] = V[chunk[0]]
+                H[r0 : r0 + len(chunk)] = V[chunk]
+        if self.n_psf:
+            live = self.live_psf
+            live.set_representation(rep[: self.n_psf])
+            H[self._psf_row] = live._row().numpy()[0]
+            H[-1, : self.n_psf] = live.drep(rep[: self.n_psf]) if as_representation else 1.0
+        self._stage_d.copy_(torch.from_numpy(H))
+        return V
+
+    def _psf_body(self, grad: bool):
+        """Sample the live PSF from the staged row and copy it into every batch's packed PSF;
+        returns its value-space derivatives when ``grad``."""
+        K, dK = self.live_psf.render(grad, staged=True)
         for part in self._jac_parts + self._fwd_parts:
             if part["psf"] is not None:
                 part["psf"].view(-1, K.numel()).copy_(K.expand(part["psf"].numel() // K.numel(), -1))
         return dK
 
+    def _run(self, key, body):
+        """``body()`` (device work only, reading staged parameters), replayed from a CUDA graph
+        captured at its first call when graphs are on; eager if the capture fails."""
+        if not self.use_graphs or key in self._graph_failed:
+            body()
+            return
+        g = self._graphs.get(key)
+        if g is None:
+            side = torch.cuda.Stream(device=self.device)
+            side.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(side):
+                body()  # this call's result, and the allocations the capture reuses
+            torch.cuda.current_stream().wait_stream(side)
+            g = torch.cuda.CUDAGraph()
+            try:
+                with torch.cuda.graph(g, capture_error_mode="thread_local"):
+                    body()
+            except Exception:
+                self._graph_failed.add(key)
+                return
+            self._graphs[key] = g
+            return
+        g.replay()
+
     # ---- device primitives -----------------------------------------------------------------
-    def _render_sources(self, V, buf, render):
+    def _render_sources(self, buf, render):
         """Every source's model render into ``buf`` (the layout of ``self.fwd``) by
-        ``render(batch, params, packed psf, out)``."""
+        ``render(batch, staged params, packed psf, out)``."""
         for part in self._fwd_parts:
             b, m, mem = part["batch"], part["m"], part["members"]
             if part["own"]:
-                render(b, torch.tensor(V[mem]), part["psf"], buf[part["off"] : part["off"] + b.out_pixels])
+                render(b, part["dpar"][0], part["psf"], buf[part["off"] : part["off"] + b.out_pixels])
                 continue
-            for c0 in range(0, len(mem), m):
-                chunk = mem[c0 : c0 + m]
-                params = np.zeros((m, 8))
-                params[:, :] = V[chunk[0]]
-                params[: len(chunk)] = V[chunk]
+            for c, c0 in enumerate(range(0, len(mem), m)):
                 out = buf[part["off"] + c0 * self.nx * self.ny : part["off"] + (c0 + m) * self.nx * self.ny]
                 if out.numel() == m * self.nx * self.ny:
-                    render(b, torch.tensor(params), part["psf"], out)
+                    render(b, part["dpar"][c], part["psf"], out)
                 else:
                     tmp = torch.empty(b.out_pixels, dtype=torch.float32, device=self.device)
-                    render(b, torch.tensor(params), part["psf"], tmp)
+                    render(b, part["dpar"][c], part["psf"], tmp)
                     out.copy_(tmp[: out.numel()])
 
     def _combine(self, buf, sky, img):
@@ -428,38 +509,43 @@ class Scene:
                                           N._stream()), "ap_scene_forward")
         return img
 
+    def _forward_body(self):
+        if self.n_psf:
+            self._psf_body(False)
+        self._render_sources(self.fwd, lambda b, p, k, out: b.render(p, k, out=out))
+        self._combine(self.fwd, self.sky, self._img)
+
     def forward(self, rep: np.ndarray) -> torch.Tensor:
         """Model image [ny * nx] (float32) at the joint representation vector."""
-        if self.n_psf:
-            self._refresh_psf(rep, False)
-        V = self.values_matrix(rep)
-        self._render_sources(V, self.fwd, lambda b, p, k, out: b.render(p, k, out=out))
-        img = torch.empty(self.nx * self.ny, dtype=torch.float32, device=self.device)
-        return self._combine(self.fwd, self.sky, img)
+        self._stage(rep)
+        self._run("forward", self._forward_body)
+        return self._img.clone()
 
-    def _psf_column(self, V, rep, dK, j, as_representation, out):
+    def _psf_column(self, dK, j, out):
         """Image-wide column ``j`` of a live PSF into ``out`` [ny * nx]: every source rendered
-        with the derivative of its kernel along d psf / d theta_j, summed like the model."""
-        scale = float(self.live_psf.drep(np.asarray(rep, dtype=np.float64)[: self.n_psf])[j]) \
-            if as_representation else 1.0
-        D = dK[j] * scale
-        self._render_sources(V, self.fwd_d, lambda b, p, k, o: b.render_psf_derivative(
+        with the derivative of its kernel along d psf / d theta_j (scaled by the staged
+        d value / d representation), summed like the model."""
+        D = dK[j] * self._stage_d[-1, j].to(torch.float32)
+        self._render_sources(self.fwd_d, lambda b, p, k, o: b.render_psf_derivative(
             p, k, D.repeat(k.numel() // D.numel()), out=o))
         return self._combine(self.fwd_d, 0.0, out)
+
+    def _jacobian_body(self, as_representation: bool):
+        dK = self._psf_body(True) if self.n_psf else None
+        for part in self._jac_parts:
+            b = part["batch"]
+            jac = self.jac[part["off"] : part["off"] + part["nf"] * b.out_pixels].view(part["nf"], b.out_pixels)
+            b.jacobian(part["dpar"], part["psf"], as_representation=as_representation, jac=jac)
+        npx = self.nx * self.ny
+        for j in range(self.n_psf):
+            self._psf_column(dK, j, self.jac[self.psf_jac_off + j * npx : self.psf_jac_off + (j + 1) * npx])
 
     def jacobian(self, rep: np.ndarray, as_representation: bool = True):
         """Own-window Jacobians of every source (representation or value space) into ``self.jac``,
         and the image-wide columns of a live PSF's parameters."""
-        dK = self._refresh_psf(rep, True) if self.n_psf else None
-        V = self.values_matrix(rep)
-        for part in self._jac_parts:
-            b = part["batch"]
-            jac = self.jac[part["off"] : part["off"] + part["nf"] * b.out_pixels].view(part["nf"], b.out_pixels)
-            b.jacobian(torch.tensor(V[part["members"]]), part["psf"], as_representation=as_representation, jac=jac)
-        npx = self.nx * self.ny
-        for j in range(self.n_psf):
-            self._psf_column(V, rep, dK, j, as_representation,
-                             self.jac[self.psf_jac_off + j * npx : self.psf_jac_off + (j + 1) * npx])
+        as_representation = bool(as_representation)
+        self._stage(rep, as_representation)
+        self._run(("jacobian", as_representation), lambda: self._jacobian_body(as_representation))
         return self.jac
 
     def jacobian_image(self, rep: np.ndarray, as_representation: bool = True) -> np.ndarray:
@@ -505,11 +591,11 @@ class Scene:
         if self.n_psf:
             # a live PSF's entries: the upstream gradient against each image-wide PSF column
             # (the render's derivative along d psf / d theta); the sources below see the current PSF
-            dK = self._refresh_psf(rep, True)
-            V = self.values_matrix(rep)
+            self._stage(rep, as_representation)
+            dK = self._psf_body(True)
             col = torch.empty(self.nx * self.ny, dtype=torch.float32, device=self.device)
             for j in range(self.n_psf):
-                self._psf_column(V, rep, dK, j, as_representation, col)
+                self._psf_column(dK, j, col)
                 out[j] = float(torch.dot(col.to(torch.float64), g_img.to(torch.float64)).item())
         V = self.values_matrix(rep)
         for part in self._fwd_parts:
