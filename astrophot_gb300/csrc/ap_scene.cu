@@ -496,4 +496,13 @@ int ap_dense_damped_solve(int32_t n, const double* H, const double* g, double L,
   return record_cuda(cudaGetLastError());
 }
 
+int ap_dense_factored_solve(int32_t n, const double* g, double* h, void* ws, size_t ws_bytes, ap_stream_t stream) {
+  if (n <= 0 || !g || !h || !ws) return AP_ERR_ARG;
+  if (ws_bytes < ap_dense_solve_workspace_bytes(n)) return AP_ERR_WORKSPACE;
+  double* A = (double*)ws;
+  double* y = A + (size_t)n * n;
+  k_chol_solve<<<1, 1024, 0, (cudaStream_t)stream>>>(A, n, g, h, y);
+  return record_cuda(cudaGetLastError());
+}
+
 }  // extern "C"

@@ -669,11 +669,16 @@ class Scene:
                                             N._stream()), "ap_scene_rpp_image")
         return out
 
-    def solve(self, H: torch.Tensor, g: torch.Tensor, L: float):
+    def solve(self, H: torch.Tensor, g: torch.Tensor, L: float, reuse: bool = False):
         """Damped solve of the n x n system H (n = H's side, at most P); None when the damped
-        matrix is not positive definite."""
+        matrix is not positive definite.  ``reuse``: the same H and L as the previous (successful)
+        call, another right-hand side: only the triangular solves on its factor run."""
         n = int(H.shape[0])
         h = torch.empty(n, dtype=torch.float64, device=self.device)
+        if reuse:
+            N.check(self.lib.ap_dense_factored_solve(n, N._ptr(g.contiguous()), N._ptr(h), N._ptr(self._solve_ws),
+                                                     self._solve_ws.numel(), N._stream()), "ap_dense_factored_solve")
+            return h
         N.check(self.lib.ap_dense_damped_solve(n, N._ptr(H.contiguous()), N._ptr(g.contiguous()), float(L), N._ptr(h),
                                                N._ptr(self._solve_ws), self._solve_ws.numel(), N._ptr(self._info),
                                                N._stream()), "ap_dense_damped_solve")
@@ -758,7 +763,7 @@ class SceneLM:
             rh = sc.residual(sc.data, Y1)   # W (Y1 - Y)
             rpp = self._sub(sc.jt(sc.rpp_image(r, rh, sc.jvp(h), d)))
             if self.L > 1e-4:
-                a_d = sc.solve(hess, rpp, self.L)
+                a_d = sc.solve(hess, rpp, self.L, reuse=True)  # the factor of the h solve above
                 a = np.zeros_like(h_np) if a_d is None else -self._full(a_d).cpu().numpy() / 2
             else:
                 a = np.zeros_like(h_np)

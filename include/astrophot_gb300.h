@@ -368,6 +368,12 @@ int ap_scene_rpp_image(const float* r, const float* rh, const float* jh, const f
 size_t ap_dense_solve_workspace_bytes(int32_t n);
 int ap_dense_damped_solve(int32_t n, const double* H, const double* g, double L, double* h,
                           void* ws, size_t ws_bytes, int32_t* info, ap_stream_t stream);
+/* h = the same damped system solved for another right-hand side g: the two triangular solves
+ * on the Cholesky factor the last ap_dense_damped_solve left in ws (it must have reported
+ * info = 0).  LM.step solves its damped system twice per trial, for the step and for the
+ * geodesic term (fit/lm.py:286-299). */
+int ap_dense_factored_solve(int32_t n, const double* g, double* h, void* ws, size_t ws_bytes,
+                            ap_stream_t stream);
 
 /* ---- learned initial guess -----------------------------------------------------------------
  * No counterpart in the reference: its initial values come from the heuristics of
