@@ -17,6 +17,11 @@
 the damping search, geodesic right-hand side, curvature test, convergence rules and
 ``res()`` of the reference, with all images, Jacobians and reductions on the device.
 
+Every evaluation stages its parameters (all renders' value rows, a live PSF's row) in one
+host-to-device copy; the forward and the Jacobian then read device memory only, so each is
+captured once as a CUDA graph and replayed (``graphs=False``: launched one by one).  The LM's
+geodesic-term solve reuses the Cholesky factor of its step solve (``ap_dense_factored_solve``).
+
 A scene's PSF may be a live Moffat PSF model (``set_aux_psf``, models/model_object.py:133-149)
 instead of a fixed image: :class:`LivePSF` samples it on its PSF image at every evaluation, its
 free parameters lead the joint vector (the linked PSF node comes before the galaxy's own
@@ -162,7 +167,8 @@ class Scene:
     """Sources on one ``nx`` x ``ny`` image (pixel scale ``scale``, the (0, 0) pixel corner at the
     origin) with a locked flat sky ``sky`` (counts per pixel), one PSF (None: no convolution) or
     a live PSF model ``psf_model`` (:class:`LivePSF`, its free parameters first in the joint
-    vector), data / weight (1 / variance) / mask (True = ignored)."""
+    vector), data / weight (1 / variance) / mask (True = ignored).  ``graphs``: replay the
+    forward and the Jacobian from CUDA graphs captured at their first call."""
 
     def __init__(self, nx: int, ny: int, sources: List[SceneSource], psf: Optional[np.ndarray], data, weight,
                  mask=None, sky: float = 0.0, scale: float = 1.0, options: Optional[dict] = None,
