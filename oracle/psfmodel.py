@@ -58,18 +58,21 @@ def render_psf(params: Dict[str, float], shape, scale: float = 1.0, grad: bool =
 
 class LivePSFProblem:
     """One galaxy (``psf_mode`` "full") with a live Moffat or Gaussian PSF (``psf_kind``) on
-    ``window``, against data ``Y`` with weights ``W``."""
+    ``window``, against data ``Y`` with weights ``W``; ``sky`` (counts per pixel) is a locked
+    flat sky of the same group (``Group_Model`` of the galaxy and a ``Flat_Sky``,
+    models/group_model_object.py:183-231, flatsky_model.py:53-55)."""
 
     def __init__(self, galaxy: Component, window: Window, psf_params: Dict[str, float], psf_shape,
                  Y: np.ndarray, W: Optional[np.ndarray] = None, psf_scale: float = 1.0,
                  psf_free: Optional[Sequence[str]] = None, mask: Optional[np.ndarray] = None,
-                 psf_kind: str = "moffat"):
+                 psf_kind: str = "moffat", sky: float = 0.0):
         self.galaxy = copy.deepcopy(galaxy)
         self.window = window
         self.psf_params = {k: float(v) for k, v in psf_params.items()}
         self.psf_shape = tuple(psf_shape)
         self.psf_scale = float(psf_scale)
         self.psf_kind = psf_kind
+        self.sky = float(sky)
         self.psf_free = tuple(DEFAULT_FREE[psf_kind] if psf_free is None else psf_free)
         self.Y, self.W, self.mask = Y, W, mask
         self.slots = [("psf", name, 0) for name in self.psf_free] + [("gal", name, k)
@@ -108,7 +111,7 @@ class LivePSFProblem:
     def forward(self, rep):
         self.set_representation(rep)
         K, _ = self.psf_image()
-        return sample_component(self.galaxy, self.window, PSF(K, self.psf_scale)).model.reshape(-1)
+        return sample_component(self.galaxy, self.window, PSF(K, self.psf_scale)).model.reshape(-1) + self.sky
 
     def jacobian_values(self):
         K, dK = self.psf_image(grad=True)

@@ -722,6 +722,37 @@ def run_init_case(ap, key, case):
     return out
 
 
+def run_auxpsf_group_case(ap, key, case):
+    """A group of the live-PSF galaxy and a locked flat sky (10^0 per pixel), psf_mode "full"."""
+    size, k = case["size"], case["psf_size"]
+    psf_target = ap.image.PSF_Image(data=np.ones((k, k)) / k**2, pixelscale=1.0)
+
+    def group_of(target, vals, tag):
+        live, gal = build_auxpsf(ap, target, psf_target, vals, tag)
+        sky = ap.models.AstroPhot_Model(name=f"sky {tag}", model_type="flat sky model", target=target,
+                                        parameters={"F": {"value": 0.0, "locked": True}})
+        sky.initialize()
+        grp = ap.models.AstroPhot_Model(name=f"group {tag}", model_type="group model", target=target,
+                                        models=[gal, sky], psf_mode="full")
+        return live, grp
+
+    blank = ap.image.Target_Image(data=np.zeros((size, size)), pixelscale=1.0)
+    _, grp_t = group_of(blank, case["truth"], f"truth {key}")
+    truth_img = grp_t().data.detach().cpu().numpy()
+    data, weight = synthetic.add_noise(truth_img, case["seed"])
+    target = ap.image.Target_Image(data=data, pixelscale=1.0, variance=1.0 / weight)
+    live, grp = group_of(target, case["init"], f"fit {key}")
+    names = [str(v) for v in grp.parameters.vector_names()]
+    model0 = grp().data.detach().cpu().numpy()
+    J_rep = grp.jacobian(as_representation=True).data.detach().cpu().numpy()
+    rep0 = grp.parameters.vector_representation().detach().cpu().numpy().copy()
+    res = ap.fit.LM(grp, initial_state=rep0).fit()
+    return dict(names=np.array(names), truth_model=truth_img, data=data, weight=weight, model0=model0,
+                jac_rep=J_rep, rep0=rep0, loss_history=np.array(res.loss_history), res=np.array(res.res()),
+                final_values=grp.parameters.vector_values().detach().cpu().numpy(), message=np.array(res.message),
+                spec=json.dumps(case))
+
+
 def main():
     ap = import_reference()
     only = sys.argv[1] if len(sys.argv) > 1 else None
@@ -730,6 +761,10 @@ def main():
             out = run_auxpsf_case(ap, key, case)
             np.savez_compressed(os.path.join(HERE, f"{key}.npz"), **out)
             print("auxpsf", key, out["names"], out["loss_history"], str(out["message"]), out["final_values"])
+        key = "auxpsf_group_48"
+        out = run_auxpsf_group_case(ap, key, dict(AUXPSF_CASES["auxpsf_48"], seed=23))
+        np.savez_compressed(os.path.join(HERE, f"{key}.npz"), **out)
+        print("auxpsf group", key, out["names"], out["loss_history"], str(out["message"]), out["final_values"])
         return
     for key, case in (INIT_CASES if only != "segmap" else {}).items():
         out = run_init_case(ap, key, case)

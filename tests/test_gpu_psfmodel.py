@@ -223,3 +223,38 @@ def test_adjoint_with_live_psf_matches_reference_jacobian(case):
     nll.backward()
     gref = np.einsum("yxk,yx->k", d["jac_rep"], d["weight"] * (d["model0"] - d["data"]))
     assert np.max(np.abs(vec.grad.numpy() - gref)) <= 1e-3 * np.max(np.abs(gref)), (vec.grad.numpy(), gref)
+
+
+def test_api_group_with_live_psf_and_sky_fits_like_reference():
+    """``auxpsf_group_48``: Group_Model([galaxy with psf= a moffat psf model, locked flat sky],
+    psf_mode="full") through the drop-in API: model, Jacobian (the PSF's n and Rd first) and
+    ``LM(group).fit()`` against the reference's own."""
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA GPU")
+    import astrophot_gb300 as ap
+
+    d = np.load(os.path.join(GOLDEN, "auxpsf_group_48.npz"))
+    spec = json.loads(str(d["spec"]))
+    ini = spec["init"]
+    k = spec["psf_size"]
+    psf_t = ap.image.PSF_Image(data=np.ones((k, k)) / k**2, pixelscale=1.0)
+    tgt = ap.image.Target_Image(data=d["data"], pixelscale=1.0, variance=1.0 / d["weight"])
+    live = ap.models.AstroPhot_Model(name="grp psf", model_type="moffat psf model", target=psf_t,
+                                     parameters=dict(ini["psf"]))
+    cx, cy, q, PA, n, Re, Ie = ini["gal"]
+    gal = ap.models.AstroPhot_Model(name="grp gal", model_type="sersic galaxy model", target=tgt, psf_mode="full",
+                                    psf=live, parameters={"center": [cx, cy], "q": q, "PA": PA, "n": n, "Re": Re,
+                                                          "Ie": Ie})
+    sky = ap.models.AstroPhot_Model(name="grp sky", model_type="flat sky model", target=tgt,
+                                    parameters={"F": {"value": 0.0, "locked": True}})
+    sky.initialize()
+    grp = ap.models.AstroPhot_Model(name="grp", model_type="group model", target=tgt, models=[gal, sky],
+                                    psf_mode="full")
+    assert [str(x) for x in grp.parameters.vector_names()] == [str(x) for x in d["names"]]
+    img = grp().data.numpy()
+    assert np.max(np.abs(img - d["model0"])) <= 1e-5 * np.max(d["model0"])
+    J = grp.jacobian(as_representation=True).data.numpy()
+    assert np.max(np.abs(J - d["jac_rep"])) <= 2e-4 * np.max(np.abs(d["jac_rep"]))
+    res = ap.fit.LM(grp).fit()
+    assert res.message == str(d["message"])
+    assert np.allclose(grp.parameters.vector_values().numpy(), d["final_values"], rtol=2e-3, atol=2e-3)

@@ -95,3 +95,27 @@ def test_api_vector_order_puts_the_live_psf_first(case):
     assert np.allclose(gal.parameters.vector_representation().numpy(), d["rep0"], atol=1e-12)
     first = "n" if kind_of(spec) == "moffat" else "sigma"
     assert isinstance(gal.psf, ap.models.PSF_Model) and torch.is_tensor(gal["order psf"][first].value)
+
+
+def test_oracle_group_with_live_psf_and_sky_matches_reference():
+    """``auxpsf_group_48``: a Group_Model of the live-PSF galaxy and a locked flat sky (1 count
+    per pixel): the PSF parameters still lead the group's vector; model, Jacobian and LM."""
+    d = np.load(os.path.join(GOLDEN, "auxpsf_group_48.npz"))
+    spec = json.loads(str(d["spec"]))
+    ini = spec["init"]
+    cx, cy, q, PA, n, Re, Ie = ini["gal"]
+    gal = Component("sersic", {"center": [cx, cy], "q": q, "PA": PA, "n": n, "Re": Re, "Ie": Ie}, psf_mode="full")
+    size, k = spec["size"], spec["psf_size"]
+    pr = LivePSFProblem(gal, Window.from_scale(size, size), psf_params(spec, "init"), (k, k), d["data"],
+                        d["weight"], sky=1.0)
+    assert [str(x) for x in d["names"]] == ["n", "Rd", "center:0", "center:1", "q", "PA", "n", "Re", "Ie"]
+    assert np.allclose(pr.representation(), d["rep0"], rtol=0, atol=1e-12)
+    m = pr.forward(d["rep0"]).reshape(d["model0"].shape)
+    assert np.max(np.abs(m - d["model0"])) <= 1e-12 * np.max(d["model0"])
+    J = pr.jacobian(d["rep0"]).reshape(d["jac_rep"].shape)
+    assert np.max(np.abs(J - d["jac_rep"])) <= 1e-10 * np.max(np.abs(d["jac_rep"]))
+    lm = LMOracle(pr, initial_state=d["rep0"].copy())
+    lm.fit()
+    assert lm.message == str(d["message"])
+    assert np.allclose(lm.loss_history, d["loss_history"], rtol=1e-10, atol=0)
+    assert np.allclose(pr.values(), d["final_values"], rtol=1e-8, atol=1e-10)
