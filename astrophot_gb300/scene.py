@@ -19,7 +19,8 @@ the damping search, geodesic right-hand side, curvature test, convergence rules 
 
 Every evaluation stages its parameters (all renders' value rows, a live PSF's row) in one
 host-to-device copy; the forward and the Jacobian then read device memory only, so each is
-captured once as a CUDA graph and replayed (``graphs=False``: launched one by one).  The LM's
+captured as a CUDA graph at its second call and replayed (``graphs=False``: launched one by
+one).  The LM's
 geodesic-term solve reuses the Cholesky factor of its step solve (``ap_dense_factored_solve``).
 
 A scene's PSF may be a live Moffat PSF model (``set_aux_psf``, models/model_object.py:133-149)
@@ -168,7 +169,7 @@ class Scene:
     origin) with a locked flat sky ``sky`` (counts per pixel), one PSF (None: no convolution) or
     a live PSF model ``psf_model`` (:class:`LivePSF`, its free parameters first in the joint
     vector), data / weight (1 / variance) / mask (True = ignored).  ``graphs``: replay the
-    forward and the Jacobian from CUDA graphs captured at their first call."""
+    forward and the Jacobian from CUDA graphs captured at their second call."""
 
     def __init__(self, nx: int, ny: int, sources: List[SceneSource], psf: Optional[np.ndarray], data, weight,
                  mask=None, sky: float = 0.0, scale: float = 1.0, options: Optional[dict] = None,
@@ -313,7 +314,7 @@ class Scene:
             psf_model.row_d = self._stage_d[self._psf_row : self._psf_row + 1]
         self._img = torch.empty(self.nx * self.ny, dtype=torch.float32, device=dev)
         self.use_graphs = bool(graphs)
-        self._graphs, self._graph_failed = {}, set()
+        self._graphs, self._graph_failed, self._graph_calls = {}, set(), {}
 
         # ---- source descriptors (+ one whole-image entry carrying the live PSF columns) --------
         ns = len(self.sources)
@@ -468,27 +469,25 @@ class Scene:
         return dK
 
     def _run(self, key, body):
-        """``body()`` (device work only, reading staged parameters), replayed from a CUDA graph
-        captured at its first call when graphs are on; eager if the capture fails."""
-        if not self.use_graphs or key in self._graph_failed:
+        """``body()`` (device work only, reading staged parameters): eager at its first call,
+        captured as a CUDA graph at its second and replayed from then on when graphs are on;
+        eager for good if the capture fails."""
+        calls = self._graph_calls.get(key, 0) + 1
+        self._graph_calls[key] = calls
+        if not self.use_graphs or key in self._graph_failed or calls < 2:
             body()
             return
         g = self._graphs.get(key)
         if g is None:
-            side = torch.cuda.Stream(device=self.device)
-            side.wait_stream(torch.cuda.current_stream())
-            with torch.cuda.stream(side):
-                body()  # this call's result, and the allocations the capture reuses
-            torch.cuda.current_stream().wait_stream(side)
             g = torch.cuda.CUDAGraph()
             try:
                 with torch.cuda.graph(g, capture_error_mode="thread_local"):
                     body()
             except Exception:
                 self._graph_failed.add(key)
+                body()
                 return
             self._graphs[key] = g
-            return
         g.replay()
 
     # ---- device primitives -----------------------------------------------------------------
