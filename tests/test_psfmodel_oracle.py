@@ -119,3 +119,23 @@ def test_oracle_group_with_live_psf_and_sky_matches_reference():
     assert lm.message == str(d["message"])
     assert np.allclose(lm.loss_history, d["loss_history"], rtol=1e-10, atol=0)
     assert np.allclose(pr.values(), d["final_values"], rtol=1e-8, atol=1e-10)
+
+
+def test_live_psf_limits_and_maps_equal_the_oracle():
+    """Host logic: the live PSF's limits and value <-> representation maps (scene.py) are the
+    oracle's for each PSF kind (Moffat n in (0.1, 10), Rd and sigma in (0, inf))."""
+    pytest.importorskip("torch")
+    from astrophot_gb300 import scene
+    from astrophot_gb300.transforms import drep_dvalue, to_rep, to_value
+    from oracle import render as R
+
+    vals = {"n": [0.15, 1.0, 2.5, 9.5], "Rd": [0.3, 2.0, 11.0], "I0": [-1.0, 0.0, 2.0], "sigma": [0.4, 1.6, 7.0],
+            "flux": [-0.5, 0.0, 1.5]}
+    for kind, limits in scene.PSF_MODEL_LIMITS.items():
+        for name, (lim, cyc) in limits.items():
+            assert (lim, cyc) == R._spec(name, kind), (kind, name)
+            for v in vals[name]:
+                r = to_rep(lim, cyc, v)
+                assert np.isclose(r, R.value_to_rep(name, v, kind), rtol=1e-14, atol=1e-14)
+                assert np.isclose(to_value(lim, cyc, r), v, rtol=1e-13, atol=1e-13)
+                assert np.isclose(drep_dvalue(lim, cyc, r), R.drep_dvalue(name, r, kind), rtol=1e-14, atol=1e-14)
