@@ -93,6 +93,7 @@ class ApLMOptions(ctypes.Structure):
         ("acceleration", ctypes.c_double),
         ("rounds_per_sync", ctypes.c_int32),
         ("use_graph", ctypes.c_int32),
+        ("precise_trials", ctypes.c_int32),
     ]
 
 
@@ -298,6 +299,7 @@ def make_lm_options(
     acceleration=0.0,
     rounds_per_sync=4,
     use_graph=True,
+    precise_trials=True,
 ) -> ApLMOptions:
     o = ApLMOptions()
     o.max_iter = int(max_iter)
@@ -310,6 +312,7 @@ def make_lm_options(
     o.acceleration = float(acceleration)
     o.rounds_per_sync = int(rounds_per_sync)
     o.use_graph = 1 if use_graph else 0
+    o.precise_trials = 1 if precise_trials else 0
     return o
 
 

@@ -782,7 +782,8 @@ int ap_damped_solve(int32_t m, int32_t p, const double* hess, const double* grad
 // ---------------------------------------------------------------------------
 namespace {
 struct LMLayout {
-  int64_t st, params_next, ops_next, hvec, y0, jbase, hist_loss, hist_L, hist_x, active, total;
+  int64_t st, params_next, ops_next, hvec, y0, jbase, base_eval, base_psf, base_deep, base_code, hist_loss, hist_L,
+      hist_x, active, total;
 };
 
 LMLayout lm_layout(const ap_batch* b, const ap_lm_options* lm) {
@@ -800,6 +801,11 @@ LMLayout lm_layout(const ap_batch* b, const ap_lm_options* lm) {
   L.hvec = take(sizeof(double) * n * NPARAM);
   L.y0 = take(sizeof(float) * b->out_pixels);
   L.jbase = take(sizeof(float) * std::max<int64_t>(1, b->args.n_free) * b->out_pixels);
+  // base point of the difference trials: evaluation constants, kernel, deep image, pattern
+  L.base_eval = take(sizeof(EvalDev) * n);
+  L.base_psf = take(sizeof(float) * n * std::max<int64_t>(1, b->max_kp2));
+  L.base_deep = take(sizeof(float) * b->work_pixels);
+  L.base_code = take(sizeof(uint32_t) * b->work_pixels);
   L.hist_loss = take(sizeof(double) * n * H);
   L.hist_L = take(sizeof(double) * n * H);
   L.hist_x = take(sizeof(double) * n * H * NPARAM);
@@ -844,6 +850,7 @@ int ap_lm_fit(ap_batch* b, const float* data, const float* weight, const uint8_t
   LMArgs a{};
   a.max_iter = lm->max_iter;
   a.max_step_iter = lm->max_step_iter;
+  a.precise = lm->precise_trials ? 1 : 0;
   a.rel_tol = lm->relative_tolerance;
   a.curvature_limit = lm->curvature_limit;
   a.Lup = lm->Lup;
@@ -875,9 +882,17 @@ int ap_lm_fit(ap_batch* b, const float* data, const float* weight, const uint8_t
   io.hvec = a.hvec;
   io.rpp_d = 0.1;
 
+  // the batch's arguments with the LM's base buffers (kept out of b->args: the other entry
+  // points render without them)
+  BatchArgs A = b->args;
+  A.base_eval = (EvalDev*)(w + L.base_eval);
+  A.base_psf = (float*)(w + L.base_psf);
+  A.base_deep = (float*)(w + L.base_deep);
+  A.base_code = (uint32_t*)(w + L.base_code);
+
   rc = check_cuda(cudaMemsetAsync(w + L.hist_loss, 0, L.active - L.hist_loss, s));
   if (rc) return rc;
-  rc = check_cuda(launch_lm_init(b->args, a, state, mask, s));
+  rc = check_cuda(launch_lm_init(A, a, state, mask, s));
   if (rc) return rc;
 
   Profiler* P = &b->prof;
@@ -888,15 +903,15 @@ int ap_lm_fit(ap_batch* b, const float* data, const float* weight, const uint8_t
   }
   auto one_round = [&](cudaStream_t st) -> cudaError_t {
     int t = P->on ? P->begin(KC_SETUP, st) : -1;
-    cudaError_t e = launch_eval_setup(b->args, a.params_next, 2 * NPARAM, NPARAM, a.ops_next, 0, st);
+    cudaError_t e = launch_eval_setup(A, a.params_next, 2 * NPARAM, NPARAM, a.ops_next, 0, st);
     if (t >= 0) P->end(t, st);
     if (e != cudaSuccess) return e;
-    e = launch_render_pass(b->args, io, b->conv_smem, true, st, P);
+    e = launch_render_pass(A, io, b->conv_smem, true, st, P);
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(a.active_count, 0, sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
     t = P->on ? P->begin(KC_LM, st) : -1;
-    e = launch_lm_update(b->args, a, st);
+    e = launch_lm_update(A, a, st);
     if (t >= 0) P->end(t, st);
     return e;
   };
@@ -942,7 +957,7 @@ int ap_lm_fit(ap_batch* b, const float* data, const float* weight, const uint8_t
   if (exec) cudaGraphExecDestroy(exec);
   if (graph) cudaGraphDestroy(graph);
   if (rc) return rc;
-  rc = check_cuda(launch_lm_finish(b->args, a, s));
+  rc = check_cuda(launch_lm_finish(A, a, s));
   b->stats[3] = rounds;
   b->hist_loss = a.hist_loss;
   b->hist_L = a.hist_L;

@@ -58,6 +58,11 @@ enum EvalOps : int32_t {
   OP_REP = 128,        // chain Jacobian columns to representation space
   OP_VJP = 256,        // accumulate sum_pixels g * d model / d theta (adjoint of the render)
   OP_VJP_COORD = 512,  // VJP in shift mode: add the sampling-coordinate path to the center
+  OP_BASE = 1024,      // keep this evaluation (constants, kernel, deep image, integration
+                       // pattern) as the base of later OP_DIFF evaluations of the stamp
+  OP_DIFF = 2048,      // render the difference to the stamp's base evaluation: the deep
+                       // difference (plane 1), convolved as K1 * dS + dK * S0; OP_CHI2 then
+                       // accumulates sum W dm (dm - 2 (y - y0)) and OP_RPP uses dm
 };
 
 struct QuadTables {
@@ -134,6 +139,14 @@ struct EvalDev {
   double amp64, bn64, c64, s64;
   double invq64, invRe64, invn64;  // reciprocals for the float64 re-decisions
   float drep[NPARAM]; // d value / d representation
+  // OP_DIFF: differences of this evaluation's constants to the stamp's base evaluation,
+  // computed in float64 without cancellation, stored FP32 (see eval_profile_delta)
+  float d_c, d_s, d_invq, d_lnire, d_invn, d_bn, d_lnamp, d_X, d_Y, d_sky;
+};
+
+// The OP_DIFF constants in registers.
+struct DeltaF {
+  float c, s, invq, lnire, invn, bn, lnamp, X, Y;
 };
 
 // The FP32 constants of one evaluation, held in registers by the pixel kernels (read once
@@ -205,7 +218,25 @@ struct BatchArgs {
   const int32_t* fft_out_pre; // [n_fft + 1] output row blocks
   float2* fft_buf;
   float* preconv;
+  // base of OP_DIFF evaluations (the LM's current point; null outside the LM): its
+  // evaluation constants, shifted kernel, deep image and integration pattern per working pixel
+  EvalDev* base_eval;         // [n_stamps]
+  float* base_psf;            // [n_stamps][max_kp2]
+  float* base_deep;           // [work_pixels]
+  uint32_t* base_code;        // [work_pixels]
 };
+
+// Stamps whose trials the LM renders as differences to the base point: the Sersic and
+// exponential profiles (direct, FFT or no convolution).
+__host__ __device__ inline bool diff_capable(const BatchArgs& b, const StampDev&) {
+  return b.kind == AP_PROFILE_SERSIC || b.kind == AP_PROFILE_EXPONENTIAL;
+}
+
+// Integration pattern of a working pixel: 0 midpoint only, 1 level 1 (one Q x Q quadrature),
+// 2 | (sub-pixels refined to level 3) << 2 for a pixel split at level 2.  Two evaluations of a
+// pixel with the same pattern use the same sample positions.
+constexpr uint32_t kCodeLevel1 = 1u;
+__device__ __forceinline__ uint32_t code_split(unsigned level3_mask) { return 2u | (level3_mask << 2); }
 
 // buffers of the convolve/accumulate pass
 struct ConvIO {
@@ -332,6 +363,89 @@ __device__ __forceinline__ Sample eval_profile(const EvalF& e, int kind, float X
     out.g[GY] = dIdR * ((-Xr * e.s + Yr * e.c * e.invq) * invR);
   }
   return out;
+}
+
+// Value of one Sersic / exponential sample (the same FP32 operations as eval_profile, so the
+// integration decisions do not change) and its difference to the base evaluation,
+// dI = I1 - I0, formed without cancellation: every difference below is built from the
+// float64 parameter differences of k_eval_setup (DeltaF) and the p1 intermediates, never by
+// subtracting two rounded values, so dI keeps a relative error of a few 1e-7 however small
+// the step.  With X, Y the sample's plane offsets at p1 and X0 = X - dX:
+//   Xr = c X - s Y,  Yr = (s X + c Y) / q,  R^2 = Xr^2 + Yr^2 + eps^2,  u = R / Re,
+//   t = u^(1/n),  ln I = ln amp - b (t - 1)   (exponential: t = u, b fixed)
+//   d(R^2) = dXr (Xr1 + Xr0) + dYr (Yr1 + Yr0),  d ln u = log1p(d(R^2) / R0^2) / 2 + d ln(1/Re)
+//   d ln t = d ln u / n1 + ln u0 d(1/n),  dt = -t1 expm1(-d ln t),  d arg = db (t1 - 1) + b0 dt
+//   dI = -I1 expm1(-(d ln amp - d arg))
+// log1p / expm1 of the difference arithmetic, from their series: below |x| = 1/2,
+// log1p(x) = 2 atanh(u) = 2 (u + u^3/3 + ... + u^11/11) with u = x / (2 + x) (|u| <= 1/3: the
+// truncation, about u^13/13, stays below 2e-7 relative there and below 1e-15 for |x| < 1/32), and
+// expm1 by its Taylor series to x^9 (truncation below 3e-10); beyond, the MUFU log / exp,
+// whose absolute error of ~2e-7 is below 5e-7 of log1p and expm1 there.
+__device__ __forceinline__ float d_log1p(float x) {
+  if (fabsf(x) < 0.5f) {
+    const float u = __fdividef(x, 2.f + x), u2 = u * u;
+    return 2.f * u * (1.f + u2 * (0.33333334f + u2 * (0.2f + u2 * (0.14285715f + u2 * (0.11111111f + u2 * 0.09090909f)))));
+  }
+  return __logf(1.f + x);
+}
+
+__device__ __forceinline__ float d_expm1(float x) {
+  if (fabsf(x) < 0.5f)
+    return x * (1.f + x * (0.5f + x * (0.16666667f + x * (0.041666668f + x * (0.008333334f + x * (1.3888889e-3f +
+               x * (1.984127e-4f + x * (2.4801588e-5f + x * 2.7557319e-6f))))))));
+  return __expf(x) - 1.f;
+}
+
+__device__ __forceinline__ Sample eval_profile_delta(const EvalF& e, const DeltaF& d, int kind, float X,
+                                                     float Y, float area_scale, float& dI) {
+  Sample out;
+  const float Xr = e.c * X - e.s * Y;
+  const float Yr0 = e.s * X + e.c * Y;
+  const float Yr = Yr0 * e.invq;
+  const float R2 = fmaf(Xr, Xr, fmaf(Yr, Yr, e.soft2));
+  const float R = sqrtf(R2);
+  const float u = R * e.invRe;
+  const float amp = e.amp * area_scale;
+  float t = u, lu2 = 0.f;
+  if (kind == AP_PROFILE_SERSIC) {
+    lu2 = __log2f(u);
+    t = exp2f(lu2 * e.invn);
+  }
+  const float arg = e.bn * (t - 1.f);
+  const float I = amp * __expf(-arg);
+  out.v = I;
+  out.arg = arg;
+  const float c0 = e.c - d.c, s0 = e.s - d.s;
+  const float dXr = d.c * X + c0 * d.X - (d.s * Y + s0 * d.Y);
+  const float dYr0 = d.s * X + s0 * d.X + (d.c * Y + c0 * d.Y);
+  const float dYr = dYr0 * e.invq + (Yr0 - dYr0) * d.invq;
+  const float dR2 = dXr * (2.f * Xr - dXr) + dYr * (2.f * Yr - dYr);
+  const float dlnu = 0.5f * d_log1p(__fdividef(dR2, R2 - dR2)) + d.lnire;
+  float darg;
+  if (kind == AP_PROFILE_SERSIC) {
+    const float lnu1 = lu2 * 0.6931471805599453f;
+    const float dlnt = dlnu * e.invn + (lnu1 - dlnu) * d.invn;
+    const float dt = -t * d_expm1(-dlnt);
+    darg = d.bn * (t - 1.f) + (e.bn - d.bn) * dt;
+  } else {
+    darg = e.bn * (-u * d_expm1(-dlnu));
+  }
+  dI = -I * d_expm1(darg - d.lnamp);
+  return out;
+}
+
+__device__ __forceinline__ DeltaF load_deltaf(const EvalDev& e) {
+  DeltaF d;
+  d.c = __ldg(&e.d_c);
+  d.s = __ldg(&e.d_s);
+  d.invq = __ldg(&e.d_invq);
+  d.lnire = __ldg(&e.d_lnire);
+  d.invn = __ldg(&e.d_invn);
+  d.bn = __ldg(&e.d_bn);
+  d.lnamp = __ldg(&e.d_lnamp);
+  d.X = __ldg(&e.d_X);
+  d.Y = __ldg(&e.d_Y);
+  return d;
 }
 
 // float64 value, same operation order as the reference.

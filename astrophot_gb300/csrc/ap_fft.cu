@@ -11,7 +11,9 @@
 // into K^ and dK/dsx^.  Buffers per (stamp, slot): K0 = K + i dKx, K1 = dKy, D = deep plane,
 // P1..P3 = pairs of partial planes.  The convolved planes land in `preconv`, from which the
 // convolve pass takes them instead of convolving directly (same Jacobian chain, chi^2 and
-// accumulations afterwards).
+// accumulations afterwards).  A difference evaluation (OP_DIFF) transforms K1, dK, dS and the
+// base's deep image S0 each on its own and returns the inverse of dS^ K1^ + S0^ dK^: a small
+// difference never shares a transform with a large array, whose rounding it would take on.
 //
 // Transforms are radix-2, decimation in time, in shared memory after a bit-reversed load: one
 // CTA per transform row (every active buffer of both evaluation slots in turn; the inputs are
@@ -34,7 +36,7 @@ enum FftBuf { FB_K0 = 0, FB_K1 = 1, FB_D = 2, FB_P1 = 3 };
 __constant__ float2 c_tw[kFftMaxSide / 2];  // exp(-2 pi i m / kFftMaxSide), m < kFftMaxSide / 2
 
 struct FftUse {
-  bool jac, shift;
+  bool jac, shift, diff;
   int npart;
   int part[NGRAD];
   unsigned fwd;  // buffers transformed forward
@@ -45,7 +47,17 @@ __device__ FftUse fft_use(const BatchArgs& b, int ops) {
   FftUse u;
   u.jac = (ops & OP_JAC) != 0;
   u.shift = b.psf_mode == AP_PSF_FULL;
+  u.diff = (ops & OP_DIFF) != 0;
   u.npart = 0;
+  if (u.diff) {
+    // four real transforms, none paired (a small difference sharing a transform with a large
+    // array would take on the large one's rounding): K0 <- K1, K1 <- dK, D <- dS, P1 <- S0 (the
+    // base's deep image); D <- dS^ K1^ + S0^ dK^, whose inverse is the model difference
+    u.fwd = (1u << FB_K0) | (1u << FB_D);
+    if (u.shift) u.fwd |= (1u << FB_K1) | (1u << FB_P1);
+    u.inv = 1u << FB_D;
+    return u;
+  }
   if (u.jac) {
     for (int q = 0; q < NGRAD; ++q) {
       if (u.shift && !(ops & OP_VJP_COORD) && (q == GX || q == GY)) continue;
@@ -117,11 +129,13 @@ __device__ __forceinline__ float2 fft_input(const BatchArgs& b, const StampDev& 
     if (v >= st.kpy || uu >= st.kpx) return make_float2(0.f, 0.f);
     const int kp2 = st.kpx * st.kpy, ki = v * st.kpx + uu;
     const float* ksrc = b.spsf + st.spsf_off + (int64_t)slot * 3 * kp2;
-    if (k == FB_K1) return make_float2(ksrc[2 * kp2 + ki], 0.f);
+    if (k == FB_K1) return make_float2(ksrc[(u.diff ? 1 : 2) * kp2 + ki], 0.f);
     return make_float2(ksrc[ki], (u.jac && u.shift) ? ksrc[kp2 + ki] : 0.f);
   }
   if (y >= st.wny || x >= st.wnx) return make_float2(0.f, 0.f);
-  const float* w = b.work + st.work_off + (int64_t)y * st.wnx + x;
+  const int64_t wi = st.work_off + (int64_t)y * st.wnx + x;
+  const float* w = b.work + wi;
+  if (u.diff) return make_float2(k == FB_D ? w[work_plane(b, slot, 1)] : b.base_deep[wi], 0.f);
   if (k == FB_D) return make_float2(w[work_plane(b, slot, 0)], 0.f);
   const int p = k - FB_P1;
   const int qa = u.part[2 * p];
@@ -228,6 +242,15 @@ __global__ void __launch_bounds__(kFftThreads) k_fft_mul(BatchArgs b) {
       const int y = y0 + r;
       const int64_t i = (int64_t)y * Nx + x;
       const float2 z = K0[i];
+      if (u.diff) {
+        float2 r = cmul(D[i], z);
+        if (u.shift) {
+          const float2 c = cmul(fft_buffer(b, st, slot, FB_P1)[i], K1[i]);
+          r = make_float2(r.x + c.x, r.y + c.y);
+        }
+        D[i] = r;
+        continue;
+      }
       float2 FK = z, FX = make_float2(0.f, 0.f);
       if (two_k) {
         const float2 zm = K0[(int64_t)((Ny - y) % Ny) * Nx + (Nx - x) % Nx];

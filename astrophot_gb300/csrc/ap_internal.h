@@ -23,6 +23,8 @@ struct LMState {
   double init_chi2;
   double ndf;
   double best_chi2, best_L, scarry_chi2, scarry_L;
+  double anchor_err;  // error bound of chi2_cur accumulated from trial differences since it was
+                      // last taken from a full render
   double x[NPARAM], h[NPARAM], a[NPARAM], ha[NPARAM];
   double best_ha[NPARAM], scarry_ha[NPARAM];
   double H[NPARAM * NPARAM], g[NPARAM];
@@ -32,6 +34,7 @@ enum LMPhase { LM_PH_INIT = 0, LM_PH_JAC = 1, LM_PH_SUB = 2, LM_PH_SUB2 = 3, LM_
 
 struct LMArgs {
   int32_t max_iter, max_step_iter;
+  int32_t precise;         // trials rendered as differences to the step's base point (OP_DIFF)
   double rel_tol, curvature_limit, Lup, Ldn, L0, acceleration;
   LMState* st;             // [n]
   double* params_next;     // [n][2][8]  value space

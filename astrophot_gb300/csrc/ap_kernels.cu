@@ -73,7 +73,9 @@ __global__ void k_eval_setup(BatchArgs b, const double* params, int64_t stamp_st
     b.counters[7] = 0;  // active working tiles
     b.counters[8] = 0;  // active output tiles
     b.counters[9] = 0;  // active (stamp, slot) pairs
-    b.counters[10] = 0; // level-2 integration queue length
+    b.counters[10] = 0; // level-2 integration list of Jacobian evaluations (front of recheck)
+    b.counters[13] = 0; // level-2 integration list of forward evaluations (back of recheck)
+    b.counters[14] = 0; // its head
     b.counters[11] = 0; // convolve-pass tile head
     b.counters[12] = 0; // level-1 float64 decisions
   }
@@ -81,10 +83,13 @@ __global__ void k_eval_setup(BatchArgs b, const double* params, int64_t stamp_st
   const int s = t >> 1, slot = t & 1;
   EvalDev& e = b.evals[t];
   b.mean_acc[t] = 0.0;
-  const int32_t op = ops ? ops[t] : (slot == 0 ? ops_uniform : 0);
+  int32_t op = ops ? ops[t] : (slot == 0 ? ops_uniform : 0);
+  const StampDev& st = b.stamps[s];
+  // (OP_BASE and OP_DIFF need the LM's base buffers; OP_DIFF also a direct-convolution stamp)
+  if ((op & OP_BASE) && !b.base_eval) op &= ~OP_BASE;
+  if ((op & OP_DIFF) && !(b.base_eval && diff_capable(b, st))) op &= ~OP_DIFF;
   e.ops = op;
   if (!op) return;
-  const StampDev& st = b.stamps[s];
   const double* v = params + s * stamp_stride + slot * slot_stride;
   for (int i = 0; i < NPARAM; ++i) e.v[i] = v[i];
   // centre in the working grid: plane_to_pixel (image/wcs.py:587-610) of the padded window
@@ -161,6 +166,39 @@ __global__ void k_eval_setup(BatchArgs b, const double* params, int64_t stamp_st
   }
   e.thresh = (float)e.thresh64;
   for (int i = 0; i < NPARAM; ++i) e.drep[i] = (float)drep_from_value(b.kind, i, v[i]);
+  if (op & OP_DIFF) {
+    // differences to the base evaluation, each formed without subtracting rounded values
+    const EvalDev& e0 = b.base_eval[s];
+    const double* v0 = e0.v;
+    // sample plane offsets X = P (ij - centre pixel - f): the centre moved by (dpx, dpy) pixels
+    const double dpx = (double)(e.cix - e0.cix) + (e.fx64 - e0.fx64);
+    const double dpy = (double)(e.cjy - e0.cjy) + (e.fy64 - e0.fy64);
+    e.d_X = (float)(-(st.P[0] * dpx + st.P[1] * dpy));
+    e.d_Y = (float)(-(st.P[2] * dpx + st.P[3] * dpy));
+    // cos / sin of theta = -(PA - pi/2) by the sum-to-product identities
+    const double th1 = -(v[PPA] - kPi / 2), th0 = -(v0[PPA] - kPi / 2);
+    const double hm = 0.5 * (th1 + th0), hd = sin(0.5 * (th1 - th0));
+    e.d_c = (float)(-2.0 * sin(hm) * hd);
+    e.d_s = (float)(2.0 * cos(hm) * hd);
+    e.d_invq = (float)((v0[PQ] - v[PQ]) / (v0[PQ] * v[PQ]));
+    e.d_lnire = (float)(-log1p((v[PRE] - v0[PRE]) / v0[PRE]));
+    if (b.kind == AP_PROFILE_SERSIC) {
+      // b(n) = 2n - 1/3 + sum_k a_k n^-k: powers of 1/n differenced as dy sum y1^j y0^(k-1-j)
+      const double n1 = v[PN], n0 = v0[PN];
+      const double y1 = 1.0 / n1, y0 = 1.0 / n0, dy = (n0 - n1) / (n0 * n1);
+      const double dy2 = dy * (y1 + y0), dy3 = dy * (y1 * y1 + y1 * y0 + y0 * y0);
+      const double dy4 = dy * (y1 * y1 * y1 + y1 * y1 * y0 + y1 * y0 * y0 + y0 * y0 * y0);
+      e.d_invn = (float)dy;
+      e.d_bn = (float)(2 * (n1 - n0) + 4.0 / 405.0 * dy + 46.0 / 25515.0 * dy2 + 131.0 / 1148175.0 * dy3 -
+                       2194697.0 / 30690717750.0 * dy4);
+    } else {
+      e.d_invn = 0.f;
+      e.d_bn = 0.f;
+    }
+    e.d_lnamp = (float)(kLn10 * (v[PIE] - v0[PIE]));
+    e.d_sky = b.has_sky ? (float)(st.pixel_area * pow(10.0, v0[PF]) * expm1(kLn10 * (v[PF] - v0[PF]))) : 0.f;
+  }
+  if (op & OP_BASE) b.base_eval[s] = e;
 }
 
 // Compacted work lists of this pass: the tiles of active (stamp, slot) pairs only, so the
@@ -231,6 +269,45 @@ __device__ __forceinline__ ShiftValF shifted_psf_at_f(const float* psf, int kx, 
   return r;
 }
 
+// Shifted value at shift s1 and its difference to the value at shift s0 (ds = s1 - s0 exact).
+// Inside one bilinear cell the value is bilinear in the shift, so the difference of each
+// weight product is expanded in ds; a tap whose cell differs between the shifts takes B1 - B0.
+__device__ __forceinline__ float2 shifted_psf_delta(const float* psf, int kx, int ky, int ix, int iy, float sx1,
+                                                    float sy1, float sx0, float sy0, float dsx, float dsy) {
+  const int w = kx + 2, h = ky + 2;
+  auto pad = [&](int r, int c) -> float {
+    const int rr = r - 1, cc = c - 1;
+    return (rr >= 0 && rr < ky && cc >= 0 && cc < kx) ? psf[rr * kx + cc] : 0.f;
+  };
+  auto cell = [](float x, int lim, int& c0, int& c1) {
+    c0 = (int)floorf(x);
+    c1 = c0 + 1;
+    c0 = min(max(c0, 0), lim - 2);
+    c1 = min(max(c1, 1), lim - 1);
+  };
+  const float x = (float)ix - sx1, y = (float)iy - sy1;
+  const float xb = (float)ix - sx0, yb = (float)iy - sy0;
+  int x0, x1, y0, y1, bx0, bx1, by0, by1;
+  cell(x, w, x0, x1);
+  cell(y, h, y0, y1);
+  cell(xb, w, bx0, bx1);
+  cell(yb, h, by0, by1);
+  const float fa = pad(y0, x0), fb = pad(y1, x0), fc = pad(y0, x1), fd = pad(y1, x1);
+  const float ax = (float)x1 - x, bx = x - (float)x0, ay = (float)y1 - y, by = y - (float)y0;
+  float2 r;
+  r.x = fa * (ax * ay) + fb * (ax * by) + fc * (bx * ay) + fd * (bx * by);
+  if (x0 == bx0 && y0 == by0) {
+    // base weights: ax - dsx, bx + dsx, ay - dsy, by + dsy
+    const float pxy = dsx * dsy;
+    const float d00 = ax * dsy + dsx * ay - pxy, d01 = -ax * dsy + dsx * by + pxy;
+    const float d10 = bx * dsy - dsx * ay + pxy, d11 = -bx * dsy - dsx * by - pxy;
+    r.y = fa * d00 + fb * d01 + fc * d10 + fd * d11;
+  } else {
+    r.y = r.x - shifted_psf_at_f(psf, kx, ky, ix, iy, sx0, sy0).v;
+  }
+  return r;
+}
+
 __device__ __forceinline__ double warp_sum_d(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
@@ -272,7 +349,29 @@ __device__ void psf_shift_warp(const BatchArgs& b, const float* psf, int s, int 
   const float* P = psf + st.psf_off;
   float* out = b.spsf + st.spsf_off + (int64_t)slot * 3 * kp2;
   const bool jac = (e.ops & OP_JAC) != 0;
-  if (b.psf_mode == AP_PSF_FULL) {
+  if (b.psf_mode == AP_PSF_FULL && (e.ops & OP_DIFF)) {
+    // K1 (kernel 0) and dK = K1 - K0 = (dB - K0 sum dB) / sum B1 (kernel 1), B the shifted
+    // unnormalised kernel and K0 the base's normalised one
+    const EvalDev& e0 = b.base_eval[s];
+    const float* K0 = b.base_psf + (int64_t)s * b.max_kp2;
+    const float sx1 = (float)e.shift[0], sy1 = (float)e.shift[1];
+    const float sx0 = (float)e0.shift[0], sy0 = (float)e0.shift[1];
+    const float dsx = (float)(e.shift[0] - e0.shift[0]), dsy = (float)(e.shift[1] - e0.shift[1]);
+    double S = 0, SD = 0;
+    for (int idx = lane; idx < kp2; idx += 32) {
+      const float2 r = shifted_psf_delta(P, st.kx, st.ky, idx % st.kpx, idx / st.kpx, sx1, sy1, sx0, sy0, dsx, dsy);
+      S += r.x;
+      SD += r.y;
+    }
+    S = warp_sum_d(S);
+    SD = warp_sum_d(SD);
+    const float inv = (float)(1.0 / S), c = (float)SD;
+    for (int idx = lane; idx < kp2; idx += 32) {
+      const float2 r = shifted_psf_delta(P, st.kx, st.ky, idx % st.kpx, idx / st.kpx, sx1, sy1, sx0, sy0, dsx, dsy);
+      out[idx] = r.x * inv;
+      out[kp2 + idx] = (r.y - K0[idx] * c) * inv;
+    }
+  } else if (b.psf_mode == AP_PSF_FULL) {
     const float sx = (float)e.shift[0], sy = (float)e.shift[1];
     double S = 0, Sx = 0, Sy = 0;
     for (int idx = lane; idx < kp2; idx += 32) {
@@ -292,6 +391,7 @@ __device__ void psf_shift_warp(const BatchArgs& b, const float* psf, int s, int 
         out[kp2 + idx] = r.dx * inv - r.v * cx;
         out[2 * kp2 + idx] = r.dy * inv - r.v * cy;
       }
+      if (e.ops & OP_BASE) b.base_psf[(int64_t)s * b.max_kp2 + idx] = r.v * inv;
     }
   } else {
     double S = 0;
@@ -319,12 +419,14 @@ __global__ void k_psf_shift(BatchArgs b, const float* psf, const float* psf_base
 // ---------------------------------------------------------------------------
 // sampling (_sample_init): deep value, partials, reference sub-sample, FP32 error bound
 // ---------------------------------------------------------------------------
-template <bool JAC, bool EXT>
-__device__ __forceinline__ void sample_pixel(const BatchArgs& b, const EvalF& e, int i, int j,
-                                             float& deep, float* g, float& refsub, float& errb) {
+// DIFF (forward only): also ddeep = the difference of deep to the base evaluation
+template <bool JAC, bool EXT, bool DIFF>
+__device__ __forceinline__ void sample_pixel(const BatchArgs& b, const EvalF& e, const DeltaF& d, int i, int j,
+                                             float& deep, float* g, float& refsub, float& errb, float& ddeep) {
   const QuadTables& T = *b.tables;
   const float di = (float)(i - e.cix), dj = (float)(j - e.cjy);
   deep = 0.f;
+  ddeep = 0.f;
 #pragma unroll
   for (int k = 0; k < NGRAD; ++k) g[k] = 0.f;
   float absb = 0.f, mag = 0.f;
@@ -333,9 +435,11 @@ __device__ __forceinline__ void sample_pixel(const BatchArgs& b, const EvalF& e,
   for (int k = 0; k < T.nsub; ++k) {
     float X, Y;
     pix_to_offset(e, di + T.sxf[k], dj + T.syf[k], X, Y);
-    const Sample sm = eval_profile<JAC, EXT>(e, b.kind, X, Y, 1.f);
+    float dI = 0.f;
+    const Sample sm = DIFF ? eval_profile_delta(e, d, b.kind, X, Y, 1.f, dI) : eval_profile<JAC, EXT>(e, b.kind, X, Y, 1.f);
     const float w = T.swf[k];
     deep = fmaf(w, sm.v, deep);
+    if (DIFF) ddeep = fmaf(w, dI, ddeep);
     if (JAC) {
 #pragma unroll
       for (int q = 0; q < NGRAD; ++q) g[q] = fmaf(w, sm.g[q], g[q]);
@@ -350,6 +454,19 @@ __device__ __forceinline__ void sample_pixel(const BatchArgs& b, const EvalF& e,
   }
   // bound on |deep_fp32 - deep_fp64| (+ the reference sub-sample's for simpsons / quad)
   errb = absb + 2.f * (float)T.nsub * kEps * mag + referr;
+}
+
+// Deep value of a working pixel that is final (not refined further): the base evaluation
+// keeps it with its integration pattern; a difference evaluation stores its difference to the
+// base, from the sample differences when the base integrated the pixel with the same pattern
+// (same sample positions), else as the plain difference of the two values.
+__device__ __forceinline__ void write_diff_base(const BatchArgs& b, int ops, int slot, int64_t wp, float v,
+                                                float dv, uint32_t code) {
+  if (ops & OP_DIFF) b.work[work_plane(b, slot, 1) + wp] = (b.base_code[wp] == code) ? dv : v - b.base_deep[wp];
+  if (ops & OP_BASE) {
+    b.base_deep[wp] = v;
+    b.base_code[wp] = code;
+  }
 }
 
 template <bool EXT>
@@ -368,8 +485,9 @@ __device__ double sample_pixel64(const BatchArgs& b, const StampDev& st, const E
   return deep;
 }
 
-template <bool JAC, bool EXT>
-__device__ void sample_tile(const BatchArgs& b, const EvalF& e, int s, int slot, int tile_local) {
+template <bool JAC, bool EXT, bool DIFF>
+__device__ void sample_tile(const BatchArgs& b, const EvalF& e, const DeltaF& d, int ops, int s, int slot,
+                            int tile_local) {
   const StampDev& st = b.stamps[s];
   const int tx = threadIdx.x & (kTile - 1), ty = threadIdx.x / kTile;
   const int i = (tile_local % st.ntw_x) * kTile + tx;
@@ -377,8 +495,8 @@ __device__ void sample_tile(const BatchArgs& b, const EvalF& e, int s, int slot,
   const bool valid = (i < st.wnx) && (j < st.wny);
   float deep = 0.f;
   if (valid) {
-    float g[NGRAD], refsub, errb;
-    sample_pixel<JAC, EXT>(b, e, i, j, deep, g, refsub, errb);
+    float g[NGRAD], refsub, errb, ddeep;
+    sample_pixel<JAC, EXT, DIFF>(b, e, d, i, j, deep, g, refsub, errb, ddeep);
     const int64_t p = st.work_off + (int64_t)j * st.wnx + i;
     b.work[work_plane(b, slot, 0) + p] = deep;
     if (JAC) {
@@ -388,6 +506,8 @@ __device__ void sample_tile(const BatchArgs& b, const EvalF& e, int s, int slot,
     float* aux = b.aux + (int64_t)slot * 2 * b.work_pixels;
     aux[p] = refsub;
     aux[b.work_pixels + p] = errb;
+    // (pixels the integration refines are written again there)
+    if (ops & (OP_DIFF | OP_BASE)) write_diff_base(b, ops, slot, p, deep, ddeep, 0u);
   }
   if (b.kind != AP_PROFILE_SERSIC && b.integrate == AP_INTEGRATE_THRESHOLD) {
     // sum(deep) for the default _integrate_reference (models/_model_methods.py:151-152)
@@ -418,9 +538,9 @@ __global__ void __launch_bounds__(256) k_sample(BatchArgs b) {
   const uint32_t n = b.counters[7];
   uint32_t c0, c1;
   tile_chunk(n, c0, c1);
-  int cur = -1;
-  bool jac = false;
+  int cur = -1, ops = 0;
   EvalF e{};
+  DeltaF d{};
   int64_t next = (c0 < c1) ? b.wlist[c0] : 0;
   for (uint32_t it = c0; it < c1; ++it) {
     const int64_t ent = next;
@@ -431,12 +551,15 @@ __global__ void __launch_bounds__(256) k_sample(BatchArgs b) {
       cur = s * 2 + slot;
       const EvalDev& ed = b.evals[cur];
       e = load_evalf(b.stamps[s], ed);
-      jac = (ed.ops & OP_JAC) != 0;
+      ops = ed.ops;
+      if (!EXT && (ops & OP_DIFF)) d = load_deltaf(ed);
     }
-    if (jac)
-      sample_tile<true, EXT>(b, e, s, slot, local);
+    if (ops & OP_JAC)
+      sample_tile<true, EXT, false>(b, e, d, ops, s, slot, local);
+    else if (!EXT && (ops & OP_DIFF))
+      sample_tile<false, false, true>(b, e, d, ops, s, slot, local);
     else
-      sample_tile<false, EXT>(b, e, s, slot, local);
+      sample_tile<false, EXT, false>(b, e, d, ops, s, slot, local);
   }
 }
 
@@ -618,20 +741,22 @@ __global__ void __launch_bounds__(256) k_recheck(BatchArgs b) {
 // ---------------------------------------------------------------------------
 struct QuadResult {
   float res, ref, errb, mag;
+  float dres;  // DIFF: difference of res to the base evaluation
   float g[NGRAD];
 };
 
 // One (sub-)pixel integrated by this lane alone: Q^2 samples at unit offsets
 // (ci + qx / scale, cj + qy / scale) with amplitude scale area.  QC > 0 fixes the quadrature
 // level at compile time (the sample loop unrolls into independent evaluations).
-template <bool JAC, int QC, bool EXT>
-__device__ __forceinline__ QuadResult quad_lane(const BatchArgs& b, const EvalF& e, float ci,
+template <bool JAC, int QC, bool EXT, bool DIFF>
+__device__ __forceinline__ QuadResult quad_lane(const BatchArgs& b, const EvalF& e, const DeltaF& d, float ci,
                                                 float cj, float inv_g, float area) {
   const QuadTables& T = *b.tables;
   const int n = QC > 0 ? QC * QC : T.quad_level * T.quad_level;
   const int mid = n / 2;
   QuadResult r;
   r.res = 0.f;
+  r.dres = 0.f;
   r.ref = 0.f;
   r.errb = 0.f;
   r.mag = 0.f;
@@ -643,9 +768,11 @@ __device__ __forceinline__ QuadResult quad_lane(const BatchArgs& b, const EvalF&
     if (QC == 0 && k >= n) break;
     float X, Y;
     pix_to_offset(e, ci + T.qxf[k] * inv_g, cj + T.qyf[k] * inv_g, X, Y);
-    const Sample sm = eval_profile<JAC, EXT>(e, b.kind, X, Y, area);
+    float dI = 0.f;
+    const Sample sm = DIFF ? eval_profile_delta(e, d, b.kind, X, Y, area, dI) : eval_profile<JAC, EXT>(e, b.kind, X, Y, area);
     const float w = T.qwf[k];
     r.res = fmaf(w, sm.v, r.res);
+    if (DIFF) r.dres = fmaf(w, dI, r.dres);
     if (JAC) {
 #pragma unroll
       for (int q = 0; q < NGRAD; ++q) r.g[q] = fmaf(w, sm.g[q], r.g[q]);
@@ -727,9 +854,18 @@ __device__ __forceinline__ void level1_pixel(const BatchArgs& b, int64_t ent, bo
   const EvalF f = load_evalf(st, e);
   const int i = (int)(p % st.wnx), j = (int)(p / st.wnx);
   const float di = (float)(i - f.cix), dj = (float)(j - f.cjy);
-  const bool jac = (e.ops & OP_JAC) != 0;
-  QuadResult r = jac ? quad_lane<true, QC, EXT>(b, f, di, dj, 1.f, 1.f)
-                     : quad_lane<false, QC, EXT>(b, f, di, dj, 1.f, 1.f);
+  const int ops = e.ops;
+  const bool jac = (ops & OP_JAC) != 0;
+  DeltaF d{};
+  QuadResult r;
+  if (jac) {
+    r = quad_lane<true, QC, EXT, false>(b, f, d, di, dj, 1.f, 1.f);
+  } else if (!EXT && (ops & OP_DIFF)) {
+    d = load_deltaf(e);
+    r = quad_lane<false, QC, false, true>(b, f, d, di, dj, 1.f, 1.f);
+  } else {
+    r = quad_lane<false, QC, EXT, false>(b, f, d, di, dj, 1.f, 1.f);
+  }
   bool split = false;
   if (b.max_depth > 1) {
     const float thr = e.thresh;
@@ -741,10 +877,12 @@ __device__ __forceinline__ void level1_pixel(const BatchArgs& b, int64_t ent, bo
     // overwrites it
     if (!split && diff >= thr - band) amb = true;
   }
-  if (split)
+  if (split) {
     push = true;
-  else
+  } else {
     write_deep(b, st, slot, p, r.res, r.g, jac);
+    if (ops & (OP_DIFF | OP_BASE)) write_diff_base(b, ops, slot, st.work_off + p, r.res, r.dres, kCodeLevel1);
+  }
 }
 
 // warp-aggregated append of flagged entries to a list (counter, capacity); returns false for
@@ -763,6 +901,41 @@ __device__ __forceinline__ bool warp_append(bool flag, int64_t ent, int64_t* lis
   if (k >= cap) return false;
   list[k] = ent;
   return true;
+}
+
+// Level-2 lists: pixels of Jacobian evaluations fill the recheck buffer from the front,
+// pixels of forward (plain or difference) evaluations from the back, so each kind gets its
+// own integration kernel (compiled, and given registers, for that kind alone).  Together they
+// hold at most one entry per working pixel of each slot: the buffer's 2 * work_pixels.
+__device__ __forceinline__ void level2_append(const BatchArgs& b, bool push, int64_t ent) {
+  bool jac = false;
+  if (push) {
+    const int slot = (int)(ent >> 62);
+    const int s = (int)((ent >> 32) & 0x3fffffff);
+    jac = (b.evals[s * 2 + slot].ops & OP_JAC) != 0;
+  }
+  const int64_t cap = (int64_t)2 * b.work_pixels;
+  const int lane = threadIdx.x & 31;
+  const unsigned mj = __ballot_sync(0xffffffffu, push && jac);
+  const unsigned mf = __ballot_sync(0xffffffffu, push && !jac);
+  uint32_t bj = 0, bf = 0;
+  if (lane == 0) {
+    if (mj) bj = atomicAdd(&b.counters[10], (unsigned)__popc(mj));
+    if (mf) bf = atomicAdd(&b.counters[13], (unsigned)__popc(mf));
+  }
+  bj = __shfl_sync(0xffffffffu, bj, 0);
+  bf = __shfl_sync(0xffffffffu, bf, 0);
+  if (!push) return;
+  const unsigned below = (1u << lane) - 1u;
+  if (jac) {
+    const int64_t k = (int64_t)bj + __popc(mj & below);
+    if (k < cap) b.recheck[k] = ent;
+    else atomicOr(&b.counters[3], 4u);
+  } else {
+    const int64_t k = (int64_t)bf + __popc(mf & below);
+    if (k < cap) b.recheck[cap - 1 - k] = ent;
+    else atomicOr(&b.counters[3], 4u);
+  }
 }
 
 template <bool EXT>
@@ -791,7 +964,7 @@ __global__ void __launch_bounds__(256, 3) k_level1(BatchArgs b) {
       push = refine64<EXT>(b, st, b.evals[s * 2 + slot], (int)(p % st.wnx), (int)(p / st.wnx), -1,
                       b.evals[s * 2 + slot].thresh64);
     }
-    warp_append(push, ent, b.recheck, &b.counters[10], (int64_t)2 * b.work_pixels);
+    level2_append(b, push, ent);
   }
   n64 = __reduce_add_sync(0xffffffffu, n64);
   if ((threadIdx.x & 31) == 0 && n64) atomicAdd(&b.counters[6], (unsigned)n64);
@@ -819,7 +992,7 @@ __global__ void __launch_bounds__(256) k_level1_amb(BatchArgs b) {
       const EvalDev& e = b.evals[s * 2 + slot];
       push = refine64<EXT>(b, st, e, (int)(p % st.wnx), (int)(p / st.wnx), -1, e.thresh64);
     }
-    warp_append(push, ent, b.recheck, &b.counters[10], (int64_t)2 * b.work_pixels);
+    level2_append(b, push, ent);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0) atomicAdd(&b.counters[6], (unsigned)n);
 }
@@ -827,7 +1000,7 @@ __global__ void __launch_bounds__(256) k_level1_amb(BatchArgs b) {
 // Levels 2 and 3 of grid_integrate for a pixel that level 1 split: one warp per pixel,
 // one sub-pixel per lane; each level-2 sub-pixel flagged for refinement is split again and
 // integrated by the whole warp.
-template <bool JAC, int QC, bool EXT>
+template <bool JAC, int QC, bool EXT, bool DIFF>
 __device__ void level23_pixel(const BatchArgs& b, int slot, int s, int64_t p, int lane,
                               unsigned long long& samples, int& n64) {
   const StampDev& st = b.stamps[s];
@@ -836,6 +1009,8 @@ __device__ void level23_pixel(const BatchArgs& b, int slot, int s, int64_t p, in
   const int Q2 = QC > 0 ? QC * QC : T.quad_level * T.quad_level;
   const int g = T.gridding, G2 = g * g;
   const EvalF f = load_evalf(st, e);
+  DeltaF d{};
+  if (DIFF) d = load_deltaf(e);
   const int i = (int)(p % st.wnx), j = (int)(p / st.wnx);
   const float di = (float)(i - f.cix), dj = (float)(j - f.cjy);
   const float thr = e.thresh;
@@ -844,6 +1019,7 @@ __device__ void level23_pixel(const BatchArgs& b, int slot, int s, int64_t p, in
   int n_samples = G2 * Q2;
   QuadResult r2;
   r2.res = 0.f;
+  r2.dres = 0.f;
 #pragma unroll
   for (int q = 0; q < NGRAD; ++q) r2.g[q] = 0.f;
   float ci2 = 0.f, cj2 = 0.f;
@@ -851,11 +1027,12 @@ __device__ void level23_pixel(const BatchArgs& b, int slot, int s, int64_t p, in
   if (lane < G2) {
     ci2 = di + T.gxf[lane];
     cj2 = dj + T.gyf[lane];
-    r2 = quad_lane<JAC, QC, EXT>(b, f, ci2, cj2, ginv, area2);
+    r2 = quad_lane<JAC, QC, EXT, DIFF>(b, f, d, ci2, cj2, ginv, area2);
     if (b.max_depth > 2) split2 = decide<EXT>(b, st, e, r2, thr * (float)G2, i, j, lane, n64);
   }
   // level 3: refine each flagged sub-pixel with the whole warp
   unsigned todo = __ballot_sync(0xffffffffu, split2);
+  const uint32_t code = code_split(todo);
   n_samples += __popc(todo) * G2 * Q2;
   const float area3 = area2 * area2;
   while (todo) {
@@ -865,13 +1042,15 @@ __device__ void level23_pixel(const BatchArgs& b, int slot, int s, int64_t p, in
     const float cjm = __shfl_sync(0xffffffffu, cj2, m);
     QuadResult r3;
     r3.res = 0.f;
+    r3.dres = 0.f;
 #pragma unroll
     for (int q = 0; q < NGRAD; ++q) r3.g[q] = 0.f;
     if (lane < G2) {
-      r3 = quad_lane<JAC, QC, EXT>(b, f, cim + T.gxf[lane] * ginv, cjm + T.gyf[lane] * ginv,
-                              ginv * ginv, area3);
+      r3 = quad_lane<JAC, QC, EXT, DIFF>(b, f, d, cim + T.gxf[lane] * ginv, cjm + T.gyf[lane] * ginv,
+                                         ginv * ginv, area3);
     }
     const float s3 = warp_sum(r3.res);
+    const float ds3 = DIFF ? warp_sum(r3.dres) : 0.f;
     float gs3[NGRAD];
     if (JAC) {
 #pragma unroll
@@ -879,6 +1058,7 @@ __device__ void level23_pixel(const BatchArgs& b, int slot, int s, int64_t p, in
     }
     if (lane == m) {
       r2.res = s3;
+      r2.dres = ds3;
       if (JAC) {
 #pragma unroll
         for (int q = 0; q < NGRAD; ++q) r2.g[q] = gs3[q];
@@ -889,40 +1069,54 @@ __device__ void level23_pixel(const BatchArgs& b, int slot, int s, int64_t p, in
   float out_g[NGRAD];
 #pragma unroll
   for (int q = 0; q < NGRAD; ++q) out_g[q] = JAC ? warp_sum(lane < G2 ? r2.g[q] : 0.f) : 0.f;
+  const float out_d = DIFF ? warp_sum(lane < G2 ? r2.dres : 0.f) : 0.f;
   samples += (unsigned long long)n_samples;
-  if (lane == 0) write_deep(b, st, slot, p, out_v, out_g, JAC);
+  if (lane == 0) {
+    write_deep(b, st, slot, p, out_v, out_g, JAC);
+    if (e.ops & (OP_DIFF | OP_BASE)) write_diff_base(b, e.ops, slot, st.work_off + p, out_v, out_d, code);
+  }
 }
 
-template <bool EXT>
+// FWD = false: the Jacobian evaluations' pixels (front of the recheck buffer); FWD = true: the
+// forward evaluations' pixels (back of the buffer), plain or as differences to the base
+template <bool EXT, bool FWD>
 __global__ void __launch_bounds__(256, 3) k_integrate(BatchArgs b) {
   const int lane = threadIdx.x & 31;
   constexpr uint32_t kChunk = 2;  // queue entries grabbed per atomic
-  const uint32_t n = min((uint32_t)b.counters[10], (uint32_t)(2 * b.work_pixels));
+  const int64_t cap = (int64_t)2 * b.work_pixels;
+  const uint32_t n = min((uint32_t)b.counters[FWD ? 13 : 10], (uint32_t)cap);
   const int Q = b.tables->quad_level;
   unsigned long long samples = 0;
   int n64 = 0;
   while (true) {
     uint32_t idx0 = 0;
-    if (lane == 0) idx0 = atomicAdd(&b.counters[1], kChunk);
+    if (lane == 0) idx0 = atomicAdd(&b.counters[FWD ? 14 : 1], kChunk);
     idx0 = __shfl_sync(0xffffffffu, idx0, 0);
     if (idx0 >= n) break;
     const uint32_t idx1 = min(idx0 + kChunk, n);
     for (uint32_t idx = idx0; idx < idx1; ++idx) {
-      const int64_t ent = b.recheck[idx];
+      const int64_t ent = FWD ? b.recheck[cap - 1 - idx] : b.recheck[idx];
       const int slot = (int)(ent >> 62);
       const int s = (int)((ent >> 32) & 0x3fffffff);
       const int64_t p = ent & 0xffffffffll;
-      const bool jac = (b.evals[s * 2 + slot].ops & OP_JAC) != 0;
-      if (Q == 3) {
-        if (jac)
-          level23_pixel<true, 3, EXT>(b, slot, s, p, lane, samples, n64);
+      if (!FWD) {
+        if (Q == 3)
+          level23_pixel<true, 3, EXT, false>(b, slot, s, p, lane, samples, n64);
         else
-          level23_pixel<false, 3, EXT>(b, slot, s, p, lane, samples, n64);
+          level23_pixel<true, 0, EXT, false>(b, slot, s, p, lane, samples, n64);
       } else {
-        if (jac)
-          level23_pixel<true, 0, EXT>(b, slot, s, p, lane, samples, n64);
-        else
-          level23_pixel<false, 0, EXT>(b, slot, s, p, lane, samples, n64);
+        const bool diff = !EXT && (b.evals[s * 2 + slot].ops & OP_DIFF);
+        if (Q == 3) {
+          if (diff)
+            level23_pixel<false, 3, false, true>(b, slot, s, p, lane, samples, n64);
+          else
+            level23_pixel<false, 3, EXT, false>(b, slot, s, p, lane, samples, n64);
+        } else {
+          if (diff)
+            level23_pixel<false, 0, false, true>(b, slot, s, p, lane, samples, n64);
+          else
+            level23_pixel<false, 0, EXT, false>(b, slot, s, p, lane, samples, n64);
+        }
       }
     }
   }
@@ -1058,6 +1252,7 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
   const int x0 = (local % st.nto_x) * kOutTileX, y0 = (local / st.nto_x) * kOutTileY;
   const int x = x0 + tx, yb = y0 + tg * kConvRows;
   const bool jac = (ops & OP_JAC) != 0;
+  const bool diff = (ops & OP_DIFF) != 0;  // (forward only: no Jacobian planes)
   const bool shiftmode = (b.psf_mode == AP_PSF_FULL);
   const int nplanes = jac ? 1 + NGRAD : 1;
 
@@ -1074,7 +1269,7 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
       const int y = yb + o;
       if (x < st.nx && y < st.ny) {
         const int64_t wp = st.work_off + (int64_t)y * st.wnx + x;
-        cv[0][o] = b.work[work_plane(b, slot, 0) + wp];
+        cv[0][o] = b.work[work_plane(b, slot, diff ? 1 : 0) + wp];
         if (jac) {
 #pragma unroll
           for (int q = 0; q < NGRAD; ++q) cv[3 + q][o] = b.work[work_plane(b, slot, 1 + q) + wp];
@@ -1112,17 +1307,21 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
     float* Tt = smem + 3 * kstride;  // input tile
     const int kp2 = kpx * kpy;
     const float* ksrc = b.spsf + st.spsf_off + (int64_t)slot * 3 * kp2;
-    const int nk = (jac && shiftmode) ? 3 : 1;
+    // kernels: K, dK/dshift_x, dK/dshift_y (Jacobian) or K1, dK (difference to the base)
+    const int nk = (jac && shiftmode) ? 3 : ((diff && shiftmode) ? 2 : 1);
     for (int idx = threadIdx.x; idx < nk * kstride; idx += blockDim.x) {
       const int kk = idx / kstride, rem = idx - kk * kstride, u = rem / ks, v = rem - u * ks;
       KT[idx] = (v < kpy) ? ksrc[kk * kp2 + v * kpx + u] : 0.f;
     }
     const int row0 = y0 + st.by - cy, col0 = x0 + st.bx - cx;
-    for (int pl = 0; pl < nplanes; ++pl) {
-      if (pl > 0 && shiftmode && !(ops & OP_VJP_COORD) && (pl - 1 == GX || pl - 1 == GY)) continue;
-      if (pl > 0 && !profile_has_n(b.kind) && pl - 1 == GN) continue;
+    // difference: dm = K1 * dS (plane 1) + dK * S0 (the base's deep image)
+    const int nsrc = diff ? nk : nplanes;
+    for (int pl = 0; pl < nsrc; ++pl) {
+      if (!diff && pl > 0 && shiftmode && !(ops & OP_VJP_COORD) && (pl - 1 == GX || pl - 1 == GY)) continue;
+      if (!diff && pl > 0 && !profile_has_n(b.kind) && pl - 1 == GN) continue;
       __syncthreads();
-      const float* src = b.work + work_plane(b, slot, pl) + st.work_off;
+      const float* src = diff ? (pl == 0 ? b.work + work_plane(b, slot, 1) : b.base_deep) + st.work_off
+                              : b.work + work_plane(b, slot, pl) + st.work_off;
       // rows over warps, columns over lanes: coalesced reads; stored column-major (pitch TP,
       // rows TH..TP-1 zero)
       for (int r = tg; r < TP; r += kConvThreads / 32) {
@@ -1135,11 +1334,12 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
         }
       }
       __syncthreads();
-      const int nkp = (pl == 0) ? nk : 1;
+      const int nkp = (diff || pl > 0) ? 1 : nk;
       for (int kk = 0; kk < nkp; ++kk) {
         float outv[kConvRows];
-        conv_col(Tt, TP, KT + kk * kstride, kpx, kpy, tx, tg * kConvRows, outv);
-        const int dst = (pl == 0) ? kk : 3 + (pl - 1);
+        const int kidx = diff ? pl : kk;
+        conv_col(Tt, TP, KT + kidx * kstride, kpx, kpy, tx, tg * kConvRows, outv);
+        const int dst = diff ? pl : ((pl == 0) ? kk : 3 + (pl - 1));
 #pragma unroll
         for (int o = 0; o < kConvRows; ++o) cv[dst][o] = outv[o];
       }
@@ -1168,8 +1368,9 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
   for (int o = 0; o < kConvRows; ++o) {
     const int y = yb + o;
     if (!(x < st.nx && y < st.ny)) continue;
-    const float mgal = cv[0][o];
-    const float m = mgal + e.sky;
+    // (difference evaluations: mgal is the galaxy's difference, m the model's)
+    const float mgal = diff ? cv[0][o] + cv[1][o] : cv[0][o];
+    const float m = mgal + (diff ? e.d_sky : e.sky);
     // value-space Jacobian in full-vector order, compacted to the fitted slots
     float Jc[NF > 0 ? NF : 1];
     if (jac) {
@@ -1220,8 +1421,9 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
     // fused reductions (fit/lm.py:374-406); masked pixels are left out entirely
     if (io.mask && io.mask[op]) continue;
     const float w = io.weight ? io.weight[op] : 1.f;
-    const float r = io.data[op] - m;
-    a_chi2 += w * r * r;
+    const float r = diff ? io.data[op] - io.y0[op] : io.data[op] - m;
+    // chi^2 or, for a difference dm, its change W [(r - dm)^2 - r^2] = W dm (dm - 2 r)
+    a_chi2 += diff ? w * m * (m - 2.f * r) : w * r * r;
     if (do_hg) {
       int h = 0;
 #pragma unroll
@@ -1241,7 +1443,7 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
         jh = fmaf(Jb[k], hf[k], jh);
       }
       // (2/d) * ((rh - r)/d - W (J h)),  rh - r = W (Y1 - Y0)
-      const float ebase = (2.f / d) * ((w * (m - io.y0[op])) / d - w * jh);
+      const float ebase = (2.f / d) * ((w * (diff ? m : m - io.y0[op])) / d - w * jh);
 #pragma unroll
       for (int k = 0; k < NF; ++k) a_rpp[k] += Jb[k] * ebase;
     }
@@ -1432,14 +1634,19 @@ cudaError_t launch_render_pass(const BatchArgs& b, const ConvIO& io, size_t conv
     E(t);
     t = B(KC_INTEGRATE);
     const int gi = nsm * knob(GK_INTEGRATE, 8);
+    // (the two level-2 kernels share the persistent-grid size of the Jacobian one, scaled by
+    // their resident blocks per SM)
+    const int gf = gi;
     if (ext) {
       k_level1<true><<<gi, 256, 0, s>>>(b);
       if (b.amb_cap > 0) k_level1_amb<true><<<nsm * 4, 256, 0, s>>>(b);
-      k_integrate<true><<<gi, 256, 0, s>>>(b);
+      k_integrate<true, false><<<gi, 256, 0, s>>>(b);
+      k_integrate<true, true><<<gf, 256, 0, s>>>(b);
     } else {
       k_level1<false><<<gi, 256, 0, s>>>(b);
       if (b.amb_cap > 0) k_level1_amb<false><<<nsm * 4, 256, 0, s>>>(b);
-      k_integrate<false><<<gi, 256, 0, s>>>(b);
+      k_integrate<false, false><<<gi, 256, 0, s>>>(b);
+      k_integrate<false, true><<<gf, 256, 0, s>>>(b);
     }
     E(t);
   }

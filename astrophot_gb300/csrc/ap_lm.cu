@@ -96,10 +96,26 @@ __device__ void finish(const BatchArgs& b, const LMArgs& lm, int s, LMState& S, 
   lm.ops_next[s * 2 + 1] = 0;
 }
 
+// Trials rendered as differences to the step's base point (k_eval_setup drops OP_DIFF for the
+// same stamps): their chi^2 is chi^2(x) + the accumulated change, and rpp uses the precise
+// model difference, so the damping search compares chi^2 values that differ by far less
+// than the FP32 rendering error of a single model.
+__device__ __forceinline__ bool trials_as_diff(const BatchArgs& b, const LMArgs& lm, int s) {
+  return lm.precise && diff_capable(b, b.stamps[s]);
+}
+
+// Relative error bounds of a chi^2 change accumulated from a difference render, and of a
+// chi^2 accumulated from a full FP32 render.  A chain of trial differences drifts by the
+// first times the sizes of its steps; the next Jacobian render of the base point (which
+// accumulates chi^2 too) re-anchors the chain once that drift exceeds the second.
+constexpr double kDiffRelErr = 2e-6;
+constexpr double kFullRelErr = 2e-8;
+
 __device__ void schedule_jac(const BatchArgs& b, const LMArgs& lm, int s, LMState& S) {
   S.phase = LM_PH_JAC;
   if (!write_eval(b, lm, s, 0, S.x,
-                  OP_FWD | OP_JAC | OP_HG | OP_WRITE_MODEL | OP_WRITE_JAC | OP_REP)) {
+                  OP_FWD | OP_JAC | OP_HG | OP_WRITE_MODEL | OP_WRITE_JAC | OP_REP |
+                      (lm.precise ? OP_BASE : 0))) {
     finish(b, lm, s, S, AP_LM_LIMIT);
     return;
   }
@@ -113,11 +129,12 @@ __device__ void start_sub(const BatchArgs& b, const LMArgs& lm, int s, LMState& 
   for (int k = 0; k < P; ++k) lm.hvec[(int64_t)s * NPARAM + k] = S.h[k];
   double xa[NPARAM];
   for (int k = 0; k < P; ++k) xa[k] = S.x[k] + 0.1 * S.h[k];
-  bool ok = write_eval(b, lm, s, 0, xa, OP_FWD | OP_RPP);
+  const int32_t dop = trials_as_diff(b, lm, s) ? OP_DIFF : 0;
+  bool ok = write_eval(b, lm, s, 0, xa, OP_FWD | OP_RPP | dop);
   if (lm.acceleration == 0.0) {
     double xb[NPARAM];
     for (int k = 0; k < P; ++k) xb[k] = S.x[k] + S.h[k];
-    ok = write_eval(b, lm, s, 1, xb, OP_FWD | OP_CHI2) && ok;
+    ok = write_eval(b, lm, s, 1, xb, OP_FWD | OP_CHI2 | dop) && ok;
   } else {
     lm.ops_next[s * 2 + 1] = 0;
   }
@@ -157,6 +174,7 @@ __device__ void end_step(const BatchArgs& b, const LMArgs& lm, int s, LMState& S
   S.L = rL;
   for (int k = 0; k < P; ++k) S.x[k] = S.x[k] + rha[k];
   S.chi2_cur = rchi2;
+  if (trials_as_diff(b, lm, s)) S.anchor_err += kDiffRelErr * fabs(rchi2 - S.init_chi2);
   record(lm, s, S, rchi2);
   S.L = fmax(1e-9, S.L / lm.Ldn);
   S.iter++;
@@ -240,6 +258,13 @@ __device__ void decide_step(const BatchArgs& b, const LMArgs& lm, int s, LMState
   end_step(b, lm, s, S);
 }
 
+// chi^2 / ndf of a trial from its accumulated sum (the change to the base point's when the
+// trial was rendered as a difference)
+__device__ __forceinline__ double trial_chi2(const BatchArgs& b, const LMArgs& lm, int s, const LMState& S,
+                                             double acc) {
+  return trials_as_diff(b, lm, s) ? S.init_chi2 + acc / S.ndf : acc / S.ndf;
+}
+
 __global__ void k_lm_count(BatchArgs b, const uint8_t* mask, LMArgs lm) {
   const int s = blockIdx.x;
   const StampDev& st = b.stamps[s];
@@ -268,6 +293,7 @@ __global__ void k_lm_init(BatchArgs b, LMArgs lm, const double* state0) {
   S.nostep = 1;
   S.scarry_valid = 0;
   S.hist_len = 0;
+  S.anchor_err = 0.0;
   S.L = lm.L0;
   S.status = AP_LM_RUNNING;
   for (int k = 0; k < NPARAM; ++k) S.x[k] = (k < P) ? state0[(int64_t)s * P + k] : 0.0;
@@ -314,6 +340,15 @@ __global__ void k_lm_update(BatchArgs b, LMArgs lm) {
           S.H[c * P + a] = acc0[idx];
           ++idx;
         }
+      if (trials_as_diff(b, lm, s) && S.anchor_err > kFullRelErr * S.chi2_cur) {
+        // the chain of differences drifted more than a full render's rounding: take chi^2 of
+        // this base point from its render (loss_history[-1] too; at this size of step no
+        // convergence test is near its threshold)
+        S.chi2_cur = acc0[0] / S.ndf;
+        S.anchor_err = 0.0;
+        const int n = lm.max_iter + 1;
+        if (S.hist_len > 0) lm.hist_loss[(int64_t)s * n + S.hist_len - 1] = S.chi2_cur;
+      }
       S.init_chi2 = S.chi2_cur;
       S.nostep = 1;
       S.best_chi2 = S.init_chi2;
@@ -339,18 +374,19 @@ __global__ void k_lm_update(BatchArgs b, LMArgs lm) {
       }
       for (int k = 0; k < P; ++k) S.ha[k] = S.h[k] + S.a[k] * lm.acceleration;
       if (lm.acceleration == 0.0) {
-        decide_step(b, lm, s, S, acc1[0] / S.ndf);
+        decide_step(b, lm, s, S, trial_chi2(b, lm, s, S, acc1[0]));
       } else {
         double xb[NPARAM];
         for (int k = 0; k < P; ++k) xb[k] = S.x[k] + S.ha[k];
         lm.ops_next[s * 2 + 0] = 0;
         S.phase = LM_PH_SUB2;
-        if (!write_eval(b, lm, s, 1, xb, OP_FWD | OP_CHI2)) finish(b, lm, s, S, AP_LM_LIMIT);
+        if (!write_eval(b, lm, s, 1, xb, OP_FWD | OP_CHI2 | (trials_as_diff(b, lm, s) ? OP_DIFF : 0)))
+          finish(b, lm, s, S, AP_LM_LIMIT);
       }
       break;
     }
     case LM_PH_SUB2: {
-      decide_step(b, lm, s, S, acc1[0] / S.ndf);
+      decide_step(b, lm, s, S, trial_chi2(b, lm, s, S, acc1[0]));
       break;
     }
     default:

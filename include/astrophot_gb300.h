@@ -107,6 +107,14 @@ typedef struct ap_lm_options {
   double acceleration;      /* 0 */
   int32_t rounds_per_sync;  /* device rounds between host checks of the active count (>= 1) */
   int32_t use_graph;        /* 1: capture rounds_per_sync rounds in a CUDA graph and replay it */
+  int32_t precise_trials;   /* 1 (default): render each damping trial as its difference to the
+                               step's base point (sample, kernel and convolution differences formed
+                               from the exact parameter differences), so chi^2 changes far below
+                               the FP32 rendering error of one model (the reference compares
+                               float64 chi^2 values near convergence) decide the damping search,
+                               the curvature test and convergence as in float64 (Sersic and
+                               exponential stamps, direct or FFT convolution).  0: plain FP32
+                               trial renders. */
 } ap_lm_options;
 
 typedef struct ap_batch ap_batch; /* opaque host-side plan (host memory only) */

@@ -1,11 +1,11 @@
 """CUDA path (through the C ABI) against the reference's golden vectors and the oracle.
 
 Tolerances (FP32 rendering against float64):
-  model images : max |gpu - ref| <= 1e-5 * max |ref|, and per pixel <= 1e-4 relative where
+  model images : max |gpu - ref| <= 1e-5 * max |ref|, and per pixel <= 1e-5 relative where
                  |ref| > 1e-3 max |ref|
   Jacobians    : per column max |gpu - ref| <= 2e-4 * max |ref column|
-  LM           : final chi2/ndf within 1e-4 relative of the reference's, fitted
-                 representation within 1e-3 (absolute + relative)
+  LM           : the reference's message and iteration count, final chi2/ndf and fitted
+                 value-space parameters within 1e-4 relative, loss history within 1e-6
 """
 
 import numpy as np
@@ -36,7 +36,7 @@ def N():
     return _native
 
 
-def assert_image_close(got, ref, rel=1e-5, pix=1e-4):
+def assert_image_close(got, ref, rel=1e-5, pix=1e-5):
     scale = np.max(np.abs(ref))
     assert np.max(np.abs(got - ref)) <= rel * scale, np.max(np.abs(got - ref)) / scale
     bright = np.abs(ref) > 1e-3 * scale
@@ -189,9 +189,13 @@ def parameter_sigma(d):
 @pytest.mark.parametrize("name", cases.lm_case_names())
 @pytest.mark.parametrize("graph", [False, True])
 def test_lm_matches_reference(N, name, graph):
-    """Final chi2/ndf within 1e-4 of the reference's; fitted vector within 0.25 sigma of the
-    reference's (its own stopping rule, chi2 change < 1e-5, leaves that much freedom along the
-    valley floor; the FP32 render changes where the last accepted step lands)."""
+    """The reference's own fit, reproduced: same message and iteration count, final chi2/ndf
+    within 1e-4 relative, fitted value-space parameters within 1e-4 relative, and the loss
+    history within 1e-6 relative at every iteration.  The damping trials are rendered as
+    differences to the step's base point (precise_trials), so the damping search takes the
+    float64 reference's decisions down to chi^2 changes of 1e-10."""
+    from astrophot_gb300.transforms import rep_to_slots
+
     d = cases.load_lm(name)
     size = d["spec"]["size"]
     opts = N.make_options(profile="sersic", psf_mode="full", free_mask=0x7F, has_sky=True)
@@ -208,15 +212,29 @@ def test_lm_matches_reference(N, name, graph):
     )
     ref_chi2 = d["loss_history"].min()
     assert abs(chi2.item() / ref_chi2 - 1) <= 1e-4
-    res = state.cpu().numpy()[0]
-    sig = parameter_sigma(d)
-    dev = np.abs(res - d["res"]) / sig
-    print(name, "fitted vector offset in sigma", np.round(dev, 4), "relative", np.abs(res - d["res"]) / np.abs(d["res"]))
-    assert np.all(dev <= 0.25), dev
-    # the trajectory follows the reference's until the chi2 changes reach FP32 resolution
+    assert N.LM_MESSAGES[status.item()] == d["message"]
+    assert iters.item() == len(d["loss_history"]) - 1
+    vals = rep_to_slots(state.cpu().numpy(), fixed.numpy(), 0x7F)[0][:7]
+    rel = np.abs(vals - d["final_values"]) / np.abs(d["final_values"])
+    print(name, "fitted value-space parameters, relative offset", rel)
+    assert np.all(rel <= 1e-4), rel
     loss, L, xs = b.lm_history()
-    assert np.allclose(loss[0, :3].cpu().numpy(), d["loss_history"][:3], rtol=1e-6)
-    assert status.item() in (N.LM_SUCCESS, N.LM_IMMOBILE, N.LM_NO_STEP)
+    np.testing.assert_allclose(loss[0, : iters.item() + 1].cpu().numpy(), d["loss_history"], rtol=1e-6)
+    np.testing.assert_allclose(L[0, : iters.item() + 1].cpu().numpy(), d["L_history"], rtol=1e-9)
+
+
+def test_lm_plain_trials_option(N):
+    """precise_trials=False keeps the plain FP32 trial renders: the same fit ends at the same
+    chi2 within 1e-4 (its decisions near convergence follow FP32 rounding instead)."""
+    d = cases.load_lm("lm_64")
+    opts = N.make_options(profile="sersic", psf_mode="full", free_mask=0x7F, has_sky=True)
+    b = N.StampBatch([(64, 64)], [(25, 25)], N.scale_geometry(1), opts)
+    args = (b.pack([d["data"]]), b.pack([d["weight"]]), None, b.pack_psf([d["psf"]]),
+            torch.tensor(np.r_[d["init"], 0.0][None, :]), torch.tensor(d["rep0"][None, :]))
+    _, c_plain, _, s_plain = b.lm_fit(*args, N.make_lm_options(precise_trials=False))
+    _, c_prec, _, s_prec = b.lm_fit(*args, N.make_lm_options())
+    assert abs(c_plain.item() / d["loss_history"].min() - 1) <= 1e-4
+    assert abs(c_prec.item() / d["loss_history"].min() - 1) <= 1e-4
 
 
 def test_batched_equals_single(N):
