@@ -37,7 +37,7 @@ _ERR_NAMES = {
 }
 
 PROFILE = {"sersic": 0, "exponential": 1, "moffat": 2, "gaussian": 3}
-SAMPLING = {"midpoint": 0, "simpsons": 1, "quad": 2, "trapezoid": 3}
+SAMPLING = {"midpoint": 0, "simpsons": 1, "quad": 2, "trapezoid": 3, "midpoint_center": 4}
 INTEGRATE = {"none": 0, "threshold": 1}
 PSF_NONE, PSF_FULL, PSF_FULL_NOSHIFT = 0, 1, 2
 VJP_REPRESENTATION, VJP_REFERENCE_CENTER = 1, 2
@@ -78,6 +78,7 @@ class ApOptions(ctypes.Structure):
         ("free_mask", ctypes.c_int32),
         ("has_sky", ctypes.c_int32),
         ("fft_min_kernel", ctypes.c_int32),
+        ("center_radius", ctypes.c_double),
     ]
 
 
@@ -242,6 +243,8 @@ def make_options(
     has_sky=False,
     psf_convolve_mode="direct",
     fft_min_kernel=None,
+    center_quad_level=3,
+    center_radius=2.0,
 ) -> ApOptions:
     o = ApOptions()
     if profile not in PROFILE:
@@ -250,12 +253,20 @@ def make_options(
     if sampling_mode.startswith("quad"):
         o.sampling_mode = SAMPLING["quad"]
         o.sampling_quad_level = int(sampling_mode[sampling_mode.find(":") + 1 :])
+    elif sampling_mode == "midpoint_center":
+        # midpoint + center_quad_level^2 Gauss-Legendre points on the pixels within center_radius
+        # pixels of the centre (no adaptive integration)
+        if integrate_mode != "none":
+            raise SpecificationConflict("sampling_mode midpoint_center needs integrate_mode none")
+        o.sampling_mode = SAMPLING[sampling_mode]
+        o.sampling_quad_level = int(center_quad_level)
     elif sampling_mode in SAMPLING:
         o.sampling_mode = SAMPLING[sampling_mode]
         o.sampling_quad_level = 0
     else:
         raise SpecificationConflict(
-            f"unknown sampling mode: {sampling_mode}. Should be one of: midpoint, simpsons, quad:level, trapezoid"
+            f"unknown sampling mode: {sampling_mode}. Should be one of: midpoint, simpsons, quad:level, trapezoid, "
+            "midpoint_center"
         )
     if integrate_mode not in INTEGRATE:
         raise SpecificationConflict(
@@ -285,6 +296,7 @@ def make_options(
     if fft_min_kernel is None:
         fft_min_kernel = FFT_MIN_KERNEL if psf_convolve_mode == "fft" else 0
     o.fft_min_kernel = int(fft_min_kernel)
+    o.center_radius = float(center_radius)
     return o
 
 

@@ -124,11 +124,15 @@ int validate_options(const ap_options* o) {
   if (!o) return AP_ERR_ARG;
   if (o->fft_min_kernel < 0) return AP_ERR_ARG;
   if (o->profile < AP_PROFILE_SERSIC || o->profile > AP_PROFILE_GAUSSIAN) return AP_ERR_UNSUPPORTED;
-  if (o->sampling_mode < AP_SAMPLING_MIDPOINT || o->sampling_mode > AP_SAMPLING_TRAPEZOID)
+  if (o->sampling_mode < AP_SAMPLING_MIDPOINT || o->sampling_mode > AP_SAMPLING_MIDPOINT_CENTER)
     return AP_ERR_UNSUPPORTED;
-  if (o->sampling_mode == AP_SAMPLING_QUAD &&
+  if ((o->sampling_mode == AP_SAMPLING_QUAD || o->sampling_mode == AP_SAMPLING_MIDPOINT_CENTER) &&
       (o->sampling_quad_level < 1 || o->sampling_quad_level > kMaxQuad))
     return AP_ERR_UNSUPPORTED;
+  if (o->sampling_mode == AP_SAMPLING_MIDPOINT_CENTER) {
+    if (o->integrate_mode != AP_INTEGRATE_NONE) return AP_ERR_UNSUPPORTED;
+    if (!(o->center_radius >= 0.0) || !std::isfinite(o->center_radius)) return AP_ERR_ARG;
+  }
   if (o->integrate_mode != AP_INTEGRATE_NONE && o->integrate_mode != AP_INTEGRATE_THRESHOLD)
     return AP_ERR_UNSUPPORTED;
   if (o->psf_mode < AP_PSF_NONE || o->psf_mode > AP_PSF_FULL_NOSHIFT) return AP_ERR_UNSUPPORTED;
@@ -369,7 +373,8 @@ int ap_batch_create(ap_batch** out, int32_t n, const int32_t* nx, const int32_t*
         }
       break;
     }
-    case AP_SAMPLING_QUAD: {
+    case AP_SAMPLING_QUAD:
+    case AP_SAMPLING_MIDPOINT_CENTER: {  // (the latter: the table of its centre pixels)
       const int k = options->sampling_quad_level;
       T.nsub = k * k;
       T.sub_center = (k * k) / 2;
@@ -430,6 +435,7 @@ int ap_batch_create(ap_batch** out, int32_t n, const int32_t* nx, const int32_t*
   A.tolerance = (float)options->sampling_tolerance;
   A.tolerance64 = options->sampling_tolerance;
   A.softening64 = options->softening;
+  A.center_r2 = (float)(options->center_radius * options->center_radius + 1e-6);
   A.work_pixels = b->work_pixels;
   A.out_pixels = b->out_pixels;
   A.n_fft = n_fft;

@@ -180,6 +180,7 @@ struct BatchArgs {
   int32_t n_work_tiles, n_out_tiles;
   int32_t max_kp2;      // largest kpy * kpx
   float tolerance;
+  float center_r2;      // AP_SAMPLING_MIDPOINT_CENTER: squared radius (+ 1e-6) in pixels
   double tolerance64, softening64;
   int64_t work_pixels, out_pixels;
   const StampDev* stamps;

@@ -420,11 +420,14 @@ __global__ void k_psf_shift(BatchArgs b, const float* psf, const float* psf_base
 // sampling (_sample_init): deep value, partials, reference sub-sample, FP32 error bound
 // ---------------------------------------------------------------------------
 // DIFF (forward only): also ddeep = the difference of deep to the base evaluation
+// mid_only: one sample at the pixel centre (sampling mode midpoint_center outside its radius)
 template <bool JAC, bool EXT, bool DIFF>
 __device__ __forceinline__ void sample_pixel(const BatchArgs& b, const EvalF& e, const DeltaF& d, int i, int j,
-                                             float& deep, float* g, float& refsub, float& errb, float& ddeep) {
+                                             bool mid_only, float& deep, float* g, float& refsub, float& errb,
+                                             float& ddeep) {
   const QuadTables& T = *b.tables;
   const float di = (float)(i - e.cix), dj = (float)(j - e.cjy);
+  const int nsub = mid_only ? 1 : T.nsub, sub_center = mid_only ? 0 : T.sub_center;
   deep = 0.f;
   ddeep = 0.f;
 #pragma unroll
@@ -432,12 +435,12 @@ __device__ __forceinline__ void sample_pixel(const BatchArgs& b, const EvalF& e,
   float absb = 0.f, mag = 0.f;
   refsub = 0.f;
   float referr = 0.f;
-  for (int k = 0; k < T.nsub; ++k) {
+  for (int k = 0; k < nsub; ++k) {
     float X, Y;
-    pix_to_offset(e, di + T.sxf[k], dj + T.syf[k], X, Y);
+    pix_to_offset(e, di + (mid_only ? 0.f : T.sxf[k]), dj + (mid_only ? 0.f : T.syf[k]), X, Y);
     float dI = 0.f;
     const Sample sm = DIFF ? eval_profile_delta(e, d, b.kind, X, Y, 1.f, dI) : eval_profile<JAC, EXT>(e, b.kind, X, Y, 1.f);
-    const float w = T.swf[k];
+    const float w = mid_only ? 1.f : T.swf[k];
     deep = fmaf(w, sm.v, deep);
     if (DIFF) ddeep = fmaf(w, dI, ddeep);
     if (JAC) {
@@ -447,13 +450,13 @@ __device__ __forceinline__ void sample_pixel(const BatchArgs& b, const EvalF& e,
     const float a = fabsf(w * sm.v);
     mag += a;
     absb += a * sample_rel_err(e, sm.arg);
-    if (k == T.sub_center) {
+    if (k == sub_center) {
       refsub = sm.v;
       referr = fabsf(sm.v) * sample_rel_err(e, sm.arg);
     }
   }
   // bound on |deep_fp32 - deep_fp64| (+ the reference sub-sample's for simpsons / quad)
-  errb = absb + 2.f * (float)T.nsub * kEps * mag + referr;
+  errb = absb + 2.f * (float)nsub * kEps * mag + referr;
 }
 
 // Deep value of a working pixel that is final (not refined further): the base evaluation
@@ -495,8 +498,14 @@ __device__ void sample_tile(const BatchArgs& b, const EvalF& e, const DeltaF& d,
   const bool valid = (i < st.wnx) && (j < st.wny);
   float deep = 0.f;
   if (valid) {
+    // midpoint_center: the quadrature table only for pixel centres within the radius
+    bool mid_only = false;
+    if (b.sampling == AP_SAMPLING_MIDPOINT_CENTER) {
+      const float ax = (float)(i - e.cix) - e.fx, ay = (float)(j - e.cjy) - e.fy;
+      mid_only = ax * ax + ay * ay > b.center_r2;
+    }
     float g[NGRAD], refsub, errb, ddeep;
-    sample_pixel<JAC, EXT, DIFF>(b, e, d, i, j, deep, g, refsub, errb, ddeep);
+    sample_pixel<JAC, EXT, DIFF>(b, e, d, i, j, mid_only, deep, g, refsub, errb, ddeep);
     const int64_t p = st.work_off + (int64_t)j * st.wnx + i;
     b.work[work_plane(b, slot, 0) + p] = deep;
     if (JAC) {
@@ -506,8 +515,11 @@ __device__ void sample_tile(const BatchArgs& b, const EvalF& e, const DeltaF& d,
     float* aux = b.aux + (int64_t)slot * 2 * b.work_pixels;
     aux[p] = refsub;
     aux[b.work_pixels + p] = errb;
-    // (pixels the integration refines are written again there)
-    if (ops & (OP_DIFF | OP_BASE)) write_diff_base(b, ops, slot, p, deep, ddeep, 0u);
+    // (pixels the integration refines are written again there; midpoint_center marks its
+    // quadrature pixels, which a moved centre may change)
+    if (ops & (OP_DIFF | OP_BASE))
+      write_diff_base(b, ops, slot, p, deep, ddeep,
+                      (b.sampling == AP_SAMPLING_MIDPOINT_CENTER && !mid_only) ? kCodeLevel1 : 0u);
   }
   if (b.kind != AP_PROFILE_SERSIC && b.integrate == AP_INTEGRATE_THRESHOLD) {
     // sum(deep) for the default _integrate_reference (models/_model_methods.py:151-152)

@@ -63,6 +63,14 @@ typedef struct CUstream_st* ap_stream_t; /* same handle as cudaStream_t */
 #define AP_SAMPLING_SIMPSONS 1
 #define AP_SAMPLING_QUAD 2
 #define AP_SAMPLING_TRAPEZOID 3
+/* Midpoint sampling with the pixels whose centres lie within options.center_radius pixels of
+ * the model centre (squared distance <= radius^2 + 1e-6) integrated by
+ * sampling_quad_level x sampling_quad_level Gauss-Legendre points (the reference's
+ * single_quad_integrate, astrophot/utils/operations.py:123-147, on those pixels of its midpoint
+ * image, astrophot/models/_model_methods.py:84-87): "midpoint sampling plus 3 x 3 supersampling
+ * within 2 px of the centre".  No counterpart mode in the reference.  integrate_mode must be
+ * AP_INTEGRATE_NONE. */
+#define AP_SAMPLING_MIDPOINT_CENTER 4
 /* ap_options.integrate_mode */
 #define AP_INTEGRATE_NONE 0
 #define AP_INTEGRATE_THRESHOLD 1
@@ -96,6 +104,7 @@ typedef struct ap_options {
                                    padding) is at least this are convolved by FFT
                                    (psf_convolve_mode "fft", models/_model_methods.py:245-257);
                                    0 = direct convolution for every stamp */
+  double center_radius;         /* AP_SAMPLING_MIDPOINT_CENTER: radius in pixels (2) */
 } ap_options;
 
 typedef struct ap_lm_options {

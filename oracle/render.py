@@ -293,6 +293,10 @@ class Component:
     integrate_gridding: int = 5
     integrate_quad_level: int = 3
     softening: float = 1e-3
+    # sampling_mode "midpoint_center" (the single-Sersic stamp configuration's "midpoint sampling
+    # plus 3 x 3 supersampling within 2 px of the centre"; no such mode in the reference)
+    center_quad_level: int = 3
+    center_radius: float = 2.0
     locked: Tuple[str, ...] = ()
     # pixel window [[x0, x1], [y0, y1]] inside the group's window (Model.window given in pixels,
     # models/core_model.py:313-325 -> Window.crop_to_pixel); None = the whole window
@@ -563,6 +567,8 @@ def sample_init(comp, win: Window, center, grad):
         cx, cy = win.meshgrid()
         res, ref = single_quad_integrate(comp, cx - center[0], cy - center[1], win.P, win.pixel_area, level, grad)
         return ref, res
+    if mode == "midpoint_center":
+        return sample_midpoint_center(comp, win, center, grad)
     if mode == "trapezoid":
         cx, cy = win.corner_meshgrid()
         D = _eval(comp, cx - center[0], cy - center[1], win.pixel_area, grad)
@@ -570,6 +576,48 @@ def sample_init(comp, win: Window, center, grad):
         curv = _laplacian_replicate(trapz.val)
         return trapz.val + curv, trapz
     raise ValueError(f"unknown sampling mode: {mode}")
+
+
+# squared pixel distances up to radius^2 + CENTER_R2_SLACK count as inside: with the sub-pixel
+# shift the pixel centres sit at whole-pixel offsets from the model centre, and a pixel exactly
+# at the radius must not fall out by the rounding of its coordinates
+CENTER_R2_SLACK = 1e-6
+
+
+def center_select(win: Window, X, Y, radius):
+    """Pixels whose centres lie within ``radius`` pixels of the model centre (plane offsets X, Y
+    mapped back to pixel units by the inverse pixel-scale matrix)."""
+    Pinv = np.linalg.inv(win.P)
+    di = Pinv[0, 0] * X + Pinv[0, 1] * Y
+    dj = Pinv[1, 0] * X + Pinv[1, 1] * Y
+    return di * di + dj * dj <= radius * radius + CENTER_R2_SLACK
+
+
+def sample_midpoint_center(comp, win: Window, center, grad):
+    """Midpoint sampling with the pixels near the centre integrated by Gauss-Legendre
+    quadrature: the midpoint image (``_sample_init`` "midpoint", models/_model_methods.py:84-87)
+    with the pixels whose centres lie within ``center_radius`` pixels of the model centre
+    replaced by ``single_quad_integrate`` (utils/operations.py:123-147) at
+    ``center_quad_level``.  Returns (reference image, deep Sampled) like ``sample_init``; the
+    adaptive integration does not run in this mode (its reference image is the curvature
+    estimate of the midpoint image, as for "midpoint")."""
+    if comp.integrate_mode != "none":
+        raise ValueError("sampling_mode midpoint_center needs integrate_mode none")
+    cx, cy = win.meshgrid()
+    X, Y = cx - center[0], cy - center[1]
+    S = _eval(comp, X, Y, win.pixel_area, grad)
+    curv = _laplacian_replicate(S.val)
+    sel = center_select(win, X, Y, comp.center_radius)
+    if np.any(sel):
+        res, _ = single_quad_integrate(comp, X[sel], Y[sel], win.P, win.pixel_area, comp.center_quad_level, grad)
+        S.val[sel] = res.val
+        if grad:
+            for k in GRAD_KEYS:
+                if res.grad[k] is not None:
+                    if S.grad[k] is None:
+                        S.grad[k] = np.zeros_like(S.val)
+                    S.grad[k][sel] = res.grad[k]
+    return S.val + curv, S
 
 
 def integrate_reference(comp, deep_val):

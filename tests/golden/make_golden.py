@@ -1,13 +1,13 @@
 """Generate the golden vectors in this folder by running the reference itself.
 
-Run in a container that has the reference checkout (default path below, or
-``ASTROPHOT_REFERENCE=<path>``):
+Run with ``ASTROPHOT_REFERENCE=<path of the reference checkout>`` set:
 
     python tests/golden/make_golden.py          # every case
     python tests/golden/make_golden.py init     # only the initial-value cases
     python tests/golden/make_golden.py iter     # the initial-value and Iter_LM cases
     python tests/golden/make_golden.py segmap   # only the segmentation-map case
     python tests/golden/make_golden.py auxpsf   # only the live-PSF-model case
+    python tests/golden/make_golden.py center   # only the centre-supersampling cases
 
 The reference (AstroPhot 0.x) is imported through a ``sys.modules`` shim for
 the optional packages it imports at module level but never calls on this
@@ -35,7 +35,7 @@ sys.path.insert(0, REPO)
 
 from astrophot_gb300 import synthetic  # noqa: E402
 
-REFERENCE = os.environ.get("ASTROPHOT_REFERENCE", "/root/reference")
+REFERENCE = os.environ.get("ASTROPHOT_REFERENCE")
 
 
 class _StubObj:
@@ -79,6 +79,8 @@ class _StubFinder(importlib.abc.MetaPathFinder, importlib.abc.Loader):
 
 
 def import_reference():
+    if not REFERENCE:
+        raise SystemExit("set ASTROPHOT_REFERENCE to the reference checkout (the folder holding astrophot/)")
     sys.meta_path.insert(0, _StubFinder())
     sys.path.insert(0, REFERENCE)
     import astrophot as ap  # noqa: E402
@@ -188,6 +190,26 @@ RENDER_CASES = {
         params={"center": [23.6, 24.2], "q": 0.6, "PA": 1.7, "Re": 7.0, "Ie": 1.5},
         knobs={"psf_mode": "full"},
     ),
+    # the single-Sersic stamp configuration's sampling: midpoint, plus 3 x 3 Gauss-Legendre on
+    # the pixels within 2 px of the centre, no adaptive integration (see center_supersample)
+    "sersic_psf_center": dict(
+        kind="sersic",
+        nx=64,
+        ny=64,
+        scale=1.0,
+        psf=MOFFAT_25,
+        params={"center": [31.7, 32.4], "q": 0.55, "PA": 0.9, "n": 2.5, "Re": 8.0, "Ie": 1.2},
+        knobs={"psf_mode": "full", "sampling_mode": "midpoint_center", "integrate_mode": "none"},
+    ),
+    "sersic_nopsf_center": dict(
+        kind="sersic",
+        nx=40,
+        ny=48,
+        scale=0.8,
+        psf=None,
+        params={"center": [14.1, 21.3], "q": 0.7, "PA": 0.3, "n": 3.3, "Re": 4.0, "Ie": 1.0},
+        knobs={"sampling_mode": "midpoint_center", "integrate_mode": "none"},
+    ),
     "sersic_scale08": dict(
         kind="sersic",
         nx=50,
@@ -205,7 +227,40 @@ LM_CASES = {
     # the 128 x 128 single-Sersic stamp workload, two seeds
     "lm_c0_seed0": dict(size=128, seed=0, psf=MOFFAT_25),
     "lm_c0_seed1": dict(size=128, seed=1, psf=MOFFAT_25),
+    # the same workload with its stated sampling: midpoint + 3 x 3 within 2 px of the centre
+    "lm_c0center_seed2": dict(size=128, seed=2, psf=MOFFAT_25, sampling_mode="midpoint_center"),
 }
+
+
+def center_supersample(model, radius=2.0, quad_level=3):
+    """Give a reference model the sampling "midpoint_center" by wrapping its ``_sample_init``:
+    the reference's own midpoint sampling (models/_model_methods.py:84-98), with the pixels whose
+    centres lie within ``radius`` pixels of the model centre replaced by the reference's own
+    ``single_quad_integrate`` (utils/operations.py:123-147) at ``quad_level``.  The model keeps
+    integrate_mode "none", so the integrated image is this deep image.  (A squared distance up
+    to radius^2 + 1e-6 counts as inside, so pixel centres exactly on the circle stay in.)"""
+    import torch
+    from astrophot import AP_config
+    from astrophot.utils.operations import single_quad_integrate
+
+    plain = model._sample_init
+
+    def _sample_init(image, parameters, center):
+        reference, deep = plain(image=image, parameters=parameters, center=center)
+        Coords = image.get_coordinate_meshgrid()
+        X, Y = Coords - center[..., None, None]
+        Pinv = torch.linalg.inv(image.header.pixelscale)
+        di = Pinv[0, 0] * X + Pinv[0, 1] * Y
+        dj = Pinv[1, 0] * X + Pinv[1, 1] * Y
+        select = di * di + dj * dj <= radius * radius + 1e-6
+        res, _ = single_quad_integrate(X=X[select], Y=Y[select], image_header=image.header,
+                                       eval_brightness=model.evaluate_model, eval_parameters=parameters,
+                                       dtype=AP_config.ap_dtype, device=AP_config.ap_device, quad_level=quad_level)
+        deep[select] = res
+        return reference, deep
+
+    model._sample_init = _sample_init
+    return model
 
 
 # --------------------------------------------------------------------------
@@ -217,7 +272,11 @@ def ref_component(ap, case, target, name):
     model_type = {"sersic": "sersic galaxy model", "exponential": "exponential galaxy model"}[case["kind"]]
     kw = dict(case["knobs"])
     params = {k: (list(v) if isinstance(v, (list, tuple)) else v) for k, v in case["params"].items()}
-    return ap.models.AstroPhot_Model(name=name, model_type=model_type, target=target, parameters=params, **kw)
+    center = kw.get("sampling_mode") == "midpoint_center"
+    if center:
+        kw["sampling_mode"] = "midpoint"
+    m = ap.models.AstroPhot_Model(name=name, model_type=model_type, target=target, parameters=params, **kw)
+    return center_supersample(m) if center else m
 
 
 def run_render_case(ap, key, case):
@@ -273,21 +332,26 @@ def make_lm_data(ap, case):
     spec = synthetic.c0_stamp(case["seed"], size=case["size"])
     psf = psf_array(case["psf"])
     target = ap.image.Target_Image(data=np.zeros((spec.ny, spec.nx)), pixelscale=1.0, psf=psf)
-    group = build_lm_group(ap, target, spec.truth, f"truth {case['seed']} {case['size']}")
+    group = build_lm_group(ap, target, spec.truth, f"truth {case['seed']} {case['size']}",
+                           case.get("sampling_mode", "midpoint"))
     truth_img = group().data.detach().cpu().numpy()
     data, weight = synthetic.add_noise(truth_img, spec.seed)
     return spec, psf, truth_img, data, weight
 
 
-def build_lm_group(ap, target, vals, name):
+def build_lm_group(ap, target, vals, name, sampling_mode="midpoint"):
     cx, cy, q, PA, n, Re, Ie = [float(v) for v in vals]
+    kw = {"integrate_mode": "none"} if sampling_mode == "midpoint_center" else {}
     gal = ap.models.AstroPhot_Model(
         name=f"{name} gal",
         model_type="sersic galaxy model",
         target=target,
         psf_mode="full",
         parameters={"center": [cx, cy], "q": q, "PA": PA, "n": n, "Re": Re, "Ie": Ie},
+        **kw,
     )
+    if sampling_mode == "midpoint_center":
+        center_supersample(gal)
     sky = ap.models.AstroPhot_Model(
         name=f"{name} sky",
         model_type="flat sky model",
@@ -303,7 +367,7 @@ def build_lm_group(ap, target, vals, name):
 def run_lm_case(ap, key, case):
     spec, psf, truth_img, data, weight = make_lm_data(ap, case)
     target = ap.image.Target_Image(data=data, pixelscale=1.0, psf=psf, variance=1.0 / weight)
-    group = build_lm_group(ap, target, spec.init, f"fit {key}")
+    group = build_lm_group(ap, target, spec.init, f"fit {key}", case.get("sampling_mode", "midpoint"))
     rep0 = group.parameters.vector_representation().detach().cpu().numpy().copy()
     res = ap.fit.LM(group, initial_state=rep0).fit()
     return dict(
@@ -756,6 +820,16 @@ def run_auxpsf_group_case(ap, key, case):
 def main():
     ap = import_reference()
     only = sys.argv[1] if len(sys.argv) > 1 else None
+    if only == "center":
+        for key in ("sersic_psf_center", "sersic_nopsf_center"):
+            out = run_render_case(ap, key, RENDER_CASES[key])
+            np.savez_compressed(os.path.join(HERE, f"render_{key}.npz"), **out)
+            print("render", key, out["model"].shape, float(out["model"].sum()))
+        for key in ("lm_c0center_seed2",):
+            out = run_lm_case(ap, key, LM_CASES[key])
+            np.savez_compressed(os.path.join(HERE, f"{key}.npz"), **out)
+            print("lm", key, len(out["loss_history"]), out["loss_history"], str(out["message"]))
+        return
     if only == "auxpsf":
         for key, case in AUXPSF_CASES.items():
             out = run_auxpsf_case(ap, key, case)

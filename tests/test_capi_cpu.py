@@ -96,6 +96,19 @@ def test_batch_create_rejects_bad_input(N, shapes, psfs, kw, code):
     assert not h.value
 
 
+def test_midpoint_center_options(N):
+    """The centre-supersampling mode: planned with integrate_mode none, refused with the
+    threshold integration (which it replaces) and with a negative radius."""
+    opts = N.make_options(sampling_mode="midpoint_center", integrate_mode="none", psf_mode="full")
+    rc, h = _create(N, [(64, 64)], [(25, 25)], opts)
+    assert rc == 0
+    N.lib().ap_batch_destroy(h)
+    opts.integrate_mode = 1  # threshold
+    assert _create(N, [(64, 64)], [(25, 25)], opts)[0] == N.AP_ERR_UNSUPPORTED
+    opts = N.make_options(sampling_mode="midpoint_center", integrate_mode="none", center_radius=-1.0)
+    assert _create(N, [(64, 64)], None, opts)[0] == N.AP_ERR_ARG
+
+
 def test_sampling_modes_without_curvature_accept_tiny_windows(N):
     rc, h = _create(N, [(1, 1)], None, N.make_options(sampling_mode="quad:3"))
     assert rc == 0

@@ -176,16 +176,6 @@ def lm_case_problem(d):
     return GroupProblem([gal, sky], Window.from_scale(size, size), PSF(d["psf"]), d["data"], d["weight"])
 
 
-def parameter_sigma(d):
-    """1-sigma statistical uncertainty of the reference's fitted representation vector:
-    sqrt(diag((J^T W J)^-1)) from the oracle's Jacobian at that solution."""
-    prob = lm_case_problem(d)
-    J = prob.jacobian(d["res"])
-    W = d["weight"].reshape(-1)
-    H = J.T @ (W[:, None] * J)
-    return np.sqrt(np.diag(np.linalg.inv(H)))
-
-
 @pytest.mark.parametrize("name", cases.lm_case_names())
 @pytest.mark.parametrize("graph", [False, True])
 def test_lm_matches_reference(N, name, graph):
@@ -198,7 +188,9 @@ def test_lm_matches_reference(N, name, graph):
 
     d = cases.load_lm(name)
     size = d["spec"]["size"]
-    opts = N.make_options(profile="sersic", psf_mode="full", free_mask=0x7F, has_sky=True)
+    sampling = d["spec"].get("sampling_mode", "midpoint")
+    opts = N.make_options(profile="sersic", psf_mode="full", free_mask=0x7F, has_sky=True, sampling_mode=sampling,
+                          integrate_mode="none" if sampling == "midpoint_center" else "threshold")
     b = N.StampBatch([(size, size)], [(25, 25)], N.scale_geometry(1), opts)
     fixed = torch.tensor(np.r_[d["init"], 0.0][None, :])
     state, chi2, iters, status = b.lm_fit(
@@ -328,6 +320,8 @@ def test_option_errors(N):
         N.make_options(sampling_mode="bogus")
     with pytest.raises(SpecificationConflict):
         N.make_options(integrate_mode="full")
+    with pytest.raises(SpecificationConflict):  # the centre supersampling replaces the integration
+        N.make_options(sampling_mode="midpoint_center", integrate_mode="threshold")
     with pytest.raises(RuntimeError):
         N.StampBatch([(10, 10)], [(4, 4)], N.scale_geometry(1), N.make_options(psf_mode="full"))
 

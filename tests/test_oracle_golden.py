@@ -87,12 +87,16 @@ def test_group_with_sky_matches_reference(tag):
 def lm_problem(d):
     size = d["spec"]["size"]
     cx, cy, q, PA, n, Re, Ie = d["init"]
-    gal = Component("sersic", {"center": [cx, cy], "q": q, "PA": PA, "n": n, "Re": Re, "Ie": Ie}, psf_mode="full")
+    knobs = {}
+    if d["spec"].get("sampling_mode") == "midpoint_center":
+        knobs = dict(sampling_mode="midpoint_center", integrate_mode="none")
+    gal = Component("sersic", {"center": [cx, cy], "q": q, "PA": PA, "n": n, "Re": Re, "Ie": Ie}, psf_mode="full",
+                    **knobs)
     sky = Component("flat_sky", {"F": 0.0}, locked=("F",))
     return GroupProblem([gal, sky], Window.from_scale(size, size), PSF(d["psf"]), d["data"], d["weight"])
 
 
-@pytest.mark.parametrize("name", [n for n in cases.lm_case_names() if n == "lm_64"])
+@pytest.mark.parametrize("name", [n for n in cases.lm_case_names() if n in ("lm_64", "lm_c0center_seed2")])
 def test_lm_trajectory_matches_reference(name):
     d = cases.load_lm(name)
     prob = lm_problem(d)
