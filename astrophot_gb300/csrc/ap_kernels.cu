@@ -13,6 +13,7 @@
 //   chi2, hess, grad, rpp astrophot/fit/lm.py:374-406
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 
 #include "ap_internal.h"
 
@@ -1590,8 +1591,17 @@ cudaError_t launch_eval_setup(const BatchArgs& b, const double* params, int64_t 
   return cudaGetLastError();
 }
 
+// The limit on the convolve pass's dynamic shared memory is a property of the kernel on the
+// current device, shared by every batch: it is only ever raised (per device), so a batch bound
+// later with smaller kernels never lowers it below what an earlier batch launches with.
 cudaError_t set_conv_smem(size_t bytes) {
-  cudaError_t e = cudaSuccess;
+  static std::mutex mu;
+  static size_t raised[64] = {0};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(mu);
+  if (dev >= 0 && dev < 64 && bytes <= raised[dev]) return cudaSuccess;
   const int nb = (int)bytes;
   auto set = [&](const void* f) {
     const cudaError_t r = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, nb);
@@ -1600,6 +1610,7 @@ cudaError_t set_conv_smem(size_t bytes) {
   set((const void*)k_conv<0>); set((const void*)k_conv<1>); set((const void*)k_conv<2>);
   set((const void*)k_conv<3>); set((const void*)k_conv<4>); set((const void*)k_conv<5>);
   set((const void*)k_conv<6>); set((const void*)k_conv<7>); set((const void*)k_conv<8>);
+  if (e == cudaSuccess && dev >= 0 && dev < 64) raised[dev] = bytes;
   return e;
 }
 

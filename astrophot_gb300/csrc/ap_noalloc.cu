@@ -13,12 +13,18 @@
 //   - At most AP_NOALLOC_SCRATCH_BYTES (8 MiB) of scratch: working windows up to about
 //     80,000 pixels (e.g. a 256 x 256 stamp with a 21 x 21 PSF).  Larger stamps are rejected
 //     with AP_ERR_WORKSPACE before any device work is queued.
+//   - Stamp sides up to 65,536 pixels and PSF sides up to 4,095 are accepted (larger ones are
+//     rejected with AP_ERR_ARG before any arithmetic on them).
 //   - The first call on each device resolves the array's device address (cudaGetSymbolAddress,
 //     with that device current); make that first call before any stream capture.
+//   - The plan reaches the device as kernel arguments (no host-to-device copy), so a call only
+//     enqueues work: it does not wait for the stream.
+//   - The convolution is always direct (options.fft_min_kernel is not used).
 //   - Every call on a device shares the one array and it keeps the last call's contents, so
 //     calls that overlap on the GPU (different streams, or threads) race: serialise them.
 //   - Nothing here calls cudaMalloc, cudaFree or any allocating routine; the caller passes the
 //     parameters, the PSF and the output buffer.
+#include <atomic>
 #include <cmath>
 #include <cstring>
 
@@ -36,7 +42,40 @@ constexpr int64_t kAlignNA = 256;
 // device address comes from cudaGetSymbolAddress, once per device.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-void* g_scratch_addr[kMaxDevices];  // device address per device (nullptr until resolved)
+// device address per device (nullptr until resolved; every thread that resolves it stores the
+// same value)
+std::atomic<void*> g_scratch_addr[kMaxDevices];
+
+constexpr int32_t kMaxSide = 1 << 16;     // stamp side limit (keeps every index product in range)
+constexpr int32_t kMaxPsfSide = 4095;     // PSF side limit
+
+// The plan, passed by value, written into the scratch, and the state the render kernels expect
+// at zero cleared there (the array keeps the previous call's contents): the tile -> stamp tables
+// (a single stamp: index 0 everywhere), the evaluation slots, the counters.
+struct NoallocOffsets {
+  int64_t stamp, tab, wt, ot, evals, cnt, wctr;
+};
+
+__global__ void k_noalloc_setup(StampDev st, QuadTables T, NoallocOffsets o, char* ws) {
+  const int t = threadIdx.x;
+  if (t == 0) {
+    *reinterpret_cast<StampDev*>(ws + o.stamp) = st;
+    *reinterpret_cast<QuadTables*>(ws + o.tab) = T;
+  }
+  int32_t* wt = reinterpret_cast<int32_t*>(ws + o.wt);
+  int32_t* ot = reinterpret_cast<int32_t*>(ws + o.ot);
+  for (int i = t; i < st.ntw; i += blockDim.x) wt[i] = 0;
+  for (int i = t; i < st.nto; i += blockDim.x) ot[i] = 0;
+  uint32_t* ev = reinterpret_cast<uint32_t*>(ws + o.evals);
+  for (int i = t; i < (int)(2 * sizeof(EvalDev) / sizeof(uint32_t)); i += blockDim.x) ev[i] = 0u;
+  uint32_t* cnt = reinterpret_cast<uint32_t*>(ws + o.cnt);
+  if (t < 16) cnt[t] = 0u;
+  unsigned long long* wc = reinterpret_cast<unsigned long long*>(ws + o.wctr);
+  if (t < 4) wc[t] = 0ull;
+}
+static_assert(sizeof(StampDev) + sizeof(QuadTables) + sizeof(NoallocOffsets) + sizeof(char*) <= 4000,
+              "the plan must fit the kernel-argument space");
+static_assert(sizeof(EvalDev) % sizeof(uint32_t) == 0, "evaluation slots are cleared by words");
 
 int64_t na_align(int64_t v) { return (v + kAlignNA - 1) / kAlignNA * kAlignNA; }
 
@@ -119,10 +158,12 @@ extern "C" int ap_render_noalloc(int32_t nx, int32_t ny, int32_t psf_kx, int32_t
                                  const double* params, const float* psf, float* model,
                                  ap_stream_t stream) {
   if (!geometry || !options || !params || !model || nx <= 0 || ny <= 0) return AP_ERR_ARG;
+  if (nx > kMaxSide || ny > kMaxSide) return AP_ERR_ARG;
   if (!na_options_ok(options)) return AP_ERR_UNSUPPORTED;
   if (options->free_mask & ~0xff) return AP_ERR_ARG;
   const bool with_psf = options->psf_mode != AP_PSF_NONE;
-  if (with_psf && (!psf || psf_kx <= 0 || psf_ky <= 0 || psf_kx % 2 != 1 || psf_ky % 2 != 1))
+  if (with_psf && (!psf || psf_kx <= 0 || psf_ky <= 0 || psf_kx % 2 != 1 || psf_ky % 2 != 1 ||
+                   psf_kx > kMaxPsfSide || psf_ky > kMaxPsfSide))
     return AP_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
 
@@ -251,25 +292,18 @@ extern "C" int ap_render_noalloc(int32_t nx, int32_t ny, int32_t psf_kx, int32_t
   // ---- device address of the scratch, once per device ----------------------------------------
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return AP_ERR_CUDA;
-  if (!g_scratch_addr[dev]) {
-    void* addr = nullptr;
+  void* addr = g_scratch_addr[dev].load();
+  if (!addr) {
     if (cudaGetSymbolAddress(&addr, g_noalloc_scratch) != cudaSuccess || !addr) return AP_ERR_CUDA;
-    g_scratch_addr[dev] = addr;
+    g_scratch_addr[dev].store(addr);
   }
-  char* ws = (char*)g_scratch_addr[dev];
+  char* ws = (char*)addr;
 
-  // ---- tables and zeroed state into the scratch ---------------------------------------------
-  if (cudaMemcpyAsync(ws + o_stamp, &st, sizeof(st), cudaMemcpyHostToDevice, s) != cudaSuccess ||
-      cudaMemcpyAsync(ws + o_tab, &T, sizeof(T), cudaMemcpyHostToDevice, s) != cudaSuccess ||
-      // tile -> stamp tables: a single stamp, index 0 everywhere
-      cudaMemsetAsync(ws + o_wt, 0, sizeof(int32_t) * st.ntw, s) != cudaSuccess ||
-      cudaMemsetAsync(ws + o_ot, 0, sizeof(int32_t) * st.nto, s) != cudaSuccess ||
-      // state the kernels expect at zero (the array keeps the previous call's contents)
-      cudaMemsetAsync(ws + o_evals, 0, sizeof(EvalDev) * 2, s) != cudaSuccess ||
-      cudaMemsetAsync(ws + o_cnt, 0, sizeof(uint32_t) * 16, s) != cudaSuccess ||
-      cudaMemsetAsync(ws + o_wctr, 0, sizeof(unsigned long long) * 4, s) != cudaSuccess)
-    return AP_ERR_CUDA;
-  if (conv_smem > 48 * 1024 && set_conv_smem(200 * 1024) != cudaSuccess) return AP_ERR_CUDA;
+  // ---- plan and zeroed state into the scratch (kernel arguments: nothing copied from host) ----
+  const NoallocOffsets no{o_stamp, o_tab, o_wt, o_ot, o_evals, o_cnt, o_wctr};
+  k_noalloc_setup<<<1, 256, 0, s>>>(st, T, no, ws);
+  if (cudaGetLastError() != cudaSuccess) return AP_ERR_CUDA;
+  if (conv_smem > 48 * 1024 && set_conv_smem(conv_smem) != cudaSuccess) return AP_ERR_CUDA;
 
   BatchArgs A{};
   std::memset(&A, 0, sizeof(A));

@@ -327,9 +327,13 @@ int ap_fma_probe(float* scratch, int32_t iters, int32_t blocks, ap_stream_t stre
  * ap_batch_create); params[8] (value space), psf[psf_ky * psf_kx] (NULL without a PSF) and
  * model[ny * nx] are device pointers.  Working windows that need more than
  * AP_NOALLOC_SCRATCH_BYTES of scratch (about 80,000 pixels, e.g. 256 x 256 with a 21 x 21
- * PSF) are rejected with AP_ERR_WORKSPACE.  The first call on each device resolves the
- * array's address; make it before any stream capture.  All calls on a device share the
- * array, so calls that overlap on the GPU race.  Calls no cudaMalloc / cudaFree. */
+ * PSF) are rejected with AP_ERR_WORKSPACE, and sides beyond 65,536 (PSF sides beyond 4,095) with
+ * AP_ERR_ARG.  The plan reaches the device as kernel arguments, so a call only enqueues work.
+ * Sersic and exponential profiles, sampling modes midpoint / simpsons / quad / trapezoid; the
+ * convolution is always direct (options.fft_min_kernel is not used).  The first call on each
+ * device resolves the array's address; make it before any stream capture.  All calls on a
+ * device share the array, so calls that overlap on the GPU race.  Calls no cudaMalloc /
+ * cudaFree. */
 #define AP_NOALLOC_SCRATCH_BYTES ((size_t)8 << 20)
 int ap_render_noalloc(int32_t nx, int32_t ny, int32_t psf_kx, int32_t psf_ky,
                       const double* geometry, const ap_options* options, const double* params,

@@ -81,8 +81,11 @@ def test_sky_first_group_keeps_vector_order(ap):
 def lm_target(ap, d, tag):
     tar = ap.image.Target_Image(data=d["data"], pixelscale=1.0, psf=d["psf"], variance=1.0 / d["weight"])
     cx, cy, q, PA, n, Re, Ie = d["init"]
+    kw = {}
+    if d["spec"].get("sampling_mode") == "midpoint_center":
+        kw = dict(sampling_mode="midpoint_center", integrate_mode="none")
     gal = ap.models.AstroPhot_Model(name=f"lm gal {tag}", model_type="sersic galaxy model", target=tar, psf_mode="full",
-                                    parameters={"center": [cx, cy], "q": q, "PA": PA, "n": n, "Re": Re, "Ie": Ie})
+                                    parameters={"center": [cx, cy], "q": q, "PA": PA, "n": n, "Re": Re, "Ie": Ie}, **kw)
     sky = ap.models.AstroPhot_Model(name=f"lm sky {tag}", model_type="flat sky model", target=tar,
                                     parameters={"F": {"value": 0.0, "locked": True}})
     sky.initialize()
