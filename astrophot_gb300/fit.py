@@ -225,7 +225,14 @@ class BatchLM:
         self.kwargs = kwargs
 
     def fit(self):
-        _run(self.fits, self.kwargs)
+        # one device run per group of models that share their options (sampling, integration,
+        # PSF mode and fitted parameters); most batches are one group
+        groups = {}
+        for f in self.fits:
+            key = (bytes(f.struct.options()), f.struct.gal is not None and f.struct.gal.psf_mode == "full")
+            groups.setdefault(key, []).append(f)
+        for fits in groups.values():
+            _run(fits, self.kwargs)
         return self
 
     @property

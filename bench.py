@@ -176,11 +176,14 @@ def _oracle_fit_full(args, knobs=None):
 
 def value_rel_diff(got, ref):
     """Relative difference of fitted value-space vectors [cx, cy, q, PA, n, Re, Ie]: |d| / |ref|,
-    except PA, whose difference is taken modulo pi (the same orientation) and divided by pi."""
+    except PA, whose difference is taken modulo pi (the same orientation) and divided by pi, and
+    Ie (log10 of the brightness), compared as the relative difference of the brightness
+    10^Ie, |d Ie| ln 10."""
     got, ref = np.asarray(got, dtype=np.float64)[:7], np.asarray(ref, dtype=np.float64)[:7]
     d = np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300)
     dpa = (got[3] - ref[3] + np.pi / 2) % np.pi - np.pi / 2
     d[3] = abs(dpa) / np.pi
+    d[6] = abs(got[6] - ref[6]) * math.log(10.0)
     return d
 
 
@@ -219,7 +222,8 @@ def oracle_parity(jobs, gpu_chi2, gpu_values, gpu_messages, processes, fit=None)
         "oracle_messages": ostat,
         "gpu_messages": gstat,
         "oracle_mean_iterations": float(np.mean([r[1] for r in res])),
-        "params_rule": "value-space [cx, cy, q, PA, n, Re, Ie], |d| / |ref|; PA difference modulo pi over pi",
+        "params_rule": "value-space [cx, cy, q, PA, n, Re, Ie], |d| / |ref|; PA difference modulo pi over pi; "
+                       "Ie as the relative brightness |d Ie| ln 10",
     }
     cpu = {"value": len(jobs) / wall, "unit": "fits/s", "cores": processes, "kind": "port"}
     return parity, cpu
