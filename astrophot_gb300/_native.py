@@ -113,6 +113,7 @@ EXPORTS = [
     ("ap_batch_offsets", [_P, _PI64, _PI64]),
     ("ap_batch_bind", [_P, _P, _I64, _P]),
     ("ap_batch_set_threshold_numel", [_P, _PD]),
+    ("ap_batch_set_threshold_window", [_P, _PI32]),
     ("ap_render", [_P, _P, _P, _P, _P]),
     ("ap_jacobian", [_P, _P, _P, _P, _P, _I32, _P]),
     ("ap_render_psf_derivative", [_P, _P, _P, _P, _P, _P]),
@@ -454,6 +455,12 @@ class StampBatch:
     def set_grid(self, blocks_per_sm):
         arr = (ctypes.c_int32 * 4)(*[int(blocks_per_sm[k]) for k in self.GRID_KNOBS])
         check(self.lib.ap_batch_set_grid(self.handle, arr), "ap_batch_set_grid")
+
+    def set_threshold_window(self, windows):
+        """Window [x0, y0, nx, ny] per stamp (working-pixel indices) whose samples an exponential
+        stamp's integration threshold sums (see ap_batch_set_threshold_window)."""
+        arr = np.ascontiguousarray(np.broadcast_to(np.asarray(windows, dtype=np.int32), (self.n, 4)))
+        check(self.lib.ap_batch_set_threshold_window(self.handle, arr.ctypes.data_as(_PI32)), "threshold window")
 
     def set_threshold_numel(self, numel):
         """Pixel count of each stamp's integration threshold (see ap_batch_set_threshold_numel)."""

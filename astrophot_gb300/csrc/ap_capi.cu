@@ -489,6 +489,28 @@ int ap_batch_set_threshold_numel(ap_batch* b, const double* numel) {
   return AP_OK;
 }
 
+int ap_batch_set_threshold_window(ap_batch* b, const int32_t* windows) {
+  if (!b || !windows) return AP_ERR_ARG;
+  for (int i = 0; i < b->n; ++i)
+    if (windows[4 * i + 2] < 0 || windows[4 * i + 3] < 0) return AP_ERR_ARG;
+  int any = 0;
+  for (int i = 0; i < b->n; ++i) {
+    StampDev& st = b->stamps[i];
+    st.gw_x0 = windows[4 * i + 0];
+    st.gw_y0 = windows[4 * i + 1];
+    st.gw_nx = windows[4 * i + 2];
+    st.gw_ny = windows[4 * i + 3];
+    if (st.gw_nx == 0 || st.gw_ny == 0) st.gw_nx = st.gw_ny = 0;
+    any |= st.gw_nx > 0;
+  }
+  b->args.thr_window = any;
+  if (b->bound) {
+    const Layout& L = b->L;
+    return check_cuda(cudaMemcpy(b->ws + L.stamps, b->stamps.data(), sizeof(StampDev) * b->n, cudaMemcpyHostToDevice));
+  }
+  return AP_OK;
+}
+
 int ap_batch_bind(ap_batch* b, void* workspace, int64_t bytes, ap_stream_t stream) {
   if (!b || !workspace) return AP_ERR_ARG;
   if (bytes < b->L.total) return AP_ERR_WORKSPACE;

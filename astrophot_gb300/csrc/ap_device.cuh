@@ -123,6 +123,9 @@ struct StampDev {
   int32_t fft_nx, fft_ny;
   int64_t fft_off;
   int64_t pre_off;
+  // window whose samples the exponential / PSF-profile integration threshold sums, in this
+  // stamp's working-pixel indices (x0, y0, nx, ny; nx = 0: the stamp's own working window)
+  int32_t gw_x0, gw_y0, gw_nx, gw_ny;
 };
 
 struct EvalDev {
@@ -179,6 +182,7 @@ struct BatchArgs {
   int32_t has_sky;
   int32_t n_work_tiles, n_out_tiles;
   int32_t max_kp2;      // largest kpy * kpx
+  int32_t thr_window;   // some stamp sums its integration threshold over its gw_* window
   float tolerance;
   float center_r2;      // AP_SAMPLING_MIDPOINT_CENTER: squared radius (+ 1e-6) in pixels
   double tolerance64, softening64;

@@ -522,7 +522,7 @@ __device__ void sample_tile(const BatchArgs& b, const EvalF& e, const DeltaF& d,
       write_diff_base(b, ops, slot, p, deep, ddeep,
                       (b.sampling == AP_SAMPLING_MIDPOINT_CENTER && !mid_only) ? kCodeLevel1 : 0u);
   }
-  if (b.kind != AP_PROFILE_SERSIC && b.integrate == AP_INTEGRATE_THRESHOLD) {
+  if (b.kind != AP_PROFILE_SERSIC && b.integrate == AP_INTEGRATE_THRESHOLD && st.gw_nx == 0) {
     // sum(deep) for the default _integrate_reference (models/_model_methods.py:151-152)
     float v = warp_sum(valid ? deep : 0.f);
     __shared__ float sh[kTile * kTile / 32];
@@ -587,6 +587,43 @@ __device__ __forceinline__ void stamp_threshold(const BatchArgs& b, const StampD
   thr64 = e.thresh64;
   // the exponential's mean comes from FP32 samples: uncertain at the 1e-6 level
   thr_err = (b.kind == AP_PROFILE_SERSIC) ? 2.f * kEps * thr : 2e-6f * thr;
+}
+
+// sum(deep) over a stamp's threshold window (gw_*) instead of its own working window: a source
+// of a group is evaluated by the reference on the group's working window, whose samples its
+// default _integrate_reference sums (models/_model_methods.py:151-152, model_object.py:290-296),
+// while the render keeps to the source's own window.  Grid (2 n_stamps, row blocks); each
+// thread sums a row's samples in FP32 (a handful) and the rows in FP64.
+template <bool EXT>
+__global__ void __launch_bounds__(256) k_window_msum(BatchArgs b) {
+  const int t = blockIdx.x;
+  if (t >= 2 * b.n_stamps) return;
+  const EvalDev& ed = b.evals[t];
+  if (!ed.ops) return;
+  const int s = t >> 1;
+  const StampDev& st = b.stamps[s];
+  if (st.gw_nx <= 0) return;
+  const EvalF e = load_evalf(st, ed);
+  const DeltaF d{};
+  double acc = 0.0;
+  for (int r = blockIdx.y; r < st.gw_ny; r += gridDim.y) {
+    float row = 0.f;
+    for (int c = threadIdx.x; c < st.gw_nx; c += blockDim.x) {
+      float deep, g[NGRAD], refsub, errb, dd;
+      sample_pixel<false, EXT, false>(b, e, d, st.gw_x0 + c, st.gw_y0 + r, false, deep, g, refsub, errb, dd);
+      row += deep;
+    }
+    acc += (double)row;
+  }
+  acc = warp_sum_d(acc);
+  __shared__ double sh[8];
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += sh[w];
+    atomicAdd(&b.mean_acc[t], tot);
+  }
 }
 
 // Exponential threshold: sampling_tolerance * sum(deep) / numel, once per (stamp, slot).
@@ -1644,8 +1681,16 @@ cudaError_t launch_render_pass(const BatchArgs& b, const ConvIO& io, size_t conv
     k_sample<true><<<sgrid, kTile * kTile, 0, s>>>(b);
   else
     k_sample<false><<<sgrid, kTile * kTile, 0, s>>>(b);
-  if (b.kind != AP_PROFILE_SERSIC && b.integrate == AP_INTEGRATE_THRESHOLD)
+  if (b.kind != AP_PROFILE_SERSIC && b.integrate == AP_INTEGRATE_THRESHOLD) {
+    if (b.thr_window) {
+      const dim3 wg(2 * b.n_stamps, 16);
+      if (ext)
+        k_window_msum<true><<<wg, 256, 0, s>>>(b);
+      else
+        k_window_msum<false><<<wg, 256, 0, s>>>(b);
+    }
     k_exp_threshold<<<(b.n_stamps * 2 + 127) / 128, 128, 0, s>>>(b);
+  }
   E(t);
   if (b.integrate == AP_INTEGRATE_THRESHOLD) {
     t = B(KC_SELECT);

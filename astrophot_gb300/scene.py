@@ -250,10 +250,10 @@ class Scene:
         self.jac = torch.zeros(max(jac_total, 1), dtype=torch.float32, device=dev)
 
         # model renders.  The reference evaluates a windowed source of a group on the group's
-        # window and keeps its own window.  A Sersic source is rendered on its own window with the
+        # window and keeps its own window.  Each source is rendered on its own window with the
         # group's working pixel count in its integration threshold, which gives the same pixels;
-        # an exponential source's threshold sums its samples over the whole group window, so it is
-        # rendered on the group window (in chunks of sources that share one plan).
+        # an exponential source's threshold also sums its samples over the whole group working
+        # window, which a separate sampling pass of the render takes (set_threshold_window).
         self._fwd_parts = []
         self.fwd_chunk = max(1, int(fwd_chunk))
         bx = by = 0
@@ -265,15 +265,19 @@ class Scene:
         for (kind, free), members in self.groups.items():
             fo = N.make_options(profile=kind, psf_mode="full" if psf is not None else "none",
                                 free_mask=sum(1 << sl for sl in _SLOTS_OF[kind]), has_sky=False, **opts_kw)
-            if kind == "sersic":
-                shapes, geoms = [], []
+            if kind in ("sersic", "exponential"):
+                shapes, geoms, gwin = [], [], []
                 for si in members:
                     (x0, x1), (y0, y1) = self._window(si)
                     shapes.append((x1 - x0, y1 - y0))
                     geoms.append(N.scale_geometry(1, self.scale, (self.origin[0] + x0 * self.scale,
                                                                   self.origin[1] + y0 * self.scale))[0])
+                    # the group's working window in this source's working-pixel indices
+                    gwin.append((-x0, -y0, self.nx + 2 * bx, self.ny + 2 * by))
                 fb = N.StampBatch(shapes, None if kpsf is None else [kpsf] * len(members), np.array(geoms), fo, dev)
                 fb.set_threshold_numel(group_numel)
+                if kind == "exponential":
+                    fb.set_threshold_window(np.array(gwin))
                 fpsf = None if psf is None else fb.pack_psf([self.psf_np] * len(members))
                 self._fwd_parts.append(dict(kind=kind, members=members, batch=fb, psf=fpsf, off=fwd_total,
                                             m=len(members), own=True))

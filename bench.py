@@ -887,6 +887,7 @@ def run_gpu_learned(args):
     if rank == 0 and not args.no_configs:
         line["single_stamp_c0"] = c0_block(args, dev)
         line["batched_cutouts"] = cutouts_block(args, dev)
+        line["bulge_disk_field"] = bulge_disk_block(args, dev)
     if rank == 0 and world == 1 and not args.no_cpu and args.cpu_sample > 0:
         from astrophot_gb300.transforms import rep_to_slots
 
@@ -1084,6 +1085,75 @@ def cutouts_block(args, dev):
         out["parity"] = par
         out["cpu_baseline"] = cpu
     return out
+
+
+def bulge_disk_block(args, dev):
+    """The adjoint configuration at its stated size: 500 Sersic bulge (n ~ U(2, 6)) + exponential
+    disk pairs sharing their centres (11 free parameters a pair, 5,500 in all) on a 2048 x 2048
+    image with a 65 x 65 Moffat PSF (FWHM 3 px, beta 3.5; the configuration gives no FWHM), sky
+    1.0, noise sqrt(model + 10), a window per pair.  Reports the render, the Jacobian + J^T W J,
+    the adjoint of the chi^2 (VJP with the PSF-convolved tiles recomputed, not stored), the
+    damped solve of the 5,500-parameter system and one LM iteration."""
+    import torch
+
+    from astrophot_gb300 import scene as SC
+    from astrophot_gb300 import synthetic
+
+    size = 2048
+    truth, init, windows, psf = synthetic.bulge_disk_field(args.seed)
+    zeros = np.zeros((size, size))
+    sc_t = SC.Scene(size, size, synthetic.bulge_disk_sources(truth, windows), psf, zeros, zeros + 1, sky=1.0,
+                    device=dev)
+    model = sc_t.forward(sc_t.representation()).cpu().numpy().astype(np.float64).reshape(size, size)
+    del sc_t
+    data, weight = synthetic.add_noise(model, args.seed)
+    sc = SC.Scene(size, size, synthetic.bulge_disk_sources(init, windows), psf, data, weight, sky=1.0, device=dev)
+    rep = sc.representation()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 3
+
+    def timed(fn):
+        fn()
+        fn()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            out = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps, out
+
+    fwd_ms, m = timed(lambda: sc.forward(rep))
+    g = (sc.weight.double() * (m.double() - sc.data.double())).float()
+    vjp_ms, _ = timed(lambda: sc.vjp(rep, g))
+
+    def jac_hess():
+        sc.jacobian(rep)
+        return sc.hess()
+
+    jac_ms, H = timed(jac_hess)
+    grad = sc.jt(sc.residual(m))
+    solve_ms, _ = timed(lambda: sc.solve(H, grad, 1.0))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lm = SC.SceneLM(sc, initial_state=rep, max_iter=1).fit()
+    torch.cuda.synchronize()
+    lm_s = time.perf_counter() - t0
+    return {
+        "workload": f"{len(truth)} bulge (Sersic n U(2,6)) + exponential disk pairs sharing centres on {size}x{size}, "
+        "65x65 Moffat (FWHM 3, beta 3.5), sky 1.0, noise sqrt(model + 10), a window per pair; "
+        f"{sc.P} parameters (centre shared: 11 a pair)",
+        "parameters": sc.P,
+        "window_pairs": sc.n_pairs,
+        "render_ms": fwd_ms,
+        "render_mpix_per_s": size * size / (fwd_ms * 1e-3) / 1e6,
+        "adjoint_vjp_ms": vjp_ms,
+        "jacobian_and_jtwj_ms": jac_ms,
+        "damped_solve_ms": solve_ms,
+        "lm_iteration_s": lm_s,
+        "chi2_ndf_start": float(lm.loss_history[0]),
+        "chi2_ndf_after_one_iteration": float(lm.loss_history[-1]),
+    }
 
 
 def crowded_block(args, dev):

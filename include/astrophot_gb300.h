@@ -152,6 +152,16 @@ int ap_batch_offsets(const ap_batch* batch, int64_t* out_offsets, int64_t* psf_o
  * pixel count gives the same pixels inside its window.  numel[n] > 0, host; may follow bind. */
 int ap_batch_set_threshold_numel(ap_batch* batch, const double* numel);
 
+/* The window whose samples an exponential (or PSF-profile) stamp's integration threshold sums,
+ * in place of its own working window: windows[n][4] = x0, y0, nx, ny in the stamp's working-pixel
+ * indices (x0, y0 may be negative; nx = 0 keeps the own window).  The reference evaluates a
+ * windowed source of a Group_Model on the group's working window (models/model_object.py:290-296)
+ * and its default _integrate_reference sums the samples there (models/_model_methods.py:151-152);
+ * with the group's working window here (and ap_batch_set_threshold_numel) the source renders on
+ * its own window with the same pixels, the sum taken by a separate sampling pass.  Host; may
+ * follow bind. */
+int ap_batch_set_threshold_window(ap_batch* batch, const int32_t* windows);
+
 /* Attach caller-owned device workspace and upload the plan's tables into it
  * (synchronous with respect to the host for the table upload). */
 int ap_batch_bind(ap_batch* batch, void* workspace, int64_t workspace_bytes, ap_stream_t stream);
