@@ -387,6 +387,8 @@ __device__ __forceinline__ Sample eval_profile(const EvalF& e, int kind, float X
 // expm1 by its Taylor series to x^9 (truncation below 3e-10); beyond, the MUFU log / exp,
 // whose absolute error of ~2e-7 is below 5e-7 of log1p and expm1 there.
 __device__ __forceinline__ float d_log1p(float x) {
+  // near convergence the arguments are tiny: three terms (truncation x^4/4 < 1e-12 relative)
+  if (fabsf(x) < 9.765625e-4f) return x * (1.f + x * (-0.5f + x * 0.33333334f));
   if (fabsf(x) < 0.5f) {
     const float u = __fdividef(x, 2.f + x), u2 = u * u;
     return 2.f * u * (1.f + u2 * (0.33333334f + u2 * (0.2f + u2 * (0.14285715f + u2 * (0.11111111f + u2 * 0.09090909f)))));
@@ -395,6 +397,7 @@ __device__ __forceinline__ float d_log1p(float x) {
 }
 
 __device__ __forceinline__ float d_expm1(float x) {
+  if (fabsf(x) < 9.765625e-4f) return x * (1.f + x * (0.5f + x * 0.16666667f));  // (x^4/24: < 1e-13)
   if (fabsf(x) < 0.5f)
     return x * (1.f + x * (0.5f + x * (0.16666667f + x * (0.041666668f + x * (0.008333334f + x * (1.3888889e-3f +
                x * (1.984127e-4f + x * (2.4801588e-5f + x * 2.7557319e-6f))))))));

@@ -131,6 +131,10 @@ __device__ void start_sub(const BatchArgs& b, const LMArgs& lm, int s, LMState& 
   for (int k = 0; k < P; ++k) xa[k] = S.x[k] + 0.1 * S.h[k];
   const int32_t dop = trials_as_diff(b, lm, s) ? OP_DIFF : 0;
   bool ok = write_eval(b, lm, s, 0, xa, OP_FWD | OP_RPP | dop);
+  // The reference renders x + 0.1 h for the geodesic term but uses it only when L > 1e-4 (the
+  // term is zero below, fit/lm.py:283-286) or with acceleration: skip that render there (the
+  // value-space check of x + 0.1 h, which can end the fit, is kept).
+  if (!(S.L > 1e-4) && lm.acceleration == 0.0) lm.ops_next[s * 2 + 0] = 0;
   if (lm.acceleration == 0.0) {
     double xb[NPARAM];
     for (int k = 0; k < P; ++k) xb[k] = S.x[k] + S.h[k];
