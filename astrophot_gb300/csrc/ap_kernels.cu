@@ -1127,6 +1127,183 @@ __device__ void level23_pixel(const BatchArgs& b, int slot, int s, int64_t p, in
   }
 }
 
+// Levels 2 and 3 of grid_integrate for forward evaluations (plain or difference to the base),
+// packed: a warp takes kPack queued pixels and spreads their G2 = gridding^2 level-2 sub-pixels
+// (and then the G2 level-3 sub-pixels of every sub-pixel flagged for refinement) over all 32
+// lanes, one sub-pixel's quadrature per lane, instead of one pixel per warp with G2 of 32 lanes
+// busy.  Each sub-pixel's result goes to shared memory and is summed per pixel in sub-pixel
+// order by one lane, so a pixel's value does not depend on which pixels share its warp.
+constexpr int kPack = 16;
+constexpr int kPackWarps = 4;  // 128-thread blocks
+
+struct PackSmem {
+  int64_t ent[kPack];
+  uint32_t mask[kPack];   // level-3 flags of each pixel's sub-pixels
+  int32_t pre[kPack + 1]; // exclusive prefix of the flag counts
+  float res[kPack * kMaxGrid * kMaxGrid], dres[kPack * kMaxGrid * kMaxGrid];
+  float res3[kPack * kMaxGrid * kMaxGrid], dres3[kPack * kMaxGrid * kMaxGrid];
+};
+
+// one level-2 or level-3 sub-pixel of queued pixel P (sub-pixel m, and sub-sub-pixel k >= 0 at
+// level 3): its quadrature, plain or as a difference
+template <int QC>
+__device__ __forceinline__ QuadResult packed_quad(const BatchArgs& b, int64_t ent, int m, int k, bool& diff,
+                                                  const StampDev*& stp, const EvalDev*& ep, int& i, int& j) {
+  const QuadTables& T = *b.tables;
+  const int slot = (int)(ent >> 62);
+  const int s = (int)((ent >> 32) & 0x3fffffff);
+  const int64_t p = ent & 0xffffffffll;
+  const StampDev& st = b.stamps[s];
+  const EvalDev& e = b.evals[s * 2 + slot];
+  stp = &st;
+  ep = &e;
+  const EvalF f = load_evalf(st, e);
+  i = (int)(p % st.wnx);
+  j = (int)(p / st.wnx);
+  const float ginv = 1.f / (float)T.gridding;
+  float ci = (float)(i - f.cix) + T.gxf[m], cj = (float)(j - f.cjy) + T.gyf[m];
+  float ig = ginv, area = ginv * ginv;
+  if (k >= 0) {
+    ci += T.gxf[k] * ginv;
+    cj += T.gyf[k] * ginv;
+    ig = ginv * ginv;
+    area = area * area;
+  }
+  diff = (e.ops & OP_DIFF) != 0;
+  if (diff) {
+    const DeltaF d = load_deltaf(e);
+    return quad_lane<false, QC, false, true>(b, f, d, ci, cj, ig, area);
+  }
+  const DeltaF d{};
+  return quad_lane<false, QC, false, false>(b, f, d, ci, cj, ig, area);
+}
+
+template <int QC>
+__device__ void level23_packed(const BatchArgs& b, PackSmem& S, int np, int lane, unsigned long long& samples,
+                               int& n64) {
+  const QuadTables& T = *b.tables;
+  const int G2 = T.gridding * T.gridding;
+  const int Q2 = QC > 0 ? QC * QC : T.quad_level * T.quad_level;
+  if (lane < kPack) S.mask[lane] = 0u;
+  __syncwarp();
+  // level 2: np * G2 sub-pixels over the lanes
+  const int items = np * G2;
+  for (int base = 0; base < items; base += 32) {
+    const int it = base + lane;
+    if (it < items) {
+      const int P = it / G2, m = it - P * G2;
+      bool diff;
+      const StampDev* st;
+      const EvalDev* e;
+      int i, j;
+      const QuadResult r = packed_quad<QC>(b, S.ent[P], m, -1, diff, st, e, i, j);
+      S.res[it] = r.res;
+      S.dres[it] = r.dres;
+      if (b.max_depth > 2 && decide<false>(b, *st, *e, r, e->thresh * (float)G2, i, j, m, n64))
+        atomicOr(&S.mask[P], 1u << m);
+    }
+  }
+  __syncwarp();
+  // flagged sub-pixels, enumerated pixel by pixel in sub-pixel order
+  const int cnt = lane < np ? __popc(S.mask[lane]) : 0;
+  int pre = cnt;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, pre, o);
+    if (lane >= o) pre += v;
+  }
+  const int total = __shfl_sync(0xffffffffu, pre, 31);
+  if (lane < np) S.pre[lane] = pre - cnt;
+  if (lane == 0) S.pre[np] = total;
+  __syncwarp();
+  samples += (unsigned long long)(items + total * G2) * (unsigned long long)Q2;
+  auto flagged = [&](int fi, int& P, int& m) {
+    P = 0;
+    while (P + 1 < np && S.pre[P + 1] <= fi) ++P;
+    unsigned msk = S.mask[P];
+    for (int r = fi - S.pre[P]; r > 0; --r) msk &= msk - 1u;
+    m = __ffs(msk) - 1;
+  };
+  // level 3 in batches of kPack flagged sub-pixels, G2 sub-sub-pixels each over the lanes
+  for (int f0 = 0; f0 < total; f0 += kPack) {
+    const int nf = min(kPack, total - f0);
+    const int tasks = nf * G2;
+    for (int base = 0; base < tasks; base += 32) {
+      const int it = base + lane;
+      if (it < tasks) {
+        const int q = it / G2, k = it - q * G2;
+        int P, m;
+        flagged(f0 + q, P, m);
+        bool diff;
+        const StampDev* st;
+        const EvalDev* e;
+        int i, j;
+        const QuadResult r = packed_quad<QC>(b, S.ent[P], m, k, diff, st, e, i, j);
+        S.res3[it] = r.res;
+        S.dres3[it] = r.dres;
+      }
+    }
+    __syncwarp();
+    if (lane < nf) {
+      int P, m;
+      flagged(f0 + lane, P, m);
+      float v = 0.f, dv = 0.f;
+      for (int k = 0; k < G2; ++k) {
+        v += S.res3[lane * G2 + k];
+        dv += S.dres3[lane * G2 + k];
+      }
+      S.res[P * G2 + m] = v;
+      S.dres[P * G2 + m] = dv;
+    }
+    __syncwarp();
+  }
+  // each pixel: its sub-pixels summed in order
+  if (lane < np) {
+    float v = 0.f, dv = 0.f;
+    for (int m = 0; m < G2; ++m) {
+      v += S.res[lane * G2 + m];
+      dv += S.dres[lane * G2 + m];
+    }
+    const int64_t ent = S.ent[lane];
+    const int slot = (int)(ent >> 62);
+    const int s = (int)((ent >> 32) & 0x3fffffff);
+    const int64_t p = ent & 0xffffffffll;
+    const StampDev& st = b.stamps[s];
+    const int ops = b.evals[s * 2 + slot].ops;
+    write_deep(b, st, slot, p, v, nullptr, false);
+    if (ops & (OP_DIFF | OP_BASE)) write_diff_base(b, ops, slot, st.work_off + p, v, dv, code_split(S.mask[lane]));
+  }
+  __syncwarp();
+}
+
+__global__ void __launch_bounds__(kPackWarps * 32, 6) k_integrate_packed(BatchArgs b) {
+  __shared__ PackSmem smem[kPackWarps];
+  const int lane = threadIdx.x & 31;
+  PackSmem& S = smem[threadIdx.x >> 5];
+  const int64_t cap = (int64_t)2 * b.work_pixels;
+  const uint32_t n = min((uint32_t)b.counters[13], (uint32_t)cap);
+  unsigned long long samples = 0;
+  int n64 = 0;
+  while (true) {
+    uint32_t idx0 = 0;
+    if (lane == 0) idx0 = atomicAdd(&b.counters[14], (unsigned)kPack);
+    idx0 = __shfl_sync(0xffffffffu, idx0, 0);
+    if (idx0 >= n) break;
+    const int np = (int)min((uint32_t)kPack, n - idx0);
+    if (lane < np) S.ent[lane] = b.recheck[cap - 1 - (idx0 + lane)];
+    __syncwarp();
+    if (b.tables->quad_level == 3)
+      level23_packed<3>(b, S, np, lane, samples, n64);
+    else
+      level23_packed<0>(b, S, np, lane, samples, n64);
+  }
+  n64 = __reduce_add_sync(0xffffffffu, n64);
+  samples = __shfl_sync(0xffffffffu, samples, 0);
+  if (lane == 0) {
+    if (samples) atomicAdd(b.work_ctr + 1, samples);
+    if (n64) atomicAdd(&b.counters[6], (unsigned)n64);
+  }
+}
+
 // FWD = false: the Jacobian evaluations' pixels (front of the recheck buffer); FWD = true: the
 // forward evaluations' pixels (back of the buffer), plain or as differences to the base
 template <bool EXT, bool FWD>
@@ -1714,7 +1891,8 @@ cudaError_t launch_render_pass(const BatchArgs& b, const ConvIO& io, size_t conv
       k_level1<false><<<gi, 256, 0, s>>>(b);
       if (b.amb_cap > 0) k_level1_amb<false><<<nsm * 4, 256, 0, s>>>(b);
       k_integrate<false, false><<<gi, 256, 0, s>>>(b);
-      k_integrate<false, true><<<gf, 256, 0, s>>>(b);
+      // forward (plain or difference) pixels: sub-pixels packed over the lanes
+      k_integrate_packed<<<(unsigned)nsm * 6, kPackWarps * 32, 0, s>>>(b);
     }
     E(t);
   }
