@@ -139,6 +139,7 @@ EXPORTS = [
     ("ap_batch_kernel_times", [_P, _PD, _PI64]),
     ("ap_batch_work_counters", [_P, ctypes.POINTER(ctypes.c_uint64), _I32, _P]),
     ("ap_fma_probe", [_P, _I32, _I32, _P]),
+    ("ap_sample_probe", [_I32, _P, _I32, _I32, _P]),
     ("ap_batch_stats", [_P, _PI64]),
     ("ap_render_noalloc", [_I32, _I32, _I32, _I32, _PD, ctypes.POINTER(ApOptions), _P, _P, _P, _P]),
     ("ap_scene_forward", [_P, _P, _P, _P, ctypes.c_float, _I32, _I32, _P, _P]),
@@ -588,15 +589,38 @@ class StampBatch:
         return {k: (ms[i], n[i]) for i, k in enumerate(self.KERNEL_CLASSES)}
 
     def work_counters(self, reset=False):
-        out = (ctypes.c_uint64 * 4)()
+        out = (ctypes.c_uint64 * 6)()
         check(self.lib.ap_batch_work_counters(self.handle, out, 1 if reset else 0, _stream()), "work counters")
-        return {"conv_flops": out[0], "integrate_samples": out[1], "sample_samples": out[2]}
+        return {"conv_flops": out[0], "integrate_samples": out[1], "sample_samples": out[2],
+                "integrate_samples_diff": out[3], "integrate_samples_jacobian": out[4]}
 
     def stats(self):
         out = (ctypes.c_int64 * 5)()
         check(self.lib.ap_batch_stats(self.handle, out), "stats")
         return {"queue": out[0], "fp64_redecisions": out[1], "overflow": out[2], "rounds": out[3],
                 "fp64_integrate": out[4]}
+
+
+def sample_probe_rate(kind: int, iters=2048, blocks=None) -> float:
+    """Measured samples/s of the integration's sample arithmetic (:func:`ap_sample_probe`; kind
+    0 plain, 1 with partials, 2 as a difference) on this GPU."""
+    dev = torch.cuda.current_device()
+    nsm = torch.cuda.get_device_properties(dev).multi_processor_count
+    blocks = blocks or nsm * 8
+    scratch = torch.empty(blocks * 256, dtype=torch.float32, device="cuda")
+    L = lib()
+    s = _stream()
+    for _ in range(2):
+        check(L.ap_sample_probe(kind, _ptr(scratch), 32, blocks, s), "sample probe")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = 0.0
+    for _ in range(5):
+        e0.record()
+        check(L.ap_sample_probe(kind, _ptr(scratch), iters, blocks, s), "sample probe")
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, blocks * 256 * 4 * iters / (e0.elapsed_time(e1) * 1e-3))
+    return best
 
 
 def fma_probe_tflops(iters=4096, blocks=None) -> float:

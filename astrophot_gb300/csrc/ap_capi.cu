@@ -408,7 +408,7 @@ int ap_batch_create(ap_batch** out, int32_t n, const int32_t* nx, const int32_t*
   L.olist = take(sizeof(int64_t) * 2 * (int64_t)b->out_tiles.size());
   L.slist = take(sizeof(int32_t) * 2 * (int64_t)n);
   L.counters = take(sizeof(uint32_t) * 16);
-  L.work_ctr = take(sizeof(unsigned long long) * 4);
+  L.work_ctr = take(sizeof(unsigned long long) * 8);
   L.mean_acc = take(sizeof(double) * 2 * (int64_t)n);
   L.tile_acc = take(sizeof(double) * 2 * kNacc * (int64_t)b->out_tiles.size());
   L.acc = take(sizeof(double) * 2 * kNacc * (int64_t)n);
@@ -554,7 +554,7 @@ int ap_batch_bind(ap_batch* b, void* workspace, int64_t bytes, ap_stream_t strea
   rc = rc ? rc : check_cuda(cudaMemcpyAsync(ws + L.out_tiles, b->out_tiles.data(), sizeof(int32_t) * b->out_tiles.size(), cudaMemcpyHostToDevice, s));
   rc = rc ? rc : check_cuda(cudaMemcpyAsync(ws + L.tables, &b->tables, sizeof(QuadTables), cudaMemcpyHostToDevice, s));
   rc = rc ? rc : check_cuda(cudaMemsetAsync(ws + L.counters, 0, sizeof(uint32_t) * 16, s));
-  rc = rc ? rc : check_cuda(cudaMemsetAsync(ws + L.work_ctr, 0, sizeof(unsigned long long) * 4, s));
+  rc = rc ? rc : check_cuda(cudaMemsetAsync(ws + L.work_ctr, 0, sizeof(unsigned long long) * 8, s));
   rc = rc ? rc : check_cuda(cudaMemsetAsync(ws + L.evals, 0, sizeof(EvalDev) * 2 * b->n, s));
   if (A.n_fft > 0) {
     rc = rc ? rc : check_cuda(cudaMemcpyAsync(ws + L.fft_lists, b->fft_lists.data(),
@@ -1028,11 +1028,11 @@ int ap_batch_work_counters(ap_batch* b, uint64_t* out, int32_t reset, ap_stream_
   if (!b || !out) return AP_ERR_ARG;
   if (!b->bound) return AP_ERR_NOT_BOUND;
   cudaStream_t s = (cudaStream_t)stream;
-  unsigned long long c[4];
+  unsigned long long c[6];
   if (cudaMemcpyAsync(c, b->args.work_ctr, sizeof(c), cudaMemcpyDeviceToHost, s) != cudaSuccess)
     return AP_ERR_CUDA;
   if (cudaStreamSynchronize(s) != cudaSuccess) return AP_ERR_CUDA;
-  for (int k = 0; k < 4; ++k) out[k] = c[k];
+  for (int k = 0; k < 6; ++k) out[k] = c[k];
   if (reset && cudaMemsetAsync(b->args.work_ctr, 0, sizeof(c), s) != cudaSuccess) return AP_ERR_CUDA;
   return AP_OK;
 }
@@ -1040,6 +1040,11 @@ int ap_batch_work_counters(ap_batch* b, uint64_t* out, int32_t reset, ap_stream_
 int ap_fma_probe(float* scratch, int32_t iters, int32_t blocks, ap_stream_t stream) {
   if (!scratch || iters < 1 || blocks < 1) return AP_ERR_ARG;
   return check_cuda(launch_fma_probe(scratch, iters, blocks, (cudaStream_t)stream));
+}
+
+int ap_sample_probe(int32_t kind, float* scratch, int32_t iters, int32_t blocks, ap_stream_t stream) {
+  if (!scratch || iters < 1 || blocks < 1 || kind < 0 || kind > 2) return AP_ERR_ARG;
+  return check_cuda(launch_sample_probe(kind, scratch, iters, blocks, (cudaStream_t)stream));
 }
 
 int ap_batch_stats(const ap_batch* b, int64_t* stats_out) {

@@ -207,7 +207,9 @@ struct BatchArgs {
   int64_t* wlist;             // [2 * n_work_tiles] active working tiles: slot<<62 | stamp<<32 | tile
   int64_t* olist;             // [2 * n_out_tiles]  active output tiles, same packing
   int32_t* slist;             // [2 * n_stamps]     active (stamp * 2 + slot)
-  unsigned long long* work_ctr;  // [0] convolution FLOPs, [1] integration samples, [2] sampling samples
+  unsigned long long* work_ctr;  // [0] convolution FLOPs, [1] integration samples, [2] sampling
+                                 // samples, [3] / [4] integration samples of difference / Jacobian
+                                 // evaluations (of [1]); [8]
   double* mean_acc;           // [n_stamps][2]
   double* tile_acc;           // [n_out_tiles][2][kNacc]
   double* acc;                // [n_stamps][2][kNacc]

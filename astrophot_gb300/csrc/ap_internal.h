@@ -83,6 +83,7 @@ cudaError_t launch_eval_setup(const BatchArgs& b, const double* params, int64_t 
 cudaError_t launch_render_pass(const BatchArgs& b, const ConvIO& io, size_t conv_smem,
                                bool accumulate, cudaStream_t s, Profiler* prof = nullptr);
 cudaError_t launch_fma_probe(float* out, int iters, int blocks, cudaStream_t s);
+cudaError_t launch_sample_probe(int kind, float* out, int iters, int blocks, cudaStream_t s);
 cudaError_t set_conv_smem(size_t bytes);
 cudaError_t launch_chi2_only(const BatchArgs& b, const ConvIO& io, const float* model,
                              double* out, cudaStream_t s);

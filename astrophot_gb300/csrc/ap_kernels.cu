@@ -221,9 +221,10 @@ __global__ void k_build_lists(BatchArgs b) {
   const int ops = b.evals[t].ops;
   if (b.psf_mode != AP_PSF_NONE && st.fft_nx == 0) {  // (FFT-convolved stamps: not k_conv's work)
     const bool jac = (ops & OP_JAC) != 0, shiftmode = (b.psf_mode == AP_PSF_FULL);
+    // (a difference evaluation convolves dS with K1 and, with the shift, S0 with dK)
     const int nconv = jac ? ((shiftmode ? 3 : 1) + (profile_has_n(b.kind) ? 4 : 3) +
                              ((shiftmode && !(ops & OP_VJP_COORD)) ? 0 : 2))
-                          : 1;
+                          : ((ops & OP_DIFF) && shiftmode ? 2 : 1);
     atomicAdd(b.work_ctr, (unsigned long long)st.nx * st.ny * 2ull *
                               (unsigned long long)(st.kpx * st.kpy) * (unsigned long long)nconv);
   }
@@ -993,12 +994,17 @@ __global__ void __launch_bounds__(256, 3) k_level1(BatchArgs b) {
   const uint32_t n = min((uint32_t)b.counters[0], (uint32_t)(2 * b.work_pixels));
   const int Q = b.tables->quad_level;
   int n64 = 0;
+  unsigned long long n_all = 0, n_diff = 0, n_jac = 0;  // samples by kind of evaluation
   for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
     const uint32_t idx = base + threadIdx.x;
     bool push = false, amb = false;
     int64_t ent = 0;
     if (idx < n) {
       ent = b.queue[idx];
+      const int ops = b.evals[((ent >> 32) & 0x3fffffff) * 2 + (int)(ent >> 62)].ops;
+      n_all += Q * Q;
+      if (ops & OP_JAC) n_jac += Q * Q;
+      else if (ops & OP_DIFF) n_diff += Q * Q;
       if (Q == 3)
         level1_pixel<3, EXT>(b, ent, push, amb, n64);
       else
@@ -1018,9 +1024,15 @@ __global__ void __launch_bounds__(256, 3) k_level1(BatchArgs b) {
   }
   n64 = __reduce_add_sync(0xffffffffu, n64);
   if ((threadIdx.x & 31) == 0 && n64) atomicAdd(&b.counters[6], (unsigned)n64);
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    const int Qn = b.tables->quad_level;
-    atomicAdd(b.work_ctr + 1, (unsigned long long)n * (unsigned long long)(Qn * Qn));
+  for (int o = 16; o > 0; o >>= 1) {
+    n_all += __shfl_xor_sync(0xffffffffu, n_all, o);
+    n_diff += __shfl_xor_sync(0xffffffffu, n_diff, o);
+    n_jac += __shfl_xor_sync(0xffffffffu, n_jac, o);
+  }
+  if ((threadIdx.x & 31) == 0 && n_all) {
+    atomicAdd(b.work_ctr + 1, n_all);
+    if (n_diff) atomicAdd(b.work_ctr + 3, n_diff);
+    if (n_jac) atomicAdd(b.work_ctr + 4, n_jac);
   }
 }
 
@@ -1180,7 +1192,7 @@ __device__ __forceinline__ QuadResult packed_quad(const BatchArgs& b, int64_t en
 
 template <int QC>
 __device__ void level23_packed(const BatchArgs& b, PackSmem& S, int np, int lane, unsigned long long& samples,
-                               int& n64) {
+                               unsigned long long& diff_samples, int& n64) {
   const QuadTables& T = *b.tables;
   const int G2 = T.gridding * T.gridding;
   const int Q2 = QC > 0 ? QC * QC : T.quad_level * T.quad_level;
@@ -1197,6 +1209,7 @@ __device__ void level23_packed(const BatchArgs& b, PackSmem& S, int np, int lane
       const EvalDev* e;
       int i, j;
       const QuadResult r = packed_quad<QC>(b, S.ent[P], m, -1, diff, st, e, i, j);
+      if (diff) diff_samples += Q2;
       S.res[it] = r.res;
       S.dres[it] = r.dres;
       if (b.max_depth > 2 && decide<false>(b, *st, *e, r, e->thresh * (float)G2, i, j, m, n64))
@@ -1238,6 +1251,7 @@ __device__ void level23_packed(const BatchArgs& b, PackSmem& S, int np, int lane
         const EvalDev* e;
         int i, j;
         const QuadResult r = packed_quad<QC>(b, S.ent[P], m, k, diff, st, e, i, j);
+        if (diff) diff_samples += Q2;
         S.res3[it] = r.res;
         S.dres3[it] = r.dres;
       }
@@ -1281,7 +1295,7 @@ __global__ void __launch_bounds__(kPackWarps * 32, 6) k_integrate_packed(BatchAr
   PackSmem& S = smem[threadIdx.x >> 5];
   const int64_t cap = (int64_t)2 * b.work_pixels;
   const uint32_t n = min((uint32_t)b.counters[13], (uint32_t)cap);
-  unsigned long long samples = 0;
+  unsigned long long samples = 0, diff_samples = 0;
   int n64 = 0;
   while (true) {
     uint32_t idx0 = 0;
@@ -1292,14 +1306,16 @@ __global__ void __launch_bounds__(kPackWarps * 32, 6) k_integrate_packed(BatchAr
     if (lane < np) S.ent[lane] = b.recheck[cap - 1 - (idx0 + lane)];
     __syncwarp();
     if (b.tables->quad_level == 3)
-      level23_packed<3>(b, S, np, lane, samples, n64);
+      level23_packed<3>(b, S, np, lane, samples, diff_samples, n64);
     else
-      level23_packed<0>(b, S, np, lane, samples, n64);
+      level23_packed<0>(b, S, np, lane, samples, diff_samples, n64);
   }
   n64 = __reduce_add_sync(0xffffffffu, n64);
   samples = __shfl_sync(0xffffffffu, samples, 0);
+  for (int o = 16; o > 0; o >>= 1) diff_samples += __shfl_xor_sync(0xffffffffu, diff_samples, o);
   if (lane == 0) {
     if (samples) atomicAdd(b.work_ctr + 1, samples);
+    if (diff_samples) atomicAdd(b.work_ctr + 3, diff_samples);
     if (n64) atomicAdd(&b.counters[6], (unsigned)n64);
   }
 }
@@ -1351,6 +1367,7 @@ __global__ void __launch_bounds__(256, 3) k_integrate(BatchArgs b) {
   n64 = __reduce_add_sync(0xffffffffu, n64);
   if (lane == 0) {
     if (samples) atomicAdd(b.work_ctr + 1, samples);
+    if (samples && !FWD) atomicAdd(b.work_ctr + 4, samples);
     if (n64) atomicAdd(&b.counters[6], (unsigned)n64);
   }
 }
@@ -1936,6 +1953,65 @@ __global__ void k_fma_probe(float* out, int iters) {
   }
   const float r = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
   if (r == 123.456f) out[blockIdx.x * blockDim.x + threadIdx.x] = r;
+}
+
+// Sample-evaluation probe: the integration's per-sample arithmetic (a Sersic sample: plain,
+// with its six partials, or as a difference to a base evaluation) at full occupancy with no
+// memory traffic, four independent samples per step: the rate these device functions reach
+// on this GPU, the compute roofline of the integration kernels.
+template <int KIND>
+__global__ void __launch_bounds__(256) k_sample_probe(float* out, int iters) {
+  EvalF e{};
+  e.c = 0.8f;
+  e.s = 0.6f;
+  e.invq = 1.6f;
+  e.invRe = 0.125f;
+  e.invn = 0.4f;
+  e.bn = 4.67f;
+  e.dbn = 2.0f;
+  e.amp = 15.8f;
+  e.soft2 = 1e-6f;
+  DeltaF d{};
+  d.c = 1e-5f;
+  d.s = -2e-5f;
+  d.invq = 3e-5f;
+  d.lnire = -1e-5f;
+  d.invn = 2e-5f;
+  d.bn = -4e-5f;
+  d.lnamp = 1e-5f;
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+  const float x0 = 0.01f * (threadIdx.x & 31), y0 = 0.013f * (threadIdx.x >> 5);
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float X = x0 + 0.37f * k + 1e-3f * it, Y = y0 - 0.29f * k + 7e-4f * it;
+      if (KIND == 1) {
+        const Sample sm = eval_profile<true, false>(e, AP_PROFILE_SERSIC, X, Y, 1.f);
+        float t = sm.v;
+#pragma unroll
+        for (int q = 0; q < NGRAD; ++q) t += sm.g[q];
+        acc[k] += t;
+      } else if (KIND == 2) {
+        float dI;
+        const Sample sm = eval_profile_delta(e, d, AP_PROFILE_SERSIC, X, Y, 1.f, dI);
+        acc[k] += sm.v + dI;
+      } else {
+        acc[k] += eval_profile<false, false>(e, AP_PROFILE_SERSIC, X, Y, 1.f).v;
+      }
+    }
+  }
+  const float r = acc[0] + acc[1] + acc[2] + acc[3];
+  if (r == 123.456f) out[blockIdx.x * blockDim.x + threadIdx.x] = r;
+}
+
+cudaError_t launch_sample_probe(int kind, float* out, int iters, int blocks, cudaStream_t s) {
+  if (kind == 1)
+    k_sample_probe<1><<<blocks, 256, 0, s>>>(out, iters);
+  else if (kind == 2)
+    k_sample_probe<2><<<blocks, 256, 0, s>>>(out, iters);
+  else
+    k_sample_probe<0><<<blocks, 256, 0, s>>>(out, iters);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_fma_probe(float* out, int iters, int blocks, cudaStream_t s) {

@@ -71,7 +71,7 @@ __global__ void k_noalloc_setup(StampDev st, QuadTables T, NoallocOffsets o, cha
   uint32_t* cnt = reinterpret_cast<uint32_t*>(ws + o.cnt);
   if (t < 16) cnt[t] = 0u;
   unsigned long long* wc = reinterpret_cast<unsigned long long*>(ws + o.wctr);
-  if (t < 4) wc[t] = 0ull;
+  if (t < 8) wc[t] = 0ull;
 }
 static_assert(sizeof(StampDev) + sizeof(QuadTables) + sizeof(NoallocOffsets) + sizeof(char*) <= 4000,
               "the plan must fit the kernel-argument space");
@@ -279,7 +279,7 @@ extern "C" int ap_render_noalloc(int32_t nx, int32_t ny, int32_t psf_kx, int32_t
   const int64_t o_olist = take(sizeof(int64_t) * 2 * st.nto);
   const int64_t o_slist = take(sizeof(int32_t) * 2);
   const int64_t o_cnt = take(sizeof(uint32_t) * 16);
-  const int64_t o_wctr = take(sizeof(unsigned long long) * 4);
+  const int64_t o_wctr = take(sizeof(unsigned long long) * 8);
   const int64_t o_mean = take(sizeof(double) * 2);
   const int64_t o_tacc = take(sizeof(double) * 2 * kNacc * st.nto);
   const int64_t o_acc = take(sizeof(double) * 2 * kNacc);

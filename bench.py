@@ -828,6 +828,25 @@ def run_gpu_learned(args):
         "algorithmic_flop_per_launch": work["conv_flops"] / max(conv_n, 1),
         "peak_source": "measured FP32 FMA probe (ap_fma_probe) on this GPU",
     }
+    # the adaptive integration (k_level1, its float64 re-decisions, k_integrate): samples of each
+    # kind of evaluation against the rate of the same sample arithmetic alone (ap_sample_probe)
+    integ_ms = ktimes["integrate"][0]
+    n_all, n_diff, n_jac = work["integrate_samples"], work["integrate_samples_diff"], work["integrate_samples_jacobian"]
+    rates = {k: N.sample_probe_rate(k) for k in (0, 1, 2)}
+    ideal_s = (n_all - n_diff - n_jac) / rates[0] + n_jac / rates[1] + n_diff / rates[2]
+    roof_int = {
+        "kernel": "k_level1 + k_level1_amb + k_integrate (adaptive sub-pixel integration)",
+        "bound": "sample arithmetic (FP32 + MUFU pipes)",
+        "achieved": n_all / (integ_ms * 1e-3) / 1e9 if integ_ms > 0 else None,
+        "peak": n_all / ideal_s / 1e9 if ideal_s > 0 else None,
+        "unit": "Gsamples/s",
+        "frac": ideal_s / (integ_ms * 1e-3) if integ_ms > 0 else None,
+        "samples_per_step": {"all": n_all / args.steps, "difference": n_diff / args.steps,
+                             "jacobian": n_jac / args.steps},
+        "peak_source": "measured: the integration's own sample functions, register-resident at full occupancy "
+                       "(ap_sample_probe: %.1f / %.1f / %.1f Gsamples/s plain / with partials / difference), "
+                       "mixed by the counted samples" % (rates[0] / 1e9, rates[1] / 1e9, rates[2] / 1e9),
+    }
     chunks = (S + 8191) // 8192
     launches = int(sum(v[1] for v in ktimes.values()) / args.steps) + CNN_LAUNCHES_PER_CHUNK * chunks + 2
     value = converged_all / (dev_ms * 1e-3)
@@ -875,6 +894,7 @@ def run_gpu_learned(args):
         "e2e": {"value": converged_all / (e2e_ms * 1e-3), "unit": "fits/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "wall_ms_per_step": e2e_wall_ms},
         "roofline": roof,
+        "roofline_integrate": roof_int,
         "autotune": tuned,
         "kernel_ms_per_step": {k: v[0] / args.steps for k, v in ktimes.items()},
         "kernel_launches_per_step": {k: v[1] / args.steps for k, v in ktimes.items()},

@@ -319,15 +319,22 @@ int ap_batch_kernel_times(ap_batch* batch, double* ms_out, int64_t* launches_out
 
 /* Algorithmic work counted on the device since bind (or the last reset): out[0] FP32
  * FLOPs of the PSF convolutions (2 per kernel tap, per convolved plane, per output pixel),
- * out[1] profile samples of the adaptive integration, out[2] samples of the sampling pass.
+ * out[1] profile samples of the adaptive integration, out[2] samples of the sampling pass,
+ * out[3] / out[4] the integration samples (of out[1]) of difference / Jacobian evaluations.
  * Synchronises the stream. */
-int ap_batch_work_counters(ap_batch* batch, uint64_t* out /* [4] */, int32_t reset,
+int ap_batch_work_counters(ap_batch* batch, uint64_t* out /* [6] */, int32_t reset,
                            ap_stream_t stream);
 
 /* FP32 FMA throughput probe: blocks x 256 threads, each running 8 independent chains of
  * 16 * iters FMAs (2 FLOP each).  scratch: >= blocks * 256 floats of device memory (never
  * written in practice).  Used to measure the FP32 pipe peak for roofline fractions. */
 int ap_fma_probe(float* scratch, int32_t iters, int32_t blocks, ap_stream_t stream);
+
+/* Sample-evaluation probe: blocks x 256 threads, each evaluating 4 * iters Sersic samples with the
+ * integration's own device functions, register-resident (kind 0: value, 1: value and its six
+ * partials, 2: value and its difference to a base evaluation).  scratch: >= blocks * 256 floats
+ * (never written in practice).  The compute roofline of the integration kernels. */
+int ap_sample_probe(int32_t kind, float* scratch, int32_t iters, int32_t blocks, ap_stream_t stream);
 
 /* Render of one stamp for callers that cannot allocate device memory (a host that owns
  * the whole device memory pool, a plugin without access to its allocator, a pipeline that
