@@ -1176,6 +1176,49 @@ def bulge_disk_block(args, dev):
     }
 
 
+def _oracle_source_window(job):
+    """One Sersic source of a field rendered by the oracle on its own window with the group's
+    working pixel count in its integration threshold (and its Jacobian when asked): (window
+    model, seconds)."""
+    params, window, psf, numel, grad, size = job
+    from oracle.render import PSF, Component, Window, sample_component, sub_window
+
+    cx, cy, q, PA, n, Re, Ie = params[:7]
+    comp = Component("sersic", {"center": [cx, cy], "q": q, "PA": PA, "n": n, "Re": Re, "Ie": Ie}, psf_mode="full",
+                     psf_convolve_mode="direct", thr_numel=numel)
+    win = sub_window(Window.from_scale(size, size), window)
+    t = time.perf_counter()
+    r = sample_component(comp, win, PSF(psf), grad=grad)
+    return r.model, time.perf_counter() - t
+
+
+def crowded_oracle(sc, rep, windows, psf, data, weight, sky, size, procs):
+    """The crowded field's chi^2 / ndf at a joint vector from the oracle (every source on its own
+    window, as the reference's pixels), and the oracle's CPU seconds for the render and for the
+    Jacobians of all sources (one windowed LM iteration's model and Jacobian work)."""
+    V = sc.values_matrix(rep)
+    # the arrays the GPU fitted (float32)
+    psf = psf.astype(np.float32).astype(np.float64)
+    data = data.astype(np.float32).astype(np.float64)
+    weight = weight.astype(np.float32).astype(np.float64)
+    ky, kx = psf.shape
+    numel = float((size + 2 * ((kx + 2) // 2)) * (size + 2 * ((ky + 2) // 2)))
+    jobs = [(V[i], windows[i], psf, numel, False, size) for i in range(len(windows))]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(processes=procs) as pool:
+        res = pool.map(_oracle_source_window, jobs)
+        k = min(len(jobs), 2 * procs)
+        jres = pool.map(_oracle_source_window, [j[:4] + (True, size) for j in jobs[:k]])
+    model = np.full((size, size), sky)
+    for (m, _), w in zip(res, windows):
+        (x0, x1), (y0, y1) = w
+        model[y0:y1, x0:x1] += m
+    chi2 = float(np.sum(weight * (data - model) ** 2) / max(1.0, size * size - sc.P))
+    render_s = sum(t for _, t in res)
+    jac_s = sum(t for _, t in jres) * len(jobs) / k
+    return chi2, render_s, jac_s, k
+
+
 def crowded_block(args, dev):
     """200 Sersic galaxies on a 1024 x 1024 image, 51 x 51 Gaussian PSF (sigma 2), sky 5.0,
     noise sigma = sqrt(model + 10), explicit per-galaxy windows; 1400 parameters fitted jointly
@@ -1245,7 +1288,7 @@ def crowded_block(args, dev):
     lm = SC.SceneLM(sc, initial_state=rep, max_iter=args.crowded_iters).fit()
     torch.cuda.synchronize()
     lm_s = time.perf_counter() - t0
-    return {
+    out = {
         "workload": f"{n_src} Sersic galaxies on a {size}x{size} image, 51x51 Gaussian PSF (sigma 2; mode fft: "
         "the convolution takes the faster of FFT and direct for the kernel size, direct at 53x53), sky 5.0, "
         "explicit windows (half-size 4 Re + 3 sigma + 2), noise sqrt(model + 10); "
@@ -1265,6 +1308,20 @@ def crowded_block(args, dev):
         "chi2_ndf_end": min(lm.loss_history),
         "lm_message": lm.message,
     }
+    if not args.no_cpu:
+        procs = os.cpu_count() or 1
+        c2o, rs, js, k = crowded_oracle(sc, lm.res(), windows, psf, data, weight, sky, size, procs)
+        out["oracle"] = {
+            "chi2_ndf_at_fitted_state": c2o,
+            "rel_diff_vs_gpu": abs(min(lm.loss_history) / c2o - 1.0),
+            "cpu_render_s": rs,
+            "cpu_jacobian_s": js,
+            "cpu_iteration_s": rs + js,
+            "sample": f"every source rendered by the float64 oracle on its own window (the group's working "
+            f"pixel count in its threshold), {procs} processes; Jacobians timed on {k} sources and scaled to "
+            f"{len(windows)}; one LM iteration's render + Jacobian work, CPU seconds summed over sources",
+        }
+    return out
 
 
 def _oracle_init(data):

@@ -297,6 +297,10 @@ class Component:
     # plus 3 x 3 supersampling within 2 px of the centre"; no such mode in the reference)
     center_quad_level: int = 3
     center_radius: float = 2.0
+    # pixel count the integration threshold divides by (None: the working window's).  A windowed
+    # source of a group is evaluated by the reference on the group's window; a Sersic source
+    # rendered on its own window with the group's working pixel count gives the same pixels.
+    thr_numel: Optional[float] = None
     locked: Tuple[str, ...] = ()
     # pixel window [[x0, x1], [y0, y1]] inside the group's window (Model.window given in pixels,
     # models/core_model.py:313-325 -> Window.crop_to_pixel); None = the whole window
@@ -623,11 +627,12 @@ def sample_midpoint_center(comp, win: Window, center, grad):
 def integrate_reference(comp, deep_val):
     """``_integrate_reference``: models/_model_methods.py:151-152 (sum / numel), overridden by
     ``Sersic_Galaxy._integrate_reference`` (models/sersic_model.py:87-89, total flux / numel)."""
+    numel = deep_val.size if comp.thr_numel is None else comp.thr_numel
     if comp.kind == "sersic":
         p = comp.params
         tot = sersic_total_flux(10 ** p["Ie"], p["n"], p["Re"], p["q"])
-        return tot / deep_val.size
-    return np.sum(deep_val) / deep_val.size
+        return tot / numel
+    return np.sum(deep_val) / numel
 
 
 def sample_integrate(comp, deep: Sampled, reference, win: Window, center, grad):
