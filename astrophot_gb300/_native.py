@@ -156,8 +156,10 @@ EXPORTS = [
     ("ap_cnn_autotune", [_I32, _PI32]),
     ("ap_cnn_workspace_bytes", [_I64]),
     ("ap_cnn_layer_offsets", [_PI64, _PI64, _PI32]),
+    ("ap_cnn_workspace_offsets", [_I64, _PI64, _PI64]),
     ("ap_cnn_to_bf16", [_P, _P, _P]),
     ("ap_cnn_forward", [_P, _P, _P, _I64, _P, _P, ctypes.c_size_t, _P]),
+    ("ap_cnn_infer", [_P, _P, _P, _I64, _P, _P, ctypes.c_size_t, _P]),
     ("ap_cnn_backward", [_P, _P, _I64, _P, _P, ctypes.c_size_t, _P]),
     ("ap_cnn_train_step", [_P, _P, _P, _P, _P, _P, _P, _I64, ctypes.c_float, _I32, ctypes.c_float, _P, _P,
                            ctypes.c_size_t, _P]),
@@ -166,6 +168,11 @@ EXPORTS = [
     ("ap_moments_init", [_P, _P, _P, _P, _I64, _P, _P]),
     ("ap_select_init", [_P, _P, _P, _P, _I64, _P, _P, _P]),
     ("ap_gemm_bf16", [_P, _I32, _I32, _P, _I32, _I32, _P, _I32, _I32, _I32, _I32, _P]),
+    ("ap_cnn_set_path", [_I32]),
+    ("ap_cnn_get_path", [_PI32]),
+    ("ap_gemm_bf16_tc", [_P, _I32, _P, _I32, _P, _I32, _I32, _I32, _I32, _P, _P, _I32, _P]),
+    ("ap_conv3x3s2_bf16_tc", [_P, _I64, _I32, _I32, _P, _I32, _P, _I32, _P, _P, _I32, _P]),
+    ("ap_tc_status", [_I32, ctypes.POINTER(ctypes.c_uint32)]),
     ("ap_version", []),
     ("ap_last_cuda_error", []),
 ]

@@ -31,8 +31,32 @@ from . import _native as N
 from .synthetic import moffat_rd, moffat_stamp
 
 __all__ = ("InitNet", "StampSet", "draw_stamp_params", "psf_bank", "make_stamps", "learned_fit", "plain_fit",
-           "heuristic_init", "subset",
+           "heuristic_init", "subset", "set_tensor_path", "get_tensor_path", "tc_status",
            "WEIGHTS_PATH")
+
+# tensor-core path of the CNN GEMMs (ap_cnn_set_path)
+TENSOR_PATHS = {"mma_sync": 0, "tcgen05": 1}
+
+
+def set_tensor_path(name: str) -> None:
+    """``"tcgen05"`` (default: TMEM accumulators, TMA-staged operands, implicit im2col at
+    inference) or ``"mma_sync"`` (ldmatrix + mma.sync tiles over explicit im2col matrices)."""
+    if name not in TENSOR_PATHS:
+        raise ValueError(f"tensor path {name!r}: one of {sorted(TENSOR_PATHS)}")
+    N.check(N.lib().ap_cnn_set_path(TENSOR_PATHS[name]), "ap_cnn_set_path")
+
+
+def get_tensor_path() -> str:
+    v = ctypes.c_int32(-1)
+    N.check(N.lib().ap_cnn_get_path(ctypes.byref(v)), "ap_cnn_get_path")
+    return {i: k for k, i in TENSOR_PATHS.items()}[v.value]
+
+
+def tc_status(clear: bool = False) -> int:
+    """Error code recorded by a tcgen05 kernel (0: none; 1-3: an mbarrier wait ran out)."""
+    v = ctypes.c_uint32(0)
+    N.check(N.lib().ap_tc_status(1 if clear else 0, ctypes.byref(v)), "ap_tc_status")
+    return int(v.value)
 
 IMG = 64
 N_OUT = 8
@@ -205,6 +229,35 @@ class InitNet:
                                         N._ptr(ws), ws.numel(), N._stream()), "ap_cnn_forward")
         return out
 
+    def infer(self, x: torch.Tensor, n: int) -> torch.Tensor:
+        """``forward`` for inference only (no im2col matrices kept: ``backward`` may not follow)."""
+        if n % 16:
+            raise ValueError("batches of the CNN are multiples of 16 stamps")
+        ws = self._workspace(n)
+        out = torch.empty((n, OUT_PAD), dtype=torch.float32, device=self.device)
+        N.check(self.lib.ap_cnn_infer(N._ptr(self.params), N._ptr(self.params_bf16), N._ptr(x), n, N._ptr(out),
+                                      N._ptr(ws), ws.numel(), N._stream()), "ap_cnn_infer")
+        return out
+
+    def kept_activations(self, n: int):
+        """The activations the last ``forward`` of ``n`` stamps kept in the workspace for the
+        backward pass: [act of layers 1-5 as float32 [rows, N]], out [n, 16]."""
+        acts = (ctypes.c_int64 * 6)()
+        out_off = ctypes.c_int64()
+        N.check(self.lib.ap_cnn_workspace_offsets(n, acts, ctypes.byref(out_off)), "ap_cnn_workspace_offsets")
+        dims = (ctypes.c_int32 * 36)()
+        wo, bo = (ctypes.c_int64 * 6)(), (ctypes.c_int64 * 6)()
+        N.check(self.lib.ap_cnn_layer_offsets(wo, bo, dims), "ap_cnn_layer_offsets")
+        ws = self._workspace(n)
+        out = []
+        for l in range(5):
+            hout, nn = dims[l * 6 + 3], dims[l * 6 + 5]
+            rows = n * hout * hout
+            raw = ws[acts[l] : acts[l] + rows * nn * 2]
+            out.append(raw.view(torch.bfloat16).float().reshape(rows, nn))
+        raw = ws[out_off.value : out_off.value + n * OUT_PAD * 4]
+        return out, raw.view(torch.float32).reshape(n, OUT_PAD).clone()
+
     def backward(self, dout: torch.Tensor, n: int) -> torch.Tensor:
         ws = self._workspace(n)
         grads = torch.empty(self.count, dtype=torch.float32, device=self.device)
@@ -226,7 +279,7 @@ class InitNet:
                 d = torch.cat([d, torch.full(((mp - m) * IMG * IMG,), sky, dtype=torch.float32, device=self.device)])
                 sg = torch.cat([sg, torch.ones(mp - m, dtype=sg.dtype, device=sg.device)])
             x, lscale = self.prepare(d.contiguous(), sg, mp, sky)
-            o = self.forward(x, mp)
+            o = self.infer(x, mp)
             skyF = torch.full((mp,), sky_F, dtype=torch.float64, device=self.device)
             p = torch.empty((mp, 8), dtype=torch.float64, device=self.device)
             N.check(self.lib.ap_cnn_decode(N._ptr(o), N._ptr(lscale), N._ptr(self.mean), N._ptr(self.std),

@@ -11,10 +11,14 @@
 //   L4 conv 3x3 s2 p1 128 -> 256    8x8  ->  4x4    ReLU
 //   L5 fc 4096 -> 192                               ReLU
 //   L6 fc  192 ->   8 (stored as 16 output rows, rows 8..15 zero)
-// 1,176,008 trainable parameters.  Every layer is one GEMM on the tensor cores
-// (mma.sync m16n8k16 bf16 -> fp32) over an im2col matrix; the backward pass is two GEMMs per
-// layer (weight gradient, input gradient) plus a col2im gather.  Master weights, gradients and
-// Adam moments are fp32; the GEMMs read a bf16 mirror of the weights.
+// 1,176,008 trainable parameters.  Every layer is one GEMM on the tensor cores, bf16 operands
+// with fp32 accumulation.  Forward (default path): the tcgen05 kernels of ap_tcgemm.cu (TMEM
+// accumulator, TMA-staged operands, bias + ReLU + bf16 in the epilogue); at inference the
+// convolutions of layers 2-4 read the NHWC activations through strided TMA loads (implicit
+// im2col), for training they run over the im2col matrices the weight gradients need.  The
+// backward pass is two GEMMs per layer (weight gradient, input gradient) plus a col2im gather, on
+// the ldmatrix + mma.sync tiles below (also the forward's second path, AP_CNN_MMA_SYNC).  Master
+// weights, gradients and Adam moments are fp32; the GEMMs read a bf16 mirror of the weights.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -81,6 +85,7 @@ struct CnnWs {
   float* dcol;          // fp32 dcol (largest layer)
   bf16* dpre;           // bf16 d loss / d pre-activation (largest layer)
   double* loss;         // [1]
+  size_t act_off[kLayers], out_off;  // byte offsets of act[l] and out in the workspace
   size_t bytes;
 };
 
@@ -100,12 +105,14 @@ CnnWs cnn_layout(char* base, int64_t B) {
     const int64_t M = (l < kNumConv) ? layer_rows(l, B) : B;
     if (l < kNumConv || l == 0) w.col[l] = (bf16*)take((size_t)M * d.K * sizeof(bf16));
     w.pre[l] = (float*)take((size_t)M * d.N * sizeof(float));
+    w.act_off[l] = off;
     w.act[l] = (bf16*)take((size_t)M * d.N * sizeof(bf16));
     max_mn = (size_t)M * d.N > max_mn ? (size_t)M * d.N : max_mn;
     max_mk = (size_t)M * d.K > max_mk ? (size_t)M * d.K : max_mk;
   }
   w.col[4] = w.act[3];
   w.col[5] = w.act[4];
+  w.out_off = off;
   w.out = (float*)take((size_t)B * kOutPad * sizeof(float));
   w.dpre_f = (float*)take(max_mk * sizeof(float));
   w.dcol = (float*)take(max_mk * sizeof(float));
@@ -248,6 +255,7 @@ __global__ void __launch_bounds__(WM* WN * 32) k_gemm(const bf16* __restrict__ A
 }
 
 int g_num_sms = 0;
+int g_cnn_path = AP_CNN_TCGEN05;
 bool g_gemm_tune = false;
 std::mutex g_tune_mutex;
 std::map<std::tuple<int, int, int, int, int>, int> g_tuned;  // (A_T, B_T, R, S, T) -> tile shape
@@ -689,7 +697,41 @@ __global__ void k_select_init(const double* __restrict__ pa, const double* __res
 // ---------------------------------------------------------------------------------------------
 // forward / backward drivers
 // ---------------------------------------------------------------------------------------------
-cudaError_t forward(const float* params, const bf16* wb, const float* x, int64_t B, const CnnWs& w, cudaStream_t st) {
+// tcgen05 forward: bias + ReLU + bf16 in every GEMM epilogue; the convolutions of layers 2-4
+// read their inputs straight from the NHWC activations (implicit im2col by strided TMA loads)
+// unless need_cols asks for the im2col matrices (kept for the weight gradients).
+cudaError_t forward_tc(const float* params, const bf16* wb, const float* x, int64_t B, const CnnWs& w,
+                       cudaStream_t st, bool need_cols) {
+  cudaError_t e;
+  k_im2col_in<<<(unsigned)((B * 1024 + 255) / 256), 256, 0, st>>>(x, w.col[0], B);
+  for (int l = 0; l < kLayers; ++l) {
+    const LayerDim d = layer_dim(l);
+    const int64_t M = (l < kNumConv) ? layer_rows(l, B) : B;
+    const bool last = (l == kLayers - 1);
+    apgb::TcEpilogue ep;
+    ep.bias = params + b_off(l);
+    ep.act = last ? nullptr : w.act[l];
+    ep.relu = last ? 0 : 1;
+    float* cout = last ? w.out : nullptr;
+    const int ldc = last ? kOutPad : d.N;
+    if (l >= 1 && l < kNumConv && !need_cols) {
+      const LayerDim dp = layer_dim(l - 1);
+      e = apgb::tc_conv3x3s2(w.act[l - 1], B, dp.hout, d.cin, wb + w_off(l), d.N, cout, ldc, ep, st);
+    } else {
+      if (l >= 1 && l < kNumConv) {
+        const LayerDim dp = layer_dim(l - 1);
+        k_im2col<<<grid_for(M * 9 * (d.cin / 8)), 256, 0, st>>>(w.act[l - 1], w.col[l], B, dp.hout, d.cin);
+      }
+      e = apgb::tc_gemm(w.col[l], d.K, wb + w_off(l), d.K, cout, ldc, (int)M, d.N, d.K, ep, st);
+    }
+    if (e != cudaSuccess) return e;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t forward(const float* params, const bf16* wb, const float* x, int64_t B, const CnnWs& w, cudaStream_t st,
+                    bool need_cols = false) {
+  if (g_cnn_path == AP_CNN_TCGEN05) return forward_tc(params, wb, x, B, w, st, need_cols);
   cudaError_t e;
   k_im2col_in<<<(unsigned)((B * 1024 + 255) / 256), 256, 0, st>>>(x, w.col[0], B);
   for (int l = 0; l < kLayers; ++l) {
@@ -767,6 +809,14 @@ size_t ap_cnn_workspace_bytes(int64_t batch) {
   return cnn_layout(nullptr, batch).bytes;
 }
 
+int ap_cnn_workspace_offsets(int64_t batch, int64_t* act_offsets, int64_t* out_offset) {
+  if (batch <= 0 || !act_offsets || !out_offset) return AP_ERR_ARG;
+  const CnnWs w = cnn_layout(nullptr, batch);
+  for (int l = 0; l < kLayers; ++l) act_offsets[l] = (int64_t)w.act_off[l];
+  *out_offset = (int64_t)w.out_off;
+  return AP_OK;
+}
+
 int ap_cnn_layer_offsets(int64_t* w_offsets, int64_t* b_offsets, int32_t* dims) {
   if (!w_offsets || !b_offsets || !dims) return AP_ERR_ARG;
   for (int l = 0; l < kLayers; ++l) {
@@ -798,7 +848,19 @@ int ap_cnn_forward(const float* params, const void* params_bf16, const float* x,
   if (ws_bytes < ap_cnn_workspace_bytes(batch)) return AP_ERR_WORKSPACE;
   cudaStream_t st = (cudaStream_t)stream;
   CnnWs w = cnn_layout((char*)ws, batch);
-  int rc = cnn_check(forward(params, (const bf16*)params_bf16, x, batch, w, st));
+  // the im2col matrices stay in the workspace for a later ap_cnn_backward
+  int rc = cnn_check(forward(params, (const bf16*)params_bf16, x, batch, w, st, true));
+  if (rc) return rc;
+  return cnn_check(cudaMemcpyAsync(out, w.out, sizeof(float) * batch * kOutPad, cudaMemcpyDeviceToDevice, st));
+}
+
+int ap_cnn_infer(const float* params, const void* params_bf16, const float* x, int64_t batch, float* out, void* ws,
+                 size_t ws_bytes, ap_stream_t stream) {
+  if (!params || !params_bf16 || !x || !out || !ws || batch <= 0 || batch % 16) return AP_ERR_ARG;
+  if (ws_bytes < ap_cnn_workspace_bytes(batch)) return AP_ERR_WORKSPACE;
+  cudaStream_t st = (cudaStream_t)stream;
+  CnnWs w = cnn_layout((char*)ws, batch);
+  int rc = cnn_check(forward(params, (const bf16*)params_bf16, x, batch, w, st, false));
   if (rc) return rc;
   return cnn_check(cudaMemcpyAsync(out, w.out, sizeof(float) * batch * kOutPad, cudaMemcpyDeviceToDevice, st));
 }
@@ -821,7 +883,7 @@ int ap_cnn_train_step(float* params, void* params_bf16, float* grads, float* ada
   cudaStream_t st = (cudaStream_t)stream;
   CnnWs w = cnn_layout((char*)ws, batch);
   bf16* wb = (bf16*)params_bf16;
-  int rc = cnn_check(forward(params, wb, x, batch, w, st));
+  int rc = cnn_check(forward(params, wb, x, batch, w, st, true));
   if (rc) return rc;
   rc = cnn_check(cudaMemsetAsync(w.loss, 0, sizeof(double), st));
   if (rc) return rc;
@@ -890,6 +952,52 @@ int ap_gemm_bf16(const void* A, int32_t lda, int32_t a_trans, const void* B, int
   else
     e = gemm<true, false>(a, lda, b, ldb, C, ldc, R, S, T, st);
   return cnn_check(e);
+}
+
+int ap_cnn_set_path(int32_t path) {
+  if (path != AP_CNN_MMA_SYNC && path != AP_CNN_TCGEN05) return AP_ERR_ARG;
+  g_cnn_path = path;
+  return AP_OK;
+}
+
+int ap_cnn_get_path(int32_t* path) {
+  if (!path) return AP_ERR_ARG;
+  *path = g_cnn_path;
+  return AP_OK;
+}
+
+int ap_gemm_bf16_tc(const void* A, int32_t lda, const void* W, int32_t ldw, float* C, int32_t ldc, int32_t R,
+                    int32_t S, int32_t T, const float* bias, void* act, int32_t relu, ap_stream_t stream) {
+  if (!A || !W || (!C && !act) || R <= 0 || S <= 0 || T <= 0) return AP_ERR_ARG;
+  apgb::TcEpilogue ep;
+  ep.bias = bias;
+  ep.act = (bf16*)act;
+  ep.relu = relu;
+  const cudaError_t e = apgb::tc_gemm((const bf16*)A, lda, (const bf16*)W, ldw, C, ldc, R, S, T, ep,
+                                      (cudaStream_t)stream);
+  if (e == cudaErrorInvalidValue) return AP_ERR_ARG;
+  return cnn_check(e);
+}
+
+int ap_conv3x3s2_bf16_tc(const void* x, int64_t batch, int32_t H, int32_t cin, const void* W, int32_t S, float* C,
+                         int32_t ldc, const float* bias, void* act, int32_t relu, ap_stream_t stream) {
+  if (!x || !W || (!C && !act) || batch <= 0 || H <= 0 || cin <= 0 || S <= 0) return AP_ERR_ARG;
+  apgb::TcEpilogue ep;
+  ep.bias = bias;
+  ep.act = (bf16*)act;
+  ep.relu = relu;
+  const cudaError_t e = apgb::tc_conv3x3s2((const bf16*)x, batch, H, cin, (const bf16*)W, S, C, ldc, ep,
+                                           (cudaStream_t)stream);
+  if (e == cudaErrorInvalidValue) return AP_ERR_ARG;
+  return cnn_check(e);
+}
+
+int ap_tc_status(int32_t clear, uint32_t* code) {
+  if (!code) return AP_ERR_ARG;
+  const unsigned v = apgb::tc_error(clear != 0);
+  if (v == 0xFFFFFFFFu) return cnn_check(cudaGetLastError());
+  *code = v;
+  return AP_OK;
 }
 
 }  // extern "C"

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "ap_device.cuh"
@@ -131,5 +132,23 @@ cudaError_t launch_lm_init(const BatchArgs& b, const LMArgs& lm, const double* s
                            const uint8_t* mask, cudaStream_t s);
 cudaError_t launch_lm_update(const BatchArgs& b, const LMArgs& lm, cudaStream_t s);
 cudaError_t launch_lm_finish(const BatchArgs& b, const LMArgs& lm, cudaStream_t s);
+
+// Tensor-core (tcgen05 + TMA) GEMMs of the learned initial guess (ap_tcgemm.cu).
+// C[r][s] = sum_t A(r, t) W(s, t), bf16 operands, fp32 accumulation in tensor memory.
+struct TcEpilogue {
+  const float* bias = nullptr;     // added per output column when set
+  __nv_bfloat16* act = nullptr;    // set: bf16 store of (bias, ReLU) into act, row stride ldc
+  int relu = 0;
+};
+// dense: A[r * lda + t], W[s * ldw + t]; S a multiple of 16, T of 16, lda / ldw of 8
+cudaError_t tc_gemm(const __nv_bfloat16* A, int lda, const __nv_bfloat16* W, int ldw, float* C, int ldc, int R, int S,
+                    int T, const TcEpilogue& ep, cudaStream_t st);
+// 3x3 stride-2 pad-1 convolution of an NHWC activation [B][H][H][cin] (cin 16, 32 or a multiple
+// of 64) with W[S][9 * cin] (t = (ky * 3 + kx) * cin + c); rows r = (b * H/2 + oy) * H/2 + ox
+cudaError_t tc_conv3x3s2(const __nv_bfloat16* act_in, int64_t B, int H, int cin, const __nv_bfloat16* W, int S,
+                         float* C, int ldc, const TcEpilogue& ep, cudaStream_t st);
+// first error code recorded by a tensor-core GEMM (0 none; 1-3 a wait that ran out), cleared on
+// request; reading it synchronises the device
+unsigned tc_error(bool clear);
 
 }  // namespace apgb

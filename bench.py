@@ -78,6 +78,7 @@ def parse():
     p.add_argument("--no-crowded", action="store_true", help="skip the crowded-field block")
     p.add_argument("--no-configs", action="store_true",
                    help="skip the single-stamp (128x128) and batched-cutout blocks of the default run")
+    p.add_argument("--no-cnn", action="store_true", help="skip the CNN inference / training block")
     p.add_argument("--c0-stamps", type=int, default=64, help="seeds of the 128x128 single-stamp block")
     p.add_argument("--c0-cpu-sample", type=int, default=32, help="of them fitted by the oracle")
     p.add_argument("--cutout-stamps", type=int, default=8192, help="stamps of the batched-cutout block")
@@ -904,6 +905,8 @@ def run_gpu_learned(args):
 
     if rank == 0 and not args.no_crowded:
         line["crowded_field"] = crowded_block(args, dev)
+    if rank == 0 and not args.no_cnn:
+        line["learned_init_cnn"] = cnn_block(args, dev)
     if rank == 0 and not args.no_configs:
         line["single_stamp_c0"] = c0_block(args, dev)
         line["batched_cutouts"] = cutouts_block(args, dev)
@@ -959,6 +962,125 @@ def run_gpu_learned(args):
 
 
 C0_KNOBS = {"sampling_mode": "midpoint_center", "integrate_mode": "none"}
+
+def measured_peaks():
+    """HBM copy bandwidth and dense bf16 throughput measured on this GPU model (the JSON file
+    beside this script), else an earlier GB300 measurement (6.8 TB/s, 1.9 PFLOP/s)."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            z = json.load(f)
+        return {"hbm_gbs": float(z["hbm_gbs"]), "bf16_tflops": float(z["bf16_tflops"]), "source": "measured"}
+    except (OSError, KeyError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
+
+
+# algorithmic work of one stamp through the CNN: 2 * rows * K * N per layer, K the true
+# reduction (9 taps of layer 1, not its zero padding to 16), N the true outputs (8 of layer 6)
+CNN_FLOP_PER_STAMP = 2 * (1024 * 9 * 32 + 256 * 288 * 64 + 64 * 576 * 128 + 16 * 1152 * 256 + 4096 * 192 + 192 * 8)
+# the least HBM traffic of an inference pass per stamp: the fp32 input stamp, the layer-1 im2col
+# matrix (written, read), each bf16 activation written once and read once, the fp32 output row
+CNN_BYTES_PER_STAMP = (4096 * 4 + 2 * 1024 * 16 * 2 + 2 * (1024 * 32 + 256 * 64 + 64 * 128 + 16 * 256 + 192) * 2
+                       + 16 * 4)
+
+
+def cnn_block(args, dev):
+    """The learned initial guess's network on its own: inference over one 8,192-stamp chunk
+    (the proposal's chunk) and Adam training steps (batch 512, the training batch, and 4,096),
+    on the tcgen05 path and on the mma.sync path; then stamps/s of the whole training loop
+    (rendering the training stamps included) on the tcgen05 path."""
+    import ctypes
+
+    import torch
+
+    from astrophot_gb300 import _native as N
+    from astrophot_gb300 import cnn
+
+    peaks = measured_peaks()
+    n = 8192
+    net = cnn.InitNet(device=dev, seed=1)
+    st = cnn.make_stamps(n, args.seed + 17, device=dev)
+    x, lscale = net.prepare(st.data, st.sigma, n)
+    raw = cnn._targets(torch.tensor(st.truth, device=dev), lscale)
+    net.set_statistics(raw)
+    t = ((raw - net.mean.double()) / net.std.double()).float().contiguous()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    lib = N.lib()
+    old = cnn.get_tensor_path()
+    out = {"chunk_stamps": n, "flop_per_stamp": CNN_FLOP_PER_STAMP, "min_bytes_per_stamp": CNN_BYTES_PER_STAMP,
+           "peaks": peaks}
+    try:
+        for path in ("tcgen05", "mma_sync"):
+            cnn.set_tensor_path(path)
+            res = {}
+            for _ in range(3):
+                net.infer(x, n)
+            torch.cuda.synchronize()
+            reps = 10
+            e0.record()
+            for _ in range(reps):
+                net.infer(x, n)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            tf = CNN_FLOP_PER_STAMP * n / (ms * 1e-3) / 1e12
+            gbs = CNN_BYTES_PER_STAMP * n / (ms * 1e-3) / 1e9
+            res["infer_ms_per_chunk"] = ms
+            res["infer_stamps_per_s"] = n / (ms * 1e-3)
+            res["infer_tflops"] = tf
+            res["infer_frac_of_bf16_peak"] = tf / peaks["bf16_tflops"] if peaks.get("bf16_tflops") else None
+            res["infer_min_traffic_gbs"] = gbs
+            res["infer_frac_of_hbm_peak"] = gbs / peaks["hbm_gbs"] if peaks.get("hbm_gbs") else None
+            for batch in (512, 4096):
+                p0 = net.params.clone()
+                m1 = torch.zeros_like(net.params)
+                m2 = torch.zeros_like(net.params)
+                grads = torch.zeros_like(net.params)
+                loss = torch.zeros(1, dtype=torch.float64, device=dev)
+                ws = net._workspace(batch)
+                steps = n // batch
+
+                def run(k0):
+                    for j in range(steps):
+                        b0 = j * batch
+                        N.check(lib.ap_cnn_train_step(
+                            N._ptr(net.params), N._ptr(net.params_bf16), N._ptr(grads), N._ptr(m1), N._ptr(m2),
+                            N._ptr(x[b0 * 4096:]), N._ptr(t[b0:]), batch, ctypes.c_float(1e-4), k0 + j + 1,
+                            ctypes.c_float(1e-4), N._ptr(loss), N._ptr(ws), ws.numel(), N._stream()),
+                            "ap_cnn_train_step")
+
+                run(0)
+                torch.cuda.synchronize()
+                e0.record()
+                run(steps)
+                e1.record()
+                torch.cuda.synchronize()
+                ms = e0.elapsed_time(e1)
+                res[f"train_b{batch}_ms_per_step"] = ms / steps
+                res[f"train_b{batch}_stamps_per_s"] = n / (ms * 1e-3)
+                # forward + backward: three GEMMs of the forward's size per layer
+                res[f"train_b{batch}_tflops"] = 3 * CNN_FLOP_PER_STAMP * n / (ms * 1e-3) / 1e12
+                net.params.copy_(p0)
+                net._sync_bf16()
+            out[path] = res
+        cnn.set_tensor_path("tcgen05")
+        # whole training loop: stamps rendered on the GPU, prepared, then Adam steps of 512
+        loop_stamps = 4 * n
+        net2 = cnn.InitNet(device=dev, seed=2)
+        net2.train(n_stamps=n, batch=512, chunk=n, seed=5)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        net2.train(n_stamps=loop_stamps, batch=512, chunk=n, seed=6)
+        torch.cuda.synchronize()
+        out["train_loop_stamps_per_s"] = loop_stamps / (time.perf_counter() - t0)
+        out["train_loop"] = f"{loop_stamps} fresh rendered stamps, chunks of {n}, Adam batch 512, tcgen05 path"
+        out["tc_status"] = cnn.tc_status()
+    finally:
+        cnn.set_tensor_path(old)
+    out["tcgen05_over_mma_sync_infer"] = out["mma_sync"]["infer_ms_per_chunk"] / out["tcgen05"]["infer_ms_per_chunk"]
+    out["tcgen05_over_mma_sync_train_b512"] = (out["mma_sync"]["train_b512_ms_per_step"]
+                                              / out["tcgen05"]["train_b512_ms_per_step"])
+    return out
 
 
 def c0_block(args, dev):

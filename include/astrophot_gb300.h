@@ -429,6 +429,10 @@ int64_t ap_cnn_param_count(void);
  * also forgets the choices made so far.  tuned_shapes (may be NULL) = shapes tuned so far. */
 int ap_cnn_autotune(int32_t enable, int32_t* tuned_shapes);
 size_t ap_cnn_workspace_bytes(int64_t batch);
+/* Byte offsets in a workspace of `batch` stamps (host outputs): act_offsets[6] of the bf16
+ * activations each layer keeps for the backward pass ([rows][N], rows = batch * hout^2; layer 6
+ * keeps none) and out_offset of the fp32 outputs [batch][16]. */
+int ap_cnn_workspace_offsets(int64_t batch, int64_t* act_offsets, int64_t* out_offset);
 /* w_offsets[6], b_offsets[6], dims[6][6] = {cin, cout, hin, hout, K, N} per layer (host). */
 int ap_cnn_layer_offsets(int64_t* w_offsets, int64_t* b_offsets, int32_t* dims);
 int ap_cnn_to_bf16(const float* params, void* params_bf16, ap_stream_t stream);
@@ -436,6 +440,10 @@ int ap_cnn_to_bf16(const float* params, void* params_bf16, ap_stream_t stream);
  * outputs in columns 0..7).  The workspace keeps the activations for ap_cnn_backward. */
 int ap_cnn_forward(const float* params, const void* params_bf16, const float* x, int64_t batch,
                    float* out, void* ws, size_t ws_bytes, ap_stream_t stream);
+/* The same outputs as ap_cnn_forward for inference only: on the tcgen05 path the convolutions
+ * read the activations directly and no im2col matrix is built, so ap_cnn_backward may not follow. */
+int ap_cnn_infer(const float* params, const void* params_bf16, const float* x, int64_t batch,
+                 float* out, void* ws, size_t ws_bytes, ap_stream_t stream);
 /* grads (flat fp32) of a loss with d loss / d out = dout[batch][16], after ap_cnn_forward on the
  * same workspace. */
 int ap_cnn_backward(const void* params_bf16, const float* dout, int64_t batch, float* grads,
@@ -469,6 +477,32 @@ int ap_select_init(const double* proposal, const double* fallback, const double*
 int ap_gemm_bf16(const void* A, int32_t lda, int32_t a_trans, const void* B, int32_t ldb,
                  int32_t b_trans, float* C, int32_t ldc, int32_t R, int32_t S, int32_t T,
                  ap_stream_t stream);
+
+/* Which tensor-core path the CNN forward and training step run: AP_CNN_TCGEN05 (default:
+ * tcgen05.mma with the accumulator in tensor memory, operands staged by TMA; the inference
+ * forward reads the convolution inputs straight from the NHWC activations, no im2col matrix) or
+ * AP_CNN_MMA_SYNC (ldmatrix + mma.sync tiles over explicit im2col matrices).  The backward GEMMs
+ * (reduction-strided operands) run on the mma.sync tiles in both modes. */
+#define AP_CNN_MMA_SYNC 0
+#define AP_CNN_TCGEN05 1
+int ap_cnn_set_path(int32_t path);
+int ap_cnn_get_path(int32_t* path);
+/* C[R][S] = sum_t A[r*lda+t] W[s*ldw+t] (+ bias[s], ReLU, bf16 store into act when act is set;
+ * else fp32 into C, row stride ldc) through the tcgen05 kernel.  S and T multiples of 16, lda and
+ * ldw of 8, pointers 16-byte aligned. */
+int ap_gemm_bf16_tc(const void* A, int32_t lda, const void* W, int32_t ldw, float* C, int32_t ldc,
+                    int32_t R, int32_t S, int32_t T, const float* bias, void* act, int32_t relu,
+                    ap_stream_t stream);
+/* 3x3 stride-2 pad-1 convolution of x[batch][H][H][cin] (NHWC bf16; cin 16, 32 or a multiple of
+ * 64) with W[S][9*cin] (k = (ky*3 + kx)*cin + c) through the tcgen05 kernel, each A tile one
+ * strided 4-D TMA load: out row (b*H/2 + oy)*H/2 + ox, epilogue as ap_gemm_bf16_tc. */
+int ap_conv3x3s2_bf16_tc(const void* x, int64_t batch, int32_t H, int32_t cin, const void* W,
+                         int32_t S, float* C, int32_t ldc, const float* bias, void* act,
+                         int32_t relu, ap_stream_t stream);
+/* First error code a tcgen05 kernel recorded (0 none; 1-3: an mbarrier wait that ran out of its
+ * 200 ms limit, after which the kernel stopped, freed its tensor memory and returned, and every
+ * later launch returns at once).  clear != 0 resets it.  Synchronises the device. */
+int ap_tc_status(int32_t clear, uint32_t* code);
 
 /* Library version string. */
 const char* ap_version(void);
