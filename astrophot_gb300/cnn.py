@@ -53,7 +53,7 @@ def get_tensor_path() -> str:
 
 
 def tc_status(clear: bool = False) -> int:
-    """Error code recorded by a tcgen05 kernel (0: none; 1-3: an mbarrier wait ran out)."""
+    """Error code recorded by a tcgen05 kernel (0: none; 1-5: an mbarrier wait ran out)."""
     v = ctypes.c_uint32(0)
     N.check(N.lib().ap_tc_status(1 if clear else 0, ctypes.byref(v)), "ap_tc_status")
     return int(v.value)

@@ -263,7 +263,8 @@ struct ConvIO {
 };
 
 // dynamic shared memory of the convolve pass for a kpx x kpy kernel: 3 kernels stored
-// transposed with columns padded to a multiple of 4 floats, and the input tile
+// transposed with columns padded to a multiple of 4 floats, and two input tiles (the next
+// plane's is filled while this one is convolved)
 __host__ __device__ inline int conv_col_stride(int kpy) { return (kpy + 3) & ~3; }
 // Row pitch of the column-major input tile: at least its kOutTileY + kpy - 1 rows plus the
 // 2 rows that the last float4 of a column may overrun, and 4 mod 8 so that the 8 lanes of a
@@ -275,7 +276,7 @@ __host__ __device__ inline int conv_tile_pitch(int kpy) {
 
 __host__ __device__ inline size_t conv_smem_bytes(int kpx, int kpy) {
   return sizeof(float) * (3 * (size_t)kpx * conv_col_stride(kpy) +
-                          (size_t)(kOutTileX + kpx - 1) * conv_tile_pitch(kpy));
+                          2 * (size_t)(kOutTileX + kpx - 1) * conv_tile_pitch(kpy));
 }
 
 __host__ __device__ inline int64_t work_plane(const BatchArgs& b, int slot, int plane) {

@@ -147,7 +147,7 @@ cudaError_t tc_gemm(const __nv_bfloat16* A, int lda, const __nv_bfloat16* W, int
 // of 64) with W[S][9 * cin] (t = (ky * 3 + kx) * cin + c); rows r = (b * H/2 + oy) * H/2 + ox
 cudaError_t tc_conv3x3s2(const __nv_bfloat16* act_in, int64_t B, int H, int cin, const __nv_bfloat16* W, int S,
                          float* C, int ldc, const TcEpilogue& ep, cudaStream_t st);
-// first error code recorded by a tensor-core GEMM (0 none; 1-3 a wait that ran out), cleared on
+// first error code recorded by a tensor-core GEMM (0 none; 1-5 a wait that ran out), cleared on
 // request; reading it synchronises the device
 unsigned tc_error(bool clear);
 

@@ -1560,33 +1560,62 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
     const int row0 = y0 + st.by - cy, col0 = x0 + st.bx - cx;
     // difference: dm = K1 * dS (plane 1) + dK * S0 (the base's deep image)
     const int nsrc = diff ? nk : nplanes;
-    for (int pl = 0; pl < nsrc; ++pl) {
-      if (!diff && pl > 0 && shiftmode && !(ops & OP_VJP_COORD) && (pl - 1 == GX || pl - 1 == GY)) continue;
-      if (!diff && pl > 0 && !profile_has_n(b.kind) && pl - 1 == GN) continue;
-      __syncthreads();
+    // the planes this evaluation convolves, in order (the others are skipped)
+    auto next_plane = [&](int pl) {
+      for (; pl < nsrc; ++pl) {
+        if (!diff && pl > 0 && shiftmode && !(ops & OP_VJP_COORD) && (pl - 1 == GX || pl - 1 == GY)) continue;
+        if (!diff && pl > 0 && !profile_has_n(b.kind) && pl - 1 == GN) continue;
+        break;
+      }
+      return pl;
+    };
+    // input tile of plane pl into buffer Tb by asynchronous copies (one commit group): rows over
+    // warps, columns over lanes, coalesced reads; stored column-major (pitch TP), out-of-range
+    // cells and rows TH..TP-1 zero-filled by the copies themselves
+    auto fill = [&](float* Tb, int pl) {
       const float* src = diff ? (pl == 0 ? b.work + work_plane(b, slot, 1) : b.base_deep) + st.work_off
                               : b.work + work_plane(b, slot, pl) + st.work_off;
-      // rows over warps, columns over lanes: coalesced reads; stored column-major (pitch TP,
-      // rows TH..TP-1 zero)
       for (int r = tg; r < TP; r += kConvThreads / 32) {
         const int wr = row0 + r;
         const bool rok = (r < TH && wr >= 0 && wr < st.wny);
-        const float* srow = src + (int64_t)wr * st.wnx;
+        const float* srow = src + (int64_t)(rok ? wr : 0) * st.wnx;
         for (int c = tx; c < TW; c += 32) {
           const int wc = col0 + c;
-          Tt[c * TP + r] = (rok && wc >= 0 && wc < st.wnx) ? srow[wc] : 0.f;
+          const bool ok = rok && wc >= 0 && wc < st.wnx;
+          const uint32_t dst = (uint32_t)__cvta_generic_to_shared(Tb + c * TP + r);
+          asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(dst), "l"(ok ? srow + wc : src),
+                       "r"(ok ? 4 : 0)
+                       : "memory");
         }
       }
+      asm volatile("cp.async.commit_group;\n" ::: "memory");
+    };
+    // two tile buffers: the next plane's copies run while this plane is convolved
+    const int tsz = TW * TP;
+    int cur = next_plane(0), bi = 0;
+    if (cur < nsrc) fill(Tt, cur);
+    while (cur < nsrc) {
+      const int nxt = next_plane(cur + 1);
+      if (nxt < nsrc) {
+        fill(Tt + (bi ? 0 : tsz), nxt);
+        asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+      } else {
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+      }
       __syncthreads();
+      const int pl = cur;
       const int nkp = (diff || pl > 0) ? 1 : nk;
       for (int kk = 0; kk < nkp; ++kk) {
         float outv[kConvRows];
         const int kidx = diff ? pl : kk;
-        conv_col(Tt, TP, KT + kidx * kstride, kpx, kpy, tx, tg * kConvRows, outv);
+        conv_col(Tt + (bi ? tsz : 0), TP, KT + kidx * kstride, kpx, kpy, tx, tg * kConvRows, outv);
         const int dst = diff ? pl : ((pl == 0) ? kk : 3 + (pl - 1));
 #pragma unroll
         for (int o = 0; o < kConvRows; ++o) cv[dst][o] = outv[o];
       }
+      __syncthreads();  // buffer bi is refilled by the next iteration's prefetch
+      cur = nxt;
+      bi ^= 1;
     }
   }
 

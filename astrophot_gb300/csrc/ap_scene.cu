@@ -221,62 +221,92 @@ __global__ void k_damp(const double* __restrict__ H, double L, int n, double* __
 
 constexpr int kNB = 32;
 
-// factor the diagonal block [k0, k0 + nb) in place (lower Cholesky); info = 1 + row on failure
-__global__ void k_chol_diag(double* __restrict__ A, int n, int k0, int* __restrict__ info) {
-  __shared__ double S[kNB][kNB + 1];
-  const int nb = min(kNB, n - k0);
-  for (int i = threadIdx.x; i < nb * nb; i += blockDim.x) S[i / nb][i % nb] = A[(int64_t)(k0 + i / nb) * n + k0 + i % nb];
-  __syncthreads();
+__device__ __forceinline__ double warp_sum_d(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Factor the nb x nb diagonal block D (lower Cholesky, in shared memory) with one warp, lane =
+// row.  A non-positive or non-finite pivot records info = 1 + row (the first one, when
+// `report`) and continues with pivot 1.
+__device__ void chol_diag_warp(double (*D)[kNB + 1], int nb, int k0, int* info, bool report) {
+  const int lane = threadIdx.x & 31;
   for (int j = 0; j < nb; ++j) {
-    if (threadIdx.x == 0) {
-      const double d = S[j][j];
+    if (lane == j) {
+      const double d = D[j][j];
       if (!(d > 0.0) || !isfinite(d)) {
-        if (*info == 0) *info = 1 + k0 + j;
-        S[j][j] = 1.0;
+        if (report) atomicCAS(info, 0, 1 + k0 + j);
+        D[j][j] = 1.0;
       } else {
-        S[j][j] = sqrt(d);
+        D[j][j] = sqrt(d);
       }
     }
-    __syncthreads();
-    const double djj = S[j][j];
-    for (int i = j + 1 + threadIdx.x; i < nb; i += blockDim.x) S[i][j] /= djj;
-    __syncthreads();
-    for (int t = threadIdx.x; t < (nb - j - 1) * (nb - j - 1); t += blockDim.x) {
-      const int i = j + 1 + t / (nb - j - 1), c = j + 1 + t % (nb - j - 1);
-      if (c <= i) S[i][c] -= S[i][j] * S[c][j];
+    __syncwarp();
+    const double djj = D[j][j];
+    if (lane > j && lane < nb) D[lane][j] /= djj;
+    __syncwarp();
+    if (lane > j && lane < nb) {
+      const double lij = D[lane][j];
+      for (int c = j + 1; c <= lane; ++c) D[lane][c] -= lij * D[c][j];
     }
-    __syncthreads();
-  }
-  for (int i = threadIdx.x; i < nb * nb; i += blockDim.x) {
-    const int r = i / nb, c = i % nb;
-    A[(int64_t)(k0 + r) * n + k0 + c] = (c <= r) ? S[r][c] : 0.0;
+    __syncwarp();
   }
 }
 
-// panel below the diagonal block: X L^T = A[k0+nb:, k0:k0+nb]  (one thread per row)
-__global__ void k_chol_panel(double* __restrict__ A, int n, int k0) {
-  __shared__ double Ld[kNB][kNB + 1];
+// Column step k0: every block (one warp) factors the diagonal block itself, from A, and solves
+// its 32 rows of the panel below (X L^T = A[k0+nb:, k0:k0+nb], lane = row).  The factored
+// diagonal block goes to dscr (block 0), copied into A by the trailing update, which reads no
+// diagonal entry: A's diagonal block stays unmodified while the other blocks read it.  On the
+// last step (no rows below, one block) it is written into A directly.
+__global__ void __launch_bounds__(32) k_chol_panel(double* __restrict__ A, int n, int k0, int* __restrict__ info,
+                                                   double* __restrict__ dscr) {
+  __shared__ double D[kNB][kNB + 1];
   const int nb = min(kNB, n - k0);
-  for (int i = threadIdx.x; i < nb * nb; i += blockDim.x) Ld[i / nb][i % nb] = A[(int64_t)(k0 + i / nb) * n + k0 + i % nb];
-  __syncthreads();
-  const int r = k0 + nb + blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x;
+  for (int i = 0; i < nb; ++i)
+    if (lane < nb) D[i][lane] = A[(int64_t)(k0 + i) * n + k0 + lane];
+  __syncwarp();
+  chol_diag_warp(D, nb, k0, info, blockIdx.x == 0);
+  const bool last = (k0 + nb >= n);
+  if (blockIdx.x == 0 && lane < nb) {
+    for (int i = 0; i < nb; ++i) {
+      const double v = lane <= i ? D[i][lane] : 0.0;
+      if (last)
+        A[(int64_t)(k0 + i) * n + k0 + lane] = v;
+      else
+        dscr[i * kNB + lane] = v;
+    }
+  }
+  const int r = k0 + nb + blockIdx.x * 32 + lane;
   if (r >= n) return;
   double x[kNB];
   double* row = A + (int64_t)r * n + k0;
-  for (int j = 0; j < nb; ++j) {
+#pragma unroll
+  for (int j = 0; j < kNB; ++j) {
+    if (j >= nb) break;
     double v = row[j];
-    for (int c = 0; c < j; ++c) v -= x[c] * Ld[j][c];
-    x[j] = v / Ld[j][j];
+#pragma unroll
+    for (int c = 0; c < j; ++c) v -= x[c] * D[j][c];
+    x[j] = v / D[j][j];
   }
-  for (int j = 0; j < nb; ++j) row[j] = x[j];
+#pragma unroll
+  for (int j = 0; j < kNB; ++j)
+    if (j < nb) row[j] = x[j];
 }
 
-// trailing update: A[i][j] -= sum_c P[i][c] P[j][c] for k0 + nb <= j <= i (tiles of 32 x 32)
-__global__ void k_chol_update(double* __restrict__ A, int n, int k0) {
+// trailing update: A[i][j] -= sum_c P[i][c] P[j][c] for k0 + nb <= j <= i (tiles of 32 x 32);
+// block (0, 0) also stores the factored diagonal block of this step from dscr
+__global__ void k_chol_update(double* __restrict__ A, int n, int k0, const double* __restrict__ dscr) {
   const int nb = min(kNB, n - k0);
   const int base = k0 + nb;
   const int ti = blockIdx.y, tj = blockIdx.x;
   if (tj > ti) return;
+  if (ti == 0 && tj == 0) {
+    for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
+      const int r = t / nb, c = t % nb;
+      A[(int64_t)(k0 + r) * n + k0 + c] = dscr[r * kNB + c];
+    }
+  }
   __shared__ double Pi[kNB][kNB + 1], Pj[kNB][kNB + 1];
   const int i0 = base + ti * kNB, j0 = base + tj * kNB;
   for (int t = threadIdx.x; t < kNB * kNB; t += blockDim.x) {
@@ -296,63 +326,78 @@ __global__ void k_chol_update(double* __restrict__ A, int n, int k0) {
   }
 }
 
-// L y = b then L^T x = y, one block, in 32-row blocks: warp 0 solves a diagonal block with
-// shuffles (no block barrier per row), then all threads apply it to the remaining rows
-__global__ void k_chol_solve(const double* __restrict__ A, int n, const double* __restrict__ b,
-                             double* __restrict__ x, double* __restrict__ y) {
-  __shared__ double yb[kNB];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) y[i] = b[i];
+// the lower nb x nb diagonal block at kb into shared memory (upper part zero)
+__device__ __forceinline__ void load_diag(const double* __restrict__ A, int n, int kb, int nb,
+                                          double (*D)[kNB + 1]) {
+  for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
+    const int i = t / nb, c = t % nb;
+    D[i][c] = (c <= i) ? A[(int64_t)(kb + i) * n + kb + c] : 0.0;
+  }
+}
+
+// Forward substitution L z = b, column block kb: every block solves the small triangle for
+// z[kb..kb+nb) from y (warp 0, shuffles; block 0 stores it), then the rows below are updated,
+// y[i] -= L[i][kb..kb+nb) . z_kb, one warp per row (coalesced row segments).  Blocks read only
+// y[kb..kb+nb) and write only rows beyond it.
+__global__ void __launch_bounds__(256) k_trsv_fwd(const double* __restrict__ A, int n, int kb,
+                                                  double* __restrict__ y, double* __restrict__ z) {
+  __shared__ double D[kNB][kNB + 1];
+  __shared__ double zb[kNB];
+  const int nb = min(kNB, n - kb);
+  load_diag(A, n, kb, nb, D);
   __syncthreads();
-  for (int kb = 0; kb < n; kb += kNB) {
-    const int nb = min(kNB, n - kb);
-    if (warp == 0) {
-      double v = lane < nb ? y[kb + lane] : 0.0;
-      for (int c = 0; c < nb; ++c) {
-        if (lane == c) v = v / A[(int64_t)(kb + c) * n + kb + c];
-        const double vc = __shfl_sync(0xffffffffu, v, c);
-        if (lane > c && lane < nb) v -= A[(int64_t)(kb + lane) * n + kb + c] * vc;
-      }
-      if (lane < nb) {
-        y[kb + lane] = v;
-        yb[lane] = v;
-      }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp == 0) {
+    double v = lane < nb ? y[kb + lane] : 0.0;
+    for (int c = 0; c < nb; ++c) {
+      if (lane == c) v = v / D[c][c];
+      const double vc = __shfl_sync(0xffffffffu, v, c);
+      if (lane > c && lane < nb) v -= D[lane][c] * vc;
     }
-    __syncthreads();
-    for (int i = kb + nb + threadIdx.x; i < n; i += blockDim.x) {
-      const double* row = A + (int64_t)i * n + kb;
-      double acc = 0.0;
-      for (int c = 0; c < nb; ++c) acc += row[c] * yb[c];
-      y[i] -= acc;
+    if (lane < nb) {
+      zb[lane] = v;
+      if (blockIdx.x == 0) z[kb + lane] = v;
     }
-    __syncthreads();
   }
-  const int last = ((n - 1) / kNB) * kNB;
-  for (int kb = last; kb >= 0; kb -= kNB) {
-    const int nb = min(kNB, n - kb);
-    if (warp == 0) {
-      // L^T block is upper triangular: rows from the bottom up
-      double v = lane < nb ? y[kb + lane] : 0.0;
-      for (int c = nb - 1; c >= 0; --c) {
-        if (lane == c) v = v / A[(int64_t)(kb + c) * n + kb + c];
-        const double vc = __shfl_sync(0xffffffffu, v, c);
-        if (lane < c) v -= A[(int64_t)(kb + c) * n + kb + lane] * vc;
-      }
-      if (lane < nb) {
-        y[kb + lane] = v;
-        yb[lane] = v;
-      }
-    }
-    __syncthreads();
-    // rows above: y[i] -= sum_c L[kb + c][i] x[kb + c]  (coalesced over i)
-    for (int i = threadIdx.x; i < kb; i += blockDim.x) {
-      double acc = 0.0;
-      for (int c = 0; c < nb; ++c) acc += A[(int64_t)(kb + c) * n + i] * yb[c];
-      y[i] -= acc;
-    }
-    __syncthreads();
+  __syncthreads();
+  const int nw = blockDim.x >> 5;
+  for (int i = kb + nb + blockIdx.x * nw + warp; i < n; i += gridDim.x * nw) {
+    double p = lane < nb ? A[(int64_t)i * n + kb + lane] * zb[lane] : 0.0;
+    p = warp_sum_d(p);
+    if (lane == 0) y[i] -= p;
   }
-  for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = y[i];
+}
+
+// Back substitution L^T x = z (z updated in place as the right-hand side), column block kb
+// from the last: x[kb..kb+nb) from z (warp 0; block 0 stores it), then z[i] -= sum_c
+// L[kb+c][i] x_kb[c] for i < kb, one thread per row (coalesced over i).
+__global__ void __launch_bounds__(256) k_trsv_bwd(const double* __restrict__ A, int n, int kb,
+                                                  double* __restrict__ z, double* __restrict__ x) {
+  __shared__ double D[kNB][kNB + 1];
+  __shared__ double xb[kNB];
+  const int nb = min(kNB, n - kb);
+  load_diag(A, n, kb, nb, D);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp == 0) {
+    // L^T's diagonal block is upper triangular: rows from the bottom up
+    double v = lane < nb ? z[kb + lane] : 0.0;
+    for (int c = nb - 1; c >= 0; --c) {
+      if (lane == c) v = v / D[c][c];
+      const double vc = __shfl_sync(0xffffffffu, v, c);
+      if (lane < c) v -= D[c][lane] * vc;
+    }
+    if (lane < nb) {
+      xb[lane] = v;
+      if (blockIdx.x == 0) x[kb + lane] = v;
+    }
+  }
+  __syncthreads();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kb; i += gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int c = 0; c < nb; ++c) acc += A[(int64_t)(kb + c) * n + i] * xb[c];
+    z[i] -= acc;
+  }
 }
 
 inline int egrid(int64_t n) {
@@ -469,8 +514,29 @@ int ap_scene_rpp_image(const float* r, const float* rh, const float* jh, const f
 
 size_t ap_dense_solve_workspace_bytes(int32_t n) {
   if (n <= 0) return 0;
-  return sizeof(double) * ((size_t)n * n + n) + sizeof(int) * 4;
+  // A (n x n), y and z (n each), the factored diagonal block of the current step
+  return sizeof(double) * ((size_t)n * n + 2 * (size_t)n + kNB * kNB) + sizeof(int) * 4;
 }
+
+namespace {
+// both triangular solves on the factor in the workspace: L z = g, then L^T h = z
+cudaError_t chol_solves(int n, const double* A, const double* g, double* h, double* y, double* z, cudaStream_t st) {
+  cudaError_t e = cudaMemcpyAsync(y, g, sizeof(double) * n, cudaMemcpyDeviceToDevice, st);
+  if (e != cudaSuccess) return e;
+  for (int kb = 0; kb < n; kb += kNB) {
+    const int rows = n - kb - (n - kb < kNB ? n - kb : kNB);
+    int grid = (rows + 7) / 8;
+    grid = grid < 1 ? 1 : (grid > 1024 ? 1024 : grid);
+    k_trsv_fwd<<<grid, 256, 0, st>>>(A, n, kb, y, z);
+  }
+  for (int kb = ((n - 1) / kNB) * kNB; kb >= 0; kb -= kNB) {
+    int grid = (kb + 255) / 256;
+    grid = grid < 1 ? 1 : grid;
+    k_trsv_bwd<<<grid, 256, 0, st>>>(A, n, kb, z, h);
+  }
+  return cudaGetLastError();
+}
+}  // namespace
 
 int ap_dense_damped_solve(int32_t n, const double* H, const double* g, double L, double* h, void* ws,
                           size_t ws_bytes, int32_t* info, ap_stream_t stream) {
@@ -479,21 +545,21 @@ int ap_dense_damped_solve(int32_t n, const double* H, const double* g, double L,
   cudaStream_t st = (cudaStream_t)stream;
   double* A = (double*)ws;
   double* y = A + (size_t)n * n;
+  double* z = y + n;
+  double* dscr = z + n;
   int rc = record_cuda(cudaMemsetAsync(info, 0, sizeof(int32_t), st));
   if (rc) return rc;
   k_damp<<<egrid((int64_t)n * n), 256, 0, st>>>(H, L, n, A);
   for (int k0 = 0; k0 < n; k0 += kNB) {
-    k_chol_diag<<<1, 256, 0, st>>>(A, n, k0, info);
     const int nb = n - k0 < kNB ? n - k0 : kNB;
     const int rest = n - k0 - nb;
+    k_chol_panel<<<rest > 0 ? (rest + 31) / 32 : 1, 32, 0, st>>>(A, n, k0, info, dscr);
     if (rest > 0) {
-      k_chol_panel<<<(rest + 127) / 128, 128, 0, st>>>(A, n, k0);
       const int nt = (rest + kNB - 1) / kNB;
-      k_chol_update<<<dim3(nt, nt), 256, 0, st>>>(A, n, k0);
+      k_chol_update<<<dim3(nt, nt), 256, 0, st>>>(A, n, k0, dscr);
     }
   }
-  k_chol_solve<<<1, 1024, 0, st>>>(A, n, g, h, y);
-  return record_cuda(cudaGetLastError());
+  return record_cuda(chol_solves(n, A, g, h, y, z, st));
 }
 
 int ap_dense_factored_solve(int32_t n, const double* g, double* h, void* ws, size_t ws_bytes, ap_stream_t stream) {
@@ -501,8 +567,8 @@ int ap_dense_factored_solve(int32_t n, const double* g, double* h, void* ws, siz
   if (ws_bytes < ap_dense_solve_workspace_bytes(n)) return AP_ERR_WORKSPACE;
   double* A = (double*)ws;
   double* y = A + (size_t)n * n;
-  k_chol_solve<<<1, 1024, 0, (cudaStream_t)stream>>>(A, n, g, h, y);
-  return record_cuda(cudaGetLastError());
+  double* z = y + n;
+  return record_cuda(chol_solves(n, A, g, h, y, z, (cudaStream_t)stream));
 }
 
 }  // extern "C"

@@ -11,9 +11,11 @@
 //          coordinates (the padding) read as zeros, and no im2col matrix is written or read.
 // Epilogue: fp32 store of C, or bias (+ ReLU) and a bf16 store of the activation.
 //
-// CTA = 128 threads, one 128 x BN output tile.  Thread 0 issues the TMA loads, thread 32 (one
-// elected thread) the MMAs; all four warps read the accumulator back with tcgen05.ld (warp w owns
-// TMEM lanes 32w..32w+31 = tile rows 32w..32w+31).  Every mbarrier wait is bounded by wall clock:
+// Persistent CTAs of 192 threads over 128 x BN output tiles.  Warp 0 (one lane) issues the TMA
+// loads through a ring of stages, warp 1 (one lane) the MMAs into one of two TMEM accumulators,
+// warps 2-5 read the other accumulator back with tcgen05.ld (warp w owns TMEM lanes
+// 32(w%4)..32(w%4)+31 = tile rows) while the next tile accumulates.  Every mbarrier wait is
+// bounded by wall clock:
 // on a timeout the kernel records an error code, stops issuing, waits (bounded) for its copies and
 // MMAs in flight, frees its tensor memory and returns; later launches see the code and return at
 // once.  ap_tc_status reads (and clears) the code.
@@ -34,7 +36,7 @@ typedef __nv_bfloat16 bf16;
 
 __device__ unsigned int g_tc_error;  // first error code of a tensor-core GEMM (0 = none)
 
-enum TcError : unsigned { TC_ERR_EMPTY = 1, TC_ERR_FULL = 2, TC_ERR_DONE = 3 };
+enum TcError : unsigned { TC_ERR_EMPTY = 1, TC_ERR_FULL = 2, TC_ERR_DONE = 3, TC_ERR_TEMPTY = 4, TC_ERR_TFULL = 5 };
 
 constexpr unsigned long long kWaitNs = 200ull * 1000 * 1000;   // one wait: 200 ms
 constexpr unsigned long long kDrainNs = 20ull * 1000 * 1000;   // draining after an abort
@@ -142,6 +144,10 @@ __host__ __device__ constexpr uint32_t instr_desc() {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
 }
 
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
 struct TcArgs {
   float* C;           // fp32 output (act == nullptr)
   bf16* act;          // bf16 output of bias (+ ReLU)
@@ -149,6 +155,7 @@ struct TcArgs {
   int ldc, R, relu;
   int ktiles;         // reduction tiles of BK elements
   int k16_last;       // K = 16 MMAs in the last tile
+  int ntn, ntiles;    // output tiles along S, in all
   int conv;           // implicit convolution (else dense)
   int cin, cchunks;   // conv: input channels, channel chunks of BK per tap
   int hout;           // conv: output side
@@ -160,21 +167,31 @@ struct TcCfg {
   static constexpr int A_BYTES = 128 * SW;
   static constexpr int B_BYTES = BN * SW;
   static constexpr int STAGE = A_BYTES + B_BYTES;
-  static constexpr int STAGES_RAW = 104448 / STAGE;  // ~102 KB of tiles: two CTAs per SM
-  static constexpr int STAGES = STAGES_RAW < 2 ? 2 : (STAGES_RAW > 8 ? 8 : STAGES_RAW);
   static constexpr int NCOLS = BN <= 32 ? 32 : (BN <= 64 ? 64 : (BN <= 128 ? 128 : 256));
+  // two accumulators per CTA; two CTAs per SM when their 4 x NCOLS TMEM columns fit in 512
+  static constexpr bool TWO_CTAS = 4 * NCOLS <= 512;
+  static constexpr int TILE_BYTES = TWO_CTAS ? 100 * 1024 : 200 * 1024;
+  static constexpr int STAGES_RAW = TILE_BYTES / STAGE;
+  static constexpr int STAGES = STAGES_RAW < 2 ? 2 : (STAGES_RAW > 8 ? 8 : STAGES_RAW);
   static constexpr int SMEM = STAGES * STAGE + 1024;  // + slack to align the tiles to 1 KB
   static_assert(BN % 16 == 0 && BN >= 16 && BN <= 256, "M = 128 MMAs take N = 16..256 in steps of 16");
 };
 
+constexpr int kTcThreads = 192;  // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
+
+// Persistent: CTA c takes output tiles c, c + gridDim.x, ...  The producer runs ahead through the
+// stage ring across tiles; the MMA thread alternates between two TMEM accumulators, so the
+// epilogue warps drain one tile while the next is accumulated.
 template <int SW, int BN>
-__global__ void __launch_bounds__(128) k_gemm_tc(const __grid_constant__ CUtensorMap tmA,
-                                                 const __grid_constant__ CUtensorMap tmB, const TcArgs a) {
+__global__ void __launch_bounds__(kTcThreads) k_gemm_tc(const __grid_constant__ CUtensorMap tmA,
+                                                       const __grid_constant__ CUtensorMap tmB, const TcArgs a) {
   using G = TcCfg<SW, BN>;
   extern __shared__ uint8_t dsm[];
   __shared__ __align__(8) uint64_t bar_full[G::STAGES];
   __shared__ __align__(8) uint64_t bar_empty[G::STAGES];
-  __shared__ __align__(8) uint64_t bar_done;
+  __shared__ __align__(8) uint64_t bar_tfull[2];   // accumulator j ready (tcgen05.commit)
+  __shared__ __align__(8) uint64_t bar_tempty[2];  // accumulator j drained (4 epilogue warps)
+  __shared__ __align__(8) uint64_t bar_drain;
   __shared__ uint32_t tmem_slot;
   __shared__ int aborted;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -188,14 +205,18 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const __grid_constant__ CUtenso
       mbar_init(smem_u32(&bar_full[s]), 1);
       mbar_init(smem_u32(&bar_empty[s]), 1);
     }
-    mbar_init(smem_u32(&bar_done), 1);
+    for (int j = 0; j < 2; ++j) {
+      mbar_init(smem_u32(&bar_tfull[j]), 1);
+      mbar_init(smem_u32(&bar_tempty[j]), 4);
+    }
+    mbar_init(smem_u32(&bar_drain), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmA) : "memory");
     asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmB) : "memory");
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
-                 "r"((uint32_t)G::NCOLS)
+                 "r"((uint32_t)(2 * G::NCOLS))
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -203,113 +224,146 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const __grid_constant__ CUtenso
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_slot;
-  const int m0 = blockIdx.x * 128, n0 = blockIdx.y * BN;
 
-  if (threadIdx.x == 0) {
-    // ---- TMA producer ----
-    int b0 = 0, y0 = 0;
-    if (a.conv) {
-      const int rps = a.hout * a.hout;  // output rows per stamp
-      b0 = m0 / rps;
-      y0 = 2 * ((m0 - b0 * rps) / a.hout);
-    }
-    int kt = 0;
-    for (; kt < a.ktiles; ++kt) {
-      const int s = kt % G::STAGES;
-      const uint32_t ph = (uint32_t)(kt / G::STAGES) & 1u;
-      if (!mbar_wait(smem_u32(&bar_empty[s]), ph ^ 1u, TC_ERR_EMPTY, kWaitNs, true)) break;
-      const uint32_t fb = smem_u32(&bar_full[s]);
-      const uint32_t sa = tiles + (uint32_t)(s * G::STAGE), sb = sa + G::A_BYTES;
-      mbar_expect_tx(fb, (uint32_t)G::STAGE);
-      if (a.conv) {
-        const int tap = kt / a.cchunks, c0 = (kt - tap * a.cchunks) * G::BK;
-        const int ky = tap / 3, kx = tap - ky * 3;
-        tma_4d(sa, &tmA, fb, c0, kx - 1, y0 + ky - 1, b0);
-        tma_2d(sb, &tmB, fb, tap * a.cin + c0, n0);
-      } else {
-        tma_2d(sa, &tmA, fb, kt * G::BK, m0);
-        tma_2d(sb, &tmB, fb, kt * G::BK, n0);
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---- TMA producer ----
+      uint32_t it = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < a.ntiles && ok; t += gridDim.x) {
+        const int m0 = (t / a.ntn) * 128, n0 = (t % a.ntn) * BN;
+        int b0 = 0, y0 = 0;
+        if (a.conv) {
+          const int rps = a.hout * a.hout;  // output rows per stamp
+          b0 = m0 / rps;
+          y0 = 2 * ((m0 - b0 * rps) / a.hout);
+        }
+        for (int kt = 0; kt < a.ktiles; ++kt, ++it) {
+          const int s = (int)(it % G::STAGES);
+          const uint32_t ph = (it / G::STAGES) & 1u;
+          if (!mbar_wait(smem_u32(&bar_empty[s]), ph ^ 1u, TC_ERR_EMPTY, kWaitNs, true)) {
+            ok = false;
+            break;
+          }
+          const uint32_t fb = smem_u32(&bar_full[s]);
+          const uint32_t sa = tiles + (uint32_t)(s * G::STAGE), sb = sa + G::A_BYTES;
+          mbar_expect_tx(fb, (uint32_t)G::STAGE);
+          if (a.conv) {
+            const int tap = kt / a.cchunks, c0 = (kt - tap * a.cchunks) * G::BK;
+            const int ky = tap / 3, kx = tap - ky * 3;
+            tma_4d(sa, &tmA, fb, c0, kx - 1, y0 + ky - 1, b0);
+            tma_2d(sb, &tmB, fb, tap * a.cin + c0, n0);
+          } else {
+            tma_2d(sa, &tmA, fb, kt * G::BK, m0);
+            tma_2d(sb, &tmB, fb, kt * G::BK, n0);
+          }
+        }
+      }
+      if (!ok) {
+        aborted = 1;
+        // let the copies already issued land before the shared memory is released
+        for (uint32_t j = (it > (uint32_t)G::STAGES ? it - G::STAGES : 0); j < it; ++j)
+          mbar_wait(smem_u32(&bar_full[j % G::STAGES]), (j / G::STAGES) & 1u, 0u, kDrainNs, false);
       }
     }
-    if (kt < a.ktiles) {
-      aborted = 1;
-      // let the copies already issued land before the shared memory is released
-      for (int j = (kt > G::STAGES ? kt - G::STAGES : 0); j < kt; ++j)
-        mbar_wait(smem_u32(&bar_full[j % G::STAGES]), (uint32_t)(j / G::STAGES) & 1u, 0u, kDrainNs, false);
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---- MMA issuer ----
+      constexpr uint32_t idesc = instr_desc<BN>();
+      uint32_t it = 0, j = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < a.ntiles && ok; t += gridDim.x, ++j) {
+        const uint32_t acc = j & 1u, aph = (j >> 1) & 1u;
+        if (!mbar_wait(smem_u32(&bar_tempty[acc]), aph ^ 1u, TC_ERR_TEMPTY, kWaitNs, true)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t d = tmem + acc * (uint32_t)G::NCOLS;
+        for (int kt = 0; kt < a.ktiles; ++kt, ++it) {
+          const int s = (int)(it % G::STAGES);
+          const uint32_t ph = (it / G::STAGES) & 1u;
+          if (!mbar_wait(smem_u32(&bar_full[s]), ph, TC_ERR_FULL, kWaitNs, true)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t sa = tiles + (uint32_t)(s * G::STAGE), sb = sa + G::A_BYTES;
+          const uint64_t da = smem_desc<SW>(sa), db = smem_desc<SW>(sb);
+          const int nk = (kt == a.ktiles - 1) ? a.k16_last : SW / 32;
+          for (int k = 0; k < nk; ++k)  // K = 16 step = 32 bytes along the swizzled row
+            tc_mma(d, da + (uint64_t)(2 * k), db + (uint64_t)(2 * k), idesc, (uint32_t)((kt | k) != 0));
+          tc_commit(smem_u32(&bar_empty[s]));  // frees the stage once these MMAs have read it
+        }
+        if (ok) tc_commit(smem_u32(&bar_tfull[acc]));
+      }
+      if (!ok) aborted = 1;
+      // arrives once every MMA issued above has completed: wait for it before TMEM is freed
+      tc_commit(smem_u32(&bar_drain));
+      mbar_wait(smem_u32(&bar_drain), 0u, TC_ERR_DONE, kWaitNs, false);
     }
-  } else if (threadIdx.x == 32) {
-    // ---- MMA issuer ----
-    constexpr uint32_t idesc = instr_desc<BN>();
-    int kt = 0;
-    for (; kt < a.ktiles; ++kt) {
-      const int s = kt % G::STAGES;
-      const uint32_t ph = (uint32_t)(kt / G::STAGES) & 1u;
-      if (!mbar_wait(smem_u32(&bar_full[s]), ph, TC_ERR_FULL, kWaitNs, true)) break;
+  } else {
+    // ---- epilogue: TMEM -> registers -> bias / ReLU -> global ----
+    const int q = warp & 3;  // TMEM lane quarter this warp may access
+    uint32_t j = 0;
+    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x, ++j) {
+      const uint32_t acc = j & 1u, aph = (j >> 1) & 1u;
+      int got = 0;
+      if (lane == 0) got = mbar_wait(smem_u32(&bar_tfull[acc]), aph, TC_ERR_TFULL, kWaitNs, true) ? 1 : 0;
+      got = __shfl_sync(0xffffffffu, got, 0);
+      if (!got) break;
       tc_fence_after();
-      const uint32_t sa = tiles + (uint32_t)(s * G::STAGE), sb = sa + G::A_BYTES;
-      const uint64_t da = smem_desc<SW>(sa), db = smem_desc<SW>(sb);
-      const int nk = (kt == a.ktiles - 1) ? a.k16_last : SW / 32;
-      for (int k = 0; k < nk; ++k)  // K = 16 step = 32 bytes along the swizzled row
-        tc_mma(tmem, da + (uint64_t)(2 * k), db + (uint64_t)(2 * k), idesc, (uint32_t)((kt | k) != 0));
-      tc_commit(smem_u32(&bar_empty[s]));  // frees the stage once these MMAs have read it
-    }
-    if (kt < a.ktiles) aborted = 1;
-    // always: arrives once every MMA issued above has completed (at once if none was)
-    tc_commit(smem_u32(&bar_done));
-  }
-  __syncwarp();
-
-  // ---- epilogue: TMEM -> registers -> bias / ReLU -> global ----
-  const bool got = mbar_wait(smem_u32(&bar_done), 0u, TC_ERR_DONE, kWaitNs, false);
-  const bool use = __all_sync(0xffffffffu, got) && !*(volatile int*)&aborted;
-  if (use) {
-    tc_fence_after();
-    const int row = m0 + warp * 32 + lane;
-    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+      const int m0 = (t / a.ntn) * 128, n0 = (t % a.ntn) * BN;
+      const int row = m0 + q * 32 + lane;
+      const uint32_t trow = tmem + acc * (uint32_t)G::NCOLS + ((uint32_t)(q * 32) << 16);
 #pragma unroll 1
-    for (int c = 0; c < BN; c += 16) {
-      float v[16];
-      tc_ld16(trow + (uint32_t)c, v);
-      if (row < a.R) {
-        const int col = n0 + c;
-        if (a.bias) {
-          const float4* bp = reinterpret_cast<const float4*>(a.bias + col);
+      for (int c = 0; c < BN; c += 16) {
+        float v[16];
+        tc_ld16(trow + (uint32_t)c, v);
+        if (row < a.R) {
+          const int col = n0 + c;
+          if (a.bias) {
+            const float4* bp = reinterpret_cast<const float4*>(a.bias + col);
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const float4 b = __ldg(bp + q);
-            v[4 * q + 0] += b.x;
-            v[4 * q + 1] += b.y;
-            v[4 * q + 2] += b.z;
-            v[4 * q + 3] += b.w;
+            for (int u = 0; u < 4; ++u) {
+              const float4 bb = __ldg(bp + u);
+              v[4 * u + 0] += bb.x;
+              v[4 * u + 1] += bb.y;
+              v[4 * u + 2] += bb.z;
+              v[4 * u + 3] += bb.w;
+            }
+            if (a.relu) {
+#pragma unroll
+              for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i], 0.f);
+            }
           }
-          if (a.relu) {
+          if (a.act) {
+            uint32_t p[8];
 #pragma unroll
-            for (int j = 0; j < 16; ++j) v[j] = fmaxf(v[j], 0.f);
+            for (int i = 0; i < 8; ++i) {
+              const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+              p[i] = *reinterpret_cast<const uint32_t*>(&h);
+            }
+            uint4* dst = reinterpret_cast<uint4*>(a.act + (int64_t)row * a.ldc + col);
+            dst[0] = make_uint4(p[0], p[1], p[2], p[3]);
+            dst[1] = make_uint4(p[4], p[5], p[6], p[7]);
+          } else {
+            float4* dst = reinterpret_cast<float4*>(a.C + (int64_t)row * a.ldc + col);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) dst[u] = make_float4(v[4 * u], v[4 * u + 1], v[4 * u + 2], v[4 * u + 3]);
           }
-        }
-        if (a.act) {
-          uint32_t p[8];
-#pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
-            p[j] = *reinterpret_cast<const uint32_t*>(&h);
-          }
-          uint4* dst = reinterpret_cast<uint4*>(a.act + (int64_t)row * a.ldc + col);
-          dst[0] = make_uint4(p[0], p[1], p[2], p[3]);
-          dst[1] = make_uint4(p[4], p[5], p[6], p[7]);
-        } else {
-          float4* dst = reinterpret_cast<float4*>(a.C + (int64_t)row * a.ldc + col);
-#pragma unroll
-          for (int q = 0; q < 4; ++q) dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
         }
       }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(smem_u32(&bar_tempty[acc]));
     }
   }
   tc_fence_before();
   __syncthreads();
   if (warp == 0) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)G::NCOLS)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)(2 * G::NCOLS))
                  : "memory");
   }
 }
@@ -343,59 +397,67 @@ bool encode_map(CUtensorMap* m, const void* base, int rank, const cuuint64_t* di
 }
 
 // dynamic shared memory of each instantiation, per device: at least G::SMEM, raised until the
-// CTAs resident on one SM need no more than the 512 TMEM columns (an allocation never waits)
+// CTAs resident on one SM need no more than the 512 TMEM columns (an allocation never waits);
+// with it the resident CTAs per SM, which size the persistent grid
 std::mutex g_cfg_mutex;
 constexpr int kMaxDev = 64;
 
 template <int SW, int BN>
-cudaError_t launch_tc(const CUtensorMap& ta, const CUtensorMap& tb, const TcArgs& a, int gx, int gy,
-                      cudaStream_t st) {
+cudaError_t launch_tc(const CUtensorMap& ta, const CUtensorMap& tb, const TcArgs& a, cudaStream_t st) {
   using G = TcCfg<SW, BN>;
   static int smem_for[kMaxDev] = {0};
+  static int grid_for[kMaxDev] = {0};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= kMaxDev) return cudaErrorInvalidDevice;
-  int smem;
+  int smem, resident;
   {
     std::lock_guard<std::mutex> lock(g_cfg_mutex);
     smem = smem_for[dev];
+    resident = grid_for[dev];
     if (!smem) {
+      int nsm = 0;
+      e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+      if (e != cudaSuccess) return e;
       smem = G::SMEM;
+      int nb = 0;
       for (;;) {
         e = cudaFuncSetAttribute(k_gemm_tc<SW, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
-        int nb = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_gemm_tc<SW, BN>, 128, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_gemm_tc<SW, BN>, kTcThreads, smem);
         if (e != cudaSuccess) return e;
-        if (nb * G::NCOLS <= 512) break;
+        if (nb * 2 * G::NCOLS <= 512) break;
         smem += 4096;
       }
+      if (nb < 1) return cudaErrorInvalidConfiguration;
+      resident = nb * nsm;
       smem_for[dev] = smem;
+      grid_for[dev] = resident;
     }
   }
-  k_gemm_tc<SW, BN><<<dim3((unsigned)gx, (unsigned)gy), 128, smem, st>>>(ta, tb, a);
+  const int grid = a.ntiles < resident ? a.ntiles : resident;
+  k_gemm_tc<SW, BN><<<(unsigned)grid, kTcThreads, smem, st>>>(ta, tb, a);
   return cudaGetLastError();
 }
 
 template <int SW>
-cudaError_t launch_bn(int bn, const CUtensorMap& ta, const CUtensorMap& tb, const TcArgs& a, int gx, int gy,
-                      cudaStream_t st) {
+cudaError_t launch_bn(int bn, const CUtensorMap& ta, const CUtensorMap& tb, const TcArgs& a, cudaStream_t st) {
   switch (bn) {
-    case 16: return launch_tc<SW, 16>(ta, tb, a, gx, gy, st);
-    case 32: return launch_tc<SW, 32>(ta, tb, a, gx, gy, st);
-    case 64: return launch_tc<SW, 64>(ta, tb, a, gx, gy, st);
-    case 128: return launch_tc<SW, 128>(ta, tb, a, gx, gy, st);
-    case 256: return launch_tc<SW, 256>(ta, tb, a, gx, gy, st);
+    case 16: return launch_tc<SW, 16>(ta, tb, a, st);
+    case 32: return launch_tc<SW, 32>(ta, tb, a, st);
+    case 64: return launch_tc<SW, 64>(ta, tb, a, st);
+    case 128: return launch_tc<SW, 128>(ta, tb, a, st);
+    case 256: return launch_tc<SW, 256>(ta, tb, a, st);
     default: return cudaErrorInvalidValue;
   }
 }
 
-cudaError_t launch_sw(int sw, int bn, const CUtensorMap& ta, const CUtensorMap& tb, const TcArgs& a, int gx, int gy,
+cudaError_t launch_sw(int sw, int bn, const CUtensorMap& ta, const CUtensorMap& tb, const TcArgs& a,
                       cudaStream_t st) {
-  if (sw == 128) return launch_bn<128>(bn, ta, tb, a, gx, gy, st);
-  if (sw == 64) return launch_bn<64>(bn, ta, tb, a, gx, gy, st);
-  if (sw == 32) return launch_bn<32>(bn, ta, tb, a, gx, gy, st);
+  if (sw == 128) return launch_bn<128>(bn, ta, tb, a, st);
+  if (sw == 64) return launch_bn<64>(bn, ta, tb, a, st);
+  if (sw == 32) return launch_bn<32>(bn, ta, tb, a, st);
   return cudaErrorInvalidValue;
 }
 
@@ -449,7 +511,11 @@ cudaError_t tc_gemm(const __nv_bfloat16* A, int lda, const __nv_bfloat16* W, int
   a.ktiles = (T + bk - 1) / bk;
   a.k16_last = (T - (a.ktiles - 1) * bk) / 16;
   a.conv = 0;
-  return launch_sw(sw, bn, ta, tb, a, (R + 127) / 128, S / bn, st);
+  a.ntn = S / bn;
+  const int64_t ntiles = (int64_t)((R + 127) / 128) * a.ntn;
+  if (ntiles > INT32_MAX) return cudaErrorInvalidValue;
+  a.ntiles = (int)ntiles;
+  return launch_sw(sw, bn, ta, tb, a, st);
 }
 
 cudaError_t tc_conv3x3s2(const __nv_bfloat16* act_in, int64_t B, int H, int cin, const __nv_bfloat16* W, int S,
@@ -517,7 +583,11 @@ cudaError_t tc_conv3x3s2(const __nv_bfloat16* act_in, int64_t B, int H, int cin,
   a.cin = cin;
   a.cchunks = cchunks;
   a.hout = hout;
-  return launch_sw(sw, bn, ta, tb, a, (int)((R64 + 127) / 128), S / bn, st);
+  a.ntn = S / bn;
+  const int64_t ntiles = ((R64 + 127) / 128) * a.ntn;
+  if (ntiles > INT32_MAX) return cudaErrorInvalidValue;
+  a.ntiles = (int)ntiles;
+  return launch_sw(sw, bn, ta, tb, a, st);
 }
 
 unsigned tc_error(bool clear) {

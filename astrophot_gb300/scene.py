@@ -768,10 +768,12 @@ class SceneLM:
                 continue
             h = self._full(h)
             h_np = h.cpu().numpy()
-            Y1 = sc.forward(x + d * h_np)
-            rh = sc.residual(sc.data, Y1)   # W (Y1 - Y)
-            rpp = self._sub(sc.jt(sc.rpp_image(r, rh, sc.jvp(h), d)))
             if self.L > 1e-4:
+                # the geodesic term from the render at x + d h; at L <= 1e-4 it is zero and that
+                # render (computed and then discarded by fit/lm.py:277-286) is skipped
+                Y1 = sc.forward(x + d * h_np)
+                rh = sc.residual(sc.data, Y1)   # W (Y1 - Y)
+                rpp = self._sub(sc.jt(sc.rpp_image(r, rh, sc.jvp(h), d)))
                 a_d = sc.solve(hess, rpp, self.L, reuse=True)  # the factor of the h solve above
                 a = np.zeros_like(h_np) if a_d is None else -self._full(a_d).cpu().numpy() / 2
             else:

@@ -1,6 +1,6 @@
 """Train the learned-initial-guess network on stamps rendered by this library and save it.
 
-    python -m astrophot_gb300.train_cnn --stamps 16000000 --out astrophot_gb300/weights/init_cnn.npz
+    python -m astrophot_gb300.train_cnn --stamps 48000000 --out astrophot_gb300/weights/init_cnn.npz
 
 Each stamp is rendered once (``ap_render``), given noise and used for one Adam step; the
 held-out loss is reported on stamps of a seed the training never draws.  The committed
@@ -20,7 +20,7 @@ from . import cnn
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
-    ap.add_argument("--stamps", type=int, default=16_000_000)
+    ap.add_argument("--stamps", type=int, default=48_000_000)
     ap.add_argument("--batch", type=int, default=512)
     ap.add_argument("--chunk", type=int, default=8192)
     ap.add_argument("--lr", type=float, default=1e-3)

@@ -499,7 +499,7 @@ int ap_gemm_bf16_tc(const void* A, int32_t lda, const void* W, int32_t ldw, floa
 int ap_conv3x3s2_bf16_tc(const void* x, int64_t batch, int32_t H, int32_t cin, const void* W,
                          int32_t S, float* C, int32_t ldc, const float* bias, void* act,
                          int32_t relu, ap_stream_t stream);
-/* First error code a tcgen05 kernel recorded (0 none; 1-3: an mbarrier wait that ran out of its
+/* First error code a tcgen05 kernel recorded (0 none; 1-5: an mbarrier wait that ran out of its
  * 200 ms limit, after which the kernel stopped, freed its tensor memory and returned, and every
  * later launch returns at once).  clear != 0 resets it.  Synchronises the device. */
 int ap_tc_status(int32_t clear, uint32_t* code);

@@ -71,7 +71,7 @@ def test_scene_primitives_match_numpy(S, name):
     assert np.max(np.abs(jv - want)) <= 1e-5 * np.max(np.abs(want))
 
 
-@pytest.mark.parametrize("n", [7, 32, 100, 257])
+@pytest.mark.parametrize("n", [7, 32, 100, 257, 1400])
 def test_dense_damped_solve_matches_numpy(S, n):
     rng = np.random.default_rng(n)
     A = rng.normal(size=(n, 2 * n))
@@ -88,6 +88,11 @@ def test_dense_damped_solve_matches_numpy(S, n):
     sc._solve_ws = torch.empty(int(sc.lib.ap_dense_solve_workspace_bytes(n)), dtype=torch.uint8, device="cuda")
     h = sc.solve(torch.tensor(H, device="cuda"), torch.tensor(g, device="cuda"), L).cpu().numpy()
     assert np.allclose(h, want, rtol=1e-9, atol=1e-12 * np.max(np.abs(want)))
+    # another right-hand side on the same factor (the geodesic term's solve)
+    g2 = rng.normal(size=n)
+    h2 = sc.solve(torch.tensor(H, device="cuda"), torch.tensor(g2, device="cuda"), L, reuse=True).cpu().numpy()
+    want2 = np.linalg.solve(M, g2)
+    assert np.allclose(h2, want2, rtol=1e-9, atol=1e-12 * np.max(np.abs(want2)))
     # not positive definite: reported, not solved
     assert sc.solve(torch.tensor(-H, device="cuda"), torch.tensor(g, device="cuda"), 0.0) is None
 
