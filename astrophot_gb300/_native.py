@@ -149,6 +149,7 @@ EXPORTS = [
     ("ap_scene_chi2", [_P, _P, _P, _P, _I64, _P, _P]),
     ("ap_scene_residual", [_P, _P, _P, _P, _I64, _P, _P]),
     ("ap_scene_rpp_image", [_P, _P, _P, _P, _P, ctypes.c_double, _I64, _P, _P]),
+    ("ap_scene_stage", [_I32, _P, _P, _P, _P, ctypes.c_double, _P, _P]),
     ("ap_dense_solve_workspace_bytes", [_I32]),
     ("ap_dense_damped_solve", [_I32, _P, _P, ctypes.c_double, _P, _P, ctypes.c_size_t, _P, _P]),
     ("ap_dense_factored_solve", [_I32, _P, _P, _P, ctypes.c_size_t, _P]),

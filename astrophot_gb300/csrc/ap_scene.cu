@@ -405,6 +405,52 @@ inline int egrid(int64_t n) {
   return (int)(g < 1 ? 1 : (g > 4096 ? 4096 : g));
 }
 
+// ---- staged parameter rows from a device joint vector -------------------------------------------
+// The value of full-vector slot `slot` at representation r, with the slot limits of the host maps
+// (utils/conversions/optimization.py:6-54: tan/arctan for two-sided limits, v - 1/(v - lim) for
+// one-sided ones, a modulo for the cyclic PA, identity otherwise), in numpy's operation order and
+// without contraction (explicit _rn operations), so the staged rows equal the host staging's.
+__device__ double stage_value(int slot, double r) {
+  constexpr double kPi = 3.141592653589793;
+  switch (slot) {
+    case 2:  // q in (0, 1)
+      return __dadd_rn(__ddiv_rn(__dmul_rn(__dadd_rn(atan(r), kPi / 2), 1.0 - 0.0), kPi), 0.0);
+    case 4:  // n in (0.36, 8)
+      return __dadd_rn(__ddiv_rn(__dmul_rn(__dadd_rn(atan(r), kPi / 2), 8.0 - 0.36), kPi), 0.36);
+    case 5: {  // Re in (0, inf)
+      const double t = __dsub_rn(r, 0.0);
+      return __dmul_rn(__dadd_rn(__dadd_rn(r, 0.0), __dsqrt_rn(__dadd_rn(__dmul_rn(t, t), 4.0))), 0.5);
+    }
+    case 3: {  // PA: 0 + mod(r - 0, pi), numpy's floating modulo (fmod, then the divisor's sign)
+      const double a = __dsub_rn(r, 0.0);
+      double m = fmod(a, kPi);
+      if (m != 0.0) {
+        if (m < 0.0) m = __dadd_rn(m, kPi);
+      } else {
+        m = 0.0;
+      }
+      return __dadd_rn(0.0, m);
+    }
+    default:
+      return r;
+  }
+}
+
+// out[c] = base[c] (gidx[c] < 0) or the value of slot c % 8 at x[g] + alpha v[g]
+__global__ void k_scene_stage(int n, const int32_t* __restrict__ gidx, const double* __restrict__ base,
+                              const double* __restrict__ x, const double* __restrict__ v, double alpha,
+                              double* __restrict__ out) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+    const int g = gidx[c];
+    if (g < 0) {
+      out[c] = base[c];
+      continue;
+    }
+    const double r = v ? __dadd_rn(x[g], __dmul_rn(alpha, v[g])) : x[g];
+    out[c] = stage_value(c % kMaxSlots, r);
+  }
+}
+
 // ---- PSF model normalisation: K / sum K and its derivatives (one block) ---------------------------
 __global__ void k_psf_normalize(int n, int m, const float* __restrict__ img, const float* __restrict__ dimg,
                                 float* __restrict__ out, float* __restrict__ dout) {
@@ -509,6 +555,13 @@ int ap_scene_rpp_image(const float* r, const float* rh, const float* jh, const f
                        double d, int64_t n, float* out, ap_stream_t stream) {
   if (!r || !rh || !jh || !out || n <= 0 || !(d > 0)) return AP_ERR_ARG;
   k_scene_rpp<<<egrid(n), 256, 0, (cudaStream_t)stream>>>(r, rh, jh, weight, mask, d, n, out);
+  return record_cuda(cudaGetLastError());
+}
+
+int ap_scene_stage(int32_t n_cells, const int32_t* gidx, const double* base, const double* x, const double* v,
+                   double alpha, double* out, ap_stream_t stream) {
+  if (n_cells <= 0 || (n_cells % kMaxSlots) != 0 || !gidx || !base || !x || !out) return AP_ERR_ARG;
+  k_scene_stage<<<egrid(n_cells), 256, 0, (cudaStream_t)stream>>>(n_cells, gidx, base, x, v, alpha, out);
   return record_cuda(cudaGetLastError());
 }
 

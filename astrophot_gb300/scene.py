@@ -22,6 +22,10 @@ host-to-device copy; the forward and the Jacobian then read device memory only, 
 captured as a CUDA graph at its second call and replayed (``graphs=False``: launched one by
 one).  The LM's
 geodesic-term solve reuses the Cholesky factor of its step solve (``ap_dense_factored_solve``).
+Without a live PSF the LM keeps its vectors on the device: parameters are staged there from the
+joint vector (``ap_scene_stage``), a damping trial reads back one packed status (factorisation
+status, chi^2, the step and geodesic vectors) on which the host takes the reference's decisions,
+and the next step's base image is the accepted trial's render.
 
 A scene's PSF may be a live Moffat PSF model (``set_aux_psf``, models/model_object.py:133-149)
 instead of a fixed image: :class:`LivePSF` samples it on its PSF image at every evaluation, its
@@ -463,6 +467,87 @@ class Scene:
         self._stage_d.copy_(torch.from_numpy(H))
         return V
 
+    # ---- parameters staged from a device vector (the LM's vectors stay on the device) --------
+    def _stage_rows(self) -> np.ndarray:
+        """Source index of every staged row (-1: the live PSF's rows), as ``_stage`` fills them."""
+        if getattr(self, "_row_src", None) is None:
+            row_src = np.full(self._stage_h.shape[0], -1, dtype=np.int64)
+            for part in self._jac_parts:
+                r0, n = part["srow"]
+                row_src[r0 : r0 + n] = part["members"]
+            for part in self._fwd_parts:
+                mem, m = part["members"], part["m"]
+                if part["own"]:
+                    r0, n = part["srow"][0]
+                    row_src[r0 : r0 + n] = mem
+                    continue
+                for (r0, n), c0 in zip(part["srow"], range(0, len(mem), m)):
+                    chunk = mem[c0 : c0 + m]
+                    row_src[r0 : r0 + n] = chunk[0]
+                    row_src[r0 : r0 + len(chunk)] = chunk
+            g = np.full(self._stage_h.shape, -1, dtype=np.int32)
+            for r, si in enumerate(row_src):
+                if si >= 0:
+                    for sl, gi in self.gidx[si].items():
+                        g[r, sl] = gi
+            self._row_src = row_src
+            self._stage_gidx = torch.tensor(g.reshape(-1), device=self.device)
+            self._stage_base = torch.zeros(g.size, dtype=torch.float64, device=self.device)
+        return self._row_src
+
+    @property
+    def device_staging(self) -> bool:
+        """Whether renders can take their parameters from a device vector (no live PSF)."""
+        return self.n_psf == 0
+
+    def set_stage_base(self, rep):
+        """The constant cells of device staging (locked slots, an exponential's n) from the
+        sources' current values; the free cells are computed from the vector at every call."""
+        row_src = self._stage_rows()
+        V = self.values_matrix(np.asarray(rep, dtype=np.float64))
+        base = np.zeros(self._stage_h.shape)
+        used = row_src >= 0
+        base[used] = V[row_src[used]]
+        self._stage_base.copy_(torch.from_numpy(base.reshape(-1)))
+
+    def _stage_dev(self, x: torch.Tensor, v: Optional[torch.Tensor] = None, alpha: float = 0.0):
+        """Every render's parameter rows at the device joint vector x + alpha v (float64)."""
+        if not self.device_staging:
+            raise NotImplementedError("device staging of a scene with a live PSF model")
+        self._stage_rows()
+        N.check(self.lib.ap_scene_stage(self._stage_d.numel(), N._ptr(self._stage_gidx), N._ptr(self._stage_base),
+                                        N._ptr(x), N._ptr(v) if v is not None else None, float(alpha),
+                                        N._ptr(self._stage_d), N._stream()), "ap_scene_stage")
+
+    def forward_device(self, x: torch.Tensor, v: Optional[torch.Tensor] = None, alpha: float = 0.0) -> torch.Tensor:
+        """Model image [ny * nx] at the device joint vector x + alpha v (``set_stage_base`` first).
+        Returns the scene's image buffer, which the next render overwrites."""
+        self._stage_dev(x, v, alpha)
+        self._run("forward", self._forward_body)
+        return self._img
+
+    def jacobian_device(self, x: torch.Tensor) -> torch.Tensor:
+        """:meth:`jacobian` (representation space) at the device joint vector x."""
+        self._stage_dev(x)
+        self._run(("jacobian", True), lambda: self._jacobian_body(True))
+        return self.jac
+
+    def chi2_into(self, model: torch.Tensor, out: torch.Tensor):
+        """chi^2 of ``model`` into the device float64 ``out[0]`` (no host read)."""
+        N.check(self.lib.ap_scene_chi2(N._ptr(model), N._ptr(self.data), N._ptr(self.weight), N._ptr(self.mask),
+                                       self.nx * self.ny, N._ptr(out), N._stream()), "ap_scene_chi2")
+
+    def solve_device(self, H: torch.Tensor, g: torch.Tensor, L: float) -> torch.Tensor:
+        """:meth:`solve` without the host read of the factorisation status: the status stays in
+        ``self._info`` and h is zero when the damped matrix was not positive definite (so that
+        nothing downstream renders a failed step)."""
+        n = int(H.shape[0])
+        h = torch.empty(n, dtype=torch.float64, device=self.device)
+        N.check(self.lib.ap_dense_damped_solve(n, N._ptr(H.contiguous()), N._ptr(g.contiguous()), float(L), N._ptr(h),
+                                               N._ptr(self._solve_ws), self._solve_ws.numel(), N._ptr(self._info),
+                                               N._stream()), "ap_dense_damped_solve")
+        return torch.where(self._info == 0, h, torch.zeros_like(h))
+
     def _psf_body(self, grad: bool):
         """Sample the live PSF from the staged row and copy it into every batch's packed PSF;
         returns its value-space derivatives when ``grad``."""
@@ -707,8 +792,11 @@ class SceneLM:
 
     def __init__(self, scene: Scene, initial_state=None, max_iter: int = 100, relative_tolerance: float = 1e-5,
                  max_step_iter: int = 10, curvature_limit: float = 1.0, Lup: float = 11.0, Ldn: float = 9.0,
-                 L0: float = 1.0, acceleration: float = 0.0, ndf=None, free=None):
+                 L0: float = 1.0, acceleration: float = 0.0, ndf=None, free=None, device_loop: bool = True):
         self.scene = scene
+        # device_loop: the vectors stay on the device, parameters are staged there, each damping
+        # trial reads one status back (scenes without a live PSF); else the host loop below
+        self.device_loop = bool(device_loop) and scene.device_staging
         self.x = np.array(scene.representation() if initial_state is None else initial_state, dtype=np.float64)
         self.free = None if free is None else np.asarray(free, dtype=np.int64)
         self._free_t = None if free is None else torch.as_tensor(self.free, device=scene.device)
@@ -818,9 +906,154 @@ class SceneLM:
             raise OptimizeStop("Could not find step to improve chi^2")
         return best
 
+    # ---- the same LM with its vectors on the device -------------------------------------------
+    def _step_device(self, chi2, have_y0: bool):
+        """:meth:`step` with x, h, a and the images on the device: parameters are staged from
+        device vectors, a failed factorisation zeroes h on the device, and each damping trial
+        reads back one packed status (factorisation status, chi^2, a, h), from which the host takes
+        the reference's decisions in its order.  Returns (step vector on the device, chi^2, L,
+        whether the model at the step is in ``self._Yb``)."""
+        sc = self.scene
+        x = self._xd
+        P = sc.P
+        if not have_y0:
+            self._Y0.copy_(sc.forward_device(x))
+            self.base_renders += 1
+        Y0 = self._Y0
+        sc.jacobian_device(x)
+        hess = sc.hess()
+        if self._free_t is not None:
+            hess = hess[self._free_t][:, self._free_t].contiguous()
+        resid = sc.residual(Y0)             # W (Y - Y0) = -r
+        grad = self._sub(sc.jt(resid))      # -J^T r
+        r = sc.residual(sc.data, Y0)        # W (Y0 - Y)
+        init_chi2 = chi2
+        nostep = True
+        best = (None, init_chi2, self.L)
+        scarry_best = (None, init_chi2, self.L)
+        direction = "none"
+        d = 0.1
+        st = self._status
+        for iteration in range(self.max_step_iter):
+            if iteration > self.max_step_iter / 2 and self.L < 1e-3:
+                self.L = 1.0
+            h = self._full(sc.solve_device(hess, grad, self.L))
+            self.trials += 1
+            if self.L > 1e-4:
+                self.geodesic_trials += 1
+                # the geodesic term from the render at x + d h (skipped at L <= 1e-4, where
+                # fit/lm.py:277-286 computes it and then discards it)
+                Y1 = sc.forward_device(x, h, d)
+                rh = sc.residual(sc.data, Y1)   # W (Y1 - Y)
+                rpp = self._sub(sc.jt(sc.rpp_image(r, rh, sc.jvp(h), d)))
+                a_d = self._full(sc.solve(hess, rpp, self.L, reuse=True))  # the factor of the h solve
+                a = torch.where(sc._info == 0, torch.neg(a_d) / 2, torch.zeros_like(a_d))
+            else:
+                a = torch.zeros_like(h)
+            ha = torch.add(h, torch.mul(a, self.acceleration))
+            Y1 = sc.forward_device(x, ha, 1.0)
+            sc.chi2_into(Y1, st[1:2])
+            st[0:1].copy_(sc._info)
+            st[2 : 2 + P].copy_(a)
+            st[2 + P :].copy_(h)
+            s = st.cpu().numpy()
+            if int(s[0]) != 0:   # the damped matrix was not positive definite
+                self.Lup()
+                if direction == "better":
+                    break
+                direction = "worse"
+                continue
+            chi2 = float(s[1]) / self.ndf
+            a_np, h_np = s[2 : 2 + P], s[2 + P :]
+            if not np.isfinite(chi2):
+                self.Lup()
+                if direction == "better":
+                    break
+                direction = "worse"
+                continue
+            if chi2 <= scarry_best[1]:
+                scarry_best = (ha, chi2, self.L)
+            rho = np.linalg.norm(a_np) / np.linalg.norm(h_np)
+            if rho > self.curvature_limit:
+                self.Lup()
+                if direction == "better":
+                    break
+                direction = "worse"
+                continue
+            if chi2 < best[1]:
+                best = (ha, chi2, self.L)
+                self._Yb.copy_(Y1)
+                nostep = False
+                self.Ldn()
+                if self.L <= 1e-8 or direction == "worse":
+                    break
+                direction = "better"
+            elif chi2 > best[1] and direction in ("none", "worse"):
+                self.Lup()
+                if self.L == 1e9:
+                    break
+                direction = "worse"
+            else:
+                break
+            if (best[1] - init_chi2) / init_chi2 < -0.1:
+                break
+        if nostep:
+            if scarry_best[0] is not None:
+                return scarry_best[0], scarry_best[1], scarry_best[2], False
+            raise OptimizeStop("Could not find step to improve chi^2")
+        return best[0], best[1], best[2], True
+
+    def _fit_device(self):
+        sc = self.scene
+        dev = sc.device
+        sc.set_stage_base(self.x)
+        self._xd = torch.tensor(self.x, dtype=torch.float64, device=dev)
+        self._Y0 = torch.empty(sc.nx * sc.ny, dtype=torch.float32, device=dev)
+        self._Yb = torch.empty_like(self._Y0)
+        self._status = torch.zeros(2 + 2 * sc.P, dtype=torch.float64, device=dev)
+        self.trials = self.geodesic_trials = self.base_renders = 0
+        self._Y0.copy_(sc.forward_device(self._xd))
+        sc.chi2_into(self._Y0, self._status[1:2])
+        self.loss_history = [float(self._status[1].item()) / self.ndf]
+        self.L_history = [self.L]
+        self.lambda_history = [self.x.copy()]
+        have_y0 = True
+        for iteration in range(self.max_iter):
+            self.iterations = iteration + 1
+            try:
+                step, chi2, L, at_best = self._step_device(self.loss_history[-1], have_y0)
+            except OptimizeStop:
+                self.message = self.message + "fail. Could not find step to improve Chi^2"
+                break
+            self.L = L
+            self._xd = self._xd + step
+            if at_best:  # the model at the new x is the accepted trial's render
+                self._Y0, self._Yb = self._Yb, self._Y0
+            have_y0 = at_best
+            self.x = self._xd.cpu().numpy().copy()
+            self.L_history.append(self.L)
+            self.loss_history.append(chi2)
+            self.lambda_history.append(self.x.copy())
+            self.Ldn()
+            if len(self.loss_history) >= 3:
+                if (self.loss_history[-3] - self.loss_history[-1]) / self.loss_history[-1] < self.relative_tolerance \
+                        and self.L < 0.1:
+                    self.message = self.message + "success"
+                    break
+            if len(self.loss_history) > 10:
+                if (self.loss_history[-10] - self.loss_history[-1]) / self.loss_history[-1] < self.relative_tolerance:
+                    self.message = self.message + "success by immobility. Convergence not guaranteed"
+                    break
+        else:
+            self.message = self.message + "fail. Maximum iterations"
+        self.scene.set_representation(self.res())
+        return self
+
     def fit(self):
         if self.scene.P == 0 or (self.free is not None and len(self.free) == 0):
             return self
+        if self.device_loop:
+            return self._fit_device()
         self.loss_history = [self._chi2(self.scene.forward(self.x))]
         self.L_history = [self.L]
         self.lambda_history = [self.x.copy()]

@@ -1410,6 +1410,16 @@ def crowded_block(args, dev):
     lm = SC.SceneLM(sc, initial_state=rep, max_iter=args.crowded_iters).fit()
     torch.cuda.synchronize()
     lm_s = time.perf_counter() - t0
+    # the same LM driven from the host (host staging, four reads per damping trial)
+    t0 = time.perf_counter()
+    lm_h = SC.SceneLM(sc, initial_state=rep, max_iter=args.crowded_iters, device_loop=False).fit()
+    torch.cuda.synchronize()
+    lm_host_s = time.perf_counter() - t0
+    # device time the LM's work takes at the kernel times measured above: a Jacobian + J^T W J
+    # per iteration, a damped solve and a render per trial, a second render for the geodesic
+    # term, the base renders not taken from an accepted trial
+    floor_ms = (lm.iterations * jac_ms + lm.trials * (solve_ms + fwd_ms) + lm.geodesic_trials * fwd_ms
+                + (1 + lm.base_renders) * fwd_ms)
     out = {
         "workload": f"{n_src} Sersic galaxies on a {size}x{size} image, 51x51 Gaussian PSF (sigma 2; mode fft: "
         "the convolution takes the faster of FFT and direct for the kernel size, direct at 53x53), sky 5.0, "
@@ -1426,6 +1436,13 @@ def crowded_block(args, dev):
         "lm_iterations": lm.iterations,
         "lm_seconds": lm_s,
         "lm_ms_per_iteration": lm_s * 1e3 / max(lm.iterations, 1),
+        "lm_damping_trials": lm.trials,
+        "lm_geodesic_trials": lm.geodesic_trials,
+        "lm_kernel_floor_ms_per_iteration": floor_ms / max(lm.iterations, 1),
+        "lm_loop": "device vectors, parameters staged on the device, one status read per damping trial",
+        "lm_host_loop_ms_per_iteration": lm_host_s * 1e3 / max(lm_h.iterations, 1),
+        "lm_host_loop_same_trajectory": bool(lm_h.message == lm.message and lm_h.iterations == lm.iterations
+                                             and np.allclose(lm_h.loss_history, lm.loss_history, rtol=1e-9)),
         "chi2_ndf_start": lm.loss_history[0],
         "chi2_ndf_end": min(lm.loss_history),
         "lm_message": lm.message,

@@ -400,6 +400,15 @@ int ap_scene_residual(const float* model, const float* data, const float* weight
  * side of LM.step (fit/lm.py:286-291). */
 int ap_scene_rpp_image(const float* r, const float* rh, const float* jh, const float* weight,
                        const uint8_t* mask, double d, int64_t n, float* out, ap_stream_t stream);
+/* The parameter rows of a scene's renders (float64 [rows][8], slots cx cy q PA n Re Ie F) at the
+ * joint representation vector x + alpha v, computed on the device so that an LM keeps its
+ * vectors there (the parameter setters of Parameter_Node through the maps of
+ * utils/conversions/optimization.py:6-54, which LM.step applies at every trial,
+ * fit/lm.py:277-293): out[c] = base[c] where gidx[c] < 0 (a locked or absent slot), else the
+ * value of slot c % 8 at representation x[g] + alpha v[g], g = gidx[c].  n_cells a multiple of
+ * 8; v may be NULL (alpha then unused). */
+int ap_scene_stage(int32_t n_cells, const int32_t* gidx, const double* base, const double* x,
+                   const double* v, double alpha, double* out, ap_stream_t stream);
 /* h = solve(H o (I + D/(1+L)) + L I (1 + diag H), g) for one dense n x n system (LM._h,
  * fit/lm.py:361-371): blocked FP64 Cholesky.  info (device) = 0, or 1 + the row whose pivot
  * was not positive (the system is then not solved). */

@@ -109,6 +109,43 @@ def test_scene_lm_matches_reference(S, name):
     assert np.allclose(lm.loss_history[:3], d["loss_history"][:3], rtol=1e-5)
 
 
+@pytest.mark.parametrize("name", cases.group_case_names())
+def test_device_staging_equals_host_staging(S, name):
+    """Parameter rows staged on the device from a device vector x + alpha v equal the host
+    staging of the same vector (values beyond the PA period and far into the limits included)."""
+    d = cases.load_group(name)
+    sc = golden_scene(S, d)
+    rep0 = sc.representation()
+    rng = np.random.default_rng(5)
+    v = rng.normal(size=sc.P) * 3.0
+    alpha = 0.7
+    x = rep0 + alpha * v
+    sc._stage(x)
+    host = sc._stage_d.clone()
+    sc.set_stage_base(rep0)
+    sc._stage_dev(torch.tensor(rep0, device="cuda"), torch.tensor(v, device="cuda"), alpha)
+    dev = sc._stage_d.clone()
+    used = sc._stage_rows() >= 0
+    assert torch.allclose(dev[used], host[used], rtol=4e-16, atol=0)
+    # without the direction vector
+    sc._stage_dev(torch.tensor(x, device="cuda"))
+    assert torch.allclose(sc._stage_d[used], host[used], rtol=4e-16, atol=0)
+
+
+@pytest.mark.parametrize("name", cases.group_case_names())
+def test_scene_lm_device_loop_equals_host_loop(S, name):
+    """The LM with its vectors on the device (one status read per damping trial) takes the host
+    loop's steps: the same message, iterations, loss history and fitted vector."""
+    d = cases.load_group(name)
+    a = S.SceneLM(golden_scene(S, d), max_iter=d["spec"]["max_iter"], device_loop=False).fit()
+    b = S.SceneLM(golden_scene(S, d), max_iter=d["spec"]["max_iter"], device_loop=True).fit()
+    assert b.device_loop and not a.device_loop
+    assert a.message == b.message and a.iterations == b.iterations
+    np.testing.assert_allclose(b.loss_history, a.loss_history, rtol=1e-9)
+    np.testing.assert_allclose(b.L_history, a.L_history, rtol=0)
+    np.testing.assert_allclose(b.res(), a.res(), rtol=1e-9, atol=1e-12)
+
+
 def test_scene_with_mask_and_no_psf_matches_oracle(S):
     """Masked pixels and no PSF: model, Jacobian and the joint LM against the oracle."""
     from oracle.lm import GroupProblem, LMOracle
