@@ -17,7 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libastrophot_gb300.so")
 SOURCES = ("ap_kernels.cu", "ap_lm.cu", "ap_capi.cu", "ap_noalloc.cu", "ap_cnn.cu", "ap_scene.cu", "ap_refinit.cu",
-           "ap_fft.cu", "ap_segmap.cu", "ap_tcgemm.cu")
+           "ap_fft.cu", "ap_segmap.cu", "ap_tcgemm.cu", "ap_solve.cu")
 # per-file flags: the initial-value heuristics round like numpy (no FMA contraction)
 EXTRA = {"ap_refinit.cu": ("-fmad=false",)}
 ARCH = ("-gencode", "arch=compute_103a,code=sm_103a")

@@ -153,6 +153,8 @@ EXPORTS = [
     ("ap_dense_solve_workspace_bytes", [_I32]),
     ("ap_dense_damped_solve", [_I32, _P, _P, ctypes.c_double, _P, _P, ctypes.c_size_t, _P, _P]),
     ("ap_dense_factored_solve", [_I32, _P, _P, _P, ctypes.c_size_t, _P]),
+    ("ap_dense_damped_solve_mixed", [_I32, _P, _P, ctypes.c_double, _P, _P, ctypes.c_size_t, _P, _P]),
+    ("ap_dense_factored_solve_mixed", [_I32, _P, _P, ctypes.c_double, _P, _P, ctypes.c_size_t, _P, _P]),
     ("ap_cnn_param_count", []),
     ("ap_cnn_autotune", [_I32, _PI32]),
     ("ap_cnn_workspace_bytes", [_I64]),

@@ -151,4 +151,13 @@ cudaError_t tc_conv3x3s2(const __nv_bfloat16* act_in, int64_t B, int H, int cin,
 // request; reading it synchronises the device
 unsigned tc_error(bool clear);
 
+// Dense damped solves (ap_scene.cu: FP64 Cholesky; ap_solve.cu: FP32 Cholesky + FP64 iterative
+// refinement).  One workspace serves both: the FP64 region first, the mixed region after it.
+inline size_t dense_fp64_ws_bytes(int32_t n) {
+  // A (n x n), y and z (n each), the factored 32 x 32 diagonal block of the current step
+  return sizeof(double) * ((size_t)n * n + 2 * (size_t)n + 32 * 32) + sizeof(int) * 4;
+}
+inline size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+size_t dense_mixed_ws_bytes(int32_t n);
+
 }  // namespace apgb

@@ -567,8 +567,8 @@ int ap_scene_stage(int32_t n_cells, const int32_t* gidx, const double* base, con
 
 size_t ap_dense_solve_workspace_bytes(int32_t n) {
   if (n <= 0) return 0;
-  // A (n x n), y and z (n each), the factored diagonal block of the current step
-  return sizeof(double) * ((size_t)n * n + 2 * (size_t)n + kNB * kNB) + sizeof(int) * 4;
+  // the FP64 factorisation's region, then the mixed-precision solver's (ap_solve.cu)
+  return apgb::align256(apgb::dense_fp64_ws_bytes(n)) + apgb::dense_mixed_ws_bytes(n);
 }
 
 namespace {

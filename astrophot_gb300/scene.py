@@ -396,6 +396,8 @@ class Scene:
         self._solve_ws = torch.empty(int(self.lib.ap_dense_solve_workspace_bytes(self.P)), dtype=torch.uint8,
                                      device=dev)
         self._info = torch.zeros(1, dtype=torch.int32, device=dev)
+        self._info2 = torch.zeros(1, dtype=torch.int32, device=dev)
+        self._last_mixed = False
         self._d64 = torch.zeros(1, dtype=torch.float64, device=dev)
 
     # ---- geometry and parameters -----------------------------------------------------------
@@ -537,16 +539,17 @@ class Scene:
         N.check(self.lib.ap_scene_chi2(N._ptr(model), N._ptr(self.data), N._ptr(self.weight), N._ptr(self.mask),
                                        self.nx * self.ny, N._ptr(out), N._stream()), "ap_scene_chi2")
 
-    def solve_device(self, H: torch.Tensor, g: torch.Tensor, L: float) -> torch.Tensor:
-        """:meth:`solve` without the host read of the factorisation status: the status stays in
-        ``self._info`` and h is zero when the damped matrix was not positive definite (so that
-        nothing downstream renders a failed step)."""
+    def solve_device(self, H: torch.Tensor, g: torch.Tensor, L: float, info: torch.Tensor, mixed: bool = True,
+                     reuse: bool = False) -> torch.Tensor:
+        """:meth:`solve` without a host read: the status goes to the device int ``info`` (0
+        solved; > 0 the damped matrix is not positive definite; -1 the mixed-precision solve did
+        not converge) and h is zero unless solved, so that nothing downstream renders a failed
+        step.  ``reuse``: another right-hand side on the factor of the previous call of the same
+        precision."""
         n = int(H.shape[0])
         h = torch.empty(n, dtype=torch.float64, device=self.device)
-        N.check(self.lib.ap_dense_damped_solve(n, N._ptr(H.contiguous()), N._ptr(g.contiguous()), float(L), N._ptr(h),
-                                               N._ptr(self._solve_ws), self._solve_ws.numel(), N._ptr(self._info),
-                                               N._stream()), "ap_dense_damped_solve")
-        return torch.where(self._info == 0, h, torch.zeros_like(h))
+        self._solve_call(H, g, L, h, info, mixed, reuse)
+        return torch.where(info == 0, h, torch.zeros_like(h))
 
     def _psf_body(self, grad: bool):
         """Sample the live PSF from the staged row and copy it into every batch's packed PSF;
@@ -763,23 +766,43 @@ class Scene:
                                             N._stream()), "ap_scene_rpp_image")
         return out
 
-    def solve(self, H: torch.Tensor, g: torch.Tensor, L: float, reuse: bool = False):
+    def _solve_call(self, H, g, L, h, info, mixed: bool, reuse: bool):
+        n = int(H.shape[0])
+        ws, wsn = N._ptr(self._solve_ws), self._solve_ws.numel()
+        Hp, gp, hp = N._ptr(H.contiguous()), N._ptr(g.contiguous()), N._ptr(h)
+        if mixed and reuse:
+            N.check(self.lib.ap_dense_factored_solve_mixed(n, Hp, gp, float(L), hp, ws, wsn, N._ptr(info), N._stream()),
+                    "ap_dense_factored_solve_mixed")
+        elif mixed:
+            N.check(self.lib.ap_dense_damped_solve_mixed(n, Hp, gp, float(L), hp, ws, wsn, N._ptr(info), N._stream()),
+                    "ap_dense_damped_solve_mixed")
+        elif reuse:
+            N.check(self.lib.ap_dense_factored_solve(n, gp, hp, ws, wsn, N._stream()), "ap_dense_factored_solve")
+            info.zero_()
+        else:
+            N.check(self.lib.ap_dense_damped_solve(n, Hp, gp, float(L), hp, ws, wsn, N._ptr(info), N._stream()),
+                    "ap_dense_damped_solve")
+
+    def solve(self, H: torch.Tensor, g: torch.Tensor, L: float, reuse: bool = False, mixed: bool = True):
         """Damped solve of the n x n system H (n = H's side, at most P); None when the damped
         matrix is not positive definite.  ``reuse``: the same H and L as the previous (successful)
-        call, another right-hand side: only the triangular solves on its factor run."""
+        call, another right-hand side: only the solves on its factor run.  ``mixed``: float32
+        factorisation + float64 refinement (``ap_dense_damped_solve_mixed``) first, the float64
+        factorisation when that does not converge."""
         n = int(H.shape[0])
         h = torch.empty(n, dtype=torch.float64, device=self.device)
-        if reuse:
-            N.check(self.lib.ap_dense_factored_solve(n, N._ptr(g.contiguous()), N._ptr(h), N._ptr(self._solve_ws),
-                                                     self._solve_ws.numel(), N._stream()), "ap_dense_factored_solve")
-            return h
-        N.check(self.lib.ap_dense_damped_solve(n, N._ptr(H.contiguous()), N._ptr(g.contiguous()), float(L), N._ptr(h),
-                                               N._ptr(self._solve_ws), self._solve_ws.numel(), N._ptr(self._info),
-                                               N._stream()), "ap_dense_damped_solve")
-        if int(self._info.item()) != 0:
+        if mixed and (not reuse or self._last_mixed):
+            self._solve_call(H, g, L, h, self._info, True, reuse)
+            if int(self._info.item()) == 0:
+                self._last_mixed = not reuse or self._last_mixed
+                return h
+            if reuse:  # the float32 factor did not serve this right-hand side: factor in float64
+                reuse = False
+        self._solve_call(H, g, L, h, self._info, False, reuse)
+        self._last_mixed = False
+        if not reuse and int(self._info.item()) != 0:
             return None
         return h
-
 
 class OptimizeStop(Exception):
     pass
@@ -907,6 +930,35 @@ class SceneLM:
         return best
 
     # ---- the same LM with its vectors on the device -------------------------------------------
+    def _trial(self, hess, grad, r, d, mixed: bool):
+        """One damping trial at the current L on the device: the step h, the geodesic term a (when
+        L > 1e-4), the render at x + h + a * acceleration and its chi^2.  Returns (h + a acc, the
+        render, the packed status [solve status, chi^2, geodesic solve status, a, h] read back)."""
+        sc = self.scene
+        x = self._xd
+        P = sc.P
+        h = self._full(sc.solve_device(hess, grad, self.L, sc._info, mixed=mixed))
+        if self.L > 1e-4:
+            # the geodesic term from the render at x + d h (skipped at L <= 1e-4, where
+            # fit/lm.py:277-286 computes it and then discards it)
+            Y1 = sc.forward_device(x, h, d)
+            rh = sc.residual(sc.data, Y1)   # W (Y1 - Y)
+            rpp = self._sub(sc.jt(sc.rpp_image(r, rh, sc.jvp(h), d)))
+            a_d = self._full(sc.solve_device(hess, rpp, self.L, sc._info2, mixed=mixed, reuse=True))
+            a = torch.where((sc._info == 0) & (sc._info2 == 0), torch.neg(a_d) / 2, torch.zeros_like(a_d))
+        else:
+            a = torch.zeros_like(h)
+            sc._info2.zero_()
+        ha = torch.add(h, torch.mul(a, self.acceleration))
+        Y1 = sc.forward_device(x, ha, 1.0)
+        st = self._status
+        sc.chi2_into(Y1, st[1:2])
+        st[0:1].copy_(sc._info)
+        st[2:3].copy_(sc._info2)
+        st[3 : 3 + P].copy_(a)
+        st[3 + P :].copy_(h)
+        return ha, Y1, st.cpu().numpy()
+
     def _step_device(self, chi2, have_y0: bool):
         """:meth:`step` with x, h, a and the images on the device: parameters are staged from
         device vectors, a failed factorisation zeroes h on the device, and each damping trial
@@ -933,30 +985,17 @@ class SceneLM:
         scarry_best = (None, init_chi2, self.L)
         direction = "none"
         d = 0.1
-        st = self._status
         for iteration in range(self.max_step_iter):
             if iteration > self.max_step_iter / 2 and self.L < 1e-3:
                 self.L = 1.0
-            h = self._full(sc.solve_device(hess, grad, self.L))
             self.trials += 1
             if self.L > 1e-4:
                 self.geodesic_trials += 1
-                # the geodesic term from the render at x + d h (skipped at L <= 1e-4, where
-                # fit/lm.py:277-286 computes it and then discards it)
-                Y1 = sc.forward_device(x, h, d)
-                rh = sc.residual(sc.data, Y1)   # W (Y1 - Y)
-                rpp = self._sub(sc.jt(sc.rpp_image(r, rh, sc.jvp(h), d)))
-                a_d = self._full(sc.solve(hess, rpp, self.L, reuse=True))  # the factor of the h solve
-                a = torch.where(sc._info == 0, torch.neg(a_d) / 2, torch.zeros_like(a_d))
-            else:
-                a = torch.zeros_like(h)
-            ha = torch.add(h, torch.mul(a, self.acceleration))
-            Y1 = sc.forward_device(x, ha, 1.0)
-            sc.chi2_into(Y1, st[1:2])
-            st[0:1].copy_(sc._info)
-            st[2 : 2 + P].copy_(a)
-            st[2 + P :].copy_(h)
-            s = st.cpu().numpy()
+            ha, Y1, s = self._trial(hess, grad, r, d, mixed=True)
+            if int(s[0]) == -1 or int(s[2]) == -1:
+                # the mixed-precision solve did not converge: the trial again, in float64
+                self.fp64_retries += 1
+                ha, Y1, s = self._trial(hess, grad, r, d, mixed=False)
             if int(s[0]) != 0:   # the damped matrix was not positive definite
                 self.Lup()
                 if direction == "better":
@@ -964,7 +1003,7 @@ class SceneLM:
                 direction = "worse"
                 continue
             chi2 = float(s[1]) / self.ndf
-            a_np, h_np = s[2 : 2 + P], s[2 + P :]
+            a_np, h_np = s[3 : 3 + P], s[3 + P :]
             if not np.isfinite(chi2):
                 self.Lup()
                 if direction == "better":
@@ -1010,8 +1049,8 @@ class SceneLM:
         self._xd = torch.tensor(self.x, dtype=torch.float64, device=dev)
         self._Y0 = torch.empty(sc.nx * sc.ny, dtype=torch.float32, device=dev)
         self._Yb = torch.empty_like(self._Y0)
-        self._status = torch.zeros(2 + 2 * sc.P, dtype=torch.float64, device=dev)
-        self.trials = self.geodesic_trials = self.base_renders = 0
+        self._status = torch.zeros(3 + 2 * sc.P, dtype=torch.float64, device=dev)
+        self.trials = self.geodesic_trials = self.base_renders = self.fp64_retries = 0
         self._Y0.copy_(sc.forward_device(self._xd))
         sc.chi2_into(self._Y0, self._status[1:2])
         self.loss_history = [float(self._status[1].item()) / self.ndf]

@@ -385,8 +385,9 @@ def run_gpu(args):
         import torch
 
         if rank_info()[0] == 0:
-            print(json.dumps({"workload": "crowded", "crowded_field": crowded_block(args, torch.device("cuda"))}),
-                  flush=True)
+            dev = torch.device("cuda")
+            print(json.dumps({"workload": "crowded", "crowded_field": crowded_block(args, dev),
+                              "bulge_disk_field": bulge_disk_block(args, dev)}), flush=True)
     else:
         run_gpu_cutouts(args)
 
@@ -1275,7 +1276,9 @@ def bulge_disk_block(args, dev):
 
     jac_ms, H = timed(jac_hess)
     grad = sc.jt(sc.residual(m))
-    solve_ms, _ = timed(lambda: sc.solve(H, grad, 1.0))
+    solve_ms, h_mixed = timed(lambda: sc.solve(H, grad, 1.0))
+    solve64_ms, h64 = timed(lambda: sc.solve(H, grad, 1.0, mixed=False))
+    solve_rel = float((h_mixed - h64).abs().max() / h64.abs().max())
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     lm = SC.SceneLM(sc, initial_state=rep, max_iter=1).fit()
@@ -1292,6 +1295,9 @@ def bulge_disk_block(args, dev):
         "adjoint_vjp_ms": vjp_ms,
         "jacobian_and_jtwj_ms": jac_ms,
         "damped_solve_ms": solve_ms,
+        "damped_solve_fp64_ms": solve64_ms,
+        "damped_solve": "float32 Cholesky + float64 refinement (float64 factorisation when it does not converge); "
+                        "max |h - h_fp64| / max |h_fp64| = %.1e" % solve_rel,
         "lm_iteration_s": lm_s,
         "chi2_ndf_start": float(lm.loss_history[0]),
         "chi2_ndf_after_one_iteration": float(lm.loss_history[-1]),
@@ -1401,10 +1407,17 @@ def crowded_block(args, dev):
     torch.cuda.synchronize()
     e0.record()
     for _ in range(reps):
-        sc.solve(H, g, 1.0)
+        h_mixed = sc.solve(H, g, 1.0)
     e1.record()
     torch.cuda.synchronize()
     solve_ms = e0.elapsed_time(e1) / reps
+    e0.record()
+    for _ in range(reps):
+        h64 = sc.solve(H, g, 1.0, mixed=False)
+    e1.record()
+    torch.cuda.synchronize()
+    solve64_ms = e0.elapsed_time(e1) / reps
+    solve_rel = float((h_mixed - h64).abs().max() / h64.abs().max())
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     lm = SC.SceneLM(sc, initial_state=rep, max_iter=args.crowded_iters).fit()
@@ -1433,6 +1446,10 @@ def crowded_block(args, dev):
         "all_fft_convolution": {"render_ms": fwd_f, "jacobian_build_ms": jac_f,
                                 "chi2_rel_diff_vs_direct": abs(chi2_f / chi2_d - 1)},
         "damped_solve_ms": solve_ms,
+        "damped_solve_fp64_ms": solve64_ms,
+        "damped_solve": "float32 Cholesky + float64 refinement (float64 factorisation when it does not converge); "
+                        "max |h - h_fp64| / max |h_fp64| = %.1e" % solve_rel,
+        "lm_fp64_retries": lm.fp64_retries,
         "lm_iterations": lm.iterations,
         "lm_seconds": lm_s,
         "lm_ms_per_iteration": lm_s * 1e3 / max(lm.iterations, 1),

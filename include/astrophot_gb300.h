@@ -421,6 +421,20 @@ int ap_dense_damped_solve(int32_t n, const double* H, const double* g, double L,
  * geodesic term (fit/lm.py:286-299). */
 int ap_dense_factored_solve(int32_t n, const double* g, double* h, void* ws, size_t ws_bytes,
                             ap_stream_t stream);
+/* The same damped system (LM._h, fit/lm.py:361-371) solved in mixed precision: float32 blocked
+ * Cholesky, then float64 iterative refinement against the float64 damped matrix (off-diagonal
+ * H_ij * fl(1/(1+L)), diagonal H_ii + L (1 + H_ii), as the reference forms it) until the residual
+ * meets LAPACK dsposv's backward-error test (at most 10 rounds).  H must hold both triangles.
+ * info (device) = 0: h solved to float64 accuracy; -1: not solved (the float32 factorisation met
+ * a non-positive pivot, or the refinement stalled), h = 0 -- call ap_dense_damped_solve.  n at
+ * most 8192 (AP_ERR_UNSUPPORTED beyond).  Everything stays on the stream; no host read. */
+int ap_dense_damped_solve_mixed(int32_t n, const double* H, const double* g, double L, double* h,
+                                void* ws, size_t ws_bytes, int32_t* info, ap_stream_t stream);
+/* Another right-hand side of the system the last ap_dense_damped_solve_mixed factored (same H,
+ * same L): refinement on its float32 factor; info as above (-1 also when that factorisation
+ * failed). */
+int ap_dense_factored_solve_mixed(int32_t n, const double* H, const double* g, double L, double* h,
+                                  void* ws, size_t ws_bytes, int32_t* info, ap_stream_t stream);
 
 /* ---- learned initial guess -----------------------------------------------------------------
  * No counterpart in the reference: its initial values come from the heuristics of

@@ -71,8 +71,11 @@ def test_scene_primitives_match_numpy(S, name):
     assert np.max(np.abs(jv - want)) <= 1e-5 * np.max(np.abs(want))
 
 
+@pytest.mark.parametrize("mixed", [True, False])
 @pytest.mark.parametrize("n", [7, 32, 100, 257, 1400])
-def test_dense_damped_solve_matches_numpy(S, n):
+def test_dense_damped_solve_matches_numpy(S, n, mixed):
+    """The damped solve (float32 Cholesky + float64 refinement, or the float64 Cholesky) against
+    numpy's float64 solve of the reference's damped matrix."""
     rng = np.random.default_rng(n)
     A = rng.normal(size=(n, 2 * n))
     H = A @ A.T
@@ -86,15 +89,45 @@ def test_dense_damped_solve_matches_numpy(S, n):
     sc = golden_scene(S, d)
     sc.P = n
     sc._solve_ws = torch.empty(int(sc.lib.ap_dense_solve_workspace_bytes(n)), dtype=torch.uint8, device="cuda")
-    h = sc.solve(torch.tensor(H, device="cuda"), torch.tensor(g, device="cuda"), L).cpu().numpy()
+    h = sc.solve(torch.tensor(H, device="cuda"), torch.tensor(g, device="cuda"), L, mixed=mixed).cpu().numpy()
+    assert sc._last_mixed == mixed  # the mixed solve converged without the float64 fallback
     assert np.allclose(h, want, rtol=1e-9, atol=1e-12 * np.max(np.abs(want)))
     # another right-hand side on the same factor (the geodesic term's solve)
     g2 = rng.normal(size=n)
-    h2 = sc.solve(torch.tensor(H, device="cuda"), torch.tensor(g2, device="cuda"), L, reuse=True).cpu().numpy()
+    h2 = sc.solve(torch.tensor(H, device="cuda"), torch.tensor(g2, device="cuda"), L, reuse=True,
+                  mixed=mixed).cpu().numpy()
     want2 = np.linalg.solve(M, g2)
     assert np.allclose(h2, want2, rtol=1e-9, atol=1e-12 * np.max(np.abs(want2)))
     # not positive definite: reported, not solved
-    assert sc.solve(torch.tensor(-H, device="cuda"), torch.tensor(g, device="cuda"), 0.0) is None
+    assert sc.solve(torch.tensor(-H, device="cuda"), torch.tensor(g, device="cuda"), 0.0, mixed=mixed) is None
+
+
+def test_mixed_solve_hands_ill_conditioned_systems_to_float64(S):
+    """A system beyond float32's reach (condition 1e12, no damping): the mixed solve reports -1
+    with h = 0 through the C ABI, and Scene.solve then returns the float64 factorisation's h."""
+    from astrophot_gb300 import _native as N
+
+    n = 200
+    rng = np.random.default_rng(11)
+    Q, _ = np.linalg.qr(rng.normal(size=(n, n)))
+    H = (Q * np.logspace(0, -12, n)) @ Q.T
+    H = (H + H.T) / 2
+    g = rng.normal(size=n)
+    d = cases.load_group(cases.group_case_names()[0])
+    sc = golden_scene(S, d)
+    sc.P = n
+    sc._solve_ws = torch.empty(int(sc.lib.ap_dense_solve_workspace_bytes(n)), dtype=torch.uint8, device="cuda")
+    Ht, gt = torch.tensor(H, device="cuda"), torch.tensor(g, device="cuda")
+    h = torch.full((n,), 7.0, dtype=torch.float64, device="cuda")
+    info = torch.zeros(1, dtype=torch.int32, device="cuda")
+    N.check(sc.lib.ap_dense_damped_solve_mixed(n, N._ptr(Ht), N._ptr(gt), 0.0, N._ptr(h), N._ptr(sc._solve_ws),
+                                               sc._solve_ws.numel(), N._ptr(info), N._stream()), "mixed")
+    assert int(info.item()) == -1
+    assert torch.all(h == 0)
+    got = sc.solve(Ht, gt, 0.0)
+    want = sc.solve(Ht, gt, 0.0, mixed=False)
+    assert got is not None and not sc._last_mixed
+    assert torch.equal(got, want)
 
 
 @pytest.mark.parametrize("name", cases.group_case_names())
