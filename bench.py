@@ -386,8 +386,10 @@ def run_gpu(args):
 
         if rank_info()[0] == 0:
             dev = torch.device("cuda")
-            print(json.dumps({"workload": "crowded", "crowded_field": crowded_block(args, dev),
-                              "bulge_disk_field": bulge_disk_block(args, dev)}), flush=True)
+            line = {"workload": "crowded", "crowded_field": crowded_block(args, dev)}
+            if not args.no_configs:
+                line["bulge_disk_field"] = bulge_disk_block(args, dev)
+            print(json.dumps(line), flush=True)
     else:
         run_gpu_cutouts(args)
 
