@@ -7,7 +7,8 @@
 //   hess      H = J^T W J over the joint vector, one block per pair of overlapping windows
 //   jt        J^T v for an image v (gradient, geodesic-acceleration right-hand side)
 //   jvp       J h as an image
-//   chi2      sum of W (Y - M)^2 over unmasked pixels (LM._chi2, astrophot/fit/lm.py:374-378)
+//   chi2      sum of W (Y - M)^2 over unmasked pixels (LM._chi2, astrophot/fit/lm.py:374-378),
+//             block partial sums added in a fixed order
 //   solve     the damped system of LM._h (astrophot/fit/lm.py:361-371) for a dense P x P
 //             matrix: blocked Cholesky in FP64 plus two triangular solves
 // Linked parameters (one node shared by several sources) are one entry of the joint vector:
@@ -164,16 +165,34 @@ __global__ void __launch_bounds__(256) k_scene_hess(const ap_scene_source* __res
 }
 
 // ---- chi2 and residual images --------------------------------------------------------------------
-__global__ void k_scene_chi2(const float* __restrict__ model, const float* __restrict__ data,
-                             const float* __restrict__ weight, const uint8_t* __restrict__ mask, int64_t n,
-                             double* __restrict__ out) {
-  // one block, partial sums added in a fixed order: the same chi^2 bits on every run
+// chi^2 in two passes with a fixed summation order (the same bits on every run): block b sums
+// the pixels [b chunk, (b + 1) chunk) into part[b], then one block sums the parts in order.  The
+// float64 arithmetic per pixel is spread over the whole GPU (its float64 pipe is narrow).
+__global__ void __launch_bounds__(256) k_scene_chi2_part(const float* __restrict__ model, const float* __restrict__ data,
+                                                         const float* __restrict__ weight,
+                                                         const uint8_t* __restrict__ mask, int64_t n, int64_t chunk,
+                                                         double* __restrict__ part) {
+  const int64_t lo = (int64_t)blockIdx.x * chunk, hi = lo + chunk < n ? lo + chunk : n;
   double acc = 0.0;
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+  for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
     if (mask && mask[i]) continue;
     const double r = (double)data[i] - (double)model[i];
     acc += (weight ? (double)weight[i] : 1.0) * r * r;
   }
+  acc = warp_sum(acc);
+  __shared__ double sh[8];
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w];
+    part[blockIdx.x] = t;
+  }
+}
+
+__global__ void k_sum_parts(const double* __restrict__ part, int m, double* __restrict__ out) {
+  double acc = 0.0;
+  for (int k = threadIdx.x; k < m; k += blockDim.x) acc += part[k];
   acc = warp_sum(acc);
   __shared__ double sh[32];
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
@@ -535,12 +554,15 @@ int ap_scene_hess(const ap_scene_source* sources, const int32_t* pairs, int32_t 
 }
 
 int ap_scene_chi2(const float* model, const float* data, const float* weight, const uint8_t* mask, int64_t n,
-                  double* out, ap_stream_t stream) {
-  if (!model || !data || !out || n <= 0) return AP_ERR_ARG;
+                  double* out, double* parts, int32_t n_parts, ap_stream_t stream) {
+  if (!model || !data || !out || !parts || n <= 0 || n_parts < 1) return AP_ERR_ARG;
   cudaStream_t st = (cudaStream_t)stream;
-  int rc = record_cuda(cudaMemsetAsync(out, 0, sizeof(double), st));
-  if (rc) return rc;
-  k_scene_chi2<<<1, 1024, 0, st>>>(model, data, weight, mask, n, out);
+  const int m = n_parts < 1024 ? n_parts : 1024;
+  int64_t chunk = (n + m - 1) / m;
+  chunk = (chunk + 255) / 256 * 256;
+  const int blocks = (int)((n + chunk - 1) / chunk);
+  k_scene_chi2_part<<<blocks, 256, 0, st>>>(model, data, weight, mask, n, chunk, parts);
+  k_sum_parts<<<1, 256, 0, st>>>(parts, blocks, out);
   return record_cuda(cudaGetLastError());
 }
 

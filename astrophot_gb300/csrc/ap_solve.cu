@@ -14,10 +14,10 @@
 //
 // Pieces:
 //   k_damp32          float32 lower triangle of the damped matrix and ||A||_inf (float64)
-//   k_chol32_panel    one 32-column step: the diagonal block factored in registers (a row per
-//                     lane, shuffles), its explicit inverse, the panel rows below as
-//                     A_panel L_kk^-T (every CTA factors the small block itself: no extra launch)
-//   k_chol32_update   the trailing lower triangle minus the panel's rank-32 product, 64 x 64 tiles
+//   k_chol32_diag     the first 32 x 32 diagonal block factored and inverted (one CTA)
+//   k_chol32_panel    one 32-column step: the panel rows below as A_panel L_kk^-T
+//   k_chol32_update   the trailing lower triangle minus the panel's rank-32 product, 64 x 64 tiles;
+//                     the CTA holding the next diagonal block then factors and inverts it
 //   k_trsv32          both triangular solves in one CTA, with the diagonal blocks' inverses
 //   k_ir_residual     r = g - A x in float64 from H (a warp per row), the inf-norms of r and x
 //   k_ir_check        the convergence test; every refinement kernel returns at once when done
@@ -76,10 +76,6 @@ inline Layout layout(int n, void* ws) {
   return L;
 }
 
-__device__ __forceinline__ float warp_sumf(float v) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
 __device__ __forceinline__ double warp_sumd(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
@@ -128,89 +124,105 @@ __global__ void k_anorm_store(MixedState* st) {
   st->rnorm = 0ull;
 }
 
-// The nb x nb diagonal block at k0 factored by one warp (lane = row, the row in registers; rows
-// nb..31 are the identity), then its inverse (lane = column).  D and Dinv: shared [32][33].
-// A non-positive or non-finite pivot records 1 + row in info32 (when `report`) and takes pivot 1.
-__device__ void chol_block32(const float* __restrict__ A, int n, int k0, int nb, float (*D)[kB + 1],
-                             float (*Dinv)[kB + 1], int* info32, bool report) {
-  const int lane = threadIdx.x & 31;
-  float a[kB];
-  const float* row = A + (int64_t)(k0 + lane) * n + k0;
+// The nb x nb diagonal block at kd (rows nb..31 the identity) factored and inverted by the 256
+// threads of a CTA, in shared memory, with small code (loops over the 32 columns are not
+// unrolled: this runs once per CTA, where a fully unrolled body would wait on instruction
+// fetch).  Thread t owns the elements (t >> 3, (t & 7) + 8 q), q < 4.  Right-looking: at step j
+// every thread updates its elements right of column j with the raw column scaled by 1/L_jj, one
+// barrier, then column j itself is scaled.  The inverse of the factor: R = I; row k of L^-1 is
+// R[k] / L_kk, subtracted from the rows below with L[i][k] as weight.  A non-positive or
+// non-finite pivot records 1 + row in info32 and takes pivot 1.  Writes L^-1 (zeros above the
+// diagonal) to Linv_blk.  S and R: shared [32][33]; uses every thread of the CTA (256).
+__device__ void diag_factor_inv(const float* __restrict__ A, int n, int kd, float* __restrict__ Linv_blk,
+                                int* info32, float (*S)[kB + 1], float (*R)[kB + 1], float* invd) {
+  const int t = threadIdx.x, i = t >> 3, cb = t & 7;
+  const int nb = min(kB, n - kd);
 #pragma unroll
-  for (int c = 0; c < kB; ++c) a[c] = (lane < nb) ? ((c <= lane && c < nb) ? row[c] : 0.f) : (c == lane ? 1.f : 0.f);
-#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int c = cb + 8 * q;
+    S[i][c] = (i < nb && c < nb) ? (c <= i ? A[(int64_t)(kd + i) * n + kd + c] : 0.f) : (i == c ? 1.f : 0.f);
+    R[i][c] = (i == c) ? 1.f : 0.f;
+  }
+  __syncthreads();
   for (int j = 0; j < kB; ++j) {
-    float djj = __shfl_sync(0xffffffffu, a[j], j);
-    if (!(djj > 0.f) || !isfinite(djj)) {
-      if (report && lane == 0) atomicCAS(info32, 0, 1 + k0 + j);
-      djj = 1.f;
+    float piv = S[j][j];
+    if (!(piv > 0.f) || !isfinite(piv)) {
+      if (t == 0) atomicCAS(info32, 0, 1 + kd + j);
+      piv = 1.f;
     }
-    const float s = sqrtf(djj), inv = 1.f / s;
-    if (lane == j) a[j] = s;
-    else if (lane > j) a[j] *= inv;
+    const float sj = sqrtf(piv), inv = 1.f / sj;
+    const float lij = S[i][j] * inv;
 #pragma unroll
-    for (int c = j + 1; c < kB; ++c) {
-      const float lcj = __shfl_sync(0xffffffffu, a[j], c);
-      if (lane >= c) a[c] = fmaf(-a[j], lcj, a[c]);
+    for (int q = 0; q < 4; ++q) {
+      const int c = cb + 8 * q;
+      if (c > j && c <= i) S[i][c] = fmaf(-lij, S[c][j] * inv, S[i][c]);
     }
+    __syncthreads();
+    if (cb == 0 && i >= j) S[i][j] = (i == j) ? sj : S[i][j] * inv;
+    __syncthreads();
+  }
+  if (t < kB) invd[t] = 1.f / S[t][t];
+  __syncthreads();
+  for (int k = 0; k < kB; ++k) {
+    const float wk = invd[k];
+    if (i > k) {
+      const float lik = S[i][k];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int c = cb + 8 * q;
+        if (c <= k) R[i][c] = fmaf(-lik, R[k][c] * wk, R[i][c]);
+      }
+    }
+    __syncthreads();
+    if (i == k) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int c = cb + 8 * q;
+        if (c <= k) R[k][c] *= wk;
+      }
+    }
+    __syncthreads();
   }
 #pragma unroll
-  for (int c = 0; c < kB; ++c) D[lane][c] = (c <= lane) ? a[c] : 0.f;
-  __syncwarp();
-  // inverse of the lower-triangular block, column `lane`: w[i] = -(sum_{k<i} L_ik w_k) / L_ii
-  float wv[kB];
-#pragma unroll
-  for (int i = 0; i < kB; ++i) {
-    if (i < lane) {
-      wv[i] = 0.f;
-    } else if (i == lane) {
-      wv[i] = 1.f / D[i][i];
-    } else {
-      float s = 0.f;
-#pragma unroll
-      for (int k = 0; k < i; ++k)
-        if (k >= lane) s = fmaf(D[i][k], wv[k], s);
-      wv[i] = -s / D[i][i];
-    }
+  for (int q = 0; q < 4; ++q) {
+    const int c = cb + 8 * q;
+    Linv_blk[i * kB + c] = (c <= i) ? R[i][c] : 0.f;
   }
-#pragma unroll
-  for (int i = 0; i < kB; ++i) Dinv[i][lane] = wv[i];
-  __syncwarp();
 }
 
-// column step k0: CTA 0 stores the inverse of the factored diagonal block; CTA b >= 1 turns
-// panel rows k0 + nb + (b - 1) * kPanelRows + t into A_panel L_kk^-T
+// the first diagonal block (the others are factored by the trailing update that finishes them)
+__global__ void __launch_bounds__(256) k_chol32_diag(const float* __restrict__ A, int n, float* __restrict__ Linv,
+                                                     MixedState* __restrict__ st) {
+  __shared__ float S[kB][kB + 1], R[kB][kB + 1], invd[kB];
+  diag_factor_inv(A, n, 0, Linv, &st->info32, S, R, invd);
+}
+
+// panel rows of step k0: row r (thread) becomes A[r][k0:k0+nb] L_kk^-T = sum_c a_c Linv[j][c]
 __global__ void __launch_bounds__(kPanelRows) k_chol32_panel(float* __restrict__ A, int n, int k0,
-                                                             float* __restrict__ Linv, MixedState* __restrict__ st) {
-  __shared__ float D[kB][kB + 1], Dinv[kB][kB + 1];
+                                                             const float* __restrict__ Linv) {
+  __shared__ float Li[kB][kB + 1];
   const int nb = min(kB, n - k0);
-  if (threadIdx.x < 32) chol_block32(A, n, k0, nb, D, Dinv, &st->info32, blockIdx.x == 0);
+  const float* Lb = Linv + (int64_t)(k0 / kB) * kB * kB;
+  for (int e = threadIdx.x; e < kB * kB; e += blockDim.x) Li[e / kB][e % kB] = Lb[e];
   __syncthreads();
-  if (blockIdx.x == 0) {
-    // only the inverse is kept (the triangular solves use it); A's diagonal block is left as it
-    // is, since the other CTAs of this launch read it
-    float* Lb = Linv + (int64_t)(k0 / kB) * kB * kB;
-    for (int t = threadIdx.x; t < kB * kB; t += blockDim.x) Lb[t] = Dinv[t / kB][t % kB];
-    return;
-  }
-  const int r = k0 + nb + (blockIdx.x - 1) * kPanelRows + threadIdx.x;
+  const int r = k0 + nb + blockIdx.x * kPanelRows + threadIdx.x;
   if (r >= n) return;
   float* row = A + (int64_t)r * n + k0;
   float a[kB];
 #pragma unroll
   for (int c = 0; c < kB; ++c) a[c] = c < nb ? row[c] : 0.f;
-#pragma unroll
-  for (int j = 0; j < kB; ++j) {
-    if (j >= nb) break;
+  for (int j = 0; j < nb; ++j) {
     float s = 0.f;
 #pragma unroll
-    for (int c = 0; c <= j; ++c) s = fmaf(a[c], Dinv[j][c], s);
+    for (int c = 0; c < kB; ++c) s = fmaf(a[c], Li[j][c], s);
     row[j] = s;
   }
 }
 
-// trailing update of the lower triangle: A[i][j] -= sum_c P[i][c] P[j][c], i >= j >= k0 + nb
-__global__ void __launch_bounds__(256) k_chol32_update(float* __restrict__ A, int n, int k0) {
+// trailing update of the lower triangle: A[i][j] -= sum_c P[i][c] P[j][c], i >= j >= k0 + nb;
+// the CTA of tile (0, 0), which holds the next diagonal block, then factors and inverts it
+__global__ void __launch_bounds__(256) k_chol32_update(float* __restrict__ A, int n, int k0, float* __restrict__ Linv,
+                                                       MixedState* __restrict__ st) {
   const int ti = blockIdx.y, tj = blockIdx.x;
   if (tj > ti) return;
   const int nb = min(kB, n - k0), base = k0 + nb;
@@ -248,6 +260,13 @@ __global__ void __launch_bounds__(256) k_chol32_update(float* __restrict__ A, in
       const int j = j0 + tx * 4 + q;
       if (j < n && j <= i) A[(int64_t)i * n + j] -= acc[p][q];
     }
+  }
+  if (ti == 0 && tj == 0) {
+    __syncthreads();  // this CTA's updates of the next diagonal block are written; Pi / Pj free
+    float (*S)[kB + 1] = reinterpret_cast<float (*)[kB + 1]>(&Pi[0][0]);
+    float (*R)[kB + 1] = reinterpret_cast<float (*)[kB + 1]>(&Pj[0][0]);
+    __shared__ float invd[kB];
+    diag_factor_inv(A, n, base, Linv + (int64_t)(base / kB) * kB * kB, &st->info32, S, R, invd);
   }
 }
 
@@ -436,14 +455,14 @@ int ap_dense_damped_solve_mixed(int32_t n, const double* H, const double* g, dou
   k_set_damping<<<1, 1, 0, st>>>(Lw.st, L, 1.0 / (1.0 + L), 1);
   k_damp32<<<n < 2048 ? n : 2048, 256, 0, st>>>(n, H, Lw.A32, Lw.st);
   k_anorm_store<<<1, 1, 0, st>>>(Lw.st);
+  k_chol32_diag<<<1, 256, 0, st>>>(Lw.A32, n, Lw.Linv, Lw.st);
   for (int k0 = 0; k0 < n; k0 += kB) {
     const int nb = n - k0 < kB ? n - k0 : kB;
     const int rest = n - k0 - nb;
-    k_chol32_panel<<<1 + (rest + kPanelRows - 1) / kPanelRows, kPanelRows, 0, st>>>(Lw.A32, n, k0, Lw.Linv, Lw.st);
-    if (rest > 0) {
-      const int nt = (rest + kTile - 1) / kTile;
-      k_chol32_update<<<dim3(nt, nt), 256, 0, st>>>(Lw.A32, n, k0);
-    }
+    if (rest <= 0) break;
+    k_chol32_panel<<<(rest + kPanelRows - 1) / kPanelRows, kPanelRows, 0, st>>>(Lw.A32, n, k0, Lw.Linv);
+    const int nt = (rest + kTile - 1) / kTile;
+    k_chol32_update<<<dim3(nt, nt), 256, 0, st>>>(Lw.A32, n, k0, Lw.Linv, Lw.st);
   }
   return record_cuda(refine(n, H, g, h, info, Lw, st));
 }

@@ -399,6 +399,7 @@ class Scene:
         self._info2 = torch.zeros(1, dtype=torch.int32, device=dev)
         self._last_mixed = False
         self._d64 = torch.zeros(1, dtype=torch.float64, device=dev)
+        self._chi2_parts = torch.zeros(1024, dtype=torch.float64, device=dev)
 
     # ---- geometry and parameters -----------------------------------------------------------
     def _window(self, si):
@@ -537,7 +538,8 @@ class Scene:
     def chi2_into(self, model: torch.Tensor, out: torch.Tensor):
         """chi^2 of ``model`` into the device float64 ``out[0]`` (no host read)."""
         N.check(self.lib.ap_scene_chi2(N._ptr(model), N._ptr(self.data), N._ptr(self.weight), N._ptr(self.mask),
-                                       self.nx * self.ny, N._ptr(out), N._stream()), "ap_scene_chi2")
+                                       self.nx * self.ny, N._ptr(out), N._ptr(self._chi2_parts),
+                                       self._chi2_parts.numel(), N._stream()), "ap_scene_chi2")
 
     def solve_device(self, H: torch.Tensor, g: torch.Tensor, L: float, info: torch.Tensor, mixed: bool = True,
                      reuse: bool = False) -> torch.Tensor:
@@ -748,7 +750,8 @@ class Scene:
 
     def chi2(self, model: torch.Tensor) -> float:
         N.check(self.lib.ap_scene_chi2(N._ptr(model), N._ptr(self.data), N._ptr(self.weight), N._ptr(self.mask),
-                                       self.nx * self.ny, N._ptr(self._d64), N._stream()), "ap_scene_chi2")
+                                       self.nx * self.ny, N._ptr(self._d64), N._ptr(self._chi2_parts),
+                                       self._chi2_parts.numel(), N._stream()), "ap_scene_chi2")
         return float(self._d64.item())
 
     def residual(self, model: torch.Tensor, data: Optional[torch.Tensor] = None) -> torch.Tensor:

@@ -390,9 +390,11 @@ int ap_scene_jt(const ap_scene_source* sources, int32_t n_sources, const float* 
 int ap_scene_hess(const ap_scene_source* sources, const int32_t* pairs, int32_t n_pairs,
                   const float* jac, const float* weight, const uint8_t* mask, int32_t nx, int32_t P,
                   double* H, ap_stream_t stream);
-/* out[0] = sum over unmasked pixels of W (data - model)^2 (float64). */
+/* out[0] = sum over unmasked pixels of W (data - model)^2 (float64).  parts: device scratch of
+ * n_parts doubles (1024 used at most) for the block partial sums, which are added in a fixed
+ * order, so the result has the same bits on every run. */
 int ap_scene_chi2(const float* model, const float* data, const float* weight, const uint8_t* mask,
-                  int64_t n, double* out, ap_stream_t stream);
+                  int64_t n, double* out, double* parts, int32_t n_parts, ap_stream_t stream);
 /* r = W (data - model) on unmasked pixels, 0 on masked ones (LM._r, fit/lm.py:381-385). */
 int ap_scene_residual(const float* model, const float* data, const float* weight,
                       const uint8_t* mask, int64_t n, float* r, ap_stream_t stream);
