@@ -432,6 +432,9 @@ int ap_batch_create(ap_batch** out, int32_t n, const int32_t* nx, const int32_t*
   A.n_work_tiles = (int32_t)b->work_tiles.size();
   A.n_out_tiles = (int32_t)b->out_tiles.size();
   A.max_kp2 = b->max_kp2;
+  A.conv_large = 0;
+  for (const StampDev& st : b->stamps)
+    if (st.kpx != st.kpy || st.kpx > 29) A.conv_large = 1;
   A.tolerance = (float)options->sampling_tolerance;
   A.tolerance64 = options->sampling_tolerance;
   A.softening64 = options->softening;

@@ -182,6 +182,7 @@ struct BatchArgs {
   int32_t has_sky;
   int32_t n_work_tiles, n_out_tiles;
   int32_t max_kp2;      // largest kpy * kpx
+  int32_t conv_large;   // some stamp's kernel is not a square of side 3..29 (k_conv's chunked flavour)
   int32_t thr_window;   // some stamp sums its integration threshold over its gw_* window
   float tolerance;
   float center_r2;      // AP_SAMPLING_MIDPOINT_CENTER: squared radius (+ 1e-6) in pixels
@@ -274,9 +275,11 @@ __host__ __device__ inline int conv_tile_pitch(int kpy) {
   return th + ((4 - th % 8) + 8) % 8;
 }
 
+// floats after the second tile: the chunked convolution of large kernels reads up to 3 past it
+constexpr int kConvSmemPad = 16;
 __host__ __device__ inline size_t conv_smem_bytes(int kpx, int kpy) {
   return sizeof(float) * (3 * (size_t)kpx * conv_col_stride(kpy) +
-                          2 * (size_t)(kOutTileX + kpx - 1) * conv_tile_pitch(kpy));
+                          2 * (size_t)(kOutTileX + kpx - 1) * conv_tile_pitch(kpy) + kConvSmemPad);
 }
 
 __host__ __device__ inline int64_t work_plane(const BatchArgs& b, int slot, int plane) {

@@ -1463,9 +1463,85 @@ __device__ __forceinline__ void conv_col_generic(const float* __restrict__ Tt, i
   for (int o = 0; o < kConvRows; ++o) out[o] = acc[o];
 }
 
-// One copy of all the kernel-size instances, shared by the k_conv<NF> instantiations.
+// Kernels the fixed instances do not cover (kpy >= 8): each kernel column in chunks of 8 rows,
+// the chunk (two float4 loads) and the input window it meets (four float4 loads) in registers,
+// 32 FMAs per chunk.  With lo = kpy - 1 - v0 - 7 the first input row of chunk v0, lo mod 4 =
+// kpy mod 4 = SH, so the window is read from the 16-byte aligned row lo - SH (the tile pitch and
+// ty0 are multiples of 4).  The window may reach up to 10 floats before the column (inside the
+// kernels stored ahead of the tile: 3 kpx ks >= 24 floats) and 3 past the last column (the
+// allocation is padded by kConvSmemPad floats); rows of the chunk at or beyond kpy are skipped.
+template <int SH>
+__device__ __forceinline__ void conv_col_chunked(const float* __restrict__ Tt, int TP, const float* __restrict__ KT,
+                                                 int kpx, int kpy, int tx, int ty0, float* out) {
+  float acc[kConvRows];
+#pragma unroll
+  for (int o = 0; o < kConvRows; ++o) acc[o] = 0.f;
+  const int ks = conv_col_stride(kpy);
+  for (int u = 0; u < kpx; ++u) {
+    const float* kcol = KT + u * ks;
+    const float* tcol = Tt + (tx + kpx - 1 - u) * TP + ty0;
+    for (int v0 = 0; v0 < kpy; v0 += 8) {
+      float kc[8];
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const float4 k4 = *reinterpret_cast<const float4*>(kcol + v0 + 4 * q);
+        kc[4 * q + 0] = k4.x;
+        kc[4 * q + 1] = k4.y;
+        kc[4 * q + 2] = k4.z;
+        kc[4 * q + 3] = k4.w;
+      }
+      const float4* w4 = reinterpret_cast<const float4*>(tcol + (kpy - 8 - v0) - SH);
+      float t[16];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float4 c4 = w4[q];
+        t[4 * q + 0] = c4.x;
+        t[4 * q + 1] = c4.y;
+        t[4 * q + 2] = c4.z;
+        t[4 * q + 3] = c4.w;
+      }
+      const int nv = min(8, kpy - v0);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        if (j < nv) {
+#pragma unroll
+          for (int o = 0; o < kConvRows; ++o) acc[o] = fmaf(kc[j], t[SH + 7 - j + o], acc[o]);
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int o = 0; o < kConvRows; ++o) out[o] = acc[o];
+}
+
+// One copy of the kernel-size instances per k_conv flavour, shared by its k_conv<NF, LARGE>
+// instantiations.  LARGE = false: the register-blocked square sizes 3..29 (and the plain loop
+// for anything else); LARGE = true (a batch with a kernel the fixed sizes do not cover): the
+// chunked columns for kpy >= 8.  Separate flavours keep the chunked code's registers out of the
+// kernels that run the fixed sizes.
+template <bool LARGE>
 __device__ __noinline__ void conv_col(const float* Tt, int TP, const float* KT, int kpx, int kpy,
                                       int tx, int ty0, float* out) {
+  if (LARGE) {
+    if (kpy >= 8) {
+      switch (kpy & 3) {
+        case 0:
+          conv_col_chunked<0>(Tt, TP, KT, kpx, kpy, tx, ty0, out);
+          return;
+        case 1:
+          conv_col_chunked<1>(Tt, TP, KT, kpx, kpy, tx, ty0, out);
+          return;
+        case 2:
+          conv_col_chunked<2>(Tt, TP, KT, kpx, kpy, tx, ty0, out);
+          return;
+        default:
+          conv_col_chunked<3>(Tt, TP, KT, kpx, kpy, tx, ty0, out);
+          return;
+      }
+    }
+    conv_col_generic(Tt, TP, KT, kpx, kpy, tx, ty0, out);
+    return;
+  }
   if (kpx == kpy) {
     switch (kpx) {
 #define AP_CONV_CASE(K) \
@@ -1485,7 +1561,7 @@ __device__ __noinline__ void conv_col(const float* Tt, int TP, const float* KT, 
 
 // Convolve/accumulate pass.  NF = number of fitted parameters (compile time, so the
 // per-pixel J^T W J accumulators stay in registers).
-template <int NF>
+template <int NF, bool LARGE>
 __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, float* smem,
                                           float* shred, int slot, int s, int local) {
   const EvalDev& e = b.evals[s * 2 + slot];
@@ -1499,6 +1575,27 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
   const bool diff = (ops & OP_DIFF) != 0;  // (forward only: no Jacobian planes)
   const bool shiftmode = (b.psf_mode == AP_PSF_FULL);
   const int nplanes = jac ? 1 + NGRAD : 1;
+
+  // the epilogue's per-pixel operands (data, weight, the base model and, for the curvature
+  // term, the base Jacobian) are requested into L2 now, so that their loads after the
+  // convolution do not wait on DRAM: one thread per (tile row, plane) row segment, both ends
+  {
+    const bool fit = (ops & (OP_CHI2 | OP_HG | OP_RPP)) != 0 && !(ops & OP_VJP);
+    const int npf = fit ? 2 + ((diff || (ops & OP_RPP)) ? 1 : 0) + ((ops & OP_RPP) ? NF : 0) : 0;
+    const int rows = min(kOutTileY, st.ny - y0), w = min(kOutTileX, st.nx - x0);
+    for (int k = threadIdx.x; k < npf * rows; k += blockDim.x) {
+      const int pl = k / rows, r = k - pl * rows;
+      const int64_t op = st.out_off + (int64_t)(y0 + r) * st.nx + x0;
+      const float* base = pl == 0 ? io.data
+                        : pl == 1 ? io.weight
+                        : (pl == 2 && (diff || (ops & OP_RPP))) ? io.y0
+                        : io.jbase + (int64_t)(pl - 3) * b.out_pixels;
+      if (base) {
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(base + op));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(base + op + w - 1));
+      }
+    }
+  }
 
   // conv results per row: [0] model, [1] d/dshift_x, [2] d/dshift_y, [3 + q] partial plane q
   float cv[3 + NGRAD][kConvRows];
@@ -1608,7 +1705,7 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
       for (int kk = 0; kk < nkp; ++kk) {
         float outv[kConvRows];
         const int kidx = diff ? pl : kk;
-        conv_col(Tt + (bi ? tsz : 0), TP, KT + kidx * kstride, kpx, kpy, tx, tg * kConvRows, outv);
+        conv_col<LARGE>(Tt + (bi ? tsz : 0), TP, KT + kidx * kstride, kpx, kpy, tx, tg * kConvRows, outv);
         const int dst = diff ? pl : ((pl == 0) ? kk : 3 + (pl - 1));
 #pragma unroll
         for (int o = 0; o < kConvRows; ++o) cv[dst][o] = outv[o];
@@ -1741,7 +1838,7 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
   conv_tile_reduce(vals, nv, tacc, shred);
 }
 
-template <int NF>
+template <int NF, bool LARGE>
 __global__ void __launch_bounds__(kConvThreads, 5) k_conv(BatchArgs b, ConvIO io) {
   extern __shared__ __align__(16) float smem[];
   __shared__ float shred[kConvWarps * kNacc];
@@ -1755,7 +1852,7 @@ __global__ void __launch_bounds__(kConvThreads, 5) k_conv(BatchArgs b, ConvIO io
     if (it >= n) break;
     int slot, s, local;
     unpack_entry(b.olist[it], slot, s, local);
-    conv_tile<NF>(b, io, smem, shred, slot, s, local);
+    conv_tile<NF, LARGE>(b, io, smem, shred, slot, s, local);
     __syncthreads();  // smem / shred / next reuse by the next tile
   }
 }
@@ -1867,9 +1964,12 @@ cudaError_t set_conv_smem(size_t bytes) {
     const cudaError_t r = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, nb);
     if (r != cudaSuccess) e = r;
   };
-  set((const void*)k_conv<0>); set((const void*)k_conv<1>); set((const void*)k_conv<2>);
-  set((const void*)k_conv<3>); set((const void*)k_conv<4>); set((const void*)k_conv<5>);
-  set((const void*)k_conv<6>); set((const void*)k_conv<7>); set((const void*)k_conv<8>);
+  set((const void*)k_conv<0, false>); set((const void*)k_conv<1, false>); set((const void*)k_conv<2, false>);
+  set((const void*)k_conv<3, false>); set((const void*)k_conv<4, false>); set((const void*)k_conv<5, false>);
+  set((const void*)k_conv<6, false>); set((const void*)k_conv<7, false>); set((const void*)k_conv<8, false>);
+  set((const void*)k_conv<0, true>); set((const void*)k_conv<1, true>); set((const void*)k_conv<2, true>);
+  set((const void*)k_conv<3, true>); set((const void*)k_conv<4, true>); set((const void*)k_conv<5, true>);
+  set((const void*)k_conv<6, true>); set((const void*)k_conv<7, true>); set((const void*)k_conv<8, true>);
   if (e == cudaSuccess && dev >= 0 && dev < 64) raised[dev] = bytes;
   return e;
 }
@@ -1948,16 +2048,30 @@ cudaError_t launch_render_pass(const BatchArgs& b, const ConvIO& io, size_t conv
     if (fe != cudaSuccess) return fe;
   }
   const dim3 cgrid(grid(2 * (int64_t)b.n_out_tiles, knob(GK_CONV, 16)));
-  switch (b.n_free) {
-    case 0: k_conv<0><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
-    case 1: k_conv<1><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
-    case 2: k_conv<2><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
-    case 3: k_conv<3><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
-    case 4: k_conv<4><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
-    case 5: k_conv<5><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
-    case 6: k_conv<6><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
-    case 7: k_conv<7><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
-    default: k_conv<8><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
+  if (b.conv_large) {
+    switch (b.n_free) {
+      case 0: k_conv<0, true><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
+      case 1: k_conv<1, true><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
+      case 2: k_conv<2, true><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
+      case 3: k_conv<3, true><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
+      case 4: k_conv<4, true><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
+      case 5: k_conv<5, true><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
+      case 6: k_conv<6, true><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
+      case 7: k_conv<7, true><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
+      default: k_conv<8, true><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
+    }
+  } else {
+    switch (b.n_free) {
+      case 0: k_conv<0, false><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
+      case 1: k_conv<1, false><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
+      case 2: k_conv<2, false><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
+      case 3: k_conv<3, false><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
+      case 4: k_conv<4, false><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
+      case 5: k_conv<5, false><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
+      case 6: k_conv<6, false><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
+      case 7: k_conv<7, false><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
+      default: k_conv<8, false><<<cgrid, kConvThreads, conv_smem, s>>>(b, io); break;
+    }
   }
   E(t);
   if (accumulate) {

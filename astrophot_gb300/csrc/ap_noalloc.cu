@@ -321,6 +321,7 @@ extern "C" int ap_render_noalloc(int32_t nx, int32_t ny, int32_t psf_kx, int32_t
   A.n_work_tiles = st.ntw;
   A.n_out_tiles = st.nto;
   A.max_kp2 = (int32_t)kp2;
+  A.conv_large = (st.kpx != st.kpy || st.kpx > 29) ? 1 : 0;
   A.tolerance = (float)options->sampling_tolerance;
   A.tolerance64 = options->sampling_tolerance;
   A.softening64 = options->softening;

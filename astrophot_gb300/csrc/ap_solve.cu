@@ -294,6 +294,7 @@ __global__ void __launch_bounds__(kTrsvThreads) k_trsv32(int n, const float* __r
   __shared__ float blk[kB];
   if (st->done) return;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const bool vec = (n & 3) == 0 && ((reinterpret_cast<uintptr_t>(A) & 15) == 0);
   for (int i = threadIdx.x; i < n; i += blockDim.x) y[i] = (float)r[i];
   __syncthreads();
   const int nbk = nblocks(n);
@@ -301,26 +302,47 @@ __global__ void __launch_bounds__(kTrsvThreads) k_trsv32(int n, const float* __r
   for (int b = 0; b < nbk; ++b) {
     const int kb = b * kB, nb = min(kB, n - kb);
     if (w == 0) {
-      const float* Lb = Linv + (int64_t)b * kB * kB;
+      // row `lane` of the block's inverse (zeros above the diagonal), as float4 loads
+      const float4* Lr = reinterpret_cast<const float4*>(Linv + (int64_t)b * kB * kB + lane * kB);
       const float yv = lane < nb ? y[kb + lane] : 0.f;
       float v = 0.f;
 #pragma unroll
-      for (int c = 0; c < kB; ++c) {
-        const float yc = __shfl_sync(0xffffffffu, yv, c);
-        if (c <= lane) v = fmaf(Lb[lane * kB + c], yc, v);
+      for (int q = 0; q < kB / 4; ++q) {
+        const float4 l4 = Lr[q];
+        v = fmaf(l4.x, __shfl_sync(0xffffffffu, yv, 4 * q + 0), v);
+        v = fmaf(l4.y, __shfl_sync(0xffffffffu, yv, 4 * q + 1), v);
+        v = fmaf(l4.z, __shfl_sync(0xffffffffu, yv, 4 * q + 2), v);
+        v = fmaf(l4.w, __shfl_sync(0xffffffffu, yv, 4 * q + 3), v);
       }
       blk[lane] = v;
       if (lane < nb) y[kb + lane] = v;
     }
     __syncthreads();
-    // rows below: a thread per row, its 32 loads of the row segment in flight together
-    for (int i = kb + nb + threadIdx.x; i < n; i += blockDim.x) {
-      const float* row = A + (int64_t)i * n + kb;
-      float s = 0.f;
+    // rows below: a thread per row, its loads of the row segment in flight together (float4
+    // when every row starts on a 16-byte boundary; a full block then has nb = 32)
+    if (vec && nb == kB) {
+      for (int i = kb + nb + threadIdx.x; i < n; i += blockDim.x) {
+        const float4* row = reinterpret_cast<const float4*>(A + (int64_t)i * n + kb);
+        float s = 0.f;
 #pragma unroll
-      for (int c = 0; c < kB; ++c)
-        if (c < nb) s = fmaf(row[c], blk[c], s);
-      y[i] -= s;
+        for (int q = 0; q < kB / 4; ++q) {
+          const float4 a4 = row[q];
+          s = fmaf(a4.x, blk[4 * q + 0], s);
+          s = fmaf(a4.y, blk[4 * q + 1], s);
+          s = fmaf(a4.z, blk[4 * q + 2], s);
+          s = fmaf(a4.w, blk[4 * q + 3], s);
+        }
+        y[i] -= s;
+      }
+    } else {
+      for (int i = kb + nb + threadIdx.x; i < n; i += blockDim.x) {
+        const float* row = A + (int64_t)i * n + kb;
+        float s = 0.f;
+#pragma unroll
+        for (int c = 0; c < kB; ++c)
+          if (c < nb) s = fmaf(row[c], blk[c], s);
+        y[i] -= s;
+      }
     }
     __syncthreads();
   }
