@@ -30,7 +30,8 @@ import torch
 from . import _native as N
 from .synthetic import moffat_rd, moffat_stamp
 
-__all__ = ("InitNet", "StampSet", "draw_stamp_params", "psf_bank", "make_stamps", "learned_fit", "plain_fit",
+__all__ = ("InitNet", "StampSet", "draw_stamp_params", "psf_bank", "make_stamps", "learned_fit", "learned_fit_host",
+           "plain_fit",
            "heuristic_init", "subset", "set_tensor_path", "get_tensor_path", "tc_status",
            "WEIGHTS_PATH")
 
@@ -427,3 +428,46 @@ def learned_fit(net: InitNet, st: StampSet, n: int, lm_options=None, judge_sigma
             init[keep] = h[sel]
             which[keep] = 2
     return init, which, (state, chi2, iters, status)
+
+
+def learned_fit_host(net: InitNet, batches, plan: "N.StampBatch", n: int, lm_options=None,
+                     judge_sigma: float = 5.0):
+    """:func:`learned_fit` of batch after batch of stamps held in host memory.  ``batches`` yields
+    (data, weight, psf, sigma) host tensors (pinned for asynchronous copies) in the layout of
+    ``plan`` (``n`` stamps).  Each batch is copied to the device on a copy stream into one of two
+    input buffer sets while the previous batch is fitted, so the host-to-device transfer overlaps
+    the fit instead of preceding it.  Yields, per batch, (state, chi^2, iterations, status) on the
+    host."""
+    dev = plan.device
+    cur = torch.cuda.current_stream(dev)
+    copy = torch.cuda.Stream(device=dev)
+    bufs, sets = [None, None], [None, None]
+    copied = [torch.cuda.Event(), torch.cuda.Event()]
+    used = [torch.cuda.Event(), torch.cuda.Event()]
+    it = iter(batches)
+
+    def upload(slot, host):
+        if bufs[slot] is None:
+            bufs[slot] = [torch.empty(h.shape, dtype=h.dtype, device=dev) for h in host]
+            sets[slot] = StampSet(np.zeros((n, 8)), bufs[slot][0], bufs[slot][1], bufs[slot][2], bufs[slot][3], plan)
+        copy.wait_event(used[slot])  # the fit that read this set is done with it
+        with torch.cuda.stream(copy):
+            for d_, h_ in zip(bufs[slot], host):
+                d_.copy_(h_, non_blocking=True)
+        copied[slot].record(copy)
+
+    nxt = next(it, None)
+    if nxt is None:
+        return
+    upload(0, nxt)
+    k = 0
+    while nxt is not None:
+        slot = k % 2
+        nxt = next(it, None)
+        if nxt is not None:
+            upload(1 - slot, nxt)
+        cur.wait_event(copied[slot])
+        _, _, (state, chi2, iters, status) = learned_fit(net, sets[slot], n, lm_options, judge_sigma)
+        used[slot].record(cur)
+        yield state.cpu(), chi2.cpu(), iters.cpu(), status.cpu()
+        k += 1

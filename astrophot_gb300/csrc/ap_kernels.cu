@@ -1466,10 +1466,12 @@ __device__ __forceinline__ void conv_col_generic(const float* __restrict__ Tt, i
 // Kernels the fixed instances do not cover (kpy >= 8): each kernel column in chunks of 8 rows,
 // the chunk (two float4 loads) and the input window it meets (four float4 loads) in registers,
 // 32 FMAs per chunk.  With lo = kpy - 1 - v0 - 7 the first input row of chunk v0, lo mod 4 =
-// kpy mod 4 = SH, so the window is read from the 16-byte aligned row lo - SH (the tile pitch and
-// ty0 are multiples of 4).  The window may reach up to 10 floats before the column (inside the
-// kernels stored ahead of the tile: 3 kpx ks >= 24 floats) and 3 past the last column (the
-// allocation is padded by kConvSmemPad floats); rows of the chunk at or beyond kpy are skipped.
+// kpy mod 4 = SH, so the window (kChunkWin floats) is read from the 16-byte aligned row lo - SH
+// (the tile pitch and ty0 are multiples of 4).  It may reach up to 10 floats before the column
+// (inside the kernels stored ahead of the tile: 3 kpx ks >= 24 floats) and 3 past the last
+// column (the allocation is padded by kConvSmemPad floats); rows of the chunk at or beyond kpy
+// are skipped.
+constexpr int kChunkWin = (kConvRows + 10 + 3) / 4 * 4;  // window rows SH .. SH + 7 + kConvRows - 1
 template <int SH>
 __device__ __forceinline__ void conv_col_chunked(const float* __restrict__ Tt, int TP, const float* __restrict__ KT,
                                                  int kpx, int kpy, int tx, int ty0, float* out) {
@@ -1491,9 +1493,9 @@ __device__ __forceinline__ void conv_col_chunked(const float* __restrict__ Tt, i
         kc[4 * q + 3] = k4.w;
       }
       const float4* w4 = reinterpret_cast<const float4*>(tcol + (kpy - 8 - v0) - SH);
-      float t[16];
+      float t[kChunkWin];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
+      for (int q = 0; q < kChunkWin / 4; ++q) {
         const float4 c4 = w4[q];
         t[4 * q + 0] = c4.x;
         t[4 * q + 1] = c4.y;

@@ -339,3 +339,25 @@ def test_learned_fit_is_reproducible(N):
     c = cnn.learned_fit(net, sub, len(idx))
     t = torch.as_tensor(idx, device=a[2][1].device)
     assert torch.equal(c[2][1], a[2][1][t])
+
+
+def test_learned_fit_host_streams_batches_like_device_fits(N):
+    """Batches held in pinned host memory, uploaded on a copy stream while the previous batch is
+    fitted (double-buffered device inputs), give bitwise the fits of the same stamps resident on
+    the device, batch by batch."""
+    from astrophot_gb300 import cnn
+
+    net = cnn.InitNet.load()
+    n = 64
+    sets = [cnn.make_stamps(n, seed=s) for s in (5, 6, 7)]
+    # the three batches share one plan: the same PSF shapes
+    plan = sets[0].batch
+    sets = [cnn.StampSet(s.truth, s.data, s.weight, sets[0].psf if k else s.psf, s.sigma, plan)
+            for k, s in enumerate(sets)]
+    host = [tuple(t.cpu().pin_memory() for t in (s.data, s.weight, s.psf, s.sigma)) for s in sets]
+    got = list(cnn.learned_fit_host(net, iter(host), plan, n))
+    assert len(got) == 3
+    for s, (state, chi2, iters, status) in zip(sets, got):
+        _, _, (s2, c2, i2, t2) = cnn.learned_fit(net, s, n)
+        assert torch.equal(state, s2.cpu()) and torch.equal(chi2, c2.cpu())
+        assert torch.equal(iters, i2.cpu()) and torch.equal(status, t2.cpu())
