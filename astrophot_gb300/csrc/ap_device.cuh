@@ -25,9 +25,9 @@ constexpr int kMaxQuad = 5;   // quad levels <= 5  (quad_level^2 <= 32 lanes)
 constexpr int kMaxGrid = 5;   // gridding <= 5     (gridding^2 <= 32 lanes)
 constexpr int kMaxDepth = 3;  // integrate_max_depth <= 3
 constexpr int kTile = 16;     // 16 x 16 working-pixel tiles (sampling / selection)
-constexpr int kOutTileX = 32; // output tiles of the convolve/accumulate pass: 32 x 16 pixels,
-constexpr int kOutTileY = 16; // 128 threads, each thread 4 consecutive rows of one column
-constexpr int kConvRows = 4;
+constexpr int kOutTileX = 32; // output tiles of the convolve/accumulate pass: 32 x 32 pixels,
+constexpr int kOutTileY = 32; // 128 threads, each thread 8 consecutive rows of one column
+constexpr int kConvRows = 8;
 constexpr int kConvThreads = kOutTileX * kOutTileY / kConvRows;
 constexpr int kConvMaxKP = 29; // square kernels up to this size use the register-blocked path
 constexpr int kNumPlanes = 7; // deep + 6 partial planes
