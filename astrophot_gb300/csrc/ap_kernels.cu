@@ -577,6 +577,15 @@ __global__ void __launch_bounds__(256) k_sample(BatchArgs b) {
   }
 }
 
+// Column i and row j of working pixel p (the low 32-bit word of a queue entry) of a window
+// wnx wide, by 32-bit unsigned division (the 64-bit one costs several times the instructions)
+__device__ __forceinline__ void pix_ij(int64_t p, int wnx, int& i, int& j) {
+  const uint32_t q = (uint32_t)p, w = (uint32_t)wnx;
+  const uint32_t jj = q / w;
+  j = (int)jj;
+  i = (int)(q - jj * w);
+}
+
 // ---------------------------------------------------------------------------
 // threshold selection (_sample_integrate) + enqueue
 // ---------------------------------------------------------------------------
@@ -750,7 +759,8 @@ __global__ void __launch_bounds__(256) k_recheck(BatchArgs b) {
       float thr, thr_err;
       double thr64;
       stamp_threshold(b, st, e, s, slot, thr, thr64, thr_err);
-      const int i = (int)(p % st.wnx), j = (int)(p / st.wnx);
+      int i, j;
+      pix_ij(p, st.wnx, i, j);
       double err64;
       if (b.sampling == AP_SAMPLING_MIDPOINT || b.sampling == AP_SAMPLING_TRAPEZOID) {
         const int ic = min(max(i, 1), st.wnx - 2), jc = min(max(j, 1), st.wny - 2);
@@ -903,7 +913,8 @@ __device__ __forceinline__ void level1_pixel(const BatchArgs& b, int64_t ent, bo
   const StampDev& st = b.stamps[s];
   const EvalDev& e = b.evals[s * 2 + slot];
   const EvalF f = load_evalf(st, e);
-  const int i = (int)(p % st.wnx), j = (int)(p / st.wnx);
+  int i, j;
+  pix_ij(p, st.wnx, i, j);
   const float di = (float)(i - f.cix), dj = (float)(j - f.cjy);
   const int ops = e.ops;
   const bool jac = (ops & OP_JAC) != 0;
@@ -1017,7 +1028,9 @@ __global__ void __launch_bounds__(256, 3) k_level1(BatchArgs b) {
       const int64_t p = ent & 0xffffffffll;
       const StampDev& st = b.stamps[s];
       ++n64;
-      push = refine64<EXT>(b, st, b.evals[s * 2 + slot], (int)(p % st.wnx), (int)(p / st.wnx), -1,
+      int pi, pj;
+      pix_ij(p, st.wnx, pi, pj);
+      push = refine64<EXT>(b, st, b.evals[s * 2 + slot], pi, pj, -1,
                       b.evals[s * 2 + slot].thresh64);
     }
     level2_append(b, push, ent);
@@ -1052,7 +1065,9 @@ __global__ void __launch_bounds__(256) k_level1_amb(BatchArgs b) {
       const int64_t p = ent & 0xffffffffll;
       const StampDev& st = b.stamps[s];
       const EvalDev& e = b.evals[s * 2 + slot];
-      push = refine64<EXT>(b, st, e, (int)(p % st.wnx), (int)(p / st.wnx), -1, e.thresh64);
+      int pi, pj;
+      pix_ij(p, st.wnx, pi, pj);
+      push = refine64<EXT>(b, st, e, pi, pj, -1, e.thresh64);
     }
     level2_append(b, push, ent);
   }
@@ -1073,7 +1088,8 @@ __device__ void level23_pixel(const BatchArgs& b, int slot, int s, int64_t p, in
   const EvalF f = load_evalf(st, e);
   DeltaF d{};
   if (DIFF) d = load_deltaf(e);
-  const int i = (int)(p % st.wnx), j = (int)(p / st.wnx);
+  int i, j;
+  pix_ij(p, st.wnx, i, j);
   const float di = (float)(i - f.cix), dj = (float)(j - f.cjy);
   const float thr = e.thresh;
   const float ginv = 1.f / (float)g;
@@ -1152,28 +1168,25 @@ struct PackSmem {
   int64_t ent[kPack];
   uint32_t mask[kPack];   // level-3 flags of each pixel's sub-pixels
   int32_t pre[kPack + 1]; // exclusive prefix of the flag counts
+  // per pixel, loaded once by its lane: evaluation constants, differences to the base, working
+  // pixel (i, j) relative to the centre pixel, threshold, difference evaluation or not
+  EvalF ef[kPack];
+  DeltaF df[kPack];
+  float di[kPack], dj[kPack], thr[kPack];
+  int32_t pi[kPack], pj[kPack], isdiff[kPack];
   float res[kPack * kMaxGrid * kMaxGrid], dres[kPack * kMaxGrid * kMaxGrid];
   float res3[kPack * kMaxGrid * kMaxGrid], dres3[kPack * kMaxGrid * kMaxGrid];
 };
 
-// one level-2 or level-3 sub-pixel of queued pixel P (sub-pixel m, and sub-sub-pixel k >= 0 at
-// level 3): its quadrature, plain or as a difference
+// one level-2 or level-3 sub-pixel of queued pixel P of the warp's batch (sub-pixel m, and
+// sub-sub-pixel k >= 0 at level 3): its quadrature, plain or as a difference, from the pixel's
+// constants staged in shared memory
 template <int QC>
-__device__ __forceinline__ QuadResult packed_quad(const BatchArgs& b, int64_t ent, int m, int k, bool& diff,
-                                                  const StampDev*& stp, const EvalDev*& ep, int& i, int& j) {
+__device__ __forceinline__ QuadResult packed_quad(const BatchArgs& b, const PackSmem& S, int P, int m, int k) {
   const QuadTables& T = *b.tables;
-  const int slot = (int)(ent >> 62);
-  const int s = (int)((ent >> 32) & 0x3fffffff);
-  const int64_t p = ent & 0xffffffffll;
-  const StampDev& st = b.stamps[s];
-  const EvalDev& e = b.evals[s * 2 + slot];
-  stp = &st;
-  ep = &e;
-  const EvalF f = load_evalf(st, e);
-  i = (int)(p % st.wnx);
-  j = (int)(p / st.wnx);
+  const EvalF f = S.ef[P];
   const float ginv = 1.f / (float)T.gridding;
-  float ci = (float)(i - f.cix) + T.gxf[m], cj = (float)(j - f.cjy) + T.gyf[m];
+  float ci = S.di[P] + T.gxf[m], cj = S.dj[P] + T.gyf[m];
   float ig = ginv, area = ginv * ginv;
   if (k >= 0) {
     ci += T.gxf[k] * ginv;
@@ -1181,13 +1194,36 @@ __device__ __forceinline__ QuadResult packed_quad(const BatchArgs& b, int64_t en
     ig = ginv * ginv;
     area = area * area;
   }
-  diff = (e.ops & OP_DIFF) != 0;
-  if (diff) {
-    const DeltaF d = load_deltaf(e);
+  if (S.isdiff[P]) {
+    const DeltaF d = S.df[P];
     return quad_lane<false, QC, false, true>(b, f, d, ci, cj, ig, area);
   }
   const DeltaF d{};
   return quad_lane<false, QC, false, false>(b, f, d, ci, cj, ig, area);
+}
+
+// the batch's pixels: each lane P < np stages its pixel's constants
+__device__ __forceinline__ void packed_stage(const BatchArgs& b, PackSmem& S, int np, int lane) {
+  if (lane < np) {
+    const int64_t ent = S.ent[lane];
+    const int slot = (int)(ent >> 62);
+    const int s = (int)((ent >> 32) & 0x3fffffff);
+    const StampDev& st = b.stamps[s];
+    const EvalDev& e = b.evals[s * 2 + slot];
+    const EvalF f = load_evalf(st, e);
+    S.ef[lane] = f;
+    const bool diff = (e.ops & OP_DIFF) != 0;
+    S.isdiff[lane] = diff ? 1 : 0;
+    if (diff) S.df[lane] = load_deltaf(e);
+    int i, j;
+    pix_ij(ent & 0xffffffffll, st.wnx, i, j);
+    S.pi[lane] = i;
+    S.pj[lane] = j;
+    S.di[lane] = (float)(i - f.cix);
+    S.dj[lane] = (float)(j - f.cjy);
+    S.thr[lane] = e.thresh;
+  }
+  __syncwarp();
 }
 
 template <int QC>
@@ -1197,23 +1233,23 @@ __device__ void level23_packed(const BatchArgs& b, PackSmem& S, int np, int lane
   const int G2 = T.gridding * T.gridding;
   const int Q2 = QC > 0 ? QC * QC : T.quad_level * T.quad_level;
   if (lane < kPack) S.mask[lane] = 0u;
-  __syncwarp();
+  packed_stage(b, S, np, lane);
   // level 2: np * G2 sub-pixels over the lanes
   const int items = np * G2;
   for (int base = 0; base < items; base += 32) {
     const int it = base + lane;
     if (it < items) {
       const int P = it / G2, m = it - P * G2;
-      bool diff;
-      const StampDev* st;
-      const EvalDev* e;
-      int i, j;
-      const QuadResult r = packed_quad<QC>(b, S.ent[P], m, -1, diff, st, e, i, j);
-      if (diff) diff_samples += Q2;
+      const QuadResult r = packed_quad<QC>(b, S, P, m, -1);
+      if (S.isdiff[P]) diff_samples += Q2;
       S.res[it] = r.res;
       S.dres[it] = r.dres;
-      if (b.max_depth > 2 && decide<false>(b, *st, *e, r, e->thresh * (float)G2, i, j, m, n64))
-        atomicOr(&S.mask[P], 1u << m);
+      if (b.max_depth > 2) {
+        const int64_t ent = S.ent[P];
+        const int slot = (int)(ent >> 62), s = (int)((ent >> 32) & 0x3fffffff);
+        if (decide<false>(b, b.stamps[s], b.evals[s * 2 + slot], r, S.thr[P] * (float)G2, S.pi[P], S.pj[P], m, n64))
+          atomicOr(&S.mask[P], 1u << m);
+      }
     }
   }
   __syncwarp();
@@ -1246,12 +1282,8 @@ __device__ void level23_packed(const BatchArgs& b, PackSmem& S, int np, int lane
         const int q = it / G2, k = it - q * G2;
         int P, m;
         flagged(f0 + q, P, m);
-        bool diff;
-        const StampDev* st;
-        const EvalDev* e;
-        int i, j;
-        const QuadResult r = packed_quad<QC>(b, S.ent[P], m, k, diff, st, e, i, j);
-        if (diff) diff_samples += Q2;
+        const QuadResult r = packed_quad<QC>(b, S, P, m, k);
+        if (S.isdiff[P]) diff_samples += Q2;
         S.res3[it] = r.res;
         S.dres3[it] = r.dres;
       }

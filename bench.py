@@ -825,9 +825,9 @@ def run_gpu_learned(args):
         "peak": fp32_peak,
         "unit": "TFLOP/s",
         "frac": achieved / fp32_peak if achieved else None,
-        # DRAM bytes per launch from an ncu capture of two LM-round launches of the 4096-stamp
-        # case (27.6 MB each on average, nearly all reads), scaled by the stamps per launch
-        "traffic": 27.6e6 * S / 4096,
+        # DRAM bytes per launch from an ncu capture of three LM-round launches of the 4096-stamp
+        # case (30.3 MB each on average, reads + writes), scaled by the stamps per launch
+        "traffic": 30.3e6 * S / 4096,
         "traffic_unit": "bytes per launch (ncu, 4096-stamp capture scaled by stamps)",
         "launches": conv_n,
         "avg_launch_ms": conv_ms / max(conv_n, 1),
