@@ -97,6 +97,7 @@ struct ap_batch {
   QuadTables tables{};
   int64_t out_pixels = 0, psf_pixels = 0, work_pixels = 0, spsf_total = 0;
   int32_t max_kp2 = 0;
+  bool conv_large = false;  // k_conv's large flavour and its tile height
   size_t conv_smem = 0;
   std::vector<int32_t> fft_lists;  // stamp list, then the row / column-group / output-row prefixes
   int64_t fft_buf_elems = 0, preconv_elems = 0;
@@ -190,6 +191,15 @@ int ap_batch_create(ap_batch** out, int32_t n, const int32_t* nx, const int32_t*
   const bool stencil = options->integrate_mode == AP_INTEGRATE_THRESHOLD &&
                        (options->sampling_mode == AP_SAMPLING_MIDPOINT ||
                         options->sampling_mode == AP_SAMPLING_TRAPEZOID);
+  // k_conv's flavour (and with it the output tile height) for the whole batch: the large one
+  // when some kernel is not covered by the register-blocked sizes
+  bool large = false;
+  if (psf) {
+    const bool shift = options->psf_mode == AP_PSF_FULL;
+    for (int s = 0; s < n; ++s)
+      if (conv_kernel_large(shift ? psf_kx[s] + 2 : psf_kx[s], shift ? psf_ky[s] + 2 : psf_ky[s])) large = true;
+  }
+  b->conv_large = large;
   for (int s = 0; s < n; ++s) {
     StampDev& st = b->stamps[s];
     std::memset(&st, 0, sizeof(st));
@@ -253,7 +263,7 @@ int ap_batch_create(ap_batch** out, int32_t n, const int32_t* nx, const int32_t*
     st.ntw_x = (st.wnx + kTile - 1) / kTile;
     st.ntw = st.ntw_x * ((st.wny + kTile - 1) / kTile);
     st.nto_x = (st.nx + kOutTileX - 1) / kOutTileX;
-    st.nto = st.nto_x * ((st.ny + kOutTileY - 1) / kOutTileY);
+    st.nto = st.nto_x * ((st.ny + conv_tile_y(large) - 1) / conv_tile_y(large));
     st.tile_w0 = tw;
     st.tile_o0 = to;
     if ((int64_t)tw + st.ntw > (int64_t)INT32_MAX / 2 || (int64_t)to + st.nto > (int64_t)INT32_MAX / 2) {
@@ -283,7 +293,7 @@ int ap_batch_create(ap_batch** out, int32_t n, const int32_t* nx, const int32_t*
       }
     }
     if (psf && st.fft_nx == 0) {
-      const size_t need = conv_smem_bytes(st.kpx, st.kpy);
+      const size_t need = conv_smem_bytes(st.kpx, st.kpy, large);
       smem = std::max(smem, need);
     }
     if ((int64_t)st.wnx * st.wny >= (int64_t)1 << 31) {
@@ -432,9 +442,7 @@ int ap_batch_create(ap_batch** out, int32_t n, const int32_t* nx, const int32_t*
   A.n_work_tiles = (int32_t)b->work_tiles.size();
   A.n_out_tiles = (int32_t)b->out_tiles.size();
   A.max_kp2 = b->max_kp2;
-  A.conv_large = 0;
-  for (const StampDev& st : b->stamps)
-    if (st.kpx != st.kpy || st.kpx > 29) A.conv_large = 1;
+  A.conv_large = b->conv_large ? 1 : 0;
   A.tolerance = (float)options->sampling_tolerance;
   A.tolerance64 = options->sampling_tolerance;
   A.softening64 = options->softening;

@@ -28,7 +28,15 @@ constexpr int kTile = 16;     // 16 x 16 working-pixel tiles (sampling / selecti
 constexpr int kOutTileX = 32; // output tiles of the convolve/accumulate pass: 32 x 32 pixels,
 constexpr int kOutTileY = 32; // 128 threads, each thread 8 consecutive rows of one column
 constexpr int kConvRows = 8;
+// Batches with a kernel the register-blocked sizes do not cover (k_conv's large flavour) use
+// 32 x 16 tiles with 4 rows per thread: their kernels and input tiles fill most of an SM's shared
+// memory, and shorter tiles keep each block's share of it and of the work small.
+constexpr int kOutTileYL = 16;
+constexpr int kConvRowsL = 4;
 constexpr int kConvThreads = kOutTileX * kOutTileY / kConvRows;
+static_assert(kOutTileX * kOutTileYL / kConvRowsL == kConvThreads, "both flavours use 128 threads");
+__host__ __device__ constexpr int conv_tile_y(bool large) { return large ? kOutTileYL : kOutTileY; }
+__host__ __device__ constexpr int conv_rows(bool large) { return large ? kConvRowsL : kConvRows; }
 constexpr int kConvMaxKP = 29; // square kernels up to this size use the register-blocked path
 constexpr int kNumPlanes = 7; // deep + 6 partial planes
 constexpr int kNacc = 56;     // per (stamp, slot) accumulator doubles
@@ -270,17 +278,19 @@ __host__ __device__ inline int conv_col_stride(int kpy) { return (kpy + 3) & ~3;
 // Row pitch of the column-major input tile: at least its kOutTileY + kpy - 1 rows plus the
 // 2 rows that the last float4 of a column may overrun, and 4 mod 8 so that the 8 lanes of a
 // quarter-warp read 16-byte slots in 8 different bank groups
-__host__ __device__ inline int conv_tile_pitch(int kpy) {
-  const int th = kOutTileY + kpy - 1 + 2;
+__host__ __device__ inline int conv_tile_pitch(int kpy, bool large) {
+  const int th = conv_tile_y(large) + kpy - 1 + 2;
   return th + ((4 - th % 8) + 8) % 8;
 }
 
 // floats after the second tile: the chunked convolution of large kernels reads up to 3 past it
 constexpr int kConvSmemPad = 16;
-__host__ __device__ inline size_t conv_smem_bytes(int kpx, int kpy) {
+__host__ __device__ inline size_t conv_smem_bytes(int kpx, int kpy, bool large) {
   return sizeof(float) * (3 * (size_t)kpx * conv_col_stride(kpy) +
-                          2 * (size_t)(kOutTileX + kpx - 1) * conv_tile_pitch(kpy) + kConvSmemPad);
+                          2 * (size_t)(kOutTileX + kpx - 1) * conv_tile_pitch(kpy, large) + kConvSmemPad);
 }
+// k_conv's large flavour: a kernel that is not a square of side 3..kConvMaxKP
+__host__ __device__ inline bool conv_kernel_large(int kpx, int kpy) { return kpx != kpy || kpx > kConvMaxKP; }
 
 __host__ __device__ inline int64_t work_plane(const BatchArgs& b, int slot, int plane) {
   return ((int64_t)slot * kNumPlanes + plane) * b.work_pixels;

@@ -1426,21 +1426,21 @@ __device__ __forceinline__ void conv_tile_reduce(const float* vals, int nvals, d
   }
 }
 
-// One column x kConvRows rows of a KP x KP convolution, register blocked: for each kernel
+// One column x R rows of a KP x KP convolution, register blocked: for each kernel
 // column u the kernel column (float4 loads of the transposed kernel) and the input column
 // window live in registers.  out[o] = sum_{v,u} K[v][u] T[ty0 + o + KP-1 - v][tx + KP-1 - u],
 // with KT[u * stride + v] = K[v][u].
-template <int KP>
+template <int KP, int R>
 __device__ __forceinline__ void conv_col_fixed(const float* __restrict__ Tt, int TP,
                                                const float* __restrict__ KT, int tx, int ty0,
                                                float* out) {
   constexpr int C2 = KP - 1;
-  constexpr int NT = kConvRows + KP - 1;
+  constexpr int NT = R + KP - 1;
   constexpr int KS = (KP + 3) & ~3;
   constexpr int NT4 = (NT + 3) / 4;
-  float acc[kConvRows];
+  float acc[R];
 #pragma unroll
-  for (int o = 0; o < kConvRows; ++o) acc[o] = 0.f;
+  for (int o = 0; o < R; ++o) acc[o] = 0.f;
   // column-major tile (pitch TP): a thread's input column is contiguous, read as float4
   const float* base = Tt + (tx + C2) * TP + ty0;
 #pragma unroll 1
@@ -1468,18 +1468,19 @@ __device__ __forceinline__ void conv_col_fixed(const float* __restrict__ Tt, int
 #pragma unroll
     for (int v = 0; v < KP; ++v)
 #pragma unroll
-      for (int o = 0; o < kConvRows; ++o) acc[o] = fmaf(kc[v], t[o + C2 - v], acc[o]);
+      for (int o = 0; o < R; ++o) acc[o] = fmaf(kc[v], t[o + C2 - v], acc[o]);
   }
 #pragma unroll
-  for (int o = 0; o < kConvRows; ++o) out[o] = acc[o];
+  for (int o = 0; o < R; ++o) out[o] = acc[o];
 }
 
+template <int R>
 __device__ __forceinline__ void conv_col_generic(const float* __restrict__ Tt, int TP,
                                                  const float* __restrict__ KT, int kpx, int kpy,
                                                  int tx, int ty0, float* out) {
-  float acc[kConvRows];
+  float acc[R];
 #pragma unroll
-  for (int o = 0; o < kConvRows; ++o) acc[o] = 0.f;
+  for (int o = 0; o < R; ++o) acc[o] = 0.f;
   const int ks = conv_col_stride(kpy);
   for (int u = 0; u < kpx; ++u) {
     const float* kcol = KT + u * ks;
@@ -1488,28 +1489,27 @@ __device__ __forceinline__ void conv_col_generic(const float* __restrict__ Tt, i
       const float k = kcol[v];
       const float* tp = tcol + (kpy - 1 - v);
 #pragma unroll
-      for (int o = 0; o < kConvRows; ++o) acc[o] = fmaf(k, tp[o], acc[o]);
+      for (int o = 0; o < R; ++o) acc[o] = fmaf(k, tp[o], acc[o]);
     }
   }
 #pragma unroll
-  for (int o = 0; o < kConvRows; ++o) out[o] = acc[o];
+  for (int o = 0; o < R; ++o) out[o] = acc[o];
 }
 
 // Kernels the fixed instances do not cover (kpy >= 8): each kernel column in chunks of 8 rows,
 // the chunk (two float4 loads) and the input window it meets (four float4 loads) in registers,
 // 32 FMAs per chunk.  With lo = kpy - 1 - v0 - 7 the first input row of chunk v0, lo mod 4 =
-// kpy mod 4 = SH, so the window (kChunkWin floats) is read from the 16-byte aligned row lo - SH
+// kpy mod 4 = SH, so the window (kWin floats) is read from the 16-byte aligned row lo - SH
 // (the tile pitch and ty0 are multiples of 4).  It may reach up to 10 floats before the column
 // (inside the kernels stored ahead of the tile: 3 kpx ks >= 24 floats) and 3 past the last
 // column (the allocation is padded by kConvSmemPad floats); rows of the chunk at or beyond kpy
 // are skipped.
-constexpr int kChunkWin = (kConvRows + 10 + 3) / 4 * 4;  // window rows SH .. SH + 7 + kConvRows - 1
-template <int SH>
+template <int SH, int R>
 __device__ __forceinline__ void conv_col_chunked(const float* __restrict__ Tt, int TP, const float* __restrict__ KT,
                                                  int kpx, int kpy, int tx, int ty0, float* out) {
-  float acc[kConvRows];
+  float acc[R];
 #pragma unroll
-  for (int o = 0; o < kConvRows; ++o) acc[o] = 0.f;
+  for (int o = 0; o < R; ++o) acc[o] = 0.f;
   const int ks = conv_col_stride(kpy);
   for (int u = 0; u < kpx; ++u) {
     const float* kcol = KT + u * ks;
@@ -1525,9 +1525,10 @@ __device__ __forceinline__ void conv_col_chunked(const float* __restrict__ Tt, i
         kc[4 * q + 3] = k4.w;
       }
       const float4* w4 = reinterpret_cast<const float4*>(tcol + (kpy - 8 - v0) - SH);
-      float t[kChunkWin];
+      constexpr int kWin = (R + 10 + 3) / 4 * 4;  // window rows SH .. SH + 7 + R - 1
+      float t[kWin];
 #pragma unroll
-      for (int q = 0; q < kChunkWin / 4; ++q) {
+      for (int q = 0; q < kWin / 4; ++q) {
         const float4 c4 = w4[q];
         t[4 * q + 0] = c4.x;
         t[4 * q + 1] = c4.y;
@@ -1539,13 +1540,13 @@ __device__ __forceinline__ void conv_col_chunked(const float* __restrict__ Tt, i
       for (int j = 0; j < 8; ++j) {
         if (j < nv) {
 #pragma unroll
-          for (int o = 0; o < kConvRows; ++o) acc[o] = fmaf(kc[j], t[SH + 7 - j + o], acc[o]);
+          for (int o = 0; o < R; ++o) acc[o] = fmaf(kc[j], t[SH + 7 - j + o], acc[o]);
         }
       }
     }
   }
 #pragma unroll
-  for (int o = 0; o < kConvRows; ++o) out[o] = acc[o];
+  for (int o = 0; o < R; ++o) out[o] = acc[o];
 }
 
 // One copy of the kernel-size instances per k_conv flavour, shared by its k_conv<NF, LARGE>
@@ -1560,27 +1561,27 @@ __device__ __noinline__ void conv_col(const float* Tt, int TP, const float* KT, 
     if (kpy >= 8) {
       switch (kpy & 3) {
         case 0:
-          conv_col_chunked<0>(Tt, TP, KT, kpx, kpy, tx, ty0, out);
+          conv_col_chunked<0, kConvRowsL>(Tt, TP, KT, kpx, kpy, tx, ty0, out);
           return;
         case 1:
-          conv_col_chunked<1>(Tt, TP, KT, kpx, kpy, tx, ty0, out);
+          conv_col_chunked<1, kConvRowsL>(Tt, TP, KT, kpx, kpy, tx, ty0, out);
           return;
         case 2:
-          conv_col_chunked<2>(Tt, TP, KT, kpx, kpy, tx, ty0, out);
+          conv_col_chunked<2, kConvRowsL>(Tt, TP, KT, kpx, kpy, tx, ty0, out);
           return;
         default:
-          conv_col_chunked<3>(Tt, TP, KT, kpx, kpy, tx, ty0, out);
+          conv_col_chunked<3, kConvRowsL>(Tt, TP, KT, kpx, kpy, tx, ty0, out);
           return;
       }
     }
-    conv_col_generic(Tt, TP, KT, kpx, kpy, tx, ty0, out);
+    conv_col_generic<kConvRowsL>(Tt, TP, KT, kpx, kpy, tx, ty0, out);
     return;
   }
   if (kpx == kpy) {
     switch (kpx) {
 #define AP_CONV_CASE(K) \
   case K:               \
-    conv_col_fixed<K>(Tt, TP, KT, tx, ty0, out); \
+    conv_col_fixed<K, kConvRows>(Tt, TP, KT, tx, ty0, out); \
     return;
       AP_CONV_CASE(3) AP_CONV_CASE(5) AP_CONV_CASE(7) AP_CONV_CASE(9) AP_CONV_CASE(11)
       AP_CONV_CASE(13) AP_CONV_CASE(15) AP_CONV_CASE(17) AP_CONV_CASE(19) AP_CONV_CASE(21)
@@ -1590,7 +1591,7 @@ __device__ __noinline__ void conv_col(const float* Tt, int TP, const float* KT, 
         break;
     }
   }
-  conv_col_generic(Tt, TP, KT, kpx, kpy, tx, ty0, out);
+  conv_col_generic<kConvRows>(Tt, TP, KT, kpx, kpy, tx, ty0, out);
 }
 
 // Convolve/accumulate pass.  NF = number of fitted parameters (compile time, so the
@@ -1603,8 +1604,9 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
   const StampDev& st = b.stamps[s];
   double* tacc = b.tile_acc + ((int64_t)(st.tile_o0 + local) * 2 + slot) * kNacc;
   const int tx = threadIdx.x & 31, tg = threadIdx.x >> 5;
-  const int x0 = (local % st.nto_x) * kOutTileX, y0 = (local / st.nto_x) * kOutTileY;
-  const int x = x0 + tx, yb = y0 + tg * kConvRows;
+  constexpr int kRows = conv_rows(LARGE), kTileY = conv_tile_y(LARGE);
+  const int x0 = (local % st.nto_x) * kOutTileX, y0 = (local / st.nto_x) * kTileY;
+  const int x = x0 + tx, yb = y0 + tg * kRows;
   const bool jac = (ops & OP_JAC) != 0;
   const bool diff = (ops & OP_DIFF) != 0;  // (forward only: no Jacobian planes)
   const bool shiftmode = (b.psf_mode == AP_PSF_FULL);
@@ -1616,7 +1618,7 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
   {
     const bool fit = (ops & (OP_CHI2 | OP_HG | OP_RPP)) != 0 && !(ops & OP_VJP);
     const int npf = fit ? 2 + ((diff || (ops & OP_RPP)) ? 1 : 0) + ((ops & OP_RPP) ? NF : 0) : 0;
-    const int rows = min(kOutTileY, st.ny - y0), w = min(kOutTileX, st.nx - x0);
+    const int rows = min(kTileY, st.ny - y0), w = min(kOutTileX, st.nx - x0);
     for (int k = threadIdx.x; k < npf * rows; k += blockDim.x) {
       const int pl = k / rows, r = k - pl * rows;
       const int64_t op = st.out_off + (int64_t)(y0 + r) * st.nx + x0;
@@ -1632,15 +1634,15 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
   }
 
   // conv results per row: [0] model, [1] d/dshift_x, [2] d/dshift_y, [3 + q] partial plane q
-  float cv[3 + NGRAD][kConvRows];
+  float cv[3 + NGRAD][kRows];
 #pragma unroll
   for (int k = 0; k < 3 + NGRAD; ++k)
 #pragma unroll
-    for (int o = 0; o < kConvRows; ++o) cv[k][o] = 0.f;
+    for (int o = 0; o < kRows; ++o) cv[k][o] = 0.f;
 
   if (b.psf_mode == AP_PSF_NONE) {
 #pragma unroll
-    for (int o = 0; o < kConvRows; ++o) {
+    for (int o = 0; o < kRows; ++o) {
       const int y = yb + o;
       if (x < st.nx && y < st.ny) {
         const int64_t wp = st.work_off + (int64_t)y * st.wnx + x;
@@ -1656,7 +1658,7 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
     const int64_t npix = (int64_t)st.nx * st.ny;
     const float* pre = b.preconv + st.pre_off + (int64_t)slot * (3 + NGRAD) * npix;
 #pragma unroll
-    for (int o = 0; o < kConvRows; ++o) {
+    for (int o = 0; o < kRows; ++o) {
       const int y = yb + o;
       if (!(x < st.nx && y < st.ny)) continue;
       const int64_t i = (int64_t)y * st.nx + x;
@@ -1677,7 +1679,7 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
   } else {
     const int kpx = st.kpx, kpy = st.kpy, ks = conv_col_stride(kpy), kstride = kpx * ks;
     const int cx = (kpx - 1) / 2, cy = (kpy - 1) / 2;
-    const int TW = kOutTileX + kpx - 1, TH = kOutTileY + kpy - 1, TP = conv_tile_pitch(kpy);
+    const int TW = kOutTileX + kpx - 1, TH = kTileY + kpy - 1, TP = conv_tile_pitch(kpy, LARGE);
     float* KT = smem;                // up to 3 kernels, transposed
     float* Tt = smem + 3 * kstride;  // input tile
     const int kp2 = kpx * kpy;
@@ -1737,12 +1739,12 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
       const int pl = cur;
       const int nkp = (diff || pl > 0) ? 1 : nk;
       for (int kk = 0; kk < nkp; ++kk) {
-        float outv[kConvRows];
+        float outv[kRows];
         const int kidx = diff ? pl : kk;
-        conv_col<LARGE>(Tt + (bi ? tsz : 0), TP, KT + kidx * kstride, kpx, kpy, tx, tg * kConvRows, outv);
+        conv_col<LARGE>(Tt + (bi ? tsz : 0), TP, KT + kidx * kstride, kpx, kpy, tx, tg * kRows, outv);
         const int dst = diff ? pl : ((pl == 0) ? kk : 3 + (pl - 1));
 #pragma unroll
-        for (int o = 0; o < kConvRows; ++o) cv[dst][o] = outv[o];
+        for (int o = 0; o < kRows; ++o) cv[dst][o] = outv[o];
       }
       __syncthreads();  // buffer bi is refilled by the next iteration's prefetch
       cur = nxt;
@@ -1769,7 +1771,7 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
   }
 
 #pragma unroll
-  for (int o = 0; o < kConvRows; ++o) {
+  for (int o = 0; o < kRows; ++o) {
     const int y = yb + o;
     if (!(x < st.nx && y < st.ny)) continue;
     // (difference evaluations: mgal is the galaxy's difference, m the model's)
@@ -1872,8 +1874,10 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
   conv_tile_reduce(vals, nv, tacc, shred);
 }
 
+// fixed sizes: 6 blocks per SM (80 registers); the large flavour is held to 1-2 blocks by its
+// shared memory anyway, so its registers are not capped
 template <int NF, bool LARGE>
-__global__ void __launch_bounds__(kConvThreads, 5) k_conv(BatchArgs b, ConvIO io) {
+__global__ void __launch_bounds__(kConvThreads, LARGE ? 2 : 6) k_conv(BatchArgs b, ConvIO io) {
   extern __shared__ __align__(16) float smem[];
   __shared__ float shred[kConvWarps * kNacc];
   __shared__ uint32_t next;
@@ -1921,10 +1925,11 @@ __global__ void __launch_bounds__(kConvThreads) k_chi2(BatchArgs b, ConvIO io, c
   const int s = b.out_tiles[tile];
   const StampDev& st = b.stamps[s];
   const int local = tile - st.tile_o0;
+  const int rows = conv_rows(b.conv_large != 0);
   const int x = (local % st.nto_x) * kOutTileX + (threadIdx.x & 31);
-  const int yb = (local / st.nto_x) * kOutTileY + (threadIdx.x >> 5) * kConvRows;
+  const int yb = (local / st.nto_x) * conv_tile_y(b.conv_large != 0) + (threadIdx.x >> 5) * rows;
   float v = 0.f;
-  for (int o = 0; o < kConvRows; ++o) {
+  for (int o = 0; o < rows; ++o) {
     const int y = yb + o;
     if (x < st.nx && y < st.ny) {
       const int64_t op = st.out_off + (int64_t)y * st.nx + x;

@@ -207,7 +207,8 @@ extern "C" int ap_render_noalloc(int32_t nx, int32_t ny, int32_t psf_kx, int32_t
   st.ntw_x = (st.wnx + kTile - 1) / kTile;
   st.ntw = st.ntw_x * ((st.wny + kTile - 1) / kTile);
   st.nto_x = (nx + kOutTileX - 1) / kOutTileX;
-  st.nto = st.nto_x * ((ny + kOutTileY - 1) / kOutTileY);
+  const bool large = with_psf && conv_kernel_large(st.kpx, st.kpy);
+  st.nto = st.nto_x * ((ny + conv_tile_y(large) - 1) / conv_tile_y(large));
   const int64_t wp = (int64_t)st.wnx * st.wny;
   const int64_t kp2 = (int64_t)st.kpx * st.kpy;
 
@@ -286,7 +287,7 @@ extern "C" int ap_render_noalloc(int32_t nx, int32_t ny, int32_t psf_kx, int32_t
   if (o > (int64_t)kScratchBytes) return AP_ERR_WORKSPACE;
   size_t conv_smem = 0;
   if (with_psf)
-    conv_smem = conv_smem_bytes(st.kpx, st.kpy);
+    conv_smem = conv_smem_bytes(st.kpx, st.kpy, large);
   if (conv_smem > 200 * 1024) return AP_ERR_UNSUPPORTED;
 
   // ---- device address of the scratch, once per device ----------------------------------------
@@ -321,7 +322,7 @@ extern "C" int ap_render_noalloc(int32_t nx, int32_t ny, int32_t psf_kx, int32_t
   A.n_work_tiles = st.ntw;
   A.n_out_tiles = st.nto;
   A.max_kp2 = (int32_t)kp2;
-  A.conv_large = (st.kpx != st.kpy || st.kpx > 29) ? 1 : 0;
+  A.conv_large = large ? 1 : 0;
   A.tolerance = (float)options->sampling_tolerance;
   A.tolerance64 = options->sampling_tolerance;
   A.softening64 = options->softening;
