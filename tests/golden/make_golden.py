@@ -8,6 +8,7 @@ Run with ``ASTROPHOT_REFERENCE=<path of the reference checkout>`` set:
     python tests/golden/make_golden.py segmap   # only the segmentation-map case
     python tests/golden/make_golden.py auxpsf   # only the live-PSF-model case
     python tests/golden/make_golden.py center   # only the centre-supersampling cases
+    python tests/golden/make_golden.py psfstamps  # only the Moffat / Gaussian PSF stamps
 
 The reference (AstroPhot 0.x) is imported through a ``sys.modules`` shim for
 the optional packages it imports at module level but never calls on this
@@ -817,9 +818,35 @@ def run_auxpsf_group_case(ap, key, case):
                 spec=json.dumps(case))
 
 
+# the reference's PSF stamp builders (utils/initialize/construct_psf.py): Moffat (n, Rd, width,
+# pixel scale) and Gaussian (sigma, width, pixel scale), 4 x 4 super-sampled and normalised
+PSF_STAMP_CASES = {
+    "moffat": [(3.5, 1.2, 9, 1.0), (3.5, 2.6, 21, 1.0), (2.5, 1.7, 25, 0.8), (4.8, 3.1, 15, 1.3)],
+    "gaussian": [(1.0, 9, 1.0), (2.0, 51, 1.0), (1.4, 15, 0.8)],
+}
+
+
+def run_psf_stamps(ap):
+    from astrophot.utils.initialize.construct_psf import gaussian_psf, moffat_psf
+
+    out = {}
+    for k, (n, rd, w, sc) in enumerate(PSF_STAMP_CASES["moffat"]):
+        out[f"moffat_{k}_args"] = np.array([n, rd, w, sc])
+        out[f"moffat_{k}"] = np.asarray(moffat_psf(n, rd, w, sc), dtype=np.float64)
+    for k, (sig, w, sc) in enumerate(PSF_STAMP_CASES["gaussian"]):
+        out[f"gaussian_{k}_args"] = np.array([sig, w, sc])
+        out[f"gaussian_{k}"] = np.asarray(gaussian_psf(sig, w, sc), dtype=np.float64)
+    return out
+
+
 def main():
     ap = import_reference()
     only = sys.argv[1] if len(sys.argv) > 1 else None
+    if only == "psfstamps":
+        out = run_psf_stamps(ap)
+        np.savez_compressed(os.path.join(HERE, "psf_stamps.npz"), **out)
+        print("psf stamps", sorted(k for k in out if not k.endswith("_args")))
+        return
     if only == "center":
         for key in ("sersic_psf_center", "sersic_nopsf_center"):
             out = run_render_case(ap, key, RENDER_CASES[key])

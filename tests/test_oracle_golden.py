@@ -4,6 +4,7 @@ tests (``tests/test_utils.py:16-38`` FFT convolution vs scipy, ``:344-435`` Sers
 closed forms, ``tests/test_model.py:49-74`` representation round trip)."""
 
 import math
+import os
 
 import numpy as np
 import pytest
@@ -373,3 +374,26 @@ def test_iter_lm_first_sweep_matches_reference(name):
     assert it.ndf == int(d["ndf"])
     assert np.isclose(it.loss_history[0], d["loss_history"][0], rtol=1e-10, atol=0)
     assert np.allclose(it.lambda_history[0], d["lambda_history"][0], rtol=1e-8, atol=1e-10)
+
+
+def test_psf_stamps_match_reference_builders():
+    """The Moffat and Gaussian PSF stamps this library builds for its fixtures and synthetic
+    workloads equal the reference's own builders (utils/initialize/construct_psf.py:8-65, recorded
+    by tests/golden/make_golden.py psfstamps): same 4 x 4 super-sampling grid and normalisation."""
+    from astrophot_gb300 import synthetic
+
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "psf_stamps.npz"))
+    k = 0
+    while f"moffat_{k}" in d:
+        n, rd, w, sc = d[f"moffat_{k}_args"]
+        got = synthetic.moffat_stamp(float(n), float(rd), int(w), float(sc))
+        np.testing.assert_allclose(got, d[f"moffat_{k}"], rtol=1e-12, atol=1e-15)
+        k += 1
+    assert k == 4
+    k = 0
+    while f"gaussian_{k}" in d:
+        sig, w, sc = d[f"gaussian_{k}_args"]
+        got = synthetic.gaussian_stamp(float(sig), int(w), float(sc))
+        np.testing.assert_allclose(got, d[f"gaussian_{k}"], rtol=1e-12, atol=1e-15)
+        k += 1
+    assert k == 3
