@@ -797,6 +797,156 @@ __global__ void __launch_bounds__(256) k_recheck(BatchArgs b) {
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&b.counters[2], n);
 }
 
+// Sampling and threshold selection in one pass, for Sersic batches with a stencil sampling mode
+// (midpoint / trapezoid), whose integration threshold (the closed-form flux) is known before
+// sampling.  A 16 x 16 working tile samples its pixels as k_sample does (value, partials, the
+// base / difference planes; not the reference sub-sample and error-bound planes, which only the
+// selection reads) and, for the Laplacian stencil, the ring of pixels around it (value and FP32
+// error bound only), into shared memory; it then decides its own pixels from there with
+// select_tile's arithmetic and enqueue.  Every ring value is computed by the same sample
+// functions as the pixel's own tile computes it, within the same FP32 error bound, and the
+// decisions inside that bound are taken in float64 by k_recheck as before.
+__device__ __forceinline__ void enqueue_selection(const BatchArgs& b, bool sel, bool redecided, int64_t entry) {
+  const int lane = threadIdx.x & 31;
+  const unsigned mask = __ballot_sync(0xffffffffu, sel);
+  if (mask) {
+    const int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(&b.counters[0], (unsigned)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (sel) {
+      const uint32_t q = base + __popc(mask & ((1u << lane) - 1u));
+      if ((int64_t)q < 2 * b.work_pixels)
+        b.queue[q] = entry;
+      else
+        atomicOr(&b.counters[3], 1u);
+    }
+  }
+  const unsigned rmask = __ballot_sync(0xffffffffu, redecided);
+  if (rmask) {
+    const int leader = __ffs(rmask) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(&b.counters[5], (unsigned)__popc(rmask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (redecided) {
+      const uint32_t q = base + __popc(rmask & ((1u << lane) - 1u));
+      if ((int64_t)q < 2 * b.work_pixels)
+        b.recheck[q] = entry;
+      else
+        atomicOr(&b.counters[3], 2u);
+    }
+  }
+}
+
+template <bool JAC, bool DIFF>
+__device__ __forceinline__ void sample_select_tile(const BatchArgs& b, const EvalF& e, const DeltaF& d, int ops,
+                                                   int s, int slot, int tile_local, float (*sd)[kTile + 2],
+                                                   float (*se)[kTile + 2]) {
+  const StampDev& st = b.stamps[s];
+  const int tx = threadIdx.x & (kTile - 1), ty = threadIdx.x / kTile;
+  const int i0 = (tile_local % st.ntw_x) * kTile, j0 = (tile_local / st.ntw_x) * kTile;
+  const int i = i0 + tx, j = j0 + ty;
+  const bool valid = (i < st.wnx) && (j < st.wny);
+  if (valid) {
+    float deep, g[NGRAD], refsub, errb, ddeep;
+    sample_pixel<JAC, false, DIFF>(b, e, d, i, j, false, deep, g, refsub, errb, ddeep);
+    const int64_t p = st.work_off + (int64_t)j * st.wnx + i;
+    b.work[work_plane(b, slot, 0) + p] = deep;
+    if (JAC) {
+#pragma unroll
+      for (int q = 0; q < NGRAD; ++q) b.work[work_plane(b, slot, 1 + q) + p] = g[q];
+    }
+    if (ops & (OP_DIFF | OP_BASE)) write_diff_base(b, ops, slot, p, deep, ddeep, 0u);
+    sd[ty + 1][tx + 1] = deep;
+    se[ty + 1][tx + 1] = errb;
+  }
+  // the ring around the tile: rows lj = 0 and kTile + 1 (li = 0 .. kTile + 1), then columns
+  // li = 0 and kTile + 1 (lj = 1 .. kTile); one point per thread
+  if (threadIdx.x < 4 * kTile + 4) {
+    const int r = threadIdx.x;
+    int li, lj;
+    if (r < kTile + 2) {
+      li = r;
+      lj = 0;
+    } else if (r < 2 * (kTile + 2)) {
+      li = r - (kTile + 2);
+      lj = kTile + 1;
+    } else if (r < 2 * (kTile + 2) + kTile) {
+      li = 0;
+      lj = 1 + r - 2 * (kTile + 2);
+    } else {
+      li = kTile + 1;
+      lj = 1 + r - 2 * (kTile + 2) - kTile;
+    }
+    const int gi = i0 - 1 + li, gj = j0 - 1 + lj;
+    if (gi >= 0 && gi < st.wnx && gj >= 0 && gj < st.wny) {
+      float deep, g[NGRAD], refsub, errb, ddeep;
+      sample_pixel<false, false, DIFF>(b, e, d, gi, gj, false, deep, g, refsub, errb, ddeep);
+      sd[lj][li] = deep;
+      se[lj][li] = errb;
+    }
+  }
+  __syncthreads();
+  bool sel = false, redecided = false;
+  int64_t pp = 0;
+  if (valid) {
+    const EvalDev& ed = b.evals[s * 2 + slot];
+    float thr, thr_err;
+    double thr64;
+    stamp_threshold(b, st, ed, s, slot, thr, thr64, thr_err);
+    pp = (int64_t)j * st.wnx + i;
+    const float deep = sd[ty + 1][tx + 1];
+    // Laplacian 3x3 'valid' then replicate pad (models/_model_methods.py:87-98)
+    const int ic = min(max(i, 1), st.wnx - 2), jc = min(max(j, 1), st.wny - 2);
+    const int lc = ic - i0 + 1, lr = jc - j0 + 1;
+    const float u = sd[lr - 1][lc], l = sd[lr][lc - 1], m = sd[lr][lc], r = sd[lr][lc + 1], dn = sd[lr + 1][lc];
+    const float lap = u + l + (-4.f) * m + r + dn;
+    const float refimg = deep + lap;
+    const float err = fabsf(deep - refimg);
+    const float mag = fabsf(u) + fabsf(l) + 4.f * fabsf(m) + fabsf(r) + fabsf(dn);
+    float bound = se[lr - 1][lc] + se[lr][lc - 1] + 4.f * se[lr][lc] + se[lr][lc + 1] + se[lr + 1][lc] +
+                  se[ty + 1][tx + 1] + 8.f * kEps * mag + 4.f * kEps * (fabsf(deep) + fabsf(refimg));
+    bound = 1.5f * bound + thr_err;
+    if (err > thr + bound) {
+      sel = true;
+    } else if (err >= thr - bound) {
+      redecided = true;  // too close to call in FP32: k_recheck decides from float64 samples
+    }
+  }
+  enqueue_selection(b, sel, redecided, ((int64_t)slot << 62) | ((int64_t)s << 32) | pp);
+  __syncthreads();  // sd / se reuse by the next tile
+}
+
+__global__ void __launch_bounds__(256) k_sample_select(BatchArgs b) {
+  __shared__ float sd[kTile + 2][kTile + 2], se[kTile + 2][kTile + 2];
+  const uint32_t n = b.counters[7];
+  uint32_t c0, c1;
+  tile_chunk(n, c0, c1);
+  int cur = -1, ops = 0;
+  EvalF e{};
+  DeltaF d{};
+  int64_t next = (c0 < c1) ? b.wlist[c0] : 0;
+  for (uint32_t it = c0; it < c1; ++it) {
+    const int64_t ent = next;
+    if (it + 1 < c1) next = b.wlist[it + 1];
+    int slot, s, local;
+    unpack_entry(ent, slot, s, local);
+    if (s * 2 + slot != cur) {
+      cur = s * 2 + slot;
+      const EvalDev& ed = b.evals[cur];
+      e = load_evalf(b.stamps[s], ed);
+      ops = ed.ops;
+      if (ops & OP_DIFF) d = load_deltaf(ed);
+    }
+    if (ops & OP_JAC)
+      sample_select_tile<true, false>(b, e, d, ops, s, slot, local, sd, se);
+    else if (ops & OP_DIFF)
+      sample_select_tile<false, true>(b, e, d, ops, s, slot, local, sd, se);
+    else
+      sample_select_tile<false, false>(b, e, d, ops, s, slot, local, sd, se);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // adaptive integration of the queued pixels (grid_integrate, max depth <= 3)
 // ---------------------------------------------------------------------------
@@ -2039,7 +2189,12 @@ cudaError_t launch_render_pass(const BatchArgs& b, const ConvIO& io, size_t conv
   // PSF-model profiles take the kernels compiled with them; galaxies the Sersic/exponential ones
   const bool ext = b.kind == AP_PROFILE_MOFFAT || b.kind == AP_PROFILE_GAUSSIAN;
   const unsigned sgrid = grid(2 * (int64_t)b.n_work_tiles, knob(GK_SAMPLE, 8));
-  if (ext)
+  // Sersic with a stencil sampling mode and threshold integration: sampling and selection fused
+  const bool fused = b.kind == AP_PROFILE_SERSIC && b.integrate == AP_INTEGRATE_THRESHOLD &&
+                     (b.sampling == AP_SAMPLING_MIDPOINT || b.sampling == AP_SAMPLING_TRAPEZOID);
+  if (fused)
+    k_sample_select<<<sgrid, kTile * kTile, 0, s>>>(b);
+  else if (ext)
     k_sample<true><<<sgrid, kTile * kTile, 0, s>>>(b);
   else
     k_sample<false><<<sgrid, kTile * kTile, 0, s>>>(b);
@@ -2056,7 +2211,7 @@ cudaError_t launch_render_pass(const BatchArgs& b, const ConvIO& io, size_t conv
   E(t);
   if (b.integrate == AP_INTEGRATE_THRESHOLD) {
     t = B(KC_SELECT);
-    k_select<<<grid(2 * (int64_t)b.n_work_tiles, knob(GK_SAMPLE, 8)), kTile * kTile, 0, s>>>(b);
+    if (!fused) k_select<<<grid(2 * (int64_t)b.n_work_tiles, knob(GK_SAMPLE, 8)), kTile * kTile, 0, s>>>(b);
     if (ext)
       k_recheck<true><<<nsm * 4, 256, 0, s>>>(b);
     else
