@@ -2024,10 +2024,11 @@ __device__ __forceinline__ void conv_tile(const BatchArgs& b, const ConvIO& io, 
   conv_tile_reduce(vals, nv, tacc, shred);
 }
 
-// fixed sizes: 6 blocks per SM (80 registers); the large flavour is held to 1-2 blocks by its
-// shared memory anyway, so its registers are not capped
+// fixed sizes: 6 blocks per SM (80 registers).  The large flavour is held to 1-2 blocks per SM
+// by its shared memory, yet its register bound of 5 blocks (94 registers) measured 15 % faster on
+// 67 x 67 kernels than no bound (114 registers)
 template <int NF, bool LARGE>
-__global__ void __launch_bounds__(kConvThreads, LARGE ? 2 : 6) k_conv(BatchArgs b, ConvIO io) {
+__global__ void __launch_bounds__(kConvThreads, LARGE ? 5 : 6) k_conv(BatchArgs b, ConvIO io) {
   extern __shared__ __align__(16) float smem[];
   __shared__ float shred[kConvWarps * kNacc];
   __shared__ uint32_t next;
