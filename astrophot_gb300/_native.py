@@ -117,6 +117,8 @@ EXPORTS = [
     ("ap_render", [_P, _P, _P, _P, _P]),
     ("ap_jacobian", [_P, _P, _P, _P, _P, _I32, _P]),
     ("ap_render_psf_derivative", [_P, _P, _P, _P, _P, _P]),
+    ("ap_render_base_bytes", [_P, _PI64]),
+    ("ap_render_precise", [_P, _P, _P, _P, _P, _I64, _I32, _P]),
     ("ap_psf_normalize", [_I32, _I32, _P, _P, _P, _P, _P]),
     ("ap_render_vjp", [_P, _P, _P, _P, _I32, _P, _P]),
     ("ap_batch_autotune", [_P, _P, _P, _I32, _PI32, _PD, _P]),
@@ -142,11 +144,12 @@ EXPORTS = [
     ("ap_sample_probe", [_I32, _P, _I32, _I32, _P]),
     ("ap_batch_stats", [_P, _PI64]),
     ("ap_render_noalloc", [_I32, _I32, _I32, _I32, _PD, ctypes.POINTER(ApOptions), _P, _P, _P, _P]),
-    ("ap_scene_forward", [_P, _P, _P, _P, ctypes.c_float, _I32, _I32, _P, _P]),
+    ("ap_scene_forward", [_P, _P, _P, _P, ctypes.c_float, _P, _P, ctypes.c_double, _I32, _I32, _P, _P]),
     ("ap_scene_jvp", [_P, _P, _P, _P, _P, _I32, _I32, _P, _P]),
     ("ap_scene_jt", [_P, _I32, _P, _P, _I32, _I32, _P, _P]),
     ("ap_scene_hess", [_P, _P, _I32, _P, _P, _P, _I32, _I32, _P, _P]),
     ("ap_scene_chi2", [_P, _P, _P, _P, _I64, _P, _P, _I32, _P]),
+    ("ap_scene_chi2_change", [_P, _P, _P, _P, _P, _I64, _P, _P, _I32, _P]),
     ("ap_scene_residual", [_P, _P, _P, _P, _I64, _P, _P]),
     ("ap_scene_rpp_image", [_P, _P, _P, _P, _P, ctypes.c_double, _I64, _P, _P]),
     ("ap_scene_stage", [_I32, _P, _P, _P, _P, ctypes.c_double, _P, _P]),
@@ -440,6 +443,25 @@ class StampBatch:
         if out is None:
             out = torch.empty(self.out_pixels, dtype=torch.float32, device=self.device)
         check(self.lib.ap_render(self.handle, _ptr(params), _ptr(psf), _ptr(out), _stream()), "ap_render")
+        return out
+
+    RENDER_BASE, RENDER_DIFFERENCE = 1, 2
+
+    def base_buffer(self) -> torch.Tensor:
+        """A device buffer for the base point of :meth:`render_precise` (ap_render_base_bytes)."""
+        n = ctypes.c_int64()
+        check(self.lib.ap_render_base_bytes(self.handle, ctypes.byref(n)), "ap_render_base_bytes")
+        return torch.empty(int(n.value), dtype=torch.uint8, device=self.device)
+
+    def render_precise(self, params: torch.Tensor, psf: Optional[torch.Tensor], base: torch.Tensor, mode: int,
+                       out: Optional[torch.Tensor] = None):
+        """RENDER_BASE: the model, recorded in ``base``; RENDER_DIFFERENCE: the model minus the
+        recorded base model, accurate relative to the difference (ap_render_precise)."""
+        params = params.to(self.device, torch.float64).contiguous()
+        if out is None:
+            out = torch.empty(self.out_pixels, dtype=torch.float32, device=self.device)
+        check(self.lib.ap_render_precise(self.handle, _ptr(params), _ptr(psf), _ptr(out), _ptr(base), base.numel(),
+                                         int(mode), _stream()), "ap_render_precise")
         return out
 
     def render_psf_derivative(self, params: torch.Tensor, psf: torch.Tensor, dpsf: torch.Tensor,

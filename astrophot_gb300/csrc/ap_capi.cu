@@ -608,6 +608,62 @@ int ap_jacobian(ap_batch* b, const double* params, const float* psf, float* mode
   return render_common(b, params, psf, model, jac, ops, stream);
 }
 
+// base point of difference renders outside the LM: evaluation constants, shifted kernel, deep
+// image and integration pattern (the buffers the batched LM keeps in its own workspace)
+namespace {
+struct BaseLayout {
+  int64_t eval, psf, deep, code, total;
+};
+
+BaseLayout base_layout(const ap_batch* b) {
+  BaseLayout L{};
+  int64_t o = 0;
+  auto take = [&o](int64_t bytes) {
+    const int64_t at = o;
+    o = align_up(o + bytes);
+    return at;
+  };
+  L.eval = take(sizeof(EvalDev) * b->n);
+  L.psf = take(sizeof(float) * b->n * std::max<int64_t>(1, b->max_kp2));
+  L.deep = take(sizeof(float) * b->work_pixels);
+  L.code = take(sizeof(uint32_t) * b->work_pixels);
+  L.total = o;
+  return L;
+}
+}  // namespace
+
+int ap_render_base_bytes(const ap_batch* b, int64_t* bytes) {
+  if (!b || !bytes) return AP_ERR_ARG;
+  *bytes = base_layout(b).total;
+  return AP_OK;
+}
+
+int ap_render_precise(ap_batch* b, const double* params, const float* psf, float* model, void* base,
+                      int64_t base_bytes, int32_t mode, ap_stream_t stream) {
+  if (!b || !params || !model || !base) return AP_ERR_ARG;
+  if (mode != AP_RENDER_BASE && mode != AP_RENDER_DIFFERENCE) return AP_ERR_ARG;
+  if (((uintptr_t)base & 15u) != 0) return AP_ERR_ARG;
+  if (!b->bound) return AP_ERR_NOT_BOUND;
+  if (b->opt.psf_mode != AP_PSF_NONE && !psf) return AP_ERR_ARG;
+  if (b->args.kind != AP_PROFILE_SERSIC && b->args.kind != AP_PROFILE_EXPONENTIAL) return AP_ERR_UNSUPPORTED;
+  const BaseLayout L = base_layout(b);
+  if (base_bytes < L.total) return AP_ERR_WORKSPACE;
+  char* w = (char*)base;
+  BatchArgs A = b->args;
+  A.base_eval = (EvalDev*)(w + L.eval);
+  A.base_psf = (float*)(w + L.psf);
+  A.base_deep = (float*)(w + L.deep);
+  A.base_code = (uint32_t*)(w + L.code);
+  cudaStream_t s = (cudaStream_t)stream;
+  const int32_t ops = OP_FWD | OP_WRITE_MODEL | (mode == AP_RENDER_BASE ? OP_BASE : OP_DIFF);
+  int rc = check_cuda(launch_eval_setup(A, params, NPARAM, 0, nullptr, ops, s));
+  if (rc) return rc;
+  ConvIO io{};
+  io.psf = psf;
+  io.model_out = model;
+  return check_cuda(launch_render_pass(A, io, b->conv_smem, false, s, &b->prof));
+}
+
 int ap_render_psf_derivative(ap_batch* b, const double* params, const float* psf, const float* dpsf,
                              float* model, ap_stream_t stream) {
   if (!b || !params || !psf || !dpsf || !model) return AP_ERR_ARG;

@@ -37,8 +37,21 @@ __device__ __forceinline__ bool in_window(const ap_scene_source& s, int x, int y
 
 // ---- forward: image = sky + sum over the tile's sources (fixed order: deterministic) -------------
 __global__ void k_scene_forward(const ap_scene_source* __restrict__ src, const int32_t* __restrict__ tile_ptr,
-                                const int32_t* __restrict__ tile_src, const float* __restrict__ fwd, float sky, int nx,
-                                int ny, float* __restrict__ image) {
+                                const int32_t* __restrict__ tile_src, const float* __restrict__ fwd, float sky,
+                                const double* __restrict__ sky_F, const double* __restrict__ sky_F0, double area,
+                                int nx, int ny, float* __restrict__ image) {
+  if (sky_F) {
+    // a free flat sky: pixel_area 10^F counts per pixel, from the staged F (float64, then
+    // rounded); for difference renders the sky's change area 10^F0 (10^(F - F0) - 1)
+    __shared__ float s_sky;
+    if (threadIdx.x == 0) {
+      constexpr double kLn10 = 2.302585092994045684;
+      s_sky = sky_F0 ? (float)(area * pow(10.0, *sky_F0) * expm1(kLn10 * (*sky_F - *sky_F0)))
+                     : (float)(area * pow(10.0, *sky_F));
+    }
+    __syncthreads();
+    sky = s_sky;
+  }
   const int tx = blockIdx.x % ((nx + kSceneTile - 1) / kSceneTile);
   const int ty = blockIdx.x / ((nx + kSceneTile - 1) / kSceneTile);
   const int t = blockIdx.x;
@@ -168,7 +181,10 @@ __global__ void __launch_bounds__(256) k_scene_hess(const ap_scene_source* __res
 // chi^2 in two passes with a fixed summation order (the same bits on every run): block b sums
 // the pixels [b chunk, (b + 1) chunk) into part[b], then one block sums the parts in order.  The
 // float64 arithmetic per pixel is spread over the whole GPU (its float64 pipe is narrow).
-__global__ void __launch_bounds__(256) k_scene_chi2_part(const float* __restrict__ model, const float* __restrict__ data,
+// With `base`, model holds a difference dm to the model base and the sum is chi^2's change
+// W dm (dm - 2 (data - base)), accurate relative to the change itself.
+__global__ void __launch_bounds__(256) k_scene_chi2_part(const float* __restrict__ model, const float* __restrict__ base,
+                                                         const float* __restrict__ data,
                                                          const float* __restrict__ weight,
                                                          const uint8_t* __restrict__ mask, int64_t n, int64_t chunk,
                                                          double* __restrict__ part) {
@@ -176,8 +192,14 @@ __global__ void __launch_bounds__(256) k_scene_chi2_part(const float* __restrict
   double acc = 0.0;
   for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
     if (mask && mask[i]) continue;
-    const double r = (double)data[i] - (double)model[i];
-    acc += (weight ? (double)weight[i] : 1.0) * r * r;
+    const double w = weight ? (double)weight[i] : 1.0;
+    if (base) {
+      const double dm = (double)model[i], r = (double)data[i] - (double)base[i];
+      acc += w * dm * (dm - 2.0 * r);
+    } else {
+      const double r = (double)data[i] - (double)model[i];
+      acc += w * r * r;
+    }
   }
   acc = warp_sum(acc);
   __shared__ double sh[8];
@@ -518,10 +540,13 @@ int ap_psf_normalize(int32_t n_pix, int32_t n_dir, const float* img, const float
 }
 
 int ap_scene_forward(const ap_scene_source* sources, const int32_t* tile_ptr, const int32_t* tile_src,
-                     const float* fwd, float sky, int32_t nx, int32_t ny, float* image, ap_stream_t stream) {
+                     const float* fwd, float sky, const double* sky_F, const double* sky_F0, double area,
+                     int32_t nx, int32_t ny, float* image, ap_stream_t stream) {
   if (!sources || !tile_ptr || !tile_src || !fwd || !image || nx <= 0 || ny <= 0) return AP_ERR_ARG;
+  if (sky_F0 && !sky_F) return AP_ERR_ARG;
   const int tiles = ((nx + kSceneTile - 1) / kSceneTile) * ((ny + kSceneTile - 1) / kSceneTile);
-  k_scene_forward<<<tiles, 256, 0, (cudaStream_t)stream>>>(sources, tile_ptr, tile_src, fwd, sky, nx, ny, image);
+  k_scene_forward<<<tiles, 256, 0, (cudaStream_t)stream>>>(sources, tile_ptr, tile_src, fwd, sky, sky_F, sky_F0, area,
+                                                          nx, ny, image);
   return record_cuda(cudaGetLastError());
 }
 
@@ -553,17 +578,29 @@ int ap_scene_hess(const ap_scene_source* sources, const int32_t* pairs, int32_t 
   return record_cuda(cudaGetLastError());
 }
 
-int ap_scene_chi2(const float* model, const float* data, const float* weight, const uint8_t* mask, int64_t n,
-                  double* out, double* parts, int32_t n_parts, ap_stream_t stream) {
+static int scene_chi2(const float* model, const float* base, const float* data, const float* weight,
+                      const uint8_t* mask, int64_t n, double* out, double* parts, int32_t n_parts,
+                      cudaStream_t st) {
   if (!model || !data || !out || !parts || n <= 0 || n_parts < 1) return AP_ERR_ARG;
-  cudaStream_t st = (cudaStream_t)stream;
   const int m = n_parts < 1024 ? n_parts : 1024;
   int64_t chunk = (n + m - 1) / m;
   chunk = (chunk + 255) / 256 * 256;
   const int blocks = (int)((n + chunk - 1) / chunk);
-  k_scene_chi2_part<<<blocks, 256, 0, st>>>(model, data, weight, mask, n, chunk, parts);
+  k_scene_chi2_part<<<blocks, 256, 0, st>>>(model, base, data, weight, mask, n, chunk, parts);
   k_sum_parts<<<1, 256, 0, st>>>(parts, blocks, out);
   return record_cuda(cudaGetLastError());
+}
+
+int ap_scene_chi2(const float* model, const float* data, const float* weight, const uint8_t* mask, int64_t n,
+                  double* out, double* parts, int32_t n_parts, ap_stream_t stream) {
+  return scene_chi2(model, nullptr, data, weight, mask, n, out, parts, n_parts, (cudaStream_t)stream);
+}
+
+int ap_scene_chi2_change(const float* dm, const float* base, const float* data, const float* weight,
+                         const uint8_t* mask, int64_t n, double* out, double* parts, int32_t n_parts,
+                         ap_stream_t stream) {
+  if (!base) return AP_ERR_ARG;
+  return scene_chi2(dm, base, data, weight, mask, n, out, parts, n_parts, (cudaStream_t)stream);
 }
 
 int ap_scene_residual(const float* model, const float* data, const float* weight, const uint8_t* mask, int64_t n,

@@ -815,12 +815,16 @@ def _scene_spec(owner, components):
     skies = [c for c in components if isinstance(c, Flat_Sky)]
     if len(gals) + len(skies) != len(components) or len(skies) > 1:
         raise NotImplementedError("the scene path covers Sersic / exponential galaxies and one flat sky")
-    sky = 0.0
+    sky, sky_free = 0.0, {}
     if skies:
         F = skies[0].parameters["F"]
-        if not F.locked:
-            raise NotImplementedError("a free sky in a group of several galaxies is not supported by the CUDA path")
-        sky = float(w.pixel_area) * 10.0 ** float(F.value.item())
+        if F.locked:
+            sky = float(w.pixel_area) * 10.0 ** float(F.value.item())
+        else:
+            # a free F: one image-wide column of the joint vector, after the galaxies listed
+            # before the sky (the group's parameter order follows its model list)
+            sky_free = dict(sky_F=float(F.value.item()),
+                            sky_after=sum(1 for c in components[: components.index(skies[0])] if c in gals))
     knobs = {k: getattr(gals[0], k) for k in _KNOBS}
     for g in gals[1:]:
         if any(getattr(g, k) != knobs[k] for k in _KNOBS):
@@ -852,13 +856,13 @@ def _scene_spec(owner, components):
         win = ((di, di + int(g.window.pixel_shape[0])), (dj, dj + int(g.window.pixel_shape[1])))
         sources.append(SceneSource(g.profile, vals, win, link, locked))
     opts = {k: knobs[k] for k in _KNOBS if k != "psf_mode"}
-    return w, sources, psf, sky, opts
+    return w, sources, psf, sky, sky_free, opts
 
 
 def _make_scene(owner, components, with_data=True):
     from .scene import Scene
 
-    w, sources, psf, sky, opts = _scene_spec(owner, components)
+    w, sources, psf, sky, sky_free, opts = _scene_spec(owner, components)
     if abs(w.pixelscale[0, 1]) > 0 or abs(w.pixelscale[1, 0]) > 0 or abs(w.pixelscale[0, 0] - w.pixelscale[1, 1]) > 0:
         raise NotImplementedError("scenes need a square, axis-aligned pixel grid on the CUDA path")
     nx, ny = int(w.pixel_shape[0]), int(w.pixel_shape[1])
@@ -875,7 +879,8 @@ def _make_scene(owner, components, with_data=True):
         raise NotImplementedError("a live PSF needs the image's pixel scale on the CUDA path")
     scene = Scene(nx, ny, sources, None if (psf is None or live is not None) else psf.data.numpy(), data, weight,
                   mask=mask, sky=sky, scale=float(w.pixelscale[0, 0]), options=opts,
-                  origin=(float(origin[0]), float(origin[1])), device=config.ap_device, psf_model=live)
+                  origin=(float(origin[0]), float(origin[1])), device=config.ap_device, psf_model=live,
+                  **sky_free)
     if scene.P != len(owner.parameters.vector_values()):
         raise NotImplementedError("this parameter structure has no joint-vector mapping on the CUDA path")
     return scene

@@ -170,20 +170,26 @@ class SceneSource:
 
 class Scene:
     """Sources on one ``nx`` x ``ny`` image (pixel scale ``scale``, the (0, 0) pixel corner at the
-    origin) with a locked flat sky ``sky`` (counts per pixel), one PSF (None: no convolution) or
-    a live PSF model ``psf_model`` (:class:`LivePSF`, its free parameters first in the joint
-    vector), data / weight (1 / variance) / mask (True = ignored).  ``graphs``: replay the
-    forward and the Jacobian from CUDA graphs captured at their second call."""
+    origin) with a locked flat sky ``sky`` (counts per pixel) or, with ``sky_F`` given, a free
+    flat sky of pixel_area * 10^F (``Flat_Sky``, models/flatsky_model.py:13-55) whose F sits in
+    the joint vector after the free slots of the first ``sky_after`` sources (after all of them
+    by default), one PSF (None: no convolution) or a live PSF
+    model ``psf_model`` (:class:`LivePSF`, its free parameters first in the joint vector), data /
+    weight (1 / variance) / mask (True = ignored).  ``graphs``: replay the forward and the
+    Jacobian from CUDA graphs captured at their second call."""
 
     def __init__(self, nx: int, ny: int, sources: List[SceneSource], psf: Optional[np.ndarray], data, weight,
                  mask=None, sky: float = 0.0, scale: float = 1.0, options: Optional[dict] = None,
                  fwd_chunk: int = 64, device="cuda", origin=(0.0, 0.0), psf_model: Optional[LivePSF] = None,
-                 graphs: bool = True):
+                 graphs: bool = True, sky_F: Optional[float] = None, sky_after: Optional[int] = None):
         self.nx, self.ny, self.scale = int(nx), int(ny), float(scale)
         self.origin = (float(origin[0]), float(origin[1]))
         self.sources = list(sources)
         self.device = torch.device(device)
-        self.sky = float(sky)
+        self.sky_free = sky_F is not None
+        self.sky_F = float(sky_F) if self.sky_free else None
+        self.pixel_area = self.scale * self.scale
+        self.sky = self.pixel_area * 10.0 ** self.sky_F if self.sky_free else float(sky)
         self.live_psf = psf_model
         if psf_model is not None:
             if psf is not None:
@@ -202,10 +208,19 @@ class Scene:
         # ---- joint vector: a live PSF's free parameters, then the sources in order and their
         # free slots in parameter order --------------------------------------------------------
         self.n_psf = 0 if psf_model is None else len(psf_model.free)
-        # per joint index: (source, full-vector slot), (-1, PSF parameter name) for the live PSF
+        # per joint index: (source, full-vector slot), (-1, PSF parameter name) for the live PSF,
+        # (-2, "F") for a free sky
         self.slot_of = [(-1, f) for f in (psf_model.free if psf_model is not None else ())]
         self.gidx = []     # per source: {slot: joint index}
+        self.sky_g = None
+        n_src = len(self.sources)
+        sky_pos = n_src if sky_after is None else int(sky_after)
+        if self.sky_free and not 0 <= sky_pos <= n_src:
+            raise ValueError("sky_after must lie between 0 and the number of sources")
         for si, src in enumerate(self.sources):
+            if self.sky_free and si == sky_pos:
+                self.sky_g = len(self.slot_of)
+                self.slot_of.append((-2, "F"))
             if src.kind not in _SLOTS_OF:
                 raise ValueError(f"unsupported source kind {src.kind}")
             g = {}
@@ -221,7 +236,12 @@ class Scene:
                 g[sl] = len(self.slot_of)
                 self.slot_of.append((si, sl))
             self.gidx.append(g)
+        if self.sky_free and self.sky_g is None:
+            self.sky_g = len(self.slot_of)
+            self.slot_of.append((-2, "F"))
         self.P = len(self.slot_of)
+        # image-wide Jacobian columns: a live PSF's free parameters, then a free sky's F
+        self.n_img = self.n_psf + (1 if self.sky_free else 0)
         self.ndf = max(1.0, n_used - self.P)
 
         # ---- stamp batches, one per (kind, fitted slots) --------------------------------------
@@ -248,9 +268,9 @@ class Scene:
             self._jac_parts.append(dict(kind=kind, free=free, members=members, batch=jb, psf=jpsf, off=jac_total,
                                         nf=nf))
             jac_total += nf * jb.out_pixels
-        # live PSF columns: image-wide, one [ny * nx] plane per free PSF parameter
+        # image-wide columns: one [ny * nx] plane per free PSF parameter, then a free sky's
         self.psf_jac_off = jac_total
-        jac_total += self.n_psf * self.nx * self.ny
+        jac_total += self.n_img * self.nx * self.ny
         self.jac = torch.zeros(max(jac_total, 1), dtype=torch.float32, device=dev)
 
         # model renders.  The reference evaluates a windowed source of a group on the group's
@@ -311,8 +331,11 @@ class Scene:
             rows += n_chunks * (len(part["members"]) if part["own"] else part["m"])
         self._psf_row = rows
         rows += 1
-        self._stage_h = np.zeros((rows + 1, 8))  # last row: the PSF columns' d value / d rep
-        self._stage_d = torch.zeros((rows + 1, 8), dtype=torch.float64, device=dev)
+        # then the PSF columns' d value / d rep, and the sky row (cell 0: a free sky's F)
+        self._scale_row, self._sky_row = rows, rows + 1
+        self._stage_h = np.zeros((rows + 2, 8))
+        self._stage_d = torch.zeros((rows + 2, 8), dtype=torch.float64, device=dev)
+        self._sky_F_d = self._stage_d[self._sky_row, 0:1]
         for part in self._jac_parts:
             r0, n = part["srow"]
             part["dpar"] = self._stage_d[r0 : r0 + n]
@@ -321,19 +344,24 @@ class Scene:
         if psf_model is not None:
             psf_model.row_d = self._stage_d[self._psf_row : self._psf_row + 1]
         self._img = torch.empty(self.nx * self.ny, dtype=torch.float32, device=dev)
+        self._dimg = torch.empty_like(self._img)   # difference renders
+        self._bases = None                          # their base points, allocated at first use
+        self._sky_F0_d = torch.zeros(1, dtype=torch.float64, device=dev)
         self.use_graphs = bool(graphs)
         self._graphs, self._graph_failed, self._graph_calls = {}, set(), {}
 
-        # ---- source descriptors (+ one whole-image entry carrying the live PSF columns) --------
+        # ---- source descriptors (+ one whole-image entry carrying the image-wide columns) ------
         ns = len(self.sources)
-        desc = (ApSceneSource * (ns + (1 if self.n_psf else 0)))()
-        if self.n_psf:
+        desc = (ApSceneSource * (ns + (1 if self.n_img else 0)))()
+        if self.n_img:
             d = desc[ns]
             d.jac_off, d.jac_stride = self.psf_jac_off, self.nx * self.ny
             d.x0, d.y0, d.wx, d.wy = 0, 0, self.nx, self.ny
-            d.n_free = self.n_psf
+            d.n_free = self.n_img
             for c in range(self.n_psf):
                 d.gidx[c] = c
+            if self.sky_free:
+                d.gidx[self.n_psf] = self.sky_g
         for part in self._fwd_parts:
             for k, si in enumerate(part["members"]):
                 d = desc[si]
@@ -371,9 +399,9 @@ class Scene:
         flat = np.array([s for l in lists for s in l] or [0], dtype=np.int32)
         self.tile_ptr = torch.tensor(ptr, device=dev)
         self.tile_src = torch.tensor(flat, device=dev)
-        # J h also sums the live PSF columns: the whole-image entry in every tile
+        # J h also sums the image-wide columns: the whole-image entry in every tile
         self.jtile_ptr, self.jtile_src = self.tile_ptr, self.tile_src
-        if self.n_psf:
+        if self.n_img:
             jl = [l + [ns] for l in lists]
             jptr = np.zeros(len(jl) + 1, dtype=np.int32)
             jptr[1:] = np.cumsum([len(l) for l in jl])
@@ -387,7 +415,7 @@ class Scene:
                 (bx0, bx1), (by0, by1) = wins[b]
                 if max(ax0, bx0) < min(ax1, bx1) and max(ay0, by0) < min(ay1, by1):
                     pairs.append((a, b))
-        if self.n_psf:
+        if self.n_img:
             pairs += [(a, ns) for a in range(ns)] + [(ns, ns)]
         self.n_pairs = len(pairs)
         self.pairs = torch.tensor(np.array(pairs, dtype=np.int32).reshape(-1, 2), device=dev).contiguous()
@@ -433,6 +461,8 @@ class Scene:
             rep[g] = to_rep(*SLOT_LIMITS[sl], self.sources[si].params[sl])
         if self.n_psf:
             rep[: self.n_psf] = self.live_psf.representation()
+        if self.sky_free:
+            rep[self.sky_g] = self.sky_F  # no limits: F is its own representation
         return rep
 
     def set_representation(self, rep):
@@ -442,6 +472,9 @@ class Scene:
             src.params = list(V[si, :7])
         if self.n_psf:
             self.live_psf.set_representation(rep[: self.n_psf])
+        if self.sky_free:
+            self.sky_F = float(rep[self.sky_g])
+            self.sky = self.pixel_area * 10.0 ** self.sky_F
 
     def _stage(self, rep, as_representation: bool = True):
         """Every render's parameter rows (and a live PSF's row and column scales) at ``rep`` into
@@ -466,7 +499,9 @@ class Scene:
             live = self.live_psf
             live.set_representation(rep[: self.n_psf])
             H[self._psf_row] = live._row().numpy()[0]
-            H[-1, : self.n_psf] = live.drep(rep[: self.n_psf]) if as_representation else 1.0
+            H[self._scale_row, : self.n_psf] = live.drep(rep[: self.n_psf]) if as_representation else 1.0
+        if self.sky_free:
+            H[self._sky_row, 0] = rep[self.sky_g]
         self._stage_d.copy_(torch.from_numpy(H))
         return V
 
@@ -493,6 +528,8 @@ class Scene:
                 if si >= 0:
                     for sl, gi in self.gidx[si].items():
                         g[r, sl] = gi
+            if self.sky_free:
+                g[self._sky_row, 0] = self.sky_g  # slot 0's map is the identity, as F's
             self._row_src = row_src
             self._stage_gidx = torch.tensor(g.reshape(-1), device=self.device)
             self._stage_base = torch.zeros(g.size, dtype=torch.float64, device=self.device)
@@ -585,28 +622,90 @@ class Scene:
         g.replay()
 
     # ---- device primitives -----------------------------------------------------------------
-    def _render_sources(self, buf, render):
+    def _render_sources(self, buf, render, base_mode: int = 0):
         """Every source's model render into ``buf`` (the layout of ``self.fwd``) by
-        ``render(batch, staged params, packed psf, out)``."""
-        for part in self._fwd_parts:
+        ``render(batch, staged params, packed psf, out)``, or, with ``base_mode`` (RENDER_BASE /
+        RENDER_DIFFERENCE), by the batch's precise render against the base buffer of that call."""
+        bases = self._base_buffers() if base_mode else None
+
+        def call(pi, c, b, p, k, out):
+            if base_mode:
+                b.render_precise(p, k, bases[pi][c], base_mode, out=out)
+            else:
+                render(b, p, k, out)
+
+        for pi, part in enumerate(self._fwd_parts):
             b, m, mem = part["batch"], part["m"], part["members"]
             if part["own"]:
-                render(b, part["dpar"][0], part["psf"], buf[part["off"] : part["off"] + b.out_pixels])
+                call(pi, 0, b, part["dpar"][0], part["psf"], buf[part["off"] : part["off"] + b.out_pixels])
                 continue
             for c, c0 in enumerate(range(0, len(mem), m)):
                 out = buf[part["off"] + c0 * self.nx * self.ny : part["off"] + (c0 + m) * self.nx * self.ny]
                 if out.numel() == m * self.nx * self.ny:
-                    render(b, part["dpar"][c], part["psf"], out)
+                    call(pi, c, b, part["dpar"][c], part["psf"], out)
                 else:
                     tmp = torch.empty(b.out_pixels, dtype=torch.float32, device=self.device)
-                    render(b, part["dpar"][c], part["psf"], tmp)
+                    call(pi, c, b, part["dpar"][c], part["psf"], tmp)
                     out.copy_(tmp[: out.numel()])
 
-    def _combine(self, buf, sky, img):
+    def _combine(self, buf, sky, img, with_sky: bool = True, difference: bool = False):
+        """img = the sources' renders in ``buf`` + the sky: ``sky`` (counts per pixel) when locked,
+        pixel_area * 10^F from the staged F when free (``with_sky`` False: no sky).  With
+        ``difference``, ``buf`` holds differences to the base renders and the sky term is the free
+        sky's change since the base (a locked sky's is zero)."""
+        sky_F = self._sky_F_d if (self.sky_free and with_sky) else None
+        sky_F0 = self._sky_F0_d if (difference and sky_F is not None) else None
+        locked = 0.0 if (difference or not with_sky) else sky
         N.check(self.lib.ap_scene_forward(N._ptr(self.desc), N._ptr(self.tile_ptr), N._ptr(self.tile_src),
-                                          N._ptr(buf), ctypes.c_float(sky), self.nx, self.ny, N._ptr(img),
+                                          N._ptr(buf), ctypes.c_float(locked), N._ptr(sky_F), N._ptr(sky_F0),
+                                          ctypes.c_double(self.pixel_area), self.nx, self.ny, N._ptr(img),
                                           N._stream()), "ap_scene_forward")
         return img
+
+    # ---- difference renders: the joint LM's damping trials near its optimum ---------------
+    def _base_buffers(self):
+        """One base-point buffer per render call of the forward (a part, or one chunk of it)."""
+        if self._bases is None:
+            self._bases = {}
+            for pi, part in enumerate(self._fwd_parts):
+                n = 1 if part["own"] else (len(part["members"]) + part["m"] - 1) // part["m"]
+                self._bases[pi] = [part["batch"].base_buffer() for _ in range(n)]
+        return self._bases
+
+    @property
+    def precise_capable(self) -> bool:
+        """Whether trials can be rendered as differences (device staging: no live PSF)."""
+        return self.device_staging
+
+    def _forward_base_body(self):
+        self._render_sources(self.fwd, None, base_mode=N.StampBatch.RENDER_BASE)
+        self._combine(self.fwd, self.sky, self._img)
+        if self.sky_free:
+            self._sky_F0_d.copy_(self._sky_F_d)
+
+    def _forward_diff_body(self):
+        self._render_sources(self.fwd, None, base_mode=N.StampBatch.RENDER_DIFFERENCE)
+        self._combine(self.fwd, self.sky, self._dimg, difference=True)
+
+    def forward_base_device(self, x: torch.Tensor) -> torch.Tensor:
+        """:meth:`forward_device` at x, recording x as the base point of difference renders."""
+        self._stage_dev(x)
+        self._run("forward_base", self._forward_base_body)
+        return self._img
+
+    def forward_diff_device(self, x: torch.Tensor, v: torch.Tensor, alpha: float) -> torch.Tensor:
+        """model(x + alpha v) - model(base point), accurate relative to the change (float32
+        image, overwritten by the next call)."""
+        self._stage_dev(x, v, alpha)
+        self._run("forward_diff", self._forward_diff_body)
+        return self._dimg
+
+    def chi2_change_into(self, dm: torch.Tensor, base: torch.Tensor, out: torch.Tensor):
+        """chi^2(base + dm) - chi^2(base) into the device float64 ``out[0]``."""
+        N.check(self.lib.ap_scene_chi2_change(N._ptr(dm), N._ptr(base), N._ptr(self.data), N._ptr(self.weight),
+                                              N._ptr(self.mask), self.nx * self.ny, N._ptr(out),
+                                              N._ptr(self._chi2_parts), self._chi2_parts.numel(), N._stream()),
+                "ap_scene_chi2_change")
 
     def _forward_body(self):
         if self.n_psf:
@@ -624,10 +723,16 @@ class Scene:
         """Image-wide column ``j`` of a live PSF into ``out`` [ny * nx]: every source rendered
         with the derivative of its kernel along d psf / d theta_j (scaled by the staged
         d value / d representation), summed like the model."""
-        D = dK[j] * self._stage_d[-1, j].to(torch.float32)
+        D = dK[j] * self._stage_d[self._scale_row, j].to(torch.float32)
         self._render_sources(self.fwd_d, lambda b, p, k, o: b.render_psf_derivative(
             p, k, D.repeat(k.numel() // D.numel()), out=o))
-        return self._combine(self.fwd_d, 0.0, out)
+        return self._combine(self.fwd_d, 0.0, out, with_sky=False)
+
+    def _sky_column(self, out):
+        """The free sky's image-wide column, d image / d F = ln(10) pixel_area 10^F everywhere
+        (F is unbounded: the same in representation space), from the staged F."""
+        c = (math.log(10.0) * self.pixel_area) * torch.pow(10.0, self._sky_F_d)
+        out.copy_(c.to(torch.float32).expand(out.numel()))
 
     def _jacobian_body(self, as_representation: bool):
         dK = self._psf_body(True) if self.n_psf else None
@@ -638,6 +743,9 @@ class Scene:
         npx = self.nx * self.ny
         for j in range(self.n_psf):
             self._psf_column(dK, j, self.jac[self.psf_jac_off + j * npx : self.psf_jac_off + (j + 1) * npx])
+        if self.sky_free:
+            j = self.n_psf
+            self._sky_column(self.jac[self.psf_jac_off + j * npx : self.psf_jac_off + (j + 1) * npx])
 
     def jacobian(self, rep: np.ndarray, as_representation: bool = True):
         """Own-window Jacobians of every source (representation or value space) into ``self.jac``,
@@ -662,8 +770,9 @@ class Scene:
                               + (x1 - x0) * (y1 - y0)]
                     out[y0:y1, x0:x1, self.gidx[si][sl]] += col.reshape(y1 - y0, x1 - x0)
         npx = self.nx * self.ny
-        for j in range(self.n_psf):
-            out[:, :, j] += jac[self.psf_jac_off + j * npx : self.psf_jac_off + (j + 1) * npx].reshape(self.ny, self.nx)
+        for j in range(self.n_img):
+            g = j if j < self.n_psf else self.sky_g
+            out[:, :, g] += jac[self.psf_jac_off + j * npx : self.psf_jac_off + (j + 1) * npx].reshape(self.ny, self.nx)
         return out
 
     def _vjp_index(self, part):
@@ -725,6 +834,11 @@ class Scene:
                     gi = self.gidx[si].get(sl)
                     if gi is not None:
                         out[gi] += r[c]
+        if self.sky_free:
+            # d image / d F = ln(10) pixel_area 10^F in every pixel (F unbounded: rep = value)
+            F = float(rep[self.sky_g])
+            out[self.sky_g] = (math.log(10.0) * self.pixel_area * 10.0 ** F
+                               * float(g_img.to(torch.float64).sum().item()))
         return torch.tensor(out, dtype=torch.float64)
 
     def hess(self) -> torch.Tensor:
@@ -736,7 +850,7 @@ class Scene:
 
     def jt(self, img: torch.Tensor) -> torch.Tensor:
         out = torch.empty(self.P, dtype=torch.float64, device=self.device)
-        N.check(self.lib.ap_scene_jt(N._ptr(self.desc), len(self.sources) + (1 if self.n_psf else 0), N._ptr(self.jac),
+        N.check(self.lib.ap_scene_jt(N._ptr(self.desc), len(self.sources) + (1 if self.n_img else 0), N._ptr(self.jac),
                                      N._ptr(img), self.nx,
                                      self.P, N._ptr(out), N._stream()), "ap_scene_jt")
         return out
@@ -807,6 +921,7 @@ class Scene:
             return None
         return h
 
+
 class OptimizeStop(Exception):
     pass
 
@@ -816,13 +931,25 @@ class SceneLM:
     it with the others held (the LM ``Iter_LM`` runs under ``Param_Mask``,
     fit/iterative.py:291-296)."""
 
+    # relative error bounds of a chi^2 change summed from a difference render, and of a chi^2
+    # summed from a full float32 render: a chain of accepted changes drifts by the first times
+    # their sizes, and the next base render's chi^2 re-anchors it once that exceeds the second
+    DIFF_REL_ERR = 2e-6
+    FULL_REL_ERR = 2e-8
+
     def __init__(self, scene: Scene, initial_state=None, max_iter: int = 100, relative_tolerance: float = 1e-5,
                  max_step_iter: int = 10, curvature_limit: float = 1.0, Lup: float = 11.0, Ldn: float = 9.0,
-                 L0: float = 1.0, acceleration: float = 0.0, ndf=None, free=None, device_loop: bool = True):
+                 L0: float = 1.0, acceleration: float = 0.0, ndf=None, free=None, device_loop: bool = True,
+                 precise_trials: bool = True):
         self.scene = scene
         # device_loop: the vectors stay on the device, parameters are staged there, each damping
         # trial reads one status back (scenes without a live PSF); else the host loop below
         self.device_loop = bool(device_loop) and scene.device_staging
+        # precise_trials (device loop): every step renders its base point once more, recording it,
+        # and each trial (and the geodesic render) as its difference to that base, so chi^2 changes
+        # far below one float32 render's rounding still order the trials as the reference's float64
+        # chi^2 does; the trial chi^2 is the step's chi^2 plus the change
+        self.precise = bool(precise_trials) and self.device_loop and scene.precise_capable
         self.x = np.array(scene.representation() if initial_state is None else initial_state, dtype=np.float64)
         self.free = None if free is None else np.asarray(free, dtype=np.int64)
         self._free_t = None if free is None else torch.as_tensor(self.free, device=scene.device)
@@ -936,30 +1063,40 @@ class SceneLM:
     def _trial(self, hess, grad, r, d, mixed: bool):
         """One damping trial at the current L on the device: the step h, the geodesic term a (when
         L > 1e-4), the render at x + h + a * acceleration and its chi^2.  Returns (h + a acc, the
-        render, the packed status [solve status, chi^2, geodesic solve status, a, h] read back)."""
+        render (with precise trials its difference to the base render), the packed status
+        [solve status, chi^2 (precise: its change from the base), geodesic solve status, the base
+        render's chi^2, a, h] read back)."""
         sc = self.scene
         x = self._xd
         P = sc.P
         h = self._full(sc.solve_device(hess, grad, self.L, sc._info, mixed=mixed))
         if self.L > 1e-4:
             # the geodesic term from the render at x + d h (skipped at L <= 1e-4, where
-            # fit/lm.py:277-286 computes it and then discards it)
-            Y1 = sc.forward_device(x, h, d)
-            rh = sc.residual(sc.data, Y1)   # W (Y1 - Y)
-            rpp = self._sub(sc.jt(sc.rpp_image(r, rh, sc.jvp(h), d)))
+            # fit/lm.py:277-286 computes it and then discards it); it needs only W (Y1 - Y0)
+            if self.precise:
+                rh = sc.residual(self._zero, sc.forward_diff_device(x, h, d))   # W (Y1 - Y0)
+                rpp = self._sub(sc.jt(sc.rpp_image(self._zero, rh, sc.jvp(h), d)))
+            else:
+                Y1 = sc.forward_device(x, h, d)
+                rh = sc.residual(sc.data, Y1)   # W (Y1 - Y)
+                rpp = self._sub(sc.jt(sc.rpp_image(r, rh, sc.jvp(h), d)))
             a_d = self._full(sc.solve_device(hess, rpp, self.L, sc._info2, mixed=mixed, reuse=True))
             a = torch.where((sc._info == 0) & (sc._info2 == 0), torch.neg(a_d) / 2, torch.zeros_like(a_d))
         else:
             a = torch.zeros_like(h)
             sc._info2.zero_()
         ha = torch.add(h, torch.mul(a, self.acceleration))
-        Y1 = sc.forward_device(x, ha, 1.0)
         st = self._status
-        sc.chi2_into(Y1, st[1:2])
+        if self.precise:
+            Y1 = sc.forward_diff_device(x, ha, 1.0)      # Y(x + ha) - Y0
+            sc.chi2_change_into(Y1, self._Y0, st[1:2])
+        else:
+            Y1 = sc.forward_device(x, ha, 1.0)
+            sc.chi2_into(Y1, st[1:2])
         st[0:1].copy_(sc._info)
         st[2:3].copy_(sc._info2)
-        st[3 : 3 + P].copy_(a)
-        st[3 + P :].copy_(h)
+        st[4 : 4 + P].copy_(a)
+        st[4 + P :].copy_(h)
         return ha, Y1, st.cpu().numpy()
 
     def _step_device(self, chi2, have_y0: bool):
@@ -971,7 +1108,13 @@ class SceneLM:
         sc = self.scene
         x = self._xd
         P = sc.P
-        if not have_y0:
+        if self.precise:
+            # the base point of this step's difference trials; its full chi^2 travels with the
+            # first trial's status and re-anchors the chain of changes once that has drifted
+            self._Y0.copy_(sc.forward_base_device(x))
+            sc.chi2_into(self._Y0, self._status[3:4])
+            self.base_renders += 1
+        elif not have_y0:
             self._Y0.copy_(sc.forward_device(x))
             self.base_renders += 1
         Y0 = self._Y0
@@ -999,14 +1142,21 @@ class SceneLM:
                 # the mixed-precision solve did not converge: the trial again, in float64
                 self.fp64_retries += 1
                 ha, Y1, s = self._trial(hess, grad, r, d, mixed=False)
+            if self.precise and iteration == 0:
+                full = float(s[3]) / self.ndf
+                if self._drift > self.FULL_REL_ERR * full:
+                    init_chi2 = full
+                    best = (None, full, self.L)
+                    scarry_best = (None, full, self.L)
+                    self._drift = 0.0
             if int(s[0]) != 0:   # the damped matrix was not positive definite
                 self.Lup()
                 if direction == "better":
                     break
                 direction = "worse"
                 continue
-            chi2 = float(s[1]) / self.ndf
-            a_np, h_np = s[3 : 3 + P], s[3 + P :]
+            chi2 = init_chi2 + float(s[1]) / self.ndf if self.precise else float(s[1]) / self.ndf
+            a_np, h_np = s[4 : 4 + P], s[4 + P :]
             if not np.isfinite(chi2):
                 self.Lup()
                 if direction == "better":
@@ -1024,7 +1174,8 @@ class SceneLM:
                 continue
             if chi2 < best[1]:
                 best = (ha, chi2, self.L)
-                self._Yb.copy_(Y1)
+                if not self.precise:
+                    self._Yb.copy_(Y1)
                 nostep = False
                 self.Ldn()
                 if self.L <= 1e-8 or direction == "worse":
@@ -1041,9 +1192,11 @@ class SceneLM:
                 break
         if nostep:
             if scarry_best[0] is not None:
+                self._drift += self.DIFF_REL_ERR * abs(scarry_best[1] - init_chi2)
                 return scarry_best[0], scarry_best[1], scarry_best[2], False
             raise OptimizeStop("Could not find step to improve chi^2")
-        return best[0], best[1], best[2], True
+        self._drift += self.DIFF_REL_ERR * abs(best[1] - init_chi2)
+        return best[0], best[1], best[2], not self.precise
 
     def _fit_device(self):
         sc = self.scene
@@ -1052,7 +1205,9 @@ class SceneLM:
         self._xd = torch.tensor(self.x, dtype=torch.float64, device=dev)
         self._Y0 = torch.empty(sc.nx * sc.ny, dtype=torch.float32, device=dev)
         self._Yb = torch.empty_like(self._Y0)
-        self._status = torch.zeros(3 + 2 * sc.P, dtype=torch.float64, device=dev)
+        self._status = torch.zeros(4 + 2 * sc.P, dtype=torch.float64, device=dev)
+        self._zero = torch.zeros(sc.nx * sc.ny, dtype=torch.float32, device=dev)
+        self._drift = 0.0
         self.trials = self.geodesic_trials = self.base_renders = self.fp64_retries = 0
         self._Y0.copy_(sc.forward_device(self._xd))
         sc.chi2_into(self._Y0, self._status[1:2])

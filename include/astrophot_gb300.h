@@ -188,6 +188,24 @@ int ap_jacobian(ap_batch* batch, const double* params, const float* psf, float* 
 int ap_render_psf_derivative(ap_batch* batch, const double* params, const float* psf, const float* dpsf,
                              float* model, ap_stream_t stream);
 
+/* Renders for damping trials that must compare chi^2 values closer than one float32 render's
+ * rounding (a joint LM near its optimum, where the reference's float64 chi^2 still sees the
+ * change).  mode AP_RENDER_BASE: model = ap_render's model, and the evaluation (its constants,
+ * shifted kernel, deep image and integration pattern) is recorded in `base`.  mode
+ * AP_RENDER_DIFFERENCE: model = the render at params minus the recorded base render, each
+ * sample's difference formed from the exact parameter differences (a pixel whose integration
+ * pattern changed is differenced from the rounded values), so the change is accurate relative
+ * to itself, not to the model.  base: device buffer of ap_render_base_bytes bytes, 16-byte
+ * aligned, one per parameter set rendered on the batch (a second BASE overwrites it).  Sersic
+ * and exponential batches only (AP_ERR_UNSUPPORTED otherwise).  Replaces, for the joint fit
+ * of many sources, the float64 trial renders of LM.step (astrophot/fit/lm.py:270-300), like
+ * the batched LM's precise_trials. */
+#define AP_RENDER_BASE 1
+#define AP_RENDER_DIFFERENCE 2
+int ap_render_base_bytes(const ap_batch* batch, int64_t* bytes);
+int ap_render_precise(ap_batch* batch, const double* params, const float* psf, float* model, void* base,
+                      int64_t base_bytes, int32_t mode, ap_stream_t stream);
+
 /* A PSF model's normalisation (PSF_Model.sample, normalize_psf: the image divided by its sum,
  * astrophot/models/psf_model_object.py:250-252) and its derivative: out = img / S and
  * dout[c] = (dimg[c] - out sum dimg[c]) / S for n_dir <= 8 directions, S = sum img (float64
@@ -376,9 +394,15 @@ typedef struct ap_scene_source {
 
 /* image = sky + sum of the sources' renders inside their own windows.  tile_ptr / tile_src: for
  * every 32 x 32 image tile (row-major, ceil(nx/32) per row) the sources whose windows touch it
- * (CSR; the order fixes the summation order). */
+ * (CSR; the order fixes the summation order).  sky: a locked flat sky (counts per pixel), used
+ * when sky_F is NULL; sky_F: device pointer to a free flat sky's log10 brightness F (float64),
+ * the sky then being area * 10^F per pixel (the reference's FlatSky, astrophot/models/flatsky_model.py:55),
+ * computed in float64 from the staged F at every launch.  With sky_F0 (device, float64) too,
+ * the renders in fwd are differences (AP_RENDER_DIFFERENCE) and the sky term is the sky's own
+ * difference area * 10^F0 * (10^(F - F0) - 1), formed without cancellation. */
 int ap_scene_forward(const ap_scene_source* sources, const int32_t* tile_ptr, const int32_t* tile_src,
-                     const float* fwd, float sky, int32_t nx, int32_t ny, float* image, ap_stream_t stream);
+                     const float* fwd, float sky, const double* sky_F, const double* sky_F0, double area,
+                     int32_t nx, int32_t ny, float* image, ap_stream_t stream);
 /* out[ny][nx] = J h (h[P] float64), own windows, same tile lists. */
 int ap_scene_jvp(const ap_scene_source* sources, const int32_t* tile_ptr, const int32_t* tile_src,
                  const float* jac, const double* h, int32_t nx, int32_t ny, float* out, ap_stream_t stream);
@@ -395,6 +419,12 @@ int ap_scene_hess(const ap_scene_source* sources, const int32_t* pairs, int32_t 
  * order, so the result has the same bits on every run. */
 int ap_scene_chi2(const float* model, const float* data, const float* weight, const uint8_t* mask,
                   int64_t n, double* out, double* parts, int32_t n_parts, ap_stream_t stream);
+/* out[0] = sum over unmasked pixels of W dm (dm - 2 (data - base)): the change of chi^2 from
+ * the model `base` to base + dm, for a difference image dm (float64 per pixel; the same
+ * fixed-order partial sums as ap_scene_chi2, parts likewise). */
+int ap_scene_chi2_change(const float* dm, const float* base, const float* data, const float* weight,
+                         const uint8_t* mask, int64_t n, double* out, double* parts, int32_t n_parts,
+                         ap_stream_t stream);
 /* r = W (data - model) on unmasked pixels, 0 on masked ones (LM._r, fit/lm.py:381-385). */
 int ap_scene_residual(const float* model, const float* data, const float* weight,
                       const uint8_t* mask, int64_t n, float* r, ap_stream_t stream);

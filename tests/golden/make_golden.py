@@ -9,6 +9,7 @@ Run with ``ASTROPHOT_REFERENCE=<path of the reference checkout>`` set:
     python tests/golden/make_golden.py auxpsf   # only the live-PSF-model case
     python tests/golden/make_golden.py center   # only the centre-supersampling cases
     python tests/golden/make_golden.py psfstamps  # only the Moffat / Gaussian PSF stamps
+    python tests/golden/make_golden.py freesky    # only the group with a free flat sky
 
 The reference (AstroPhot 0.x) is imported through a ``sys.modules`` shim for
 the optional packages it imports at module level but never calls on this
@@ -449,6 +450,10 @@ GROUP_CASES = {
     # "full" with a 25 x 25 Moffat.  Recorded: model, representation Jacobian (linked columns
     # merged), vector names, and an LM trajectory.
     "group_linked_96": dict(size=96, seed=13, psf=MOFFAT_25, max_iter=12),
+    # the same group with its flat sky free (F = 0.3 in the truth, started at 0.22): the sky's
+    # F is the last entry of the joint vector, its Jacobian column image-wide
+    "group_freesky_96": dict(size=96, seed=19, psf=MOFFAT_25, max_iter=12, sky_free=True, sky_F_truth=0.3,
+                             sky_F_init=0.22),
 }
 
 GROUP_SOURCES = (
@@ -476,7 +481,7 @@ def group_init_values(vals):
     return (cx + 0.8, cy - 0.6, min(q * 1.1, 0.95), PA + 0.1, n * 0.85, Re * 1.15, Ie - 0.1)
 
 
-def build_group(ap, target, values, tag, psf_mode="full"):
+def build_group(ap, target, values, tag, psf_mode="full", sky_F=0.0, sky_free=False):
     models = {}
     for (name, kind, window, _, link), vals in zip(GROUP_SOURCES, values):
         m = ap.models.AstroPhot_Model(name=f"{tag} {name}", model_type=f"{kind} galaxy model", target=target,
@@ -485,7 +490,7 @@ def build_group(ap, target, values, tag, psf_mode="full"):
             m.parameters["center"].value = models[link].parameters["center"]
         models[name] = m
     sky = ap.models.AstroPhot_Model(name=f"{tag} sky", model_type="flat sky model", target=target,
-                                    parameters={"F": {"value": 0.0, "locked": True}})
+                                    parameters={"F": {"value": sky_F, "locked": not sky_free}})
     sky.initialize()  # sets the (unused) sky centre the sampler reads
     group = ap.models.AstroPhot_Model(name=f"{tag} group", model_type="group model", target=target,
                                       models=list(models.values()) + [sky], psf_mode=psf_mode)
@@ -497,12 +502,14 @@ def run_group_case(ap, key, case):
     psf = psf_array(case["psf"])
     target = ap.image.Target_Image(data=np.zeros((N, N)), pixelscale=1.0, psf=psf)
     truth_vals = [src[3] for src in GROUP_SOURCES]
-    truth_group = build_group(ap, target, truth_vals, f"{key} truth")
+    sky_free = bool(case.get("sky_free", False))
+    truth_group = build_group(ap, target, truth_vals, f"{key} truth", sky_F=case.get("sky_F_truth", 0.0),
+                              sky_free=sky_free)
     truth_img = truth_group().data.detach().cpu().numpy()
     data, weight = synthetic.add_noise(truth_img, case["seed"])
     target = ap.image.Target_Image(data=data, pixelscale=1.0, psf=psf, variance=1.0 / weight)
     init_vals = [group_init_values(v) for v in truth_vals]
-    group = build_group(ap, target, init_vals, key)
+    group = build_group(ap, target, init_vals, key, sky_F=case.get("sky_F_init", 0.0), sky_free=sky_free)
     init_img = group().data.detach().cpu().numpy()
     jac = group.jacobian(as_representation=True).data.detach().cpu().numpy()
     names = [str(n) for n in group.parameters.vector_names()]
@@ -842,6 +849,12 @@ def run_psf_stamps(ap):
 def main():
     ap = import_reference()
     only = sys.argv[1] if len(sys.argv) > 1 else None
+    if only == "freesky":
+        key = "group_freesky_96"
+        out = run_group_case(ap, key, GROUP_CASES[key])
+        np.savez_compressed(os.path.join(HERE, f"{key}.npz"), **out)
+        print("group", key, out["names"], out["jac_rep"].shape, out["loss_history"], str(out["message"]))
+        return
     if only == "psfstamps":
         out = run_psf_stamps(ap)
         np.savez_compressed(os.path.join(HERE, "psf_stamps.npz"), **out)

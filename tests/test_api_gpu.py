@@ -184,7 +184,8 @@ GROUP_SOURCES = (
 )
 
 
-def build_group(ap, target, values, tag):
+def build_group(ap, target, values, tag, spec=None):
+    spec = spec or {}
     models = {}
     for (name, kind, window, link), v in zip(GROUP_SOURCES, values):
         cx, cy, q, PA, n, Re, Ie = [float(x) for x in v]
@@ -198,8 +199,9 @@ def build_group(ap, target, values, tag):
         if link is not None:
             m.parameters["center"].value = models[link].parameters["center"]
         models[name] = m
+    free = bool(spec.get("sky_free", False))
     sky = ap.models.AstroPhot_Model(name=f"{tag} sky", model_type="flat sky model", target=target,
-                                    parameters={"F": {"value": 0.0, "locked": True}})
+                                    parameters={"F": {"value": spec.get("sky_F_init", 0.0), "locked": not free}})
     sky.initialize()
     return ap.models.AstroPhot_Model(name=f"{tag} group", model_type="group model", target=target,
                                      models=list(models.values()) + [sky], psf_mode="full")
@@ -210,7 +212,7 @@ def test_multi_galaxy_group_matches_reference(ap, name):
     """Windows per galaxy, a linked centre, PSF: model, representation Jacobian and LM."""
     d = cases.load_group(name)
     target = ap.image.Target_Image(data=d["data"], pixelscale=1.0, psf=d["psf"], variance=1.0 / d["weight"])
-    grp = build_group(ap, target, d["init_values"], f"api {name}")
+    grp = build_group(ap, target, d["init_values"], f"api {name}", d["spec"])
     assert list(grp.parameters.vector_names()) == [str(n) for n in d["names"]]
     assert np.allclose(grp.parameters.vector_representation().numpy(), d["rep0"], atol=1e-12)
     assert close(grp().data.numpy(), d["init_model"])

@@ -27,10 +27,14 @@ LINKS = (None, 0, None, None)
 
 
 def golden_scene(S, d, values=None):
+    """The golden group as a scene: a locked sky of 10^0 = 1 per pixel, or a free flat sky
+    (F last in the joint vector, after the galaxies)."""
     values = d["init_values"] if values is None else values
     srcs = [S.SceneSource(k, list(v), w, l) for k, v, w, l in zip(KINDS, values, WINDOWS, LINKS)]
-    N = d["spec"]["size"]
-    return S.Scene(N, N, srcs, d["psf"], d["data"], d["weight"], sky=1.0)
+    spec = d["spec"]
+    N = spec["size"]
+    sky = dict(sky_F=spec["sky_F_init"]) if spec.get("sky_free") else dict(sky=1.0)
+    return S.Scene(N, N, srcs, d["psf"], d["data"], d["weight"], **sky)
 
 
 @pytest.mark.parametrize("name", cases.group_case_names())
@@ -38,7 +42,7 @@ def test_scene_model_and_jacobian_match_reference(S, name):
     d = cases.load_group(name)
     sc = golden_scene(S, d)
     rep0 = sc.representation()
-    assert sc.P == 25
+    assert sc.P == len(d["names"])
     assert np.allclose(rep0, d["rep0"], rtol=0, atol=1e-12)
     m = sc.forward(rep0).cpu().numpy().reshape(d["init_model"].shape)
     ref = d["init_model"]
@@ -159,6 +163,8 @@ def test_device_staging_equals_host_staging(S, name):
     sc._stage_dev(torch.tensor(rep0, device="cuda"), torch.tensor(v, device="cuda"), alpha)
     dev = sc._stage_d.clone()
     used = sc._stage_rows() >= 0
+    if sc.sky_free:
+        used[sc._sky_row] = True  # the free sky's F in cell 0 of its row
     assert torch.allclose(dev[used], host[used], rtol=4e-16, atol=0)
     # without the direction vector
     sc._stage_dev(torch.tensor(x, device="cuda"))
@@ -171,12 +177,57 @@ def test_scene_lm_device_loop_equals_host_loop(S, name):
     loop's steps: the same message, iterations, loss history and fitted vector."""
     d = cases.load_group(name)
     a = S.SceneLM(golden_scene(S, d), max_iter=d["spec"]["max_iter"], device_loop=False).fit()
-    b = S.SceneLM(golden_scene(S, d), max_iter=d["spec"]["max_iter"], device_loop=True).fit()
+    b = S.SceneLM(golden_scene(S, d), max_iter=d["spec"]["max_iter"], device_loop=True,
+                  precise_trials=False).fit()
     assert b.device_loop and not a.device_loop
     assert a.message == b.message and a.iterations == b.iterations
     np.testing.assert_allclose(b.loss_history, a.loss_history, rtol=1e-9)
     np.testing.assert_allclose(b.L_history, a.L_history, rtol=0)
     np.testing.assert_allclose(b.res(), a.res(), rtol=1e-9, atol=1e-12)
+
+
+@pytest.mark.parametrize("name", cases.group_case_names())
+def test_difference_render_is_precise(S, name):
+    """A trial rendered as its difference to the recorded base render against the float64
+    oracle's difference, for a change far below float32's resolution of the model (a free sky's
+    term included): the plain float32 renders' difference misses it by orders of magnitude more.
+    The base point moves every centre off the golden's whole and half pixels: a centre on a
+    half pixel rounds to the other pixel under the smallest step (the model jumps there, in the
+    reference too), and one on a pixel centre has a zero sub-pixel shift, whose kernel change is
+    formed by subtraction."""
+    from test_oracle_golden import group_problem
+
+    d = cases.load_group(name)
+    sc = golden_scene(S, d)
+    rep0 = sc.representation()
+    centre = np.array([str(n).startswith("center") for n in d["names"]])
+    rep0 = rep0 + np.where(centre, 0.137, 0.0)
+    rng = np.random.default_rng(7)
+    v = rng.normal(size=sc.P)
+    v /= np.linalg.norm(v)
+    alpha = 1e-6
+    sc.set_stage_base(rep0)
+    x, vd = torch.tensor(rep0, device="cuda"), torch.tensor(v, device="cuda")
+    Y0 = sc.forward_base_device(x).clone()
+    assert torch.equal(Y0, sc.forward_device(x))  # the base render is the plain render
+    dY = sc.forward_diff_device(x, vd, alpha).double().cpu().numpy()
+    Y1 = sc.forward_device(x, vd, alpha).double().cpu().numpy()
+    prob = group_problem(d)
+    assert np.allclose(prob.representation() + np.where(centre, 0.137, 0.0), rep0, rtol=0, atol=1e-12)
+    want = prob.forward(rep0 + alpha * v) - prob.forward(rep0)
+    scale = np.max(np.abs(want))
+    err = np.max(np.abs(dY - want)) / scale
+    err_plain = np.max(np.abs(Y1 - Y0.double().cpu().numpy() - want)) / scale
+    print(name, err, err_plain)
+    assert err <= 1e-3 and err <= err_plain / 10, (err, err_plain)
+    # chi^2's change W dm (dm - 2 (data - base)) summed in float64 from the float32 images
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    sc.chi2_change_into(sc.forward_diff_device(x, vd, alpha), Y0, out)
+    W = d["weight"].reshape(-1).astype(np.float32).astype(np.float64)
+    D = d["data"].reshape(-1).astype(np.float32).astype(np.float64)
+    y0 = Y0.double().cpu().numpy()
+    dchi2 = np.sum(W * dY * (dY - 2 * (D - y0)))
+    assert abs(float(out.item()) - dchi2) <= 1e-9 * np.sum(np.abs(W * dY * (dY - 2 * (D - y0))))
 
 
 def test_scene_with_mask_and_no_psf_matches_oracle(S):

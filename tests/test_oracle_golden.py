@@ -251,8 +251,9 @@ def test_reverse_mode_center_gradient_is_shift_plus_coordinate_path():
 # ---- Group_Model with per-component windows and a linked centre ------------------------------
 
 
-def group_problem(d, values=None):
-    """The group of ``tests/golden/make_golden.py`` GROUP_SOURCES on the oracle."""
+def group_problem(d, values=None, truth=False):
+    """The group of ``tests/golden/make_golden.py`` GROUP_SOURCES on the oracle (its flat sky
+    locked at F = 0, or free from the case's initial / truth F)."""
     sources = (
         ("sersic", ((8, 72), (10, 74)), None),
         ("exponential", ((8, 72), (10, 74)), 0),
@@ -269,8 +270,12 @@ def group_problem(d, values=None):
         comps.append(Component(kind, p, psf_mode="full", window=win))
         if link is not None:
             links[(ci, "center")] = (link, "center")
-    comps.append(Component("flat_sky", {"F": 0.0}, locked=("F",)))
-    N = d["spec"]["size"]
+    spec = d["spec"]
+    if spec.get("sky_free"):
+        comps.append(Component("flat_sky", {"F": spec["sky_F_truth" if truth else "sky_F_init"]}))
+    else:
+        comps.append(Component("flat_sky", {"F": 0.0}, locked=("F",)))
+    N = spec["size"]
     return GroupProblem(comps, Window.from_scale(N, N), PSF(d["psf"]), d["data"], d["weight"], links=links)
 
 
@@ -279,11 +284,11 @@ def test_group_windows_links_match_reference(name):
     d = cases.load_group(name)
     prob = group_problem(d)
     rep0 = prob.representation()
-    assert len(rep0) == len(d["names"]) == 25
+    assert len(rep0) == len(d["names"]) == 25 + bool(d["spec"].get("sky_free"))
     assert np.allclose(rep0, d["rep0"], rtol=0, atol=1e-13)
     m = prob.forward(rep0).reshape(d["init_model"].shape)
     assert np.max(np.abs(m - d["init_model"])) <= 1e-12 * np.max(np.abs(d["init_model"]))
-    truth = group_problem(d, d["truth_values"])
+    truth = group_problem(d, d["truth_values"], truth=True)
     mt = truth.forward(truth.representation()).reshape(d["truth_model"].shape)
     assert np.max(np.abs(mt - d["truth_model"])) <= 1e-12 * np.max(np.abs(d["truth_model"]))
     J = prob.jacobian(rep0).reshape(d["jac_rep"].shape)
