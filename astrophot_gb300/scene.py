@@ -940,16 +940,22 @@ class SceneLM:
     def __init__(self, scene: Scene, initial_state=None, max_iter: int = 100, relative_tolerance: float = 1e-5,
                  max_step_iter: int = 10, curvature_limit: float = 1.0, Lup: float = 11.0, Ldn: float = 9.0,
                  L0: float = 1.0, acceleration: float = 0.0, ndf=None, free=None, device_loop: bool = True,
-                 precise_trials: bool = True):
+                 precise_trials: bool = True, precise_below: float = 1e-2):
         self.scene = scene
         # device_loop: the vectors stay on the device, parameters are staged there, each damping
         # trial reads one status back (scenes without a live PSF); else the host loop below
         self.device_loop = bool(device_loop) and scene.device_staging
-        # precise_trials (device loop): every step renders its base point once more, recording it,
-        # and each trial (and the geodesic render) as its difference to that base, so chi^2 changes
-        # far below one float32 render's rounding still order the trials as the reference's float64
-        # chi^2 does; the trial chi^2 is the step's chi^2 plus the change
+        # precise_trials (device loop): once an accepted step lowers chi^2 by less than
+        # precise_below (relative; inf: from the first step) or finds no better trial, every step
+        # renders its base point once more, recording it, and each trial (and the geodesic render)
+        # as its difference to that base, so chi^2 changes far below one float32 render's rounding
+        # (~1e-7 relative) still order the trials as the reference's float64 chi^2 does; the trial
+        # chi^2 is then the step's chi^2 plus the change.  Before, trials are full float32 renders:
+        # while steps gain more than 1 % the damping is large enough that its trials' chi^2 differ
+        # by far more than the rounding, and the accepted trial's render is the next base image.
         self.precise = bool(precise_trials) and self.device_loop and scene.precise_capable
+        self.precise_below = float(precise_below)
+        self._diff = False   # trials rendered as differences in the current step
         self.x = np.array(scene.representation() if initial_state is None else initial_state, dtype=np.float64)
         self.free = None if free is None else np.asarray(free, dtype=np.int64)
         self._free_t = None if free is None else torch.as_tensor(self.free, device=scene.device)
@@ -1073,10 +1079,12 @@ class SceneLM:
         if self.L > 1e-4:
             # the geodesic term from the render at x + d h (skipped at L <= 1e-4, where
             # fit/lm.py:277-286 computes it and then discards it); it needs only W (Y1 - Y0)
-            if self.precise:
+            if self._diff:
                 rh = sc.residual(self._zero, sc.forward_diff_device(x, h, d))   # W (Y1 - Y0)
                 rpp = self._sub(sc.jt(sc.rpp_image(self._zero, rh, sc.jvp(h), d)))
+                self.diff_renders += 1
             else:
+                self.full_renders += 1
                 Y1 = sc.forward_device(x, h, d)
                 rh = sc.residual(sc.data, Y1)   # W (Y1 - Y)
                 rpp = self._sub(sc.jt(sc.rpp_image(r, rh, sc.jvp(h), d)))
@@ -1087,10 +1095,12 @@ class SceneLM:
             sc._info2.zero_()
         ha = torch.add(h, torch.mul(a, self.acceleration))
         st = self._status
-        if self.precise:
+        if self._diff:
             Y1 = sc.forward_diff_device(x, ha, 1.0)      # Y(x + ha) - Y0
             sc.chi2_change_into(Y1, self._Y0, st[1:2])
+            self.diff_renders += 1
         else:
+            self.full_renders += 1
             Y1 = sc.forward_device(x, ha, 1.0)
             sc.chi2_into(Y1, st[1:2])
         st[0:1].copy_(sc._info)
@@ -1108,7 +1118,7 @@ class SceneLM:
         sc = self.scene
         x = self._xd
         P = sc.P
-        if self.precise:
+        if self._diff:
             # the base point of this step's difference trials; its full chi^2 travels with the
             # first trial's status and re-anchors the chain of changes once that has drifted
             self._Y0.copy_(sc.forward_base_device(x))
@@ -1142,7 +1152,7 @@ class SceneLM:
                 # the mixed-precision solve did not converge: the trial again, in float64
                 self.fp64_retries += 1
                 ha, Y1, s = self._trial(hess, grad, r, d, mixed=False)
-            if self.precise and iteration == 0:
+            if self._diff and iteration == 0:
                 full = float(s[3]) / self.ndf
                 if self._drift > self.FULL_REL_ERR * full:
                     init_chi2 = full
@@ -1155,7 +1165,7 @@ class SceneLM:
                     break
                 direction = "worse"
                 continue
-            chi2 = init_chi2 + float(s[1]) / self.ndf if self.precise else float(s[1]) / self.ndf
+            chi2 = init_chi2 + float(s[1]) / self.ndf if self._diff else float(s[1]) / self.ndf
             a_np, h_np = s[4 : 4 + P], s[4 + P :]
             if not np.isfinite(chi2):
                 self.Lup()
@@ -1174,7 +1184,7 @@ class SceneLM:
                 continue
             if chi2 < best[1]:
                 best = (ha, chi2, self.L)
-                if not self.precise:
+                if not self._diff:
                     self._Yb.copy_(Y1)
                 nostep = False
                 self.Ldn()
@@ -1196,7 +1206,7 @@ class SceneLM:
                 return scarry_best[0], scarry_best[1], scarry_best[2], False
             raise OptimizeStop("Could not find step to improve chi^2")
         self._drift += self.DIFF_REL_ERR * abs(best[1] - init_chi2)
-        return best[0], best[1], best[2], not self.precise
+        return best[0], best[1], best[2], not self._diff
 
     def _fit_device(self):
         sc = self.scene
@@ -1208,6 +1218,8 @@ class SceneLM:
         self._status = torch.zeros(4 + 2 * sc.P, dtype=torch.float64, device=dev)
         self._zero = torch.zeros(sc.nx * sc.ny, dtype=torch.float32, device=dev)
         self._drift = 0.0
+        self._diff = self.precise and self.precise_below == float("inf")
+        self.diff_steps = self.diff_renders = self.full_renders = 0
         self.trials = self.geodesic_trials = self.base_renders = self.fp64_retries = 0
         self._Y0.copy_(sc.forward_device(self._xd))
         sc.chi2_into(self._Y0, self._status[1:2])
@@ -1218,10 +1230,14 @@ class SceneLM:
         for iteration in range(self.max_iter):
             self.iterations = iteration + 1
             try:
+                self.diff_steps += int(self._diff)
                 step, chi2, L, at_best = self._step_device(self.loss_history[-1], have_y0)
             except OptimizeStop:
                 self.message = self.message + "fail. Could not find step to improve Chi^2"
                 break
+            if self.precise and not self._diff and (
+                    not at_best or (self.loss_history[-1] - chi2) < self.precise_below * chi2):
+                self._diff = True   # from the next step on, trials as differences
             self.L = L
             self._xd = self._xd + step
             if at_best:  # the model at the new x is the accepted trial's render

@@ -1410,6 +1410,20 @@ def crowded_block(args, dev):
     # the reference's default mode "fft": FFT where it is faster for the kernel size, else direct
     sc = SC.Scene(size, size, src_i, psf, data, weight, sky=sky, device=dev, options={"psf_convolve_mode": "fft"})
     fwd_ms, jac_ms, H = timed(sc, rep)
+    # a damping trial rendered as its difference to the recorded base render
+    xd = torch.tensor(rep, device=dev)
+    vd = torch.tensor(np.random.default_rng(args.seed).normal(size=sc.P) * 1e-3, device=dev)
+    sc.set_stage_base(rep)
+    sc.forward_base_device(xd)
+    for _ in range(2):
+        sc.forward_diff_device(xd, vd, 1.0)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        sc.forward_diff_device(xd, vd, 1.0)
+    e1.record()
+    torch.cuda.synchronize()
+    diff_ms = e0.elapsed_time(e1) / reps
     chi2_d = float(sc.chi2(sc.forward(rep)))
     g = sc.jt(sc.residual(sc.forward(rep)))
     torch.cuda.synchronize()
@@ -1449,10 +1463,11 @@ def crowded_block(args, dev):
     torch.cuda.synchronize()
     lm_host_s = time.perf_counter() - t0
     # device time the LM's work takes at the kernel times measured above: a Jacobian + J^T W J
-    # per iteration, a damped solve and a render per trial, a second render for the geodesic
-    # term, the base renders not taken from an accepted trial
-    floor_ms = (lm.iterations * jac_ms + lm.trials * (solve_ms + fwd_ms) + lm.geodesic_trials * fwd_ms
-                + (1 + lm.base_renders) * fwd_ms)
+    # per iteration, a damped solve per trial, its render and the geodesic term's (full or as a
+    # difference), the base renders (every difference step's, and those not taken from an
+    # accepted trial)
+    floor_ms = (lm.iterations * jac_ms + lm.trials * solve_ms + lm.full_renders * fwd_ms
+                + lm.diff_renders * diff_ms + (1 + lm.base_renders) * fwd_ms)
     out = {
         "workload": f"{n_src} Sersic galaxies on a {size}x{size} image, 51x51 Gaussian PSF (sigma 2; mode fft: "
         "the convolution takes the faster of FFT and direct for the kernel size, direct at 53x53), sky 5.0, "
@@ -1462,6 +1477,7 @@ def crowded_block(args, dev):
         "window_pairs": sc.n_pairs,
         "render_ms": fwd_ms,
         "render_mpix_per_s": size * size / (fwd_ms * 1e-3) / 1e6,
+        "difference_render_ms": diff_ms,
         "jacobian_build_ms": jac_ms,
         "all_fft_convolution": {"render_ms": fwd_f, "jacobian_build_ms": jac_f,
                                 "chi2_rel_diff_vs_direct": abs(chi2_f / chi2_d - 1)},
@@ -1474,10 +1490,12 @@ def crowded_block(args, dev):
         "lm_seconds": lm_s,
         "lm_ms_per_iteration": lm_s * 1e3 / max(lm.iterations, 1),
         "lm_damping_trials": lm.trials,
+        "lm_difference_steps": lm.diff_steps,
         "lm_geodesic_trials": lm.geodesic_trials,
         "lm_kernel_floor_ms_per_iteration": floor_ms / max(lm.iterations, 1),
         "lm_loop": "device vectors, parameters staged on the device, one status read per damping trial; "
-                   "trials and geodesic renders as differences to the step's recorded base render",
+                   "once a step gains less than 1 %, trials and geodesic renders as differences to the "
+                   "step's recorded base render",
         "lm_full_trials_ms_per_iteration": lm_plain_s * 1e3 / max(lm_p.iterations, 1),
         "lm_full_trials_iterations": lm_p.iterations,
         "lm_full_trials_message": lm_p.message,
