@@ -825,10 +825,11 @@ def _scene_spec(owner, components):
             # before the sky (the group's parameter order follows its model list)
             sky_free = dict(sky_F=float(F.value.item()),
                             sky_after=sum(1 for c in components[: components.index(skies[0])] if c in gals))
+    # the scene's settings are the first galaxy's; a galaxy whose own differ carries them as its
+    # source's options (its own stamp batch).  The PSF mode and the PSF are shared.
     knobs = {k: getattr(gals[0], k) for k in _KNOBS}
-    for g in gals[1:]:
-        if any(getattr(g, k) != knobs[k] for k in _KNOBS):
-            raise NotImplementedError("galaxies of one group must share their sampling / PSF settings on the CUDA path")
+    if any(g.psf_mode != knobs["psf_mode"] for g in gals[1:]):
+        raise NotImplementedError("galaxies of one group must share their psf_mode on the CUDA path")
     psf = gals[0].psf if knobs["psf_mode"] == "full" else None
     if psf is not None and any(g.psf is not psf for g in gals[1:]):
         raise NotImplementedError("galaxies of one group must share one PSF on the CUDA path")
@@ -854,7 +855,8 @@ def _scene_spec(owner, components):
                        for sl in slots if p[name].locked and not (name == "center" and link is not None))
         di, dj = g.window.offset_in(w)
         win = ((di, di + int(g.window.pixel_shape[0])), (dj, dj + int(g.window.pixel_shape[1])))
-        sources.append(SceneSource(g.profile, vals, win, link, locked))
+        own = {k: getattr(g, k) for k in _KNOBS if k != "psf_mode" and getattr(g, k) != knobs[k]}
+        sources.append(SceneSource(g.profile, vals, win, link, locked, options=own or None))
     opts = {k: knobs[k] for k in _KNOBS if k != "psf_mode"}
     return w, sources, psf, sky, sky_free, opts
 

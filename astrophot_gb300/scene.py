@@ -159,13 +159,16 @@ class SceneSource:
     """One galaxy: ``kind`` "sersic" or "exponential", value-space ``params``
     [cx, cy, q, PA, n, Re, Ie] (n ignored for exponential), pixel ``window``
     ((x0, x1), (y0, y1)) or None for the whole image, ``link_center`` = index of the source
-    whose centre node this one shares, ``locked`` = full-vector slots held fixed."""
+    whose centre node this one shares, ``locked`` = full-vector slots held fixed, ``options`` =
+    this source's own sampling settings over the scene's (sampling_mode, integrate_mode, ...:
+    each model of a reference group samples with its own, models/model_object.py:64-95)."""
 
     kind: str
     params: Sequence[float]
     window: Optional[tuple] = None
     link_center: Optional[int] = None
     locked: tuple = ()
+    options: Optional[dict] = None
 
 
 class Scene:
@@ -244,18 +247,21 @@ class Scene:
         self.n_img = self.n_psf + (1 if self.sky_free else 0)
         self.ndf = max(1.0, n_used - self.P)
 
-        # ---- stamp batches, one per (kind, fitted slots) --------------------------------------
+        # ---- stamp batches, one per (kind, fitted slots, sampling settings) --------------------
         self.groups = {}
         for si, src in enumerate(self.sources):
             free = tuple(sl for sl in _SLOTS_OF[src.kind] if sl not in src.locked)
-            self.groups.setdefault((src.kind, free), []).append(si)
+            own = tuple(sorted((src.options or {}).items()))
+            if any(k == "psf_mode" for k, _ in own):
+                raise ValueError("a scene's sources share its PSF: psf_mode is not a per-source option")
+            self.groups.setdefault((src.kind, free, own), []).append(si)
         kpsf = None if psf is None else (self.psf_np.shape[1], self.psf_np.shape[0])
         self._jac_parts = []
         jac_total = 0
-        for (kind, free), members in self.groups.items():
+        for (kind, free, own), members in self.groups.items():
             mask_bits = sum(1 << sl for sl in free)
             o = N.make_options(profile=kind, psf_mode="full" if psf is not None else "none", free_mask=mask_bits,
-                               has_sky=False, **opts_kw)
+                               has_sky=False, **{**opts_kw, **dict(own)})
             shapes, geoms = [], []
             for si in members:
                 (x0, x1), (y0, y1) = self._window(si)
@@ -286,9 +292,10 @@ class Scene:
             bx, by = int(math.ceil((1 + kx_) / 2)), int(math.ceil((1 + ky_) / 2))
         group_numel = float((self.nx + 2 * bx) * (self.ny + 2 * by))
         fwd_total = 0
-        for (kind, free), members in self.groups.items():
+        for (kind, free, own), members in self.groups.items():
             fo = N.make_options(profile=kind, psf_mode="full" if psf is not None else "none",
-                                free_mask=sum(1 << sl for sl in _SLOTS_OF[kind]), has_sky=False, **opts_kw)
+                                free_mask=sum(1 << sl for sl in _SLOTS_OF[kind]), has_sky=False,
+                                **{**opts_kw, **dict(own)})
             if kind in ("sersic", "exponential"):
                 shapes, geoms, gwin = [], [], []
                 for si in members:

@@ -10,6 +10,7 @@ Run with ``ASTROPHOT_REFERENCE=<path of the reference checkout>`` set:
     python tests/golden/make_golden.py center   # only the centre-supersampling cases
     python tests/golden/make_golden.py psfstamps  # only the Moffat / Gaussian PSF stamps
     python tests/golden/make_golden.py freesky    # only the group with a free flat sky
+    python tests/golden/make_golden.py knobs      # only the group with per-galaxy sampling settings
 
 The reference (AstroPhot 0.x) is imported through a ``sys.modules`` shim for
 the optional packages it imports at module level but never calls on this
@@ -454,6 +455,12 @@ GROUP_CASES = {
     # F is the last entry of the joint vector, its Jacobian column image-wide
     "group_freesky_96": dict(size=96, seed=19, psf=MOFFAT_25, max_iter=12, sky_free=True, sky_F_truth=0.3,
                              sky_F_init=0.22),
+    # the group with different sampling settings per galaxy (model attributes, per source in
+    # GROUP_SOURCES order): the disk sampled by Simpson's rule, the east galaxy without adaptive
+    # integration, the south galaxy by 3 x 3 Gauss-Legendre quadrature
+    "group_knobs_96": dict(size=96, seed=23, psf=MOFFAT_25, max_iter=12,
+                           knobs=[{}, {"sampling_mode": "simpsons"}, {"integrate_mode": "none"},
+                                  {"sampling_mode": "quad:3"}]),
 }
 
 GROUP_SOURCES = (
@@ -481,11 +488,13 @@ def group_init_values(vals):
     return (cx + 0.8, cy - 0.6, min(q * 1.1, 0.95), PA + 0.1, n * 0.85, Re * 1.15, Ie - 0.1)
 
 
-def build_group(ap, target, values, tag, psf_mode="full", sky_F=0.0, sky_free=False):
+def build_group(ap, target, values, tag, psf_mode="full", sky_F=0.0, sky_free=False, knobs=None):
     models = {}
-    for (name, kind, window, _, link), vals in zip(GROUP_SOURCES, values):
+    for i, ((name, kind, window, _, link), vals) in enumerate(zip(GROUP_SOURCES, values)):
+        kw = dict(knobs[i]) if knobs else {}
         m = ap.models.AstroPhot_Model(name=f"{tag} {name}", model_type=f"{kind} galaxy model", target=target,
-                                      window=window, parameters=group_source_params(kind, vals, link is not None))
+                                      window=window, parameters=group_source_params(kind, vals, link is not None),
+                                      **kw)
         if link is not None:
             m.parameters["center"].value = models[link].parameters["center"]
         models[name] = m
@@ -503,13 +512,15 @@ def run_group_case(ap, key, case):
     target = ap.image.Target_Image(data=np.zeros((N, N)), pixelscale=1.0, psf=psf)
     truth_vals = [src[3] for src in GROUP_SOURCES]
     sky_free = bool(case.get("sky_free", False))
+    knobs = case.get("knobs")
     truth_group = build_group(ap, target, truth_vals, f"{key} truth", sky_F=case.get("sky_F_truth", 0.0),
-                              sky_free=sky_free)
+                              sky_free=sky_free, knobs=knobs)
     truth_img = truth_group().data.detach().cpu().numpy()
     data, weight = synthetic.add_noise(truth_img, case["seed"])
     target = ap.image.Target_Image(data=data, pixelscale=1.0, psf=psf, variance=1.0 / weight)
     init_vals = [group_init_values(v) for v in truth_vals]
-    group = build_group(ap, target, init_vals, key, sky_F=case.get("sky_F_init", 0.0), sky_free=sky_free)
+    group = build_group(ap, target, init_vals, key, sky_F=case.get("sky_F_init", 0.0), sky_free=sky_free,
+                        knobs=knobs)
     init_img = group().data.detach().cpu().numpy()
     jac = group.jacobian(as_representation=True).data.detach().cpu().numpy()
     names = [str(n) for n in group.parameters.vector_names()]
@@ -849,8 +860,8 @@ def run_psf_stamps(ap):
 def main():
     ap = import_reference()
     only = sys.argv[1] if len(sys.argv) > 1 else None
-    if only == "freesky":
-        key = "group_freesky_96"
+    if only in ("freesky", "knobs"):
+        key = {"freesky": "group_freesky_96", "knobs": "group_knobs_96"}[only]
         out = run_group_case(ap, key, GROUP_CASES[key])
         np.savez_compressed(os.path.join(HERE, f"{key}.npz"), **out)
         print("group", key, out["names"], out["jac_rep"].shape, out["loss_history"], str(out["message"]))

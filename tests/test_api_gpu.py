@@ -186,8 +186,9 @@ GROUP_SOURCES = (
 
 def build_group(ap, target, values, tag, spec=None):
     spec = spec or {}
+    knobs = spec.get("knobs") or [{}] * len(GROUP_SOURCES)
     models = {}
-    for (name, kind, window, link), v in zip(GROUP_SOURCES, values):
+    for (name, kind, window, link), v, kw in zip(GROUP_SOURCES, values, knobs):
         cx, cy, q, PA, n, Re, Ie = [float(x) for x in v]
         p = {"q": q, "PA": PA, "Re": Re, "Ie": Ie}
         if link is None:
@@ -195,7 +196,7 @@ def build_group(ap, target, values, tag, spec=None):
         if kind == "sersic":
             p["n"] = n
         m = ap.models.AstroPhot_Model(name=f"{tag} {name}", model_type=f"{kind} galaxy model", target=target,
-                                      window=window, parameters=p)
+                                      window=window, parameters=p, **kw)
         if link is not None:
             m.parameters["center"].value = models[link].parameters["center"]
         models[name] = m

@@ -28,10 +28,13 @@ LINKS = (None, 0, None, None)
 
 def golden_scene(S, d, values=None):
     """The golden group as a scene: a locked sky of 10^0 = 1 per pixel, or a free flat sky
-    (F last in the joint vector, after the galaxies)."""
+    (F last in the joint vector, after the galaxies); per-galaxy sampling settings as the
+    sources' options."""
     values = d["init_values"] if values is None else values
-    srcs = [S.SceneSource(k, list(v), w, l) for k, v, w, l in zip(KINDS, values, WINDOWS, LINKS)]
     spec = d["spec"]
+    knobs = spec.get("knobs") or [None] * len(KINDS)
+    srcs = [S.SceneSource(k, list(v), w, l, options=o or None)
+            for k, v, w, l, o in zip(KINDS, values, WINDOWS, LINKS, knobs)]
     N = spec["size"]
     sky = dict(sky_F=spec["sky_F_init"]) if spec.get("sky_free") else dict(sky=1.0)
     return S.Scene(N, N, srcs, d["psf"], d["data"], d["weight"], **sky)

@@ -261,13 +261,14 @@ def group_problem(d, values=None, truth=False):
         ("sersic", ((0, 44), (52, 96)), None),
     )
     values = d["init_values"] if values is None else values
+    knobs = d["spec"].get("knobs") or [{}] * len(sources)
     comps, links = [], {}
     for ci, ((kind, win, link), v) in enumerate(zip(sources, values)):
         cx, cy, q, PA, n, Re, Ie = v
         p = {"center": [cx, cy], "q": q, "PA": PA, "Re": Re, "Ie": Ie}
         if kind == "sersic":
             p["n"] = n
-        comps.append(Component(kind, p, psf_mode="full", window=win))
+        comps.append(Component(kind, p, psf_mode="full", window=win, **knobs[ci]))
         if link is not None:
             links[(ci, "center")] = (link, "center")
     spec = d["spec"]
