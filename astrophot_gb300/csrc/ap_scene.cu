@@ -226,6 +226,34 @@ __global__ void k_sum_parts(const double* __restrict__ part, int m, double* __re
   }
 }
 
+// ---- a PSF finer than the image: fine renders summed back in u x u blocks ----------------------
+// (Image.reduce after the crop of the working image, astrophot/image/image_object.py:348-376,
+// models/model_object.py:346-350).  One thread per (plane, coarse pixel); the stamp of a coarse
+// pixel by binary search over the coarse offsets.
+__global__ void k_reduce_upscaled(int n_stamps, const int64_t* __restrict__ in_off, const int64_t* __restrict__ out_off,
+                                  const int32_t* __restrict__ cnx, int u, int n_planes, const float* __restrict__ in,
+                                  int64_t in_stride, float* __restrict__ out, int64_t out_stride, int64_t out_total) {
+  const int64_t n = (int64_t)n_planes * out_total;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t pl = t / out_total, i = t - pl * out_total;
+    int lo = 0, hi = n_stamps - 1;
+    while (lo < hi) {  // last stamp whose coarse offset is <= i
+      const int mid = (lo + hi + 1) >> 1;
+      if (out_off[mid] <= i) lo = mid;
+      else hi = mid - 1;
+    }
+    const int64_t local = i - out_off[lo];
+    const int w = cnx[lo];
+    const int64_t cy = local / w, cx = local - cy * w;
+    const int64_t fw = (int64_t)w * u;
+    const float* src = in + pl * in_stride + in_off[lo] + (cy * u) * fw + cx * u;
+    float acc = 0.f;
+    for (int b = 0; b < u; ++b)
+      for (int a = 0; a < u; ++a) acc += src[(int64_t)b * fw + a];
+    out[pl * out_stride + i] = acc;
+  }
+}
+
 // r = W (Y - M) on unmasked pixels, 0 elsewhere (LM._r, astrophot/fit/lm.py:381-385)
 __global__ void k_scene_residual(const float* __restrict__ model, const float* __restrict__ data,
                                  const float* __restrict__ weight, const uint8_t* __restrict__ mask, int64_t n,
@@ -601,6 +629,18 @@ int ap_scene_chi2_change(const float* dm, const float* base, const float* data, 
                          ap_stream_t stream) {
   if (!base) return AP_ERR_ARG;
   return scene_chi2(dm, base, data, weight, mask, n, out, parts, n_parts, (cudaStream_t)stream);
+}
+
+int ap_reduce_upscaled(int32_t n_stamps, const int64_t* in_off, const int64_t* out_off, const int32_t* cnx, int32_t u,
+                       int32_t n_planes, const float* in, int64_t in_stride, float* out, int64_t out_stride,
+                       int64_t out_total, ap_stream_t stream) {
+  if (n_stamps <= 0 || !in_off || !out_off || !cnx || u < 1 || n_planes < 1 || !in || !out || out_total <= 0 ||
+      in_stride < 0 || out_stride < out_total)
+    return AP_ERR_ARG;
+  const int64_t n = (int64_t)n_planes * out_total;
+  k_reduce_upscaled<<<egrid(n), 256, 0, (cudaStream_t)stream>>>(n_stamps, in_off, out_off, cnx, u, n_planes, in,
+                                                               in_stride, out, out_stride, out_total);
+  return record_cuda(cudaGetLastError());
 }
 
 int ap_scene_residual(const float* model, const float* data, const float* weight, const uint8_t* mask, int64_t n,

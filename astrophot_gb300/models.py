@@ -790,13 +790,26 @@ def _galaxies(components):
     return [c for c in components if isinstance(c, (Sersic_Galaxy, Exponential_Galaxy))]
 
 
+def _psf_upscale(psf, window) -> int:
+    """round(image pixel / PSF pixel) (models/model_object.py:313); 1 for no PSF or a PSF model."""
+    if psf is None or isinstance(psf, PSF_Model):
+        return 1
+    ratio = float(window.pixel_length) / float(psf.pixel_length)
+    u = int(round(ratio))
+    if u < 1 or abs(ratio - u) > 1e-6 * ratio:
+        raise SpecificationConflict("the PSF's pixels must divide the image's pixels on the CUDA path")
+    return u
+
+
 def _needs_scene(owner, components):
     """More than one galaxy, a galaxy whose own window is not the group's window, or a galaxy
-    convolved with a live PSF model."""
+    convolved with a live PSF model or a PSF image finer than the image pixels."""
     gals = _galaxies(components)
     if len(gals) > 1:
         return True
     if gals and gals[0].psf_mode == "full" and isinstance(gals[0].psf, PSF_Model):
+        return True
+    if gals and gals[0].psf_mode == "full" and _psf_upscale(gals[0].psf, owner.window) > 1:
         return True
     if gals and gals[0] is not owner and gals[0]._window is not None and not (gals[0].window == owner.window):
         return True
@@ -882,7 +895,7 @@ def _make_scene(owner, components, with_data=True):
     scene = Scene(nx, ny, sources, None if (psf is None or live is not None) else psf.data.numpy(), data, weight,
                   mask=mask, sky=sky, scale=float(w.pixelscale[0, 0]), options=opts,
                   origin=(float(origin[0]), float(origin[1])), device=config.ap_device, psf_model=live,
-                  **sky_free)
+                  psf_upscale=_psf_upscale(psf, w), **sky_free)
     if scene.P != len(owner.parameters.vector_values()):
         raise NotImplementedError("this parameter structure has no joint-vector mapping on the CUDA path")
     return scene

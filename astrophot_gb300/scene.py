@@ -184,8 +184,17 @@ class Scene:
     def __init__(self, nx: int, ny: int, sources: List[SceneSource], psf: Optional[np.ndarray], data, weight,
                  mask=None, sky: float = 0.0, scale: float = 1.0, options: Optional[dict] = None,
                  fwd_chunk: int = 64, device="cuda", origin=(0.0, 0.0), psf_model: Optional[LivePSF] = None,
-                 graphs: bool = True, sky_F: Optional[float] = None, sky_after: Optional[int] = None):
+                 graphs: bool = True, sky_F: Optional[float] = None, sky_after: Optional[int] = None,
+                 psf_upscale: int = 1):
         self.nx, self.ny, self.scale = int(nx), int(ny), float(scale)
+        # psf_upscale u: the PSF image has pixels u times finer than the image's; every source is
+        # sampled, integrated and convolved on a u-times finer window and summed back in u x u
+        # blocks (models/model_object.py:308-350)
+        self.upscale = int(psf_upscale)
+        if self.upscale < 1:
+            raise ValueError("psf_upscale must be a positive integer")
+        if self.upscale > 1 and (psf is None or psf_model is not None):
+            raise NotImplementedError("psf_upscale needs a fixed PSF image (no live PSF model)")
         self.origin = (float(origin[0]), float(origin[1]))
         self.sources = list(sources)
         self.device = torch.device(device)
@@ -262,18 +271,14 @@ class Scene:
             mask_bits = sum(1 << sl for sl in free)
             o = N.make_options(profile=kind, psf_mode="full" if psf is not None else "none", free_mask=mask_bits,
                                has_sky=False, **{**opts_kw, **dict(own)})
-            shapes, geoms = [], []
-            for si in members:
-                (x0, x1), (y0, y1) = self._window(si)
-                shapes.append((x1 - x0, y1 - y0))
-                geoms.append(N.scale_geometry(1, self.scale, (self.origin[0] + x0 * self.scale,
-                                                              self.origin[1] + y0 * self.scale))[0])
+            shapes, geoms = self._fine_windows(members)
             jb = N.StampBatch(shapes, None if kpsf is None else [kpsf] * len(members), np.array(geoms), o, dev)
             jpsf = None if psf is None else jb.pack_psf([self.psf_np] * len(members))
             nf = len(free)
-            self._jac_parts.append(dict(kind=kind, free=free, members=members, batch=jb, psf=jpsf, off=jac_total,
-                                        nf=nf))
-            jac_total += nf * jb.out_pixels
+            part = dict(kind=kind, free=free, members=members, batch=jb, psf=jpsf, off=jac_total, nf=nf,
+                        **self._coarse_layout(jb, members, nf))
+            self._jac_parts.append(part)
+            jac_total += nf * part["cpix"]
         # image-wide columns: one [ny * nx] plane per free PSF parameter, then a free sky's
         self.psf_jac_off = jac_total
         jac_total += self.n_img * self.nx * self.ny
@@ -290,29 +295,29 @@ class Scene:
         if psf is not None:
             ky_, kx_ = self.psf_np.shape
             bx, by = int(math.ceil((1 + kx_) / 2)), int(math.ceil((1 + ky_) / 2))
-        group_numel = float((self.nx + 2 * bx) * (self.ny + 2 * by))
+        u = self.upscale
+        group_numel = float((u * self.nx + 2 * bx) * (u * self.ny + 2 * by))
         fwd_total = 0
         for (kind, free, own), members in self.groups.items():
             fo = N.make_options(profile=kind, psf_mode="full" if psf is not None else "none",
                                 free_mask=sum(1 << sl for sl in _SLOTS_OF[kind]), has_sky=False,
                                 **{**opts_kw, **dict(own)})
             if kind in ("sersic", "exponential"):
-                shapes, geoms, gwin = [], [], []
+                shapes, geoms = self._fine_windows(members)
+                # the group's working window in each source's working-pixel indices
+                gwin = []
                 for si in members:
                     (x0, x1), (y0, y1) = self._window(si)
-                    shapes.append((x1 - x0, y1 - y0))
-                    geoms.append(N.scale_geometry(1, self.scale, (self.origin[0] + x0 * self.scale,
-                                                                  self.origin[1] + y0 * self.scale))[0])
-                    # the group's working window in this source's working-pixel indices
-                    gwin.append((-x0, -y0, self.nx + 2 * bx, self.ny + 2 * by))
+                    gwin.append((-u * x0, -u * y0, u * self.nx + 2 * bx, u * self.ny + 2 * by))
                 fb = N.StampBatch(shapes, None if kpsf is None else [kpsf] * len(members), np.array(geoms), fo, dev)
                 fb.set_threshold_numel(group_numel)
                 if kind == "exponential":
                     fb.set_threshold_window(np.array(gwin))
                 fpsf = None if psf is None else fb.pack_psf([self.psf_np] * len(members))
-                self._fwd_parts.append(dict(kind=kind, members=members, batch=fb, psf=fpsf, off=fwd_total,
-                                            m=len(members), own=True))
-                fwd_total += int(fb.out_pixels)
+                part = dict(kind=kind, members=members, batch=fb, psf=fpsf, off=fwd_total, m=len(members), own=True,
+                            **self._coarse_layout(fb, members, 1))
+                self._fwd_parts.append(part)
+                fwd_total += part["cpix"]
             else:
                 m = min(self.fwd_chunk, len(members))
                 fb = N.StampBatch([(self.nx, self.ny)] * m, None if kpsf is None else [kpsf] * m,
@@ -374,7 +379,7 @@ class Scene:
                 d = desc[si]
                 if part["own"]:
                     (x0, x1), (y0, y1) = self._window(si)
-                    d.fwd_off = part["off"] + int(part["batch"].out_offsets[k])
+                    d.fwd_off = part["off"] + int(part["coff"][k])
                     d.fwd_x0, d.fwd_y0, d.fwd_nx = x0, y0, x1 - x0
                 else:
                     d.fwd_off = part["off"] + k * self.nx * self.ny
@@ -384,8 +389,8 @@ class Scene:
             for k, si in enumerate(part["members"]):
                 d = desc[si]
                 (x0, x1), (y0, y1) = self._window(si)
-                d.jac_off = part["off"] + int(b.out_offsets[k])
-                d.jac_stride = int(b.out_pixels)
+                d.jac_off = part["off"] + int(part["coff"][k])
+                d.jac_stride = int(part["cpix"])
                 d.x0, d.y0, d.wx, d.wy = x0, y0, x1 - x0, y1 - y0
                 d.n_free = part["nf"]
                 for c, sl in enumerate(part["free"]):
@@ -447,6 +452,46 @@ class Scene:
         if x1 <= x0 or y1 <= y0:
             raise ValueError(f"source {si} window lies outside the image")
         return (x0, x1), (y0, y1)
+
+    def _fine_windows(self, members):
+        """Render shapes and geometry rows of the sources ``members``: their own windows, on
+        the u-times finer grid of the PSF (the same corner, pixel scale / u)."""
+        u = self.upscale
+        shapes, geoms = [], []
+        for si in members:
+            (x0, x1), (y0, y1) = self._window(si)
+            shapes.append((u * (x1 - x0), u * (y1 - y0)))
+            geoms.append(N.scale_geometry(1, self.scale / u, (self.origin[0] + x0 * self.scale,
+                                                              self.origin[1] + y0 * self.scale))[0])
+        return shapes, geoms
+
+    def _coarse_layout(self, batch, members, n_planes):
+        """The image-pixel layout of a batch's renders: per member its window's offset ``coff``,
+        the total ``cpix``; with psf_upscale, a fine scratch of ``n_planes`` planes for the
+        batch's output and the tables of the block sums into the coarse layout."""
+        if self.upscale == 1:
+            return dict(coff=np.asarray(batch.out_offsets, dtype=np.int64), cpix=int(batch.out_pixels), fine=None)
+        sizes = []
+        cnx = []
+        for si in members:
+            (x0, x1), (y0, y1) = self._window(si)
+            sizes.append((x1 - x0) * (y1 - y0))
+            cnx.append(x1 - x0)
+        coff = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
+        dev = self.device
+        return dict(coff=coff, cpix=int(np.sum(sizes)),
+                    fine=torch.zeros(n_planes * int(batch.out_pixels), dtype=torch.float32, device=dev),
+                    foff_d=torch.tensor(np.asarray(batch.out_offsets, dtype=np.int64), device=dev),
+                    coff_d=torch.tensor(coff, device=dev),
+                    cnx_d=torch.tensor(np.asarray(cnx, dtype=np.int32), device=dev))
+
+    def _reduce(self, part, fine, out, n_planes):
+        """out (coarse layout, planes cpix apart) = u x u block sums of ``fine`` (the batch's
+        layout, planes out_pixels apart)."""
+        N.check(self.lib.ap_reduce_upscaled(len(part["members"]), N._ptr(part["foff_d"]), N._ptr(part["coff_d"]),
+                                            N._ptr(part["cnx_d"]), self.upscale, n_planes, N._ptr(fine),
+                                            int(part["batch"].out_pixels), N._ptr(out), int(part["cpix"]),
+                                            int(part["cpix"]), N._stream()), "ap_reduce_upscaled")
 
     def values_matrix(self, rep: np.ndarray) -> np.ndarray:
         """[n_sources, 8] value-space rows from a joint representation vector."""
@@ -644,7 +689,12 @@ class Scene:
         for pi, part in enumerate(self._fwd_parts):
             b, m, mem = part["batch"], part["m"], part["members"]
             if part["own"]:
-                call(pi, 0, b, part["dpar"][0], part["psf"], buf[part["off"] : part["off"] + b.out_pixels])
+                dst = buf[part["off"] : part["off"] + part["cpix"]]
+                if part["fine"] is None:
+                    call(pi, 0, b, part["dpar"][0], part["psf"], dst)
+                else:  # rendered on the PSF's finer grid, then summed back in blocks
+                    call(pi, 0, b, part["dpar"][0], part["psf"], part["fine"])
+                    self._reduce(part, part["fine"], dst, 1)
                 continue
             for c, c0 in enumerate(range(0, len(mem), m)):
                 out = buf[part["off"] + c0 * self.nx * self.ny : part["off"] + (c0 + m) * self.nx * self.ny]
@@ -744,9 +794,15 @@ class Scene:
     def _jacobian_body(self, as_representation: bool):
         dK = self._psf_body(True) if self.n_psf else None
         for part in self._jac_parts:
-            b = part["batch"]
-            jac = self.jac[part["off"] : part["off"] + part["nf"] * b.out_pixels].view(part["nf"], b.out_pixels)
-            b.jacobian(part["dpar"], part["psf"], as_representation=as_representation, jac=jac)
+            b, nf = part["batch"], part["nf"]
+            jac = self.jac[part["off"] : part["off"] + nf * part["cpix"]]
+            if part["fine"] is None:
+                b.jacobian(part["dpar"], part["psf"], as_representation=as_representation,
+                           jac=jac.view(nf, b.out_pixels))
+            else:  # on the PSF's finer grid, each plane summed back in blocks (the sum is linear)
+                b.jacobian(part["dpar"], part["psf"], as_representation=as_representation,
+                           jac=part["fine"].view(nf, b.out_pixels))
+                self._reduce(part, part["fine"], jac, nf)
         npx = self.nx * self.ny
         for j in range(self.n_psf):
             self._psf_column(dK, j, self.jac[self.psf_jac_off + j * npx : self.psf_jac_off + (j + 1) * npx])
@@ -768,13 +824,12 @@ class Scene:
         out = np.zeros((self.ny, self.nx, self.P))
         jac = self.jac.cpu().numpy()
         for part in self._jac_parts:
-            b = part["batch"]
+            cp = part["cpix"]
             for k, si in enumerate(part["members"]):
                 (x0, x1), (y0, y1) = self._window(si)
-                o = int(b.out_offsets[k])
+                o = int(part["coff"][k])
                 for c, sl in enumerate(part["free"]):
-                    col = jac[part["off"] + c * b.out_pixels + o : part["off"] + c * b.out_pixels + o
-                              + (x1 - x0) * (y1 - y0)]
+                    col = jac[part["off"] + c * cp + o : part["off"] + c * cp + o + (x1 - x0) * (y1 - y0)]
                     out[y0:y1, x0:x1, self.gidx[si][sl]] += col.reshape(y1 - y0, x1 - x0)
         npx = self.nx * self.ny
         for j in range(self.n_img):
@@ -783,15 +838,17 @@ class Scene:
         return out
 
     def _vjp_index(self, part):
-        """For an own-window forward batch: image index of every packed output pixel."""
+        """For an own-window forward batch: image index of every packed output pixel (with
+        psf_upscale, of the image pixel whose block holds the fine pixel: the block sum passes
+        the image's gradient to each of its pixels unchanged)."""
         if "vjp_idx" not in part:
-            b = part["batch"]
-            idx = np.empty(b.out_pixels, dtype=np.int64)
+            b, u = part["batch"], self.upscale
+            idx = np.zeros(b.out_pixels, dtype=np.int64)
             for k, si in enumerate(part["members"]):
                 (x0, x1), (y0, y1) = self._window(si)
-                yy, xx = np.mgrid[y0:y1, x0:x1]
+                yy, xx = np.mgrid[u * y0 : u * y1, u * x0 : u * x1] // u
                 o = int(b.out_offsets[k])
-                idx[o : o + (x1 - x0) * (y1 - y0)] = (yy * self.nx + xx).ravel()
+                idx[o : o + u * u * (x1 - x0) * (y1 - y0)] = (yy * self.nx + xx).ravel()
             part["vjp_idx"] = torch.tensor(idx, device=self.device)
         return part["vjp_idx"]
 

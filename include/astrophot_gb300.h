@@ -425,6 +425,15 @@ int ap_scene_chi2(const float* model, const float* data, const float* weight, co
 int ap_scene_chi2_change(const float* dm, const float* base, const float* data, const float* weight,
                          const uint8_t* mask, int64_t n, double* out, double* parts, int32_t n_parts,
                          ap_stream_t stream);
+/* A PSF image finer than the image pixels (psf_upscale u = image pixel / PSF pixel): sources are
+ * rendered on u-times finer windows and summed back in u x u blocks (Image.reduce of the cropped
+ * working image, astrophot/models/model_object.py:308-350).  out[p][i] for every plane p <
+ * n_planes and coarse pixel i < out_total: stamp k's coarse image, cnx[k] pixels wide, starts at
+ * out_off[k] (ascending, out_off[0] = 0), its fine image (u cnx[k] wide, row-major) at in_off[k];
+ * planes lie in_stride / out_stride floats apart.  All arrays device. */
+int ap_reduce_upscaled(int32_t n_stamps, const int64_t* in_off, const int64_t* out_off, const int32_t* cnx,
+                       int32_t u, int32_t n_planes, const float* in, int64_t in_stride, float* out,
+                       int64_t out_stride, int64_t out_total, ap_stream_t stream);
 /* r = W (data - model) on unmasked pixels, 0 on masked ones (LM._r, fit/lm.py:381-385). */
 int ap_scene_residual(const float* model, const float* data, const float* weight,
                       const uint8_t* mask, int64_t n, float* r, ap_stream_t stream);

@@ -110,3 +110,18 @@ def load_segmap(name):
     d = {k: z[k] for k in z.files}
     d["spec"] = json.loads(str(d["spec"]))
     return d
+
+
+def upscale_case_names():
+    return sorted(os.path.basename(p)[: -len(".npz")] for p in glob.glob(os.path.join(HERE, "upscale_*.npz")))
+
+
+def load_upscale(name):
+    """A model whose PSF image has pixels ``upscale`` times finer than the image's: the inputs
+    (psf at the fine scale, data, weight, truth / initial values) and the reference's model,
+    representation Jacobian and LM trajectory."""
+    z = np.load(os.path.join(HERE, f"{name}.npz"))
+    d = {k: z[k] for k in z.files}
+    d["spec"] = json.loads(str(d["spec"]))
+    d["message"] = str(d["message"])
+    return d

@@ -11,6 +11,7 @@ Run with ``ASTROPHOT_REFERENCE=<path of the reference checkout>`` set:
     python tests/golden/make_golden.py psfstamps  # only the Moffat / Gaussian PSF stamps
     python tests/golden/make_golden.py freesky    # only the group with a free flat sky
     python tests/golden/make_golden.py knobs      # only the group with per-galaxy sampling settings
+    python tests/golden/make_golden.py upscale    # only the PSF finer than the image pixels
 
 The reference (AstroPhot 0.x) is imported through a ``sys.modules`` shim for
 the optional packages it imports at module level but never calls on this
@@ -857,9 +858,56 @@ def run_psf_stamps(ap):
     return out
 
 
+UPSCALE_CASES = {
+    # one Sersic galaxy on a 40 x 40 image of 1"-pixels whose PSF image has 0.5"-pixels (a
+    # 25 x 25 Moffat, FWHM 3"): the reference samples, integrates and convolves on the 2x finer
+    # grid and sums 2 x 2 blocks back (models/model_object.py:308-350).  Model, representation
+    # Jacobian and an LM fit from a perturbed start.
+    "upscale_sersic_40": dict(kind="sersic", nx=40, ny=40, scale=1.0, upscale=2, psf=("moffat", 3.5, 3.0, 25),
+                              truth={"center": [19.6, 20.3], "q": 0.65, "PA": 1.1, "n": 2.2, "Re": 5.5, "Ie": 1.6},
+                              init={"center": [20.1, 19.9], "q": 0.72, "PA": 1.2, "n": 1.9, "Re": 6.3, "Ie": 1.5},
+                              seed=29, max_iter=20),
+}
+
+
+def run_upscale_case(ap, key, case):
+    u, scale = case["upscale"], case["scale"]
+    _, beta, fwhm, width = case["psf"]
+    psf = synthetic.moffat_stamp(beta, synthetic.moffat_rd(fwhm, beta), width, scale / u)
+    model_type = {"sersic": "sersic galaxy model", "exponential": "exponential galaxy model"}[case["kind"]]
+
+    def target_of(data, variance=None):
+        kw = {} if variance is None else {"variance": variance}
+        return ap.image.Target_Image(data=data, pixelscale=scale, psf=ap.image.PSF_Image(data=psf, pixelscale=scale / u),
+                                     **kw)
+
+    shape = (case["ny"], case["nx"])
+    truth = ap.models.AstroPhot_Model(name=f"{key} truth", model_type=model_type, target=target_of(np.zeros(shape)),
+                                      parameters=dict(case["truth"]), psf_mode="full")
+    truth_img = truth().data.detach().cpu().numpy()
+    data, weight = synthetic.add_noise(truth_img, case["seed"])
+    model = ap.models.AstroPhot_Model(name=f"{key} fit", model_type=model_type, target=target_of(data, 1.0 / weight),
+                                      parameters=dict(case["init"]), psf_mode="full")
+    init_img = model().data.detach().cpu().numpy()
+    jac = model.jacobian(as_representation=True).data.detach().cpu().numpy()
+    names = [str(n) for n in model.parameters.vector_names()]
+    rep0 = model.parameters.vector_representation().detach().cpu().numpy().copy()
+    res = ap.fit.LM(model, initial_state=rep0, max_iter=case["max_iter"]).fit()
+    return dict(psf=psf, data=data, weight=weight, truth_model=truth_img, init_model=init_img, jac_rep=jac,
+                names=np.array(names), rep0=rep0, loss_history=np.array(res.loss_history),
+                L_history=np.array(res.L_history), res=np.array(res.res()), message=np.array(res.message),
+                spec=json.dumps(case))
+
+
 def main():
     ap = import_reference()
     only = sys.argv[1] if len(sys.argv) > 1 else None
+    if only == "upscale":
+        for key, case in UPSCALE_CASES.items():
+            out = run_upscale_case(ap, key, case)
+            np.savez_compressed(os.path.join(HERE, f"{key}.npz"), **out)
+            print("upscale", key, out["names"], out["jac_rep"].shape, out["loss_history"], str(out["message"]))
+        return
     if only in ("freesky", "knobs"):
         key = {"freesky": "group_freesky_96", "knobs": "group_knobs_96"}[only]
         out = run_group_case(ap, key, GROUP_CASES[key])

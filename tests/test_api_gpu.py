@@ -243,3 +243,36 @@ def test_initialize_matches_reference(ap, name):
         ref = d[f"value_{k}"]
         tol = 1e-9 if k in ("center", "PA", "q") else 1e-3
         assert np.max(np.abs(got - ref) / np.maximum(1.0, np.abs(ref))) <= tol, (k, got, ref)
+
+
+@pytest.mark.parametrize("name", cases.upscale_case_names())
+def test_psf_finer_than_image_matches_reference(ap, name):
+    """A PSF image with pixels twice finer than the image's (``PSF_Image(pixelscale=0.5)`` on a
+    1"-pixel target): sampled, integrated and convolved on the finer grid and summed back in
+    2 x 2 blocks, as the reference does; model, Jacobian and LM against its golden."""
+    d = cases.load_upscale(name)
+    spec = d["spec"]
+    u, scale = spec["upscale"], spec["scale"]
+    kind = {"sersic": "sersic galaxy model", "exponential": "exponential galaxy model"}[spec["kind"]]
+    tar = ap.image.Target_Image(data=d["data"], pixelscale=scale, variance=1.0 / d["weight"],
+                                psf=ap.image.PSF_Image(data=d["psf"], pixelscale=scale / u))
+    m = ap.models.AstroPhot_Model(name=f"api {name}", model_type=kind, target=tar, parameters=dict(spec["init"]),
+                                  psf_mode="full")
+    assert list(m.parameters.vector_names()) == [str(n) for n in d["names"]]
+    assert np.allclose(m.parameters.vector_representation().numpy(), d["rep0"], atol=1e-12)
+    assert close(m().data.numpy(), d["init_model"])
+    J = m.jacobian(as_representation=True).data.numpy()
+    for k in range(J.shape[-1]):
+        assert close(J[..., k], d["jac_rep"][..., k], rel=2e-4), k
+    # the adjoint through the finer grid and the block sums: d nll / d rep = J^T W (model - data)
+    # with the reference's Jacobian and model
+    vec = torch.tensor(d["rep0"], dtype=torch.float64, requires_grad=True)
+    m.negative_log_likelihood(parameters=vec, as_representation=True).backward()
+    want = np.einsum("yxk,yx->k", d["jac_rep"], d["weight"] * (d["init_model"] - d["data"]))
+    assert np.allclose(vec.grad.numpy(), want, rtol=1e-3, atol=1e-3 * np.max(np.abs(want)))
+    res = ap.fit.LM(m, max_iter=spec["max_iter"]).fit()
+    print(name, res.loss_history, d["loss_history"], res.message)
+    assert res.message == d["message"]
+    assert abs(min(res.loss_history) / d["loss_history"].min() - 1) <= 1e-5
+    assert np.allclose(res.loss_history[:3], d["loss_history"][:3], rtol=1e-5)
+    assert np.allclose(res.res(), d["res"], rtol=1e-4, atol=1e-6)
