@@ -151,6 +151,9 @@ EXPORTS = [
     ("ap_scene_chi2", [_P, _P, _P, _P, _I64, _P, _P, _I32, _P]),
     ("ap_scene_chi2_change", [_P, _P, _P, _P, _P, _I64, _P, _P, _I32, _P]),
     ("ap_reduce_upscaled", [_I32, _P, _P, _P, _I32, _I32, _P, _I64, _P, _I64, _I64, _P]),
+    ("ap_scene_hess_blocks", [_P, _P, _I32, _P, _P, _P, _I32, _P, _P]),
+    ("ap_scene_jt_blocks", [_P, _I32, _P, _P, _I32, _P, _P]),
+    ("ap_gather_sum", [_I64, _P, _P, _P, _P, _P, _I64, _P]),
     ("ap_scene_residual", [_P, _P, _P, _P, _I64, _P, _P]),
     ("ap_scene_rpp_image", [_P, _P, _P, _P, _P, ctypes.c_double, _I64, _P, _P]),
     ("ap_scene_stage", [_I32, _P, _P, _P, _P, ctypes.c_double, _P, _P]),

@@ -90,8 +90,11 @@ __global__ void k_scene_jvp(const ap_scene_source* __restrict__ src, const int32
 }
 
 // ---- jt: out[g] += sum over the source's window of J_c(p) v(p) -----------------------------------
+// With `part` (n_sources x kMaxSlots doubles), each source's sums go to its own slots instead
+// of being added into out: ap_gather_sum then adds them in a fixed order.
 __global__ void k_scene_jt(const ap_scene_source* __restrict__ src, const float* __restrict__ jac,
-                           const float* __restrict__ v, int nx, double* __restrict__ out) {
+                           const float* __restrict__ v, int nx, double* __restrict__ out,
+                           double* __restrict__ part) {
   const ap_scene_source& s = src[blockIdx.x];
   double acc[kMaxSlots];
 #pragma unroll
@@ -115,7 +118,8 @@ __global__ void k_scene_jt(const ap_scene_source* __restrict__ src, const float*
   if (threadIdx.x < s.n_free) {
     double t = 0.0;
     for (int k = 0; k < nw; ++k) t += sh[threadIdx.x][k];
-    atomicAdd(out + s.gidx[threadIdx.x], t);
+    if (part) part[(int64_t)blockIdx.x * kMaxSlots + threadIdx.x] = t;
+    else atomicAdd(out + s.gidx[threadIdx.x], t);
   }
 }
 
@@ -123,7 +127,7 @@ __global__ void k_scene_jt(const ap_scene_source* __restrict__ src, const float*
 __global__ void __launch_bounds__(256) k_scene_hess(const ap_scene_source* __restrict__ src,
                                                     const int32_t* __restrict__ pairs, const float* __restrict__ jac,
                                                     const float* __restrict__ weight, const uint8_t* __restrict__ mask,
-                                                    int nx, int P, double* __restrict__ H) {
+                                                    int nx, int P, double* __restrict__ H, double* __restrict__ part) {
   const ap_scene_source& A = src[pairs[2 * blockIdx.x]];
   const ap_scene_source& B = src[pairs[2 * blockIdx.x + 1]];
   const bool same = pairs[2 * blockIdx.x] == pairs[2 * blockIdx.x + 1];
@@ -171,9 +175,25 @@ __global__ void __launch_bounds__(256) k_scene_hess(const ap_scene_source* __res
     if (a >= A.n_free || c >= B.n_free) continue;
     double t = 0.0;
     for (int q = 0; q < nw; ++q) t += sh[k][q];
+    if (part) {  // the pair's block, summed into H by ap_gather_sum in a fixed order
+      part[(int64_t)blockIdx.x * kMaxSlots * kMaxSlots + k] = t;
+      continue;
+    }
     const int ga = A.gidx[a], gb = B.gidx[c];
     atomicAdd(H + (int64_t)ga * P + gb, t);
     if (!same) atomicAdd(H + (int64_t)gb * P + ga, t);
+  }
+}
+
+// out[entry[e]] = sum of part[contrib[k]], k in [ptr[e], ptr[e + 1]), in that order
+__global__ void k_gather_sum(int64_t n_entries, const int64_t* __restrict__ entry, const int32_t* __restrict__ ptr,
+                             const int32_t* __restrict__ contrib, const double* __restrict__ part,
+                             double* __restrict__ out) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n_entries;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    double t = 0.0;
+    for (int k = ptr[e]; k < ptr[e + 1]; ++k) t += part[contrib[k]];
+    out[entry[e]] = t;
   }
 }
 
@@ -592,7 +612,7 @@ int ap_scene_jt(const ap_scene_source* sources, int32_t n_sources, const float* 
   cudaStream_t st = (cudaStream_t)stream;
   int rc = record_cuda(cudaMemsetAsync(out, 0, sizeof(double) * P, st));
   if (rc || n_sources == 0) return rc;
-  k_scene_jt<<<n_sources, 256, 0, st>>>(sources, jac, v, nx, out);
+  k_scene_jt<<<n_sources, 256, 0, st>>>(sources, jac, v, nx, out, nullptr);
   return record_cuda(cudaGetLastError());
 }
 
@@ -602,7 +622,34 @@ int ap_scene_hess(const ap_scene_source* sources, const int32_t* pairs, int32_t 
   cudaStream_t st = (cudaStream_t)stream;
   int rc = record_cuda(cudaMemsetAsync(H, 0, sizeof(double) * P * P, st));
   if (rc || n_pairs == 0) return rc;
-  k_scene_hess<<<n_pairs, 256, 0, st>>>(sources, pairs, jac, weight, mask, nx, P, H);
+  k_scene_hess<<<n_pairs, 256, 0, st>>>(sources, pairs, jac, weight, mask, nx, P, H, nullptr);
+  return record_cuda(cudaGetLastError());
+}
+
+int ap_scene_hess_blocks(const ap_scene_source* sources, const int32_t* pairs, int32_t n_pairs, const float* jac,
+                         const float* weight, const uint8_t* mask, int32_t nx, double* part, ap_stream_t stream) {
+  if (!sources || !jac || !part || n_pairs < 0 || (n_pairs > 0 && !pairs)) return AP_ERR_ARG;
+  if (n_pairs == 0) return AP_OK;
+  k_scene_hess<<<n_pairs, 256, 0, (cudaStream_t)stream>>>(sources, pairs, jac, weight, mask, nx, 0, nullptr, part);
+  return record_cuda(cudaGetLastError());
+}
+
+int ap_scene_jt_blocks(const ap_scene_source* sources, int32_t n_sources, const float* jac, const float* v,
+                       int32_t nx, double* part, ap_stream_t stream) {
+  if (!sources || !jac || !v || !part || n_sources < 0) return AP_ERR_ARG;
+  if (n_sources == 0) return AP_OK;
+  k_scene_jt<<<n_sources, 256, 0, (cudaStream_t)stream>>>(sources, jac, v, nx, nullptr, part);
+  return record_cuda(cudaGetLastError());
+}
+
+int ap_gather_sum(int64_t n_entries, const int64_t* entry, const int32_t* ptr, const int32_t* contrib,
+                  const double* part, double* out, int64_t out_n, ap_stream_t stream) {
+  if (n_entries < 0 || !out || out_n <= 0 || (n_entries > 0 && (!entry || !ptr || !contrib || !part)))
+    return AP_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = record_cuda(cudaMemsetAsync(out, 0, sizeof(double) * out_n, st));
+  if (rc || n_entries == 0) return rc;
+  k_gather_sum<<<egrid(n_entries), 256, 0, st>>>(n_entries, entry, ptr, contrib, part, out);
   return record_cuda(cudaGetLastError());
 }
 

@@ -432,6 +432,32 @@ class Scene:
         self.n_pairs = len(pairs)
         self.pairs = torch.tensor(np.array(pairs, dtype=np.int32).reshape(-1, 2), device=dev).contiguous()
 
+        # fixed-order sums of J^T W J and J^T v: every block (a pair, a source) writes its own
+        # partial sums and each entry adds its blocks' in one order (linked centres make several
+        # blocks meet in one entry, where atomic adds would depend on the order blocks run in)
+        n_desc = ns + (1 if self.n_img else 0)
+        nf = np.array([desc[i].n_free for i in range(n_desc)], dtype=np.int64)
+        gid = np.array([[desc[i].gidx[c] for c in range(8)] for i in range(n_desc)], dtype=np.int64)
+        slot = np.arange(8)
+        ok = slot[None, :] < nf[:, None]
+        src_i, c_i = np.nonzero(ok)
+        self._jt_table = self._gather_table(gid[src_i, c_i], src_i * 8 + c_i)
+        self._jt_part = torch.empty(max(n_desc, 1) * 8, dtype=torch.float64, device=dev)
+        pa = np.array(pairs, dtype=np.int64).reshape(-1, 2)
+        p_i, a_i, c_i = np.nonzero((slot[None, :, None] < nf[pa[:, 0]][:, None, None])
+                                   & (slot[None, None, :] < nf[pa[:, 1]][:, None, None]))
+        # a pair of two sources adds its block and the block's transpose; a source's own block
+        # gives its upper triangle, mirrored, so that H is exactly symmetric
+        two = pa[p_i, 0] != pa[p_i, 1]
+        keep = two | (a_i <= c_i)
+        p_i, a_i, c_i, two = p_i[keep], a_i[keep], c_i[keep], two[keep]
+        ga, gb = gid[pa[p_i, 0], a_i], gid[pa[p_i, 1], c_i]
+        contrib = p_i * 64 + a_i * 8 + c_i
+        mirror = two | (a_i < c_i)
+        self._hess_table = self._gather_table(np.concatenate([ga * self.P + gb, gb[mirror] * self.P + ga[mirror]]),
+                                              np.concatenate([contrib, contrib[mirror]]))
+        self._hess_part = torch.empty(max(self.n_pairs, 1) * 64, dtype=torch.float64, device=dev)
+
         self.lib = N.lib()
         self._solve_ws = torch.empty(int(self.lib.ap_dense_solve_workspace_bytes(self.P)), dtype=torch.uint8,
                                      device=dev)
@@ -905,19 +931,40 @@ class Scene:
                                * float(g_img.to(torch.float64).sum().item()))
         return torch.tensor(out, dtype=torch.float64)
 
+    def _gather_table(self, entries, contribs):
+        """(entry, ptr, contrib, n) device tables of ap_gather_sum: each entry's contributions in
+        ascending order."""
+        entries = np.asarray(entries, dtype=np.int64)
+        contribs = np.asarray(contribs, dtype=np.int64)
+        order = np.lexsort((contribs, entries))
+        e, c = entries[order], contribs[order]
+        uniq, start = np.unique(e, return_index=True)
+        ptr = np.append(start, len(e)).astype(np.int32)
+        dev = self.device
+        return (torch.tensor(uniq, device=dev), torch.tensor(ptr, device=dev),
+                torch.tensor(c.astype(np.int32), device=dev), len(uniq))
+
+    def _gather(self, table, part, out):
+        entry, ptr, contrib, n = table
+        N.check(self.lib.ap_gather_sum(n, N._ptr(entry), N._ptr(ptr), N._ptr(contrib), N._ptr(part), N._ptr(out),
+                                       out.numel(), N._stream()), "ap_gather_sum")
+        return out
+
     def hess(self) -> torch.Tensor:
+        """J^T W J [P, P] (float64), the same bits on every run."""
         H = torch.empty((self.P, self.P), dtype=torch.float64, device=self.device)
-        N.check(self.lib.ap_scene_hess(N._ptr(self.desc), N._ptr(self.pairs), self.n_pairs, N._ptr(self.jac),
-                                       N._ptr(self.weight), N._ptr(self.mask), self.nx, self.P, N._ptr(H),
-                                       N._stream()), "ap_scene_hess")
-        return H
+        N.check(self.lib.ap_scene_hess_blocks(N._ptr(self.desc), N._ptr(self.pairs), self.n_pairs, N._ptr(self.jac),
+                                              N._ptr(self.weight), N._ptr(self.mask), self.nx, N._ptr(self._hess_part),
+                                              N._stream()), "ap_scene_hess_blocks")
+        return self._gather(self._hess_table, self._hess_part, H)
 
     def jt(self, img: torch.Tensor) -> torch.Tensor:
+        """J^T img [P] (float64), the same bits on every run."""
         out = torch.empty(self.P, dtype=torch.float64, device=self.device)
-        N.check(self.lib.ap_scene_jt(N._ptr(self.desc), len(self.sources) + (1 if self.n_img else 0), N._ptr(self.jac),
-                                     N._ptr(img), self.nx,
-                                     self.P, N._ptr(out), N._stream()), "ap_scene_jt")
-        return out
+        N.check(self.lib.ap_scene_jt_blocks(N._ptr(self.desc), len(self.sources) + (1 if self.n_img else 0),
+                                            N._ptr(self.jac), N._ptr(img), self.nx, N._ptr(self._jt_part),
+                                            N._stream()), "ap_scene_jt_blocks")
+        return self._gather(self._jt_table, self._jt_part, out)
 
     def jvp(self, h: torch.Tensor) -> torch.Tensor:
         out = torch.empty(self.nx * self.ny, dtype=torch.float32, device=self.device)

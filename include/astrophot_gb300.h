@@ -414,6 +414,19 @@ int ap_scene_jt(const ap_scene_source* sources, int32_t n_sources, const float* 
 int ap_scene_hess(const ap_scene_source* sources, const int32_t* pairs, int32_t n_pairs,
                   const float* jac, const float* weight, const uint8_t* mask, int32_t nx, int32_t P,
                   double* H, ap_stream_t stream);
+/* The same two products with a result that does not depend on the order in which blocks run
+ * (linked centres make several blocks add into one entry): ap_scene_hess_blocks writes each
+ * pair's 8 x 8 block, part[p][a][c] = sum J_a W J_c (n_pairs x 64 doubles), ap_scene_jt_blocks
+ * each source's sums, part[s][c] (n_sources x 8 doubles); ap_gather_sum then zeroes out[out_n]
+ * and sets out[entry[e]] = sum of part[contrib[k]] for k in [ptr[e], ptr[e + 1]) in that order
+ * (e < n_entries; the tables are the caller's, from the pairs and the sources' gidx). */
+int ap_scene_hess_blocks(const ap_scene_source* sources, const int32_t* pairs, int32_t n_pairs,
+                         const float* jac, const float* weight, const uint8_t* mask, int32_t nx, double* part,
+                         ap_stream_t stream);
+int ap_scene_jt_blocks(const ap_scene_source* sources, int32_t n_sources, const float* jac, const float* v,
+                       int32_t nx, double* part, ap_stream_t stream);
+int ap_gather_sum(int64_t n_entries, const int64_t* entry, const int32_t* ptr, const int32_t* contrib,
+                  const double* part, double* out, int64_t out_n, ap_stream_t stream);
 /* out[0] = sum over unmasked pixels of W (data - model)^2 (float64).  parts: device scratch of
  * n_parts doubles (1024 used at most) for the block partial sums, which are added in a fixed
  * order, so the result has the same bits on every run. */

@@ -871,6 +871,8 @@ UPSCALE_CASES = {
 
 
 def run_upscale_case(ap, key, case):
+    import torch
+
     u, scale = case["upscale"], case["scale"]
     _, beta, fwhm, width = case["psf"]
     psf = synthetic.moffat_stamp(beta, synthetic.moffat_rd(fwhm, beta), width, scale / u)
@@ -892,8 +894,15 @@ def run_upscale_case(ap, key, case):
     jac = model.jacobian(as_representation=True).data.detach().cpu().numpy()
     names = [str(n) for n in model.parameters.vector_names()]
     rep0 = model.parameters.vector_representation().detach().cpu().numpy().copy()
+    # negative_log_likelihood and its reverse-mode autograd gradient at the initial point
+    rep = model.parameters.vector_representation().detach().clone().requires_grad_(True)
+    nll = model.negative_log_likelihood(parameters=rep, as_representation=True)
+    nll.backward()
+    nll_grad = rep.grad.detach().cpu().numpy().copy()
+    model.parameters.vector_set_representation(torch.tensor(rep0))
     res = ap.fit.LM(model, initial_state=rep0, max_iter=case["max_iter"]).fit()
     return dict(psf=psf, data=data, weight=weight, truth_model=truth_img, init_model=init_img, jac_rep=jac,
+                nll=np.array(float(nll.detach())), nll_grad=nll_grad,
                 names=np.array(names), rep0=rep0, loss_history=np.array(res.loss_history),
                 L_history=np.array(res.L_history), res=np.array(res.res()), message=np.array(res.message),
                 spec=json.dumps(case))

@@ -264,8 +264,17 @@ def test_psf_finer_than_image_matches_reference(ap, name):
     J = m.jacobian(as_representation=True).data.numpy()
     for k in range(J.shape[-1]):
         assert close(J[..., k], d["jac_rep"][..., k], rel=2e-4), k
-    # the adjoint through the finer grid and the block sums: d nll / d rep = J^T W (model - data)
-    # with the reference's Jacobian and model
+    # the adjoint through the finer grid and the block sums: negative_log_likelihood().backward()
+    # against the reference's autograd gradient, and, for the render's own derivative (without
+    # the sampling-coordinate path reverse-mode autograd adds to the centre under a PSF shift),
+    # against J^T W (model - data) of the reference's Jacobian
+    vec = torch.tensor(d["rep0"], dtype=torch.float64, requires_grad=True)
+    nll = m.negative_log_likelihood(parameters=vec, as_representation=True)
+    assert abs(float(nll.detach()) / float(d["nll"]) - 1) <= 1e-5
+    nll.backward()
+    want = d["nll_grad"]
+    assert np.allclose(vec.grad.numpy(), want, rtol=1e-3, atol=1e-3 * np.max(np.abs(want)))
+    m.reference_center_gradient = False
     vec = torch.tensor(d["rep0"], dtype=torch.float64, requires_grad=True)
     m.negative_log_likelihood(parameters=vec, as_representation=True).backward()
     want = np.einsum("yxk,yx->k", d["jac_rep"], d["weight"] * (d["init_model"] - d["data"]))

@@ -64,14 +64,23 @@ def test_scene_primitives_match_numpy(S, name):
     rep0 = sc.representation()
     J = sc.jacobian_image(rep0).reshape(-1, sc.P)
     W = d["weight"].astype(np.float32).astype(np.float64).reshape(-1)
-    H = sc.hess().cpu().numpy()
+    Ht = sc.hess()
+    H = Ht.cpu().numpy()
     Hn = J.T @ (W[:, None] * J)
     assert np.max(np.abs(H - Hn)) <= 1e-5 * np.max(np.abs(Hn))
+    # the linked centre's entries gather several blocks: in a fixed order, so the same bits
+    # every time (and symmetric, each transpose entry being the same sum)
+    for _ in range(3):
+        assert torch.equal(sc.hess(), Ht)
+    assert np.array_equal(H, H.T)
     rng = np.random.default_rng(3)
     v = rng.normal(size=J.shape[0]).astype(np.float32)
-    jt = sc.jt(torch.tensor(v, device="cuda")).cpu().numpy()
+    vt = torch.tensor(v, device="cuda")
+    jt_t = sc.jt(vt)
+    jt = jt_t.cpu().numpy()
     want = J.T @ v.astype(np.float64)
     assert np.max(np.abs(jt - want)) <= 1e-5 * np.max(np.abs(want))
+    assert all(torch.equal(sc.jt(vt), jt_t) for _ in range(3))
     h = rng.normal(size=sc.P)
     jv = sc.jvp(torch.tensor(h, device="cuda")).cpu().numpy()
     want = J @ h
