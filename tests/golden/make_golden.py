@@ -12,6 +12,7 @@ Run with ``ASTROPHOT_REFERENCE=<path of the reference checkout>`` set:
     python tests/golden/make_golden.py freesky    # only the group with a free flat sky
     python tests/golden/make_golden.py knobs      # only the group with per-galaxy sampling settings
     python tests/golden/make_golden.py upscale    # only the PSF finer than the image pixels
+    python tests/golden/make_golden.py groupupscale  # only the group with that PSF
 
 The reference (AstroPhot 0.x) is imported through a ``sys.modules`` shim for
 the optional packages it imports at module level but never calls on this
@@ -462,6 +463,9 @@ GROUP_CASES = {
     "group_knobs_96": dict(size=96, seed=23, psf=MOFFAT_25, max_iter=12,
                            knobs=[{}, {"sampling_mode": "simpsons"}, {"integrate_mode": "none"},
                                   {"sampling_mode": "quad:3"}]),
+    # the group with a PSF image of pixels twice finer than the image's (the 25 x 25 Moffat of
+    # FWHM 3" on 0.5" pixels): every galaxy sampled on its window rescaled to the PSF's grid
+    "group_upscale_96": dict(size=96, seed=31, psf=MOFFAT_25, max_iter=12, psf_upscale=2),
 }
 
 GROUP_SOURCES = (
@@ -507,10 +511,22 @@ def build_group(ap, target, values, tag, psf_mode="full", sky_F=0.0, sky_free=Fa
     return group
 
 
+def group_psf(ap, case):
+    """The case's PSF array and the target's psf argument (a PSF_Image of finer pixels when the
+    case has psf_upscale)."""
+    u = case.get("psf_upscale", 1)
+    if u == 1:
+        psf = psf_array(case["psf"])
+        return psf, psf
+    _, beta, fwhm, width = case["psf"]
+    psf = synthetic.moffat_stamp(beta, synthetic.moffat_rd(fwhm, beta), width, 1.0 / u)
+    return psf, ap.image.PSF_Image(data=psf, pixelscale=1.0 / u)
+
+
 def run_group_case(ap, key, case):
     N = case["size"]
-    psf = psf_array(case["psf"])
-    target = ap.image.Target_Image(data=np.zeros((N, N)), pixelscale=1.0, psf=psf)
+    psf, psf_arg = group_psf(ap, case)
+    target = ap.image.Target_Image(data=np.zeros((N, N)), pixelscale=1.0, psf=psf_arg)
     truth_vals = [src[3] for src in GROUP_SOURCES]
     sky_free = bool(case.get("sky_free", False))
     knobs = case.get("knobs")
@@ -518,7 +534,7 @@ def run_group_case(ap, key, case):
                               sky_free=sky_free, knobs=knobs)
     truth_img = truth_group().data.detach().cpu().numpy()
     data, weight = synthetic.add_noise(truth_img, case["seed"])
-    target = ap.image.Target_Image(data=data, pixelscale=1.0, psf=psf, variance=1.0 / weight)
+    target = ap.image.Target_Image(data=data, pixelscale=1.0, psf=psf_arg, variance=1.0 / weight)
     init_vals = [group_init_values(v) for v in truth_vals]
     group = build_group(ap, target, init_vals, key, sky_F=case.get("sky_F_init", 0.0), sky_free=sky_free,
                         knobs=knobs)
@@ -917,8 +933,8 @@ def main():
             np.savez_compressed(os.path.join(HERE, f"{key}.npz"), **out)
             print("upscale", key, out["names"], out["jac_rep"].shape, out["loss_history"], str(out["message"]))
         return
-    if only in ("freesky", "knobs"):
-        key = {"freesky": "group_freesky_96", "knobs": "group_knobs_96"}[only]
+    if only in ("freesky", "knobs", "groupupscale"):
+        key = {"freesky": "group_freesky_96", "knobs": "group_knobs_96", "groupupscale": "group_upscale_96"}[only]
         out = run_group_case(ap, key, GROUP_CASES[key])
         np.savez_compressed(os.path.join(HERE, f"{key}.npz"), **out)
         print("group", key, out["names"], out["jac_rep"].shape, out["loss_history"], str(out["message"]))

@@ -212,7 +212,9 @@ def build_group(ap, target, values, tag, spec=None):
 def test_multi_galaxy_group_matches_reference(ap, name):
     """Windows per galaxy, a linked centre, PSF: model, representation Jacobian and LM."""
     d = cases.load_group(name)
-    target = ap.image.Target_Image(data=d["data"], pixelscale=1.0, psf=d["psf"], variance=1.0 / d["weight"])
+    u = d["spec"].get("psf_upscale", 1)
+    psf = d["psf"] if u == 1 else ap.image.PSF_Image(data=d["psf"], pixelscale=1.0 / u)
+    target = ap.image.Target_Image(data=d["data"], pixelscale=1.0, psf=psf, variance=1.0 / d["weight"])
     grp = build_group(ap, target, d["init_values"], f"api {name}", d["spec"])
     assert list(grp.parameters.vector_names()) == [str(n) for n in d["names"]]
     assert np.allclose(grp.parameters.vector_representation().numpy(), d["rep0"], atol=1e-12)

@@ -37,7 +37,7 @@ def golden_scene(S, d, values=None):
             for k, v, w, l, o in zip(KINDS, values, WINDOWS, LINKS, knobs)]
     N = spec["size"]
     sky = dict(sky_F=spec["sky_F_init"]) if spec.get("sky_free") else dict(sky=1.0)
-    return S.Scene(N, N, srcs, d["psf"], d["data"], d["weight"], **sky)
+    return S.Scene(N, N, srcs, d["psf"], d["data"], d["weight"], psf_upscale=spec.get("psf_upscale", 1), **sky)
 
 
 @pytest.mark.parametrize("name", cases.group_case_names())

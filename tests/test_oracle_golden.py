@@ -65,6 +65,32 @@ def test_render_and_jacobian_match_reference(name):
         assert np.max(np.abs(Jr[..., k] - d["jac_rep"][..., k])) <= 1e-11 * colscale
 
 
+@pytest.mark.parametrize("name", cases.upscale_case_names())
+def test_psf_finer_than_image_matches_reference(name):
+    """A PSF image of pixels ``upscale`` times finer than the image's: the oracle samples on the
+    rescaled working window and sums the blocks back; model, Jacobian and the LM trajectory
+    against the reference's."""
+    d = cases.load_upscale(name)
+    spec = d["spec"]
+    p = dict(spec["init"])
+    p["center"] = np.array(p["center"], dtype=float)
+    comp = Component(spec["kind"], p, psf_mode="full")
+    prob = GroupProblem([comp], Window.from_scale(spec["nx"], spec["ny"], spec["scale"]),
+                        PSF(d["psf"], spec["scale"] / spec["upscale"]), d["data"], d["weight"])
+    rep0 = prob.representation()
+    assert np.allclose(rep0, d["rep0"], rtol=0, atol=1e-13)
+    m = prob.forward(rep0).reshape(d["init_model"].shape)
+    assert np.max(np.abs(m - d["init_model"])) <= 1e-12 * np.max(np.abs(d["init_model"]))
+    J = prob.jacobian(rep0).reshape(d["jac_rep"].shape)
+    for k in range(J.shape[-1]):
+        ref = d["jac_rep"][..., k]
+        assert np.max(np.abs(J[..., k] - ref)) <= 1e-11 * np.max(np.abs(ref)), k
+    lm = LMOracle(prob, rep0, max_iter=spec["max_iter"]).fit()
+    assert lm.message == d["message"]
+    assert np.allclose(lm.loss_history, d["loss_history"], rtol=1e-10, atol=0)
+    assert np.allclose(lm.res(), d["res"], rtol=1e-8, atol=1e-10)
+
+
 @pytest.mark.parametrize("tag", ["locked", "free", "quirk"])
 def test_group_with_sky_matches_reference(tag):
     d = cases.load_render("sersic_psf_64")
@@ -277,7 +303,8 @@ def group_problem(d, values=None, truth=False):
     else:
         comps.append(Component("flat_sky", {"F": 0.0}, locked=("F",)))
     N = spec["size"]
-    return GroupProblem(comps, Window.from_scale(N, N), PSF(d["psf"]), d["data"], d["weight"], links=links)
+    psf = PSF(d["psf"], scale=1.0 / spec.get("psf_upscale", 1))  # a finer PSF grid: psf_upscale
+    return GroupProblem(comps, Window.from_scale(N, N), psf, d["data"], d["weight"], links=links)
 
 
 @pytest.mark.parametrize("name", cases.group_case_names())
