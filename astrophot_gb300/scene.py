@@ -438,24 +438,9 @@ class Scene:
         n_desc = ns + (1 if self.n_img else 0)
         nf = np.array([desc[i].n_free for i in range(n_desc)], dtype=np.int64)
         gid = np.array([[desc[i].gidx[c] for c in range(8)] for i in range(n_desc)], dtype=np.int64)
-        slot = np.arange(8)
-        ok = slot[None, :] < nf[:, None]
-        src_i, c_i = np.nonzero(ok)
-        self._jt_table = self._gather_table(gid[src_i, c_i], src_i * 8 + c_i)
+        self._jt_table = self._gather_table(*jt_contributions(nf, gid))
         self._jt_part = torch.empty(max(n_desc, 1) * 8, dtype=torch.float64, device=dev)
-        pa = np.array(pairs, dtype=np.int64).reshape(-1, 2)
-        p_i, a_i, c_i = np.nonzero((slot[None, :, None] < nf[pa[:, 0]][:, None, None])
-                                   & (slot[None, None, :] < nf[pa[:, 1]][:, None, None]))
-        # a pair of two sources adds its block and the block's transpose; a source's own block
-        # gives its upper triangle, mirrored, so that H is exactly symmetric
-        two = pa[p_i, 0] != pa[p_i, 1]
-        keep = two | (a_i <= c_i)
-        p_i, a_i, c_i, two = p_i[keep], a_i[keep], c_i[keep], two[keep]
-        ga, gb = gid[pa[p_i, 0], a_i], gid[pa[p_i, 1], c_i]
-        contrib = p_i * 64 + a_i * 8 + c_i
-        mirror = two | (a_i < c_i)
-        self._hess_table = self._gather_table(np.concatenate([ga * self.P + gb, gb[mirror] * self.P + ga[mirror]]),
-                                              np.concatenate([contrib, contrib[mirror]]))
+        self._hess_table = self._gather_table(*hess_contributions(nf, gid, pairs, self.P))
         self._hess_part = torch.empty(max(self.n_pairs, 1) * 64, dtype=torch.float64, device=dev)
 
         self.lib = N.lib()
@@ -932,17 +917,11 @@ class Scene:
         return torch.tensor(out, dtype=torch.float64)
 
     def _gather_table(self, entries, contribs):
-        """(entry, ptr, contrib, n) device tables of ap_gather_sum: each entry's contributions in
-        ascending order."""
-        entries = np.asarray(entries, dtype=np.int64)
-        contribs = np.asarray(contribs, dtype=np.int64)
-        order = np.lexsort((contribs, entries))
-        e, c = entries[order], contribs[order]
-        uniq, start = np.unique(e, return_index=True)
-        ptr = np.append(start, len(e)).astype(np.int32)
+        """The device tables (entry, ptr, contrib, n) of ap_gather_sum."""
+        uniq, ptr, c = gather_table(entries, contribs)
         dev = self.device
-        return (torch.tensor(uniq, device=dev), torch.tensor(ptr, device=dev),
-                torch.tensor(c.astype(np.int32), device=dev), len(uniq))
+        return (torch.tensor(uniq, device=dev), torch.tensor(ptr, device=dev), torch.tensor(c, device=dev),
+                len(uniq))
 
     def _gather(self, table, part, out):
         entry, ptr, contrib, n = table
@@ -1031,6 +1010,45 @@ class Scene:
         if not reuse and int(self._info.item()) != 0:
             return None
         return h
+
+
+def gather_table(entries, contribs):
+    """ap_gather_sum's tables: the distinct entries (ascending, int64), ptr (int32, one past each
+    entry's last contribution) and the contributions of each entry in ascending order (int32)."""
+    entries = np.asarray(entries, dtype=np.int64)
+    contribs = np.asarray(contribs, dtype=np.int64)
+    order = np.lexsort((contribs, entries))
+    e, c = entries[order], contribs[order]
+    uniq, start = np.unique(e, return_index=True)
+    return uniq, np.append(start, len(e)).astype(np.int32), c.astype(np.int32)
+
+
+def jt_contributions(nf, gid):
+    """(entry, contribution) pairs of J^T v: source s's sum for its compact slot c (part index
+    8 s + c) goes to the joint-vector entry gid[s][c].  nf[s]: the source's fitted slots."""
+    nf, gid = np.asarray(nf, dtype=np.int64), np.asarray(gid, dtype=np.int64)
+    src_i, c_i = np.nonzero(np.arange(8)[None, :] < nf[:, None])
+    return gid[src_i, c_i], src_i * 8 + c_i
+
+
+def hess_contributions(nf, gid, pairs, P):
+    """(entry, contribution) pairs of J^T W J over a [P, P] row-major matrix: pair p = (A, B)'s
+    block element (a, c) (part index 64 p + 8 a + c) goes to (gid[A][a], gid[B][c]) and, for two
+    sources, to its transpose too; a source's own block gives its upper triangle, mirrored, so
+    the matrix comes out exactly symmetric."""
+    nf, gid = np.asarray(nf, dtype=np.int64), np.asarray(gid, dtype=np.int64)
+    pa = np.asarray(pairs, dtype=np.int64).reshape(-1, 2)
+    slot = np.arange(8)
+    p_i, a_i, c_i = np.nonzero((slot[None, :, None] < nf[pa[:, 0]][:, None, None])
+                               & (slot[None, None, :] < nf[pa[:, 1]][:, None, None]))
+    two = pa[p_i, 0] != pa[p_i, 1]
+    keep = two | (a_i <= c_i)
+    p_i, a_i, c_i, two = p_i[keep], a_i[keep], c_i[keep], two[keep]
+    ga, gb = gid[pa[p_i, 0], a_i], gid[pa[p_i, 1], c_i]
+    contrib = p_i * 64 + a_i * 8 + c_i
+    mirror = two | (a_i < c_i)
+    return (np.concatenate([ga * P + gb, gb[mirror] * P + ga[mirror]]),
+            np.concatenate([contrib, contrib[mirror]]))
 
 
 class OptimizeStop(Exception):
