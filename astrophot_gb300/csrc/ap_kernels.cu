@@ -914,11 +914,13 @@ __device__ __forceinline__ void sample_select_tile(const BatchArgs& b, const Eva
     }
   }
   enqueue_selection(b, sel, redecided, ((int64_t)slot << 62) | ((int64_t)s << 32) | pp);
-  __syncthreads();  // sd / se reuse by the next tile
+  // no barrier here: the caller alternates two sd / se buffers, and the next tile's barrier
+  // (which every thread reaches only after its reads of this tile) orders them before the
+  // writes of the tile after it into this buffer
 }
 
 __global__ void __launch_bounds__(256) k_sample_select(BatchArgs b) {
-  __shared__ float sd[kTile + 2][kTile + 2], se[kTile + 2][kTile + 2];
+  __shared__ float sdb[2][kTile + 2][kTile + 2], seb[2][kTile + 2][kTile + 2];
   const uint32_t n = b.counters[7];
   uint32_t c0, c1;
   tile_chunk(n, c0, c1);
@@ -938,6 +940,8 @@ __global__ void __launch_bounds__(256) k_sample_select(BatchArgs b) {
       ops = ed.ops;
       if (ops & OP_DIFF) d = load_deltaf(ed);
     }
+    float(*sd)[kTile + 2] = sdb[(it - c0) & 1];
+    float(*se)[kTile + 2] = seb[(it - c0) & 1];
     if (ops & OP_JAC)
       sample_select_tile<true, false>(b, e, d, ops, s, slot, local, sd, se);
     else if (ops & OP_DIFF)
