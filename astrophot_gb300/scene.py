@@ -1038,6 +1038,8 @@ def hess_contributions(nf, gid, pairs, P):
     the matrix comes out exactly symmetric."""
     nf, gid = np.asarray(nf, dtype=np.int64), np.asarray(gid, dtype=np.int64)
     pa = np.asarray(pairs, dtype=np.int64).reshape(-1, 2)
+    if len(pa) * 64 >= 2**31:
+        raise ValueError("too many overlapping source pairs for int32 contribution indices")
     slot = np.arange(8)
     p_i, a_i, c_i = np.nonzero((slot[None, :, None] < nf[pa[:, 0]][:, None, None])
                                & (slot[None, None, :] < nf[pa[:, 1]][:, None, None]))
