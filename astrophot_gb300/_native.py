@@ -79,6 +79,7 @@ class ApOptions(ctypes.Structure):
         ("has_sky", ctypes.c_int32),
         ("fft_min_kernel", ctypes.c_int32),
         ("center_radius", ctypes.c_double),
+        ("lanczos_order", ctypes.c_int32),
     ]
 
 
@@ -247,6 +248,19 @@ def _stream():
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 
+def lanczos_order(psf_subpixel_shift: str) -> int:
+    """k of a "lanczos:k" sub-pixel shift (models/_model_methods.py:209-210), else 0."""
+    if not isinstance(psf_subpixel_shift, str) or "lanczos" not in psf_subpixel_shift:
+        return 0
+    try:
+        k = int(psf_subpixel_shift[psf_subpixel_shift.find(":") + 1 :])
+    except ValueError:
+        raise SpecificationConflict(f"unrecognized subpixel shift method: {psf_subpixel_shift}") from None
+    if not 1 <= k <= 8:
+        raise SpecificationConflict(f"Lanczos order {k} outside 1..8 on the CUDA path")
+    return k
+
+
 def make_options(
     profile="sersic",
     sampling_mode="midpoint",
@@ -295,7 +309,8 @@ def make_options(
     if psf_mode == "none":
         o.psf_mode = PSF_NONE
     elif psf_mode == "full":
-        if psf_subpixel_shift == "bilinear":
+        o.lanczos_order = lanczos_order(psf_subpixel_shift)
+        if psf_subpixel_shift == "bilinear" or o.lanczos_order > 0:
             o.psf_mode = PSF_FULL
         elif psf_subpixel_shift == "none":
             o.psf_mode = PSF_FULL_NOSHIFT

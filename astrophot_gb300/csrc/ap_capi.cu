@@ -137,6 +137,8 @@ int validate_options(const ap_options* o) {
   if (o->integrate_mode != AP_INTEGRATE_NONE && o->integrate_mode != AP_INTEGRATE_THRESHOLD)
     return AP_ERR_UNSUPPORTED;
   if (o->psf_mode < AP_PSF_NONE || o->psf_mode > AP_PSF_FULL_NOSHIFT) return AP_ERR_UNSUPPORTED;
+  if (o->lanczos_order < 0 || o->lanczos_order > kMaxLanczos) return AP_ERR_UNSUPPORTED;
+  if (o->lanczos_order > 0 && o->psf_mode != AP_PSF_FULL) return AP_ERR_UNSUPPORTED;
   if (o->integrate_mode == AP_INTEGRATE_THRESHOLD) {
     if (o->integrate_max_depth < 1 || o->integrate_max_depth > kMaxDepth) return AP_ERR_UNSUPPORTED;
     if (o->integrate_gridding < 1 || o->integrate_gridding > kMaxGrid) return AP_ERR_UNSUPPORTED;
@@ -194,10 +196,11 @@ int ap_batch_create(ap_batch** out, int32_t n, const int32_t* nx, const int32_t*
   // k_conv's flavour (and with it the output tile height) for the whole batch: the large one
   // when some kernel is not covered by the register-blocked sizes
   bool large = false;
+  // the shifted kernel grows by the shift's padding: 1 a side (bilinear), k a side (Lanczos k)
+  const int shift_pad = options->psf_mode != AP_PSF_FULL ? 0 : (options->lanczos_order > 0 ? 2 * options->lanczos_order : 2);
   if (psf) {
-    const bool shift = options->psf_mode == AP_PSF_FULL;
     for (int s = 0; s < n; ++s)
-      if (conv_kernel_large(shift ? psf_kx[s] + 2 : psf_kx[s], shift ? psf_ky[s] + 2 : psf_ky[s])) large = true;
+      if (conv_kernel_large(psf_kx[s] + shift_pad, psf_ky[s] + shift_pad)) large = true;
   }
   b->conv_large = large;
   for (int s = 0; s < n; ++s) {
@@ -219,9 +222,8 @@ int ap_batch_create(ap_batch** out, int32_t n, const int32_t* nx, const int32_t*
       // psf_border_int = ceil((1 + shape) / 2)  (image/psf_image.py:71-93)
       st.bx = (st.kx + 2) / 2;
       st.by = (st.ky + 2) / 2;
-      const bool shift = options->psf_mode == AP_PSF_FULL;
-      st.kpx = shift ? st.kx + 2 : st.kx;
-      st.kpy = shift ? st.ky + 2 : st.ky;
+      st.kpx = st.kx + shift_pad;
+      st.kpy = st.ky + shift_pad;
     }
     st.wnx = st.nx + 2 * st.bx;
     st.wny = st.ny + 2 * st.by;
@@ -433,6 +435,7 @@ int ap_batch_create(ap_batch** out, int32_t n, const int32_t* nx, const int32_t*
   A.sampling = options->sampling_mode;
   A.integrate = options->integrate_mode;
   A.psf_mode = options->psf_mode;
+  A.lanczos = options->psf_mode == AP_PSF_FULL ? options->lanczos_order : 0;
   A.max_depth = options->integrate_max_depth;
   A.free_mask = options->free_mask;
   int nf = 0;
@@ -646,6 +649,7 @@ int ap_render_precise(ap_batch* b, const double* params, const float* psf, float
   if (!b->bound) return AP_ERR_NOT_BOUND;
   if (b->opt.psf_mode != AP_PSF_NONE && !psf) return AP_ERR_ARG;
   if (b->args.kind != AP_PROFILE_SERSIC && b->args.kind != AP_PROFILE_EXPONENTIAL) return AP_ERR_UNSUPPORTED;
+  if (b->args.lanczos > 0) return AP_ERR_UNSUPPORTED;  // no difference form of a Lanczos shift
   const BaseLayout L = base_layout(b);
   if (base_bytes < L.total) return AP_ERR_WORKSPACE;
   char* w = (char*)base;
@@ -669,6 +673,7 @@ int ap_render_psf_derivative(ap_batch* b, const double* params, const float* psf
   if (!b || !params || !psf || !dpsf || !model) return AP_ERR_ARG;
   if (!b->bound) return AP_ERR_NOT_BOUND;
   if (b->opt.psf_mode == AP_PSF_NONE || b->opt.has_sky) return AP_ERR_ARG;
+  if (b->args.lanczos > 0) return AP_ERR_UNSUPPORTED;  // the derivative's shift is bilinear
   cudaStream_t s = (cudaStream_t)stream;
   int rc = check_cuda(launch_eval_setup(b->args, params, NPARAM, 0, nullptr, OP_FWD | OP_WRITE_MODEL, s));
   if (rc) return rc;

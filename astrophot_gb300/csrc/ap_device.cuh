@@ -24,6 +24,7 @@ namespace apgb {
 constexpr int kMaxQuad = 5;   // quad levels <= 5  (quad_level^2 <= 32 lanes)
 constexpr int kMaxGrid = 5;   // gridding <= 5     (gridding^2 <= 32 lanes)
 constexpr int kMaxDepth = 3;  // integrate_max_depth <= 3
+constexpr int kMaxLanczos = 8; // psf_subpixel_shift "lanczos:k", k <= 8
 constexpr int kTile = 16;     // 16 x 16 working-pixel tiles (sampling / selection)
 constexpr int kOutTileX = 32; // output tiles of the convolve/accumulate pass: 32 x 32 pixels,
 constexpr int kOutTileY = 32; // 128 threads, each thread 8 consecutive rows of one column
@@ -184,6 +185,7 @@ struct BatchArgs {
   int32_t sampling;     // AP_SAMPLING_*
   int32_t integrate;    // AP_INTEGRATE_*
   int32_t psf_mode;     // AP_PSF_*
+  int32_t lanczos;      // psf_mode AP_PSF_FULL: 0 bilinear shift, k > 0 Lanczos of order k
   int32_t max_depth;
   int32_t free_mask;
   int32_t n_free;
@@ -244,8 +246,9 @@ struct BatchArgs {
 
 // Stamps whose trials the LM renders as differences to the base point: the Sersic and
 // exponential profiles (direct, FFT or no convolution).
+// (a Lanczos shift has no kernel-difference form: its trials render in full)
 __host__ __device__ inline bool diff_capable(const BatchArgs& b, const StampDev&) {
-  return b.kind == AP_PROFILE_SERSIC || b.kind == AP_PROFILE_EXPONENTIAL;
+  return (b.kind == AP_PROFILE_SERSIC || b.kind == AP_PROFILE_EXPONENTIAL) && b.lanczos == 0;
 }
 
 // Integration pattern of a working pixel: 0 midpoint only, 1 level 1 (one Q x Q quadrature),

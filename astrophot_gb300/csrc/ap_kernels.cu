@@ -271,6 +271,62 @@ __device__ __forceinline__ ShiftValF shifted_psf_at_f(const float* psf, int kx, 
   return r;
 }
 
+// ---- Lanczos sub-pixel shift (psf_subpixel_shift "lanczos:k", models/_model_methods.py:209-227):
+// the PSF zero-padded by k and cross-correlated ("same") with the (2k+1)^2 kernel
+// LL[b][a] = Lx[a] Ly[b], Lx[a] = f(a - k + shift_x), f(t) = sinc(t) sinc(t / k)
+// (utils/interpolate.py:145-163), then renormalised.  LL's own normalisation cancels in the
+// renormalisation, so the weights here are unnormalised.
+__device__ __forceinline__ void sinc_and_slope(double t, double& v, double& dv) {
+  constexpr double kPi = 3.14159265358979323846;
+  const double x = kPi * t;
+  if (fabs(x) < 1e-4) {  // series: sinc = 1 - x^2/6 + x^4/120, d/dt = pi (-x/3 + x^3/30)
+    const double x2 = x * x;
+    v = 1.0 - x2 / 6.0 + x2 * x2 / 120.0;
+    dv = kPi * x * (-1.0 / 3.0 + x2 / 30.0);
+  } else {
+    double sn, cs;
+    sincos(x, &sn, &cs);
+    v = sn / x;
+    dv = kPi * (cs - v) / x;
+  }
+}
+
+// w[a] = f(a - k + shift), dw[a] = d w[a] / d shift, a = 0 .. 2k
+__device__ __forceinline__ void lanczos_weights(double shift, int k, float* w, float* dw) {
+  for (int a = 0; a <= 2 * k; ++a) {
+    const double t = (double)(a - k) + shift;
+    double s1, d1, s2, d2;
+    sinc_and_slope(t, s1, d1);
+    sinc_and_slope(t / k, s2, d2);
+    w[a] = (float)(s1 * s2);
+    dw[a] = (float)(d1 * s2 + s1 * d2 / k);
+  }
+}
+
+// The shifted kernel (size (kx + 2k) x (ky + 2k)) at (ix, iy) and its shift derivatives:
+// sum over a, b of Lx[a] Ly[b] psf[iy + b - 2k][ix + a - 2k] (zero outside the PSF)
+__device__ __forceinline__ ShiftValF lanczos_psf_at_f(const float* psf, int kx, int ky, int ix, int iy, int k,
+                                                      const float* wx, const float* dwx, const float* wy,
+                                                      const float* dwy) {
+  ShiftValF r{0.f, 0.f, 0.f};
+  for (int b = 0; b <= 2 * k; ++b) {
+    const int rr = iy + b - 2 * k;
+    if (rr < 0 || rr >= ky) continue;
+    float sv = 0.f, sdx = 0.f;
+    for (int a = 0; a <= 2 * k; ++a) {
+      const int cc = ix + a - 2 * k;
+      if (cc < 0 || cc >= kx) continue;
+      const float p = psf[rr * kx + cc];
+      sv = fmaf(wx[a], p, sv);
+      sdx = fmaf(dwx[a], p, sdx);
+    }
+    r.v = fmaf(wy[b], sv, r.v);
+    r.dx = fmaf(wy[b], sdx, r.dx);
+    r.dy = fmaf(dwy[b], sv, r.dy);
+  }
+  return r;
+}
+
 // Shifted value at shift s1 and its difference to the value at shift s0 (ds = s1 - s0 exact).
 // Inside one bilinear cell the value is bilinear in the shift, so the difference of each
 // weight product is expanded in ds; a tap whose cell differs between the shifts takes B1 - B0.
@@ -372,6 +428,31 @@ __device__ void psf_shift_warp(const BatchArgs& b, const float* psf, int s, int 
       const float2 r = shifted_psf_delta(P, st.kx, st.ky, idx % st.kpx, idx / st.kpx, sx1, sy1, sx0, sy0, dsx, dsy);
       out[idx] = r.x * inv;
       out[kp2 + idx] = (r.y - K0[idx] * c) * inv;
+    }
+  } else if (b.psf_mode == AP_PSF_FULL && b.lanczos > 0) {
+    // Lanczos shift: the same renormalisation and derivative rule as the bilinear one below
+    const int k = b.lanczos;
+    float wx[2 * kMaxLanczos + 1], dwx[2 * kMaxLanczos + 1], wy[2 * kMaxLanczos + 1], dwy[2 * kMaxLanczos + 1];
+    lanczos_weights(e.shift[0], k, wx, dwx);
+    lanczos_weights(e.shift[1], k, wy, dwy);
+    double S = 0, Sx = 0, Sy = 0;
+    for (int idx = lane; idx < kp2; idx += 32) {
+      const ShiftValF r = lanczos_psf_at_f(P, st.kx, st.ky, idx % st.kpx, idx / st.kpx, k, wx, dwx, wy, dwy);
+      S += r.v;
+      Sx += r.dx;
+      Sy += r.dy;
+    }
+    S = warp_sum_d(S);
+    Sx = warp_sum_d(Sx);
+    Sy = warp_sum_d(Sy);
+    const float inv = (float)(1.0 / S), cx = (float)(Sx / (S * S)), cy = (float)(Sy / (S * S));
+    for (int idx = lane; idx < kp2; idx += 32) {
+      const ShiftValF r = lanczos_psf_at_f(P, st.kx, st.ky, idx % st.kpx, idx / st.kpx, k, wx, dwx, wy, dwy);
+      out[idx] = r.v * inv;
+      if (jac) {
+        out[kp2 + idx] = r.dx * inv - r.v * cx;
+        out[2 * kp2 + idx] = r.dy * inv - r.v * cy;
+      }
     }
   } else if (b.psf_mode == AP_PSF_FULL) {
     const float sx = (float)e.shift[0], sy = (float)e.shift[1];

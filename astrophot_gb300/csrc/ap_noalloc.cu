@@ -144,6 +144,7 @@ bool na_options_ok(const ap_options* o) {
     return false;
   if (o->integrate_mode != AP_INTEGRATE_NONE && o->integrate_mode != AP_INTEGRATE_THRESHOLD) return false;
   if (o->psf_mode < AP_PSF_NONE || o->psf_mode > AP_PSF_FULL_NOSHIFT) return false;
+  if (o->lanczos_order != 0) return false;  // the bilinear shift only
   if (o->integrate_mode == AP_INTEGRATE_THRESHOLD &&
       (o->integrate_max_depth < 1 || o->integrate_max_depth > kMaxDepth || o->integrate_gridding < 1 ||
        o->integrate_gridding > kMaxGrid || o->integrate_quad_level < 1 || o->integrate_quad_level > kMaxQuad))

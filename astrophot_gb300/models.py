@@ -620,7 +620,11 @@ class _Structure:
             if g.psf_mode == "full" and g.psf_convolve_mode not in ("fft", "direct"):
                 raise ValueError(f"unrecognized psf_convolve_mode: {g.psf_convolve_mode}")
             if g.psf_mode == "full" and g.psf_subpixel_shift not in ("bilinear", "none"):
-                raise SpecificationConflict(f"unrecognized subpixel shift method: {g.psf_subpixel_shift}")
+                from . import _native as N
+
+                N.lanczos_order(g.psf_subpixel_shift)  # "lanczos:k", or SpecificationConflict
+                if "lanczos" not in g.psf_subpixel_shift:
+                    raise SpecificationConflict(f"unrecognized subpixel shift method: {g.psf_subpixel_shift}")
 
     def options(self):
         from . import _native as N

@@ -742,8 +742,9 @@ class Scene:
 
     @property
     def precise_capable(self) -> bool:
-        """Whether trials can be rendered as differences (device staging: no live PSF)."""
-        return self.device_staging
+        """Whether trials can be rendered as differences (device staging: no live PSF; no
+        Lanczos sub-pixel shift, which has no kernel-difference form)."""
+        return self.device_staging and not any(p["batch"].options.lanczos_order > 0 for p in self._fwd_parts)
 
     def _forward_base_body(self):
         self._render_sources(self.fwd, None, base_mode=N.StampBatch.RENDER_BASE)

@@ -105,6 +105,11 @@ typedef struct ap_options {
                                    (psf_convolve_mode "fft", models/_model_methods.py:245-257);
                                    0 = direct convolution for every stamp */
   double center_radius;         /* AP_SAMPLING_MIDPOINT_CENTER: radius in pixels (2) */
+  int32_t lanczos_order;        /* psf_mode AP_PSF_FULL: 0 = bilinear sub-pixel shift (the
+                                   reference default); k = 1..8: psf_subpixel_shift "lanczos:k"
+                                   (models/_model_methods.py:209-227): the kernel grows by 2k
+                                   instead of 2, and the LM renders its trials in full (no
+                                   difference form; ap_render_precise refuses such batches) */
 } ap_options;
 
 typedef struct ap_lm_options {

@@ -708,6 +708,50 @@ def shift_psf_bilinear(psf: np.ndarray, shift, grad: bool):
     return out, dsx, dsy
 
 
+def _lanczos_1d(shift, order):
+    """Lanczos weights f(a - order + shift), f(t) = sinc(t) sinc(t / order), a = 0..2 order, and
+    their shift derivatives (``_shift_Lanczos_kernel_torch``, utils/interpolate.py:145-163, with
+    dx = -shift; f is even, so the reference's sign flip of the argument changes nothing)."""
+    t = np.arange(-order, order + 1, dtype=float) + shift
+
+    def sinc_d(u):
+        x = np.pi * u
+        small = np.abs(x) < 1e-4
+        xs = np.where(small, 1.0, x)
+        v = np.where(small, 1.0 - x * x / 6.0, np.sin(xs) / xs)
+        dv = np.where(small, np.pi * (-x / 3.0), np.pi * (np.cos(xs) - np.sin(xs) / xs) / xs)
+        return v, dv
+
+    s1, d1 = sinc_d(t)
+    s2, d2 = sinc_d(t / order)
+    return s1 * s2, d1 * s2 + s1 * d2 / order
+
+
+def shift_psf_lanczos(psf: np.ndarray, shift, order: int, grad: bool):
+    """``_shift_psf`` "lanczos:order" (models/_model_methods.py:209-227): the PSF zero-padded by
+    ``order`` and cross-correlated ("same") with Lx (x) Ly, kept padded, plus d/d(shift_x),
+    d/d(shift_y).  The kernel is left unnormalised: the caller renormalises the shifted PSF,
+    which cancels the reference's normalisation of the kernel."""
+    k = int(order)
+    lx, dlx = _lanczos_1d(shift[0], k)
+    ly, dly = _lanczos_1d(shift[1], k)
+    pad = np.pad(psf, k)
+    big = np.pad(pad, k)  # the "same" correlation's zero border
+    h, w = pad.shape
+
+    def corr(wx, wy):
+        out = np.zeros((h, w))
+        for b in range(2 * k + 1):
+            for a in range(2 * k + 1):
+                out += wy[b] * wx[a] * big[b : b + h, a : a + w]
+        return out
+
+    out = corr(lx, ly)
+    if not grad:
+        return out, None, None
+    return out, corr(dlx, ly), corr(lx, dly)
+
+
 def convolve_fft_semantics(img, kern):
     """``fft_convolve_torch(img, psf, img_prepadded=True)`` (utils/operations.py:9-36): circular
     convolution at the image size, rolled by -(k-1)/2 -- written as the equivalent direct sum."""
@@ -766,8 +810,9 @@ def sample_component(comp: Component, win: Window, psf: Optional[PSF] = None, gr
         work = win.rescale_pixel(1 / upscale) if upscale != 1 else win.copy()
         bx, by = psf.border
         work.pad_pixel(bx, by)
+        lanczos = "lanczos" in comp.psf_subpixel_shift
         if comp.psf_subpixel_shift != "none":
-            if comp.psf_subpixel_shift != "bilinear":
+            if comp.psf_subpixel_shift != "bilinear" and not lanczos:
                 raise ValueError(f"unsupported subpixel shift {comp.psf_subpixel_shift}")
             pcx, pcy = work.plane_to_pixel(center[0], center[1])
             pc = np.array([pcx, pcy])
@@ -778,7 +823,10 @@ def sample_component(comp: Component, win: Window, psf: Optional[PSF] = None, gr
             shift = None
         reference, deep = sample_init(comp, work, center, grad)
         deep, select = sample_integrate(comp, deep, reference, work, center, grad)
-        if shift is not None:
+        if shift is not None and lanczos:
+            order = int(comp.psf_subpixel_shift[comp.psf_subpixel_shift.find(":") + 1 :])
+            spsf, dsx, dsy = shift_psf_lanczos(psf.data, shift, order, grad)
+        elif shift is not None:
             spsf, dsx, dsy = shift_psf_bilinear(psf.data, shift, grad)
         else:
             spsf, dsx, dsy = psf.data.copy(), None, None
@@ -806,7 +854,12 @@ def sample_component(comp: Component, win: Window, psf: Optional[PSF] = None, gr
                 jac[("center", 0)] = dmod[0] * Pi[0, 0] + dmod[1] * Pi[1, 0]
                 jac[("center", 1)] = dmod[0] * Pi[0, 1] + dmod[1] * Pi[1, 1]
             for name, D in (psf_dirs or {}).items():
-                SD = shift_psf_bilinear(D, shift, False)[0] if shift is not None else D
+                if shift is None:
+                    SD = D
+                elif lanczos:
+                    SD = shift_psf_lanczos(D, shift, order, False)[0]
+                else:
+                    SD = shift_psf_bilinear(D, shift, False)[0]
                 dk = SD / norm - spsf * np.sum(SD) / norm**2
                 jac[("psf", name)] = _reduce(conv(deep.val, dk)[by : ny - by, bx : nx - bx], upscale)
         return Rendered(model, jac, select, (ny, nx))

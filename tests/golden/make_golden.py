@@ -13,6 +13,7 @@ Run with ``ASTROPHOT_REFERENCE=<path of the reference checkout>`` set:
     python tests/golden/make_golden.py knobs      # only the group with per-galaxy sampling settings
     python tests/golden/make_golden.py upscale    # only the PSF finer than the image pixels
     python tests/golden/make_golden.py groupupscale  # only the group with that PSF
+    python tests/golden/make_golden.py lanczos    # only the Lanczos PSF shifts
 
 The reference (AstroPhot 0.x) is imported through a ``sys.modules`` shim for
 the optional packages it imports at module level but never calls on this
@@ -140,6 +141,25 @@ RENDER_CASES = {
         psf=MOFFAT_25,
         params={"center": [31.7, 32.4], "q": 0.55, "PA": 0.9, "n": 2.5, "Re": 8.0, "Ie": 1.2},
         knobs={"psf_mode": "full", "psf_convolve_mode": "direct"},
+    ),
+    # the Lanczos sub-pixel shifts of the PSF ("lanczos:3" and "lanczos:2")
+    "sersic_psf_lanczos3": dict(
+        kind="sersic",
+        nx=64,
+        ny=64,
+        scale=1.0,
+        psf=MOFFAT_25,
+        params={"center": [31.7, 32.4], "q": 0.55, "PA": 0.9, "n": 2.5, "Re": 8.0, "Ie": 1.2},
+        knobs={"psf_mode": "full", "psf_subpixel_shift": "lanczos:3"},
+    ),
+    "exp_psf_lanczos2": dict(
+        kind="exponential",
+        nx=48,
+        ny=48,
+        scale=1.0,
+        psf=("gaussian", 1.5, 13),
+        params={"center": [23.6, 24.2], "q": 0.6, "PA": 1.7, "Re": 7.0, "Ie": 1.5},
+        knobs={"psf_mode": "full", "psf_subpixel_shift": "lanczos:2", "psf_convolve_mode": "direct"},
     ),
     "sersic_nopsf": dict(
         kind="sersic",
@@ -943,6 +963,12 @@ def main():
         out = run_psf_stamps(ap)
         np.savez_compressed(os.path.join(HERE, "psf_stamps.npz"), **out)
         print("psf stamps", sorted(k for k in out if not k.endswith("_args")))
+        return
+    if only == "lanczos":
+        for key in ("sersic_psf_lanczos3", "exp_psf_lanczos2"):
+            out = run_render_case(ap, key, RENDER_CASES[key])
+            np.savez_compressed(os.path.join(HERE, f"render_{key}.npz"), **out)
+            print("render", key, out["model"].shape, float(out["model"].sum()))
         return
     if only == "center":
         for key in ("sersic_psf_center", "sersic_nopsf_center"):

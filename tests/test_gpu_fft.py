@@ -46,6 +46,7 @@ def test_fft_convolution_matches_reference_goldens(N, name):
     kind = spec["kind"]
     opts = N.make_options(profile=kind, sampling_mode=spec["knobs"].get("sampling_mode", "midpoint"),
                           integrate_mode=spec["knobs"].get("integrate_mode", "threshold"), psf_mode="full",
+                          psf_subpixel_shift=spec["knobs"].get("psf_subpixel_shift", "bilinear"),
                           free_mask=0x7F if kind == "sersic" else 0x6F, fft_min_kernel=1)
     psf = d["psf"]
     b = N.StampBatch([(spec["nx"], spec["ny"])], [(psf.shape[1], psf.shape[0])], N.scale_geometry(1, spec["scale"]), opts)

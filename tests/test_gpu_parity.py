@@ -60,6 +60,7 @@ def batch_for_case(N, d, free_mask=None, has_sky=False):
         sampling_mode=knobs.get("sampling_mode", "midpoint"),
         integrate_mode=knobs.get("integrate_mode", "threshold"),
         psf_mode=knobs.get("psf_mode", "none"),
+        psf_subpixel_shift=knobs.get("psf_subpixel_shift", "bilinear"),
         free_mask=free_mask,
         has_sky=has_sky,
     )
