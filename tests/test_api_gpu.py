@@ -287,3 +287,41 @@ def test_psf_finer_than_image_matches_reference(ap, name):
     assert abs(min(res.loss_history) / d["loss_history"].min() - 1) <= 1e-5
     assert np.allclose(res.loss_history[:3], d["loss_history"][:3], rtol=1e-5)
     assert np.allclose(res.res(), d["res"], rtol=1e-4, atol=1e-6)
+
+
+def test_lanczos_shift_adjoint_and_fit_match_oracle(ap):
+    """psf_subpixel_shift "lanczos:3": the adjoint (the render's own derivative) against
+    J^T W (model - data) of the reference's Jacobian, and LM(model).fit() from a perturbed start
+    against the oracle's LM from the same start (a Lanczos stamp's trials render in full)."""
+    from oracle.lm import GroupProblem, LMOracle
+    from oracle.render import PSF, Component, Window
+
+    d = cases.load_render("sersic_psf_lanczos3")
+    spec = d["spec"]
+    rng = np.random.default_rng(41)
+    var = d["model"] + 10.0
+    data = d["model"] + rng.normal(size=d["model"].shape) * np.sqrt(var)
+    tar = ap.image.Target_Image(data=data, pixelscale=spec["scale"], psf=d["psf"], variance=var)
+    m = ap.models.AstroPhot_Model(name="api lanczos fit", model_type="sersic galaxy model", target=tar,
+                                  parameters=dict(spec["params"]), **spec["knobs"])
+    m.reference_center_gradient = False
+    rep0 = torch.tensor(d["rep"], dtype=torch.float64, requires_grad=True)
+    m.negative_log_likelihood(parameters=rep0, as_representation=True).backward()
+    want = np.einsum("yxk,yx->k", d["jac_rep"], (d["model"] - data) / var)
+    assert np.allclose(rep0.grad.numpy(), want, rtol=1e-3, atol=1e-3 * np.max(np.abs(want)))
+
+    start = dict(spec["params"])
+    start.update(center=[spec["params"]["center"][0] + 0.4, spec["params"]["center"][1] - 0.3],
+                 q=0.6, PA=1.0, n=2.2, Re=8.8, Ie=1.1)
+    m2 = ap.models.AstroPhot_Model(name="api lanczos fit 2", model_type="sersic galaxy model", target=tar,
+                                   parameters=start, **spec["knobs"])
+    x0 = m2.parameters.vector_representation().numpy().copy()
+    res = ap.fit.LM(m2, max_iter=30).fit()
+    p = {k: (np.array(v, dtype=float) if k == "center" else v) for k, v in start.items()}
+    comp = Component("sersic", p, **spec["knobs"])
+    prob = GroupProblem([comp], Window.from_scale(spec["nx"], spec["ny"], spec["scale"]),
+                        PSF(d["psf"], spec["scale"]), data, 1.0 / var)
+    lm = LMOracle(prob, x0, max_iter=30).fit()
+    print(res.loss_history, lm.loss_history, res.message, lm.message)
+    assert abs(min(res.loss_history) / min(lm.loss_history) - 1) <= 1e-5
+    assert np.allclose(res.res(), lm.res(), rtol=1e-3, atol=1e-4)
