@@ -143,3 +143,24 @@ def test_synthetic_workload_is_seeded_and_in_range():
         cx, cy, q, PA, n, Re, Ie = s.truth
         assert 0.3 <= q < 1 and 0.5 <= n <= 4 and 5 <= Re <= 20 and 0 <= PA < np.pi and 0 <= Ie <= 2
         assert abs(s.psf.sum() - 1) < 1e-12
+
+
+def test_lanczos_shift_options(N):
+    """psf_subpixel_shift "lanczos:k": parsed into ap_options.lanczos_order with the full PSF mode,
+    planned by ap_batch_create; orders outside 1..8, or a Lanczos order without the shifted
+    PSF mode, are refused."""
+    from astrophot_gb300.errors import SpecificationConflict
+
+    o = N.make_options(psf_mode="full", psf_subpixel_shift="lanczos:3")
+    assert o.lanczos_order == 3 and o.psf_mode == N.PSF_FULL
+    assert N.make_options(psf_mode="full").lanczos_order == 0
+    rc, h = _create(N, [(32, 32)], [(9, 9)], o)
+    assert rc == N.AP_OK
+    N.lib().ap_batch_destroy(h)
+    for bad in ("lanczos:9", "lanczos:0", "lanczos:x"):
+        with pytest.raises(SpecificationConflict):
+            N.make_options(psf_mode="full", psf_subpixel_shift=bad)
+    o = N.make_options(psf_mode="full", psf_subpixel_shift="none")
+    o.lanczos_order = 3
+    rc, h = _create(N, [(32, 32)], [(9, 9)], o)
+    assert rc == N.AP_ERR_UNSUPPORTED and not h.value
